@@ -1,0 +1,134 @@
+/*
+ * macaw_gb300.h -- C-ABI of the GB300-native G-MCTDH propagation core.
+ *
+ * The entry points replace the equation-of-motion and integrator calls of the
+ * reference's time loop (Macaw, source/propagator.f90).  A Fortran driver binds
+ * them with ISO_C_BINDING; every integer that crosses the
+ * boundary is int64_t because the reference is built with -fdefault-integer-8
+ * (Makefile:18), every complex is interleaved FP64 (double complex), every
+ * array is column-major, and every index is 0-based (the Fortran shim subtracts 1).
+ *
+ * Calls are synchronous at return, one context owns one CUDA stream on the
+ * current device, and a context is not thread-safe.  All functions return 0 on
+ * success or a negative status:
+ *   -1 unsupported feature   -2 eigensolver did not converge   -3 Krylov cap
+ *   -4 step underflow        -5 non-finite state                -6 CUDA error
+ *   -7 bad argument
+ * There is no CPU fallback: without a usable GPU mctdh_create returns -6.
+ */
+#ifndef MACAW_GB300_H
+#define MACAW_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mctdh_ctx mctdh_ctx_t;
+
+/* Contents of the reference's global modules after set-up (psidef.f90,
+ * hamilton.f90:17-62, dvr.f90:11-29, storage.f90, globals.f90:26-44).
+ * Array element (i, j) of a Fortran array X(n1, n2) is X[i + n1*j]. */
+typedef struct mctdh_setup {
+  int64_t nstates, nmodes, ndof, nham, maxdof;
+  const int64_t *nspf;          /* nSPF(nmodes, nstates)                         */
+  const int64_t *nmodedof;      /* nmodeDOF(nmodes)                              */
+  const int64_t *idof;          /* iDOF(maxdof, nmodes), 0-based dofs            */
+  const int64_t *multiset;      /* MultiSet(nmodes), 0/1                         */
+  const int64_t *is_gwp;        /* 1 if the mode uses Gaussian SPFs              */
+  const int64_t *ngp;           /* ngp(ndof)                                     */
+  const double *dvr_grid;       /* grid(:, dof) packed; offsets in dvr_grid_off  */
+  const int64_t *dvr_grid_off;  /* (ndof), -1 for gwp dofs                       */
+  const double *dvr_mats;       /* d1DVR, d2DVR, xd1DVR per dof, each ngp x ngp  */
+  const int64_t *dvr_mat_off;   /* (ndof) offset of d1DVR; d2 at +ngp^2, xd1 at +2 ngp^2 */
+  const double *ae;             /* ae(nham), interleaved complex                 */
+  const int64_t *lhs_el;        /* lhs_el(nham), 0-based                         */
+  const int64_t *rhs_el;        /* rhs_el(nham), 0-based                         */
+  int64_t nopermax;
+  const int64_t *noper;         /* nOper(nmodes)                                 */
+  const int64_t *oper;          /* Oper(-1:maxdof, nopermax, nmodes) as [(2+maxdof) x nopermax x nmodes] */
+  const int64_t *ioper;         /* iOper(nmodes, nham), 0-based                  */
+  const int64_t *is_identity;   /* IsIdentity(nmodes, nopermax)                  */
+  const int64_t *skip_term;     /* SkipTerm(nmodes, nham)                        */
+  const int64_t *ipsispf;       /* ipsiSPF(nmodes, nstates), 0-based offsets     */
+  int64_t dimpsi;
+  const double *gwpa;           /* GWPa(maxdof, ns00max, nmodgwp)                */
+  int64_t ns00max;
+  double eps_rho, eps_ovl, eps_C, eps_int, eps_A, eps_psi;
+  double min_stepsize, writetime;
+  double der_factor_re, der_factor_im;  /* -i for propagation, -1 for relaxation */
+  int64_t int_type_psi;                 /* 1 = Cash-Karp for the CMF2 SPF sweeps  */
+  int64_t precision;                    /* 0 = FP64, 1 = split-FP32 contractions  */
+} mctdh_setup_t;
+
+/* Build the device context: uploads the operators, plans the batched kernels
+ * and allocates device mirrors of A and psi.  Replaces the allocation part of
+ * init_calc.f90:1-226 (alloc_h1mode, alloc_MeanField, alloc_rho, alloc_AVec). */
+int64_t mctdh_create(const mctdh_setup_t *setup, mctdh_ctx_t **ctx);
+int64_t mctdh_destroy(mctdh_ctx_t *ctx);
+
+/* Equation of motion (A, psi, t) -> (dA, dpsi) on host buffers.
+ * Replaces Calc_Derivs(A0, psi0, dA, dpsi, tt) -- derivatives.f90:39. */
+int64_t mctdh_calc_derivs(mctdh_ctx_t *ctx, const double *A, const double *psi,
+                          double *dA, double *dpsi, double t);
+
+/* One adaptive Runge-Kutta step on host buffers (A, psi updated in place; dA,
+ * dpsi are the derivatives at t on entry and, for Dormand-Prince, at t+hdid on
+ * return).  method: 1 Cash-Karp, 2 Dormand-Prince.
+ * Replaces rkqs(A0, psi0, dA, dpsi, tt, htry, hdid, hnext, int_method) --
+ * integrator.f90:36. */
+int64_t mctdh_rkqs(mctdh_ctx_t *ctx, double *A, double *psi, double *dA, double *dpsi,
+                   double t, double htry, double *hdid, double *hnext, int64_t method);
+
+/* One CMF2 step on host buffers (DVR models).
+ * Replaces cmf2(A0, psi0, DD0, tt, htry, hdid, hnext) -- cmf2_base.f90:47. */
+int64_t mctdh_cmf2(mctdh_ctx_t *ctx, double *A, double *psi, double t, double htry,
+                   double *hdid, double *hnext);
+
+/* Step replay.  One rkck/rkdp attempt of fixed length dt (integrator.f90:95-221
+ * plus the DeltaPsi error of :60-61): A, psi <- the 5th-order state, errmax <-
+ * DeltaPsi / eps_int, no step control.  And one CMF2 attempt of length h that is
+ * always completed as if accepted (cmf2_base.f90:76-176 and :186-190), error <-
+ * max(err_A, err_psi) / eps_int.  They let a caller replay a recorded step
+ * sequence: the reference's error norm sqrt|2(1 - Re<1|2>/sqrt(<1|1><2|2>))|
+ * (gmctdh_objects.f90:222) sits at its rounding floor for accepted steps, so
+ * free-running step sequences of two FP64 implementations differ by noise. */
+int64_t mctdh_rk_attempt(mctdh_ctx_t *ctx, double *A, double *psi, double *dA, double *dpsi,
+                         double t, double dt, int64_t method, double *errmax);
+int64_t mctdh_cmf2_attempt(mctdh_ctx_t *ctx, double *A, double *psi, double t, double h, double *error);
+
+/* Device-resident state: upload (also records the start state used by C(t)),
+ * download.  Download replaces the host copies WriteOutput needs for the
+ * restart and psi files (output.f90:231-252). */
+int64_t mctdh_set_state(mctdh_ctx_t *ctx, const double *A, const double *psi, int64_t as_start);
+int64_t mctdh_get_state(mctdh_ctx_t *ctx, double *A, double *psi);
+
+/* The inner loop of propagate_wf (propagator.f90:115-134 RK, :276-296 CMF2) on
+ * the resident state, from *t up to the next output time tnext.  *step carries
+ * the proposed step size between calls exactly like `stepsize` in the
+ * reference.  int_type: 1 rk45, 2 dopri, 10 cmf2.  Returns steps/attempts/EOMs. */
+int64_t mctdh_propagate(mctdh_ctx_t *ctx, int64_t int_type, double tnext, double *t, double *step,
+                        int64_t *nsteps, int64_t *nattempts, int64_t *neom);
+
+/* Observables written by WriteOutput (output.f90:35-87, :144-150) for the
+ * resident state: energyMF / sum(pop), state populations from rho of mode 1,
+ * norm = sum(pop), and C(t) = <Psi(0)|Psi(t)>. */
+int64_t mctdh_observables(mctdh_ctx_t *ctx, double t, double *energy, double *pop, double *norm,
+                          double *auto_re, double *auto_im);
+
+/* norm_wf (gmctdh_objects.f90:21) and WF_Ovl (gmctdh_objects.f90:101) on host buffers. */
+int64_t mctdh_norm_wf(mctdh_ctx_t *ctx, const double *A, const double *psi, double *norm);
+int64_t mctdh_wf_ovl(mctdh_ctx_t *ctx, const double *A1, const double *psi1, const double *A2,
+                     const double *psi2, double *ovl_re, double *ovl_im);
+
+/* Kernel launches issued by this context since creation (for accounting). */
+int64_t mctdh_launch_count(mctdh_ctx_t *ctx);
+
+/* Last error message of the context (or of the last failed create when ctx is NULL). */
+const char *mctdh_last_error(mctdh_ctx_t *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MACAW_GB300_H */

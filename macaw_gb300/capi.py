@@ -1,0 +1,320 @@
+"""ctypes binding of ``libmacaw_gb300.so`` (the C-ABI of include/macaw_gb300.h).
+
+``GpuCore`` mirrors the reference routines the C-ABI replaces, with the same
+names and argument meaning: ``calc_derivs`` (derivatives.f90:39), ``rkqs``
+(integrator.f90:36), ``cmf2`` (cmf2_base.f90:47), ``norm_wf`` / ``wf_ovl``
+(gmctdh_objects.f90:21, :101) and the inner loop of ``propagate_wf``
+(propagator.f90:110-146).  Errors come back as ``MctdhError`` carrying the
+C-ABI status, the way the reference would ``stop``.  There is no CPU path:
+if the library or a GPU is missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from .model import Model, INT_CMF2
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "libmacaw_gb300.so")
+
+I64P = C.POINTER(C.c_int64)
+DP = C.POINTER(C.c_double)
+
+STATUS = {0: "ok", -1: "unsupported feature", -2: "eigensolver did not converge", -3: "Krylov cap reached",
+          -4: "step underflow", -5: "non-finite state", -6: "CUDA error", -7: "bad argument"}
+
+
+class MctdhError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {STATUS.get(code, 'error')}: {msg}")
+        self.code = code
+
+
+class Setup(C.Structure):
+    _fields_ = [
+        ("nstates", C.c_int64), ("nmodes", C.c_int64), ("ndof", C.c_int64), ("nham", C.c_int64),
+        ("maxdof", C.c_int64),
+        ("nspf", I64P), ("nmodedof", I64P), ("idof", I64P), ("multiset", I64P), ("is_gwp", I64P),
+        ("ngp", I64P), ("dvr_grid", DP), ("dvr_grid_off", I64P), ("dvr_mats", DP), ("dvr_mat_off", I64P),
+        ("ae", DP), ("lhs_el", I64P), ("rhs_el", I64P), ("nopermax", C.c_int64), ("noper", I64P),
+        ("oper", I64P), ("ioper", I64P), ("is_identity", I64P), ("skip_term", I64P), ("ipsispf", I64P),
+        ("dimpsi", C.c_int64), ("gwpa", DP), ("ns00max", C.c_int64),
+        ("eps_rho", C.c_double), ("eps_ovl", C.c_double), ("eps_C", C.c_double), ("eps_int", C.c_double),
+        ("eps_A", C.c_double), ("eps_psi", C.c_double), ("min_stepsize", C.c_double),
+        ("writetime", C.c_double), ("der_factor_re", C.c_double), ("der_factor_im", C.c_double),
+        ("int_type_psi", C.c_int64), ("precision", C.c_int64),
+    ]
+
+
+_lib = None
+
+
+def load_library() -> C.CDLL:
+    """Load the in-tree shared library; raise loudly if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise MctdhError(-6, f"{LIBPATH} is missing: run __graft_entry__.build() (there is no CPU fallback)")
+    lib = C.CDLL(LIBPATH)
+    vp = C.c_void_p
+    lib.mctdh_create.argtypes = [C.POINTER(Setup), C.POINTER(vp)]
+    lib.mctdh_destroy.argtypes = [vp]
+    lib.mctdh_calc_derivs.argtypes = [vp, DP, DP, DP, DP, C.c_double]
+    lib.mctdh_rkqs.argtypes = [vp, DP, DP, DP, DP, C.c_double, C.c_double, DP, DP, C.c_int64]
+    lib.mctdh_cmf2.argtypes = [vp, DP, DP, C.c_double, C.c_double, DP, DP]
+    lib.mctdh_rk_attempt.argtypes = [vp, DP, DP, DP, DP, C.c_double, C.c_double, C.c_int64, DP]
+    lib.mctdh_cmf2_attempt.argtypes = [vp, DP, DP, C.c_double, C.c_double, DP]
+    lib.mctdh_set_state.argtypes = [vp, DP, DP, C.c_int64]
+    lib.mctdh_get_state.argtypes = [vp, DP, DP]
+    lib.mctdh_propagate.argtypes = [vp, C.c_int64, C.c_double, DP, DP, I64P, I64P, I64P]
+    lib.mctdh_observables.argtypes = [vp, C.c_double, DP, DP, DP, DP, DP]
+    lib.mctdh_norm_wf.argtypes = [vp, DP, DP, DP]
+    lib.mctdh_wf_ovl.argtypes = [vp, DP, DP, DP, DP, DP, DP]
+    lib.mctdh_launch_count.argtypes = [vp]
+    lib.mctdh_last_error.argtypes = [vp]
+    lib.mctdh_last_error.restype = C.c_char_p
+    for name in ("mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", "mctdh_cmf2",
+                 "mctdh_rk_attempt", "mctdh_cmf2_attempt",
+                 "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
+                 "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count"):
+        getattr(lib, name).restype = C.c_int64
+    _lib = lib
+    return lib
+
+
+EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", "mctdh_cmf2",
+            "mctdh_rk_attempt", "mctdh_cmf2_attempt",
+            "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
+            "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error"]
+
+
+def _i64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int64))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _ptr(a: np.ndarray, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
+    """Flatten the model into the C struct (Fortran column-major conventions)."""
+    keep: list = []
+    nm, ns, nd = model.nmodes, model.nstates, model.ndof
+    maxdof = max(len(d) for d in model.mode_dofs)
+
+    def I(a):
+        arr = _i64(a)
+        keep.append(arr)
+        return _ptr(arr, C.c_int64)
+
+    def F(a):
+        arr = _f64(a)
+        keep.append(arr)
+        return _ptr(arr)
+
+    idof = np.full((maxdof, nm), -1, dtype=np.int64)
+    for m in range(nm):
+        idof[:len(model.mode_dofs[m]), m] = model.mode_dofs[m]
+    grid_parts, grid_off, mat_parts, mat_off = [], [], [], []
+    go = mo = 0
+    for d in range(nd):
+        if model.dvr_type[d] == "gwp":
+            grid_off.append(-1)
+            mat_off.append(-1)
+            continue
+        g = model.grid[d]
+        grid_parts.append(g)
+        grid_off.append(go)
+        go += len(g)
+        mats = np.concatenate([model.d1[d].reshape(-1, order="F"), model.d2[d].reshape(-1, order="F"),
+                               model.xd1[d].reshape(-1, order="F")])
+        mat_parts.append(mats)
+        mat_off.append(mo)
+        mo += len(mats)
+    grid = np.concatenate(grid_parts) if grid_parts else np.zeros(1)
+    mats = np.concatenate(mat_parts) if mat_parts else np.zeros(1)
+    w = 2 + maxdof
+    oper = np.zeros((w, model.nopermax, nm), dtype=np.int64)
+    for m in range(nm):
+        for k, (l, r, dops) in enumerate(model.oper[m]):
+            oper[0, k, m] = l
+            oper[1, k, m] = r
+            oper[2:2 + len(dops), k, m] = dops
+    ae = np.empty(2 * model.nham)
+    ae[0::2] = model.ae.real
+    ae[1::2] = model.ae.imag
+    gwpa = getattr(model, "gwpa", None)
+    if gwpa is None or gwpa.size == 0:
+        gwpa = np.zeros(1)
+    s = Setup()
+    s.nstates, s.nmodes, s.ndof, s.nham, s.maxdof = ns, nm, nd, model.nham, maxdof
+    s.nspf = I(model.nspf.reshape(-1, order="F"))
+    s.nmodedof = I([len(d) for d in model.mode_dofs])
+    s.idof = I(idof.reshape(-1, order="F"))
+    s.multiset = I([1 if x else 0 for x in model.multiset])
+    s.is_gwp = I([1 if x else 0 for x in model.is_gwp_mode])
+    s.ngp = I(model.ngp)
+    s.dvr_grid = F(grid)
+    s.dvr_grid_off = I(grid_off)
+    s.dvr_mats = F(mats)
+    s.dvr_mat_off = I(mat_off)
+    s.ae = F(ae)
+    s.lhs_el = I(model.lhs_el)
+    s.rhs_el = I(model.rhs_el)
+    s.nopermax = model.nopermax
+    s.noper = I([len(o) for o in model.oper])
+    s.oper = I(oper.reshape(-1, order="F"))
+    s.ioper = I(model.ioper.reshape(-1, order="F"))
+    s.is_identity = I(model.is_identity.astype(np.int64).reshape(-1, order="F"))
+    s.skip_term = I(model.skip_term.astype(np.int64).reshape(-1, order="F"))
+    s.ipsispf = I(model.ipsispf.reshape(-1, order="F"))
+    s.dimpsi = model.dimpsi
+    s.gwpa = F(np.asarray(gwpa).reshape(-1, order="F"))
+    s.ns00max = model.ns00max
+    s.eps_rho, s.eps_ovl, s.eps_C = model.eps_rho, model.eps_ovl, model.eps_C
+    s.eps_int, s.eps_A, s.eps_psi = model.eps_int, model.eps_A, model.eps_psi
+    s.min_stepsize, s.writetime = model.min_stepsize, model.tout
+    s.der_factor_re, s.der_factor_im = model.der_factor.real, model.der_factor.imag
+    s.int_type_psi = model.int_type_psi
+    s.precision = precision
+    return s, keep
+
+
+def _cbuf(x: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+
+
+class GpuCore:
+    """One device context for one model (one CUDA stream on the current device)."""
+
+    def __init__(self, model: Model, precision: int = 0):
+        self.lib = load_library()
+        self.model = model
+        setup, self._keep = build_setup(model, precision)
+        h = C.c_void_p()
+        rc = self.lib.mctdh_create(C.byref(setup), C.byref(h))
+        if rc != 0:
+            raise MctdhError(rc, self.lib.mctdh_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mctdh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise MctdhError(rc, self.lib.mctdh_last_error(self.h).decode())
+
+    # -- reference-shaped calls on host buffers --
+    def calc_derivs(self, A, psi, t: float = 0.0):
+        A, psi = _cbuf(A), _cbuf(psi)
+        dA = np.empty_like(A)
+        dpsi = np.empty_like(psi)
+        self._check(self.lib.mctdh_calc_derivs(self.h, _ptr(A), _ptr(psi), _ptr(dA), _ptr(dpsi), t))
+        return dA, dpsi
+
+    def rkqs(self, A, psi, dA, dpsi, t: float, htry: float, method: int = 1):
+        A, psi, dA, dpsi = _cbuf(A).copy(), _cbuf(psi).copy(), _cbuf(dA).copy(), _cbuf(dpsi).copy()
+        hdid, hnext = C.c_double(), C.c_double()
+        self._check(self.lib.mctdh_rkqs(self.h, _ptr(A), _ptr(psi), _ptr(dA), _ptr(dpsi), t, htry,
+                                        C.byref(hdid), C.byref(hnext), method))
+        return A, psi, dA, dpsi, hdid.value, hnext.value
+
+    def cmf2(self, A, psi, t: float, htry: float):
+        A, psi = _cbuf(A).copy(), _cbuf(psi).copy()
+        hdid, hnext = C.c_double(), C.c_double()
+        self._check(self.lib.mctdh_cmf2(self.h, _ptr(A), _ptr(psi), t, htry, C.byref(hdid), C.byref(hnext)))
+        return A, psi, hdid.value, hnext.value
+
+    def rk_attempt(self, A, psi, dA, dpsi, t: float, dt: float, method: int = 1):
+        """Fixed-length rkck/rkdp attempt (step replay): returns (A, psi, dA, dpsi, errmax)."""
+        A, psi, dA, dpsi = _cbuf(A).copy(), _cbuf(psi).copy(), _cbuf(dA).copy(), _cbuf(dpsi).copy()
+        err = C.c_double()
+        self._check(self.lib.mctdh_rk_attempt(self.h, _ptr(A), _ptr(psi), _ptr(dA), _ptr(dpsi), t, dt,
+                                              method, C.byref(err)))
+        return A, psi, dA, dpsi, err.value
+
+    def cmf2_attempt(self, A, psi, t: float, h: float):
+        """One CMF2 attempt of length h completed as accepted (step replay)."""
+        A, psi = _cbuf(A).copy(), _cbuf(psi).copy()
+        err = C.c_double()
+        self._check(self.lib.mctdh_cmf2_attempt(self.h, _ptr(A), _ptr(psi), t, h, C.byref(err)))
+        return A, psi, err.value
+
+    def norm_wf(self, A, psi) -> float:
+        A, psi = _cbuf(A), _cbuf(psi)
+        out = C.c_double()
+        self._check(self.lib.mctdh_norm_wf(self.h, _ptr(A), _ptr(psi), C.byref(out)))
+        return out.value
+
+    def wf_ovl(self, A1, psi1, A2, psi2) -> complex:
+        A1, psi1, A2, psi2 = _cbuf(A1), _cbuf(psi1), _cbuf(A2), _cbuf(psi2)
+        re, im = C.c_double(), C.c_double()
+        self._check(self.lib.mctdh_wf_ovl(self.h, _ptr(A1), _ptr(psi1), _ptr(A2), _ptr(psi2),
+                                          C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+    # -- device-resident propagation --
+    def set_state(self, A, psi, as_start: bool = True):
+        A, psi = _cbuf(A), _cbuf(psi)
+        self._check(self.lib.mctdh_set_state(self.h, _ptr(A), _ptr(psi), 1 if as_start else 0))
+
+    def get_state(self):
+        A = np.empty(self.model.naconftot, dtype=np.complex128)
+        psi = np.empty(self.model.dimpsi, dtype=np.complex128)
+        self._check(self.lib.mctdh_get_state(self.h, _ptr(A), _ptr(psi)))
+        return A, psi
+
+    def observables(self, t: float) -> Dict:
+        e, nrm, ar, ai = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        pop = np.zeros(self.model.nstates)
+        self._check(self.lib.mctdh_observables(self.h, t, C.byref(e), _ptr(pop), C.byref(nrm),
+                                               C.byref(ar), C.byref(ai)))
+        return dict(t=t, pop=pop, norm=nrm.value, energy=e.value, auto=complex(ar.value, ai.value))
+
+    def propagate_interval(self, int_type: int, tnext: float, t: float, step: float):
+        tt, ss = C.c_double(t), C.c_double(step)
+        ns, na, ne = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.mctdh_propagate(self.h, int_type, tnext, C.byref(tt), C.byref(ss),
+                                             C.byref(ns), C.byref(na), C.byref(ne)))
+        return tt.value, ss.value, ns.value, na.value, ne.value
+
+    def launch_count(self) -> int:
+        return int(self.lib.mctdh_launch_count(self.h))
+
+    def propagate(self, A, psi, tfinal: Optional[float] = None, int_type: Optional[int] = None):
+        """propagate_wf (propagator.f90:87-146, :257-306) on the device; returns the
+        outputs written every tout, like the oracle's ``propagate``."""
+        md = self.model
+        it = md.int_type if int_type is None else int_type
+        self.set_state(A, psi, as_start=True)
+        tfin = md.tfinal if tfinal is None else tfinal
+        maxtime = tfin + md.tout * 0.1
+        t = md.tinit
+        step = md.tout * md.eps_int
+        outs = []
+        stats = dict(steps=0, attempts=0, eom=0)
+        while t < maxtime:
+            outs.append(self.observables(t))
+            t, step, ns, na, ne = self.propagate_interval(it, t + md.tout, t, step)
+            stats["steps"] += ns
+            stats["attempts"] += na
+            stats["eom"] += ne
+        self.stats = stats
+        return outs

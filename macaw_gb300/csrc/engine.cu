@@ -1,0 +1,1585 @@
+// Host side of the G-MCTDH propagation core: plans the batched kernels for one
+// model once (mctdh_create), then runs the equation of motion, the adaptive
+// Runge-Kutta steps, the CMF2 steps and the observables on device-resident
+// state.  The C-ABI it exports is declared in include/macaw_gb300.h.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/macaw_gb300.h"
+#include "kernels.cuh"
+
+namespace {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+struct StatusError : std::runtime_error {
+  int64_t code;
+  StatusError(int64_t c, const std::string& s) : std::runtime_error(s), code(c) {}
+};
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_) + " at " __FILE__ ":" + \
+                      std::to_string(__LINE__));                                                  \
+  } while (0)
+
+std::string g_create_error;
+
+// Bump allocator over large device chunks; buffers live as long as the context.
+struct DevArena {
+  std::vector<void*> chunks;
+  char* cur = nullptr;
+  size_t left = 0;
+  size_t total = 0;
+  void* alloc(size_t bytes) {
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (bytes == 0) bytes = 256;
+    if (bytes > left) {
+      size_t sz = std::max(bytes, (size_t)64 << 20);
+      void* p = nullptr;
+      CK(cudaMalloc(&p, sz));
+      chunks.push_back(p);
+      cur = (char*)p;
+      left = sz;
+      total += sz;
+    }
+    void* r = cur;
+    cur += bytes;
+    left -= bytes;
+    return r;
+  }
+  cplx* calloc_c(long long n) { return (cplx*)alloc(sizeof(cplx) * (size_t)std::max(n, 1LL)); }
+  ~DevArena() {
+    for (void* p : chunks) cudaFree(p);
+  }
+};
+
+template <typename T>
+T* upload_vec(DevArena& ar, const std::vector<T>& v) {
+  if (v.empty()) return nullptr;
+  T* d = (T*)ar.alloc(sizeof(T) * v.size());
+  CK(cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return d;
+}
+
+// A tensor view: device pointer + per-mode sizes (mode 1 fastest).
+struct TRef {
+  cplx* p = nullptr;
+  std::vector<int> shape;
+};
+long long prod_range(const std::vector<int>& s, int a, int b) {
+  long long r = 1;
+  for (int i = a; i < b; ++i) r *= s[i];
+  return r;
+}
+
+struct ProdBatch {
+  std::vector<ProdDesc> h;
+  ProdDesc* d = nullptr;
+  long long nblocks = 0;
+  int maxn = 0;
+  void add(const cplx* X, cplx* Y, const cplx* M, int ldm, int conjT, const std::vector<int>& shape, int mode,
+           int nout, cplx alpha, int accumulate) {
+    ProdDesc pd;
+    memset(&pd, 0, sizeof(pd));
+    pd.X = X;
+    pd.Y = Y;
+    pd.M = M;
+    pd.ldm = ldm;
+    pd.conjT = conjT;
+    pd.L = prod_range(shape, 0, mode);
+    pd.R = prod_range(shape, mode + 1, (int)shape.size());
+    pd.nin = shape[mode];
+    pd.nout = nout;
+    pd.alpha = alpha;
+    pd.accumulate = accumulate;
+    h.push_back(pd);
+  }
+  void finalize(DevArena& ar) {
+    nblocks = 0;
+    maxn = 0;
+    for (auto& pd : h) {
+      pd.block_start = nblocks;
+      nblocks += (pd.L * pd.R + 127) / 128;
+      maxn = std::max(maxn, std::max(pd.nin, pd.nout));
+    }
+    d = upload_vec(ar, h);
+  }
+};
+
+struct HoleBatch {
+  std::vector<HoleDesc> h;
+  HoleDesc* d = nullptr;
+  long long nblocks = 0;
+  // returns index of the hole
+  int add(DevArena& ar, const cplx* X, const cplx* Y, long long L, long long R, int n1, int n2) {
+    HoleDesc hd;
+    memset(&hd, 0, sizeof(hd));
+    hd.X = X;
+    hd.Y = Y;
+    hd.L = L;
+    hd.R = R;
+    hd.n1 = n1;
+    hd.n2 = n2;
+    long long ntiles = (L * R + HOLE_TILE - 1) / HOLE_TILE;
+    hd.nblk = (int)std::min<long long>(std::max<long long>(ntiles / 8, 1), 64);
+    hd.partial = ar.calloc_c((long long)hd.nblk * n1 * n2);
+    h.push_back(hd);
+    return (int)h.size() - 1;
+  }
+  void finalize(DevArena& ar) {
+    nblocks = 0;
+    for (auto& hd : h) {
+      hd.block_start = nblocks;
+      nblocks += hd.nblk;
+    }
+    d = upload_vec(ar, h);
+  }
+};
+
+struct RedBatch {
+  std::vector<RedTarget> tg;
+  std::vector<RedTerm> terms;
+  std::vector<std::vector<RedTerm>> pending;
+  RedTarget* d_tg = nullptr;
+  RedTerm* d_terms = nullptr;
+  int add_target(cplx* out, int n1, int n2, int ld, int hermitize, int accumulate = 0) {
+    RedTarget t;
+    memset(&t, 0, sizeof(t));
+    t.out = out;
+    t.n1 = n1;
+    t.n2 = n2;
+    t.ld = ld;
+    t.hermitize = hermitize;
+    t.accumulate = accumulate;
+    tg.push_back(t);
+    pending.emplace_back();
+    return (int)tg.size() - 1;
+  }
+  void add_term(int target, const HoleDesc& hd, cplx alpha) {
+    RedTerm rt;
+    memset(&rt, 0, sizeof(rt));
+    rt.partial = hd.partial;
+    rt.nblk = hd.nblk;
+    rt.alpha = alpha;
+    pending[target].push_back(rt);
+  }
+  void finalize(DevArena& ar) {
+    terms.clear();
+    for (size_t i = 0; i < tg.size(); ++i) {
+      tg[i].first = (int)terms.size();
+      tg[i].count = (int)pending[i].size();
+      for (auto& r : pending[i]) terms.push_back(r);
+    }
+    d_tg = upload_vec(ar, tg);
+    d_terms = upload_vec(ar, terms);
+  }
+};
+
+// Holes whose partials must be finalised before the reduce: the hole descriptors
+// are finalised first, then the reduce terms are built from them.
+struct HoleRef {
+  int hole;
+  int target;
+  cplx alpha;
+};
+
+// Plan of one overlap evaluation <Psi1|Psi2> / norms (norm_wf, WF_Ovl, DeltaPsi).
+struct OvlPlan {
+  HoleBatch spf_holes;           // SPF overlap matrices
+  RedBatch spf_red;
+  std::vector<ProdBatch> chain;  // one batch per mode step
+  HoleBatch dots;
+  RedBatch dot_red;
+  cplx* d_result = nullptr;      // [3] o11, o22, o12
+};
+
+struct DotPlan {
+  HoleBatch hb;
+  RedBatch red;
+  cplx* res = nullptr;
+};
+
+struct Ctx {
+  std::map<std::pair<const void*, const void*>, DotPlan*> dots;
+  bool fsal_valid = false;   // Dormand-Prince derivative carried between steps
+  // model
+  int nstates = 0, nmodes = 0, ndof = 0, nham = 0, maxdof = 0, nopermax = 0;
+  std::vector<int> nspf;  // [m + nmodes*s]
+  std::vector<int> nmodedof, multiset, is_gwp, ngp;
+  std::vector<std::vector<int>> mode_dofs;
+  std::vector<cplx> ae;
+  std::vector<int> lhs, rhs, noper, ioper, is_identity, skip_term;
+  std::vector<std::vector<std::vector<int>>> oper;  // [m][k] -> {l, r, codes...}
+  std::vector<long long> naconf, aoff, ipsi;
+  long long naconftot = 0, dimpsi = 0, ntot = 0;
+  std::vector<int> modes_dvr;
+  std::vector<int> gmode;  // grid size G of DVR modes
+  double eps_rho = 1e-8, eps_ovl = 1e-8, eps_C = 1e-8, eps_int = 1e-8, eps_A = 1e-8, eps_psi = 1e-8;
+  double min_stepsize = 0, writetime = 0;
+  cplx der = mkc(0, -1);
+  int int_type_psi = 1;
+  int precision = 0;
+  std::string last_error;
+  long long launches = 0;
+  long long eom_count = 0, hb_count = 0;
+
+  cudaStream_t st = nullptr;
+  DevArena ar;
+  int* d_status = nullptr;
+  cplx* d_y = nullptr;      // resident state [A | psi]
+  cplx* d_y0 = nullptr;     // start state (for C(t))
+  cplx* d_in = nullptr;     // EOM input
+  cplx* d_out = nullptr;    // EOM output scratch
+  cplx* d_k[7] = {};
+  cplx* d_tmp = nullptr;
+  cplx* d_err = nullptr;
+  cplx* d_hb = nullptr;     // H*B output
+  double* d_scal = nullptr; // small scalars
+
+  // DVR operator matrices on device: (dof, code) -> pointer
+  std::map<std::pair<int, int>, cplx*> dofmat;
+  std::map<std::pair<int, int>, int> dofkind;
+
+  // per (mode, op) storage
+  std::vector<std::vector<cplx*>> hmat, ophi, mf, rhom1mf;  // [m][k]
+  std::vector<std::vector<cplx*>> rho;                      // [m][s]
+  std::vector<cplx*> rho_ave;                               // [m]
+
+  // EOM plan
+  std::vector<H1Desc> h1_h;
+  H1Desc* h1_d = nullptr;
+  size_t h1_smem = 0;
+  std::vector<ProdBatch> chains;  // per depth
+  HoleBatch holes;
+  RedBatch red;
+  std::vector<RegInvDesc> reg_h;
+  std::vector<MFOp> mfop_h;
+  RegInvDesc* reg_d = nullptr;
+  MFOp* mfop_d = nullptr;
+  std::vector<SpfDesc> spf_h;
+  std::vector<SpfOp> spfop_h;
+  SpfDesc* spf_d = nullptr;
+  SpfOp* spfop_d = nullptr;
+  size_t spf_smem = 0;
+  std::vector<SumRange> sum_h;
+  std::vector<SumSrc> src_h;
+  SumRange* sum_d = nullptr;
+  SumSrc* src_d = nullptr;
+  // H_B * B plan for CMF2 (Calc_DHD_B): reads d_hbin, writes d_hb
+  cplx* d_hbin = nullptr;
+  std::vector<ProdBatch> hb_chains;
+  std::vector<SumSrc> hbsrc_h;
+  SumSrc* hbsrc_d = nullptr;
+  SumRange* hbsum_d = nullptr;
+  // ophi-only h1 plan (CMF2 SPF sweeps: operators on the current SPFs, mean fields frozen)
+  std::vector<std::vector<int>> h1_of_mode;  // indices into h1_h per DVR mode
+  // overlap plans
+  OvlPlan dpsi_plan;   // d_tmp vs d_err
+  OvlPlan auto_plan;   // d_y0 vs d_y (o12), d_y norm (o22)
+  OvlPlan io_plan;     // d_in vs d_out (host API norm/ovl)
+  // CMF2 / Lanczos
+  cplx* d_krylov = nullptr;  // [ntotA x 21]
+  double* d_lan = nullptr;   // alpha[20], beta[20], evals[20], evecs[400]
+  int lan_nk = 0;
+  std::vector<double> lan_evals, lan_evecs;
+  cplx* d_coef = nullptr;
+
+  int m_of(int m, int s) const { return nspf[m + nmodes * s]; }
+  std::vector<int> shape_of(int s) const {
+    std::vector<int> v(nmodes);
+    for (int m = 0; m < nmodes; ++m) v[m] = m_of(m, s);
+    return v;
+  }
+  void count(int n = 1) { launches += n; }
+};
+
+// ---------------------------------------------------------------------------
+// Set-up
+// ---------------------------------------------------------------------------
+void load_setup(Ctx& c, const mctdh_setup_t* s) {
+  c.nstates = (int)s->nstates;
+  c.nmodes = (int)s->nmodes;
+  c.ndof = (int)s->ndof;
+  c.nham = (int)s->nham;
+  c.maxdof = (int)s->maxdof;
+  c.nopermax = (int)s->nopermax;
+  if (c.nstates < 1 || c.nmodes < 1 || c.nham < 1) throw StatusError(MCTDH_EARG, "empty model");
+  c.nspf.resize(c.nmodes * c.nstates);
+  for (int i = 0; i < c.nmodes * c.nstates; ++i) c.nspf[i] = (int)s->nspf[i];
+  c.nmodedof.resize(c.nmodes);
+  c.multiset.resize(c.nmodes);
+  c.is_gwp.resize(c.nmodes);
+  c.mode_dofs.resize(c.nmodes);
+  for (int m = 0; m < c.nmodes; ++m) {
+    c.nmodedof[m] = (int)s->nmodedof[m];
+    c.multiset[m] = (int)s->multiset[m];
+    c.is_gwp[m] = (int)s->is_gwp[m];
+    for (int k = 0; k < c.nmodedof[m]; ++k) c.mode_dofs[m].push_back((int)s->idof[k + c.maxdof * m]);
+    if (c.is_gwp[m]) throw StatusError(MCTDH_EUNSUPPORTED, "Gaussian (GWP) modes are not supported by this build");
+    if (c.nmodedof[m] > MAXDOF_MODE) throw StatusError(MCTDH_EUNSUPPORTED, "too many DOFs in one DVR mode");
+    for (int st = 0; st < c.nstates; ++st)
+      if (c.m_of(m, st) > MAXN_SPF || c.m_of(m, st) < 1)
+        throw StatusError(MCTDH_EUNSUPPORTED, "SPF count outside 1..32");
+  }
+  c.ngp.resize(c.ndof);
+  for (int d = 0; d < c.ndof; ++d) c.ngp[d] = (int)s->ngp[d];
+  c.ae.resize(c.nham);
+  c.lhs.resize(c.nham);
+  c.rhs.resize(c.nham);
+  for (int t = 0; t < c.nham; ++t) {
+    c.ae[t] = mkc(s->ae[2 * t], s->ae[2 * t + 1]);
+    c.lhs[t] = (int)s->lhs_el[t];
+    c.rhs[t] = (int)s->rhs_el[t];
+  }
+  c.noper.resize(c.nmodes);
+  c.oper.resize(c.nmodes);
+  const int w = 2 + c.maxdof;
+  for (int m = 0; m < c.nmodes; ++m) {
+    c.noper[m] = (int)s->noper[m];
+    for (int k = 0; k < c.noper[m]; ++k) {
+      std::vector<int> v;
+      for (int q = 0; q < 2 + c.nmodedof[m]; ++q) v.push_back((int)s->oper[q + w * (k + c.nopermax * m)]);
+      c.oper[m].push_back(v);
+    }
+  }
+  c.ioper.resize(c.nmodes * c.nham);
+  c.skip_term.resize(c.nmodes * c.nham);
+  for (int i = 0; i < c.nmodes * c.nham; ++i) {
+    c.ioper[i] = (int)s->ioper[i];
+    c.skip_term[i] = (int)s->skip_term[i];
+  }
+  c.is_identity.resize(c.nmodes * c.nopermax);
+  for (int i = 0; i < c.nmodes * c.nopermax; ++i) c.is_identity[i] = (int)s->is_identity[i];
+  c.naconf.resize(c.nstates);
+  c.aoff.resize(c.nstates);
+  long long off = 0;
+  for (int st = 0; st < c.nstates; ++st) {
+    long long n = 1;
+    for (int m = 0; m < c.nmodes; ++m) n *= c.m_of(m, st);
+    c.naconf[st] = n;
+    c.aoff[st] = off;
+    off += n;
+  }
+  c.naconftot = off;
+  c.dimpsi = s->dimpsi;
+  c.ntot = c.naconftot + c.dimpsi;
+  c.ipsi.resize(c.nmodes * c.nstates);
+  for (int i = 0; i < c.nmodes * c.nstates; ++i) c.ipsi[i] = s->ipsispf[i];
+  c.gmode.assign(c.nmodes, 0);
+  for (int m = 0; m < c.nmodes; ++m) {
+    if (c.is_gwp[m]) continue;
+    c.modes_dvr.push_back(m);
+    int G = 1;
+    for (int d : c.mode_dofs[m]) G *= c.ngp[d];
+    c.gmode[m] = G;
+  }
+  c.eps_rho = s->eps_rho;
+  c.eps_ovl = s->eps_ovl;
+  c.eps_C = s->eps_C;
+  c.eps_int = s->eps_int;
+  c.eps_A = s->eps_A;
+  c.eps_psi = s->eps_psi;
+  c.min_stepsize = s->min_stepsize;
+  c.writetime = s->writetime;
+  c.der = mkc(s->der_factor_re, s->der_factor_im);
+  c.int_type_psi = (int)s->int_type_psi;
+  c.precision = (int)s->precision;
+  if (c.precision != 0) throw StatusError(MCTDH_EUNSUPPORTED, "split-FP32 precision not available in this build");
+
+  // primitive DOF operator matrices (dense ones in the zlacrm-from-the-right form
+  // with the +i factor of p and qp, hamilton.f90:455-461; diagonal q^k)
+  for (int m : c.modes_dvr) {
+    for (int k = 0; k < c.noper[m]; ++k) {
+      for (int q = 0; q < c.nmodedof[m]; ++q) {
+        int code = c.oper[m][k][2 + q];
+        int d = c.mode_dofs[m][q];
+        if (code == 0) continue;
+        auto key = std::make_pair(d, code);
+        if (c.dofmat.count(key)) continue;
+        int ng = c.ngp[d];
+        const double* mats = s->dvr_mats + s->dvr_mat_off[d];
+        const double* grid = s->dvr_grid + s->dvr_grid_off[d];
+        std::vector<cplx> v;
+        int kind;
+        if (code == -1 || code == -2 || code == -3) {
+          kind = 1;
+          const double* src = code == -1 ? mats : (code == -2 ? mats + ng * ng : mats + 2 * ng * ng);
+          v.resize(ng * ng);
+          for (int i = 0; i < ng * ng; ++i) v[i] = (code == -2) ? mkc(src[i], 0.0) : mkc(0.0, src[i]);
+        } else if (code >= 1 && code <= 20) {
+          kind = 2;
+          v.resize(ng);
+          for (int i = 0; i < ng; ++i) v[i] = mkc(code == 1 ? grid[i] : pow(grid[i], (double)code), 0.0);
+        } else {
+          throw StatusError(MCTDH_EUNSUPPORTED, "primitive operator code " + std::to_string(code) + " not supported");
+        }
+        c.dofmat[key] = upload_vec(c.ar, v);
+        c.dofkind[key] = kind;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Planning of the EOM (Calc_Derivs for DVR models, derivatives.f90:39-156)
+// ---------------------------------------------------------------------------
+void plan_eom(Ctx& c) {
+  const int f = c.nmodes;
+  const int nsm = MAXN_SPF;
+  (void)nsm;
+  c.hmat.assign(f, {});
+  c.ophi.assign(f, {});
+  c.mf.assign(f, {});
+  c.rhom1mf.assign(f, {});
+  c.rho.assign(f, std::vector<cplx*>(c.nstates, nullptr));
+  c.rho_ave.assign(f, nullptr);
+  c.h1_of_mode.assign(f, {});
+  // h1mode / ophi descriptors
+  size_t smem = 0;
+  for (int m : c.modes_dvr) {
+    const int G = c.gmode[m];
+    c.hmat[m].assign(c.noper[m], nullptr);
+    c.ophi[m].assign(c.noper[m], nullptr);
+    c.mf[m].assign(c.noper[m], nullptr);
+    c.rhom1mf[m].assign(c.noper[m], nullptr);
+    for (int k = 0; k < c.noper[m]; ++k) {
+      const int l = c.oper[m][k][0], r = c.oper[m][k][1];
+      const int n1 = c.m_of(m, l), n2 = c.m_of(m, r);
+      c.hmat[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      if (c.is_identity[m + f * k]) {
+        std::vector<cplx> I(n1 * n2, mkc(0, 0));
+        for (int j = 0; j < std::min(n1, n2); ++j) I[j + n1 * j] = mkc(1, 0);
+        CK(cudaMemcpy(c.hmat[m][k], I.data(), sizeof(cplx) * I.size(), cudaMemcpyHostToDevice));
+        continue;
+      }
+      c.ophi[m][k] = c.ar.calloc_c((long long)G * n2);
+      c.mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      c.rhom1mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      H1Desc hd;
+      memset(&hd, 0, sizeof(hd));
+      hd.phi_r = c.d_in + c.naconftot + c.ipsi[m + f * r];
+      hd.phi_l = c.d_in + c.naconftot + c.ipsi[m + f * l];
+      hd.ophi = c.ophi[m][k];
+      hd.h = c.hmat[m][k];
+      hd.G = G;
+      hd.n1 = n1;
+      hd.n2 = n2;
+      hd.same_state = (l == r);
+      hd.ndof = c.nmodedof[m];
+      for (int q = 0; q < hd.ndof; ++q) {
+        int d = c.mode_dofs[m][q];
+        int code = c.oper[m][k][2 + q];
+        hd.ng[q] = c.ngp[d];
+        if (code == 0) {
+          hd.optype[q] = 0;
+        } else {
+          auto key = std::make_pair(d, code);
+          hd.optype[q] = c.dofkind[key];
+          hd.mat[q] = c.dofmat[key];
+        }
+      }
+      c.h1_of_mode[m].push_back((int)c.h1_h.size());
+      c.h1_h.push_back(hd);
+      smem = std::max(smem, sizeof(cplx) * (size_t)(2 * G * n2 + MAXN_SPF * MAXN_SPF));
+    }
+  }
+  c.h1_smem = smem;
+  c.h1_d = upload_vec(c.ar, c.h1_h);
+
+  // term chains (Calc_MeanField, gmctdh_objects.f90:513-601)
+  c.chains.assign(f + 1, ProdBatch());
+  std::vector<HoleRef> hrefs;
+  std::vector<std::vector<SumSrc>> srcs(c.nstates);
+  std::map<std::pair<int, int>, int> mf_target;   // (m,k) -> red target
+  for (int t = 0; t < c.nham; ++t) {
+    const int s1 = c.lhs[t], s2 = c.rhs[t];
+    std::vector<TRef> R(f + 1), L(f);
+    R[0].p = c.d_in + c.aoff[s2];
+    R[0].shape = c.shape_of(s2);
+    for (int i = 1; i <= f; ++i) {
+      const int jm = f - i;
+      if (c.skip_term[jm + f * t]) { R[i] = R[i - 1]; continue; }
+      const int k = c.ioper[jm + f * t];
+      const int n1 = c.m_of(jm, s1);
+      std::vector<int> ns = R[i - 1].shape;
+      ns[jm] = n1;
+      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+      c.chains[i].add(R[i - 1].p, out, c.hmat[jm][k], n1, 0, R[i - 1].shape, jm, n1, mkc(1, 0), 0);
+      R[i].p = out;
+      R[i].shape = ns;
+    }
+    L[0].p = c.d_in + c.aoff[s1];
+    L[0].shape = c.shape_of(s1);
+    for (int i = 1; i <= f - 1; ++i) {
+      const int im = i - 1;
+      if (c.skip_term[im + f * t]) { L[i] = L[i - 1]; continue; }
+      const int k = c.ioper[im + f * t];
+      const int n1 = c.m_of(im, s1), n2 = c.m_of(im, s2);
+      std::vector<int> ns = L[i - 1].shape;
+      ns[im] = n2;
+      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+      c.chains[i].add(L[i - 1].p, out, c.hmat[im][k], n1, 1, L[i - 1].shape, im, n2, mkc(1, 0), 0);
+      L[i].p = out;
+      L[i].shape = ns;
+    }
+    srcs[s1].push_back(SumSrc{R[f].p, cmul(c.der, c.ae[t])});
+    for (int im = 0; im < f; ++im) {
+      const int k = c.ioper[im + f * t];
+      if (c.is_identity[im + f * k]) continue;
+      const TRef& X = L[im];
+      const TRef& Y = R[f - 1 - im];
+      long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, f);
+      int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im]);
+      auto key = std::make_pair(im, k);
+      if (!mf_target.count(key)) {
+        const int l = c.oper[im][k][0], r = c.oper[im][k][1];
+        int n1 = c.m_of(im, l), n2 = c.m_of(im, r);
+        mf_target[key] = c.red.add_target(c.mf[im][k], n1, n2, n1, 0);
+      }
+      hrefs.push_back(HoleRef{hidx, mf_target[key], c.ae[t]});
+    }
+  }
+  // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
+  for (int m : c.modes_dvr) {
+    int ave_target = -1;
+    if (!c.multiset[m]) {
+      int n = c.m_of(m, 0);
+      c.rho_ave[m] = c.ar.calloc_c((long long)n * n);
+      ave_target = c.red.add_target(c.rho_ave[m], n, n, n, 1);
+    }
+    for (int s = 0; s < c.nstates; ++s) {
+      int n = c.m_of(m, s);
+      c.rho[m][s] = c.ar.calloc_c((long long)n * n);
+      std::vector<int> sh = c.shape_of(s);
+      int hidx = c.holes.add(c.ar, c.d_in + c.aoff[s], c.d_in + c.aoff[s], prod_range(sh, 0, m),
+                             prod_range(sh, m + 1, f), n, n);
+      int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
+      hrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
+      if (ave_target >= 0) hrefs.push_back(HoleRef{hidx, ave_target, mkc(1, 0)});
+    }
+  }
+  for (auto& b : c.chains) b.finalize(c.ar);
+  c.holes.finalize(c.ar);
+  for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha);
+  c.red.finalize(c.ar);
+
+  // regularised inverse of rho times the mean fields (Calc_rhom1MF, gmctdh_objects.f90:1147-1194)
+  for (int m : c.modes_dvr) {
+    std::vector<int> states;
+    if (c.multiset[m]) for (int s = 0; s < c.nstates; ++s) states.push_back(s);
+    else states.push_back(0);
+    for (int s : states) {
+      RegInvDesc rd;
+      memset(&rd, 0, sizeof(rd));
+      rd.A = c.multiset[m] ? c.rho[m][s] : c.rho_ave[m];
+      rd.n = c.m_of(m, s);
+      rd.regtype = 0;
+      rd.eps = c.eps_rho;
+      rd.op_first = (int)c.mfop_h.size();
+      for (int k = 0; k < c.noper[m]; ++k) {
+        if (c.is_identity[m + f * k]) continue;
+        if (c.multiset[m] && c.oper[m][k][0] != s) continue;
+        MFOp op;
+        memset(&op, 0, sizeof(op));
+        op.mf = c.mf[m][k];
+        op.out = c.rhom1mf[m][k];
+        op.n2 = c.m_of(m, c.oper[m][k][1]);
+        c.mfop_h.push_back(op);
+      }
+      rd.op_count = (int)c.mfop_h.size() - rd.op_first;
+      c.reg_h.push_back(rd);
+    }
+  }
+  c.reg_d = upload_vec(c.ar, c.reg_h);
+  c.mfop_d = upload_vec(c.ar, c.mfop_h);
+
+  // SPF derivatives (derivatives.f90:96-153)
+  size_t ssmem = 0;
+  for (int m : c.modes_dvr) {
+    std::vector<int> states;
+    if (c.multiset[m]) for (int s = 0; s < c.nstates; ++s) states.push_back(s);
+    else states.push_back(0);
+    for (int s : states) {
+      SpfDesc sd;
+      memset(&sd, 0, sizeof(sd));
+      sd.phi = c.d_in + c.naconftot + c.ipsi[m + f * s];
+      sd.out_offset = c.naconftot + c.ipsi[m + f * s];
+      sd.G = c.gmode[m];
+      sd.n = c.m_of(m, s);
+      sd.op_first = (int)c.spfop_h.size();
+      for (int k = 0; k < c.noper[m]; ++k) {
+        if (c.is_identity[m + f * k]) continue;
+        if (c.multiset[m] && c.oper[m][k][0] != s) continue;
+        SpfOp op;
+        memset(&op, 0, sizeof(op));
+        op.ophi = c.ophi[m][k];
+        op.rm = c.rhom1mf[m][k];
+        op.n2 = c.m_of(m, c.oper[m][k][1]);
+        c.spfop_h.push_back(op);
+      }
+      sd.op_count = (int)c.spfop_h.size() - sd.op_first;
+      c.spf_h.push_back(sd);
+      ssmem = std::max(ssmem, sizeof(cplx) * (size_t)(2 * sd.G * sd.n));
+    }
+  }
+  c.spf_smem = ssmem;
+  c.spf_d = upload_vec(c.ar, c.spf_h);
+  c.spfop_d = upload_vec(c.ar, c.spfop_h);
+
+  // dA = f * sum_t ae_t * (H_t A)   (conjugate of Adot_tmp, gmctdh_objects.f90:578; derivatives.f90:155-156)
+  for (int s = 0; s < c.nstates; ++s) {
+    SumRange r;
+    r.offset = c.aoff[s];
+    r.n = c.naconf[s];
+    r.first = (int)c.src_h.size();
+    r.count = (int)srcs[s].size();
+    for (auto& x : srcs[s]) c.src_h.push_back(x);
+    c.sum_h.push_back(r);
+  }
+  c.sum_d = upload_vec(c.ar, c.sum_h);
+  c.src_d = upload_vec(c.ar, c.src_h);
+}
+
+// H_B * B for the CMF2 Lanczos (Calc_DHD_B, cmf2_derivatives.f90:1-80): chains over
+// the non-identity operators of each term, no der_factor.
+void plan_hb(Ctx& c) {
+  const int f = c.nmodes;
+  c.hb_chains.assign(f + 1, ProdBatch());
+  std::vector<std::vector<SumSrc>> srcs(c.nstates);
+  for (int t = 0; t < c.nham; ++t) {
+    const int s1 = c.lhs[t], s2 = c.rhs[t];
+    TRef cur;
+    cur.p = c.d_hbin + c.aoff[s2];
+    cur.shape = c.shape_of(s2);
+    int depth = 0;
+    for (int m : c.modes_dvr) {
+      const int k = c.ioper[m + f * t];
+      if (c.is_identity[m + f * k]) continue;
+      const int n1 = c.m_of(m, s1);
+      std::vector<int> ns = cur.shape;
+      ns[m] = n1;
+      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+      ++depth;
+      c.hb_chains[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0);
+      cur.p = out;
+      cur.shape = ns;
+    }
+    srcs[s1].push_back(SumSrc{cur.p, c.ae[t]});
+  }
+  for (auto& b : c.hb_chains) b.finalize(c.ar);
+  std::vector<SumRange> ranges;
+  for (int s = 0; s < c.nstates; ++s) {
+    SumRange r;
+    r.offset = c.aoff[s];
+    r.n = c.naconf[s];
+    r.first = (int)c.hbsrc_h.size();
+    r.count = (int)srcs[s].size();
+    for (auto& x : srcs[s]) c.hbsrc_h.push_back(x);
+    ranges.push_back(r);
+  }
+  c.hbsum_d = upload_vec(c.ar, ranges);
+  c.hbsrc_d = upload_vec(c.ar, c.hbsrc_h);
+}
+
+// Overlap plan between states y1 and y2: o11 = <1|1>, o22 = <2|2>, o12 = <1|2>
+// (norm_wf / WF_Ovl / DeltaPsi, gmctdh_objects.f90:21-226).
+void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2) {
+  const int f = c.nmodes;
+  P.d_result = c.ar.calloc_c(3);
+  struct Smat { cplx* s11; cplx* s22; cplx* s12; };
+  std::vector<std::vector<Smat>> S(f, std::vector<Smat>(c.nstates));
+  std::vector<HoleRef> hrefs;
+  for (int m : c.modes_dvr) {
+    for (int s = 0; s < c.nstates; ++s) {
+      if (!c.multiset[m] && s > 0) { S[m][s] = S[m][0]; continue; }
+      const int n = c.m_of(m, s);
+      const long long G = c.gmode[m];
+      cplx* p1 = y1 + c.naconftot + c.ipsi[m + f * s];
+      cplx* p2 = y2 + c.naconftot + c.ipsi[m + f * s];
+      Smat sm;
+      sm.s11 = c.ar.calloc_c((long long)n * n);
+      sm.s22 = c.ar.calloc_c((long long)n * n);
+      sm.s12 = c.ar.calloc_c((long long)n * n);
+      int h11 = P.spf_holes.add(c.ar, p1, p1, G, 1, n, n);
+      int h22 = P.spf_holes.add(c.ar, p2, p2, G, 1, n, n);
+      int h12 = P.spf_holes.add(c.ar, p1, p2, G, 1, n, n);
+      hrefs.push_back(HoleRef{h11, P.spf_red.add_target(sm.s11, n, n, n, 1), mkc(1, 0)});
+      hrefs.push_back(HoleRef{h22, P.spf_red.add_target(sm.s22, n, n, n, 1), mkc(1, 0)});
+      hrefs.push_back(HoleRef{h12, P.spf_red.add_target(sm.s12, n, n, n, 0), mkc(1, 0)});
+      S[m][s] = sm;
+    }
+  }
+  P.spf_holes.finalize(c.ar);
+  for (auto& hr : hrefs) P.spf_red.add_term(hr.target, P.spf_holes.h[hr.hole], hr.alpha);
+  P.spf_red.finalize(c.ar);
+  P.chain.assign(c.modes_dvr.size() + 1, ProdBatch());
+  std::vector<HoleRef> drefs;
+  int t11 = P.dot_red.add_target(P.d_result + 0, 1, 1, 1, 0);
+  int t22 = P.dot_red.add_target(P.d_result + 1, 1, 1, 1, 0);
+  int t12 = P.dot_red.add_target(P.d_result + 2, 1, 1, 1, 0);
+  for (int s = 0; s < c.nstates; ++s) {
+    std::vector<int> sh = c.shape_of(s);
+    const long long N = c.naconf[s];
+    cplx* a1 = y1 + c.aoff[s];
+    cplx* a2 = y2 + c.aoff[s];
+    cplx* cur[3] = {a1, a2, a2};
+    for (size_t i = 0; i < c.modes_dvr.size(); ++i) {
+      const int m = c.modes_dvr[i];
+      const int n = sh[m];
+      cplx* mats[3] = {S[m][s].s11, S[m][s].s22, S[m][s].s12};
+      for (int q = 0; q < 3; ++q) {
+        cplx* out = c.ar.calloc_c(N);
+        P.chain[i + 1].add(cur[q], out, mats[q], n, 0, sh, m, n, mkc(1, 0), 0);
+        cur[q] = out;
+      }
+    }
+    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[0], N, 1, 1, 1), t11, mkc(1, 0)});
+    drefs.push_back(HoleRef{P.dots.add(c.ar, a2, cur[1], N, 1, 1, 1), t22, mkc(1, 0)});
+    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[2], N, 1, 1, 1), t12, mkc(1, 0)});
+  }
+  for (auto& b : P.chain) b.finalize(c.ar);
+  P.dots.finalize(c.ar);
+  for (auto& hr : drefs) P.dot_red.add_term(hr.target, P.dots.h[hr.hole], hr.alpha);
+  P.dot_red.finalize(c.ar);
+}
+
+// ---------------------------------------------------------------------------
+// Execution
+// ---------------------------------------------------------------------------
+void run_prod(Ctx& c, const ProdBatch& b) {
+  if (b.h.empty()) return;
+  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, c.st);
+  c.count();
+}
+void run_hole(Ctx& c, const HoleBatch& b) {
+  if (b.h.empty()) return;
+  launch_hole(b.d, (int)b.h.size(), b.nblocks, c.st);
+  c.count();
+}
+void run_red(Ctx& c, const RedBatch& b) {
+  if (b.tg.empty()) return;
+  launch_reduce(b.d_tg, (int)b.tg.size(), b.d_terms, c.st);
+  c.count();
+}
+
+// EOM on d_in -> out (full vector [dA | dpsi]).
+void eom(Ctx& c, cplx* out) {
+  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
+  c.count();
+  for (size_t i = 1; i < c.chains.size(); ++i) run_prod(c, c.chains[i]);
+  run_hole(c, c.holes);
+  run_red(c, c.red);
+  launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
+  c.count();
+  launch_termsum(out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st);
+  c.count();
+  launch_spf(c.spf_d, (int)c.spf_h.size(), c.spfop_d, out, c.der, c.spf_smem, c.d_status, c.st);
+  c.count();
+  c.eom_count++;
+}
+
+void eom_from(Ctx& c, const cplx* y, cplx* out) {
+  if (y != c.d_in) CK(cudaMemcpyAsync(c.d_in, y, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+  eom(c, out);
+}
+
+void run_ovl(Ctx& c, OvlPlan& P) {
+  run_hole(c, P.spf_holes);
+  run_red(c, P.spf_red);
+  for (auto& b : P.chain) run_prod(c, b);
+  run_hole(c, P.dots);
+  run_red(c, P.dot_red);
+}
+
+void check_status(Ctx& c) {
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  if (st != 0) {
+    CK(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.st));
+    if (st & DEVST_EIG_NOCONV) throw StatusError(MCTDH_EEIG, "Jacobi eigensolver did not converge");
+    if (st & DEVST_CHOL_FAIL) throw StatusError(MCTDH_EEIG, "SPF overlap matrix is not positive definite");
+    throw StatusError(MCTDH_ENONFINITE, "device status " + std::to_string(st));
+  }
+}
+
+void read_ovl(Ctx& c, OvlPlan& P, cplx out[3]) {
+  CK(cudaMemcpyAsync(out, P.d_result, sizeof(cplx) * 3, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+}
+
+// Cash-Karp and Dormand-Prince tableaux (integrator.f90:107-121, :171-185)
+const double CK_A[6] = {0.0, 0.2, 0.3, 0.6, 1.0, 0.875};
+const double CK_B[6][5] = {{0},
+                           {0.2},
+                           {0.075, 0.225},
+                           {0.3, -0.9, 1.2},
+                           {-11.0 / 54.0, 2.5, -70.0 / 27.0, 35.0 / 27.0},
+                           {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0}};
+const double CK_C[6] = {37.0 / 378.0, 0.0, 250.0 / 621.0, 125.0 / 594.0, 0.0, 512.0 / 1771.0};
+const double CK_D[6] = {2825.0 / 27648.0, 0.0, 18575.0 / 48384.0, 13525.0 / 55296.0, 277.0 / 14336.0, 0.25};
+const double DP_B[6][5] = {{0},
+                           {0.2},
+                           {0.075, 0.225},
+                           {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0},
+                           {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0},
+                           {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0}};
+const double DP_C[6] = {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0};
+const double DP_D[7] = {5179.0 / 57600.0, 0.0, 7571.0 / 16695.0, 393.0 / 640.0, -92097.0 / 339200.0,
+                        187.0 / 2100.0, 0.025};
+const double RK_SAFETY = 0.9, RK_PGROW = -0.2, RK_PSHRNK = -0.25, RK_MINSCAL = 0.1, RK_MAXSCAL = 5.0;
+
+void stage(Ctx& c, cplx* out, const cplx* base, const double* coef, int nk, int kofs, double dt) {
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  int n = 0;
+  for (int j = 0; j < nk; ++j) {
+    if (coef[j] == 0.0) continue;
+    a.k[n] = c.d_k[kofs + j];
+    a.c[n] = coef[j];
+    ++n;
+  }
+  a.nk = n;
+  launch_stage(out, base, a, dt, c.ntot, c.st);
+  c.count();
+}
+
+// One rkck/rkdp attempt from d_y with k1 in d_k[0]; leaves the 5th-order state in
+// d_tmp, the embedded state in d_err; returns errmax / eps (DeltaPsi).
+double rk_attempt(Ctx& c, double t, double dt, int method) {
+  const bool dp = (method == 2);
+  for (int st = 1; st < 6; ++st) {
+    stage(c, c.d_in, c.d_y, dp ? DP_B[st] : CK_B[st], st, 0, dt);
+    eom(c, c.d_k[st]);
+  }
+  stage(c, c.d_tmp, c.d_y, dp ? DP_C : CK_C, 6, 0, dt);
+  if (dp) {
+    CK(cudaMemcpyAsync(c.d_in, c.d_tmp, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+    eom(c, c.d_k[6]);
+    stage(c, c.d_err, c.d_y, DP_D, 7, 0, dt);
+  } else {
+    stage(c, c.d_err, c.d_y, CK_D, 6, 0, dt);
+  }
+  run_ovl(c, c.dpsi_plan);
+  cplx o[3];
+  read_ovl(c, c.dpsi_plan, o);
+  check_status(c);
+  double o11 = o[0].x, o22 = o[1].x, o12 = o[2].x;
+  double delta = sqrt(fabs(2.0 * (1.0 - o12 / sqrt(o11 * o22))));
+  if (!std::isfinite(delta)) throw StatusError(MCTDH_ENONFINITE, "non-finite RK error estimate");
+  return delta / c.eps_int;
+}
+
+// rkqs (integrator.f90:36-91) on d_y; d_k[0] holds dA/dpsi at t on entry.
+void rkqs(Ctx& c, double t, double htry, double* hdid, double* hnext, int method, long long* attempts) {
+  double dt = htry, errmax;
+  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
+  while (true) {
+    ++*attempts;
+    errmax = rk_attempt(c, t, dt, method);
+    if (errmax < 1.0 || dt <= c.min_stepsize) break;
+    dt = std::max(RK_MINSCAL * dt, RK_SAFETY * dt * pow(errmax, RK_PSHRNK));
+    dt = std::max(dt, c.min_stepsize);
+  }
+  double hn = (errmax > errcon) ? RK_SAFETY * dt * pow(errmax, RK_PGROW) : dt * RK_MAXSCAL;
+  hn = std::max(hn, c.min_stepsize);
+  hn = std::min(hn, c.writetime);
+  *hdid = dt;
+  *hnext = hn;
+  CK(cudaMemcpyAsync(c.d_y, c.d_tmp, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+  if (method == 2)
+    CK(cudaMemcpyAsync(c.d_k[0], c.d_k[6], sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+}
+
+// ---------------------------------------------------------------------------
+// CMF2 (cmf2_base.f90:47-206) for DVR models
+// ---------------------------------------------------------------------------
+void hb(Ctx& c, const cplx* B, cplx* out) {
+  if (B != c.d_hbin) CK(cudaMemcpyAsync(c.d_hbin, B, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
+  for (size_t i = 1; i < c.hb_chains.size(); ++i) run_prod(c, c.hb_chains[i]);
+  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st);
+  c.count();
+  c.hb_count++;
+}
+
+// <a|b> over the coefficient vector (FP64, deterministic)
+cplx dot_now(Ctx& c, const cplx* a, const cplx* b, long long n) {
+  // plans are cached per context, keyed by the pointer pair
+  auto key = std::make_pair((const void*)a, (const void*)b);
+  DotPlan* P = c.dots.count(key) ? c.dots[key] : nullptr;
+  if (!P) {
+    P = new DotPlan();
+    P->res = c.ar.calloc_c(1);
+    int h = P->hb.add(c.ar, a, b, n, 1, 1, 1);
+    P->hb.finalize(c.ar);
+    int tg = P->red.add_target(P->res, 1, 1, 1, 0);
+    P->red.add_term(tg, P->hb.h[h], mkc(1, 0));
+    P->red.finalize(c.ar);
+    c.dots[key] = P;
+  }
+  run_hole(c, P->hb);
+  run_red(c, P->red);
+  cplx r;
+  CK(cudaMemcpyAsync(&r, P->res, sizeof(cplx), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  return r;
+}
+
+const double EPS_B = 1e-8;  // cmf2_integration.f90:13
+const int NKRYLOV_MAX = 20; // cmf2_integration.f90:11
+
+// Lanczos (cmf2_integration.f90:30-103) from B0 (device, naconftot) into BT.
+void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
+  const long long n = c.naconftot;
+  cplx* K = c.d_krylov;
+  if (build) {
+    cplx nrm2 = dot_now(c, B0, B0, n);
+    double nrm = sqrt(nrm2.x);
+    launch_copy_scale(K, B0, mkc(1.0 / nrm, 0), n, c.st);
+    c.count();
+    double alpha[NKRYLOV_MAX] = {0}, beta[NKRYLOV_MAX] = {0};
+    hb(c, K, K + n);
+    alpha[0] = dot_now(c, K, K + n, n).x;
+    launch_axpy(K + n, K, mkc(-alpha[0], 0), n, c.st);
+    c.count();
+    beta[0] = sqrt(dot_now(c, K + n, K + n, n).x);
+    launch_copy_scale(K + n, K + n, mkc(1.0 / beta[0], 0), n, c.st);
+    c.count();
+    double error = beta[0] * fabs(dt);
+    int j = 2;
+    while (true) {
+      if (j == NKRYLOV_MAX) throw StatusError(MCTDH_EKRYLOV, "Maximum number of Krylov vectors reached");
+      cplx* Kj = K + (long long)(j - 1) * n;
+      cplx* Kn = K + (long long)j * n;
+      cplx* Kp = K + (long long)(j - 2) * n;
+      hb(c, Kj, Kn);
+      alpha[j - 1] = dot_now(c, Kj, Kn, n).x;
+      launch_axpy(Kn, Kp, mkc(-beta[j - 2], 0), n, c.st);
+      launch_axpy(Kn, Kj, mkc(-alpha[j - 1], 0), n, c.st);
+      c.count(2);
+      beta[j - 1] = sqrt(dot_now(c, Kn, Kn, n).x);
+      launch_copy_scale(Kn, Kn, mkc(1.0 / beta[j - 1], 0), n, c.st);
+      c.count();
+      error = error * beta[j - 1] / (double)j * fabs(dt);
+      if (error < EPS_B) break;
+      ++j;
+    }
+    const int nk = j;
+    CK(cudaMemcpyAsync(c.d_lan, alpha, sizeof(double) * NKRYLOV_MAX, cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.d_lan + NKRYLOV_MAX, beta, sizeof(double) * NKRYLOV_MAX, cudaMemcpyHostToDevice, c.st));
+    launch_jacobi_tridiag(c.d_lan, c.d_lan + NKRYLOV_MAX, nk, c.d_lan + 2 * NKRYLOV_MAX,
+                          c.d_lan + 3 * NKRYLOV_MAX, c.d_status, c.st);
+    c.count();
+    c.lan_evals.assign(nk, 0.0);
+    c.lan_evecs.assign(nk * nk, 0.0);
+    CK(cudaMemcpyAsync(c.lan_evals.data(), c.d_lan + 2 * NKRYLOV_MAX, sizeof(double) * nk, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaMemcpyAsync(c.lan_evecs.data(), c.d_lan + 3 * NKRYLOV_MAX, sizeof(double) * nk * nk,
+                       cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    check_status(c);
+    c.lan_nk = nk;
+  }
+  const int nk = c.lan_nk;
+  // BT = sum_j BK_j * (sum_r U_jr U_1r exp(f alpha_r dt))
+  std::vector<cplx> coef(nk, mkc(0, 0));
+  for (int r = 0; r < nk; ++r) {
+    double u1 = c.lan_evecs[0 + nk * r];
+    cplx e = mkc(c.der.x * c.lan_evals[r] * dt, c.der.y * c.lan_evals[r] * dt);
+    double mag = exp(e.x);
+    cplx ex = mkc(mag * cos(e.y), mag * sin(e.y));
+    for (int jj = 0; jj < nk; ++jj) {
+      double ujr = c.lan_evecs[jj + nk * r];
+      coef[jj] = cadd(coef[jj], cscale(ex, ujr * u1));
+    }
+  }
+  CK(cudaMemcpyAsync(c.d_coef, coef.data(), sizeof(cplx) * nk, cudaMemcpyHostToDevice, c.st));
+  launch_gemv_cols(BT, K, n, c.d_coef, nk, n, c.st);
+  c.count();
+  double nrm = sqrt(dot_now(c, BT, BT, n).x);
+  launch_copy_scale(BT, BT, mkc(1.0 / nrm, 0), n, c.st);
+  c.count();
+}
+
+// operators and mean fields on the state y (Calc_rho1mode, Calc_h1mode,
+// Calc_MeanField, Calc_rhom1MF): one EOM into d_out (the derivative is unused).
+void operators_and_mf(Ctx& c, const cplx* y) { eom_from(c, y, c.d_out); }
+
+// SPF derivative of one DVR mode with frozen mean fields (Calc_Der_SPF,
+// cmf2_derivatives.f90:84-173) from the SPFs in d_in into out.
+struct ModeSpfPlan {
+  std::vector<H1Desc> h1;
+  H1Desc* h1_d = nullptr;
+  std::vector<SpfDesc> spf;
+  SpfDesc* spf_d = nullptr;
+  std::vector<long long> blocks;  // (offset, length) pairs in the psi part
+  HoleBatch err_holes;            // Calc_Err_SPF: (dphi)^H dphi per state block
+  RedBatch err_red;
+  std::vector<cplx*> err_mat;     // per state block
+};
+
+void plan_mode_spf(Ctx& c, std::vector<ModeSpfPlan>& plans) {
+  const int f = c.nmodes;
+  plans.assign(f, ModeSpfPlan());
+  for (int m : c.modes_dvr) {
+    ModeSpfPlan& P = plans[m];
+    for (int idx : c.h1_of_mode[m]) {
+      H1Desc hd = c.h1_h[idx];
+      hd.h = nullptr;   // mean fields and h1mode stay frozen; only ophi is refreshed
+      P.h1.push_back(hd);
+    }
+    P.h1_d = upload_vec(c.ar, P.h1);
+    for (auto& sd : c.spf_h) {
+      // the spf descriptors of this mode: phi pointer lies in this mode's blocks
+      for (int s = 0; s < c.nstates; ++s) {
+        if (!c.multiset[m] && s > 0) break;
+        if (sd.out_offset == c.naconftot + c.ipsi[m + f * s]) P.spf.push_back(sd);
+      }
+    }
+    P.spf_d = upload_vec(c.ar, P.spf);
+    for (int s = 0; s < c.nstates; ++s) {
+      if (!c.multiset[m] && s > 0) break;
+      P.blocks.push_back(c.naconftot + c.ipsi[m + f * s]);
+      P.blocks.push_back((long long)c.gmode[m] * c.m_of(m, s));
+    }
+  }
+}
+
+struct CmfState {
+  std::vector<ModeSpfPlan> mode_plans;
+  bool planned = false;
+  cplx *B0, *BHalf, *B02, *psiHalf, *psiHalf2, *AHalf;  // full-length vectors (ntot)
+  cplx* ytmp;
+};
+std::map<const Ctx*, CmfState*> g_cmf;
+
+void stage_blocks(Ctx& c, cplx* out, const cplx* base, const double* coef, int nk, double dt,
+                  const std::vector<long long>& blocks) {
+  for (size_t b = 0; b + 1 < blocks.size(); b += 2) {
+    StageArgs a;
+    memset(&a, 0, sizeof(a));
+    int n = 0;
+    for (int j = 0; j < nk; ++j) {
+      if (coef[j] == 0.0) continue;
+      a.k[n] = c.d_k[j] + blocks[b];
+      a.c[n] = coef[j];
+      ++n;
+    }
+    a.nk = n;
+    launch_stage(out + blocks[b], base + blocks[b], a, dt, blocks[b + 1], c.st);
+    c.count();
+  }
+}
+
+void spf_eval(Ctx& c, ModeSpfPlan& P, cplx* out) {
+  launch_h1(P.h1_d, (int)P.h1.size(), c.h1_smem, c.st);
+  launch_spf(P.spf_d, (int)P.spf.size(), c.spfop_d, out, c.der, c.spf_smem, c.d_status, c.st);
+  c.count(2);
+}
+
+double err_spf(Ctx& c, CmfState& S, int m, const cplx* p1, const cplx* p2);
+
+// rk_SPF_ck (cmf2_integration.f90:105-253), DVR branch; psi part of y updated in place.
+void rk_spf_ck(Ctx& c, CmfState& S, int m, cplx* y, double htry, double* hdid, double* hnext) {
+  ModeSpfPlan& P = S.mode_plans[m];
+  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
+  double dt = htry, error;
+  while (true) {
+    // d_in carries the SPFs on which the operators act
+    for (size_t b = 0; b + 1 < P.blocks.size(); b += 2)
+      CK(cudaMemcpyAsync(c.d_in + P.blocks[b], y + P.blocks[b], sizeof(cplx) * P.blocks[b + 1],
+                         cudaMemcpyDeviceToDevice, c.st));
+    spf_eval(c, P, c.d_k[0]);
+    for (int st = 1; st < 6; ++st) {
+      stage_blocks(c, c.d_in, y, CK_B[st], st, dt, P.blocks);
+      spf_eval(c, P, c.d_k[st]);
+    }
+    stage_blocks(c, c.d_tmp, y, CK_C, 6, dt, P.blocks);
+    stage_blocks(c, c.d_err, y, CK_D, 6, dt, P.blocks);
+    error = err_spf(c, S, m, c.d_tmp, c.d_err) / c.eps_psi;
+    if (error < 1.0) break;
+    dt = std::max(RK_MINSCAL * dt, RK_SAFETY * dt * pow(error, RK_PSHRNK));
+  }
+  *hnext = (error > errcon) ? RK_SAFETY * dt * pow(error, RK_PGROW) : dt * RK_MAXSCAL;
+  *hdid = dt;
+  for (size_t b = 0; b + 1 < P.blocks.size(); b += 2)
+    CK(cudaMemcpyAsync(y + P.blocks[b], c.d_tmp + P.blocks[b], sizeof(cplx) * P.blocks[b + 1],
+                       cudaMemcpyDeviceToDevice, c.st));
+}
+
+void propagate_spf(Ctx& c, CmfState& S, double dt, int m, cplx* y) {
+  if (c.int_type_psi != 1) throw StatusError(MCTDH_EUNSUPPORTED, "only Cash-Karp SPF integration is supported");
+  double done = 0.0, step = dt, sdone, snext;
+  while (true) {
+    rk_spf_ck(c, S, m, y, step, &sdone, &snext);
+    done += sdone;
+    if (done >= dt) break;
+    snext = std::max(snext, c.min_stepsize * 2);
+    step = (dt - done) / ((double)(long long)((dt - done) / snext) + 1);
+    step = std::min(step, dt - done);
+  }
+}
+
+// Calc_Err_SPF, DVR branch (cmf2_derivatives.f90:239-283): error^2 = Tr(rho * dS),
+// dS = (phi1 - phi2)^H (phi1 - phi2).  Computed as a hole contraction of the
+// difference vector (d_err <- p1 - p2 over the mode's blocks).
+double err_spf(Ctx& c, CmfState& S, int m, const cplx* p1, const cplx* p2) {
+  ModeSpfPlan& P = S.mode_plans[m];
+  for (size_t b = 0; b + 1 < P.blocks.size(); b += 2) {
+    StageArgs a;
+    memset(&a, 0, sizeof(a));
+    a.k[0] = p2 + P.blocks[b];
+    a.c[0] = -1.0;
+    a.nk = 1;
+    launch_stage(S.ytmp + P.blocks[b], p1 + P.blocks[b], a, 1.0, P.blocks[b + 1], c.st);
+    c.count();
+  }
+  run_hole(c, P.err_holes);
+  run_red(c, P.err_red);
+  double err = 0.0;
+  int si = 0;
+  for (int s = 0; s < c.nstates; ++s) {
+    if (!c.multiset[m] && s > 0) break;
+    const int n = c.m_of(m, s);
+    std::vector<cplx> dS(n * n), rho(n * n);
+    CK(cudaMemcpyAsync(dS.data(), P.err_mat[si], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c.st));
+    const cplx* rp = c.multiset[m] ? c.rho[m][s] : c.rho_ave[m];
+    CK(cudaMemcpyAsync(rho.data(), rp, sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int j2 = 0; j2 < n; ++j2) {
+      for (int j1 = 0; j1 < j2; ++j1) {
+        cplx r = rho[j1 + n * j2], o = dS[j1 + n * j2];
+        err += 2.0 * (r.x * o.x + r.y * o.y);   // Re(rho * conj(ovl))
+      }
+      cplx r = rho[j2 + n * j2], o = dS[j2 + n * j2];
+      err += r.x * o.x - r.y * o.y;               // Re(rho * ovl)
+    }
+    ++si;
+  }
+  return sqrt(fabs(err));
+}
+
+void plan_cmf(Ctx& c, CmfState& S) {
+  const int f = c.nmodes;
+  plan_mode_spf(c, S.mode_plans);
+  S.B0 = c.ar.calloc_c(c.ntot);
+  S.BHalf = c.ar.calloc_c(c.ntot);
+  S.B02 = c.ar.calloc_c(c.ntot);
+  S.psiHalf = c.ar.calloc_c(c.ntot);
+  S.psiHalf2 = c.ar.calloc_c(c.ntot);
+  S.AHalf = c.ar.calloc_c(c.ntot);
+  S.ytmp = c.ar.calloc_c(c.ntot);
+  // Calc_Err_SPF holes: one per (mode, state block) on the difference vector ytmp
+  for (int m : c.modes_dvr) {
+    ModeSpfPlan& P = S.mode_plans[m];
+    std::vector<HoleRef> hrefs;
+    for (int s = 0; s < c.nstates; ++s) {
+      if (!c.multiset[m] && s > 0) break;
+      const int n = c.m_of(m, s);
+      cplx* mat = c.ar.calloc_c((long long)n * n);
+      P.err_mat.push_back(mat);
+      cplx* p = S.ytmp + c.naconftot + c.ipsi[m + f * s];
+      int h = P.err_holes.add(c.ar, p, p, c.gmode[m], 1, n, n);
+      hrefs.push_back(HoleRef{h, P.err_red.add_target(mat, n, n, n, 1), mkc(1, 0)});
+    }
+    P.err_holes.finalize(c.ar);
+    for (auto& hr : hrefs) P.err_red.add_term(hr.target, P.err_holes.h[hr.hole], hr.alpha);
+    P.err_red.finalize(c.ar);
+  }
+  S.planned = true;
+}
+
+void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
+  CK(cudaMemcpyAsync(dst, src, sizeof(cplx) * n, cudaMemcpyDeviceToDevice, c.st));
+}
+
+// h1mode only (no mean fields) on the SPFs of y: used before the back-propagation.
+void h1_only(Ctx& c, const cplx* y) {
+  copy_dev(c, c.d_in + c.naconftot, y + c.naconftot, c.dimpsi);
+  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
+  c.count();
+}
+
+CmfState& cmf_state(Ctx& c) {
+  CmfState*& Sp = g_cmf[&c];
+  if (!Sp) {
+    Sp = new CmfState();
+    plan_cmf(c, *Sp);
+  }
+  return *Sp;
+}
+
+// One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
+// max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
+double cmf2_attempt(Ctx& c, double t, double hdid) {
+  CmfState& S = cmf_state(c);
+  const long long nA = c.naconftot;
+  operators_and_mf(c, c.d_y);                       // cmf2_base.f90:78-87
+  copy_dev(c, S.B0, c.d_y, nA);                     // A_to_B (DVR only)
+  lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);      // :97
+  copy_dev(c, S.psiHalf, c.d_y, c.ntot);
+  for (int m : c.modes_dvr) propagate_spf(c, S, 0.5 * hdid, m, S.psiHalf);   // :109-115
+  copy_dev(c, S.AHalf, S.BHalf, nA);                // B_to_A  :120
+  copy_dev(c, S.AHalf + nA, S.psiHalf + nA, c.dimpsi);
+  operators_and_mf(c, S.AHalf);                     // :122-130
+  copy_dev(c, S.psiHalf2, c.d_y, c.ntot);
+  for (int m : c.modes_dvr) propagate_spf(c, S, 0.5 * hdid, m, S.psiHalf2);  // :132-141
+  // err_psi = DeltaPsi(AHalf, psiHalf, AHalf, psiHalf2)  (:143)
+  copy_dev(c, c.d_tmp, S.AHalf, c.ntot);
+  copy_dev(c, c.d_err, S.AHalf, nA);
+  copy_dev(c, c.d_err + nA, S.psiHalf2 + nA, c.dimpsi);
+  run_ovl(c, c.dpsi_plan);
+  cplx o[3];
+  read_ovl(c, c.dpsi_plan, o);
+  double err_psi = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x))));
+  for (int m : c.modes_dvr) propagate_spf(c, S, 0.5 * hdid, m, S.psiHalf2);  // :148-154
+  h1_only(c, S.psiHalf2);                           // :158-165
+  lanczos(c, S.BHalf, S.B02, -0.5 * hdid, true);    // :169
+  launch_axpy(S.B02, S.B0, mkc(-1, 0), nA, c.st);
+  c.count();
+  double err_A = sqrt(dot_now(c, S.B02, S.B02, nA).x) * 0.5;
+  check_status(c);
+  double error = std::max(err_A, err_psi) / c.eps_int;
+  if (!std::isfinite(error)) throw StatusError(MCTDH_ENONFINITE, "non-finite CMF2 error estimate");
+  return error;
+}
+
+// Accept: finish the coefficients with the reused Krylov space (:189) and update.
+void cmf2_accept(Ctx& c, double hdid) {
+  CmfState& S = cmf_state(c);
+  lanczos(c, S.BHalf, c.d_y, 0.5 * hdid, false);
+  copy_dev(c, c.d_y + c.naconftot, S.psiHalf2 + c.naconftot, c.dimpsi);
+}
+
+void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, long long* tries) {
+  double hdid = htry;
+  while (true) {
+    ++*tries;
+    double error = cmf2_attempt(c, t, hdid);
+    if (error > 1.0) {
+      hdid = hdid / sqrt(error) * 0.95;
+      continue;
+    }
+    cmf2_accept(c, hdid);
+    double hn = (error > 0.0) ? std::min(hdid / sqrt(error), hdid * 1.5) : hdid * 1.5;
+    hn = std::min(hn, c.writetime);
+    *hdid_out = hdid;
+    *hnext_out = hn;
+    return;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Context creation
+// ---------------------------------------------------------------------------
+Ctx* create(const mctdh_setup_t* s) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    throw StatusError(MCTDH_ECUDA, "no CUDA device available (this core has no CPU fallback)");
+  Ctx* c = new Ctx();
+  try {
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    load_setup(*c, s);
+    c->d_status = (int*)c->ar.alloc(64);
+    CK(cudaMemset(c->d_status, 0, 64));
+    c->d_y = c->ar.calloc_c(c->ntot);
+    c->d_y0 = c->ar.calloc_c(c->ntot);
+    c->d_in = c->ar.calloc_c(c->ntot);
+    c->d_out = c->ar.calloc_c(c->ntot);
+    for (int i = 0; i < 7; ++i) c->d_k[i] = c->ar.calloc_c(c->ntot);
+    c->d_tmp = c->ar.calloc_c(c->ntot);
+    c->d_err = c->ar.calloc_c(c->ntot);
+    c->d_hbin = c->ar.calloc_c(c->naconftot);
+    c->d_hb = c->ar.calloc_c(c->naconftot);
+    c->d_scal = (double*)c->ar.alloc(4096);
+    c->d_krylov = c->ar.calloc_c(c->naconftot * (NKRYLOV_MAX + 1));
+    c->d_lan = (double*)c->ar.alloc(sizeof(double) * (3 * NKRYLOV_MAX + NKRYLOV_MAX * NKRYLOV_MAX));
+    c->d_coef = c->ar.calloc_c(NKRYLOV_MAX);
+    plan_eom(*c);
+    plan_hb(*c);
+    plan_ovl(*c, c->dpsi_plan, c->d_tmp, c->d_err);
+    plan_ovl(*c, c->auto_plan, c->d_y0, c->d_y);
+    plan_ovl(*c, c->io_plan, c->d_in, c->d_out);
+    CK(cudaDeviceSynchronize());
+  } catch (...) {
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    throw;
+  }
+  return c;
+}
+
+template <typename F>
+int64_t guarded(Ctx* c, F&& fn) {
+  try {
+    fn();
+    return MCTDH_OK;
+  } catch (const StatusError& e) {
+    if (c) c->last_error = e.what();
+    return e.code;
+  } catch (const CudaError& e) {
+    if (c) c->last_error = e.what();
+    return MCTDH_ECUDA;
+  } catch (const std::exception& e) {
+    if (c) c->last_error = e.what();
+    return MCTDH_EARG;
+  }
+}
+
+void upload(Ctx& c, cplx* dst, const double* A, const double* psi) {
+  CK(cudaMemcpyAsync(dst, A, sizeof(cplx) * c.naconftot, cudaMemcpyHostToDevice, c.st));
+  if (c.dimpsi > 0)
+    CK(cudaMemcpyAsync(dst + c.naconftot, psi, sizeof(cplx) * c.dimpsi, cudaMemcpyHostToDevice, c.st));
+}
+void download(Ctx& c, const cplx* src, double* A, double* psi) {
+  CK(cudaMemcpyAsync(A, src, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToHost, c.st));
+  if (c.dimpsi > 0)
+    CK(cudaMemcpyAsync(psi, src + c.naconftot, sizeof(cplx) * c.dimpsi, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+}
+
+}  // namespace
+
+struct mctdh_ctx {
+  Ctx* c;
+};
+
+extern "C" {
+
+int64_t mctdh_create(const mctdh_setup_t* setup, mctdh_ctx_t** out) {
+  if (!setup || !out) return MCTDH_EARG;
+  *out = nullptr;
+  try {
+    Ctx* c = create(setup);
+    *out = new mctdh_ctx{c};
+    g_create_error.clear();
+    return MCTDH_OK;
+  } catch (const StatusError& e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_error = e.what();
+    return MCTDH_ECUDA;
+  }
+}
+
+int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  cudaStreamSynchronize(c->st);
+  auto it = g_cmf.find(c);
+  if (it != g_cmf.end()) {
+    delete it->second;
+    g_cmf.erase(it);
+  }
+  for (auto& kv : c->dots) delete kv.second;
+  cudaStreamDestroy(c->st);
+  delete c;
+  delete ctx;
+  return MCTDH_OK;
+}
+
+const char* mctdh_last_error(mctdh_ctx_t* ctx) {
+  if (!ctx) return g_create_error.c_str();
+  return ctx->c->last_error.c_str();
+}
+
+int64_t mctdh_launch_count(mctdh_ctx_t* ctx) { return ctx ? ctx->c->launches : 0; }
+
+int64_t mctdh_calc_derivs(mctdh_ctx_t* ctx, const double* A, const double* psi, double* dA, double* dpsi,
+                          double t) {
+  if (!ctx || !A || !psi || !dA || !dpsi) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    (void)t;
+    upload(*c, c->d_in, A, psi);
+    eom(*c, c->d_out);
+    check_status(*c);
+    download(*c, c->d_out, dA, dpsi);
+  });
+}
+
+int64_t mctdh_set_state(mctdh_ctx_t* ctx, const double* A, const double* psi, int64_t as_start) {
+  if (!ctx || !A || !psi) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_y, A, psi);
+    c->fsal_valid = false;
+    if (as_start) copy_dev(*c, c->d_y0, c->d_y, c->ntot);
+    CK(cudaStreamSynchronize(c->st));
+  });
+}
+
+int64_t mctdh_get_state(mctdh_ctx_t* ctx, double* A, double* psi) {
+  if (!ctx || !A || !psi) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] { download(*c, c->d_y, A, psi); });
+}
+
+int64_t mctdh_rkqs(mctdh_ctx_t* ctx, double* A, double* psi, double* dA, double* dpsi, double t, double htry,
+                   double* hdid, double* hnext, int64_t method) {
+  if (!ctx || !A || !psi || !dA || !dpsi || !hdid || !hnext) return MCTDH_EARG;
+  if (method != 1 && method != 2) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_y, A, psi);
+    upload(*c, c->d_k[0], dA, dpsi);
+    long long att = 0;
+    rkqs(*c, t, htry, hdid, hnext, (int)method, &att);
+    download(*c, c->d_y, A, psi);
+    if (method == 2) download(*c, c->d_k[0], dA, dpsi);
+  });
+}
+
+int64_t mctdh_rk_attempt(mctdh_ctx_t* ctx, double* A, double* psi, double* dA, double* dpsi, double t,
+                         double dt, int64_t method, double* errmax) {
+  if (!ctx || !A || !psi || !dA || !dpsi || !errmax) return MCTDH_EARG;
+  if (method != 1 && method != 2) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_y, A, psi);
+    upload(*c, c->d_k[0], dA, dpsi);
+    *errmax = rk_attempt(*c, t, dt, (int)method);
+    download(*c, c->d_tmp, A, psi);
+    if (method == 2) download(*c, c->d_k[6], dA, dpsi);
+  });
+}
+
+int64_t mctdh_cmf2_attempt(mctdh_ctx_t* ctx, double* A, double* psi, double t, double h, double* error) {
+  if (!ctx || !A || !psi || !error) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_y, A, psi);
+    *error = cmf2_attempt(*c, t, h);
+    cmf2_accept(*c, h);
+    download(*c, c->d_y, A, psi);
+  });
+}
+
+int64_t mctdh_cmf2(mctdh_ctx_t* ctx, double* A, double* psi, double t, double htry, double* hdid,
+                   double* hnext) {
+  if (!ctx || !A || !psi || !hdid || !hnext) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_y, A, psi);
+    long long tries = 0;
+    cmf2(*c, t, htry, hdid, hnext, &tries);
+    download(*c, c->d_y, A, psi);
+  });
+}
+
+int64_t mctdh_propagate(mctdh_ctx_t* ctx, int64_t int_type, double tnext, double* t, double* step,
+                        int64_t* nsteps, int64_t* nattempts, int64_t* neom) {
+  if (!ctx || !t || !step) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    long long steps = 0, att = 0;
+    long long eom0 = c->eom_count;
+    double time = *t, stepsize = *step;
+    while (true) {
+      double sdone, snext;
+      if (int_type == 10) {
+        cmf2(*c, time, stepsize, &sdone, &snext, &att);
+      } else if (int_type == 1 || int_type == 2) {
+        if (int_type == 1 || !c->fsal_valid) {
+          // propagator.f90:116 (Cash-Karp).  Dormand-Prince reuses the last stage
+          // (FSAL); its very first derivative is evaluated here, where the reference
+          // reads a never-computed dAVector (propagator.f90:98, integrator.f90:187).
+          eom_from(*c, c->d_y, c->d_k[0]);
+        }
+        rkqs(*c, time, stepsize, &sdone, &snext, (int)int_type, &att);
+        c->fsal_valid = (int_type == 2);
+      } else {
+        throw StatusError(MCTDH_EUNSUPPORTED, "integrator type not supported");
+      }
+      ++steps;
+      time += sdone;
+      if (time >= tnext - c->min_stepsize) break;
+      long long q = (long long)((tnext - time) / snext);
+      stepsize = (q == 0) ? (tnext - time) : (tnext - time) / (double)(q + 1);
+    }
+    CK(cudaStreamSynchronize(c->st));
+    *t = time;
+    *step = stepsize;
+    if (nsteps) *nsteps = steps;
+    if (nattempts) *nattempts = att;
+    if (neom) *neom = c->eom_count - eom0;
+  });
+}
+
+int64_t mctdh_observables(mctdh_ctx_t* ctx, double t, double* energy, double* pop, double* norm,
+                          double* auto_re, double* auto_im) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    (void)t;
+    eom_from(*c, c->d_y, c->d_out);
+    cplx e = dot_now(*c, c->d_y, c->d_out, c->naconftot);
+    // energy = Re <A| H A> = Re( <A|dA> / der_factor )
+    double dr = c->der.x, di = c->der.y, den = dr * dr + di * di;
+    double en = (e.x * dr + e.y * di) / den;
+    std::vector<double> p(c->nstates);
+    double tot = 0.0;
+    const int m0 = 0;
+    for (int s = 0; s < c->nstates; ++s) {
+      int n = c->m_of(m0, s);
+      std::vector<cplx> r(n * n);
+      CK(cudaMemcpyAsync(r.data(), c->rho[m0][s], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      double tr = 0.0;
+      for (int j = 0; j < n; ++j) tr += r[j + n * j].x;
+      p[s] = tr;
+      tot += tr;
+    }
+    run_ovl(*c, c->auto_plan);
+    cplx o[3];
+    read_ovl(*c, c->auto_plan, o);
+    check_status(*c);
+    if (energy) *energy = en / tot;
+    if (pop) for (int s = 0; s < c->nstates; ++s) pop[s] = p[s];
+    if (norm) *norm = tot;
+    if (auto_re) *auto_re = o[2].x;
+    if (auto_im) *auto_im = o[2].y;
+  });
+}
+
+int64_t mctdh_norm_wf(mctdh_ctx_t* ctx, const double* A, const double* psi, double* norm) {
+  if (!ctx || !A || !psi || !norm) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_in, A, psi);
+    upload(*c, c->d_out, A, psi);
+    run_ovl(*c, c->io_plan);
+    cplx o[3];
+    read_ovl(*c, c->io_plan, o);
+    *norm = o[0].x;
+  });
+}
+
+int64_t mctdh_wf_ovl(mctdh_ctx_t* ctx, const double* A1, const double* psi1, const double* A2,
+                     const double* psi2, double* re, double* im) {
+  if (!ctx || !A1 || !psi1 || !A2 || !psi2 || !re || !im) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    upload(*c, c->d_in, A1, psi1);
+    upload(*c, c->d_out, A2, psi2);
+    run_ovl(*c, c->io_plan);
+    cplx o[3];
+    read_ovl(*c, c->io_plan, o);
+    *re = o[2].x;
+    *im = o[2].y;
+  });
+}
+
+}  // extern "C"

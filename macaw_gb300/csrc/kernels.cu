@@ -1,0 +1,584 @@
+// FP64 kernels of the G-MCTDH equation-of-motion path for sm_103a.
+//
+// On GB300 FP64 runs on the CUDA cores at a small fraction of the FP32 rate, so
+// these kernels are written to spend FP64 FMAs only on the algebra the EOM needs:
+// each fibre of a tensor is read once into registers (mode products), fibre tiles
+// are staged in shared memory for the single-hole contractions, and reductions
+// are two-stage with a fixed summation order so reruns are bitwise identical.
+#include "kernels.cuh"
+#include <stdio.h>
+
+// ---------------------------------------------------------------------------
+// descriptor lookup: descriptors are sorted by block_start
+// ---------------------------------------------------------------------------
+template <typename D>
+__device__ __forceinline__ int find_desc(const D* descs, int ndesc) {
+  int lo = 0, hi = ndesc - 1;
+  const long long b = blockIdx.x;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (descs[mid].block_start <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Batched mode product (Mult_HeM_MatV / Mult_GM_MatV, gmctdh_objects.f90:1407-1468)
+// One thread owns one fibre (l, :, r): it reads the nin inputs once into
+// registers and writes the nout outputs.
+// ---------------------------------------------------------------------------
+template <int MAXN>
+__global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
+  __shared__ int s_di;
+  __shared__ cplx Ms[MAXN * MAXN];
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const ProdDesc& d = descs[s_di];
+  const int nin = d.nin, nout = d.nout;
+  for (int e = threadIdx.x; e < nin * nout; e += blockDim.x) {
+    int jo = e % nout, ji = e / nout;
+    cplx v = d.conjT ? cconj(d.M[ji + (long long)d.ldm * jo]) : d.M[jo + (long long)d.ldm * ji];
+    Ms[jo + MAXN * ji] = v;
+  }
+  __syncthreads();
+  const long long p = (long long)(blockIdx.x - d.block_start) * blockDim.x + threadIdx.x;
+  const long long L = d.L;
+  if (p >= L * d.R) return;
+  const long long l = p % L, r = p / L;
+  const cplx* __restrict__ x0 = d.X + l + L * (long long)nin * r;
+  cplx x[MAXN];
+#pragma unroll
+  for (int j = 0; j < MAXN; ++j) x[j] = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
+  cplx* y0 = d.Y + l + L * (long long)nout * r;
+  const cplx alpha = d.alpha;
+  for (int jo = 0; jo < nout; ++jo) {
+    cplx acc = mkc(0.0, 0.0);
+#pragma unroll
+    for (int j = 0; j < MAXN; ++j)
+      if (j < nin) cfma(acc, Ms[jo + MAXN * j], x[j]);
+    cplx v = cmul(alpha, acc);
+    if (d.accumulate) v = cadd(v, y0[L * jo]);
+    y0[L * jo] = v;
+  }
+}
+
+void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st) {
+  if (ndesc <= 0 || nblocks <= 0) return;
+  if (maxn <= 12)
+    prod_kernel<12><<<(unsigned)nblocks, 128, 0, st>>>(d_descs, ndesc);
+  else
+    prod_kernel<MAXN_SPF><<<(unsigned)nblocks, 128, 0, st>>>(d_descs, ndesc);
+}
+
+// ---------------------------------------------------------------------------
+// Batched single-hole contraction, first stage (zher2k / zgemm('T','N') loops of
+// Calc_rho1mode and Calc_MeanField, gmctdh_objects.f90:452-457, :595-600).
+// Block b of a descriptor handles fibre tiles b, b + nblk, ...; every thread owns
+// one (j1, j2) pair and a fibre group; groups are summed in shared memory.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
+  __shared__ int s_di;
+  __shared__ cplx Xs[HOLE_TILE * MAXN_SPF];
+  __shared__ cplx Ys[HOLE_TILE * MAXN_SPF];
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const HoleDesc& d = descs[s_di];
+  const int b = (int)(blockIdx.x - d.block_start);
+  const int n1 = d.n1, n2 = d.n2, npairs = n1 * n2;
+  const long long L = d.L, nfib = d.L * d.R;
+  const long long ntiles = (nfib + HOLE_TILE - 1) / HOLE_TILE;
+  const int tid = threadIdx.x;
+  const bool small = npairs <= HOLE_THREADS;
+  const int G = small ? HOLE_THREADS / npairs : 1;
+  const int pair0 = small ? tid % npairs : tid;
+  const int g = small ? tid / npairs : 0;
+  cplx acc[4] = {mkc(0, 0), mkc(0, 0), mkc(0, 0), mkc(0, 0)};
+  for (long long tile = b; tile < ntiles; tile += d.nblk) {
+    const long long p0 = tile * HOLE_TILE;
+    for (int e = tid; e < HOLE_TILE * n1; e += HOLE_THREADS) {
+      int q = e % HOLE_TILE, j = e / HOLE_TILE;
+      long long p = p0 + q;
+      cplx v = mkc(0, 0);
+      if (p < nfib) { long long l = p % L, r = p / L; v = d.X[l + L * (j + (long long)n1 * r)]; }
+      Xs[q * MAXN_SPF + j] = v;
+    }
+    for (int e = tid; e < HOLE_TILE * n2; e += HOLE_THREADS) {
+      int q = e % HOLE_TILE, j = e / HOLE_TILE;
+      long long p = p0 + q;
+      cplx v = mkc(0, 0);
+      if (p < nfib) { long long l = p % L, r = p / L; v = d.Y[l + L * (j + (long long)n2 * r)]; }
+      Ys[q * MAXN_SPF + j] = v;
+    }
+    __syncthreads();
+    if (small) {
+      if (g < G) {
+        const int j1 = pair0 % n1, j2 = pair0 / n1;
+        for (int q = g; q < HOLE_TILE; q += G) cfma_conj(acc[0], Xs[q * MAXN_SPF + j1], Ys[q * MAXN_SPF + j2]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        int pr = pair0 + HOLE_THREADS * k;
+        if (pr < npairs) {
+          const int j1 = pr % n1, j2 = pr / n1;
+          for (int q = 0; q < HOLE_TILE; ++q) cfma_conj(acc[k], Xs[q * MAXN_SPF + j1], Ys[q * MAXN_SPF + j2]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  cplx* out = d.partial + (long long)b * npairs;
+  if (small) {
+    cplx* red = Xs;   // reuse (HOLE_TILE*MAXN_SPF >= HOLE_THREADS)
+    red[tid] = acc[0];
+    __syncthreads();
+    if (tid < npairs) {
+      cplx s = mkc(0, 0);
+      for (int gg = 0; gg < G; ++gg) s = cadd(s, red[gg * npairs + tid]);
+      out[tid] = s;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int pr = pair0 + HOLE_THREADS * k;
+      if (pr < npairs) out[pr] = acc[k];
+    }
+  }
+}
+
+void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st) {
+  if (ndesc <= 0 || nblocks <= 0) return;
+  hole_kernel<<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
+}
+
+// ---------------------------------------------------------------------------
+// Second stage: deterministic sum of partials into the target matrices.
+// ---------------------------------------------------------------------------
+__global__ void reduce_kernel(const RedTarget* __restrict__ tg, const RedTerm* __restrict__ terms) {
+  const RedTarget& t = tg[blockIdx.x];
+  const int npairs = t.n1 * t.n2;
+  for (int pr = threadIdx.x; pr < npairs; pr += blockDim.x) {
+    const int j1 = pr % t.n1, j2 = pr / t.n1;
+    const int prT = j2 + t.n1 * j1;
+    cplx s = mkc(0, 0), sT = mkc(0, 0);
+    for (int k = 0; k < t.count; ++k) {
+      const RedTerm& rt = terms[t.first + k];
+      cplx a = mkc(0, 0), aT = mkc(0, 0);
+      for (int bb = 0; bb < rt.nblk; ++bb) {
+        a = cadd(a, rt.partial[(long long)bb * npairs + pr]);
+        if (t.hermitize) aT = cadd(aT, rt.partial[(long long)bb * npairs + prT]);
+      }
+      s = cadd(s, cmul(rt.alpha, a));
+      if (t.hermitize) sT = cadd(sT, cmul(rt.alpha, aT));
+    }
+    if (t.hermitize) s = cscale(cadd(s, cconj(sT)), 0.5);
+    cplx* o = t.out + j1 + (long long)t.ld * j2;
+    *o = t.accumulate ? cadd(*o, s) : s;
+  }
+}
+
+void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st) {
+  if (ntg <= 0) return;
+  reduce_kernel<<<ntg, 128, 0, st>>>(d_tg, d_terms);
+}
+
+// ---------------------------------------------------------------------------
+// h1mode and operator-applied SPFs for DVR modes (Calc_h1mode, hamilton.f90:416-482;
+// MultTens / MultTensDiag, :577-629).  One block per (mode, operator).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) h1_kernel(const H1Desc* __restrict__ descs) {
+  extern __shared__ cplx sm[];
+  const H1Desc& d = descs[blockIdx.x];
+  const int G = d.G, n2 = d.n2, n1 = d.n1;
+  const int tot = G * n2;
+  cplx* bufA = sm;
+  cplx* bufB = sm + tot;
+  cplx* X = sm + 2 * tot;   // n1*n2 scratch for the Hermitian part
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) bufA[e] = d.phi_r[e];
+  __syncthreads();
+  int ll = 1;
+  for (int k = 0; k < d.ndof; ++k) {
+    const int ng = d.ng[k];
+    const int ot = d.optype[k];
+    if (ot != 0) {
+      const cplx* M = d.mat[k];
+      for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int a = e % ll;
+        const int gg = (e / ll) % ng;
+        const int bidx = e / (ll * ng);
+        cplx v;
+        if (ot == 1) {
+          // psi(.., g, ..) <- sum_g' psi(.., g', ..) M(g', g)   (zlacrm from the right)
+          v = mkc(0, 0);
+          const cplx* in = bufA + a + (long long)ll * ng * bidx;
+          const cplx* mc = M + (long long)ng * gg;
+          for (int gp = 0; gp < ng; ++gp) cfma(v, mc[gp], in[(long long)ll * gp]);
+        } else {
+          v = cscale(bufA[e], M[gg].x);
+        }
+        bufB[e] = v;
+      }
+      __syncthreads();
+      cplx* t = bufA; bufA = bufB; bufB = t;
+    }
+    ll *= ng;
+  }
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) d.ophi[e] = bufA[e];
+  if (d.h == nullptr) return;
+  for (int pr = threadIdx.x; pr < n1 * n2; pr += blockDim.x) {
+    const int j1 = pr % n1, j2 = pr / n1;
+    cplx s = mkc(0, 0);
+    const cplx* pl = d.phi_l + (long long)G * j1;
+    const cplx* po = bufA + (long long)G * j2;
+    for (int gg = 0; gg < G; ++gg) cfma_conj(s, pl[gg], po[gg]);
+    X[pr] = s;
+  }
+  __syncthreads();
+  for (int pr = threadIdx.x; pr < n1 * n2; pr += blockDim.x) {
+    const int j1 = pr % n1, j2 = pr / n1;
+    cplx v = X[pr];
+    if (d.same_state) v = cscale(cadd(v, cconj(X[j2 + n1 * j1])), 0.5);
+    d.h[pr] = v;
+  }
+}
+
+void launch_h1(const H1Desc* d_descs, int ndesc, size_t smem_bytes, cudaStream_t st) {
+  if (ndesc <= 0) return;
+  static size_t configured = 0;
+  if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
+    cudaFuncSetAttribute(h1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    configured = smem_bytes;
+  }
+  h1_kernel<<<ndesc, 256, smem_bytes, st>>>(d_descs);
+}
+
+// ---------------------------------------------------------------------------
+// Cyclic complex Jacobi eigen-decomposition of a Hermitian matrix held in shared
+// memory (the work zheev does inside StdRegInv, maths.f90:36).  Rotations are
+// computed by one thread and applied by all; the sweep count is capped.
+// A[i + ld*j], V likewise.  Returns through *ok whether the sweeps converged.
+// ---------------------------------------------------------------------------
+#define JAC_MAX_SWEEPS 40
+__device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, volatile int* s_flag, volatile double* s_rot,
+                            bool* ok) {
+  const int tid = threadIdx.x;
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    V[i + ld * j] = mkc(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  double fro2 = 0.0;
+  for (int e = 0; e < n * n; ++e) { int i = e % n, j = e / n; fro2 += cabs2(A[i + ld * j]); }
+  const double fro = sqrt(fro2);
+  bool converged = false;
+  for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep) {
+    if (tid == 0) s_flag[0] = 0;
+    __syncthreads();
+    for (int p = 0; p < n - 1; ++p) {
+      for (int q = p + 1; q < n; ++q) {
+        if (tid == 0) {
+          cplx apq = A[p + ld * q];
+          double mag = sqrt(cabs2(apq));
+          double app = A[p + ld * p].x, aqq = A[q + ld * q].x;
+          int rot = (mag > 1e-19 * fro) && (mag * mag > 1e-32 * fabs(app * aqq));
+          s_rot[0] = rot;
+          if (rot) {
+            double ux = apq.x / mag, uy = apq.y / mag;
+            double tau = (aqq - app) / (2.0 * mag);
+            double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            double c = 1.0 / sqrt(1.0 + t * t);
+            double s = t * c;
+            s_rot[1] = c; s_rot[2] = s; s_rot[3] = ux; s_rot[4] = uy; s_rot[5] = t * mag;
+            s_flag[0] = 1;
+          }
+        }
+        __syncthreads();
+        if (s_rot[0] != 0.0) {
+          const double c = s_rot[1], s = s_rot[2];
+          const cplx u = mkc(s_rot[3], s_rot[4]);
+          const cplx uc = cconj(u);
+          for (int k = tid; k < n; k += blockDim.x) {
+            cplx vp = V[k + ld * p], vq = V[k + ld * q];
+            V[k + ld * p] = csub(cscale(vp, c), cscale(cmul(uc, vq), s));
+            V[k + ld * q] = cadd(cscale(cmul(u, vp), s), cscale(vq, c));
+            if (k == p || k == q) continue;
+            cplx akp = A[k + ld * p], akq = A[k + ld * q];
+            cplx nkp = csub(cscale(akp, c), cscale(cmul(uc, akq), s));
+            cplx nkq = cadd(cscale(cmul(u, akp), s), cscale(akq, c));
+            A[k + ld * p] = nkp; A[p + ld * k] = cconj(nkp);
+            A[k + ld * q] = nkq; A[q + ld * k] = cconj(nkq);
+          }
+          if (tid == 0) {
+            const double tm = s_rot[5];
+            A[p + ld * p] = mkc(A[p + ld * p].x - tm, 0.0);
+            A[q + ld * q] = mkc(A[q + ld * q].x + tm, 0.0);
+            A[p + ld * q] = mkc(0, 0);
+            A[q + ld * p] = mkc(0, 0);
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (s_flag[0] == 0) { converged = true; break; }
+    __syncthreads();
+  }
+  *ok = converged;
+}
+
+__global__ void __launch_bounds__(64) reginv_kernel(const RegInvDesc* __restrict__ descs, const MFOp* __restrict__ ops,
+                                                    int* status) {
+  __shared__ cplx A[MAXN_SPF * MAXN_SPF];
+  __shared__ cplx V[MAXN_SPF * MAXN_SPF];
+  __shared__ cplx Inv[MAXN_SPF * MAXN_SPF];
+  __shared__ double w[MAXN_SPF];
+  __shared__ int s_flag[1];
+  __shared__ double s_rot[8];
+  const RegInvDesc& d = descs[blockIdx.x];
+  const int n = d.n, ld = MAXN_SPF;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    // upper triangle is authoritative (zheev 'U'): mirror it
+    cplx v = (i <= j) ? d.A[i + n * j] : cconj(d.A[j + n * i]);
+    if (i == j) v.y = 0.0;
+    A[i + ld * j] = v;
+  }
+  __syncthreads();
+  bool ok;
+  jacobi_herm(A, V, n, ld, s_flag, s_rot, &ok);
+  if (!ok && threadIdx.x == 0) atomicOr(status, DEVST_EIG_NOCONV);
+  if (threadIdx.x < n) {
+    double wv = A[threadIdx.x + ld * threadIdx.x].x;
+    double f;
+    if (d.regtype == 0) {   // 'poly'
+      double eps = d.eps;
+      double wr = (wv < eps) ? 0.5 * (eps + wv * wv / eps) : wv;
+      f = 1.0 / wr;
+    } else {                // 'tikh'
+      f = wv / (wv * wv + d.eps * d.eps);
+    }
+    w[threadIdx.x] = f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    cplx s = mkc(0, 0);
+    for (int k = 0; k < n; ++k) {
+      cplx vik = V[i + ld * k], vjk = V[j + ld * k];
+      s = cadd(s, cscale(cmul(vik, cconj(vjk)), w[k]));
+    }
+    Inv[i + ld * j] = s;
+    if (d.inv_out) d.inv_out[i + n * j] = s;
+  }
+  __syncthreads();
+  for (int o = 0; o < d.op_count; ++o) {
+    const MFOp& op = ops[d.op_first + o];
+    for (int e = threadIdx.x; e < n * op.n2; e += blockDim.x) {
+      int i = e % n, j = e / n;
+      cplx s = mkc(0, 0);
+      for (int k = 0; k < n; ++k) cfma(s, Inv[i + ld * k], op.mf[k + n * j]);
+      op.out[i + n * j] = s;
+    }
+  }
+}
+
+void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st) {
+  if (ndesc <= 0) return;
+  reginv_kernel<<<ndesc, 64, 0, st>>>(d_descs, d_ops, d_status);
+}
+
+// Tridiagonal eigenproblem of the Lanczos matrix (dstev, cmf2_integration.f90:85)
+__global__ void tridiag_kernel(const double* alpha, const double* beta, int n, double* evals, double* evecs,
+                               int* status) {
+  __shared__ cplx A[MAXN_SPF * MAXN_SPF];
+  __shared__ cplx V[MAXN_SPF * MAXN_SPF];
+  __shared__ int s_flag[1];
+  __shared__ double s_rot[8];
+  const int ld = MAXN_SPF;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    double v = 0.0;
+    if (i == j) v = alpha[i];
+    else if (j == i + 1) v = beta[i];
+    else if (i == j + 1) v = beta[j];
+    A[i + ld * j] = mkc(v, 0.0);
+  }
+  __syncthreads();
+  bool ok;
+  jacobi_herm(A, V, n, ld, s_flag, s_rot, &ok);
+  if (!ok && threadIdx.x == 0) atomicOr(status, DEVST_EIG_NOCONV);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    evecs[i + n * j] = V[i + ld * j].x;   // real symmetric input keeps V real
+  }
+  if (threadIdx.x < n) evals[threadIdx.x] = A[threadIdx.x + ld * threadIdx.x].x;
+}
+
+void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, double* evals, double* evecs,
+                           int* d_status, cudaStream_t st) {
+  tridiag_kernel<<<1, 64, 0, st>>>(alpha, beta, n, evals, evecs, d_status);
+}
+
+// ---------------------------------------------------------------------------
+// DVR SPF derivative with the (1 - P) projector (derivatives.f90:96-153).
+// One block per (mode, state).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) spf_kernel(const SpfDesc* __restrict__ descs, const SpfOp* __restrict__ ops,
+                                                  cplx* __restrict__ out, cplx der, int* status) {
+  extern __shared__ cplx sm[];
+  const SpfDesc& d = descs[blockIdx.x];
+  const int G = d.G, n = d.n;
+  cplx* phi = sm;
+  cplx* dph = sm + (long long)G * n;
+  __shared__ cplx S[MAXN_SPF * MAXN_SPF];
+  __shared__ cplx O[MAXN_SPF * MAXN_SPF];
+  for (int e = threadIdx.x; e < G * n; e += blockDim.x) phi[e] = d.phi[e];
+  for (int e = threadIdx.x; e < G * n; e += blockDim.x) {
+    const int g = e % G, j1 = e / G;
+    cplx acc = mkc(0, 0);
+    for (int o = 0; o < d.op_count; ++o) {
+      const SpfOp& op = ops[d.op_first + o];
+      const cplx* oph = op.ophi + g;
+      for (int j2 = 0; j2 < op.n2; ++j2) cfma(acc, oph[(long long)G * j2], op.rm[j1 + n * j2]);
+    }
+    dph[e] = cmul(der, acc);
+  }
+  __syncthreads();
+  for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
+    const int which = pr / (n * n);
+    const int q = pr % (n * n);
+    const int j1 = q % n, j2 = q / n;
+    const cplx* a = phi + (long long)G * j1;
+    const cplx* b = (which == 0 ? phi : dph) + (long long)G * j2;
+    cplx s = mkc(0, 0);
+    for (int g = 0; g < G; ++g) cfma_conj(s, a[g], b[g]);
+    if (which == 0) S[j1 + MAXN_SPF * j2] = s; else O[j1 + MAXN_SPF * j2] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // zposv('U'): S = U^H U, solve for the n right-hand sides in O (overwritten by X)
+    const int ld = MAXN_SPF;
+    bool fail = false;
+    for (int j = 0; j < n; ++j) {
+      double djj = S[j + ld * j].x;
+      for (int k = 0; k < j; ++k) djj -= cabs2(S[k + ld * j]);
+      if (!(djj > 0.0)) { fail = true; djj = 1e-300; }
+      double ujj = sqrt(djj);
+      S[j + ld * j] = mkc(ujj, 0.0);
+      for (int i = j + 1; i < n; ++i) {
+        cplx sji = S[j + ld * i];
+        for (int k = 0; k < j; ++k) sji = csub(sji, cmul(cconj(S[k + ld * j]), S[k + ld * i]));
+        S[j + ld * i] = cscale(sji, 1.0 / ujj);
+      }
+    }
+    for (int c = 0; c < n; ++c) {
+      // forward: U^H y = o
+      for (int i = 0; i < n; ++i) {
+        cplx v = O[i + ld * c];
+        for (int k = 0; k < i; ++k) v = csub(v, cmul(cconj(S[k + ld * i]), O[k + ld * c]));
+        O[i + ld * c] = cscale(v, 1.0 / S[i + ld * i].x);
+      }
+      // backward: U x = y
+      for (int i = n - 1; i >= 0; --i) {
+        cplx v = O[i + ld * c];
+        for (int k = i + 1; k < n; ++k) v = csub(v, cmul(S[i + ld * k], O[k + ld * c]));
+        O[i + ld * c] = cscale(v, 1.0 / S[i + ld * i].x);
+      }
+    }
+    if (fail) atomicOr(status, DEVST_CHOL_FAIL);
+  }
+  __syncthreads();
+  cplx* o = out + d.out_offset;
+  for (int e = threadIdx.x; e < G * n; e += blockDim.x) {
+    const int g = e % G, j = e / G;
+    cplx v = dph[e];
+    for (int k = 0; k < n; ++k) v = csub(v, cmul(phi[g + (long long)G * k], O[k + MAXN_SPF * j]));
+    o[e] = v;
+  }
+}
+
+void launch_spf(const SpfDesc* d_descs, int ndesc, const SpfOp* d_ops, cplx* out, cplx der_factor,
+                size_t smem_bytes, int* d_status, cudaStream_t st) {
+  if (ndesc <= 0) return;
+  static size_t configured = 0;
+  if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
+    cudaFuncSetAttribute(spf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    configured = smem_bytes;
+  }
+  spf_kernel<<<ndesc, 256, smem_bytes, st>>>(d_descs, d_ops, out, der_factor, d_status);
+}
+
+// ---------------------------------------------------------------------------
+// Elementwise helpers
+// ---------------------------------------------------------------------------
+__global__ void termsum_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges, int nr,
+                               const SumSrc* __restrict__ srcs, long long total) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  int r = 0;
+  while (r + 1 < nr && i >= ranges[r + 1].offset) ++r;
+  const SumRange& rg = ranges[r];
+  const long long li = i - rg.offset;
+  if (li < 0 || li >= rg.n) return;
+  cplx acc = mkc(0, 0);
+  for (int k = 0; k < rg.count; ++k) {
+    const SumSrc& s = srcs[rg.first + k];
+    cfma(acc, s.coeff, s.src[li]);
+  }
+  out[i] = acc;
+}
+
+void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs, long long total,
+                    cudaStream_t st) {
+  if (total <= 0) return;
+  termsum_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total);
+}
+
+__global__ void stage_kernel(cplx* __restrict__ out, const cplx* __restrict__ base, StageArgs a, double dt,
+                             long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cplx s = mkc(0, 0);
+  for (int k = 0; k < a.nk; ++k) {
+    cplx v = a.k[k][i];
+    s.x = fma(a.c[k], v.x, s.x);
+    s.y = fma(a.c[k], v.y, s.y);
+  }
+  cplx b = base[i];
+  out[i] = mkc(fma(dt, s.x, b.x), fma(dt, s.y, b.y));
+}
+
+void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  stage_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, base, a, dt, n);
+}
+
+__global__ void copy_scale_kernel(cplx* out, const cplx* in, cplx s, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = cmul(s, in[i]);
+}
+void launch_copy_scale(cplx* out, const cplx* in, cplx s, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  copy_scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, in, s, n);
+}
+
+__global__ void axpy_kernel(cplx* y, const cplx* x, cplx a, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { cplx v = y[i]; cfma(v, a, x[i]); y[i] = v; }
+}
+void launch_axpy(cplx* y, const cplx* x, cplx a, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, x, a, n);
+}
+
+__global__ void gemv_cols_kernel(cplx* out, const cplx* basis, long long ld, const cplx* coef, int ncol, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cplx s = mkc(0, 0);
+  for (int j = 0; j < ncol; ++j) cfma(s, coef[j], basis[i + ld * j]);
+  out[i] = s;
+}
+void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* coef, int ncol, long long n,
+                      cudaStream_t st) {
+  if (n <= 0) return;
+  gemv_cols_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, basis, ld, coef, ncol, n);
+}

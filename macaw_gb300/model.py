@@ -1,0 +1,712 @@
+"""Host-side model set-up for the G-MCTDH propagation core.
+
+This module stands in for the reference's one-off host work that precedes the
+time loop: reading the keyword input and the operator file
+(input.f90:30-426, :812-1144), building the primitive DVR grids and matrices
+(dvr.f90:107-357), deduplicating the per-mode operators
+(hamilton.f90:91-167, :353-399), laying out the coefficient and SPF vectors
+(init_calc.f90:22-53, :160-181) and building the initial wavefunction
+(init_calc.f90:230-761 single-conf, :763-1068 SetSPF).
+
+Everything here is FP64 NumPy and runs once per model.  The arrays produced
+are exactly what the reference keeps in its global modules (psidef, storage,
+hamilton, dvr); they are handed to the GPU core through the C-ABI
+(``include/macaw_gb300.h``) and to the CPU oracle.
+
+Indexing is 0-based throughout (the reference is 1-based); tensors keep the
+reference's column-major order with mode 1 fastest (init_calc.f90:531-536).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import os
+import re
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+AU2EV = 27.2113961          # globals.f90:17
+AU2FS = 0.02418884326505    # globals.f90:17
+AU2CMM1 = 219474.63         # globals.f90:18
+
+# Primitive DOF operator codes (input.f90:1098-1137, hamilton.f90:27-30)
+OP_ID = 0
+OP_P = -1        # p = -i d/dq
+OP_DQ2 = -2      # d^2/dq^2
+OP_QP = -3       # qp + pq
+OP_SINM2 = -4    # sin^-2 (Legendre DVR only)
+
+INT_RK45 = 1     # Cash-Karp (input.f90:280-282)
+INT_DOPRI = 2    # Dormand-Prince (input.f90:283-285)
+INT_CMF2 = 10    # constant mean field (input.f90:295-331)
+
+
+class ModelError(ValueError):
+    """Raised for input the reference would reject with ``stop``."""
+
+
+# ----------------------------------------------------------------------------
+# Primitive DVRs
+# ----------------------------------------------------------------------------
+
+def harm_dvr(n: int, x0: float, mw: float):
+    """Harmonic-oscillator DVR (dvr.f90:263-357).
+
+    Returns grid, weights, d1 (d/dq), d2 (d^2/dq^2), xd1 (x d/dx + d/dx x)
+    as float64 arrays.  Eigenvector signs are fixed by making the first row
+    of the transformation non-negative, as the reference does (dvr.f90:287).
+    """
+    if n < 2:
+        raise ModelError("too few grid points selected for a DVR")
+    xmat = np.zeros((n, n))
+    for i in range(1, n):
+        xmat[i - 1, i] = math.sqrt(0.5 * i / mw)
+        xmat[i, i - 1] = xmat[i - 1, i]
+    grid, trafo = np.linalg.eigh(xmat)
+    grid = grid.copy()
+    for i in range(1, n // 2 + 1):
+        d = 0.5 * (-grid[i - 1] + grid[n - i])
+        grid[i - 1] = -d
+        grid[n - i] = d
+    if n % 2 == 1:
+        grid[n // 2] = 0.0
+    grid = grid + x0
+    for i in range(n):
+        if trafo[0, i] < 0.0:
+            trafo[:, i] = -trafo[:, i]
+    w = trafo[0, :] ** 2 * np.exp(mw * (grid - x0) ** 2) * math.sqrt(math.pi / mw)
+    aux = np.zeros((n, n))
+    for i in range(1, n):
+        aux[i - 1, i] = math.sqrt(i)
+        aux[i, i - 1] = -math.sqrt(i)
+    aux *= math.sqrt(0.5 * mw)
+    d1 = trafo.T @ (aux @ trafo)
+    aux = np.zeros((n, n))
+    for i in range(1, n - 1):
+        aux[i - 1, i + 1] = math.sqrt(i * (i + 1))
+        aux[i + 1, i - 1] = -math.sqrt(i * (i + 1))
+    xd1 = trafo.T @ (aux @ trafo)
+    d1 = 0.5 * (d1 - d1.T)
+    xd1 = 0.5 * (xd1 - xd1.T)
+    np.fill_diagonal(d1, 0.0)
+    np.fill_diagonal(xd1, 0.0)
+    aux = np.zeros((n, n))
+    for i in range(1, n + 1):
+        aux[i - 1, i - 1] = -(2 * i - 1)
+    for i in range(1, n - 1):
+        aux[i - 1, i + 1] = math.sqrt(i * (i + 1))
+        aux[i + 1, i - 1] = aux[i - 1, i + 1]
+    d2 = 0.5 * mw * (trafo.T @ (aux @ trafo))
+    d2 = np.triu(d2) + np.triu(d2, 1).T
+    return grid, w, d1, d2, xd1
+
+
+def sin_dvr(n: int, xi: float, xf: float):
+    """Sine (particle-in-a-box) DVR (dvr.f90:107-186)."""
+    if n < 2:
+        raise ModelError("too few grid points selected for a DVR")
+    dx = (xf - xi) / (n - 1)
+    grid = xi + dx * np.arange(n, dtype=np.float64)
+    w = np.full(n, dx)
+    if abs(abs(xf) - abs(xi)) < np.finfo(float).eps:
+        for i in range(1, n // 2 + 1):
+            d = 0.5 * (-grid[i - 1] + grid[n - i])
+            grid[i - 1] = -d
+            grid[n - i] = d
+        if n % 2 == 1:
+            grid[n // 2] = 0.0
+    np1 = float(n + 1)
+    ii = np.arange(1, n + 1)
+    trafo = np.sin(np.outer(ii, ii) * math.pi / np1) * math.sqrt(2.0 / np1)
+    aux = np.zeros((n, n))
+    for i in range(1, n + 1):
+        for j in range(1, n + 1):
+            if i != j:
+                aux[i - 1, j - 1] = (abs(i - j) % 2) * i * j / float(i * i - j * j)
+    aux1 = (4.0 / (xf - xi)) * (aux @ trafo)
+    d1 = trafo @ aux1
+    xd1 = d1 * (grid[:, None] + grid[None, :])
+    d2 = np.zeros((n, n))
+    for i in range(1, n + 1):
+        d2[i - 1, i - 1] = (2 * n * n + 4 * n + 3) / 3.0 - 1.0 / math.sin(math.pi * i / np1) ** 2
+    ph = 0.5 * math.pi
+    for i in range(1, n):
+        s = -1.0
+        for j in range(i + 1, n + 1):
+            d2[i - 1, j - 1] = (1.0 / math.sin(ph * (i - j) / np1) ** 2
+                                - 1.0 / math.sin(ph * (i + j) / np1) ** 2) * s
+            s = -s
+    fac = 0.5 * (math.pi / (xf - xi + 2 * dx)) ** 2
+    d2 = -np.triu(d2) * fac
+    d2 = d2 + np.triu(d2, 1).T
+    return grid, w, d1, d2, xd1
+
+
+# ----------------------------------------------------------------------------
+# Model description
+# ----------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class Term:
+    """One Hamiltonian term ae * |lhs><rhs| * prod_k op_k (input.f90:812-1144)."""
+    coeff: complex
+    lhs: int                   # 0-based electronic state
+    rhs: int
+    dof_ops: Dict[int, int]    # 0-based dof -> primitive operator code
+
+
+@dataclasses.dataclass
+class Model:
+    """The state of the reference's global modules after set-up."""
+    nstates: int
+    mode_dofs: List[List[int]]              # iDOF (0-based dofs per mode)
+    multiset: List[bool]                    # MultiSet
+    nspf: np.ndarray                        # (nmodes, nstates) int64
+    dvr_type: List[str]                     # per dof: 'HO', 'sin', 'gwp'
+    ngp: List[int]                          # per dof
+    dvrpar: List[Tuple[float, float]]       # per dof
+    terms: List[Term]
+    # propagation parameters (globals.f90)
+    tinit: float = 0.0                      # a.u.
+    tfinal: float = 100.0 / AU2FS
+    tout: float = 1.0 / AU2FS               # writetime
+    eps_int: float = 1e-8
+    eps_rho: float = 1e-8
+    eps_ovl: float = 1e-8                   # eps_S
+    eps_C: float = 1e-8
+    eps_A: float = 1e-8
+    eps_psi: float = 1e-8
+    min_stepsize: float = 1e-9 / AU2FS
+    int_type: int = INT_RK45
+    int_type_A: int = 5                     # Lanczos
+    int_type_psi: int = 1                   # rk45 (Cash-Karp) for the SPFs
+    relaxation: bool = False
+    inorm_psi: int = 0
+    init_state: int = 0                     # populated electronic state (0-based)
+    init_spf: Dict[int, Tuple[str, tuple]] = dataclasses.field(default_factory=dict)
+    label: str = "model"
+
+    # ---- derived (filled by finalize) ----
+    def finalize(self) -> "Model":
+        self.nmodes = len(self.mode_dofs)
+        self.ndof = len(self.dvr_type)
+        self.nspf = np.asarray(self.nspf, dtype=np.int64).reshape(self.nmodes, self.nstates)
+        for m in range(self.nmodes):
+            if not self.multiset[m]:
+                self.nspf[m, :] = self.nspf[m, 0]
+        self.is_gwp_mode = [self.dvr_type[self.mode_dofs[m][0]] == "gwp" for m in range(self.nmodes)]
+        for m in range(self.nmodes):
+            kinds = {self.dvr_type[d] == "gwp" for d in self.mode_dofs[m]}
+            if len(kinds) != 1:
+                raise ModelError(f"mode {m + 1} mixes dvr and gwp representations")
+        self.modes_dvr = [m for m in range(self.nmodes) if not self.is_gwp_mode[m]]
+        self.modes_gwp = [m for m in range(self.nmodes) if self.is_gwp_mode[m]]
+        self.der_factor = complex(-1.0, 0.0) if self.relaxation else complex(0.0, -1.0)
+        self._build_dvr()
+        self._build_operators()
+        self._build_layout()
+        return self
+
+    # init_calc.f90:97-123 (DVR matrices), :126-133 (ngpm)
+    def _build_dvr(self):
+        self.grid: Dict[int, np.ndarray] = {}
+        self.wgrid: Dict[int, np.ndarray] = {}
+        self.d1: Dict[int, np.ndarray] = {}
+        self.d2: Dict[int, np.ndarray] = {}
+        self.xd1: Dict[int, np.ndarray] = {}
+        for d in range(self.ndof):
+            t = self.dvr_type[d]
+            if t == "HO":
+                g, w, d1, d2, xd1 = harm_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1])
+            elif t == "sin":
+                g, w, d1, d2, xd1 = sin_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1])
+            elif t == "gwp":
+                continue
+            else:
+                raise ModelError(f"DVR type {t!r} is not supported by this core")
+            self.grid[d], self.wgrid[d], self.d1[d], self.d2[d], self.xd1[d] = g, w, d1, d2, xd1
+        self.ngpm = {}
+        for m in self.modes_dvr:
+            self.ngpm[m] = int(np.prod([self.ngp[d] for d in self.mode_dofs[m]]))
+
+    # hamilton.f90:91-167 (operator dedup), :353-374 (IsIdentity), :377-399 (SkipTerm)
+    def _build_operators(self):
+        nham = len(self.terms)
+        self.nham = nham
+        self.iopdof = np.zeros((self.ndof, nham), dtype=np.int64)
+        for t, term in enumerate(self.terms):
+            for d, op in term.dof_ops.items():
+                self.iopdof[d, t] = op
+        self.oper: List[List[Tuple[int, int, Tuple[int, ...]]]] = []
+        self.ioper = np.zeros((self.nmodes, nham), dtype=np.int64)
+        for m in range(self.nmodes):
+            ops: List[Tuple[int, int, Tuple[int, ...]]] = []
+            for t, term in enumerate(self.terms):
+                if self.multiset[m]:
+                    el = (term.lhs, term.rhs)
+                else:
+                    el = (0, 0)
+                vec = (el[0], el[1], tuple(int(self.iopdof[d, t]) for d in self.mode_dofs[m]))
+                try:
+                    k = ops.index(vec)
+                except ValueError:
+                    ops.append(vec)
+                    k = len(ops) - 1
+                self.ioper[m, t] = k
+            self.oper.append(ops)
+        self.nopermax = max(len(o) for o in self.oper)
+        self.is_identity = np.zeros((self.nmodes, self.nopermax), dtype=bool)
+        for m in range(self.nmodes):
+            for k, (l, r, dops) in enumerate(self.oper[m]):
+                if l == r and all(o == 0 for o in dops):
+                    self.is_identity[m, k] = True
+        self.skip_term = np.zeros((self.nmodes, nham), dtype=bool)
+        for t in range(nham):
+            for m in range(self.nmodes):
+                if (not self.is_gwp_mode[m]) and self.is_identity[m, self.ioper[m, t]]:
+                    self.skip_term[m, t] = True
+        self.ae = np.array([term.coeff for term in self.terms], dtype=np.complex128)
+        self.lhs_el = np.array([term.lhs for term in self.terms], dtype=np.int64)
+        self.rhs_el = np.array([term.rhs for term in self.terms], dtype=np.int64)
+        for d in range(self.ndof):
+            if self.dvr_type[d] == "gwp":
+                continue
+            for code in set(int(c) for c in self.iopdof[d]):
+                if code in (OP_ID, OP_P, OP_DQ2, OP_QP) or 1 <= code <= 20:
+                    continue
+                raise ModelError(f"primitive operator code {code} on dof {d + 1} is not supported")
+
+    # init_calc.f90:22-53 (nAConf, AStateOffset), :160-181 (ipsiSPF, dimPsi)
+    def _build_layout(self):
+        self.naconf = np.array([int(np.prod(self.nspf[:, s])) for s in range(self.nstates)], dtype=np.int64)
+        self.astate_offset = np.zeros(self.nstates, dtype=np.int64)
+        off = 0
+        for s in range(self.nstates):
+            self.astate_offset[s] = off
+            off += int(self.naconf[s])
+        self.naconftot = off
+        self.ipsispf = np.zeros((self.nmodes, self.nstates), dtype=np.int64)
+        dim = 0
+        for s in range(self.nstates):
+            for m in range(self.nmodes):
+                if (not self.multiset[m]) and s > 0:
+                    self.ipsispf[m, s] = self.ipsispf[m, 0]
+                    continue
+                self.ipsispf[m, s] = dim
+                if self.is_gwp_mode[m]:
+                    dim += len(self.mode_dofs[m]) * int(self.nspf[m, s])
+                else:
+                    dim += self.ngpm[m] * int(self.nspf[m, s])
+        self.dimpsi = dim
+        self.nspfmax = int(self.nspf.max())
+        self.ns00max = int(max([self.nspf[m, :].max() for m in self.modes_gwp], default=0))
+
+    # ---- helpers ----
+    def a_state(self, A: np.ndarray, s: int) -> np.ndarray:
+        """View of state s's coefficient tensor, shape nspf[:, s], Fortran order."""
+        o = int(self.astate_offset[s])
+        return A[o:o + int(self.naconf[s])].reshape(tuple(int(x) for x in self.nspf[:, s]), order="F")
+
+    def spf_block(self, psi: np.ndarray, m: int, s: int) -> np.ndarray:
+        """SPF block of DVR mode m, state s: (G, n) Fortran-ordered view."""
+        o = int(self.ipsispf[m, s])
+        n = int(self.nspf[m, s])
+        if self.is_gwp_mode[m]:
+            nd = len(self.mode_dofs[m])
+            return psi[o:o + nd * n].reshape((nd, n), order="F")
+        G = self.ngpm[m]
+        return psi[o:o + G * n].reshape((G, n), order="F")
+
+    def dof_op_matrix(self, d: int, code: int) -> Tuple[str, np.ndarray]:
+        """('dense', M) or ('diag', v) for primitive operator ``code`` on DVR dof d.
+
+        Dense matrices are applied from the right by MultTens (hamilton.f90:577-602)
+        as psi(.., g, ..) <- sum_g' psi(.., g', ..) M(g', g); p and qp carry the
+        +i factor of hamilton.f90:455-461.
+        """
+        if code == OP_P:
+            return "dense", 1j * self.d1[d]
+        if code == OP_DQ2:
+            return "dense", self.d2[d].astype(np.complex128)
+        if code == OP_QP:
+            return "dense", 1j * self.xd1[d]
+        if 1 <= code <= 20:
+            return "diag", self.grid[d] ** code
+        raise ModelError(f"operator code {code} not supported on a DVR dof")
+
+
+# ----------------------------------------------------------------------------
+# Initial wavefunction (init_calc.f90:230-761 single-conf, SetSPF :763-1068)
+# ----------------------------------------------------------------------------
+
+def initial_wavefunction(model: Model) -> Tuple[np.ndarray, np.ndarray]:
+    """Single-configuration initial state: A = e_1 on ``init_state`` and SPFs
+    built by SetSPF (DVR: product Gaussian, then q-multiplied virtual SPFs,
+    Gram-Schmidt + QR; GWP: lattice of Gaussians).  Returns (A, psi) with the
+    normalisation of init_calc.f90:208-221 applied."""
+    A = np.zeros(model.naconftot, dtype=np.complex128)
+    A[int(model.astate_offset[model.init_state])] = 1.0
+    psi = np.zeros(model.dimpsi, dtype=np.complex128)
+    phi: Dict[int, np.ndarray] = {}
+    gwp_par: Dict[int, tuple] = {}
+    for d in range(model.ndof):
+        kind, par = model.init_spf.get(d, ("gauss", (0.0, 0.0, 0.707107)))
+        if kind == "gauss":
+            if model.dvr_type[d] == "gwp":
+                raise ModelError('Input Error: use "gwp" instead of "gauss"')
+            x0, p0, dx = par
+            g, w = model.grid[d], model.wgrid[d]
+            n = len(g)
+            f = np.zeros(n, dtype=np.complex128)
+            eps = np.finfo(float).eps
+            if abs(x0) < eps and abs(p0) < eps:
+                for j in range(n // 2 + 1):
+                    f[j] = math.exp(-(0.5 * g[j] / dx) ** 2) * math.sqrt(w[j])
+                    f[n - j - 1] = f[j]
+            else:
+                xx = g - x0
+                f = np.exp(-(0.5 * xx / dx) ** 2 + 1j * p0 * xx) * np.sqrt(w)
+            phi[d] = f
+        elif kind == "gwp":
+            if model.dvr_type[d] != "gwp":
+                raise ModelError('gwp initial SPFs are allowed only for "gwp representation"')
+            dist, x0, p0, dx, ovl, scw = par
+            gwp_par[d] = (dist, dx, ovl, scw)
+            eps = np.finfo(float).eps
+            phi[d] = np.array([0.0 if max(abs(x0), abs(p0)) < eps else complex(0.5 * x0 / dx ** 2, p0)],
+                              dtype=np.complex128)
+        else:
+            raise ModelError(f"initial SPF kind {kind!r} not supported")
+    # DVR modes
+    for m in model.modes_dvr:
+        dofs = model.mode_dofs[m]
+        nmd = len(dofs)
+        G = model.ngpm[m]
+        ns = int(model.nspf[m, :].max())
+        shape = tuple(model.ngp[d] for d in dofs)
+        prod = np.ones(shape, dtype=np.complex128)
+        for k, d in enumerate(dofs):
+            sh = [1] * nmd
+            sh[k] = model.ngp[d]
+            prod = prod * phi[d].reshape(sh)
+        psi_t = np.zeros((G, ns), dtype=np.complex128)
+        psi_t[:, 0] = prod.reshape(-1, order="F")
+        psi_t[:, 0] /= np.linalg.norm(psi_t[:, 0])
+        kg = 0
+        jj = 1
+        for j in range(2, ns + 1):
+            jj += 1
+            kg = kg % nmd + 1
+            l = (jj - 2) // nmd + 1
+            col = psi_t[:, l - 1].reshape(shape, order="F").copy()
+            d = dofs[kg - 1]
+            sh = [1] * nmd
+            sh[kg - 1] = model.ngp[d]
+            col = col * model.grid[d].reshape(sh)
+            psi_t[:, j - 1] = col.reshape(-1, order="F")
+        for j in range(1, ns):
+            c = -np.vdot(psi_t[:, 0], psi_t[:, j])
+            psi_t[:, j] += c * psi_t[:, 0]
+        if ns > 1:
+            q, _ = np.linalg.qr(psi_t[:, 1:ns], mode="reduced")
+            psi_t[:, 1:ns] = q
+        for s in range(model.nstates):
+            if (not model.multiset[m]) and s > 0:
+                continue
+            o = int(model.ipsispf[m, s])
+            n = int(model.nspf[m, s])
+            psi[o:o + G * n] = psi_t[:, :n].reshape(-1, order="F")
+    # GWP modes
+    model.gwpa = np.zeros((max([len(model.mode_dofs[m]) for m in model.modes_gwp], default=0),
+                           max(model.ns00max, 1), len(model.modes_gwp)))
+    for i, m in enumerate(model.modes_gwp):
+        dofs = model.mode_dofs[m]
+        nmd = len(dofs)
+        nsm = model.nspfmax
+        xi_values = np.zeros((2 * nsm + 1, nmd), dtype=np.complex128)
+        w_values = np.zeros((2 * nsm + 1, nmd))
+        for j, d in enumerate(dofs):
+            dist, dx, ovl, scw = gwp_par[d]
+            for l in range(-nsm, nsm + 1):
+                w_values[l + nsm, j] = dx * scw ** abs(l)
+            xi_values[nsm, j] = 0.0
+            for l in range(1, nsm + 1):
+                dd = -math.log(ovl) + 0.5 * math.log(2 * scw / (1.0 + scw ** 2))
+                dd = dd * (1.0 + scw ** 2) / w_values[l - 1 + nsm, j] ** 2
+                dd = (xi_values[l - 1 + nsm, j].real + math.sqrt(dd)) / scw ** 2
+                xi_values[l + nsm, j] = dd
+                xi_values[-l + nsm, j] = -dd
+            if abs(phi[d][0]) > np.finfo(float).eps:
+                xi_values[:, j] += phi[d][0]
+        dists = {gwp_par[d][0] for d in dofs}
+        if len(dists) != 1:
+            raise ModelError("the same GWP distribution must be used for all dofs of a mode")
+        ns = int(model.nspf[m, :].max())
+        index_lat = np.zeros((nmd, ns), dtype=np.int64)
+        if ns > 1:
+            if dists.pop() != 0:
+                raise ModelError("only the lattice GWP distribution (0) is supported")
+            i1, i2, l = 1, 1, 2
+            done = False
+            while not done:
+                for i3 in range(i1, i2 + 1):
+                    for j in range(nmd):
+                        for i4 in (-1, 1):
+                            cand = index_lat[:, i3 - 1].copy()
+                            cand[j] += i4
+                            if any(np.array_equal(cand, index_lat[:, j1]) for j1 in range(l - 1)):
+                                continue
+                            index_lat[:, l - 1] = cand
+                            l += 1
+                            if l > ns:
+                                done = True
+                                break
+                        if done:
+                            break
+                    if done:
+                        break
+                i1 = i2 + 1
+                i2 = l - 1
+        psi_t = np.zeros((nmd, ns), dtype=np.complex128)
+        for l in range(ns):
+            for j in range(nmd):
+                psi_t[j, l] = xi_values[index_lat[j, l] + nsm, j]
+                model.gwpa[j, l, i] = -(0.5 / w_values[index_lat[j, l] + nsm, j]) ** 2
+        for s in range(model.nstates):
+            if (not model.multiset[m]) and s > 0:
+                continue
+            o = int(model.ipsispf[m, s])
+            n = int(model.nspf[m, s])
+            psi[o:o + nmd * n] = psi_t[:, :n].reshape(-1, order="F")
+    return A, psi
+
+
+# ----------------------------------------------------------------------------
+# Reader for the reference's keyword input and operator file
+# ----------------------------------------------------------------------------
+
+_OPNAMES = {"p": OP_P, "dq^2": OP_DQ2, "qp": OP_QP, "q": 1}
+
+
+def _parse_dof_op(name: str) -> int:
+    name = name.strip()
+    if name in _OPNAMES:
+        return _OPNAMES[name]
+    mm = re.fullmatch(r"q\^(\d+)", name)
+    if mm and 1 <= int(mm.group(1)) <= 10:
+        return int(mm.group(1))
+    raise ModelError(f"Operator {name} not implemented")
+
+
+def parse_operator_file(text: str, nstates: int) -> List[Term]:
+    """Operator grammar of input.f90:812-1144: ``coeff | el-op | k op | k op ...``.
+
+    Supported el-ops: none or ``1`` (one term per state), ``Sa&b`` (one term, or
+    two Hermitian-conjugate terms for a != b), ``Za&b``."""
+    terms: List[Term] = []
+    for raw in text.splitlines():
+        if raw.startswith("----"):
+            break
+        line = raw.split("#", 1)[0]
+        if not line.strip():
+            continue
+        parts = line.split("|")
+        cstr = parts[0].strip()
+        cstr_num = cstr.replace("d", "e").replace("D", "e")
+        imag = "i" in cstr_num
+        coeff = float(cstr_num.replace("i", "")) * (1j if imag else 1.0)
+        pairs: List[Tuple[int, int]]
+        if len(parts) == 1 or parts[1].strip() == "1":
+            pairs = [(s, s) for s in range(nstates)]
+        else:
+            el = parts[1].strip()
+            mm = re.fullmatch(r"([SZ])\s*(\d+)\s*&\s*(\d+)", el)
+            if not mm:
+                raise ModelError('Only operator labels "1", "Sa&b" or "Za&b" are allowed')
+            a, b = int(mm.group(2)) - 1, int(mm.group(3)) - 1
+            if mm.group(1) == "S":
+                pairs = [(a, b)] if a == b else [(a, b), (b, a)]
+            else:
+                if a == b:
+                    raise ModelError('Electronic operators "Za&b" are allowed only between different states')
+                pairs = [(a, b)]
+        dof_ops: Dict[int, int] = {}
+        for seg in parts[2:]:
+            toks = seg.split(None, 1)
+            if not toks:
+                continue
+            k = int(toks[0]) - 1
+            opname = toks[1].strip() if len(toks) > 1 else "1"
+            if opname == "1":
+                continue
+            dof_ops[k] = _parse_dof_op(opname)
+        for (a, b) in pairs:
+            terms.append(Term(coeff, a, b, dict(dof_ops)))
+    return terms
+
+
+def _read_float(v: str) -> float:
+    return float(v.lower().replace("d", "e"))
+
+
+def parse_input(path: str) -> Model:
+    """Read a reference ``.inp`` file (input.f90:30-426) and its operator file."""
+    base = os.path.dirname(os.path.abspath(path))
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    kw: Dict[str, str] = {}
+    spf_lines: List[str] = []
+    grid_lines: List[str] = []
+    init_lines: List[str] = []
+    cmf_lines: List[str] = []
+    nstates, ndof, nmodes = 1, -1, 0
+    i = 0
+    flags = set()
+    while i < len(lines):
+        line = lines[i].split("#", 1)[0]
+        i += 1
+        s = line.strip()
+        if not s:
+            continue
+        if s == "INIT-WF":
+            while i < len(lines):
+                l2 = lines[i].split("#", 1)[0]
+                i += 1
+                if l2.strip() == "END-INIT-WF":
+                    break
+                if l2.strip():
+                    init_lines.append(l2.strip())
+            continue
+        if "=" in s:
+            name, val = s.split("=", 1)
+            name, val = name.strip().lower(), val.strip().lower()
+        else:
+            name, val = s.lower(), "blank"
+        if name == "nstates":
+            nstates = int(val)
+        elif name == "ndof":
+            ndof = int(val)
+            if ndof > 99:
+                raise ModelError("Error: the maximum number of degrees of freedom is 99")
+        elif name == "nmodes":
+            nmodes = int(val)
+        elif name == "spf":
+            spf_lines = [lines[i + k].split("#", 1)[0] for k in range(nmodes)]
+            i += nmodes
+        elif name == "grid":
+            grid_lines = [lines[i + k].split("#", 1)[0] for k in range(ndof)]
+            i += ndof
+        elif name == "integration":
+            kw[name] = val
+            if val.startswith("cmf2"):
+                cmf_lines = [lines[i].split("#", 1)[0], lines[i + 1].split("#", 1)[0]]
+                i += 2
+        elif name in ("steps", "density", "wp_ovl", "relaxation"):
+            flags.add(name)
+        elif name in ("hamiltonian", "tinit", "tfinal", "tout", "eps_rho", "eps_c", "eps_int",
+                      "eps_s", "eps_pop", "minstep", "normalize", "psi", "npackets"):
+            kw[name] = val
+        elif name in ("expect", "densmat"):
+            continue
+        else:
+            raise ModelError(f"Input instruction: {s} cannot be understood")
+    if int(kw.get("npackets", "1")) != 1:
+        raise ModelError("npackets > 1 is not supported by this core")
+    mode_dofs: List[List[int]] = []
+    multiset: List[bool] = []
+    nspf = np.zeros((nmodes, nstates), dtype=np.int64)
+    for m, ln in enumerate(spf_lines):
+        lhs, rhs = ln.split("=", 1)
+        fields = [f.strip() for f in lhs.split(",")]
+        multiset.append(fields[0] != "S")
+        mode_dofs.append([int(f) - 1 for f in fields[1:]])
+        vals = [int(v) for v in rhs.split(",")]
+        for s in range(nstates):
+            nspf[m, s] = vals[s] if s < len(vals) else vals[0]
+    dvr_type = [""] * ndof
+    ngp = [0] * ndof
+    dvrpar = [(0.0, 0.0)] * ndof
+    for ln in grid_lines:
+        toks = ln.split()
+        d = int(toks[0]) - 1
+        t = toks[1]
+        dvr_type[d] = t
+        if t == "gwp" and len(toks) == 2:
+            ngp[d], dvrpar[d] = 101, (-10.0, 10.0)
+        else:
+            ngp[d] = int(toks[2])
+            dvrpar[d] = (_read_float(toks[3]), _read_float(toks[4]))
+    hfile = kw.get("hamiltonian")
+    if not hfile:
+        raise ModelError("Input error: Hamiltonian file not given")
+    hpath = os.path.join(base, hfile)
+    if not os.path.exists(hpath):
+        # the reference lower-cases input values (input.f90:145-147)
+        raise ModelError(f"Operator file, {hfile} not found")
+    with open(hpath) as fh:
+        terms = parse_operator_file(fh.read(), nstates)
+    model = Model(nstates=nstates, mode_dofs=mode_dofs, multiset=multiset, nspf=nspf,
+                  dvr_type=dvr_type, ngp=ngp, dvrpar=dvrpar, terms=terms,
+                  label=os.path.basename(path))
+    if "tinit" in kw:
+        model.tinit = _read_float(kw["tinit"]) / AU2FS
+    if "tfinal" in kw:
+        model.tfinal = _read_float(kw["tfinal"]) / AU2FS
+    if "tout" in kw:
+        model.tout = _read_float(kw["tout"]) / AU2FS
+    for k_in, attr in (("eps_rho", "eps_rho"), ("eps_c", "eps_C"), ("eps_int", "eps_int"),
+                       ("eps_s", "eps_ovl")):
+        if k_in in kw:
+            setattr(model, attr, _read_float(kw[k_in]))
+    if "minstep" in kw:
+        model.min_stepsize = _read_float(kw["minstep"]) / AU2FS
+    if "relaxation" in flags:
+        model.relaxation = True
+        model.inorm_psi = 2
+    if "normalize" in kw:
+        model.inorm_psi = int(kw["normalize"])
+    integ = kw.get("integration", "rk45")
+    if integ == "rk45":
+        model.int_type = INT_RK45
+    elif integ == "dopri":
+        model.int_type = INT_DOPRI
+    elif integ.startswith("cmf2"):
+        model.int_type = INT_CMF2
+        a_name, a_eps = cmf_lines[0].split()[:2]
+        p_name, p_eps = cmf_lines[1].split()[:2]
+        if a_name.lower() != "lanczos":
+            raise ModelError("only Lanczos is supported for the A coefficients in CMF2")
+        model.eps_A = _read_float(a_eps)
+        model.int_type_psi = {"rk45": 1, "dopri": 2}[p_name.lower()]
+        model.eps_psi = _read_float(p_eps)
+    else:
+        raise ModelError(f"unknown integrator: {integ}")
+    # INIT-WF single-conf
+    if not init_lines or init_lines[0] != "single-conf":
+        raise ModelError("only the single-conf INIT-WF block is supported")
+    mm = re.match(r"el\s+(\d+)", init_lines[1])
+    if not mm:
+        raise ModelError("INIT-WF: expecting 'el <state>'")
+    model.init_state = int(mm.group(1)) - 1
+    for ln in init_lines[2:]:
+        if "gauss" in ln:
+            k, rest = ln.split("gauss", 1)
+            x0, p0, dx = [_read_float(v) for v in rest.split()[:3]]
+            model.init_spf[int(k) - 1] = ("gauss", (x0, p0, dx))
+        elif "gwp" in ln:
+            k, rest = ln.split("gwp", 1)
+            toks = rest.split()
+            dist, x0, p0, dx = int(toks[0]), _read_float(toks[1]), _read_float(toks[2]), _read_float(toks[3])
+            ovl = 0.7
+            scw = 1.0
+            mo = re.search(r"ovl\s*=\s*([-+0-9.eEdD]+)", rest)
+            if mo:
+                ovl = _read_float(mo.group(1))
+            ms = re.search(r"scw\s*=\s*([-+0-9.eEdD]+)", rest)
+            if ms:
+                scw = _read_float(ms.group(1))
+            model.init_spf[int(k) - 1] = ("gwp", (dist, x0, p0, dx, ovl, scw))
+        else:
+            raise ModelError(f"The chosen initial SPF is unknown: {ln}")
+    return model.finalize()

@@ -1,0 +1,990 @@
+"""CPU oracle: a NumPy restatement of the reference's G-MCTDH EOM + integrator path.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; only
+``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+use it, and only as the checker / CPU reference arm.
+
+PARITY STATUS: unpinned against the reference binary.  The reference is Fortran
+(no Fortran compiler exists in this build environment) and ships no tests or
+golden outputs, so this restatement is pinned instead against physics
+known-answer tests in ``tests/test_oracle.py`` (analytic autocorrelation of a
+displaced harmonic oscillator, the exact limit n_SPF = n_grid against direct
+propagation, norm and energy conservation, Hermiticity).
+
+Each routine follows the reference routine it names, in FP64, with the same
+regularisations and control arithmetic:
+
+  Calc_Derivs      derivatives.f90:39-237
+  Calc_MeanField   gmctdh_objects.f90:481-604   (Hamiltonian part, term by term)
+  Calc_rho1mode    gmctdh_objects.f90:408-477
+  Calc_rhom1MF     gmctdh_objects.f90:1147-1194
+  Calc_h1mode      hamilton.f90:416-531, MultTens* :577-661
+  StdRegInv/Sol    maths.f90:8-162;  InverseSquareRoot(U) maths.f90:588-644
+  Calc_S00/S00m1   gmctdh_objects.f90:323-404;  Calc_CY :1198-1333
+  GauInt1D         hamilton.f90:745-849;  Gau10Int1D :853-902;  GauOvlMultiD gmctdh_objects.f90:1497-1519
+  norm_wf/WF_Ovl   gmctdh_objects.f90:21-180;  DeltaPsi :206-275
+  rkqs/rkck/rkdp   integrator.f90:36-221
+  cmf2, A_to_B/B_to_A, propagate_SPF   cmf2_base.f90:47-345
+  Lanczos, rk_SPF_ck                    cmf2_integration.f90:30-253
+  Calc_DHD_B, Calc_Der_SPF, Calc_Err_SPF cmf2_derivatives.f90:1-338;  Calc_DHD hamilton.f90:535-574
+  propagate_wf     propagator.f90:87-146, :257-306;  observables output.f90:35-87, :144-150
+
+The reference works on complex-conjugated coefficient vectors so that BLAS
+right-multiplications give the wanted left mode products (e.g.
+gmctdh_objects.f90:531-532, :544).  The restatement uses the equivalent
+left mode products on the unconjugated tensors; every conjugation pair of the
+reference cancels exactly, so the arithmetic is the same up to rounding.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from macaw_gb300.model import Model, AU2FS, INT_RK45, INT_DOPRI, INT_CMF2
+
+_EPS = np.finfo(np.float64).eps
+
+# Cash-Karp tableau (integrator.f90:107-121, cmf2_integration.f90:122-133)
+CK = dict(
+    A=(0.0, 0.2, 0.3, 0.6, 1.0, 0.875),
+    B=((), (0.2,), (0.075, 0.225), (0.3, -0.9, 1.2),
+       (-11.0 / 54.0, 2.5, -70.0 / 27.0, 35.0 / 27.0),
+       (1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0)),
+    C=(37.0 / 378.0, 0.0, 250.0 / 621.0, 125.0 / 594.0, 0.0, 512.0 / 1771.0),
+    D=(2825.0 / 27648.0, 0.0, 18575.0 / 48384.0, 13525.0 / 55296.0, 277.0 / 14336.0, 0.25),
+)
+# Dormand-Prince tableau (integrator.f90:171-185)
+DP = dict(
+    A=(0.0, 0.2, 0.3, 0.8, 8.0 / 9.0, 1.0, 1.0),
+    B=((), (0.2,), (0.075, 0.225), (44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0),
+       (19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0),
+       (9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0)),
+    C=(35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0),
+    D=(5179.0 / 57600.0, 0.0, 7571.0 / 16695.0, 393.0 / 640.0, -92097.0 / 339200.0, 187.0 / 2100.0, 0.025),
+)
+RK_SAFETY, RK_PGROW, RK_PSHRNK, RK_MINSCAL, RK_MAXSCAL = 0.9, -0.2, -0.25, 0.1, 5.0
+RK_ERRCON = (5.0 / RK_SAFETY) ** (1.0 / RK_PGROW)
+EPS_B = 1e-8          # cmf2_integration.f90:13
+NKRYLOV_MAX = 20      # cmf2_integration.f90:11
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+# ----------------------------------------------------------------------------
+# Small dense helpers
+# ----------------------------------------------------------------------------
+
+def mode_product(M: np.ndarray, X: np.ndarray, m: int) -> np.ndarray:
+    """Y(..., j', ...) = sum_j M(j', j) X(..., j, ...) along axis m."""
+    return np.moveaxis(np.tensordot(M, X, axes=([1], [m])), 0, m)
+
+
+def hole_contract(X: np.ndarray, Y: np.ndarray, m: int) -> np.ndarray:
+    """C(j1, j2) = sum_{other indices} conj(X(.., j1, ..)) Y(.., j2, ..)."""
+    axes = [k for k in range(X.ndim) if k != m]
+    return np.tensordot(X.conj(), Y, axes=(axes, axes))
+
+
+def herm_from_upper(U: np.ndarray) -> np.ndarray:
+    """Full Hermitian matrix from the upper triangle (how zhemm/zheev 'U' read it)."""
+    return np.triu(U) + np.triu(U, 1).conj().T
+
+
+def std_reg_inv(Amat: np.ndarray, eps: float, regtype: str) -> np.ndarray:
+    """StdRegInv (maths.f90:8-83): eigen-decomposition + regularised inverse."""
+    w, U = np.linalg.eigh(herm_from_upper(Amat), UPLO="U")
+    if regtype == "tikh":
+        w = w / (w ** 2 + eps ** 2)
+    elif regtype == "tik2":
+        w2e2 = w ** 2 + eps ** 2
+        w = w * (w2e2 + eps ** 2) / w2e2 ** 2
+    elif regtype == "poly":
+        w = np.where(w < eps, 0.5 * (eps + w ** 2 / eps), w)
+        w = 1.0 / w
+    elif regtype == "expo":
+        ew = eps * np.exp(-(w / eps) ** 2)
+        w = w / (w ** 2 + ew ** 2)
+    elif regtype == "strd":
+        w = np.where(w < eps * 64.0, w + eps * np.exp(-w / eps), w)
+        w = 1.0 / w
+    else:
+        raise OracleError(f"no regularization type {regtype}")
+    return (U * w) @ U.conj().T
+
+
+def std_reg_sol(Amat: np.ndarray, Y: np.ndarray, eps: float, regtype: str) -> np.ndarray:
+    """StdRegSol (maths.f90:87-162)."""
+    w, U = np.linalg.eigh(herm_from_upper(Amat), UPLO="U")
+    uy = U.conj().T @ Y
+    if regtype == "tikh":
+        uy = uy * w / (w ** 2 + eps ** 2)
+    elif regtype == "poly":
+        uy = np.where(w < eps, uy * 2 * eps / (eps ** 2 + w ** 2), uy / w)
+    else:
+        raise OracleError(f"regularization {regtype} not restated")
+    return U @ uy
+
+
+def inverse_square_root(Amat: np.ndarray, eps: float) -> np.ndarray:
+    """InverseSquareRoot (maths.f90:588-618)."""
+    w, U = np.linalg.eigh(herm_from_upper(Amat), UPLO="U")
+    f = np.sqrt(w / (w ** 2 + eps ** 2))
+    return (U * f) @ U.conj().T
+
+
+def inverse_square_root_u(Amat: np.ndarray) -> np.ndarray:
+    """InverseSquareRootU (maths.f90:621-644): inverse of the upper Cholesky factor."""
+    Lc = np.linalg.cholesky(herm_from_upper(Amat))   # A = L L^H, U = L^H
+    Uc = Lc.conj().T
+    return np.triu(np.linalg.inv(Uc))
+
+
+# ----------------------------------------------------------------------------
+# Gaussian integrals (hamilton.f90:745-902, gmctdh_objects.f90:1476-1519)
+# ----------------------------------------------------------------------------
+
+# T(k, n) = Binomial(n, 2k) * (2k-1)!!  (hamilton.f90:761-785)
+def _coeff_table():
+    T = np.zeros((11, 21))
+    for n in range(21):
+        for k in range(0, n // 2 + 1):
+            df = 1
+            for x in range(2 * k - 1, 0, -2):
+                df *= x
+            T[k, n] = math.comb(n, 2 * k) * df
+    return T
+
+
+GAU_COEFF = _coeff_table()
+
+
+def gau_int_1d(a1: float, a2: float, xi1: complex, xi2: complex, iop: int) -> complex:
+    """<g1|op|g2>/<g1|g2> for g = exp(a x^2 + xi x) (GauInt1D, hamilton.f90:745-849)."""
+    xi1c = np.conj(xi1)
+    if iop == 0:
+        return 1.0 + 0j
+    if iop == -1:
+        return -1j * (a1 * xi2 - a2 * xi1c) / (a1 + a2)
+    if iop == -2:
+        a12 = a1 + a2
+        return ((a2 * xi1c - a1 * xi2) / a12) ** 2 + 2.0 * a1 * a2 / a12
+    if iop == -3:
+        g = a1 ** 2 - a2 ** 2 + (a2 * xi1c - a1 * xi2) * (xi1c + xi2)
+        return -1j * g / (a1 + a2) ** 2
+    if iop == 1:
+        return (xi1c + xi2) / (-2.0 * (a1 + a2))
+    if iop == 2:
+        a12 = 2.0 * (a1 + a2)
+        return ((xi1c + xi2) / a12) ** 2 - 1.0 / a12
+    if 3 <= iop <= 19 and iop % 2 == 1:
+        g = 0j
+        c1 = xi1c + xi2
+        a12 = -2.0 * (a1 + a2)
+        for k in range(0, iop // 2 + 1):
+            g = g + GAU_COEFF[k, iop] / a12 ** (iop - k) * c1 ** (iop - k - k)
+        return g
+    if 4 <= iop <= 20 and iop % 2 == 0:
+        g = 0j
+        a12 = -2.0 * (a1 + a2)
+        c2 = (xi1c + xi2) ** 2 / a12
+        c1 = 1.0 + 0j
+        for k in range(iop // 2, -1, -1):
+            g = g + GAU_COEFF[k, iop] * c1
+            c1 = c1 * c2
+        return g / a12 ** (iop // 2)
+    raise OracleError(f"GauInt1D operator {iop} not restated")
+
+
+def gau10_int_1d(a1: float, a2: float, xi1: complex, xi2: complex, iop: int) -> complex:
+    """<dg1/dxi1|op|g2>/<g1|g2> (Gau10Int1D, hamilton.f90:853-902)."""
+    if iop == -1:
+        return -1j * xi2 * gau_int_1d(a1, a2, xi1, xi2, 1) - 2j * a2 * gau_int_1d(a1, a2, xi1, xi2, 2)
+    if iop == -2:
+        return ((a2 + a2 + xi2 ** 2) * gau_int_1d(a1, a2, xi1, xi2, 1)
+                + 4.0 * a2 * xi2 * gau_int_1d(a1, a2, xi1, xi2, 2)
+                + 4.0 * a2 ** 2 * gau_int_1d(a1, a2, xi1, xi2, 3))
+    if iop == -3:
+        return -1j * (gau_int_1d(a1, a2, xi1, xi2, 1) + 2.0 * xi2 * gau_int_1d(a1, a2, xi1, xi2, 2)
+                      + 4.0 * a2 * gau_int_1d(a1, a2, xi1, xi2, 3))
+    if 0 <= iop <= 19:
+        return gau_int_1d(a1, a2, xi1, xi2, iop + 1)
+    raise OracleError(f"Gau10Int1D operator {iop} not restated")
+
+
+def gau_ovl_multid(a1: np.ndarray, a2: np.ndarray, xi1: np.ndarray, xi2: np.ndarray) -> complex:
+    """Overlap of normalised multi-D Gaussians (GauOvlMultiD, gmctdh_objects.f90:1497-1519)."""
+    if np.all(np.abs(a1 - a2) < _EPS):
+        c = np.sum((xi1.real ** 2 + xi2.real ** 2 - 0.5 * (xi1.conj() + xi2) ** 2) / a1)
+        return complex(np.exp(0.25 * c))
+    c = np.sum(xi1.real ** 2 / a1 + xi2.real ** 2 / a2 - (xi1.conj() + xi2) ** 2 / (a1 + a2))
+    d = math.sqrt(float(np.prod(4 * a1 * a2 / (a1 + a2) ** 2)))
+    return complex(np.exp(0.25 * c) * math.sqrt(d))
+
+
+# ----------------------------------------------------------------------------
+# The oracle proper
+# ----------------------------------------------------------------------------
+
+class Oracle:
+    """Stateful like the reference's modules: h1mode, rho, MeanField, rhom1MF,
+    S00, ... are recomputed by the same calls in the same order."""
+
+    def __init__(self, model: Model):
+        self.m = model
+        self.eom_calls = 0
+        self.hb_calls = 0
+
+    # ---------------- SPF-side objects ----------------
+    def apply_oper(self, mode: int, k: int, phi: np.ndarray) -> np.ndarray:
+        """Apply operator k of DVR mode `mode` to a (G, n) SPF block
+        (hamilton.f90:447-471, MultTens/MultTensDiag :577-629)."""
+        md = self.m
+        dofs = md.mode_dofs[mode]
+        _, _, dops = md.oper[mode][k]
+        n = phi.shape[1]
+        shape = tuple(md.ngp[d] for d in dofs) + (n,)
+        X = phi.reshape(shape, order="F")
+        for kk, d in enumerate(dofs):
+            code = dops[kk]
+            if code == 0:
+                continue
+            kind, M = md.dof_op_matrix(d, code)
+            if kind == "dense":
+                # psi(.., g, ..) <- sum_g' psi(.., g', ..) M(g', g)   (zlacrm from the right)
+                X = mode_product(M.T, X, kk)
+            else:
+                sh = [1] * len(shape)
+                sh[kk] = md.ngp[d]
+                X = X * M.reshape(sh)
+        return X.reshape((-1, n), order="F")
+
+    def gwp_params(self, psi: np.ndarray, i: int, s: int):
+        md = self.m
+        m = md.modes_gwp[i]
+        nmd = len(md.mode_dofs[m])
+        ns = int(md.nspf[m, s])
+        xi = md.spf_block(psi, m, s)          # (nmd, ns)
+        a = md.gwpa[:nmd, :ns, i]             # (nmd, ns)
+        return xi, a
+
+    def calc_s00(self, psi: np.ndarray, i: int):
+        """Calc_S00 (gmctdh_objects.f90:323-381): full matrices S00[i][s1][s2]."""
+        md = self.m
+        m = md.modes_gwp[i]
+        S = self.S00.setdefault(i, {})
+        states = range(md.nstates) if md.multiset[m] else [0]
+        for s in states:
+            xi, a = self.gwp_params(psi, i, s)
+            ns = xi.shape[1]
+            M = np.eye(ns, dtype=np.complex128)
+            for j1 in range(ns):
+                for j2 in range(j1 + 1, ns):
+                    M[j1, j2] = gau_ovl_multid(a[:, j1], a[:, j2], xi[:, j1], xi[:, j2])
+                    M[j2, j1] = np.conj(M[j1, j2])
+            S[(s, s)] = M
+        if not md.multiset[m]:
+            return
+        for s2 in range(md.nstates):
+            for s1 in range(s2):
+                xi1, a1 = self.gwp_params(psi, i, s1)
+                xi2, a2 = self.gwp_params(psi, i, s2)
+                M = np.zeros((xi1.shape[1], xi2.shape[1]), dtype=np.complex128)
+                for j1 in range(xi1.shape[1]):
+                    for j2 in range(xi2.shape[1]):
+                        M[j1, j2] = gau_ovl_multid(a1[:, j1], md.gwpa[:len(xi2), j2, i], xi1[:, j1], xi2[:, j2])
+                S[(s1, s2)] = M
+                S[(s2, s1)] = M.conj().T
+
+    def s00(self, i: int, s1: int, s2: int) -> np.ndarray:
+        m = self.m.modes_gwp[i]
+        if not self.m.multiset[m]:
+            s1 = s2 = 0
+        return self.S00[i][(s1, s2)]
+
+    def calc_s00m1(self, i: int):
+        """Calc_S00m1 (gmctdh_objects.f90:385-404): Tikhonov inverse of S."""
+        md = self.m
+        m = md.modes_gwp[i]
+        states = range(md.nstates) if md.multiset[m] else [0]
+        for s in states:
+            self.S00m1[(i, s)] = std_reg_inv(self.S00[i][(s, s)], md.eps_ovl, "tikh")
+
+    def calc_h1mode(self, psi: np.ndarray, mode: int):
+        """Calc_h1mode (hamilton.f90:416-531).  Same-state matrices are the
+        Hermitian part 1/2 (phi^H op phi + (op phi)^H phi) as zher2k builds them."""
+        md = self.m
+        hm = self.h1mode.setdefault(mode, {})
+        if not md.is_gwp_mode[mode]:
+            for k, (l, r, dops) in enumerate(md.oper[mode]):
+                if md.is_identity[mode, k]:
+                    hm[k] = np.eye(int(md.nspf[mode, l]), dtype=np.complex128)
+                    continue
+                phi2 = md.spf_block(psi, mode, r)
+                ophi = self.apply_oper(mode, k, phi2)
+                if l == r:
+                    X = phi2.conj().T @ ophi
+                    hm[k] = 0.5 * (X + X.conj().T)
+                else:
+                    phi1 = md.spf_block(psi, mode, l)
+                    hm[k] = phi1.conj().T @ ophi
+        else:
+            i = md.modes_gwp.index(mode)
+            for k, (l, r, dops) in enumerate(md.oper[mode]):
+                if md.is_identity[mode, k]:
+                    hm[k] = self.s00(i, l, r).copy()
+                    continue
+                xi1, a1 = self.gwp_params(psi, i, l)
+                xi2, a2 = self.gwp_params(psi, i, r)
+                n1, n2 = xi1.shape[1], xi2.shape[1]
+                S = self.s00(i, l, r)
+                H = np.zeros((n1, n2), dtype=np.complex128)
+                for j2 in range(n2):
+                    for j1 in range(n1):
+                        if l == r and j1 > j2:
+                            continue
+                        g = 1.0 + 0j
+                        for kk in range(len(dops)):
+                            g *= gau_int_1d(a1[kk, j1], a2[kk, j2], xi1[kk, j1], xi2[kk, j2], dops[kk])
+                        H[j1, j2] = S[j1, j2] * g
+                hm[k] = herm_from_upper(H) if l == r else H
+
+    # ---------------- A-side objects ----------------
+    def calc_rho1mode(self, mode: int, A: np.ndarray):
+        """Calc_rho1mode (gmctdh_objects.f90:408-477)."""
+        md = self.m
+        for s in range(md.nstates):
+            X = md.a_state(A, s)
+            Y = X
+            for i, m2 in enumerate(md.modes_gwp):
+                if m2 == mode:
+                    continue
+                Y = mode_product(self.s00(i, s, s), Y, m2)
+            R = hole_contract(Y, X, mode)
+            self.rho[(mode, s)] = 0.5 * (R + R.conj().T)
+        if not md.multiset[mode]:
+            ra = self.rho[(mode, 0)].copy()
+            for s in range(1, md.nstates):
+                ra = ra + self.rho[(mode, s)]
+            self.rho_ave[mode] = ra
+
+    def calc_meanfield(self, A: np.ndarray, t: float):
+        """Hamiltonian part of Calc_MeanField (gmctdh_objects.f90:513-604).
+
+        Returns Adot = f * H A (the reference stores its complex conjugate in
+        Adot_tmp) and sets self.MF[(mode, op)] and self.energyMF."""
+        md = self.m
+        f = md.nmodes
+        self.MF = {}
+        adot = np.zeros(md.naconftot, dtype=np.complex128)
+        energy = 0.0
+        for t_ in range(md.nham):
+            s1, s2 = int(md.lhs_el[t_]), int(md.rhs_el[t_])
+            ae = md.ae[t_]
+            # right chain: H_f x A, H_(f-1) x H_f x A, ...   (:527-550)
+            R = [md.a_state(A, s2)]
+            for im in range(f):
+                jm = f - 1 - im
+                if md.skip_term[jm, t_]:
+                    R.append(R[-1])
+                    continue
+                h = self.h1mode[jm][int(md.ioper[jm, t_])]
+                R.append(mode_product(h, R[-1], jm))
+            # left chain: A x H_1, A x H_1 x H_2, ...   (:552-573)
+            L = [md.a_state(A, s1)]
+            for im in range(f - 1):
+                if md.skip_term[im, t_]:
+                    L.append(L[-1])
+                    continue
+                h = self.h1mode[im][int(md.ioper[im, t_])]
+                L.append(mode_product(h.conj().T, L[-1], im))
+            o1 = int(md.astate_offset[s1])
+            n1 = int(md.naconf[s1])
+            Rf = R[f].reshape(-1, order="F")
+            adot[o1:o1 + n1] += md.der_factor * ae * Rf                      # :578
+            energy += float((ae * np.vdot(A[o1:o1 + n1], Rf)).real)          # :580
+            for im in range(f):                                               # :582-601
+                k = int(md.ioper[im, t_])
+                if md.is_identity[im, k]:
+                    continue
+                C = hole_contract(L[im], R[f - 1 - im], im)
+                key = (im, k)
+                self.MF[key] = self.MF.get(key, 0) + ae * C
+        self.energyMF = energy
+        return adot
+
+    def calc_rhom1mf(self):
+        """Calc_rhom1MF (gmctdh_objects.f90:1147-1194) with 'poly' regularisation."""
+        md = self.m
+        self.rhom1MF = {}
+        for mode in md.modes_dvr:
+            if md.multiset[mode]:
+                for s in range(md.nstates):
+                    rinv = std_reg_inv(self.rho[(mode, s)], md.eps_rho, "poly")
+                    for k, (l, r, _) in enumerate(md.oper[mode]):
+                        if l != s or md.is_identity[mode, k]:
+                            continue
+                        self.rhom1MF[(mode, k)] = rinv @ self.MF.get((mode, k), np.zeros((rinv.shape[0], int(md.nspf[mode, r])), np.complex128))
+            else:
+                rinv = std_reg_inv(self.rho_ave[mode], md.eps_rho, "poly")
+                for k in range(len(md.oper[mode])):
+                    if md.is_identity[mode, k]:
+                        continue
+                    self.rhom1MF[(mode, k)] = rinv @ self.MF.get((mode, k), np.zeros_like(rinv))
+
+    def dvr_spf_derivative(self, psi: np.ndarray, mode: int, dpsi: np.ndarray):
+        """DVR SPF derivative with the (1 - P) projector (derivatives.f90:96-153,
+        cmf2_derivatives.f90:118-173)."""
+        md = self.m
+        G = md.ngpm[mode]
+        acc: Dict[int, np.ndarray] = {}
+        for k, (l, r, _) in enumerate(md.oper[mode]):
+            if md.is_identity[mode, k]:
+                continue
+            ophi = self.apply_oper(mode, k, md.spf_block(psi, mode, r))
+            contrib = md.der_factor * (ophi @ self.rhom1MF[(mode, k)].T)
+            acc[l] = acc.get(l, 0) + contrib
+        states = range(md.nstates) if md.multiset[mode] else [0]
+        for s in states:
+            phi = md.spf_block(psi, mode, s)
+            n = phi.shape[1]
+            d = acc.get(s, np.zeros((G, n), np.complex128))
+            if not isinstance(d, np.ndarray):
+                d = np.zeros((G, n), np.complex128)
+            ovl = phi.conj().T @ phi
+            ovldot = phi.conj().T @ d
+            x = np.linalg.solve(herm_from_upper(np.triu(ovl)), ovldot)     # zposv 'U'
+            d = d - phi @ x
+            o = int(md.ipsispf[mode, s])
+            dpsi[o:o + G * n] = d.reshape(-1, order="F")
+
+    # ---------------- G-MCTDH block ----------------
+    def calc_cy(self, psi: np.ndarray, i: int):
+        """Calc_CY (gmctdh_objects.f90:1198-1333), without the D-matrix variant."""
+        md = self.m
+        mode = md.modes_gwp[i]
+        nmd = len(md.mode_dofs[mode])
+        states = range(md.nstates) if md.multiset[mode] else [0]
+        for s in states:
+            xi, a = self.gwp_params(psi, i, s)
+            ns = xi.shape[1]
+            S = self.s00(i, s, s)
+            gx = np.zeros((nmd, ns, ns), dtype=np.complex128)
+            for j2 in range(ns):
+                for j1 in range(j2 + 1):
+                    for k in range(nmd):
+                        gx[k, j1, j2] = gau_int_1d(a[k, j1], a[k, j2], xi[k, j1], xi[k, j2], 1)
+            nG = ns * nmd
+            Sa0 = np.zeros((nG, ns), dtype=np.complex128)
+            for j2 in range(ns):
+                for j1 in range(ns):
+                    for k in range(nmd):
+                        if j1 <= j2:
+                            Sa0[j1 * nmd + k, j2] = S[j1, j2] * gx[k, j1, j2]
+            for j2 in range(ns):
+                for j1 in range(ns):
+                    if j1 > j2:
+                        for k in range(nmd):
+                            Sa0[j1 * nmd + k, j2] = np.conj(Sa0[j2 * nmd + k, j1])
+            Sa0Sm1 = Sa0 @ self.S00m1[(i, s)]
+            self.Sa0Sm1[(i, s)] = Sa0Sm1
+            Sab = np.zeros((nG, nG), dtype=np.complex128)
+            for j2 in range(ns):
+                for k2 in range(nmd):
+                    for j1 in range(j2 + 1):
+                        for k1 in range(nmd):
+                            if k1 == k2:
+                                v = gau_int_1d(a[k1, j1], a[k2, j2], xi[k1, j1], xi[k2, j2], 2)
+                            else:
+                                v = gx[k1, j1, j2] * gx[k2, j1, j2]
+                            Sab[j1 * nmd + k1, j2 * nmd + k2] = S[j1, j2] * v
+            # zher2k('U','N', -1/2, Sa0S00m1, Sa0): only the upper triangle is meaningful
+            Sab = Sab - 0.5 * (Sa0Sm1 @ Sa0.conj().T + Sa0 @ Sa0Sm1.conj().T)
+            rho = self.rho[(mode, s)] if md.multiset[mode] else self.rho_ave[mode]
+            C = np.zeros((nG, nG), dtype=np.complex128)
+            for j2 in range(ns):
+                for j1 in range(j2 + 1):
+                    C[j1 * nmd:(j1 + 1) * nmd, j2 * nmd:(j2 + 1) * nmd] = \
+                        rho[j1, j2] * Sab[j1 * nmd:(j1 + 1) * nmd, j2 * nmd:(j2 + 1) * nmd]
+            self.Cmat[(i, s)] = np.triu(C)
+            Y = np.zeros(nG, dtype=np.complex128)
+            for k_op, (l, r, dops) in enumerate(md.oper[mode]):
+                if md.is_identity[mode, k_op]:
+                    continue
+                if md.multiset[mode] and l != s:
+                    continue
+                s2 = r
+                xi2, a2 = self.gwp_params(psi, i, s2)
+                ns2 = xi2.shape[1]
+                S12 = self.s00(i, s, s2)
+                Ha0 = np.zeros((nG, ns2), dtype=np.complex128)
+                for j2 in range(ns2):
+                    for j1 in range(ns):
+                        gi = np.array([gau_int_1d(a[k, j1], md.gwpa[k, j2, i], xi[k, j1], xi2[k, j2], dops[k])
+                                       for k in range(nmd)])
+                        for k in range(nmd):
+                            p = np.prod(gi[:k]) * np.prod(gi[k + 1:])
+                            Ha0[j1 * nmd + k, j2] = S12[j1, j2] * p * gau10_int_1d(
+                                a[k, j1], md.gwpa[k, j2, i], xi[k, j1], xi2[k, j2], dops[k])
+                h = self.h1mode[mode][k_op]
+                Ha0 = Ha0 - Sa0Sm1 @ h
+                MF = self.MF.get((mode, k_op), np.zeros((ns, ns2), np.complex128))
+                for j2 in range(ns2):
+                    for j1 in range(ns):
+                        Y[j1 * nmd:(j1 + 1) * nmd] += MF[j1, j2] * Ha0[j1 * nmd:(j1 + 1) * nmd, j2]
+            self.Yvec[(i, s)] = Y
+
+    # ---------------- Calc_Derivs ----------------
+    def _prepare(self, A: np.ndarray, psi: np.ndarray):
+        md = self.m
+        self.S00: Dict[int, Dict] = {}
+        self.S00m1: Dict = {}
+        self.Sa0Sm1: Dict = {}
+        self.Cmat: Dict = {}
+        self.Yvec: Dict = {}
+        self.h1mode: Dict[int, Dict[int, np.ndarray]] = {}
+        self.rho: Dict = {}
+        self.rho_ave: Dict = {}
+        for i in range(len(md.modes_gwp)):
+            self.calc_s00(psi, i)
+            self.calc_s00m1(i)
+        for mode in range(md.nmodes):
+            self.calc_rho1mode(mode, A)
+            self.calc_h1mode(psi, mode)
+
+    def calc_derivs(self, A: np.ndarray, psi: np.ndarray, t: float) -> Tuple[np.ndarray, np.ndarray]:
+        """Calc_Derivs (derivatives.f90:39-237) for npackets = 1."""
+        md = self.m
+        self.eom_calls += 1
+        self._prepare(A, psi)
+        adot = self.calc_meanfield(A, t)
+        self.calc_rhom1mf()
+        for i in range(len(md.modes_gwp)):
+            self.calc_cy(psi, i)
+        dpsi = np.zeros(md.dimpsi, dtype=np.complex128)
+        for mode in md.modes_dvr:
+            self.dvr_spf_derivative(psi, mode, dpsi)
+        if not md.modes_gwp:
+            return adot, dpsi
+        # Gaussian parameter derivatives (derivatives.f90:158-173)
+        for i, mode in enumerate(md.modes_gwp):
+            states = range(md.nstates) if md.multiset[mode] else [0]
+            for s in states:
+                x = std_reg_sol(self.Cmat[(i, s)], self.Yvec[(i, s)], md.eps_C, "tikh")
+                o = int(md.ipsispf[mode, s])
+                dpsi[o:o + len(x)] = md.der_factor * x
+        # S^-1 and tau on the coefficients (derivatives.f90:177-235)
+        dA = np.zeros_like(adot)
+        for s in range(md.nstates):
+            o = int(md.astate_offset[s])
+            n = int(md.naconf[s])
+            shape = tuple(int(x) for x in md.nspf[:, s])
+            X = adot[o:o + n].reshape(shape, order="F")
+            for i, mode in enumerate(md.modes_gwp):
+                js = s if md.multiset[mode] else 0
+                X = mode_product(self.S00m1[(i, js)], X, mode)
+            A0 = md.a_state(A, s)
+            for i, mode in enumerate(md.modes_gwp):
+                js = s if md.multiset[mode] else 0
+                nmd = len(md.mode_dofs[mode])
+                ns = int(md.nspf[mode, s])
+                Sa0Sm1 = self.Sa0Sm1[(i, js)]
+                op = int(md.ipsispf[mode, s])
+                dxi = dpsi[op:op + nmd * ns].reshape((nmd, ns), order="F")
+                xi = psi[op:op + nmd * ns].reshape((nmd, ns), order="F")
+                tau = np.zeros((ns, ns), dtype=np.complex128)
+                for j2 in range(ns):
+                    for j1 in range(ns):
+                        tau[j1, j2] = np.vdot(Sa0Sm1[j2 * nmd:(j2 + 1) * nmd, j1], dxi[:, j2])
+                for j2 in range(ns):
+                    dd = 0.0
+                    for k in range(nmd):
+                        dd += xi[k, j2].real * dxi[k, j2].real / md.gwpa[k, j2, i]
+                    tau[j2, j2] += dd * 0.5
+                X = X - mode_product(tau, A0, mode)
+            dA[o:o + n] = X.reshape(-1, order="F")
+        return dA, dpsi
+
+    # ---------------- norms and overlaps ----------------
+    def _spf_overlap(self, psi1: np.ndarray, psi2: np.ndarray, mode: int, s: int) -> np.ndarray:
+        md = self.m
+        if not md.is_gwp_mode[mode]:
+            return md.spf_block(psi1, mode, s).conj().T @ md.spf_block(psi2, mode, s)
+        i = md.modes_gwp.index(mode)
+        xi1, a = self.gwp_params(psi1, i, s)
+        xi2, _ = self.gwp_params(psi2, i, s)
+        ns = xi1.shape[1]
+        M = np.zeros((ns, ns), dtype=np.complex128)
+        for j1 in range(ns):
+            for j2 in range(ns):
+                M[j1, j2] = gau_ovl_multid(a[:, j1], a[:, j2], xi1[:, j1], xi2[:, j2])
+        return M
+
+    def norm_wf(self, A: np.ndarray, psi: np.ndarray) -> float:
+        """norm_wf (gmctdh_objects.f90:21-97)."""
+        md = self.m
+        tot = 0.0
+        for s in range(md.nstates):
+            X = md.a_state(A, s)
+            Y = X
+            for mode in md.modes_dvr + md.modes_gwp:
+                S = self._spf_overlap(psi, psi, mode, s)
+                if md.is_gwp_mode[mode]:
+                    S = herm_from_upper(np.triu(S, 1) + np.eye(S.shape[0]))
+                else:
+                    S = herm_from_upper(S)
+                Y = mode_product(S, Y, mode)
+            tot += float(np.vdot(X, Y).real)
+        return tot
+
+    def wf_ovl(self, A1, psi1, A2, psi2) -> complex:
+        """WF_Ovl (gmctdh_objects.f90:101-180): <Psi1|Psi2>."""
+        md = self.m
+        tot = 0j
+        for s in range(md.nstates):
+            Y = md.a_state(A2, s)
+            for mode in md.modes_dvr + md.modes_gwp:
+                Y = mode_product(self._spf_overlap(psi1, psi2, mode, s), Y, mode)
+            tot += complex(np.vdot(md.a_state(A1, s), Y))
+        return tot
+
+    def delta_psi(self, A1, psi1, A2, psi2) -> float:
+        """DeltaPsi (gmctdh_objects.f90:206-226), npackets = 1."""
+        o11 = self.norm_wf(A1, psi1)
+        o22 = self.norm_wf(A2, psi2)
+        o12 = self.wf_ovl(A1, psi1, A2, psi2)
+        return math.sqrt(abs(2.0 * (1.0 - o12.real / math.sqrt(o11 * o22))))
+
+    # ---------------- adaptive RK ----------------
+    def rk_attempt(self, A, psi, dA, dpsi, t, dt, method):
+        """rkck / rkdp (integrator.f90:95-221): 5th-order state and error state."""
+        tab = CK if method == INT_RK45 else DP
+        kA, kp = [dA], [dpsi]
+        nst = 6
+        for st in range(1, nst):
+            b = tab["B"][st]
+            At = A + dt * sum(b[j] * kA[j] for j in range(len(b)))
+            pt = psi + dt * sum(b[j] * kp[j] for j in range(len(b)))
+            a_, p_ = self.calc_derivs(At, pt, t + tab["A"][st] * dt)
+            kA.append(a_)
+            kp.append(p_)
+        C = tab["C"]
+        Atemp = A + dt * sum(C[j] * kA[j] for j in range(6) if C[j] != 0.0)
+        ptemp = psi + dt * sum(C[j] * kp[j] for j in range(6) if C[j] != 0.0)
+        D = tab["D"]
+        if method == INT_RK45:
+            Aerr = A + dt * sum(D[j] * kA[j] for j in range(6) if D[j] != 0.0)
+            perr = psi + dt * sum(D[j] * kp[j] for j in range(6) if D[j] != 0.0)
+            return Atemp, ptemp, Aerr, perr, None, None
+        a7, p7 = self.calc_derivs(Atemp, ptemp, t + dt)
+        kA.append(a7)
+        kp.append(p7)
+        Aerr = A + dt * sum(D[j] * kA[j] for j in range(7) if D[j] != 0.0)
+        perr = psi + dt * sum(D[j] * kp[j] for j in range(7) if D[j] != 0.0)
+        return Atemp, ptemp, Aerr, perr, a7, p7
+
+    def rk_fixed(self, A, psi, dA, dpsi, t, dt, method):
+        """One attempt of fixed length (step replay): (A, psi, dA_next, dpsi_next, errmax)."""
+        At, pt, Ae, pe, a7, p7 = self.rk_attempt(A, psi, dA, dpsi, t, dt, method)
+        errmax = self.delta_psi(At, pt, Ae, pe) / self.m.eps_int
+        return At, pt, a7, p7, errmax
+
+    def rkqs(self, A, psi, dA, dpsi, t, htry, method):
+        """rkqs (integrator.f90:36-91).  Returns (A, psi, dA, dpsi, hdid, hnext, attempts)."""
+        md = self.m
+        dt = htry
+        attempts = 0
+        while True:
+            attempts += 1
+            At, pt, Ae, pe, a7, p7 = self.rk_attempt(A, psi, dA, dpsi, t, dt, method)
+            errmax = self.delta_psi(At, pt, Ae, pe) / md.eps_int
+            if errmax < 1.0 or dt <= md.min_stepsize:
+                break
+            dt = max(RK_MINSCAL * dt, RK_SAFETY * dt * errmax ** RK_PSHRNK)
+            dt = max(dt, md.min_stepsize)
+        if errmax > RK_ERRCON:
+            hnext = RK_SAFETY * dt * errmax ** RK_PGROW
+        else:
+            hnext = dt * RK_MAXSCAL
+        hnext = max(hnext, md.min_stepsize)
+        hnext = min(hnext, md.tout)
+        if method == INT_DOPRI:
+            dA, dpsi = a7, p7
+        return At, pt, dA, dpsi, dt, hnext, attempts
+
+    # ---------------- CMF2 ----------------
+    def calc_dhd_b(self, B: np.ndarray) -> np.ndarray:
+        """Calc_DHD_B (cmf2_derivatives.f90:1-80): H_B * B (no der_factor)."""
+        md = self.m
+        self.hb_calls += 1
+        HB = np.zeros_like(B)
+        for t_ in range(md.nham):
+            s1, s2 = int(md.lhs_el[t_]), int(md.rhs_el[t_])
+            X = md.a_state(B, s2)
+            for mode in md.modes_dvr:
+                k = int(md.ioper[mode, t_])
+                if md.is_identity[mode, k]:
+                    continue
+                X = mode_product(self.h1mode[mode][k], X, mode)
+            for i, mode in enumerate(md.modes_gwp):
+                k = int(md.ioper[mode, t_])
+                if md.is_identity[mode, k]:
+                    continue
+                X = mode_product(self.dhd[(i, k)], X, mode)
+            o1 = int(md.astate_offset[s1])
+            HB[o1:o1 + int(md.naconf[s1])] += md.ae[t_] * X.reshape(-1, order="F")
+        return HB
+
+    def calc_dhd(self, DD: Dict):
+        """Calc_DHD (hamilton.f90:535-574): D^H h D for GWP modes."""
+        md = self.m
+        self.dhd = {}
+        for i, mode in enumerate(md.modes_gwp):
+            for k, (l, r, _) in enumerate(md.oper[mode]):
+                n1, n2 = int(md.nspf[mode, l]), int(md.nspf[mode, r])
+                if md.is_identity[mode, k]:
+                    self.dhd[(i, k)] = np.eye(n1, n2, dtype=np.complex128)
+                    continue
+                jl = l if md.multiset[mode] else 0
+                jr = r if md.multiset[mode] else 0
+                M = DD[(i, jl)].conj().T @ self.h1mode[mode][k] @ DD[(i, jr)]
+                if l == r:
+                    M = herm_from_upper(M)
+                M = np.where(np.abs(M) > _EPS, M, 0)
+                self.dhd[(i, k)] = M
+
+    def lanczos(self, B0: np.ndarray, dt: float, build: bool) -> np.ndarray:
+        """Lanczos (cmf2_integration.f90:30-103)."""
+        md = self.m
+        if build:
+            n = B0.shape[0]
+            BK = [B0 / np.linalg.norm(B0)]
+            alpha = np.zeros(NKRYLOV_MAX)
+            beta = np.zeros(NKRYLOV_MAX)
+            w = self.calc_dhd_b(BK[0])
+            alpha[0] = float(np.vdot(BK[0], w).real)
+            w = w - alpha[0] * BK[0]
+            beta[0] = np.linalg.norm(w)
+            BK.append(w / beta[0])
+            error = beta[0] * abs(dt)
+            j = 2
+            while True:
+                if j == NKRYLOV_MAX:
+                    raise OracleError("Maximum number of Krylov vectors reached")
+                w = self.calc_dhd_b(BK[j - 1])
+                alpha[j - 1] = float(np.vdot(BK[j - 1], w).real)
+                w = w - beta[j - 2] * BK[j - 2]
+                w = w - alpha[j - 1] * BK[j - 1]
+                beta[j - 1] = np.linalg.norm(w)
+                BK.append(w / beta[j - 1])
+                error = error * beta[j - 1] / float(j) * abs(dt)
+                if error < EPS_B:
+                    break
+                j += 1
+            nk = j
+            T = np.diag(alpha[:nk]) + np.diag(beta[:nk - 1], 1) + np.diag(beta[:nk - 1], -1)
+            ev, U = np.linalg.eigh(T)                                         # dstev('V')
+            self.lan_alpha = ev
+            self.lan_U = U
+            self.lan_BU = np.stack(BK[:nk], axis=1) @ U
+            self.lan_nk = nk
+        aux = self.lan_U[0, :] * np.exp(md.der_factor * self.lan_alpha * dt)
+        BT = self.lan_BU @ aux
+        return BT / np.linalg.norm(BT)
+
+    def calc_der_spf_dvr(self, psi: np.ndarray, mode: int) -> np.ndarray:
+        dpsi = np.zeros(self.m.dimpsi, dtype=np.complex128)
+        self.dvr_spf_derivative(psi, mode, dpsi)
+        return dpsi
+
+    def calc_err_spf_dvr(self, psi1, psi2, mode) -> float:
+        """Calc_Err_SPF, DVR branch (cmf2_derivatives.f90:239-283)."""
+        md = self.m
+        err = 0.0
+        states = range(md.nstates) if md.multiset[mode] else [0]
+        for s in states:
+            d = md.spf_block(psi1, mode, s) - md.spf_block(psi2, mode, s)
+            ovl = d.conj().T @ d
+            rho = self.rho[(mode, s)] if md.multiset[mode] else self.rho_ave[mode]
+            n = ovl.shape[0]
+            for j2 in range(n):
+                for j1 in range(j2):
+                    err += 2 * float((rho[j1, j2] * np.conj(ovl[j1, j2])).real)
+                err += float((rho[j2, j2] * ovl[j2, j2]).real)
+        return math.sqrt(abs(err))
+
+    def _spf_slices(self, mode):
+        md = self.m
+        states = range(md.nstates) if md.multiset[mode] else [0]
+        out = []
+        for s in states:
+            o = int(md.ipsispf[mode, s])
+            n = int(md.nspf[mode, s]) * md.ngpm[mode]
+            out.append(slice(o, o + n))
+        return out
+
+    def rk_spf_ck(self, psi: np.ndarray, mode: int, htry: float):
+        """rk_SPF_ck, DVR branch (cmf2_integration.f90:105-253)."""
+        md = self.m
+        sl = self._spf_slices(mode)
+        dt = htry
+        while True:
+            k = [self.calc_der_spf_dvr(psi, mode)]
+            for st in range(1, 6):
+                b = CK["B"][st]
+                pt = psi.copy()
+                for s_ in sl:
+                    pt[s_] = psi[s_] + dt * sum(b[j] * k[j][s_] for j in range(len(b)))
+                k.append(self.calc_der_spf_dvr(pt, mode))
+            ptemp = psi.copy()
+            perr = psi.copy()
+            for s_ in sl:
+                ptemp[s_] = psi[s_] + dt * (CK["C"][0] * k[0][s_] + CK["C"][2] * k[2][s_]
+                                            + CK["C"][3] * k[3][s_] + CK["C"][5] * k[5][s_])
+                perr[s_] = psi[s_] + dt * (CK["D"][0] * k[0][s_] + CK["D"][2] * k[2][s_]
+                                           + CK["D"][3] * k[3][s_] + CK["D"][4] * k[4][s_]
+                                           + CK["D"][5] * k[5][s_])
+            error = self.calc_err_spf_dvr(ptemp, perr, mode) / md.eps_psi
+            if error < 1.0:
+                break
+            dt = max(RK_MINSCAL * dt, RK_SAFETY * dt * error ** RK_PSHRNK)
+        if error > RK_ERRCON:
+            hnext = RK_SAFETY * dt * error ** RK_PGROW
+        else:
+            hnext = dt * RK_MAXSCAL
+        out = psi.copy()
+        for s_ in sl:
+            out[s_] = ptemp[s_]
+        return out, dt, hnext
+
+    def propagate_spf(self, dt: float, mode: int, psi: np.ndarray) -> np.ndarray:
+        """propagate_SPF (cmf2_base.f90:210-260), Cash-Karp branch."""
+        md = self.m
+        if md.int_type_psi != 1:
+            raise OracleError("only the Cash-Karp SPF integrator is restated")
+        done = 0.0
+        step = dt
+        while True:
+            psi, sdone, snext = self.rk_spf_ck(psi, mode, step)
+            done += sdone
+            if done >= dt:
+                break
+            snext = max(snext, md.min_stepsize * 2)
+            step = (dt - done) / (int((dt - done) / snext) + 1)
+            step = min(step, dt - done)
+        return psi
+
+    def _operators_and_mf(self, A, psi, t):
+        self._prepare(A, psi)
+        self.calc_meanfield(A, t)
+        self.calc_rhom1mf()
+
+    def cmf2_fixed(self, A, psi, t, h):
+        """One CMF2 attempt of length h completed as accepted (step replay)."""
+        return self.cmf2(A, psi, t, h, fixed=True)
+
+    def cmf2(self, A, psi, t, htry, fixed=False):
+        """cmf2 (cmf2_base.f90:47-206) for DVR-only models.  Returns (A, psi, hdid, hnext, tries);
+        with fixed=True one attempt of length htry is completed: (A, psi, error)."""
+        md = self.m
+        if md.modes_gwp:
+            raise OracleError("CMF2 with GWP modes is not restated")
+        hdid = htry
+        tries = 0
+        while True:
+            tries += 1
+            self._operators_and_mf(A, psi, t)
+            B0 = A.copy()
+            BHalf = self.lanczos(B0, 0.5 * hdid, True)
+            psiHalf = psi.copy()
+            for mode in md.modes_dvr:
+                psiHalf = self.propagate_spf(0.5 * hdid, mode, psiHalf)
+            AHalf = BHalf.copy()
+            self._operators_and_mf(AHalf, psiHalf, t + 0.5 * hdid)
+            psiHalf2 = psi.copy()
+            for mode in md.modes_dvr:
+                psiHalf2 = self.propagate_spf(0.5 * hdid, mode, psiHalf2)
+            err_psi = self.delta_psi(AHalf, psiHalf, AHalf, psiHalf2)
+            for mode in md.modes_dvr:
+                psiHalf2 = self.propagate_spf(0.5 * hdid, mode, psiHalf2)
+            self.h1mode = {}
+            for mode in range(md.nmodes):
+                self.calc_h1mode(psiHalf2, mode)
+            B02 = self.lanczos(BHalf, -0.5 * hdid, True)
+            err_A = np.linalg.norm(B02 - B0) * 0.5
+            error = max(err_A, err_psi) / md.eps_int
+            if fixed:
+                return self.lanczos(BHalf, 0.5 * hdid, False), psiHalf2, error
+            if error > 1.0:
+                hdid = hdid / math.sqrt(error) * 0.95
+                continue
+            Bend = self.lanczos(BHalf, 0.5 * hdid, False)
+            hnext = min(hdid / math.sqrt(error), hdid * 1.5) if error > 0 else hdid * 1.5
+            hnext = min(hnext, md.tout)
+            return Bend, psiHalf2, hdid, hnext, tries
+
+    # ---------------- observables and driver ----------------
+    def observables(self, A, psi, A0, psi0, t):
+        """WriteOutput quantities (output.f90:35-87, :144-150): populations from
+        rho of mode 1, energy = energyMF / sum(pop), norm = sum(pop), C(t)."""
+        md = self.m
+        self._prepare(A, psi)
+        self.calc_meanfield(A, t)
+        pop = np.zeros(md.nstates)
+        for s in range(md.nstates):
+            r = self.rho[(0, s)]
+            if md.is_gwp_mode[0]:
+                S = self.s00(0, s, s)
+                n = r.shape[0]
+                v = 0.0
+                for j2 in range(n):
+                    for j1 in range(j2):
+                        v += 2.0 * float((r[j1, j2] * S[j1, j2]).real)
+                    v += float((r[j2, j2] * S[j2, j2]).real)
+                pop[s] = v
+            else:
+                pop[s] = float(np.trace(r).real)
+        auto = self.wf_ovl(A0, psi0, A, psi)
+        return dict(t=t, pop=pop, norm=float(pop.sum()), energy=self.energyMF / pop.sum(), auto=auto)
+
+    def propagate(self, A, psi, tfinal: Optional[float] = None, max_steps: Optional[int] = None,
+                  record_steps: bool = False):
+        """propagate_wf (propagator.f90:87-146 RK, :257-306 CMF2).  Returns the list
+        of outputs written every tout and the step history."""
+        md = self.m
+        A = A.copy()
+        psi = psi.copy()
+        A0, psi0 = A.copy(), psi.copy()
+        tfin = md.tfinal if tfinal is None else tfinal
+        maxtime = tfin + md.tout * 0.1
+        t = md.tinit
+        step = md.tout * md.eps_int
+        outputs = []
+        steps = []
+        nsteps = 0
+        while t < maxtime:
+            outputs.append(self.observables(A, psi, A0, psi0, t))
+            tnext = t + md.tout
+            while True:
+                if md.int_type == INT_CMF2:
+                    A, psi, sdone, snext, tries = self.cmf2(A, psi, t, step)
+                else:
+                    if md.int_type == INT_RK45:
+                        dA, dpsi = self.calc_derivs(A, psi, t)
+                    else:
+                        raise OracleError("DOPRI driver needs the carried derivative; use rk45")
+                    A, psi, dA, dpsi, sdone, snext, tries = self.rkqs(A, psi, dA, dpsi, t, step, md.int_type)
+                if record_steps:
+                    steps.append((t, step, sdone, snext, tries))
+                t = t + sdone
+                nsteps += 1
+                if max_steps is not None and nsteps >= max_steps:
+                    return outputs, steps, (A, psi, t)
+                if t >= tnext - md.min_stepsize:
+                    break
+                q = int((tnext - t) / snext)
+                step = (tnext - t) if q == 0 else (tnext - t) / (q + 1)
+        return outputs, steps, (A, psi, t)

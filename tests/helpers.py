@@ -1,0 +1,36 @@
+"""Shared test helpers: small seeded models and random MCTDH states."""
+import numpy as np
+
+from macaw_gb300.generate import lvc5, qvc
+from macaw_gb300.model import initial_wavefunction, INT_CMF2, INT_RK45
+
+
+def small_lvc(nspf=3, grid=(12, 10, 11, 9, 10), eps_int=1e-7, tfinal_fs=2.0):
+    return lvc5(grid=list(grid), nspf=nspf, eps_int=eps_int, tfinal_fs=tfinal_fs)
+
+
+def small_qvc(nstates=3, ndof=4, grid=6, nspf=4, integrator=INT_CMF2, eps_int=1e-5, tfinal_fs=1.0, seed=7):
+    return qvc(nstates, ndof, grid, nspf, 2, seed, (200.0, 3500.0), (0.05, 0.2),
+               tuple(np.linspace(0.0, 0.7, nstates)), "qvc-small", integrator=integrator,
+               eps_int=eps_int, eps_lanczos=1e-8, eps_spf=1e-7, tfinal_fs=tfinal_fs)
+
+
+def random_state(model, seed=0, spread=1.0):
+    """Random normalised A and SPF blocks with orthonormal columns (per mode and state)."""
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=model.naconftot) + 1j * rng.normal(size=model.naconftot)
+    A *= spread
+    psi = np.zeros(model.dimpsi, dtype=np.complex128)
+    for m in range(model.nmodes):
+        for s in range(model.nstates):
+            if (not model.multiset[m]) and s > 0:
+                continue
+            G = model.ngpm[m]
+            n = int(model.nspf[m, s])
+            X = rng.normal(size=(G, n)) + 1j * rng.normal(size=(G, n))
+            q, _ = np.linalg.qr(X)
+            o = int(model.ipsispf[m, s])
+            psi[o:o + G * n] = q.reshape(-1, order="F")
+    from oracle.mctdh import Oracle
+    nrm = Oracle(model).norm_wf(A, psi)
+    return A / np.sqrt(nrm), psi

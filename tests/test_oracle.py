@@ -1,0 +1,176 @@
+"""Pins for the CPU oracle (no GPU).
+
+The reference ships no tests or golden outputs and cannot be compiled here (no
+Fortran compiler), so the oracle is pinned by physics known-answer tests:
+  * analytic autocorrelation of uncoupled displaced harmonic oscillators;
+  * the exact limit n_SPF = n_grid against direct propagation with expm;
+  * conservation of norm and energy, Hermiticity of rho and h1mode;
+  * the committed golden fixtures (tests/golden/make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg
+
+from macaw_gb300.model import (Model, Term, AU2FS, AU2EV, AU2CMM1, OP_DQ2, INT_RK45, initial_wavefunction,
+                               harm_dvr, parse_input)
+from macaw_gb300.generate import lvc5, write_inputs
+from oracle.mctdh import Oracle, std_reg_inv, herm_from_upper
+from tests.helpers import small_lvc, small_qvc, random_state
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _displaced_ho(omegas, kappas, nspf=4, grid=28, eps_int=1e-10, tfinal_fs=6.0):
+    terms = []
+    for k, (w, kap) in enumerate(zip(omegas, kappas)):
+        terms.append(Term(-0.5 * w + 0j, 0, 0, {k: OP_DQ2}))
+        terms.append(Term(0.5 * w + 0j, 0, 0, {k: 2}))
+        terms.append(Term(kap + 0j, 0, 0, {k: 1}))
+    f = len(omegas)
+    m = Model(nstates=1, mode_dofs=[[k] for k in range(f)], multiset=[True] * f,
+              nspf=np.full((f, 1), nspf), dvr_type=["HO"] * f, ngp=[grid] * f,
+              dvrpar=[(0.0, 1.0)] * f, terms=terms, tfinal=tfinal_fs / AU2FS, tout=1.0 / AU2FS,
+              eps_int=eps_int, int_type=INT_RK45, init_state=0, label="dho")
+    return m.finalize()
+
+
+def test_harmonic_dvr_spectrum():
+    g, w, d1, d2, xd1 = harm_dvr(30, 0.0, 1.0)
+    assert np.allclose(d2, d2.T) and np.allclose(d1, -d1.T)
+    ev = np.linalg.eigvalsh(-0.5 * d2 + np.diag(0.5 * g ** 2))
+    assert np.allclose(ev[:10], np.arange(10) + 0.5, atol=1e-10)
+    assert abs(np.sum(w * np.exp(-g ** 2)) - np.sqrt(np.pi)) < 1e-10
+
+
+def test_displaced_oscillators_analytic_autocorrelation():
+    omegas = np.array([1200.0, 2300.0]) / AU2CMM1
+    kappas = np.array([0.05, -0.08]) / AU2EV
+    model = _displaced_ho(omegas, kappas)
+    A, psi = initial_wavefunction(model)
+    outs, _, _ = Oracle(model).propagate(A, psi)
+    for o in outs:
+        t = o["t"]
+        c = 1.0 + 0j
+        for w, k in zip(omegas, kappas):
+            S = 0.5 * (k / w) ** 2
+            c *= np.exp(-1j * (0.5 * w - k * k / (2 * w)) * t) * np.exp(-S * (1 - np.exp(-1j * w * t)))
+        assert abs(o["auto"] - c) < 2e-7, (t * AU2FS, o["auto"], c)
+        assert abs(o["norm"] - 1.0) < 1e-8
+
+
+def _full_hamiltonian(model):
+    dims = [model.ngp[d] for d in range(model.ndof)]
+    nprim = int(np.prod(dims))
+    H = np.zeros((model.nstates * nprim, model.nstates * nprim), dtype=np.complex128)
+    for term in model.terms:
+        op = np.eye(1, dtype=np.complex128)
+        for d in reversed(range(model.ndof)):
+            code = term.dof_ops.get(d, 0)
+            if code == 0:
+                M = np.eye(dims[d])
+            else:
+                kind, mat = model.dof_op_matrix(d, code)
+                M = mat.T if kind == "dense" else np.diag(mat)
+            op = np.kron(op, M)
+        E = np.zeros((model.nstates, model.nstates))
+        E[term.lhs, term.rhs] = 1.0
+        H += term.coeff * np.kron(E, op)
+    return H
+
+
+def test_exact_limit_full_spf_basis():
+    """n_SPF = n_grid makes MCTDH exact: C(t) and populations match expm."""
+    from tests.helpers import small_qvc  # noqa
+    from macaw_gb300.generate import qvc
+    model = qvc(2, 2, 6, 6, 1, 11, (800.0, 2500.0), (0.1, 0.2), (0.0, 0.3), "exact", integrator=INT_RK45,
+                eps_int=1e-10, tfinal_fs=3.0)
+    # 1 DOF per mode: rebuild as two single-DOF modes with a full SPF basis
+    model = Model(nstates=2, mode_dofs=[[0], [1]], multiset=[True, True], nspf=np.full((2, 2), 6),
+                  dvr_type=["HO", "HO"], ngp=[6, 6], dvrpar=[(0.0, 1.0)] * 2, terms=model.terms,
+                  tfinal=3.0 / AU2FS, tout=0.5 / AU2FS, eps_int=1e-10, int_type=INT_RK45,
+                  init_state=1, label="exact").finalize()
+    A, psi = initial_wavefunction(model)
+    outs, _, _ = Oracle(model).propagate(A, psi)
+    H = _full_hamiltonian(model)
+    # the initial state on the primitive grid: A_{11} phi_1(q1) phi_1(q2) on state 2
+    phi1 = model.spf_block(psi, 0, 1)[:, 0]
+    phi2 = model.spf_block(psi, 1, 1)[:, 0]
+    nprim = 36
+    v0 = np.zeros(2 * nprim, dtype=np.complex128)
+    v0[nprim:] = np.kron(phi2, phi1)
+    for o in outs:
+        v = scipy.linalg.expm(-1j * H * o["t"]) @ v0
+        c = np.vdot(v0, v)
+        assert abs(o["auto"] - c) < 1e-7
+        pops = [np.linalg.norm(v[:nprim]) ** 2, np.linalg.norm(v[nprim:]) ** 2]
+        assert np.abs(o["pop"] - pops).max() < 1e-7
+
+
+def test_conservation_and_hermiticity():
+    model = small_lvc(eps_int=1e-9, tfinal_fs=2.0)
+    A, psi = initial_wavefunction(model)
+    o = Oracle(model)
+    outs, _, _ = o.propagate(A, psi)
+    e0 = outs[0]["energy"]
+    for r in outs:
+        assert abs(r["norm"] - 1.0) < 1e-7
+        assert abs(r["energy"] - e0) < 1e-8
+    A, psi = random_state(model, seed=3)
+    o.calc_derivs(A, psi, 0.0)
+    for (m, s), rho in o.rho.items():
+        assert np.allclose(rho, rho.conj().T, atol=1e-15)
+    for m, hm in o.h1mode.items():
+        for k, h in hm.items():
+            l, r, _ = model.oper[m][k]
+            if l == r:
+                assert np.allclose(h, h.conj().T, atol=1e-14)
+
+
+def test_regularised_inverse_poly():
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(5, 5)) + 1j * rng.normal(size=(5, 5))
+    rho = X @ X.conj().T
+    rho[:, -1] = 0
+    rho[-1, :] = 0
+    eps = 1e-8
+    inv = std_reg_inv(rho, eps, "poly")
+    w, U = np.linalg.eigh(rho)
+    assert np.allclose(inv @ U[:, 0], U[:, 0] / (0.5 * (eps + w[0] ** 2 / eps)), rtol=1e-6)
+    assert np.allclose(herm_from_upper(np.triu(rho)), rho)
+
+
+def test_parser_round_trip(tmp_path):
+    model = lvc5(grid=[12, 10, 11, 9, 10], nspf=3, eps_int=1e-7)
+    path = write_inputs(model, str(tmp_path), "lvc")
+    m2 = parse_input(path)
+    assert m2.nham == model.nham
+    assert np.array_equal(m2.nspf, model.nspf)
+    assert np.allclose(m2.ae, model.ae, rtol=1e-13)
+    A, psi = initial_wavefunction(model)
+    A2, psi2 = initial_wavefunction(m2)
+    assert np.allclose(A, A2) and np.allclose(psi, psi2)
+    d1 = Oracle(model).calc_derivs(A, psi, 0.0)
+    d2 = Oracle(m2).calc_derivs(A2, psi2, 0.0)
+    assert np.allclose(d1[0], d2[0], rtol=1e-12, atol=1e-15)
+
+
+def test_reference_example_is_parsed():
+    """The butadiene example grammar (SPF/GRID/INIT-WF blocks, S/M sets) parses up
+    to the features this core supports (interp splines are reported as unsupported)."""
+    from macaw_gb300.model import ModelError
+    ex = "/root/reference/Examples/Butadiene_5modes/but_5D.inp"
+    if not os.path.exists(ex):
+        pytest.skip("reference examples not present")
+    with pytest.raises(ModelError, match="interp|not implemented"):
+        parse_input(ex)
+
+
+@pytest.mark.parametrize("name", ["lvc_small", "qvc_small"])
+def test_golden_fixtures(name):
+    from tests.golden.make_golden import compute
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    cur = compute(name)
+    for key in g.files:
+        assert np.allclose(cur[key], g[key], rtol=1e-11, atol=1e-13), key
