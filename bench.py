@@ -1,0 +1,314 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the G-MCTDH propagation core on one GB300.
+
+Workload: the 3-state quadratic vibronic-coupling model over 12 DOFs combined
+pairwise into 6 logical modes of 20x20 harmonic DVR grids, 8 SPFs per mode and
+state (262,144 complex coefficients per state), propagated with the CMF2
+integrator and short-iterative Lanczos (seeded synthetic parameters,
+``macaw_gb300.generate.qvc12``).  A step is one accepted CMF2 step of the
+resident wavefunction; the metric is simulated femtoseconds per second of
+device time (EOM evaluations per second reported beside it).
+
+``--impl reference`` times the CPU oracle (the NumPy restatement of the
+reference's Fortran path) on the host cores instead.  Under torchrun every rank
+propagates an independent replica (the path has no data-parallel exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from macaw_gb300.model import AU2FS, INT_CMF2, initial_wavefunction  # noqa: E402
+from macaw_gb300.generate import qvc12  # noqa: E402
+
+METRIC = "simulated fs/s & EOM evals/s vs plain FP64 GPU path at |dC(t)|<=1e-6"
+WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/state, CMF2+Lanczos"
+EPS_CMF = 1e-5
+PRE_FS = 1.0
+REF_STEP_FS = 0.1   # CMF2 step length the reference arm times (steady-state steps are of this order)
+
+
+def make_model():
+    return qvc12(eps_int=EPS_CMF, eps_lanczos=1e-8, eps_spf=1e-7)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.idx = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl")
+        return ws, rank, tdist
+    return 1, 0, None
+
+
+def barrier(tdist):
+    if tdist is not None:
+        tdist.barrier()
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+def cpu_baseline(model, A, psi, h, budget_s=40.0):
+    """The oracle on a bounded sample: fixed-length CMF2 attempts of length h."""
+    from oracle.mctdh import Oracle
+    o = Oracle(model)
+    t0 = time.perf_counter()
+    n = 0
+    A_, p_ = A.copy(), psi.copy()
+    while True:
+        A_, p_, _ = o.cmf2_fixed(A_, p_, 0.0, h)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 3:
+            break
+    return dict(value=n * h * AU2FS / el, unit="fs/s", cores=os.cpu_count(), kind="port",
+                sample=f"{n} CMF2 step(s) of {h * AU2FS:.4f} fs on the full qvc12 model, NumPy oracle "
+                       f"(BLAS threads = host cores), {el:.1f} s")
+
+
+def run_reference(args):
+    ws, rank, tdist = dist_setup()
+    if rank != 0:
+        return 0
+    model = make_model()
+    A, psi = initial_wavefunction(model)
+    h = REF_STEP_FS / AU2FS
+    from oracle.mctdh import Oracle
+    o = Oracle(model)
+    # each step: one fixed-length CMF2 step of the oracle; bounded to a few minutes
+    t_total, fs_total, n = 0.0, 0.0, 0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        A, psi, _ = o.cmf2_fixed(A, psi, 0.0, h)
+        el = time.perf_counter() - t0
+        if i >= min(args.warmup, 1):
+            t_total += el
+            fs_total += h * AU2FS
+            n += 1
+        if t_total > 150.0 and n >= 1:
+            break
+    v = fs_total / t_total
+    line = {"metric": METRIC, "value": v, "unit": "fs/s", "n_gpus": ws, "steps": n, "warmup": min(args.warmup, 1),
+            "ms_per_step": 1e3 * t_total / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic (seeded qvc12 model)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "integrator": "cmf2", "step_fs": h * AU2FS},
+            "cpu_baseline": {"value": v, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{n} fixed CMF2 steps of {h * AU2FS} fs, NumPy oracle on host cores"},
+            "e2e": {"value": v, "unit": "fs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    from macaw_gb300.capi import GpuCore, fp64_peak_tflops
+    ws, rank, tdist = dist_setup()
+    torch.cuda.init()
+    model = make_model()
+    A0, psi0 = initial_wavefunction(model)
+    core = GpuCore(model, precision=0)
+    core.set_state(A0, psi0, as_start=True)
+    l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    # leave the start-up transient of the step control (the reference starts at
+    # tout * eps_int, propagator.f90:103, and grows by at most 1.5x per CMF2 step):
+    # propagate 1 fs untimed, then warm up and time steady-state steps
+    t, h, _, _, _ = core.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
+    for _ in range(args.warmup):
+        hdid, h, _ = core.step(INT_CMF2, t, h)
+        t += hdid
+    c0 = core.counters()
+    core.profile(2)
+    ms_total = 0.0
+    fs_total = 0.0
+    hdids = []
+    barrier(tdist)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            flush_l2(l2)
+            torch.cuda.synchronize()
+            core.event_record(0)
+            hdid, hnext, _ = core.step(INT_CMF2, t, h)
+            core.event_record(1)
+            ms_total += core.event_elapsed(0, 1)
+            t += hdid
+            h = hnext
+            fs_total += hdid * AU2FS
+            hdids.append(hdid * AU2FS)
+        torch.cuda.synchronize()
+    barrier(tdist)
+    prof = core.profile_read()
+    core.profile(0)
+    c1 = core.counters()
+    if tdist is not None:
+        tt = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    value = ws * fs_total / (ms_total * 1e-3)
+    eom_per_s = (c1["eom"] - c0["eom"]) / (ms_total * 1e-3)
+    hb_per_s = (c1["hb"] - c0["hb"]) / (ms_total * 1e-3)
+    launches = c1["launches"] - c0["launches"]
+
+    # e2e: the reference-facing host-buffer call (mctdh_cmf2) with pinned buffers,
+    # host<->device copies of A and psi inside every step
+    Ah, ph = core.get_state()
+    pA = torch.from_numpy(Ah.copy()).pin_memory()
+    pP = torch.from_numpy(ph.copy()).pin_memory()
+    import ctypes as C
+    DPp = C.POINTER(C.c_double)
+    hd, hn = C.c_double(), C.c_double()
+    e2e_fs, e2e_s = 0.0, 0.0
+    te, he = t, h
+    for _ in range(max(1, args.steps // 2)):
+        flush_l2(l2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = core.lib.mctdh_cmf2(core.h, C.cast(pA.data_ptr(), DPp), C.cast(pP.data_ptr(), DPp), te, he,
+                                 C.byref(hd), C.byref(hn))
+        e2e_s += time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(core.lib.mctdh_last_error(core.h).decode())
+        te += hd.value
+        he = hn.value
+        e2e_fs += hd.value * AU2FS
+    nbytes = 16 * (model.naconftot + model.dimpsi)
+
+    peaks, peak_src = load_peaks()
+    fp64_peak = fp64_peak_tflops()
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    dname, d = dom
+    avg_ms = d["ms"] / max(d["launches"], 1)
+    fl_launch = d["flops"] / max(d["launches"], 1)
+    by_launch = d["bytes"] / max(d["launches"], 1)
+    achieved_gbs = by_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    achieved_tf = fl_launch / (avg_ms * 1e-3) / 1e12 if avg_ms > 0 else 0.0
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded qvc12 model)",
+        "config": {"workload": WORKLOAD, "integrator": "cmf2", "precision": "fp64",
+                   "eps_cmf": EPS_CMF, "l2": "flushed (256 MB write) before every timed step",
+                   "step_fs_mean": statistics.mean(hdids), "parallelism": f"replicas x{ws}"},
+        "eom_per_s": eom_per_s, "hb_per_s": hb_per_s,
+        "e2e": {"value": e2e_fs / e2e_s, "unit": "fs/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peak_src},
+        "fp64_roofline": {"kernel": dname, "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                          "frac": achieved_tf / fp64_peak if fp64_peak > 0 else None,
+                          "peak_source": "measured FP64 FMA chain on this GPU"},
+        "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                               "share": round(v["ms"] / max(sum(x["ms"] for x in prof.values()), 1e-9), 4)}
+                           for k, v in prof.items() if v["launches"]},
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(model, A0, psi0, statistics.mean(hdids) / AU2FS)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    core.close()
+    if tdist is not None:
+        tdist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -111,6 +111,33 @@ int64_t mctdh_get_state(mctdh_ctx_t *ctx, double *A, double *psi);
 int64_t mctdh_propagate(mctdh_ctx_t *ctx, int64_t int_type, double tnext, double *t, double *step,
                         int64_t *nsteps, int64_t *nattempts, int64_t *neom);
 
+/* One accepted step on the resident state: the body of the inner loop of
+ * propagate_wf (propagator.f90:116-117 for rk45/dopri, :276 for cmf2), with the
+ * reference's retry logic inside.  int_type: 1 rk45, 2 dopri, 10 cmf2. */
+int64_t mctdh_step(mctdh_ctx_t *ctx, int64_t int_type, double t, double htry, double *hdid, double *hnext,
+                   int64_t *nattempts);
+
+/* Work counters: kernel launches, EOM evaluations (Calc_Derivs equivalents,
+ * including the mean-field evaluations of CMF2) and H_B * B products. */
+int64_t mctdh_counters(mctdh_ctx_t *ctx, int64_t *launches, int64_t *eom, int64_t *hb);
+
+/* Measured FP64 FMA throughput of the current device (TFLOP/s), the roofline
+ * denominator of the FP64 kernels. */
+int64_t mctdh_fp64_peak(double *tflops);
+
+/* CUDA events on the context's stream (slots 0..15) for device-side timing. */
+int64_t mctdh_event_record(mctdh_ctx_t *ctx, int64_t slot);
+int64_t mctdh_event_elapsed(mctdh_ctx_t *ctx, int64_t slot0, int64_t slot1, double *ms);
+
+/* Per-kernel-class timing (replaces the 8 timers of timingmod.f90:16-103 with
+ * CUDA events).  enable: 0 off, 1 on, 2 on and reset.  kid: 0 mode products,
+ * 1 single-hole contractions, 2 reductions, 3 h1mode/SPF operators, 4 regularised
+ * inverses, 5 term sums, 6 SPF derivatives, 7 elementwise.  flops/bytes are the
+ * algorithmic work of the timed launches. */
+int64_t mctdh_profile(mctdh_ctx_t *ctx, int64_t enable);
+int64_t mctdh_profile_read(mctdh_ctx_t *ctx, int64_t kid, double *ms, int64_t *launches, double *flops,
+                           double *bytes);
+
 /* Observables written by WriteOutput (output.f90:35-87, :144-150) for the
  * resident state: energyMF / sum(pop), state populations from rho of mode 1,
  * norm = sum(pop), and C(t) = <Psi(0)|Psi(t)>. */

@@ -76,12 +76,21 @@ def load_library() -> C.CDLL:
     lib.mctdh_norm_wf.argtypes = [vp, DP, DP, DP]
     lib.mctdh_wf_ovl.argtypes = [vp, DP, DP, DP, DP, DP, DP]
     lib.mctdh_launch_count.argtypes = [vp]
+    lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
+    lib.mctdh_event_record.argtypes = [vp, C.c_int64]
+    lib.mctdh_event_elapsed.argtypes = [vp, C.c_int64, C.c_int64, DP]
+    lib.mctdh_profile.argtypes = [vp, C.c_int64]
+    lib.mctdh_counters.argtypes = [vp, I64P, I64P, I64P]
+    lib.mctdh_fp64_peak.argtypes = [DP]
+    lib.mctdh_profile_read.argtypes = [vp, C.c_int64, DP, I64P, DP, DP]
     lib.mctdh_last_error.argtypes = [vp]
     lib.mctdh_last_error.restype = C.c_char_p
     for name in ("mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", "mctdh_cmf2",
                  "mctdh_rk_attempt", "mctdh_cmf2_attempt",
                  "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
-                 "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count"):
+                 "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_step",
+                 "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
+                 "mctdh_counters", "mctdh_fp64_peak"):
         getattr(lib, name).restype = C.c_int64
     _lib = lib
     return lib
@@ -90,7 +99,12 @@ def load_library() -> C.CDLL:
 EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", "mctdh_cmf2",
             "mctdh_rk_attempt", "mctdh_cmf2_attempt",
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
-            "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error"]
+            "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
+            "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
+            "mctdh_counters", "mctdh_fp64_peak"]
+
+KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
+                  "spf_derivative", "elementwise"]
 
 
 def _i64(a) -> np.ndarray:
@@ -295,6 +309,37 @@ class GpuCore:
                                              C.byref(ns), C.byref(na), C.byref(ne)))
         return tt.value, ss.value, ns.value, na.value, ne.value
 
+    def step(self, int_type: int, t: float, htry: float):
+        """One accepted step on the resident state: (hdid, hnext, attempts)."""
+        hdid, hnext, att = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self.lib.mctdh_step(self.h, int_type, t, htry, C.byref(hdid), C.byref(hnext), C.byref(att)))
+        return hdid.value, hnext.value, att.value
+
+    def event_record(self, slot: int):
+        self._check(self.lib.mctdh_event_record(self.h, slot))
+
+    def event_elapsed(self, s0: int, s1: int) -> float:
+        ms = C.c_double()
+        self._check(self.lib.mctdh_event_elapsed(self.h, s0, s1, C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable: int):
+        self._check(self.lib.mctdh_profile(self.h, enable))
+
+    def profile_read(self) -> Dict[str, Dict]:
+        out = {}
+        for kid, name in enumerate(KERNEL_CLASSES):
+            ms, fl, by = C.c_double(), C.c_double(), C.c_double()
+            n = C.c_int64()
+            self._check(self.lib.mctdh_profile_read(self.h, kid, C.byref(ms), C.byref(n), C.byref(fl), C.byref(by)))
+            out[name] = dict(ms=ms.value, launches=n.value, flops=fl.value, bytes=by.value)
+        return out
+
+    def counters(self) -> Dict[str, int]:
+        a, b, d = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.mctdh_counters(self.h, C.byref(a), C.byref(b), C.byref(d)))
+        return dict(launches=a.value, eom=b.value, hb=d.value)
+
     def launch_count(self) -> int:
         return int(self.lib.mctdh_launch_count(self.h))
 
@@ -318,3 +363,13 @@ class GpuCore:
             stats["eom"] += ne
         self.stats = stats
         return outs
+
+
+def fp64_peak_tflops() -> float:
+    """Measured FP64 FMA throughput of the current GPU (TFLOP/s)."""
+    lib = load_library()
+    v = C.c_double()
+    rc = lib.mctdh_fp64_peak(C.byref(v))
+    if rc != 0:
+        raise MctdhError(rc, "FP64 calibration failed")
+    return v.value

@@ -89,6 +89,7 @@ struct ProdBatch {
   ProdDesc* d = nullptr;
   long long nblocks = 0;
   int maxn = 0;
+  double flops = 0, bytes = 0;   // algorithmic work of one launch
   void add(const cplx* X, cplx* Y, const cplx* M, int ldm, int conjT, const std::vector<int>& shape, int mode,
            int nout, cplx alpha, int accumulate) {
     ProdDesc pd;
@@ -109,10 +110,14 @@ struct ProdBatch {
   void finalize(DevArena& ar) {
     nblocks = 0;
     maxn = 0;
+    flops = bytes = 0;
     for (auto& pd : h) {
       pd.block_start = nblocks;
       nblocks += (pd.L * pd.R + 127) / 128;
       maxn = std::max(maxn, std::max(pd.nin, pd.nout));
+      const double fib = (double)pd.L * (double)pd.R;
+      flops += 8.0 * pd.nin * pd.nout * fib;
+      bytes += 16.0 * (pd.nin + pd.nout * (pd.accumulate ? 2 : 1)) * fib;
     }
     d = upload_vec(ar, h);
   }
@@ -122,6 +127,7 @@ struct HoleBatch {
   std::vector<HoleDesc> h;
   HoleDesc* d = nullptr;
   long long nblocks = 0;
+  double flops = 0, bytes = 0;
   // returns index of the hole
   int add(DevArena& ar, const cplx* X, const cplx* Y, long long L, long long R, int n1, int n2) {
     HoleDesc hd;
@@ -140,9 +146,13 @@ struct HoleBatch {
   }
   void finalize(DevArena& ar) {
     nblocks = 0;
+    flops = bytes = 0;
     for (auto& hd : h) {
       hd.block_start = nblocks;
       nblocks += hd.nblk;
+      const double fib = (double)hd.L * (double)hd.R;
+      flops += 8.0 * hd.n1 * hd.n2 * fib;
+      bytes += 16.0 * (hd.n1 + (hd.X == hd.Y ? 0 : hd.n2)) * fib;
     }
     d = upload_vec(ar, h);
   }
@@ -211,7 +221,23 @@ struct DotPlan {
   cplx* res = nullptr;
 };
 
+enum { KP_PROD, KP_HOLE, KP_RED, KP_H1, KP_REGINV, KP_TERMSUM, KP_SPF, KP_ELEM, KP_N };
+struct KProf {
+  double ms = 0, flops = 0, bytes = 0;
+  long long launches = 0;
+};
+struct PendingEv {
+  int kid;
+  cudaEvent_t a, b;
+  double flops, bytes;
+};
+
 struct Ctx {
+  bool profiling = false;
+  KProf prof[KP_N];
+  std::vector<PendingEv> pending;
+  std::vector<cudaEvent_t> evpool;
+  cudaEvent_t user_ev[16] = {};
   std::map<std::pair<const void*, const void*>, DotPlan*> dots;
   bool fsal_valid = false;   // Dormand-Prince derivative carried between steps
   // model
@@ -277,6 +303,15 @@ struct Ctx {
   std::vector<SumSrc> src_h;
   SumRange* sum_d = nullptr;
   SumSrc* src_d = nullptr;
+  // pre-summed same-state single-mode operators
+  std::vector<int> term_single;      // mode of a same-state single-mode term, -1 none, -2 general
+  std::vector<int> general_terms;
+  std::vector<cplx> c0;              // sum of the pure-electronic same-state coefficients per state
+  std::vector<MatSumDesc> msum_h;
+  std::vector<MatSumSrc> msum_src_h;
+  MatSumDesc* msum_d = nullptr;
+  MatSumSrc* msum_src_d = nullptr;
+  std::map<std::pair<int, int>, cplx*> gmat;   // (s, m) -> G_{s,m}
   // H_B * B plan for CMF2 (Calc_DHD_B): reads d_hbin, writes d_hb
   cplx* d_hbin = nullptr;
   std::vector<ProdBatch> hb_chains;
@@ -498,13 +533,72 @@ void plan_eom(Ctx& c) {
   c.h1_smem = smem;
   c.h1_d = upload_vec(c.ar, c.h1_h);
 
-  // term chains (Calc_MeanField, gmctdh_objects.f90:513-601)
-  c.chains.assign(f + 1, ProdBatch());
+  // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
   std::vector<HoleRef> hrefs;
+  std::vector<std::vector<int>> rho_hole(f, std::vector<int>(c.nstates, -1));
+  for (int m : c.modes_dvr) {
+    int ave_target = -1;
+    if (!c.multiset[m]) {
+      int n = c.m_of(m, 0);
+      c.rho_ave[m] = c.ar.calloc_c((long long)n * n);
+      ave_target = c.red.add_target(c.rho_ave[m], n, n, n, 1);
+    }
+    for (int s = 0; s < c.nstates; ++s) {
+      int n = c.m_of(m, s);
+      c.rho[m][s] = c.ar.calloc_c((long long)n * n);
+      std::vector<int> sh = c.shape_of(s);
+      int hidx = c.holes.add(c.ar, c.d_in + c.aoff[s], c.d_in + c.aoff[s], prod_range(sh, 0, m),
+                             prod_range(sh, m + 1, f), n, n);
+      rho_hole[m][s] = hidx;
+      int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
+      hrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
+      if (ave_target >= 0) hrefs.push_back(HoleRef{hidx, ave_target, mkc(1, 0)});
+    }
+  }
+  // Hamiltonian terms (Calc_MeanField, gmctdh_objects.f90:513-601).
+  // A same-state term that touches at most one mode (all other modes are the
+  // skipped identity) has AL = A and AR = A around that mode, so its mean field
+  // is ae * sum conj(A) A -- the very contraction the density matrix is built
+  // from -- and its A-derivative is ae * h x_m A.  Such terms reuse the density
+  // contraction for the mean field and are pre-summed per (state, mode) into one
+  // operator G_{s,m} = sum_t ae_t h_t applied once.  All other terms run the
+  // reference's left/right chains.
+  c.chains.assign(f + 1, ProdBatch());
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
   std::map<std::pair<int, int>, int> mf_target;   // (m,k) -> red target
+  auto mf_tg = [&](int im, int k) {
+    auto key = std::make_pair(im, k);
+    if (!mf_target.count(key)) {
+      const int l = c.oper[im][k][0], r = c.oper[im][k][1];
+      int n1 = c.m_of(im, l), n2 = c.m_of(im, r);
+      mf_target[key] = c.red.add_target(c.mf[im][k], n1, n2, n1, 0);
+    }
+    return mf_target[key];
+  };
+  std::vector<cplx> c0(c.nstates, mkc(0, 0));
+  std::map<std::pair<int, int>, std::vector<MatSumSrc>> gsum;  // (s, m) -> sum_t ae_t h_t
+  c.term_single.assign(c.nham, -2);
   for (int t = 0; t < c.nham; ++t) {
     const int s1 = c.lhs[t], s2 = c.rhs[t];
+    int nact = 0, mact = -1;
+    for (int m = 0; m < f; ++m)
+      if (!c.skip_term[m + f * t]) { ++nact; mact = m; }
+    if (s1 == s2 && nact <= 1 && (mact < 0 || !c.is_gwp[mact])) {
+      c.term_single[t] = mact;
+      if (mact < 0) {
+        c0[s1] = cadd(c0[s1], c.ae[t]);
+        continue;
+      }
+      const int k = c.ioper[mact + f * t];
+      gsum[std::make_pair(s1, mact)].push_back(MatSumSrc{c.hmat[mact][k], c.ae[t]});
+      if (!c.is_identity[mact + f * k]) hrefs.push_back(HoleRef{rho_hole[mact][s1], mf_tg(mact, k), c.ae[t]});
+      continue;
+    }
+    // general term: right chain always reaches R_f; the left chain stops at the
+    // last mode whose mean field is needed
+    int lmax = 0;
+    for (int im = 0; im < f; ++im)
+      if (!c.is_identity[im + f * c.ioper[im + f * t]]) lmax = im;
     std::vector<TRef> R(f + 1), L(f);
     R[0].p = c.d_in + c.aoff[s2];
     R[0].shape = c.shape_of(s2);
@@ -522,7 +616,7 @@ void plan_eom(Ctx& c) {
     }
     L[0].p = c.d_in + c.aoff[s1];
     L[0].shape = c.shape_of(s1);
-    for (int i = 1; i <= f - 1; ++i) {
+    for (int i = 1; i <= lmax; ++i) {
       const int im = i - 1;
       if (c.skip_term[im + f * t]) { L[i] = L[i - 1]; continue; }
       const int k = c.ioper[im + f * t];
@@ -535,6 +629,7 @@ void plan_eom(Ctx& c) {
       L[i].shape = ns;
     }
     srcs[s1].push_back(SumSrc{R[f].p, cmul(c.der, c.ae[t])});
+    c.general_terms.push_back(t);
     for (int im = 0; im < f; ++im) {
       const int k = c.ioper[im + f * t];
       if (c.is_identity[im + f * k]) continue;
@@ -542,34 +637,32 @@ void plan_eom(Ctx& c) {
       const TRef& Y = R[f - 1 - im];
       long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, f);
       int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im]);
-      auto key = std::make_pair(im, k);
-      if (!mf_target.count(key)) {
-        const int l = c.oper[im][k][0], r = c.oper[im][k][1];
-        int n1 = c.m_of(im, l), n2 = c.m_of(im, r);
-        mf_target[key] = c.red.add_target(c.mf[im][k], n1, n2, n1, 0);
-      }
-      hrefs.push_back(HoleRef{hidx, mf_target[key], c.ae[t]});
+      hrefs.push_back(HoleRef{hidx, mf_tg(im, k), c.ae[t]});
     }
   }
-  // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
-  for (int m : c.modes_dvr) {
-    int ave_target = -1;
-    if (!c.multiset[m]) {
-      int n = c.m_of(m, 0);
-      c.rho_ave[m] = c.ar.calloc_c((long long)n * n);
-      ave_target = c.red.add_target(c.rho_ave[m], n, n, n, 1);
-    }
-    for (int s = 0; s < c.nstates; ++s) {
-      int n = c.m_of(m, s);
-      c.rho[m][s] = c.ar.calloc_c((long long)n * n);
-      std::vector<int> sh = c.shape_of(s);
-      int hidx = c.holes.add(c.ar, c.d_in + c.aoff[s], c.d_in + c.aoff[s], prod_range(sh, 0, m),
-                             prod_range(sh, m + 1, f), n, n);
-      int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
-      hrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
-      if (ave_target >= 0) hrefs.push_back(HoleRef{hidx, ave_target, mkc(1, 0)});
-    }
+  // pre-summed single-mode operators and their products with A
+  for (auto& kv : gsum) {
+    const int s = kv.first.first, m = kv.first.second;
+    const int n = c.m_of(m, s);
+    MatSumDesc md;
+    md.out = c.ar.calloc_c((long long)n * n);
+    md.n1 = n;
+    md.n2 = n;
+    md.first = (int)c.msum_src_h.size();
+    md.count = (int)kv.second.size();
+    for (auto& x : kv.second) c.msum_src_h.push_back(x);
+    c.msum_h.push_back(md);
+    c.gmat[kv.first] = md.out;
+    std::vector<int> sh = c.shape_of(s);
+    cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
+    c.chains[1].add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0);
+    srcs[s].push_back(SumSrc{out, c.der});
   }
+  for (int s = 0; s < c.nstates; ++s)
+    if (c0[s].x != 0.0 || c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_in + c.aoff[s], cmul(c.der, c0[s])});
+  c.c0 = c0;
+  c.msum_d = upload_vec(c.ar, c.msum_h);
+  c.msum_src_d = upload_vec(c.ar, c.msum_src_h);
   for (auto& b : c.chains) b.finalize(c.ar);
   c.holes.finalize(c.ar);
   for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha);
@@ -658,7 +751,7 @@ void plan_hb(Ctx& c) {
   const int f = c.nmodes;
   c.hb_chains.assign(f + 1, ProdBatch());
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
-  for (int t = 0; t < c.nham; ++t) {
+  for (int t : c.general_terms) {
     const int s1 = c.lhs[t], s2 = c.rhs[t];
     TRef cur;
     cur.p = c.d_hbin + c.aoff[s2];
@@ -678,6 +771,16 @@ void plan_hb(Ctx& c) {
     }
     srcs[s1].push_back(SumSrc{cur.p, c.ae[t]});
   }
+  for (auto& kv : c.gmat) {
+    const int s = kv.first.first, m = kv.first.second;
+    const int n = c.m_of(m, s);
+    std::vector<int> sh = c.shape_of(s);
+    cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
+    c.hb_chains[1].add(c.d_hbin + c.aoff[s], out, kv.second, n, 0, sh, m, n, mkc(1, 0), 0);
+    srcs[s].push_back(SumSrc{out, mkc(1, 0)});
+  }
+  for (int s = 0; s < c.nstates; ++s)
+    if (c.c0[s].x != 0.0 || c.c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_hbin + c.aoff[s], c.c0[s]});
   for (auto& b : c.hb_chains) b.finalize(c.ar);
   std::vector<SumRange> ranges;
   for (int s = 0; s < c.nstates; ++s) {
@@ -758,35 +861,98 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2) {
 // ---------------------------------------------------------------------------
 // Execution
 // ---------------------------------------------------------------------------
+cudaEvent_t take_event(Ctx& c) {
+  if (!c.evpool.empty()) {
+    cudaEvent_t e = c.evpool.back();
+    c.evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  CK(cudaEventCreate(&e));
+  return e;
+}
+// Bracket one launch with events when profiling (on the context stream).
+struct ProfScope {
+  Ctx& c;
+  int kid;
+  double flops, bytes;
+  cudaEvent_t a = nullptr;
+  ProfScope(Ctx& cc, int k, double f = 0, double b = 0) : c(cc), kid(k), flops(f), bytes(b) {
+    if (c.profiling) {
+      a = take_event(c);
+      CK(cudaEventRecord(a, c.st));
+    }
+  }
+  ~ProfScope() {
+    if (c.profiling && a) {
+      cudaEvent_t b = take_event(c);
+      cudaEventRecord(b, c.st);
+      c.pending.push_back(PendingEv{kid, a, b, flops, bytes});
+    }
+  }
+};
+void drain_profile(Ctx& c) {
+  if (c.pending.empty()) return;
+  CK(cudaStreamSynchronize(c.st));
+  for (auto& p : c.pending) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, p.a, p.b));
+    KProf& k = c.prof[p.kid];
+    k.ms += ms;
+    k.launches += 1;
+    k.flops += p.flops;
+    k.bytes += p.bytes;
+    c.evpool.push_back(p.a);
+    c.evpool.push_back(p.b);
+  }
+  c.pending.clear();
+}
+
 void run_prod(Ctx& c, const ProdBatch& b) {
   if (b.h.empty()) return;
+  ProfScope ps(c, KP_PROD, b.flops, b.bytes);
   launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, c.st);
   c.count();
 }
 void run_hole(Ctx& c, const HoleBatch& b) {
   if (b.h.empty()) return;
+  ProfScope ps(c, KP_HOLE, b.flops, b.bytes);
   launch_hole(b.d, (int)b.h.size(), b.nblocks, c.st);
   c.count();
 }
 void run_red(Ctx& c, const RedBatch& b) {
   if (b.tg.empty()) return;
+  ProfScope ps(c, KP_RED);
   launch_reduce(b.d_tg, (int)b.tg.size(), b.d_terms, c.st);
   c.count();
 }
 
 // EOM on d_in -> out (full vector [dA | dpsi]).
 void eom(Ctx& c, cplx* out) {
-  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
-  c.count();
+  {
+    ProfScope ps(c, KP_H1);
+    launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
+    launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
+    c.count(2);
+  }
   for (size_t i = 1; i < c.chains.size(); ++i) run_prod(c, c.chains[i]);
   run_hole(c, c.holes);
   run_red(c, c.red);
-  launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
-  c.count();
-  launch_termsum(out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st);
-  c.count();
-  launch_spf(c.spf_d, (int)c.spf_h.size(), c.spfop_d, out, c.der, c.spf_smem, c.d_status, c.st);
-  c.count();
+  {
+    ProfScope ps(c, KP_REGINV);
+    launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
+    c.count();
+  }
+  {
+    ProfScope ps(c, KP_TERMSUM, 0.0, 16.0 * (double)c.src_h.size() * (double)c.naconftot / std::max(1, c.nstates));
+    launch_termsum(out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st);
+    c.count();
+  }
+  {
+    ProfScope ps(c, KP_SPF);
+    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spfop_d, out, c.der, c.spf_smem, c.d_status, c.st);
+    c.count();
+  }
   c.eom_count++;
 }
 
@@ -1208,7 +1374,8 @@ void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
 void h1_only(Ctx& c, const cplx* y) {
   copy_dev(c, c.d_in + c.naconftot, y + c.naconftot, c.dimpsi);
   launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
-  c.count();
+  launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
+  c.count(2);
 }
 
 CmfState& cmf_state(Ctx& c) {
@@ -1384,6 +1551,9 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
     g_cmf.erase(it);
   }
   for (auto& kv : c->dots) delete kv.second;
+  drain_profile(*c);
+  for (auto e : c->evpool) cudaEventDestroy(e);
+  for (auto e : c->user_ev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(c->st);
   delete c;
   delete ctx;
@@ -1515,6 +1685,85 @@ int64_t mctdh_propagate(mctdh_ctx_t* ctx, int64_t int_type, double tnext, double
     if (nsteps) *nsteps = steps;
     if (nattempts) *nattempts = att;
     if (neom) *neom = c->eom_count - eom0;
+  });
+}
+
+int64_t mctdh_step(mctdh_ctx_t* ctx, int64_t int_type, double t, double htry, double* hdid, double* hnext,
+                   int64_t* nattempts) {
+  if (!ctx || !hdid || !hnext) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    long long att = 0;
+    if (int_type == 10) {
+      cmf2(*c, t, htry, hdid, hnext, &att);
+    } else if (int_type == 1 || int_type == 2) {
+      if (int_type == 1 || !c->fsal_valid) eom_from(*c, c->d_y, c->d_k[0]);
+      rkqs(*c, t, htry, hdid, hnext, (int)int_type, &att);
+      c->fsal_valid = (int_type == 2);
+    } else {
+      throw StatusError(MCTDH_EUNSUPPORTED, "integrator type not supported");
+    }
+    if (nattempts) *nattempts = att;
+  });
+}
+
+int64_t mctdh_counters(mctdh_ctx_t* ctx, int64_t* launches, int64_t* eom, int64_t* hb) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  if (launches) *launches = c->launches;
+  if (eom) *eom = c->eom_count;
+  if (hb) *hb = c->hb_count;
+  return MCTDH_OK;
+}
+
+int64_t mctdh_fp64_peak(double* tflops) {
+  if (!tflops) return MCTDH_EARG;
+  *tflops = measure_fp64_tflops();
+  return *tflops > 0 ? MCTDH_OK : MCTDH_ECUDA;
+}
+
+int64_t mctdh_event_record(mctdh_ctx_t* ctx, int64_t slot) {
+  if (!ctx || slot < 0 || slot >= 16) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    if (!c->user_ev[slot]) CK(cudaEventCreate(&c->user_ev[slot]));
+    CK(cudaEventRecord(c->user_ev[slot], c->st));
+  });
+}
+
+int64_t mctdh_event_elapsed(mctdh_ctx_t* ctx, int64_t s0, int64_t s1, double* ms) {
+  if (!ctx || !ms || s0 < 0 || s1 < 0 || s0 >= 16 || s1 >= 16) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    if (!c->user_ev[s0] || !c->user_ev[s1]) throw StatusError(MCTDH_EARG, "event slot not recorded");
+    CK(cudaEventSynchronize(c->user_ev[s1]));
+    float f = 0;
+    CK(cudaEventElapsedTime(&f, c->user_ev[s0], c->user_ev[s1]));
+    *ms = f;
+  });
+}
+
+int64_t mctdh_profile(mctdh_ctx_t* ctx, int64_t enable) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    drain_profile(*c);
+    if (enable == 2) for (auto& k : c->prof) k = KProf();
+    c->profiling = enable != 0;
+  });
+}
+
+int64_t mctdh_profile_read(mctdh_ctx_t* ctx, int64_t kid, double* ms, int64_t* launches, double* flops,
+                           double* bytes) {
+  if (!ctx || kid < 0 || kid >= KP_N) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    drain_profile(*c);
+    const KProf& k = c->prof[kid];
+    if (ms) *ms = k.ms;
+    if (launches) *launches = k.launches;
+    if (flops) *flops = k.flops;
+    if (bytes) *bytes = k.bytes;
   });
 }
 

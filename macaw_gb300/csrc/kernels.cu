@@ -582,3 +582,58 @@ void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* co
   if (n <= 0) return;
   gemv_cols_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, basis, ld, coef, ncol, n);
 }
+
+__global__ void matsum_kernel(const MatSumDesc* __restrict__ descs, const MatSumSrc* __restrict__ srcs) {
+  const MatSumDesc& d = descs[blockIdx.x];
+  for (int e = threadIdx.x; e < d.n1 * d.n2; e += blockDim.x) {
+    cplx acc = mkc(0, 0);
+    for (int k = 0; k < d.count; ++k) cfma(acc, srcs[d.first + k].coeff, srcs[d.first + k].src[e]);
+    d.out[e] = acc;
+  }
+}
+void launch_matsum(const MatSumDesc* d_descs, int ndesc, const MatSumSrc* d_srcs, cudaStream_t st) {
+  if (ndesc <= 0) return;
+  matsum_kernel<<<ndesc, 128, 0, st>>>(d_descs, d_srcs);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 FMA throughput calibration (independent FMA chains, no memory traffic).
+// ---------------------------------------------------------------------------
+__global__ void fp64_peak_kernel(double* out, int iters, double a) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+         x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, 1e-9); x1 = fma(x1, a, 1e-9); x2 = fma(x2, a, 1e-9); x3 = fma(x3, a, 1e-9);
+    x4 = fma(x4, a, 1e-9); x5 = fma(x5, a, 1e-9); x6 = fma(x6, a, 1e-9); x7 = fma(x7, a, 1e-9);
+  }
+  double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678) out[0] = s;
+}
+
+double measure_fp64_tflops() {
+  double* d = nullptr;
+  if (cudaMalloc(&d, 64) != cudaSuccess) return 0.0;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = nsm * 8, threads = 256, iters = 4096;
+  fp64_peak_kernel<<<blocks, threads>>>(d, 16, 0.999999);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(a);
+    fp64_peak_kernel<<<blocks, threads>>>(d, iters, 0.999999);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms;
+    cudaEventElapsedTime(&ms, a, b);
+    best = ms < best ? ms : best;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d);
+  const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+  return flops / (best * 1e-3) / 1e12;
+}

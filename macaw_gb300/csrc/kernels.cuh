@@ -113,6 +113,17 @@ struct SumSrc {
   cplx coeff;
 };
 
+// out (n1 x n2, ld n1) = sum_k coeff_k * src_k  (operators pre-summed per state and mode)
+struct MatSumDesc {
+  cplx* out;
+  int n1, n2;
+  int first, count;
+};
+struct MatSumSrc {
+  const cplx* src;
+  cplx coeff;
+};
+
 struct StageArgs {
   const cplx* k[7];
   double c[7];
@@ -136,3 +147,5 @@ void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* co
                       cudaStream_t st);
 void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, double* evals, double* evecs,
                            int* d_status, cudaStream_t st);
+void launch_matsum(const MatSumDesc* d_descs, int ndesc, const MatSumSrc* d_srcs, cudaStream_t st);
+double measure_fp64_tflops();
