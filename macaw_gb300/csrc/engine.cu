@@ -89,6 +89,7 @@ struct ProdBatch {
   ProdDesc* d = nullptr;
   long long nblocks = 0;
   int maxn = 0;
+  int prec = 0;                  // 0 FP64, 1 split FP32, 2 split FP32 compensated
   double flops = 0, bytes = 0;   // algorithmic work of one launch
   void add(const cplx* X, cplx* Y, const cplx* M, int ldm, int conjT, const std::vector<int>& shape, int mode,
            int nout, cplx alpha, int accumulate) {
@@ -312,6 +313,7 @@ struct Ctx {
   MatSumDesc* msum_d = nullptr;
   MatSumSrc* msum_src_d = nullptr;
   std::map<std::pair<int, int>, cplx*> gmat;   // (s, m) -> G_{s,m}
+  ProdBatch gprods;                            // G_{s,m} x_m A_s
   // H_B * B plan for CMF2 (Calc_DHD_B): reads d_hbin, writes d_hb
   cplx* d_hbin = nullptr;
   std::vector<ProdBatch> hb_chains;
@@ -431,7 +433,7 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.der = mkc(s->der_factor_re, s->der_factor_im);
   c.int_type_psi = (int)s->int_type_psi;
   c.precision = (int)s->precision;
-  if (c.precision != 0) throw StatusError(MCTDH_EUNSUPPORTED, "split-FP32 precision not available in this build");
+  if (c.precision < 0 || c.precision > 2) throw StatusError(MCTDH_EARG, "precision must be 0, 1 or 2");
 
   // primitive DOF operator matrices (dense ones in the zlacrm-from-the-right form
   // with the +i factor of p and qp, hamilton.f90:455-461; diagonal q^k)
@@ -655,7 +657,7 @@ void plan_eom(Ctx& c) {
     c.gmat[kv.first] = md.out;
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
-    c.chains[1].add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0);
+    c.gprods.add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0);
     srcs[s].push_back(SumSrc{out, c.der});
   }
   for (int s = 0; s < c.nstates; ++s)
@@ -664,6 +666,10 @@ void plan_eom(Ctx& c) {
   c.msum_d = upload_vec(c.ar, c.msum_h);
   c.msum_src_d = upload_vec(c.ar, c.msum_src_h);
   for (auto& b : c.chains) b.finalize(c.ar);
+  // the pre-summed products feed only dA: they run in the context's precision;
+  // the chains feeding the mean-field contractions stay FP64
+  c.gprods.prec = c.precision;
+  c.gprods.finalize(c.ar);
   c.holes.finalize(c.ar);
   for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha);
   c.red.finalize(c.ar);
@@ -781,7 +787,10 @@ void plan_hb(Ctx& c) {
   }
   for (int s = 0; s < c.nstates; ++s)
     if (c.c0[s].x != 0.0 || c.c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_hbin + c.aoff[s], c.c0[s]});
-  for (auto& b : c.hb_chains) b.finalize(c.ar);
+  for (auto& b : c.hb_chains) {
+    b.prec = c.precision;   // H_B * B feeds the Lanczos recurrence, which stays FP64
+    b.finalize(c.ar);
+  }
   std::vector<SumRange> ranges;
   for (int s = 0; s < c.nstates; ++s) {
     SumRange r;
@@ -911,7 +920,7 @@ void drain_profile(Ctx& c) {
 void run_prod(Ctx& c, const ProdBatch& b) {
   if (b.h.empty()) return;
   ProfScope ps(c, KP_PROD, b.flops, b.bytes);
-  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, c.st);
+  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, c.st, b.prec);
   c.count();
 }
 void run_hole(Ctx& c, const HoleBatch& b) {
@@ -936,6 +945,7 @@ void eom(Ctx& c, cplx* out) {
     c.count(2);
   }
   for (size_t i = 1; i < c.chains.size(); ++i) run_prod(c, c.chains[i]);
+  run_prod(c, c.gprods);
   run_hole(c, c.holes);
   run_red(c, c.red);
   {

@@ -27,10 +27,29 @@ __device__ __forceinline__ int find_desc(const D* descs, int ndesc) {
 // One thread owns one fibre (l, :, r): it reads the nin inputs once into
 // registers and writes the nout outputs.
 // ---------------------------------------------------------------------------
-template <int MAXN>
+// acc (hi, lo) += a * b for FP32 pairs a = ah + al, b = bh + bl: the leading
+// product is split exactly with an FMA, the sum keeps its rounding error in lo.
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  const float s = sh + p;
+  const float bp = s - sh;
+  const float t = (sh - (s - bp)) + (p - bp);
+  sh = s;
+  sl += t + e;
+}
+
+// PREC 0: FP64.  PREC 1: split FP32 -- x and M are split into hi + lo FP32 parts
+// and x*M = xh*Mh + xh*Ml + xl*Mh is accumulated in FP32.  PREC 2: the same split
+// with the sum carried as an FP32 hi/lo pair (compensated), ~1e-13 relative.
+template <int MAXN, int PREC>
 __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
   __shared__ int s_di;
-  __shared__ cplx Ms[MAXN * MAXN];
+  __shared__ cplx Ms[PREC == 0 ? MAXN * MAXN : 1];
+  __shared__ cplxf Mh[PREC == 0 ? 1 : MAXN * MAXN];
+  __shared__ cplxf Ml[PREC == 0 ? 1 : MAXN * MAXN];
   if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
   __syncthreads();
   const ProdDesc& d = descs[s_di];
@@ -38,7 +57,13 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   for (int e = threadIdx.x; e < nin * nout; e += blockDim.x) {
     int jo = e % nout, ji = e / nout;
     cplx v = d.conjT ? cconj(d.M[ji + (long long)d.ldm * jo]) : d.M[jo + (long long)d.ldm * ji];
-    Ms[jo + MAXN * ji] = v;
+    if (PREC == 0) {
+      Ms[jo + MAXN * ji] = v;
+    } else {
+      const float hx = (float)v.x, hy = (float)v.y;
+      Mh[jo + MAXN * ji] = make_float2(hx, hy);
+      Ml[jo + MAXN * ji] = make_float2((float)(v.x - (double)hx), (float)(v.y - (double)hy));
+    }
   }
   __syncthreads();
   const long long p = (long long)(blockIdx.x - d.block_start) * blockDim.x + threadIdx.x;
@@ -46,28 +71,76 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   if (p >= L * d.R) return;
   const long long l = p % L, r = p / L;
   const cplx* __restrict__ x0 = d.X + l + L * (long long)nin * r;
-  cplx x[MAXN];
-#pragma unroll
-  for (int j = 0; j < MAXN; ++j) x[j] = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
   cplx* y0 = d.Y + l + L * (long long)nout * r;
   const cplx alpha = d.alpha;
-  for (int jo = 0; jo < nout; ++jo) {
-    cplx acc = mkc(0.0, 0.0);
+  if (PREC == 0) {
+    cplx x[MAXN];
 #pragma unroll
-    for (int j = 0; j < MAXN; ++j)
-      if (j < nin) cfma(acc, Ms[jo + MAXN * j], x[j]);
-    cplx v = cmul(alpha, acc);
-    if (d.accumulate) v = cadd(v, y0[L * jo]);
-    y0[L * jo] = v;
+    for (int j = 0; j < MAXN; ++j) x[j] = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
+    for (int jo = 0; jo < nout; ++jo) {
+      cplx acc = mkc(0.0, 0.0);
+#pragma unroll
+      for (int j = 0; j < MAXN; ++j)
+        if (j < nin) cfma(acc, Ms[jo + MAXN * j], x[j]);
+      cplx v = cmul(alpha, acc);
+      if (d.accumulate) v = cadd(v, y0[L * jo]);
+      y0[L * jo] = v;
+    }
+  } else {
+    cplxf xh[MAXN], xl[MAXN];
+#pragma unroll
+    for (int j = 0; j < MAXN; ++j) {
+      cplx v = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
+      const float hx = (float)v.x, hy = (float)v.y;
+      xh[j] = make_float2(hx, hy);
+      xl[j] = make_float2((float)(v.x - (double)hx), (float)(v.y - (double)hy));
+    }
+    for (int jo = 0; jo < nout; ++jo) {
+      cplx accd;
+      if (PREC == 1) {
+        cplxf acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < MAXN; ++j)
+          if (j < nin) {
+            const cplxf mh = Mh[jo + MAXN * j], ml = Ml[jo + MAXN * j];
+            acc = cfmaf_(acc, mh, xh[j]);
+            acc = cfmaf_(acc, mh, xl[j]);
+            acc = cfmaf_(acc, ml, xh[j]);
+          }
+        accd = mkc((double)acc.x, (double)acc.y);
+      } else {
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+#pragma unroll
+        for (int j = 0; j < MAXN; ++j)
+          if (j < nin) {
+            const cplxf mh = Mh[jo + MAXN * j], ml = Ml[jo + MAXN * j];
+            // real: mr*xr - mi*xi ; imag: mr*xi + mi*xr
+            df_fma(rh, rl, mh.x, ml.x, xh[j].x, xl[j].x);
+            df_fma(rh, rl, -mh.y, -ml.y, xh[j].y, xl[j].y);
+            df_fma(ih, il, mh.x, ml.x, xh[j].y, xl[j].y);
+            df_fma(ih, il, mh.y, ml.y, xh[j].x, xl[j].x);
+          }
+        accd = mkc((double)rh + (double)rl, (double)ih + (double)il);
+      }
+      cplx v = cmul(alpha, accd);
+      if (d.accumulate) v = cadd(v, y0[L * jo]);
+      y0[L * jo] = v;
+    }
   }
 }
 
-void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st) {
+void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, int prec) {
   if (ndesc <= 0 || nblocks <= 0) return;
-  if (maxn <= 12)
-    prod_kernel<12><<<(unsigned)nblocks, 128, 0, st>>>(d_descs, ndesc);
-  else
-    prod_kernel<MAXN_SPF><<<(unsigned)nblocks, 128, 0, st>>>(d_descs, ndesc);
+  const unsigned nb = (unsigned)nblocks;
+  if (maxn <= 12) {
+    if (prec == 0) prod_kernel<12, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
+    else if (prec == 1) prod_kernel<12, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
+    else prod_kernel<12, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
+  } else {
+    if (prec == 0) prod_kernel<MAXN_SPF, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
+    else if (prec == 1) prod_kernel<MAXN_SPF, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
+    else prod_kernel<MAXN_SPF, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -131,7 +131,8 @@ struct StageArgs {
 };
 
 // Launch helpers (kernels.cu)
-void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st);
+void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st,
+                 int prec = 0);
 void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st);
 void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st);
 void launch_h1(const H1Desc* d_descs, int ndesc, size_t smem_bytes, cudaStream_t st);
