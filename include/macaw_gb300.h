@@ -152,6 +152,30 @@ int64_t mctdh_wf_ovl(mctdh_ctx_t *ctx, const double *A1, const double *psi1, con
 /* Kernel launches issued by this context since creation (for accounting). */
 int64_t mctdh_launch_count(mctdh_ctx_t *ctx);
 
+/* Density matrix of one mode without any device allocation.  This entry point
+ * has no counterpart in the reference (which always allocates on the host).  It
+ * serves callers that cannot call cudaMalloc where they need the result: code
+ * running while a stream is captured into a CUDA graph, programs that give the
+ * GPU a fixed memory budget, or a driver that already keeps A in device memory
+ * it manages itself.
+ *   A      device pointer: one state's coefficient tensor, sizes nspf[0..nmodes-1],
+ *          mode 1 fastest (init_calc.f90:531-536)
+ *   rho    device pointer, column-major with leading dimension ld:
+ *          rho(j1, j2) = sum over all other modes of conj(A(.., j1, ..)) A(.., j2, ..),
+ *          the contraction of Calc_rho1mode (gmctdh_objects.f90:452-457) for a grid mode
+ *   stream cudaStream_t to launch on (NULL: the legacy default stream); the call
+ *          returns after launching, rho is ready once the stream has run.
+ * Limit: nspf[mode] <= 32.  Larger sizes, host pointers or a bad mode return -7
+ * (message in mctdh_last_error(NULL)) without touching the GPU.
+ * Scratch: a 2 MiB file-scope __device__ array that every GPU loading this
+ * library holds until exit.  The first call on a device looks up its address
+ * with cudaGetSymbolAddress (make that first call before any stream capture).
+ * All calls share the array: calls that overlap on the GPU (different streams
+ * without ordering) race and return wrong results.  Each call writes every
+ * scratch entry it later reads, so nothing carries over between calls. */
+int64_t mctdh_density_matrix_noalloc(const double *A, const int64_t *nspf, int64_t nmodes, int64_t mode,
+                                     double *rho, int64_t ld, void *stream);
+
 /* Last error message of the context (or of the last failed create when ctx is NULL). */
 const char *mctdh_last_error(mctdh_ctx_t *ctx);
 

@@ -82,6 +82,8 @@ def load_library() -> C.CDLL:
     lib.mctdh_profile.argtypes = [vp, C.c_int64]
     lib.mctdh_counters.argtypes = [vp, I64P, I64P, I64P]
     lib.mctdh_fp64_peak.argtypes = [DP]
+    lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
+                                                 C.c_int64, C.c_void_p]
     lib.mctdh_profile_read.argtypes = [vp, C.c_int64, DP, I64P, DP, DP]
     lib.mctdh_last_error.argtypes = [vp]
     lib.mctdh_last_error.restype = C.c_char_p
@@ -90,7 +92,7 @@ def load_library() -> C.CDLL:
                  "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
                  "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_step",
                  "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
-                 "mctdh_counters", "mctdh_fp64_peak"):
+                 "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"):
         getattr(lib, name).restype = C.c_int64
     _lib = lib
     return lib
@@ -101,7 +103,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
-            "mctdh_counters", "mctdh_fp64_peak"]
+            "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"]
 
 KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
                   "spf_derivative", "elementwise"]

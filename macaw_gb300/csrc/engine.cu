@@ -1532,6 +1532,9 @@ struct mctdh_ctx {
   Ctx* c;
 };
 
+// Error text for calls that run without a context (read with mctdh_last_error(NULL)).
+void mctdh_set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+
 extern "C" {
 
 int64_t mctdh_create(const mctdh_setup_t* setup, mctdh_ctx_t** out) {
