@@ -38,6 +38,7 @@ METRIC = "simulated fs/s & EOM evals/s vs plain FP64 GPU path at |dC(t)|<=1e-6"
 WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/state, CMF2+Lanczos"
 EPS_CMF = 1e-5
 PRE_FS = 1.0
+ACC_FS = 0.5   # interval over which the split path is compared with the FP64 path
 REF_STEP_FS = 0.1   # CMF2 step length the reference arm times (steady-state steps are of this order)
 
 
@@ -181,6 +182,49 @@ def run_reference(args):
     return 0
 
 
+def timed_steps(core, t, h, steps, l2, torch):
+    """K accepted CMF2 steps on the resident state, each bracketed by CUDA events on
+    the library's stream after an L2 flush; returns (t, h, device ms, simulated fs, hdids)."""
+    ms_total, fs_total, hdids = 0.0, 0.0, []
+    for _ in range(steps):
+        flush_l2(l2)
+        torch.cuda.synchronize()
+        core.event_record(0)
+        hdid, hnext, _ = core.step(INT_CMF2, t, h)
+        core.event_record(1)
+        ms_total += core.event_elapsed(0, 1)
+        t += hdid
+        h = hnext
+        fs_total += hdid * AU2FS
+        hdids.append(hdid * AU2FS)
+    return t, h, ms_total, fs_total, hdids
+
+
+def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile):
+    from macaw_gb300.capi import GpuCore
+    A0, psi0, A1, psi1 = state
+    core = GpuCore(model, precision=precision)
+    core.set_state(A0, psi0, as_start=True)
+    core.set_state(A1, psi1, as_start=False)
+    t, h = t0, h0
+    for _ in range(args.warmup):
+        hdid, h, _ = core.step(INT_CMF2, t, h)
+        t += hdid
+    c0 = core.counters()
+    if profile:
+        core.profile(2)
+    barrier(tdist)
+    torch.cuda.synchronize()
+    t, h, ms, fs, hdids = timed_steps(core, t, h, args.steps, l2, torch)
+    torch.cuda.synchronize()
+    barrier(tdist)
+    prof = core.profile_read() if profile else None
+    core.profile(0)
+    c1 = core.counters()
+    return core, dict(t=t, h=h, ms=ms, fs=fs, hdids=hdids, prof=prof,
+                      eom=c1["eom"] - c0["eom"], hb=c1["hb"] - c0["hb"], launches=c1["launches"] - c0["launches"])
+
+
 def run_gpu(args):
     import torch
     from macaw_gb300.capi import GpuCore, fp64_peak_tflops
@@ -188,73 +232,61 @@ def run_gpu(args):
     torch.cuda.init()
     model = make_model()
     A0, psi0 = initial_wavefunction(model)
-    core = GpuCore(model, precision=0)
-    core.set_state(A0, psi0, as_start=True)
     l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
     # leave the start-up transient of the step control (the reference starts at
     # tout * eps_int, propagator.f90:103, and grows by at most 1.5x per CMF2 step):
-    # propagate 1 fs untimed, then warm up and time steady-state steps
-    t, h, _, _, _ = core.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
-    for _ in range(args.warmup):
-        hdid, h, _ = core.step(INT_CMF2, t, h)
-        t += hdid
-    c0 = core.counters()
-    core.profile(2)
-    ms_total = 0.0
-    fs_total = 0.0
-    hdids = []
-    barrier(tdist)
-    torch.cuda.synchronize()
+    # propagate 1 fs untimed with the FP64 path; both arms start from that state
+    pre = GpuCore(model, precision=0)
+    pre.set_state(A0, psi0, as_start=True)
+    t1, h1, _, _, _ = pre.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
+    A1, psi1 = pre.get_state()
+    pre.close()
+    state = (A0, psi0, A1, psi1)
     with ClockSampler(torch.cuda.current_device()) as clk:
-        for _ in range(args.steps):
-            flush_l2(l2)
-            torch.cuda.synchronize()
-            core.event_record(0)
-            hdid, hnext, _ = core.step(INT_CMF2, t, h)
-            core.event_record(1)
-            ms_total += core.event_elapsed(0, 1)
-            t += hdid
-            h = hnext
-            fs_total += hdid * AU2FS
-            hdids.append(hdid * AU2FS)
-        torch.cuda.synchronize()
-    barrier(tdist)
-    prof = core.profile_read()
-    core.profile(0)
-    c1 = core.counters()
+        ref_core, ref = run_arm(model, 0, state, t1, h1, args, l2, torch, tdist, profile=False)
+        mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=True)
+    # accuracy of the split path against the plain FP64 path: both propagate the same
+    # state over the same output interval; C(t) and populations are compared there
+    cmp = {}
+    for name, core in (("fp64", ref_core), ("mixed", mix_core)):
+        core.set_state(A1, psi1, as_start=False)
+        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + ACC_FS / AU2FS, t1, h1)
+        cmp[name] = core.observables(tt)
+    dC = abs(cmp["mixed"]["auto"] - cmp["fp64"]["auto"])
+    dpop = float(np.abs(cmp["mixed"]["pop"] - cmp["fp64"]["pop"]).max())
+    ms_total, fs_total = mix["ms"], mix["fs"]
     if tdist is not None:
-        tt = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+        tt = torch.tensor([ms_total, ref["ms"]], device="cuda", dtype=torch.float64)
         tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        ms_total = float(tt.item())
+        ms_total, ref["ms"] = float(tt[0].item()), float(tt[1].item())
     value = ws * fs_total / (ms_total * 1e-3)
-    eom_per_s = (c1["eom"] - c0["eom"]) / (ms_total * 1e-3)
-    hb_per_s = (c1["hb"] - c0["hb"]) / (ms_total * 1e-3)
-    launches = c1["launches"] - c0["launches"]
+    fp64_value = ws * ref["fs"] / (ref["ms"] * 1e-3)
 
     # e2e: the reference-facing host-buffer call (mctdh_cmf2) with pinned buffers,
     # host<->device copies of A and psi inside every step
-    Ah, ph = core.get_state()
+    Ah, ph = mix_core.get_state()
     pA = torch.from_numpy(Ah.copy()).pin_memory()
     pP = torch.from_numpy(ph.copy()).pin_memory()
     import ctypes as C
     DPp = C.POINTER(C.c_double)
     hd, hn = C.c_double(), C.c_double()
     e2e_fs, e2e_s = 0.0, 0.0
-    te, he = t, h
+    te, he = mix["t"], mix["h"]
     for _ in range(max(1, args.steps // 2)):
         flush_l2(l2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rc = core.lib.mctdh_cmf2(core.h, C.cast(pA.data_ptr(), DPp), C.cast(pP.data_ptr(), DPp), te, he,
-                                 C.byref(hd), C.byref(hn))
+        rc = mix_core.lib.mctdh_cmf2(mix_core.h, C.cast(pA.data_ptr(), DPp), C.cast(pP.data_ptr(), DPp), te, he,
+                                     C.byref(hd), C.byref(hn))
         e2e_s += time.perf_counter() - t0
         if rc != 0:
-            raise RuntimeError(core.lib.mctdh_last_error(core.h).decode())
+            raise RuntimeError(mix_core.lib.mctdh_last_error(mix_core.h).decode())
         te += hd.value
         he = hn.value
         e2e_fs += hd.value * AU2FS
     nbytes = 16 * (model.naconftot + model.dimpsi)
 
+    prof = mix["prof"]
     peaks, peak_src = load_peaks()
     fp64_peak = fp64_peak_tflops()
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
@@ -265,17 +297,24 @@ def run_gpu(args):
     achieved_gbs = by_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     achieved_tf = fl_launch / (avg_ms * 1e-3) / 1e12 if avg_ms > 0 else 0.0
     clocks = clk.summary()
+    tot_ms = max(sum(x["ms"] for x in prof.values()), 1e-9)
     line = {
         "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded qvc12 model)",
-        "config": {"workload": WORKLOAD, "integrator": "cmf2", "precision": "fp64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded qvc12 model)",
+        "config": {"workload": WORKLOAD, "integrator": "cmf2",
+                   "precision": {0: "fp64", 1: "split-fp32", 2: "split-fp32-compensated"}[args.precision],
                    "eps_cmf": EPS_CMF, "l2": "flushed (256 MB write) before every timed step",
-                   "step_fs_mean": statistics.mean(hdids), "parallelism": f"replicas x{ws}"},
-        "eom_per_s": eom_per_s, "hb_per_s": hb_per_s,
+                   "step_fs_mean": statistics.mean(mix["hdids"]), "parallelism": f"replicas x{ws}"},
+        "fp64_path": {"value": fp64_value, "unit": "fs/s", "ms_per_step": ref["ms"] / args.steps,
+                      "step_fs_mean": statistics.mean(ref["hdids"])},
+        "speedup_vs_fp64_path": value / fp64_value,
+        "accuracy_vs_fp64_path": {"dC": dC, "dpop": dpop, "over_fs": ACC_FS, "from_fs": t1 * AU2FS},
+        "eom_per_s": mix["eom"] / (ms_total * 1e-3), "hb_per_s": mix["hb"] / (ms_total * 1e-3),
         "e2e": {"value": e2e_fs / e2e_s, "unit": "fs/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
-        "gpu_launches": launches,
+        "gpu_launches": mix["launches"],
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
                      "peak_source": peak_src},
@@ -283,17 +322,37 @@ def run_gpu(args):
                           "frac": achieved_tf / fp64_peak if fp64_peak > 0 else None,
                           "peak_source": "measured FP64 FMA chain on this GPU"},
         "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
-                               "share": round(v["ms"] / max(sum(x["ms"] for x in prof.values()), 1e-9), 4)}
+                               "share": round(v["ms"] / tot_ms, 4)}
                            for k, v in prof.items() if v["launches"]},
+        "gpu_busy_frac": tot_ms / ms_total,
         "clocks": clocks,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(model, A0, psi0, statistics.mean(hdids) / AU2FS)
+        line["cpu_baseline"] = cpu_baseline(model, A0, psi0, statistics.mean(mix["hdids"]) / AU2FS)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    core.close()
+    ref_core.close()
+    mix_core.close()
     if tdist is not None:
         tdist.destroy_process_group()
+    return 0
+
+
+def run_profile_case(args):
+    """A short, fixed piece of the workload for profiler captures: three CMF2 steps
+    of 1e-3 fs from the initial state of the qvc12 model (about 1,700 launches)."""
+    from macaw_gb300.capi import GpuCore
+    model = make_model()
+    A0, psi0 = initial_wavefunction(model)
+    core = GpuCore(model, precision=args.precision)
+    core.set_state(A0, psi0, as_start=True)
+    t, h = 0.0, 1e-3 / AU2FS
+    for _ in range(3):
+        hdid, h, _ = core.step(INT_CMF2, t, h)
+        t += hdid
+    print(json.dumps({"profile_case": "qvc12", "precision": args.precision, "t_fs": t * AU2FS,
+                      "launches": core.launch_count()}), flush=True)
+    core.close()
     return 0
 
 
@@ -304,7 +363,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
+                    help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run a short fixed piece of the workload (for profiler captures) instead of the benchmark")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -176,6 +176,23 @@ int64_t mctdh_launch_count(mctdh_ctx_t *ctx);
 int64_t mctdh_density_matrix_noalloc(const double *A, const int64_t *nspf, int64_t nmodes, int64_t mode,
                                      double *rho, int64_t ld, void *stream);
 
+/* Learned mean-field extrapolator: a multilayer perceptron with BF16 weights and
+ * activations and FP32 accumulation (tanh hidden layers, linear output), trained
+ * with hand-written forward, backward and Adam kernels.  No reference
+ * counterpart: it plugs into CMF2 between the mean-field evaluations of
+ * cmf2_base.f90:78-87 and :122-130.  widths[0..nlayers]: layer sizes.
+ * Parameters are flat FP32: per layer W (N x K, row-major) then b (N). */
+typedef struct mctdh_mlp mctdh_mlp_t;
+int64_t mctdh_mlp_create(const int64_t *widths, int64_t nlayers, uint64_t seed, mctdh_mlp_t **mlp);
+int64_t mctdh_mlp_destroy(mctdh_mlp_t *mlp);
+int64_t mctdh_mlp_nparams(mctdh_mlp_t *mlp, int64_t *n);
+int64_t mctdh_mlp_set_params(mctdh_mlp_t *mlp, const float *params);
+int64_t mctdh_mlp_get_params(mctdh_mlp_t *mlp, float *params);
+int64_t mctdh_mlp_predict(mctdh_mlp_t *mlp, const float *X, float *Y, int64_t M);
+int64_t mctdh_mlp_grad(mctdh_mlp_t *mlp, const float *X, const float *T, int64_t M, float *grad, double *loss);
+int64_t mctdh_mlp_train(mctdh_mlp_t *mlp, const float *X, const float *T, int64_t M, int64_t batch, int64_t epochs,
+                        double lr, double *loss);
+
 /* Last error message of the context (or of the last failed create when ctx is NULL). */
 const char *mctdh_last_error(mctdh_ctx_t *ctx);
 

@@ -82,6 +82,18 @@ def load_library() -> C.CDLL:
     lib.mctdh_profile.argtypes = [vp, C.c_int64]
     lib.mctdh_counters.argtypes = [vp, I64P, I64P, I64P]
     lib.mctdh_fp64_peak.argtypes = [DP]
+    FP = C.POINTER(C.c_float)
+    lib.mctdh_mlp_create.argtypes = [I64P, C.c_int64, C.c_uint64, C.POINTER(vp)]
+    lib.mctdh_mlp_destroy.argtypes = [vp]
+    lib.mctdh_mlp_nparams.argtypes = [vp, I64P]
+    lib.mctdh_mlp_set_params.argtypes = [vp, FP]
+    lib.mctdh_mlp_get_params.argtypes = [vp, FP]
+    lib.mctdh_mlp_predict.argtypes = [vp, FP, FP, C.c_int64]
+    lib.mctdh_mlp_grad.argtypes = [vp, FP, FP, C.c_int64, FP, DP]
+    lib.mctdh_mlp_train.argtypes = [vp, FP, FP, C.c_int64, C.c_int64, C.c_int64, C.c_double, DP]
+    for name in ("mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
+                 "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train"):
+        getattr(lib, name).restype = C.c_int64
     lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
                                                  C.c_int64, C.c_void_p]
     lib.mctdh_profile_read.argtypes = [vp, C.c_int64, DP, I64P, DP, DP]
@@ -103,7 +115,9 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
-            "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"]
+            "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
+            "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
+            "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train"]
 
 KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
                   "spf_derivative", "elementwise"]
@@ -375,3 +389,69 @@ def fp64_peak_tflops() -> float:
     if rc != 0:
         raise MctdhError(rc, "FP64 calibration failed")
     return v.value
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+
+
+class Mlp:
+    """The extrapolator network on the GPU (BF16 weights/activations, FP32 accumulation)."""
+
+    def __init__(self, widths=(8, 256, 256, 256, 4), seed: int = 1):
+        self.lib = load_library()
+        self.widths = tuple(int(w) for w in widths)
+        w = _i64(self.widths)
+        h = C.c_void_p()
+        rc = self.lib.mctdh_mlp_create(_ptr(w, C.c_int64), len(self.widths) - 1, seed, C.byref(h))
+        if rc != 0:
+            raise MctdhError(rc, self.lib.mctdh_last_error(None).decode())
+        self.h = h
+        n = C.c_int64()
+        self.lib.mctdh_mlp_nparams(self.h, C.byref(n))
+        self.nparams = n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mctdh_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise MctdhError(rc, self.lib.mctdh_last_error(None).decode())
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.nparams, dtype=np.float32)
+        self._check(self.lib.mctdh_mlp_get_params(self.h, _ptr(p, C.c_float)))
+        return p
+
+    def set_params(self, p):
+        p = _f32(p)
+        self._check(self.lib.mctdh_mlp_set_params(self.h, _ptr(p, C.c_float)))
+
+    def predict(self, X) -> np.ndarray:
+        X = _f32(X)
+        Y = np.zeros((X.shape[0], self.widths[-1]), dtype=np.float32)
+        self._check(self.lib.mctdh_mlp_predict(self.h, _ptr(X, C.c_float), _ptr(Y, C.c_float), X.shape[0]))
+        return Y
+
+    def grad(self, X, T):
+        X, T = _f32(X), _f32(T)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.mctdh_mlp_grad(self.h, _ptr(X, C.c_float), _ptr(T, C.c_float), X.shape[0],
+                                            _ptr(g, C.c_float), C.byref(loss)))
+        return loss.value, g
+
+    def train(self, X, T, batch=4096, epochs=10, lr=1e-3) -> float:
+        X, T = _f32(X), _f32(T)
+        loss = C.c_double()
+        self._check(self.lib.mctdh_mlp_train(self.h, _ptr(X, C.c_float), _ptr(T, C.c_float), X.shape[0], batch,
+                                             epochs, lr, C.byref(loss)))
+        return loss.value

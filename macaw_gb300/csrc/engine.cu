@@ -128,6 +128,7 @@ struct HoleBatch {
   std::vector<HoleDesc> h;
   HoleDesc* d = nullptr;
   long long nblocks = 0;
+  int prec = 0;                  // 0 FP64, 2 compensated split FP32
   double flops = 0, bytes = 0;
   // returns index of the hole
   int add(DevArena& ar, const cplx* X, const cplx* Y, long long L, long long R, int n1, int n2) {
@@ -289,7 +290,8 @@ struct Ctx {
   H1Desc* h1_d = nullptr;
   size_t h1_smem = 0;
   std::vector<ProdBatch> chains;  // per depth
-  HoleBatch holes;
+  HoleBatch holes;       // mean-field contractions of the general terms
+  HoleBatch rho_holes;   // density matrices (FP64 always)
   RedBatch red;
   std::vector<RegInvDesc> reg_h;
   std::vector<MFOp> mfop_h;
@@ -300,6 +302,7 @@ struct Ctx {
   SpfDesc* spf_d = nullptr;
   SpfOp* spfop_d = nullptr;
   size_t spf_smem = 0;
+  long long spf_tiles = 0;
   std::vector<SumRange> sum_h;
   std::vector<SumSrc> src_h;
   SumRange* sum_d = nullptr;
@@ -536,7 +539,8 @@ void plan_eom(Ctx& c) {
   c.h1_d = upload_vec(c.ar, c.h1_h);
 
   // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
-  std::vector<HoleRef> hrefs;
+  std::vector<HoleRef> hrefs;       // mean-field contractions (c.holes)
+  std::vector<HoleRef> rrefs;       // density-matrix contractions (c.rho_holes, FP64)
   std::vector<std::vector<int>> rho_hole(f, std::vector<int>(c.nstates, -1));
   for (int m : c.modes_dvr) {
     int ave_target = -1;
@@ -549,12 +553,12 @@ void plan_eom(Ctx& c) {
       int n = c.m_of(m, s);
       c.rho[m][s] = c.ar.calloc_c((long long)n * n);
       std::vector<int> sh = c.shape_of(s);
-      int hidx = c.holes.add(c.ar, c.d_in + c.aoff[s], c.d_in + c.aoff[s], prod_range(sh, 0, m),
-                             prod_range(sh, m + 1, f), n, n);
+      int hidx = c.rho_holes.add(c.ar, c.d_in + c.aoff[s], c.d_in + c.aoff[s], prod_range(sh, 0, m),
+                                 prod_range(sh, m + 1, f), n, n);
       rho_hole[m][s] = hidx;
       int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
-      hrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
-      if (ave_target >= 0) hrefs.push_back(HoleRef{hidx, ave_target, mkc(1, 0)});
+      rrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
+      if (ave_target >= 0) rrefs.push_back(HoleRef{hidx, ave_target, mkc(1, 0)});
     }
   }
   // Hamiltonian terms (Calc_MeanField, gmctdh_objects.f90:513-601).
@@ -593,7 +597,7 @@ void plan_eom(Ctx& c) {
       }
       const int k = c.ioper[mact + f * t];
       gsum[std::make_pair(s1, mact)].push_back(MatSumSrc{c.hmat[mact][k], c.ae[t]});
-      if (!c.is_identity[mact + f * k]) hrefs.push_back(HoleRef{rho_hole[mact][s1], mf_tg(mact, k), c.ae[t]});
+      if (!c.is_identity[mact + f * k]) rrefs.push_back(HoleRef{rho_hole[mact][s1], mf_tg(mact, k), c.ae[t]});
       continue;
     }
     // general term: right chain always reaches R_f; the left chain stops at the
@@ -665,12 +669,21 @@ void plan_eom(Ctx& c) {
   c.c0 = c0;
   c.msum_d = upload_vec(c.ar, c.msum_h);
   c.msum_src_d = upload_vec(c.ar, c.msum_src_h);
-  for (auto& b : c.chains) b.finalize(c.ar);
-  // the pre-summed products feed only dA: they run in the context's precision;
-  // the chains feeding the mean-field contractions stay FP64
+  // Precision: the pre-summed products feed only dA and run in the context's
+  // precision.  The chains and contractions of the mean fields use the
+  // compensated split (about 1e-13 relative) whenever a split mode is chosen,
+  // because the regularised inverse of rho scales mean-field errors by up to
+  // 1/eps_rho.  The density matrices themselves stay FP64.
+  for (auto& b : c.chains) {
+    b.prec = c.precision ? 2 : 0;
+    b.finalize(c.ar);
+  }
   c.gprods.prec = c.precision;
   c.gprods.finalize(c.ar);
+  c.holes.prec = c.precision ? 2 : 0;
   c.holes.finalize(c.ar);
+  c.rho_holes.finalize(c.ar);
+  for (auto& hr : rrefs) c.red.add_term(hr.target, c.rho_holes.h[hr.hole], hr.alpha);
   for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha);
   c.red.finalize(c.ar);
 
@@ -729,6 +742,11 @@ void plan_eom(Ctx& c) {
         c.spfop_h.push_back(op);
       }
       sd.op_count = (int)c.spfop_h.size() - sd.op_first;
+      sd.ntile = (sd.G + SPF_TILE - 1) / SPF_TILE;
+      sd.block_start = c.spf_tiles;
+      c.spf_tiles += sd.ntile;
+      sd.partial = c.ar.calloc_c((long long)sd.ntile * 2 * sd.n * sd.n);
+      sd.X = c.ar.calloc_c((long long)sd.n * sd.n);
       c.spf_h.push_back(sd);
       ssmem = std::max(ssmem, sizeof(cplx) * (size_t)(2 * sd.G * sd.n));
     }
@@ -926,7 +944,7 @@ void run_prod(Ctx& c, const ProdBatch& b) {
 void run_hole(Ctx& c, const HoleBatch& b) {
   if (b.h.empty()) return;
   ProfScope ps(c, KP_HOLE, b.flops, b.bytes);
-  launch_hole(b.d, (int)b.h.size(), b.nblocks, c.st);
+  launch_hole(b.d, (int)b.h.size(), b.nblocks, c.st, b.prec);
   c.count();
 }
 void run_red(Ctx& c, const RedBatch& b) {
@@ -946,6 +964,7 @@ void eom(Ctx& c, cplx* out) {
   }
   for (size_t i = 1; i < c.chains.size(); ++i) run_prod(c, c.chains[i]);
   run_prod(c, c.gprods);
+  run_hole(c, c.rho_holes);
   run_hole(c, c.holes);
   run_red(c, c.red);
   {
@@ -960,8 +979,8 @@ void eom(Ctx& c, cplx* out) {
   }
   {
     ProfScope ps(c, KP_SPF);
-    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spfop_d, out, c.der, c.spf_smem, c.d_status, c.st);
-    c.count();
+    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st);
+    c.count(3);
   }
   c.eom_count++;
 }
@@ -1090,8 +1109,8 @@ void hb(Ctx& c, const cplx* B, cplx* out) {
   c.hb_count++;
 }
 
-// <a|b> over the coefficient vector (FP64, deterministic)
-cplx dot_now(Ctx& c, const cplx* a, const cplx* b, long long n) {
+// <a|b> over the coefficient vector (FP64, deterministic); result left on the device
+cplx* dot_dev(Ctx& c, const cplx* a, const cplx* b, long long n) {
   // plans are cached per context, keyed by the pointer pair
   auto key = std::make_pair((const void*)a, (const void*)b);
   DotPlan* P = c.dots.count(key) ? c.dots[key] : nullptr;
@@ -1107,8 +1126,13 @@ cplx dot_now(Ctx& c, const cplx* a, const cplx* b, long long n) {
   }
   run_hole(c, P->hb);
   run_red(c, P->red);
+  return P->res;
+}
+
+cplx dot_now(Ctx& c, const cplx* a, const cplx* b, long long n) {
+  cplx* d = dot_dev(c, a, b, n);
   cplx r;
-  CK(cudaMemcpyAsync(&r, P->res, sizeof(cplx), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaMemcpyAsync(&r, d, sizeof(cplx), cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
   return r;
 }
@@ -1121,18 +1145,19 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
   const long long n = c.naconftot;
   cplx* K = c.d_krylov;
   if (build) {
-    cplx nrm2 = dot_now(c, B0, B0, n);
-    double nrm = sqrt(nrm2.x);
-    launch_copy_scale(K, B0, mkc(1.0 / nrm, 0), n, c.st);
+    // alpha_j, beta_j stay on the device (d_lan[0..19], d_lan[20..39]); only beta_j
+    // comes back for the stopping rule: one host synchronisation per Krylov vector
+    double* d_alpha = c.d_lan;
+    double* d_beta = c.d_lan + NKRYLOV_MAX;
+    launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st);
     c.count();
-    double alpha[NKRYLOV_MAX] = {0}, beta[NKRYLOV_MAX] = {0};
+    double beta[NKRYLOV_MAX] = {0};
     hb(c, K, K + n);
-    alpha[0] = dot_now(c, K, K + n, n).x;
-    launch_axpy(K + n, K, mkc(-alpha[0], 0), n, c.st);
-    c.count();
-    beta[0] = sqrt(dot_now(c, K + n, K + n, n).x);
-    launch_copy_scale(K + n, K + n, mkc(1.0 / beta[0], 0), n, c.st);
-    c.count();
+    launch_lan_axpy(K + n, K, nullptr, dot_dev(c, K, K + n, n), nullptr, d_alpha, n, c.st);
+    launch_lan_normalize(K + n, K + n, dot_dev(c, K + n, K + n, n), d_beta, n, c.st);
+    c.count(2);
+    CK(cudaMemcpyAsync(&beta[0], d_beta, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
     double error = beta[0] * fabs(dt);
     int j = 2;
     while (true) {
@@ -1141,20 +1166,16 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
       cplx* Kn = K + (long long)j * n;
       cplx* Kp = K + (long long)(j - 2) * n;
       hb(c, Kj, Kn);
-      alpha[j - 1] = dot_now(c, Kj, Kn, n).x;
-      launch_axpy(Kn, Kp, mkc(-beta[j - 2], 0), n, c.st);
-      launch_axpy(Kn, Kj, mkc(-alpha[j - 1], 0), n, c.st);
+      launch_lan_axpy(Kn, Kj, Kp, dot_dev(c, Kj, Kn, n), d_beta + (j - 2), d_alpha + (j - 1), n, c.st);
+      launch_lan_normalize(Kn, Kn, dot_dev(c, Kn, Kn, n), d_beta + (j - 1), n, c.st);
       c.count(2);
-      beta[j - 1] = sqrt(dot_now(c, Kn, Kn, n).x);
-      launch_copy_scale(Kn, Kn, mkc(1.0 / beta[j - 1], 0), n, c.st);
-      c.count();
+      CK(cudaMemcpyAsync(&beta[j - 1], d_beta + (j - 1), sizeof(double), cudaMemcpyDeviceToHost, c.st));
+      CK(cudaStreamSynchronize(c.st));
       error = error * beta[j - 1] / (double)j * fabs(dt);
       if (error < EPS_B) break;
       ++j;
     }
     const int nk = j;
-    CK(cudaMemcpyAsync(c.d_lan, alpha, sizeof(double) * NKRYLOV_MAX, cudaMemcpyHostToDevice, c.st));
-    CK(cudaMemcpyAsync(c.d_lan + NKRYLOV_MAX, beta, sizeof(double) * NKRYLOV_MAX, cudaMemcpyHostToDevice, c.st));
     launch_jacobi_tridiag(c.d_lan, c.d_lan + NKRYLOV_MAX, nk, c.d_lan + 2 * NKRYLOV_MAX,
                           c.d_lan + 3 * NKRYLOV_MAX, c.d_status, c.st);
     c.count();
@@ -1182,199 +1203,13 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
   }
   CK(cudaMemcpyAsync(c.d_coef, coef.data(), sizeof(cplx) * nk, cudaMemcpyHostToDevice, c.st));
   launch_gemv_cols(BT, K, n, c.d_coef, nk, n, c.st);
-  c.count();
-  double nrm = sqrt(dot_now(c, BT, BT, n).x);
-  launch_copy_scale(BT, BT, mkc(1.0 / nrm, 0), n, c.st);
-  c.count();
+  launch_lan_normalize(BT, BT, dot_dev(c, BT, BT, n), nullptr, n, c.st);
+  c.count(2);
 }
 
 // operators and mean fields on the state y (Calc_rho1mode, Calc_h1mode,
 // Calc_MeanField, Calc_rhom1MF): one EOM into d_out (the derivative is unused).
 void operators_and_mf(Ctx& c, const cplx* y) { eom_from(c, y, c.d_out); }
-
-// SPF derivative of one DVR mode with frozen mean fields (Calc_Der_SPF,
-// cmf2_derivatives.f90:84-173) from the SPFs in d_in into out.
-struct ModeSpfPlan {
-  std::vector<H1Desc> h1;
-  H1Desc* h1_d = nullptr;
-  std::vector<SpfDesc> spf;
-  SpfDesc* spf_d = nullptr;
-  std::vector<long long> blocks;  // (offset, length) pairs in the psi part
-  HoleBatch err_holes;            // Calc_Err_SPF: (dphi)^H dphi per state block
-  RedBatch err_red;
-  std::vector<cplx*> err_mat;     // per state block
-};
-
-void plan_mode_spf(Ctx& c, std::vector<ModeSpfPlan>& plans) {
-  const int f = c.nmodes;
-  plans.assign(f, ModeSpfPlan());
-  for (int m : c.modes_dvr) {
-    ModeSpfPlan& P = plans[m];
-    for (int idx : c.h1_of_mode[m]) {
-      H1Desc hd = c.h1_h[idx];
-      hd.h = nullptr;   // mean fields and h1mode stay frozen; only ophi is refreshed
-      P.h1.push_back(hd);
-    }
-    P.h1_d = upload_vec(c.ar, P.h1);
-    for (auto& sd : c.spf_h) {
-      // the spf descriptors of this mode: phi pointer lies in this mode's blocks
-      for (int s = 0; s < c.nstates; ++s) {
-        if (!c.multiset[m] && s > 0) break;
-        if (sd.out_offset == c.naconftot + c.ipsi[m + f * s]) P.spf.push_back(sd);
-      }
-    }
-    P.spf_d = upload_vec(c.ar, P.spf);
-    for (int s = 0; s < c.nstates; ++s) {
-      if (!c.multiset[m] && s > 0) break;
-      P.blocks.push_back(c.naconftot + c.ipsi[m + f * s]);
-      P.blocks.push_back((long long)c.gmode[m] * c.m_of(m, s));
-    }
-  }
-}
-
-struct CmfState {
-  std::vector<ModeSpfPlan> mode_plans;
-  bool planned = false;
-  cplx *B0, *BHalf, *B02, *psiHalf, *psiHalf2, *AHalf;  // full-length vectors (ntot)
-  cplx* ytmp;
-};
-std::map<const Ctx*, CmfState*> g_cmf;
-
-void stage_blocks(Ctx& c, cplx* out, const cplx* base, const double* coef, int nk, double dt,
-                  const std::vector<long long>& blocks) {
-  for (size_t b = 0; b + 1 < blocks.size(); b += 2) {
-    StageArgs a;
-    memset(&a, 0, sizeof(a));
-    int n = 0;
-    for (int j = 0; j < nk; ++j) {
-      if (coef[j] == 0.0) continue;
-      a.k[n] = c.d_k[j] + blocks[b];
-      a.c[n] = coef[j];
-      ++n;
-    }
-    a.nk = n;
-    launch_stage(out + blocks[b], base + blocks[b], a, dt, blocks[b + 1], c.st);
-    c.count();
-  }
-}
-
-void spf_eval(Ctx& c, ModeSpfPlan& P, cplx* out) {
-  launch_h1(P.h1_d, (int)P.h1.size(), c.h1_smem, c.st);
-  launch_spf(P.spf_d, (int)P.spf.size(), c.spfop_d, out, c.der, c.spf_smem, c.d_status, c.st);
-  c.count(2);
-}
-
-double err_spf(Ctx& c, CmfState& S, int m, const cplx* p1, const cplx* p2);
-
-// rk_SPF_ck (cmf2_integration.f90:105-253), DVR branch; psi part of y updated in place.
-void rk_spf_ck(Ctx& c, CmfState& S, int m, cplx* y, double htry, double* hdid, double* hnext) {
-  ModeSpfPlan& P = S.mode_plans[m];
-  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
-  double dt = htry, error;
-  while (true) {
-    // d_in carries the SPFs on which the operators act
-    for (size_t b = 0; b + 1 < P.blocks.size(); b += 2)
-      CK(cudaMemcpyAsync(c.d_in + P.blocks[b], y + P.blocks[b], sizeof(cplx) * P.blocks[b + 1],
-                         cudaMemcpyDeviceToDevice, c.st));
-    spf_eval(c, P, c.d_k[0]);
-    for (int st = 1; st < 6; ++st) {
-      stage_blocks(c, c.d_in, y, CK_B[st], st, dt, P.blocks);
-      spf_eval(c, P, c.d_k[st]);
-    }
-    stage_blocks(c, c.d_tmp, y, CK_C, 6, dt, P.blocks);
-    stage_blocks(c, c.d_err, y, CK_D, 6, dt, P.blocks);
-    error = err_spf(c, S, m, c.d_tmp, c.d_err) / c.eps_psi;
-    if (error < 1.0) break;
-    dt = std::max(RK_MINSCAL * dt, RK_SAFETY * dt * pow(error, RK_PSHRNK));
-  }
-  *hnext = (error > errcon) ? RK_SAFETY * dt * pow(error, RK_PGROW) : dt * RK_MAXSCAL;
-  *hdid = dt;
-  for (size_t b = 0; b + 1 < P.blocks.size(); b += 2)
-    CK(cudaMemcpyAsync(y + P.blocks[b], c.d_tmp + P.blocks[b], sizeof(cplx) * P.blocks[b + 1],
-                       cudaMemcpyDeviceToDevice, c.st));
-}
-
-void propagate_spf(Ctx& c, CmfState& S, double dt, int m, cplx* y) {
-  if (c.int_type_psi != 1) throw StatusError(MCTDH_EUNSUPPORTED, "only Cash-Karp SPF integration is supported");
-  double done = 0.0, step = dt, sdone, snext;
-  while (true) {
-    rk_spf_ck(c, S, m, y, step, &sdone, &snext);
-    done += sdone;
-    if (done >= dt) break;
-    snext = std::max(snext, c.min_stepsize * 2);
-    step = (dt - done) / ((double)(long long)((dt - done) / snext) + 1);
-    step = std::min(step, dt - done);
-  }
-}
-
-// Calc_Err_SPF, DVR branch (cmf2_derivatives.f90:239-283): error^2 = Tr(rho * dS),
-// dS = (phi1 - phi2)^H (phi1 - phi2).  Computed as a hole contraction of the
-// difference vector (d_err <- p1 - p2 over the mode's blocks).
-double err_spf(Ctx& c, CmfState& S, int m, const cplx* p1, const cplx* p2) {
-  ModeSpfPlan& P = S.mode_plans[m];
-  for (size_t b = 0; b + 1 < P.blocks.size(); b += 2) {
-    StageArgs a;
-    memset(&a, 0, sizeof(a));
-    a.k[0] = p2 + P.blocks[b];
-    a.c[0] = -1.0;
-    a.nk = 1;
-    launch_stage(S.ytmp + P.blocks[b], p1 + P.blocks[b], a, 1.0, P.blocks[b + 1], c.st);
-    c.count();
-  }
-  run_hole(c, P.err_holes);
-  run_red(c, P.err_red);
-  double err = 0.0;
-  int si = 0;
-  for (int s = 0; s < c.nstates; ++s) {
-    if (!c.multiset[m] && s > 0) break;
-    const int n = c.m_of(m, s);
-    std::vector<cplx> dS(n * n), rho(n * n);
-    CK(cudaMemcpyAsync(dS.data(), P.err_mat[si], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c.st));
-    const cplx* rp = c.multiset[m] ? c.rho[m][s] : c.rho_ave[m];
-    CK(cudaMemcpyAsync(rho.data(), rp, sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c.st));
-    CK(cudaStreamSynchronize(c.st));
-    for (int j2 = 0; j2 < n; ++j2) {
-      for (int j1 = 0; j1 < j2; ++j1) {
-        cplx r = rho[j1 + n * j2], o = dS[j1 + n * j2];
-        err += 2.0 * (r.x * o.x + r.y * o.y);   // Re(rho * conj(ovl))
-      }
-      cplx r = rho[j2 + n * j2], o = dS[j2 + n * j2];
-      err += r.x * o.x - r.y * o.y;               // Re(rho * ovl)
-    }
-    ++si;
-  }
-  return sqrt(fabs(err));
-}
-
-void plan_cmf(Ctx& c, CmfState& S) {
-  const int f = c.nmodes;
-  plan_mode_spf(c, S.mode_plans);
-  S.B0 = c.ar.calloc_c(c.ntot);
-  S.BHalf = c.ar.calloc_c(c.ntot);
-  S.B02 = c.ar.calloc_c(c.ntot);
-  S.psiHalf = c.ar.calloc_c(c.ntot);
-  S.psiHalf2 = c.ar.calloc_c(c.ntot);
-  S.AHalf = c.ar.calloc_c(c.ntot);
-  S.ytmp = c.ar.calloc_c(c.ntot);
-  // Calc_Err_SPF holes: one per (mode, state block) on the difference vector ytmp
-  for (int m : c.modes_dvr) {
-    ModeSpfPlan& P = S.mode_plans[m];
-    std::vector<HoleRef> hrefs;
-    for (int s = 0; s < c.nstates; ++s) {
-      if (!c.multiset[m] && s > 0) break;
-      const int n = c.m_of(m, s);
-      cplx* mat = c.ar.calloc_c((long long)n * n);
-      P.err_mat.push_back(mat);
-      cplx* p = S.ytmp + c.naconftot + c.ipsi[m + f * s];
-      int h = P.err_holes.add(c.ar, p, p, c.gmode[m], 1, n, n);
-      hrefs.push_back(HoleRef{h, P.err_red.add_target(mat, n, n, n, 1), mkc(1, 0)});
-    }
-    P.err_holes.finalize(c.ar);
-    for (auto& hr : hrefs) P.err_red.add_term(hr.target, P.err_holes.h[hr.hole], hr.alpha);
-    P.err_red.finalize(c.ar);
-  }
-  S.planned = true;
-}
 
 void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
   CK(cudaMemcpyAsync(dst, src, sizeof(cplx) * n, cudaMemcpyDeviceToDevice, c.st));
@@ -1386,6 +1221,176 @@ void h1_only(Ctx& c, const cplx* y) {
   launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
   launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
   c.count(2);
+}
+
+// SPF integration of all DVR modes with frozen mean fields, in lockstep: one
+// launch per Runge-Kutta stage covers every mode, each mode keeps the step
+// control of propagate_SPF / rk_SPF_ck (cmf2_base.f90:210-260,
+// cmf2_integration.f90:105-253) with its own step length.  Modes are
+// independent (their SPF equations see only their own SPFs and the frozen mean
+// fields), so the result equals mode-by-mode integration.
+struct CmfState {
+  bool planned = false;
+  cplx *B0, *BHalf, *B02, *psiHalf, *psiHalf2, *AHalf;  // full-length vectors (ntot)
+  cplx* ytmp;
+  std::vector<H1Desc> h1;       // operators on the current SPFs (h1mode frozen)
+  H1Desc* h1_d = nullptr;
+  unsigned char* elem_mode = nullptr;   // mode of every psi element
+  double* dt_mode = nullptr;            // device, per mode
+  int* accept = nullptr;                // device, per mode
+  double* err_mode = nullptr;           // device, per mode
+  HoleBatch err_holes;                  // (dphi)^H dphi per (mode, state block)
+  RedBatch err_red;
+  std::vector<SpfErrDesc> errd_h;
+  SpfErrDesc* errd_d = nullptr;
+  long long rk_iters = 0;
+};
+std::map<const Ctx*, CmfState*> g_cmf;
+
+void stage_modes(Ctx& c, CmfState& S, cplx* out, const cplx* base, const double* coef, int nk) {
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  int n = 0;
+  for (int j = 0; j < nk; ++j) {
+    if (coef[j] == 0.0) continue;
+    a.k[n] = c.d_k[j];
+    a.c[n] = coef[j];
+    ++n;
+  }
+  a.nk = n;
+  ProfScope ps(c, KP_ELEM);
+  launch_stage_modes(out, base, a, S.dt_mode, S.elem_mode, c.naconftot, c.dimpsi, c.st);
+  c.count();
+}
+
+void spf_eval_all(Ctx& c, CmfState& S, cplx* out) {
+  {
+    ProfScope ps(c, KP_H1);
+    launch_h1(S.h1_d, (int)S.h1.size(), c.h1_smem, c.st);
+  }
+  {
+    ProfScope ps(c, KP_SPF);
+    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st);
+  }
+  c.count(4);
+}
+
+void plan_cmf(Ctx& c, CmfState& S) {
+  const int f = c.nmodes;
+  S.B0 = c.ar.calloc_c(c.ntot);
+  S.BHalf = c.ar.calloc_c(c.ntot);
+  S.B02 = c.ar.calloc_c(c.ntot);
+  S.psiHalf = c.ar.calloc_c(c.ntot);
+  S.psiHalf2 = c.ar.calloc_c(c.ntot);
+  S.AHalf = c.ar.calloc_c(c.ntot);
+  S.ytmp = c.ar.calloc_c(c.ntot);
+  for (auto hd : c.h1_h) {
+    hd.h = nullptr;   // mean fields and h1mode stay frozen; only ophi is refreshed
+    S.h1.push_back(hd);
+  }
+  S.h1_d = upload_vec(c.ar, S.h1);
+  std::vector<unsigned char> em((size_t)std::max<long long>(c.dimpsi, 1), 0);
+  std::vector<HoleRef> hrefs;
+  for (int m : c.modes_dvr) {
+    for (int s = 0; s < c.nstates; ++s) {
+      if (!c.multiset[m] && s > 0) break;
+      const int n = c.m_of(m, s);
+      const long long o = c.ipsi[m + f * s], len = (long long)c.gmode[m] * n;
+      for (long long i = 0; i < len; ++i) em[o + i] = (unsigned char)m;
+      cplx* mat = c.ar.calloc_c((long long)n * n);
+      cplx* p = S.ytmp + c.naconftot + o;
+      int h = S.err_holes.add(c.ar, p, p, c.gmode[m], 1, n, n);
+      hrefs.push_back(HoleRef{h, S.err_red.add_target(mat, n, n, n, 1), mkc(1, 0)});
+      SpfErrDesc ed;
+      ed.ds = mat;
+      ed.rho = c.multiset[m] ? c.rho[m][s] : c.rho_ave[m];
+      ed.n = n;
+      ed.mode = m;
+      S.errd_h.push_back(ed);
+    }
+  }
+  S.elem_mode = upload_vec(c.ar, em);
+  S.err_holes.finalize(c.ar);
+  for (auto& hr : hrefs) S.err_red.add_term(hr.target, S.err_holes.h[hr.hole], hr.alpha);
+  S.err_red.finalize(c.ar);
+  S.errd_d = upload_vec(c.ar, S.errd_h);
+  S.dt_mode = (double*)c.ar.alloc(sizeof(double) * 64);
+  S.accept = (int*)c.ar.alloc(sizeof(int) * 64);
+  S.err_mode = (double*)c.ar.alloc(sizeof(double) * 64);
+  if (f > 64) throw StatusError(MCTDH_EUNSUPPORTED, "more than 64 modes");
+  S.planned = true;
+}
+
+// propagate_SPF for every DVR mode over dt_total, on the psi part of y.
+void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
+  if (c.int_type_psi != 1) throw StatusError(MCTDH_EUNSUPPORTED, "only Cash-Karp SPF integration is supported");
+  const int f = c.nmodes;
+  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
+  std::vector<double> done(f, 0.0), dtry(f, 0.0), dt_h(64, 0.0), err_h(64, 0.0);
+  std::vector<int> active(f, 0), acc_h(64, 0);
+  for (int m : c.modes_dvr) {
+    active[m] = 1;
+    dtry[m] = dt_total;
+  }
+  const long long nA = c.naconftot;
+  for (int iter = 0;; ++iter) {
+    bool any = false;
+    for (int m = 0; m < f; ++m) {
+      dt_h[m] = active[m] ? dtry[m] : 0.0;
+      any = any || active[m];
+    }
+    if (!any) break;
+    if (iter > 100000) throw StatusError(MCTDH_ESTEP, "SPF integration did not finish");
+    ++S.rk_iters;
+    CK(cudaMemcpyAsync(S.dt_mode, dt_h.data(), sizeof(double) * 64, cudaMemcpyHostToDevice, c.st));
+    copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
+    spf_eval_all(c, S, c.d_k[0]);
+    for (int st = 1; st < 6; ++st) {
+      stage_modes(c, S, c.d_in, y, CK_B[st], st);
+      spf_eval_all(c, S, c.d_k[st]);
+    }
+    stage_modes(c, S, c.d_tmp, y, CK_C, 6);
+    stage_modes(c, S, c.d_err, y, CK_D, 6);
+    {
+      StageArgs a;
+      memset(&a, 0, sizeof(a));
+      a.k[0] = c.d_err + nA;
+      a.c[0] = -1.0;
+      a.nk = 1;
+      launch_stage(S.ytmp + nA, c.d_tmp + nA, a, 1.0, c.dimpsi, c.st);
+      c.count();
+    }
+    run_hole(c, S.err_holes);
+    run_red(c, S.err_red);
+    launch_spf_err(S.errd_d, (int)S.errd_h.size(), S.err_mode, f, c.st);
+    c.count();
+    CK(cudaMemcpyAsync(err_h.data(), S.err_mode, sizeof(double) * f, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int m = 0; m < f; ++m) {
+      acc_h[m] = 0;
+      if (!active[m]) continue;
+      const double error = err_h[m] / c.eps_psi;
+      if (!std::isfinite(error)) throw StatusError(MCTDH_ENONFINITE, "non-finite SPF error estimate");
+      if (error >= 1.0) {   // retry with a shorter step (rk_SPF_ck :231)
+        dtry[m] = std::max(RK_MINSCAL * dtry[m], RK_SAFETY * dtry[m] * pow(error, RK_PSHRNK));
+        continue;
+      }
+      acc_h[m] = 1;
+      const double hdid = dtry[m];
+      double hnext = (error > errcon) ? RK_SAFETY * hdid * pow(error, RK_PGROW) : hdid * RK_MAXSCAL;
+      done[m] += hdid;
+      if (done[m] >= dt_total) {   // propagate_SPF :229
+        active[m] = 0;
+        continue;
+      }
+      hnext = std::max(hnext, c.min_stepsize * 2);
+      double step = (dt_total - done[m]) / ((double)(long long)((dt_total - done[m]) / hnext) + 1);
+      dtry[m] = std::min(step, dt_total - done[m]);
+    }
+    CK(cudaMemcpyAsync(S.accept, acc_h.data(), sizeof(int) * 64, cudaMemcpyHostToDevice, c.st));
+    launch_masked_copy(y, c.d_tmp, S.elem_mode, S.accept, nA, c.dimpsi, c.st);
+    c.count();
+  }
 }
 
 CmfState& cmf_state(Ctx& c) {
@@ -1406,12 +1411,12 @@ double cmf2_attempt(Ctx& c, double t, double hdid) {
   copy_dev(c, S.B0, c.d_y, nA);                     // A_to_B (DVR only)
   lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);      // :97
   copy_dev(c, S.psiHalf, c.d_y, c.ntot);
-  for (int m : c.modes_dvr) propagate_spf(c, S, 0.5 * hdid, m, S.psiHalf);   // :109-115
+  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf);   // :109-115
   copy_dev(c, S.AHalf, S.BHalf, nA);                // B_to_A  :120
   copy_dev(c, S.AHalf + nA, S.psiHalf + nA, c.dimpsi);
   operators_and_mf(c, S.AHalf);                     // :122-130
   copy_dev(c, S.psiHalf2, c.d_y, c.ntot);
-  for (int m : c.modes_dvr) propagate_spf(c, S, 0.5 * hdid, m, S.psiHalf2);  // :132-141
+  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2);  // :132-141
   // err_psi = DeltaPsi(AHalf, psiHalf, AHalf, psiHalf2)  (:143)
   copy_dev(c, c.d_tmp, S.AHalf, c.ntot);
   copy_dev(c, c.d_err, S.AHalf, nA);
@@ -1420,7 +1425,7 @@ double cmf2_attempt(Ctx& c, double t, double hdid) {
   cplx o[3];
   read_ovl(c, c.dpsi_plan, o);
   double err_psi = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x))));
-  for (int m : c.modes_dvr) propagate_spf(c, S, 0.5 * hdid, m, S.psiHalf2);  // :148-154
+  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2);  // :148-154
   h1_only(c, S.psiHalf2);                           // :158-165
   lanczos(c, S.BHalf, S.B02, -0.5 * hdid, true);    // :169
   launch_axpy(S.B02, S.B0, mkc(-1, 0), nA, c.st);

@@ -149,6 +149,27 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
 // Block b of a descriptor handles fibre tiles b, b + nblk, ...; every thread owns
 // one (j1, j2) pair and a fibre group; groups are summed in shared memory.
 // ---------------------------------------------------------------------------
+// 1 x 1 contractions (inner products): every thread strides over elements with
+// coalesced loads, the block reduces in shared memory.
+template <int PREC>
+__device__ void dot_block(const HoleDesc& d, int b, cplx* red) {
+  const long long n = d.L * d.R;
+  const int tid = threadIdx.x;
+  cplx acc = mkc(0, 0);
+  for (long long i = (long long)b * HOLE_THREADS + tid; i < n; i += (long long)d.nblk * HOLE_THREADS)
+    cfma_conj(acc, d.X[i], d.Y[i]);
+  red[tid] = acc;
+  __syncthreads();
+  for (int s = HOLE_THREADS / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] = cadd(red[tid], red[tid + s]);
+    __syncthreads();
+  }
+  if (tid == 0) d.partial[b] = red[0];
+}
+
+// PREC 0: FP64.  PREC 2: operands split into FP32 hi + lo parts, products and sums
+// carried as compensated FP32 pairs (df_fma), ~1e-13 relative.
+template <int PREC>
 __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
   __shared__ int s_di;
   __shared__ cplx Xs[HOLE_TILE * MAXN_SPF];
@@ -158,6 +179,10 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   const HoleDesc& d = descs[s_di];
   const int b = (int)(blockIdx.x - d.block_start);
   const int n1 = d.n1, n2 = d.n2, npairs = n1 * n2;
+  if (npairs == 1 && d.L * d.R >= HOLE_THREADS) {
+    dot_block<PREC>(d, b, Xs);
+    return;
+  }
   const long long L = d.L, nfib = d.L * d.R;
   const long long ntiles = (nfib + HOLE_TILE - 1) / HOLE_TILE;
   const int tid = threadIdx.x;
@@ -166,6 +191,8 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   const int pair0 = small ? tid % npairs : tid;
   const int g = small ? tid / npairs : 0;
   cplx acc[4] = {mkc(0, 0), mkc(0, 0), mkc(0, 0), mkc(0, 0)};
+  float ah[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  float al[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   for (long long tile = b; tile < ntiles; tile += d.nblk) {
     const long long p0 = tile * HOLE_TILE;
     for (int e = tid; e < HOLE_TILE * n1; e += HOLE_THREADS) {
@@ -183,22 +210,40 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
       Ys[q * MAXN_SPF + j] = v;
     }
     __syncthreads();
-    if (small) {
-      if (g < G) {
-        const int j1 = pair0 % n1, j2 = pair0 / n1;
-        for (int q = g; q < HOLE_TILE; q += G) cfma_conj(acc[0], Xs[q * MAXN_SPF + j1], Ys[q * MAXN_SPF + j2]);
-      }
-    } else {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        int pr = pair0 + HOLE_THREADS * k;
-        if (pr < npairs) {
-          const int j1 = pr % n1, j2 = pr / n1;
-          for (int q = 0; q < HOLE_TILE; ++q) cfma_conj(acc[k], Xs[q * MAXN_SPF + j1], Ys[q * MAXN_SPF + j2]);
+    for (int k = 0; k < 4; ++k) {
+      int pr, q0, qs;
+      if (small) {
+        if (k > 0 || g >= G) break;
+        pr = pair0; q0 = g; qs = G;
+      } else {
+        pr = pair0 + HOLE_THREADS * k;
+        if (pr >= npairs) break;
+        q0 = 0; qs = 1;
+      }
+      const int j1 = pr % n1, j2 = pr / n1;
+      for (int q = q0; q < HOLE_TILE; q += qs) {
+        const cplx x = Xs[q * MAXN_SPF + j1], y = Ys[q * MAXN_SPF + j2];
+        if (PREC == 0) {
+          cfma_conj(acc[k], x, y);
+        } else {
+          // conj(x) y: re = xr yr + xi yi, im = xr yi - xi yr
+          const float xrh = (float)x.x, xih = (float)x.y, yrh = (float)y.x, yih = (float)y.y;
+          const float xrl = (float)(x.x - (double)xrh), xil = (float)(x.y - (double)xih);
+          const float yrl = (float)(y.x - (double)yrh), yil = (float)(y.y - (double)yih);
+          df_fma(ah[k][0], al[k][0], xrh, xrl, yrh, yrl);
+          df_fma(ah[k][0], al[k][0], xih, xil, yih, yil);
+          df_fma(ah[k][1], al[k][1], xrh, xrl, yih, yil);
+          df_fma(ah[k][1], al[k][1], -xih, -xil, yrh, yrl);
         }
       }
     }
     __syncthreads();
+  }
+  if (PREC != 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      acc[k] = mkc((double)ah[k][0] + (double)al[k][0], (double)ah[k][1] + (double)al[k][1]);
   }
   cplx* out = d.partial + (long long)b * npairs;
   if (small) {
@@ -219,9 +264,12 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   }
 }
 
-void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st) {
+void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec) {
   if (ndesc <= 0 || nblocks <= 0) return;
-  hole_kernel<<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
+  if (prec == 0)
+    hole_kernel<0><<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
+  else
+    hole_kernel<2><<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
 }
 
 // ---------------------------------------------------------------------------
@@ -492,50 +540,75 @@ void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, doubl
 }
 
 // ---------------------------------------------------------------------------
-// DVR SPF derivative with the (1 - P) projector (derivatives.f90:96-153).
-// One block per (mode, state).
+// DVR SPF derivative with the (1 - P) projector (derivatives.f90:96-153), tiled
+// over the grid so every (mode, state) block spreads over many SMs:
+//  (1) spf_tile_kernel: dphi rows = f * sum_k ophi_k rhom1MF_k^T for SPF_TILE grid
+//      rows, plus this tile's share of phi^H phi and phi^H dphi;
+//  (2) spf_solve_kernel: sum the tile shares (fixed order), Cholesky solve
+//      (phi^H phi) X = phi^H dphi  (zposv 'U');
+//  (3) spf_proj_kernel: dphi rows -= phi rows * X.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) spf_kernel(const SpfDesc* __restrict__ descs, const SpfOp* __restrict__ ops,
-                                                  cplx* __restrict__ out, cplx der, int* status) {
-  extern __shared__ cplx sm[];
-  const SpfDesc& d = descs[blockIdx.x];
+__global__ void __launch_bounds__(256) spf_tile_kernel(const SpfDesc* __restrict__ descs, int ndesc,
+                                                       const SpfOp* __restrict__ ops, cplx* __restrict__ out,
+                                                       cplx der) {
+  __shared__ int s_di;
+  __shared__ cplx phs[SPF_TILE * MAXN_SPF];
+  __shared__ cplx dps[SPF_TILE * MAXN_SPF];
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const SpfDesc& d = descs[s_di];
+  const int t = (int)(blockIdx.x - d.block_start);
   const int G = d.G, n = d.n;
-  cplx* phi = sm;
-  cplx* dph = sm + (long long)G * n;
-  __shared__ cplx S[MAXN_SPF * MAXN_SPF];
-  __shared__ cplx O[MAXN_SPF * MAXN_SPF];
-  for (int e = threadIdx.x; e < G * n; e += blockDim.x) phi[e] = d.phi[e];
-  for (int e = threadIdx.x; e < G * n; e += blockDim.x) {
-    const int g = e % G, j1 = e / G;
+  const int g0 = t * SPF_TILE;
+  const int rows = min(SPF_TILE, G - g0);
+  cplx* o = out + d.out_offset;
+  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
+    const int r = e % rows, j1 = e / rows;
+    const int g = g0 + r;
+    phs[r + SPF_TILE * j1] = d.phi[g + (long long)G * j1];
     cplx acc = mkc(0, 0);
-    for (int o = 0; o < d.op_count; ++o) {
-      const SpfOp& op = ops[d.op_first + o];
+    for (int q = 0; q < d.op_count; ++q) {
+      const SpfOp& op = ops[d.op_first + q];
       const cplx* oph = op.ophi + g;
       for (int j2 = 0; j2 < op.n2; ++j2) cfma(acc, oph[(long long)G * j2], op.rm[j1 + n * j2]);
     }
-    dph[e] = cmul(der, acc);
+    acc = cmul(der, acc);
+    dps[r + SPF_TILE * j1] = acc;
+    o[g + (long long)G * j1] = acc;
   }
   __syncthreads();
+  cplx* part = d.partial + (long long)t * 2 * n * n;
   for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
-    const int which = pr / (n * n);
-    const int q = pr % (n * n);
+    const int which = pr / (n * n), q = pr % (n * n);
     const int j1 = q % n, j2 = q / n;
-    const cplx* a = phi + (long long)G * j1;
-    const cplx* b = (which == 0 ? phi : dph) + (long long)G * j2;
+    const cplx* a = phs + SPF_TILE * j1;
+    const cplx* b = (which == 0 ? phs : dps) + SPF_TILE * j2;
     cplx s = mkc(0, 0);
-    for (int g = 0; g < G; ++g) cfma_conj(s, a[g], b[g]);
-    if (which == 0) S[j1 + MAXN_SPF * j2] = s; else O[j1 + MAXN_SPF * j2] = s;
+    for (int r = 0; r < rows; ++r) cfma_conj(s, a[r], b[r]);
+    part[pr] = s;
+  }
+}
+
+__global__ void spf_solve_kernel(const SpfDesc* __restrict__ descs, int* status) {
+  __shared__ cplx S[MAXN_SPF * MAXN_SPF];
+  __shared__ cplx O[MAXN_SPF * MAXN_SPF];
+  const SpfDesc& d = descs[blockIdx.x];
+  const int n = d.n, ld = MAXN_SPF;
+  for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
+    const int which = pr / (n * n), q = pr % (n * n);
+    const int j1 = q % n, j2 = q / n;
+    cplx s = mkc(0, 0);
+    for (int t = 0; t < d.ntile; ++t) s = cadd(s, d.partial[(long long)t * 2 * n * n + pr]);
+    if (which == 0) S[j1 + ld * j2] = s; else O[j1 + ld * j2] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    // zposv('U'): S = U^H U, solve for the n right-hand sides in O (overwritten by X)
-    const int ld = MAXN_SPF;
     bool fail = false;
     for (int j = 0; j < n; ++j) {
       double djj = S[j + ld * j].x;
       for (int k = 0; k < j; ++k) djj -= cabs2(S[k + ld * j]);
       if (!(djj > 0.0)) { fail = true; djj = 1e-300; }
-      double ujj = sqrt(djj);
+      const double ujj = sqrt(djj);
       S[j + ld * j] = mkc(ujj, 0.0);
       for (int i = j + 1; i < n; ++i) {
         cplx sji = S[j + ld * i];
@@ -544,13 +617,11 @@ __global__ void __launch_bounds__(256) spf_kernel(const SpfDesc* __restrict__ de
       }
     }
     for (int c = 0; c < n; ++c) {
-      // forward: U^H y = o
       for (int i = 0; i < n; ++i) {
         cplx v = O[i + ld * c];
         for (int k = 0; k < i; ++k) v = csub(v, cmul(cconj(S[k + ld * i]), O[k + ld * c]));
         O[i + ld * c] = cscale(v, 1.0 / S[i + ld * i].x);
       }
-      // backward: U x = y
       for (int i = n - 1; i >= 0; --i) {
         cplx v = O[i + ld * c];
         for (int k = i + 1; k < n; ++k) v = csub(v, cmul(S[i + ld * k], O[k + ld * c]));
@@ -560,24 +631,38 @@ __global__ void __launch_bounds__(256) spf_kernel(const SpfDesc* __restrict__ de
     if (fail) atomicOr(status, DEVST_CHOL_FAIL);
   }
   __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) d.X[e] = O[(e % n) + ld * (e / n)];
+}
+
+__global__ void __launch_bounds__(256) spf_proj_kernel(const SpfDesc* __restrict__ descs, int ndesc,
+                                                       cplx* __restrict__ out) {
+  __shared__ int s_di;
+  __shared__ cplx Xs[MAXN_SPF * MAXN_SPF];
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const SpfDesc& d = descs[s_di];
+  const int n = d.n, G = d.G;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Xs[e] = d.X[e];
+  __syncthreads();
+  const int t = (int)(blockIdx.x - d.block_start);
+  const int g0 = t * SPF_TILE;
+  const int rows = min(SPF_TILE, G - g0);
   cplx* o = out + d.out_offset;
-  for (int e = threadIdx.x; e < G * n; e += blockDim.x) {
-    const int g = e % G, j = e / G;
-    cplx v = dph[e];
-    for (int k = 0; k < n; ++k) v = csub(v, cmul(phi[g + (long long)G * k], O[k + MAXN_SPF * j]));
-    o[e] = v;
+  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
+    const int r = e % rows, j = e / rows;
+    const int g = g0 + r;
+    cplx v = o[g + (long long)G * j];
+    for (int k = 0; k < n; ++k) v = csub(v, cmul(d.phi[g + (long long)G * k], Xs[k + n * j]));
+    o[g + (long long)G * j] = v;
   }
 }
 
-void launch_spf(const SpfDesc* d_descs, int ndesc, const SpfOp* d_ops, cplx* out, cplx der_factor,
-                size_t smem_bytes, int* d_status, cudaStream_t st) {
+void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
+                cplx der_factor, int* d_status, cudaStream_t st) {
   if (ndesc <= 0) return;
-  static size_t configured = 0;
-  if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
-    cudaFuncSetAttribute(spf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-    configured = smem_bytes;
-  }
-  spf_kernel<<<ndesc, 256, smem_bytes, st>>>(d_descs, d_ops, out, der_factor, d_status);
+  spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  spf_solve_kernel<<<ndesc, 128, 0, st>>>(d_descs, d_status);
+  spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -709,4 +794,113 @@ double measure_fp64_tflops() {
   cudaFree(d);
   const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
   return flops / (best * 1e-3) / 1e12;
+}
+
+// ---------------------------------------------------------------------------
+// Lockstep SPF integration of all DVR modes (rk_SPF_ck with frozen mean fields,
+// cmf2_integration.f90:105-253): every psi element carries its mode, each mode its
+// own step length (0 for a mode that has finished its interval).
+// ---------------------------------------------------------------------------
+__global__ void stage_modes_kernel(cplx* __restrict__ out, const cplx* __restrict__ base, StageArgs a,
+                                   const double* __restrict__ dt_mode, const unsigned char* __restrict__ elem_mode,
+                                   long long off, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long g = off + i;
+  const double dt = dt_mode[elem_mode[i]];
+  cplx s = mkc(0, 0);
+  for (int k = 0; k < a.nk; ++k) {
+    cplx v = a.k[k][g];
+    s.x = fma(a.c[k], v.x, s.x);
+    s.y = fma(a.c[k], v.y, s.y);
+  }
+  cplx b = base[g];
+  out[g] = mkc(fma(dt, s.x, b.x), fma(dt, s.y, b.y));
+}
+void launch_stage_modes(cplx* out, const cplx* base, const StageArgs& a, const double* dt_mode,
+                        const unsigned char* elem_mode, long long off, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  stage_modes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, base, a, dt_mode, elem_mode, off, n);
+}
+
+// y <- src on the elements of accepted modes
+__global__ void masked_copy_kernel(cplx* __restrict__ y, const cplx* __restrict__ src,
+                                   const unsigned char* __restrict__ elem_mode, const int* __restrict__ accept,
+                                   long long off, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (accept[elem_mode[i]]) y[off + i] = src[off + i];
+}
+void launch_masked_copy(cplx* y, const cplx* src, const unsigned char* elem_mode, const int* accept, long long off,
+                        long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  masked_copy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, src, elem_mode, accept, off, n);
+}
+
+// Calc_Err_SPF (cmf2_derivatives.f90:239-283): err_m = sqrt|sum_blocks Tr(rho dS)| with
+// the reference's upper-triangle evaluation; one thread per mode.
+__global__ void spf_err_kernel(const SpfErrDesc* __restrict__ d, int nd, double* err_mode, int nmodes) {
+  const int m = threadIdx.x;
+  if (m >= nmodes) return;
+  double e = 0.0;
+  bool any = false;
+  for (int q = 0; q < nd; ++q) {
+    if (d[q].mode != m) continue;
+    any = true;
+    const int n = d[q].n;
+    const cplx* r = d[q].rho;
+    const cplx* o = d[q].ds;
+    for (int j2 = 0; j2 < n; ++j2) {
+      for (int j1 = 0; j1 < j2; ++j1) {
+        cplx rv = r[j1 + n * j2], ov = o[j1 + n * j2];
+        e += 2.0 * (rv.x * ov.x + rv.y * ov.y);
+      }
+      cplx rv = r[j2 + n * j2], ov = o[j2 + n * j2];
+      e += rv.x * ov.x - rv.y * ov.y;
+    }
+  }
+  err_mode[m] = any ? sqrt(fabs(e)) : 0.0;
+}
+void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, cudaStream_t st) {
+  spf_err_kernel<<<1, 64, 0, st>>>(d, nd, err_mode, nmodes);
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos recurrence with device-resident scalars (cmf2_integration.f90:53-79):
+// Kn <- (Kn - beta_prev * Kp) - alpha * Kj, alpha = Re <Kj|Kn> (two zaxpy in the
+// reference order), then Kn <- Kn / ||Kn||.
+// ---------------------------------------------------------------------------
+__global__ void lan_axpy_kernel(cplx* __restrict__ Kn, const cplx* __restrict__ Kj, const cplx* __restrict__ Kp,
+                                const cplx* __restrict__ dot_alpha, const double* __restrict__ beta_prev,
+                                double* alpha_out, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const double alpha = dot_alpha->x;
+  if (i == 0) *alpha_out = alpha;
+  if (i >= n) return;
+  cplx v = Kn[i];
+  if (Kp) {
+    const double b = *beta_prev;
+    cplx p = Kp[i];
+    v = mkc(fma(-b, p.x, v.x), fma(-b, p.y, v.y));
+  }
+  cplx q = Kj[i];
+  Kn[i] = mkc(fma(-alpha, q.x, v.x), fma(-alpha, q.y, v.y));
+}
+void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
+                     double* alpha_out, long long n, cudaStream_t st) {
+  lan_axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Kn, Kj, Kp, dot_alpha, beta_prev, alpha_out, n);
+}
+
+__global__ void lan_normalize_kernel(cplx* __restrict__ out, const cplx* __restrict__ in, const cplx* __restrict__ nrm2,
+                                     double* beta_out, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const double beta = sqrt(nrm2->x);
+  if (i == 0 && beta_out) *beta_out = beta;
+  if (i >= n) return;
+  const double s = 1.0 / beta;
+  cplx v = in[i];
+  out[i] = mkc(v.x * s, v.y * s);
+}
+void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st) {
+  lan_normalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, in, nrm2, beta_out, n);
 }

@@ -95,7 +95,13 @@ struct SpfDesc {
   long long out_offset;    // offset of the block in the output vector
   int G, n;
   int op_first, op_count;
+  cplx* partial;           // [ntile][2 n^2]: per grid tile phi^H phi and phi^H dphi
+  cplx* X;                 // n x n: (phi^H phi)^-1 phi^H dphi
+  long long block_start;   // first tile block of this descriptor
+  int ntile;
+  int pad;
 };
+#define SPF_TILE 32          // grid rows per block of the tiled SPF derivative
 struct SpfOp {
   const cplx* ophi;        // G x n2
   const cplx* rm;          // n x n2 (ld n)
@@ -124,6 +130,12 @@ struct MatSumSrc {
   cplx coeff;
 };
 
+struct SpfErrDesc {
+  const cplx* ds;          // n x n overlap of the SPF difference
+  const cplx* rho;         // n x n density matrix (frozen)
+  int n, mode;
+};
+
 struct StageArgs {
   const cplx* k[7];
   double c[7];
@@ -133,12 +145,12 @@ struct StageArgs {
 // Launch helpers (kernels.cu)
 void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st,
                  int prec = 0);
-void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st);
+void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec = 0);
 void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st);
 void launch_h1(const H1Desc* d_descs, int ndesc, size_t smem_bytes, cudaStream_t st);
 void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st);
-void launch_spf(const SpfDesc* d_descs, int ndesc, const SpfOp* d_ops, cplx* out, cplx der_factor,
-                size_t smem_bytes, int* d_status, cudaStream_t st);
+void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
+                cplx der_factor, int* d_status, cudaStream_t st);
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
                     long long total, cudaStream_t st);
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st);
@@ -149,4 +161,12 @@ void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* co
 void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, double* evals, double* evecs,
                            int* d_status, cudaStream_t st);
 void launch_matsum(const MatSumDesc* d_descs, int ndesc, const MatSumSrc* d_srcs, cudaStream_t st);
+void launch_stage_modes(cplx* out, const cplx* base, const StageArgs& a, const double* dt_mode,
+                        const unsigned char* elem_mode, long long off, long long n, cudaStream_t st);
+void launch_masked_copy(cplx* y, const cplx* src, const unsigned char* elem_mode, const int* accept, long long off,
+                        long long n, cudaStream_t st);
+void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, cudaStream_t st);
+void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
+                     double* alpha_out, long long n, cudaStream_t st);
+void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st);
 double measure_fp64_tflops();

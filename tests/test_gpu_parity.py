@@ -190,6 +190,29 @@ def test_cmf2_free_running(core_cls):
     _compare(outs, ref, 10 * model.eps_int)
 
 
+@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-10)])
+def test_split_precision_eom(core_cls, prec, tol):
+    """Split-FP32 mode products (1: FP32 sums, 2: compensated FP32 sums; mean
+    fields always compensated) against the FP64 oracle."""
+    for builder, seed in ((lambda: small_lvc(), 21), (lambda: small_qvc(), 22)):
+        model = builder()
+        A, psi = random_state(model, seed=seed)
+        ref_dA, ref_dpsi = Oracle(model).calc_derivs(A, psi, 0.0)
+        dA, dpsi = core_cls(model, precision=prec).calc_derivs(A, psi, 0.0)
+        assert _rel(dA, ref_dA) < tol
+        assert _rel(dpsi, ref_dpsi) < tol
+
+
+def test_split_precision_cmf2_replay(core_cls):
+    """The split-FP32 CMF2 path on the oracle's step sequence stays within 1e-7 of C(t)."""
+    model = small_qvc(tfinal_fs=1.0)
+    A, psi = initial_wavefunction(model)
+    ref, steps, _ = Oracle(model).propagate(A, psi, record_steps=True)
+    gpu = core_cls(model, precision=1)
+    outs, _ = _replay(gpu, model, A, psi, steps, lambda A, psi, t, h: gpu.cmf2_attempt(A, psi, t, h))
+    _compare(outs, ref, 1e-7)
+
+
 def test_gpu_stays_usable_after_error(core_cls):
     """A rejected call (bad method) returns a status and the context keeps working."""
     from macaw_gb300.capi import MctdhError
