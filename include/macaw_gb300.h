@@ -193,6 +193,22 @@ int64_t mctdh_mlp_grad(mctdh_mlp_t *mlp, const float *X, const float *T, int64_t
 int64_t mctdh_mlp_train(mctdh_mlp_t *mlp, const float *X, const float *T, int64_t M, int64_t batch, int64_t epochs,
                         double lr, double *loss);
 
+/* Mean-field extrapolation inside CMF2 (no reference counterpart).  A snapshot is
+ * every density matrix and mean field of the grid modes (E complex entries).
+ * record: 1 start, 0 stop and clear, 2 clear and start; during plain CMF2 steps
+ * each accepted step stores (t0, h, snapshot at t0, snapshot at t0 + h/2).
+ * attach: with a trained network (NULL detaches) the half-step mean fields of
+ * cmf2_base.f90:122-130 come from the network, and a step whose predicted
+ * step-end snapshot differs from the recomputed one by more than tol (relative
+ * 2-norm) is redone with the plain scheme.  tscale: the target scale the network
+ * was trained with. */
+int64_t mctdh_mfx_size(mctdh_ctx_t *ctx, int64_t *E);
+int64_t mctdh_mfx_record(mctdh_ctx_t *ctx, int64_t enable);
+int64_t mctdh_mfx_fetch(mctdh_ctx_t *ctx, int64_t maxrec, double *t0, double *h, double *snap0, double *snaphalf,
+                        int64_t *n);
+int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, double tscale, double tol);
+int64_t mctdh_mfx_stats(mctdh_ctx_t *ctx, int64_t *mlp_steps, int64_t *fallbacks);
+
 /* Last error message of the context (or of the last failed create when ctx is NULL). */
 const char *mctdh_last_error(mctdh_ctx_t *ctx);
 

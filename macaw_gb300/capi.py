@@ -94,6 +94,13 @@ def load_library() -> C.CDLL:
     for name in ("mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
                  "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train"):
         getattr(lib, name).restype = C.c_int64
+    lib.mctdh_mfx_size.argtypes = [vp, I64P]
+    lib.mctdh_mfx_record.argtypes = [vp, C.c_int64]
+    lib.mctdh_mfx_fetch.argtypes = [vp, C.c_int64, DP, DP, DP, DP, I64P]
+    lib.mctdh_mfx_attach.argtypes = [vp, vp, C.c_double, C.c_double]
+    lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P]
+    for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats"):
+        getattr(lib, name).restype = C.c_int64
     lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
                                                  C.c_int64, C.c_void_p]
     lib.mctdh_profile_read.argtypes = [vp, C.c_int64, DP, I64P, DP, DP]
@@ -117,7 +124,8 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
-            "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train"]
+            "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
+            "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats"]
 
 KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
                   "spf_derivative", "elementwise"]
@@ -355,6 +363,37 @@ class GpuCore:
         a, b, d = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self.lib.mctdh_counters(self.h, C.byref(a), C.byref(b), C.byref(d)))
         return dict(launches=a.value, eom=b.value, hb=d.value)
+
+    # -- learned mean-field extrapolation (CMF2) --
+    def mfx_size(self) -> int:
+        e = C.c_int64()
+        self._check(self.lib.mctdh_mfx_size(self.h, C.byref(e)))
+        return e.value
+
+    def mfx_record(self, enable: int = 2):
+        self._check(self.lib.mctdh_mfx_record(self.h, enable))
+
+    def mfx_fetch(self):
+        """Recorded plain-CMF2 steps: (t0[n], h[n], snap0[n, E], snaphalf[n, E])."""
+        n = C.c_int64()
+        self._check(self.lib.mctdh_mfx_fetch(self.h, 0, None, None, None, None, C.byref(n)))
+        E = self.mfx_size()
+        k = n.value
+        t0, h = np.zeros(k), np.zeros(k)
+        s0 = np.zeros((k, E), dtype=np.complex128)
+        sh = np.zeros((k, E), dtype=np.complex128)
+        if k:
+            self._check(self.lib.mctdh_mfx_fetch(self.h, k, _ptr(t0), _ptr(h), _ptr(s0), _ptr(sh), C.byref(n)))
+        return t0, h, s0, sh
+
+    def mfx_attach(self, mlp, tscale: float, tol: float):
+        self._check(self.lib.mctdh_mfx_attach(self.h, mlp.h if mlp is not None else None, tscale, tol))
+        self._mlp_ref = mlp
+
+    def mfx_stats(self):
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.lib.mctdh_mfx_stats(self.h, C.byref(a), C.byref(b)))
+        return dict(mlp_steps=a.value, fallbacks=b.value)
 
     def launch_count(self) -> int:
         return int(self.lib.mctdh_launch_count(self.h))

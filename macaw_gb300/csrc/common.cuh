@@ -38,6 +38,37 @@ __device__ __forceinline__ cplxf cfmaf_(cplxf acc, cplxf a, cplxf b) {
   return acc;
 }
 
+// Exact FP64 -> FP32 hi + lo split and FP32 -> FP64 widening with integer
+// operations only.  On GB300 the F2F conversions run on the FP64 pipe, which is
+// 1/64 of the FP32 rate; these keep the split-precision kernels off that pipe.
+// hi takes the leading 24 mantissa bits (truncated), lo the next 24, so
+// hi + lo = x to 2^-48 relative.  Magnitudes below 2^-126 are flushed to zero.
+__device__ __forceinline__ void split_d2f(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int sign = (unsigned int)(b >> 63) << 31;
+  const int E = (int)((b >> 52) & 0x7FF) - 1023;
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFULL;
+  if (E < -126) { hi = 0.f; lo = 0.f; return; }
+  if (E > 127) { hi = __uint_as_float(sign | 0x7F800000u | (m ? 1u : 0u)); lo = 0.f; return; }
+  hi = __uint_as_float(sign | ((unsigned int)(E + 127) << 23) | (unsigned int)(m >> 29));
+  const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFu);
+  if (rem == 0) { lo = 0.f; return; }
+  const int p = 31 - __clz(rem);              // top bit of the remainder, 0..28
+  const int el = E - 52 + p + 127;            // biased exponent of lo
+  if (el <= 0) { lo = 0.f; return; }
+  const unsigned int mant = (p <= 23) ? (rem << (23 - p)) : (rem >> (p - 23));
+  lo = __uint_as_float(sign | ((unsigned int)el << 23) | (mant & 0x7FFFFFu));
+}
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned int e = (u >> 23) & 0xFF;
+  const unsigned long long m = u & 0x7FFFFFu;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  if (e == 0xFF) return __longlong_as_double((long long)(sign | (0x7FFULL << 52) | (m << 29)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29)));
+}
+
 // Status codes returned through the C-ABI (negative = error).
 enum {
   MCTDH_OK = 0,

@@ -235,6 +235,8 @@ struct PendingEv {
 };
 
 struct Ctx {
+  bool ops_fresh = false;    // operators/mean fields at d_y are in place (time ops_fresh_t)
+  double ops_fresh_t = -1.0;
   bool profiling = false;
   KProf prof[KP_N];
   std::vector<PendingEv> pending;
@@ -1404,17 +1406,145 @@ CmfState& cmf_state(Ctx& c) {
 
 // One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
-double cmf2_attempt(Ctx& c, double t, double hdid) {
+// ---------------------------------------------------------------------------
+// Learned mean-field extrapolation inside CMF2.  A snapshot is every density
+// matrix and mean field of the grid modes (the inputs of Calc_rhom1MF and of the
+// SPF error norm).  With a trained network attached and three accepted step
+// starts in the history, the mean fields at the half step (cmf2_base.f90:122-130)
+// come from the network instead of an EOM evaluation, and the network's
+// prediction for the step end is checked against the mean fields recomputed
+// there: if they differ by more than the tolerance the step is redone with the
+// plain scheme.  The end-of-step evaluation is the next step's first one.
+// ---------------------------------------------------------------------------
+struct MfxState {
+  long long E = 0;
+  std::vector<SnapSeg> segs_h;
+  SnapSeg* segs_d = nullptr;
+  cplx* hist[3] = {};
+  double thist[3] = {0, 0, 0};
+  int nhist = 0, head = 0;         // head: index of the newest entry
+  cplx *half = nullptr, *pred_half = nullptr, *pred_full = nullptr, *now = nullptr, *backup = nullptr;
+  mctdh_mlp* mlp = nullptr;
+  double tscale = 1.0, tol = 0.0;
+  bool recording = false;
+  std::vector<double> rec_t0, rec_h;
+  std::vector<cplx> rec_s0, rec_sh;
+  long long mlp_steps = 0, fallbacks = 0;
+  HoleBatch dh;                     // ||now - pred_full||^2 and ||now||^2
+  RedBatch dr;
+  cplx* dres = nullptr;
+  cplx* diff = nullptr;
+};
+std::map<const Ctx*, MfxState*> g_mfx;
+
+MfxState& mfx_state(Ctx& c) {
+  MfxState*& M = g_mfx[&c];
+  if (M) return *M;
+  M = new MfxState();
+  long long off = 0;
+  const int f = c.nmodes;
+  for (int m : c.modes_dvr) {
+    for (int s = 0; s < c.nstates; ++s) {
+      M->segs_h.push_back(SnapSeg{c.rho[m][s], off});
+      off += (long long)c.m_of(m, s) * c.m_of(m, s);
+    }
+    if (!c.multiset[m]) {
+      M->segs_h.push_back(SnapSeg{c.rho_ave[m], off});
+      off += (long long)c.m_of(m, 0) * c.m_of(m, 0);
+    }
+    for (int k = 0; k < c.noper[m]; ++k) {
+      if (c.is_identity[m + f * k]) continue;
+      M->segs_h.push_back(SnapSeg{c.mf[m][k], off});
+      off += (long long)c.m_of(m, c.oper[m][k][0]) * c.m_of(m, c.oper[m][k][1]);
+    }
+  }
+  M->E = off;
+  M->segs_d = upload_vec(c.ar, M->segs_h);
+  for (auto& h : M->hist) h = c.ar.calloc_c(off);
+  M->half = c.ar.calloc_c(off);
+  M->pred_half = c.ar.calloc_c(off);
+  M->pred_full = c.ar.calloc_c(off);
+  M->now = c.ar.calloc_c(off);
+  M->diff = c.ar.calloc_c(off);
+  M->backup = c.ar.calloc_c(c.ntot);
+  M->dres = c.ar.calloc_c(2);
+  int h1 = M->dh.add(c.ar, M->diff, M->diff, off, 1, 1, 1);
+  int h2 = M->dh.add(c.ar, M->now, M->now, off, 1, 1, 1);
+  M->dh.finalize(c.ar);
+  M->dr.add_term(M->dr.add_target(M->dres, 1, 1, 1, 0), M->dh.h[h1], mkc(1, 0));
+  M->dr.add_term(M->dr.add_target(M->dres + 1, 1, 1, 1, 0), M->dh.h[h2], mkc(1, 0));
+  M->dr.finalize(c.ar);
+  return *M;
+}
+
+void snap_gather(Ctx& c, MfxState& M, cplx* flat) {
+  launch_snap(M.segs_d, (int)M.segs_h.size(), flat, M.E, 0, c.st);
+  c.count();
+}
+
+// relative distance of the recomputed snapshot (M.now) from the predicted one
+double snap_rel_diff(Ctx& c, MfxState& M) {
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  a.k[0] = M.pred_full;
+  a.c[0] = -1.0;
+  a.nk = 1;
+  launch_stage(M.diff, M.now, a, 1.0, M.E, c.st);
+  run_hole(c, M.dh);
+  run_red(c, M.dr);
+  cplx r[2];
+  CK(cudaMemcpyAsync(r, M.dres, sizeof(cplx) * 2, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  return sqrt(r[0].x / std::max(r[1].x, 1e-300));
+}
+
+// Predict the half-step and step-end snapshots from the history for step length h.
+void mfx_predict(Ctx& c, MfxState& M, double h) {
+  const int i2 = M.head, i1 = (M.head + 2) % 3, i0 = (M.head + 1) % 3;
+  const double t0 = M.thist[i0], t1 = M.thist[i1], t2 = M.thist[i2];
+  MfxWeights w;
+  const double th = t2 + 0.5 * h, tf = t2 + h;
+  auto lag = [&](double tau, double* o) {
+    o[0] = (tau - t1) * (tau - t2) / ((t0 - t1) * (t0 - t2));
+    o[1] = (tau - t0) * (tau - t2) / ((t1 - t0) * (t1 - t2));
+    o[2] = (tau - t0) * (tau - t1) / ((t2 - t0) * (t2 - t1));
+  };
+  lag(th, w.h);
+  lag(tf, w.f);
+  float* X = mlp_input_buffer(M.mlp, M.E);
+  launch_mfx_features(M.hist[i0], M.hist[i1], M.hist[i2], (float)((t1 - t0) / (t2 - t1)), (float)(h / (t2 - t1)),
+                      X, M.E, c.st);
+  const float* Y = mlp_forward_on(M.mlp, M.E, c.st);
+  launch_mfx_combine(M.hist[i0], M.hist[i1], M.hist[i2], w, Y, M.tscale, M.pred_half, M.pred_full, M.E, c.st);
+  c.count(6);
+}
+
+// One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
+// max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
+// ops_fresh: the operators and mean fields at d_y are already in place.
+double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh) {
   CmfState& S = cmf_state(c);
   const long long nA = c.naconftot;
-  operators_and_mf(c, c.d_y);                       // cmf2_base.f90:78-87
+  if (!ops_fresh) operators_and_mf(c, c.d_y);       // cmf2_base.f90:78-87
   copy_dev(c, S.B0, c.d_y, nA);                     // A_to_B (DVR only)
   lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);      // :97
   copy_dev(c, S.psiHalf, c.d_y, c.ntot);
   propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf);   // :109-115
   copy_dev(c, S.AHalf, S.BHalf, nA);                // B_to_A  :120
   copy_dev(c, S.AHalf + nA, S.psiHalf + nA, c.dimpsi);
-  operators_and_mf(c, S.AHalf);                     // :122-130
+  MfxState* M = nullptr;
+  auto it = g_mfx.find(&c);
+  if (it != g_mfx.end()) M = it->second;
+  if (use_mlp) {
+    // mean fields at the half step from the network (replaces :122-130)
+    mfx_predict(c, *M, hdid);
+    launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred_half, M->E, 1, c.st);
+    launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
+    c.count(2);
+  } else {
+    operators_and_mf(c, S.AHalf);                   // :122-130
+    if (M && M->recording) snap_gather(c, *M, M->half);
+  }
   copy_dev(c, S.psiHalf2, c.d_y, c.ntot);
   propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2);  // :132-141
   // err_psi = DeltaPsi(AHalf, psiHalf, AHalf, psiHalf2)  (:143)
@@ -1445,15 +1575,62 @@ void cmf2_accept(Ctx& c, double hdid) {
 }
 
 void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, long long* tries) {
+  MfxState* M = nullptr;
+  auto it = g_mfx.find(&c);
+  if (it != g_mfx.end()) M = it->second;
+  // the operators at the step start: recomputed unless the last step's validation left them
+  bool fresh = c.ops_fresh_t == t && c.ops_fresh;
+  if (!fresh) operators_and_mf(c, c.d_y);
+  c.ops_fresh = false;
+  if (M) {
+    // push the step-start snapshot into the history (once per accepted step start)
+    if (M->nhist == 0 || M->thist[M->head] != t) {
+      M->head = (M->head + 1) % 3;
+      snap_gather(c, *M, M->hist[M->head]);
+      M->thist[M->head] = t;
+      M->nhist = std::min(M->nhist + 1, 3);
+    }
+  }
+  bool use_mlp = M && M->mlp && M->nhist == 3;
+  if (use_mlp) copy_dev(c, M->backup, c.d_y, c.ntot);
   double hdid = htry;
+  bool first = true;
   while (true) {
     ++*tries;
-    double error = cmf2_attempt(c, t, hdid);
+    double error = cmf2_attempt(c, t, hdid, use_mlp, first);
+    first = false;
     if (error > 1.0) {
       hdid = hdid / sqrt(error) * 0.95;
       continue;
     }
     cmf2_accept(c, hdid);
+    if (use_mlp) {
+      // validation against the mean fields recomputed at the step end
+      operators_and_mf(c, c.d_y);
+      snap_gather(c, *M, M->now);
+      const double rel = snap_rel_diff(c, *M);
+      if (!(rel <= M->tol)) {
+        ++M->fallbacks;
+        copy_dev(c, c.d_y, M->backup, c.ntot);
+        use_mlp = false;
+        first = false;
+        hdid = htry;
+        continue;
+      }
+      ++M->mlp_steps;
+      c.ops_fresh = true;
+      c.ops_fresh_t = t + hdid;
+    }
+    if (M && M->recording && !use_mlp) {
+      std::vector<cplx> s0(M->E), sh(M->E);
+      CK(cudaMemcpyAsync(s0.data(), M->hist[M->head], sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
+      CK(cudaMemcpyAsync(sh.data(), M->half, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
+      CK(cudaStreamSynchronize(c.st));
+      M->rec_t0.push_back(t);
+      M->rec_h.push_back(hdid);
+      M->rec_s0.insert(M->rec_s0.end(), s0.begin(), s0.end());
+      M->rec_sh.insert(M->rec_sh.end(), sh.begin(), sh.end());
+    }
     double hn = (error > 0.0) ? std::min(hdid / sqrt(error), hdid * 1.5) : hdid * 1.5;
     hn = std::min(hn, c.writetime);
     *hdid_out = hdid;
@@ -1568,6 +1745,11 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
     delete it->second;
     g_cmf.erase(it);
   }
+  auto mi = g_mfx.find(c);
+  if (mi != g_mfx.end()) {
+    delete mi->second;
+    g_mfx.erase(mi);
+  }
   for (auto& kv : c->dots) delete kv.second;
   drain_profile(*c);
   for (auto e : c->evpool) cudaEventDestroy(e);
@@ -1604,6 +1786,9 @@ int64_t mctdh_set_state(mctdh_ctx_t* ctx, const double* A, const double* psi, in
   return guarded(c, [&] {
     upload(*c, c->d_y, A, psi);
     c->fsal_valid = false;
+    c->ops_fresh = false;
+    auto mi = g_mfx.find(c);
+    if (mi != g_mfx.end()) mi->second->nhist = 0;
     if (as_start) copy_dev(*c, c->d_y0, c->d_y, c->ntot);
     CK(cudaStreamSynchronize(c->st));
   });
@@ -1649,7 +1834,8 @@ int64_t mctdh_cmf2_attempt(mctdh_ctx_t* ctx, double* A, double* psi, double t, d
   Ctx* c = ctx->c;
   return guarded(c, [&] {
     upload(*c, c->d_y, A, psi);
-    *error = cmf2_attempt(*c, t, h);
+    c->ops_fresh = false;
+    *error = cmf2_attempt(*c, t, h, false, false);
     cmf2_accept(*c, h);
     download(*c, c->d_y, A, psi);
   });
@@ -1722,6 +1908,66 @@ int64_t mctdh_step(mctdh_ctx_t* ctx, int64_t int_type, double t, double htry, do
       throw StatusError(MCTDH_EUNSUPPORTED, "integrator type not supported");
     }
     if (nattempts) *nattempts = att;
+  });
+}
+
+int64_t mctdh_mfx_size(mctdh_ctx_t* ctx, int64_t* E) {
+  if (!ctx || !E) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] { *E = mfx_state(*c).E; });
+}
+
+int64_t mctdh_mfx_record(mctdh_ctx_t* ctx, int64_t enable) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    if (enable == 2 || enable == 0) {
+      M.rec_t0.clear();
+      M.rec_h.clear();
+      M.rec_s0.clear();
+      M.rec_sh.clear();
+    }
+    M.recording = enable != 0;
+  });
+}
+
+int64_t mctdh_mfx_fetch(mctdh_ctx_t* ctx, int64_t maxrec, double* t0, double* h, double* snap0, double* snaphalf,
+                        int64_t* n) {
+  if (!ctx || !n) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    const long long nr = (long long)M.rec_t0.size();
+    *n = nr;
+    const long long k = std::min<long long>(nr, maxrec);
+    for (long long i = 0; i < k; ++i) {
+      if (t0) t0[i] = M.rec_t0[i];
+      if (h) h[i] = M.rec_h[i];
+    }
+    if (snap0) memcpy(snap0, M.rec_s0.data(), sizeof(cplx) * M.E * k);
+    if (snaphalf) memcpy(snaphalf, M.rec_sh.data(), sizeof(cplx) * M.E * k);
+  });
+}
+
+int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, double tscale, double tol) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    M.mlp = mlp;
+    M.tscale = tscale;
+    M.tol = tol;
+  });
+}
+
+int64_t mctdh_mfx_stats(mctdh_ctx_t* ctx, int64_t* mlp_steps, int64_t* fallbacks) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    if (mlp_steps) *mlp_steps = M.mlp_steps;
+    if (fallbacks) *fallbacks = M.fallbacks;
   });
 }
 

@@ -60,9 +60,11 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
     if (PREC == 0) {
       Ms[jo + MAXN * ji] = v;
     } else {
-      const float hx = (float)v.x, hy = (float)v.y;
+      float hx, lx, hy, ly;
+      split_d2f(v.x, hx, lx);
+      split_d2f(v.y, hy, ly);
       Mh[jo + MAXN * ji] = make_float2(hx, hy);
-      Ml[jo + MAXN * ji] = make_float2((float)(v.x - (double)hx), (float)(v.y - (double)hy));
+      Ml[jo + MAXN * ji] = make_float2(lx, ly);
     }
   }
   __syncthreads();
@@ -91,10 +93,13 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
 #pragma unroll
     for (int j = 0; j < MAXN; ++j) {
       cplx v = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
-      const float hx = (float)v.x, hy = (float)v.y;
+      float hx, lx, hy, ly;
+      split_d2f(v.x, hx, lx);
+      split_d2f(v.y, hy, ly);
       xh[j] = make_float2(hx, hy);
-      xl[j] = make_float2((float)(v.x - (double)hx), (float)(v.y - (double)hy));
+      xl[j] = make_float2(lx, ly);
     }
+    const bool unit_alpha = (alpha.x == 1.0 && alpha.y == 0.0);
     for (int jo = 0; jo < nout; ++jo) {
       cplx accd;
       if (PREC == 1) {
@@ -107,7 +112,7 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
             acc = cfmaf_(acc, mh, xl[j]);
             acc = cfmaf_(acc, ml, xh[j]);
           }
-        accd = mkc((double)acc.x, (double)acc.y);
+        accd = mkc(f2d_exact(acc.x), f2d_exact(acc.y));
       } else {
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
 #pragma unroll
@@ -120,9 +125,9 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
             df_fma(ih, il, mh.x, ml.x, xh[j].y, xl[j].y);
             df_fma(ih, il, mh.y, ml.y, xh[j].x, xl[j].x);
           }
-        accd = mkc((double)rh + (double)rl, (double)ih + (double)il);
+        accd = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
       }
-      cplx v = cmul(alpha, accd);
+      cplx v = unit_alpha ? accd : cmul(alpha, accd);
       if (d.accumulate) v = cadd(v, y0[L * jo]);
       y0[L * jo] = v;
     }
@@ -174,6 +179,8 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   __shared__ int s_di;
   __shared__ cplx Xs[HOLE_TILE * MAXN_SPF];
   __shared__ cplx Ys[HOLE_TILE * MAXN_SPF];
+  float4* Xf = reinterpret_cast<float4*>(Xs);   // PREC 2: (re hi, im hi, re lo, im lo)
+  float4* Yf = reinterpret_cast<float4*>(Ys);
   if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
   __syncthreads();
   const HoleDesc& d = descs[s_di];
@@ -200,14 +207,28 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
       long long p = p0 + q;
       cplx v = mkc(0, 0);
       if (p < nfib) { long long l = p % L, r = p / L; v = d.X[l + L * (j + (long long)n1 * r)]; }
-      Xs[q * MAXN_SPF + j] = v;
+      if (PREC == 0) {
+        Xs[q * MAXN_SPF + j] = v;
+      } else {
+        float4 w;
+        split_d2f(v.x, w.x, w.z);
+        split_d2f(v.y, w.y, w.w);
+        Xf[q * MAXN_SPF + j] = w;
+      }
     }
     for (int e = tid; e < HOLE_TILE * n2; e += HOLE_THREADS) {
       int q = e % HOLE_TILE, j = e / HOLE_TILE;
       long long p = p0 + q;
       cplx v = mkc(0, 0);
       if (p < nfib) { long long l = p % L, r = p / L; v = d.Y[l + L * (j + (long long)n2 * r)]; }
-      Ys[q * MAXN_SPF + j] = v;
+      if (PREC == 0) {
+        Ys[q * MAXN_SPF + j] = v;
+      } else {
+        float4 w;
+        split_d2f(v.x, w.x, w.z);
+        split_d2f(v.y, w.y, w.w);
+        Yf[q * MAXN_SPF + j] = w;
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -223,18 +244,15 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
       }
       const int j1 = pr % n1, j2 = pr / n1;
       for (int q = q0; q < HOLE_TILE; q += qs) {
-        const cplx x = Xs[q * MAXN_SPF + j1], y = Ys[q * MAXN_SPF + j2];
         if (PREC == 0) {
-          cfma_conj(acc[k], x, y);
+          cfma_conj(acc[k], Xs[q * MAXN_SPF + j1], Ys[q * MAXN_SPF + j2]);
         } else {
           // conj(x) y: re = xr yr + xi yi, im = xr yi - xi yr
-          const float xrh = (float)x.x, xih = (float)x.y, yrh = (float)y.x, yih = (float)y.y;
-          const float xrl = (float)(x.x - (double)xrh), xil = (float)(x.y - (double)xih);
-          const float yrl = (float)(y.x - (double)yrh), yil = (float)(y.y - (double)yih);
-          df_fma(ah[k][0], al[k][0], xrh, xrl, yrh, yrl);
-          df_fma(ah[k][0], al[k][0], xih, xil, yih, yil);
-          df_fma(ah[k][1], al[k][1], xrh, xrl, yih, yil);
-          df_fma(ah[k][1], al[k][1], -xih, -xil, yrh, yrl);
+          const float4 x = Xf[q * MAXN_SPF + j1], y = Yf[q * MAXN_SPF + j2];
+          df_fma(ah[k][0], al[k][0], x.x, x.z, y.x, y.z);
+          df_fma(ah[k][0], al[k][0], x.y, x.w, y.y, y.w);
+          df_fma(ah[k][1], al[k][1], x.x, x.z, y.y, y.w);
+          df_fma(ah[k][1], al[k][1], -x.y, -x.w, y.x, y.z);
         }
       }
     }
@@ -243,7 +261,7 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   if (PREC != 0) {
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      acc[k] = mkc((double)ah[k][0] + (double)al[k][0], (double)ah[k][1] + (double)al[k][1]);
+      acc[k] = mkc(f2d_exact(ah[k][0]) + f2d_exact(al[k][0]), f2d_exact(ah[k][1]) + f2d_exact(al[k][1]));
   }
   cplx* out = d.partial + (long long)b * npairs;
   if (small) {
@@ -602,34 +620,40 @@ __global__ void spf_solve_kernel(const SpfDesc* __restrict__ descs, int* status)
     if (which == 0) S[j1 + ld * j2] = s; else O[j1 + ld * j2] = s;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    bool fail = false;
-    for (int j = 0; j < n; ++j) {
+  // zposv('U'): S = U^H U by columns (row j of U finished by all threads), then
+  // one thread per right-hand side for the two triangular solves
+  __shared__ int s_fail;
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (threadIdx.x == 0) {
       double djj = S[j + ld * j].x;
       for (int k = 0; k < j; ++k) djj -= cabs2(S[k + ld * j]);
-      if (!(djj > 0.0)) { fail = true; djj = 1e-300; }
-      const double ujj = sqrt(djj);
-      S[j + ld * j] = mkc(ujj, 0.0);
-      for (int i = j + 1; i < n; ++i) {
-        cplx sji = S[j + ld * i];
-        for (int k = 0; k < j; ++k) sji = csub(sji, cmul(cconj(S[k + ld * j]), S[k + ld * i]));
-        S[j + ld * i] = cscale(sji, 1.0 / ujj);
-      }
+      if (!(djj > 0.0)) { s_fail = 1; djj = 1e-300; }
+      S[j + ld * j] = mkc(sqrt(djj), 0.0);
     }
-    for (int c = 0; c < n; ++c) {
-      for (int i = 0; i < n; ++i) {
-        cplx v = O[i + ld * c];
-        for (int k = 0; k < i; ++k) v = csub(v, cmul(cconj(S[k + ld * i]), O[k + ld * c]));
-        O[i + ld * c] = cscale(v, 1.0 / S[i + ld * i].x);
-      }
-      for (int i = n - 1; i >= 0; --i) {
-        cplx v = O[i + ld * c];
-        for (int k = i + 1; k < n; ++k) v = csub(v, cmul(S[i + ld * k], O[k + ld * c]));
-        O[i + ld * c] = cscale(v, 1.0 / S[i + ld * i].x);
-      }
+    __syncthreads();
+    const double inv = 1.0 / S[j + ld * j].x;
+    for (int i = j + 1 + (int)threadIdx.x; i < n; i += blockDim.x) {
+      cplx sji = S[j + ld * i];
+      for (int k = 0; k < j; ++k) sji = csub(sji, cmul(cconj(S[k + ld * j]), S[k + ld * i]));
+      S[j + ld * i] = cscale(sji, inv);
     }
-    if (fail) atomicOr(status, DEVST_CHOL_FAIL);
+    __syncthreads();
   }
+  for (int cidx = threadIdx.x; cidx < n; cidx += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      cplx v = O[i + ld * cidx];
+      for (int k = 0; k < i; ++k) v = csub(v, cmul(cconj(S[k + ld * i]), O[k + ld * cidx]));
+      O[i + ld * cidx] = cscale(v, 1.0 / S[i + ld * i].x);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      cplx v = O[i + ld * cidx];
+      for (int k = i + 1; k < n; ++k) v = csub(v, cmul(S[i + ld * k], O[k + ld * cidx]));
+      O[i + ld * cidx] = cscale(v, 1.0 / S[i + ld * i].x);
+    }
+  }
+  if (threadIdx.x == 0 && s_fail) atomicOr(status, DEVST_CHOL_FAIL);
   __syncthreads();
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) d.X[e] = O[(e % n) + ld * (e / n)];
 }
@@ -903,4 +927,70 @@ __global__ void lan_normalize_kernel(cplx* __restrict__ out, const cplx* __restr
 }
 void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st) {
   lan_normalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, in, nrm2, beta_out, n);
+}
+
+// ---------------------------------------------------------------------------
+// Mean-field snapshots for the learned extrapolator: all density matrices and
+// mean fields of the grid modes gathered into one complex vector (and back).
+// ---------------------------------------------------------------------------
+__global__ void snap_gather_kernel(const SnapSeg* __restrict__ segs, int nseg, cplx* __restrict__ flat, long long E,
+                                   int scatter) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (segs[mid].offset <= i) lo = mid; else hi = mid - 1;
+  }
+  cplx* p = segs[lo].ptr + (i - segs[lo].offset);
+  if (scatter) *p = flat[i]; else flat[i] = *p;
+}
+void launch_snap(const SnapSeg* segs, int nseg, cplx* flat, long long E, int scatter, cudaStream_t st) {
+  if (E <= 0) return;
+  snap_gather_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(segs, nseg, flat, E, scatter);
+}
+
+// Features of every entry from its three last values z0, z1, z2 (times t0<t1<t2):
+// z_i / s (s = max |z_i|), (t1-t0)/(t2-t1), h/(t2-t1).
+__global__ void mfx_features_kernel(const cplx* __restrict__ z0, const cplx* __restrict__ z1,
+                                    const cplx* __restrict__ z2, float r1, float r2, float* __restrict__ X,
+                                    long long E) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const cplx a = z0[i], b = z1[i], c = z2[i];
+  double s = fmax(sqrt(cabs2(a)), fmax(sqrt(cabs2(b)), sqrt(cabs2(c))));
+  s = fmax(s, 1e-300);
+  const double q = 1.0 / s;
+  float* x = X + 8 * i;
+  x[0] = (float)(a.x * q); x[1] = (float)(a.y * q);
+  x[2] = (float)(b.x * q); x[3] = (float)(b.y * q);
+  x[4] = (float)(c.x * q); x[5] = (float)(c.y * q);
+  x[6] = r1; x[7] = r2;
+}
+void launch_mfx_features(const cplx* z0, const cplx* z1, const cplx* z2, float r1, float r2, float* X, long long E,
+                         cudaStream_t st) {
+  if (E <= 0) return;
+  mfx_features_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(z0, z1, z2, r1, r2, X, E);
+}
+
+// z(tau) = quadratic extrapolation + s * tscale * y for the half step and the step end
+__global__ void mfx_combine_kernel(const cplx* __restrict__ z0, const cplx* __restrict__ z1,
+                                   const cplx* __restrict__ z2, MfxWeights w, const float* __restrict__ Y,
+                                   double tscale, cplx* __restrict__ half, cplx* __restrict__ full, long long E) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const cplx a = z0[i], b = z1[i], c = z2[i];
+  double s = fmax(sqrt(cabs2(a)), fmax(sqrt(cabs2(b)), sqrt(cabs2(c))));
+  s = fmax(s, 1e-300);
+  const float* y = Y + 4 * i;
+  const double f = s * tscale;
+  half[i] = mkc(w.h[0] * a.x + w.h[1] * b.x + w.h[2] * c.x + f * y[0],
+                w.h[0] * a.y + w.h[1] * b.y + w.h[2] * c.y + f * y[1]);
+  full[i] = mkc(w.f[0] * a.x + w.f[1] * b.x + w.f[2] * c.x + f * y[2],
+                w.f[0] * a.y + w.f[1] * b.y + w.f[2] * c.y + f * y[3]);
+}
+void launch_mfx_combine(const cplx* z0, const cplx* z1, const cplx* z2, const MfxWeights& w, const float* Y,
+                        double tscale, cplx* half, cplx* full, long long E, cudaStream_t st) {
+  if (E <= 0) return;
+  mfx_combine_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(z0, z1, z2, w, Y, tscale, half, full, E);
 }

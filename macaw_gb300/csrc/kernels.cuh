@@ -136,6 +136,14 @@ struct SpfErrDesc {
   int n, mode;
 };
 
+struct SnapSeg {
+  cplx* ptr;               // matrix storage
+  long long offset;        // first index in the flat snapshot
+};
+struct MfxWeights {
+  double h[3], f[3];       // Lagrange weights of t0, t1, t2 at the half step and the step end
+};
+
 struct StageArgs {
   const cplx* k[7];
   double c[7];
@@ -169,4 +177,13 @@ void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, c
 void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
                      double* alpha_out, long long n, cudaStream_t st);
 void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st);
+void launch_snap(const SnapSeg* segs, int nseg, cplx* flat, long long E, int scatter, cudaStream_t st);
+void launch_mfx_features(const cplx* z0, const cplx* z1, const cplx* z2, float r1, float r2, float* X, long long E,
+                         cudaStream_t st);
+void launch_mfx_combine(const cplx* z0, const cplx* z1, const cplx* z2, const MfxWeights& w, const float* Y,
+                        double tscale, cplx* half, cplx* full, long long E, cudaStream_t st);
+// MLP forward on a given stream (mlp.cu): input buffer for M rows, then the output
+struct mctdh_mlp;
+float* mlp_input_buffer(mctdh_mlp* m, long long M);
+const float* mlp_forward_on(mctdh_mlp* m, long long M, cudaStream_t st);
 double measure_fp64_tflops();

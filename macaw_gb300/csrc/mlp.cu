@@ -11,7 +11,7 @@
 #include <vector>
 
 #include "../../include/macaw_gb300.h"
-#include "common.cuh"
+#include "kernels.cuh"
 
 void mctdh_set_global_error(const char* msg);
 
@@ -265,7 +265,8 @@ struct mctdh_mlp {
     part = (double*)alloc(sizeof(double) * (r * L.back().N / 256 + 2));
     cap = r;
   }
-  void forward(long long M) {
+  void forward(long long M) { forward_on(M, st); }
+  void forward_on(long long M, cudaStream_t st) {
     const int nl = (int)L.size();
     for (int i = 0; i < nl; ++i) {
       dim3 grid((L[i].N + GT - 1) / GT, (unsigned)((M + GT - 1) / GT));
@@ -503,3 +504,13 @@ int64_t mctdh_mlp_train(mctdh_mlp_t* m, const float* X, const float* T, int64_t 
 }
 
 }  // extern "C"
+
+float* mlp_input_buffer(mctdh_mlp* m, long long M) {
+  m->ensure(M);
+  return m->X;
+}
+
+const float* mlp_forward_on(mctdh_mlp* m, long long M, cudaStream_t st) {
+  m->forward_on(M, st);
+  return m->Y;
+}

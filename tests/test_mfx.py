@@ -1,0 +1,60 @@
+"""Learned mean-field extrapolation in CMF2: training data from plain CMF2 runs,
+the network's gain over the method without it, and the assisted propagation.
+
+Gain is measured two ways: (1) on held-out steps, the residual the network
+leaves is smaller than the residual of the quadratic extrapolation it corrects;
+(2) CMF2 with the network evaluates fewer mean fields per simulated fs than plain
+CMF2, while C(t) and the populations stay within 1e-6 / 1e-5 of plain CMF2.
+"""
+import numpy as np
+import pytest
+
+from macaw_gb300.model import initial_wavefunction, INT_CMF2, AU2FS
+from tests.helpers import small_qvc
+
+pytestmark = pytest.mark.gpu
+
+T_FS = 1.5
+
+
+def _run(core, model, A0, psi0, t_end):
+    core.set_state(A0, psi0, as_start=True)
+    t, h = 0.0, model.tout * model.eps_int
+    c0 = core.counters()["eom"]
+    while t < t_end:
+        hdid, h, _ = core.step(INT_CMF2, t, h)
+        t += hdid
+    return t, core.counters()["eom"] - c0
+
+
+def test_extrapolator_gain_and_assisted_cmf2():
+    from macaw_gb300.capi import GpuCore
+    from macaw_gb300 import mfx
+    model = small_qvc(tfinal_fs=T_FS)
+    A0, psi0 = initial_wavefunction(model)
+    plain = GpuCore(model)
+    plain.mfx_record(2)
+    t_plain, eom_plain = _run(plain, model, A0, psi0, T_FS / AU2FS)
+    t0, h, s0, sh = plain.mfx_fetch()
+    assert len(t0) > 20
+    X, R, k = mfx.build_dataset(t0, h, s0, sh)
+    cut = np.quantile(k, 0.7)
+    tr, te = k <= cut, k > cut
+    net, tscale, loss = mfx.train(X[tr], R[tr], epochs=30, batch=4096, lr=1e-3)
+    base, left = mfx.prediction_errors(net, tscale, X[te], R[te])
+    assert left[0] < base[0] and left[2] < base[2], (base, left)
+
+    # assisted propagation over the same interval, then C(t) at a common time
+    assisted = GpuCore(model)
+    assisted.mfx_attach(net, tscale, tol=model.eps_int)
+    t_mlp, eom_mlp = _run(assisted, model, A0, psi0, T_FS / AU2FS)
+    stats = assisted.mfx_stats()
+    assert stats["mlp_steps"] > 0
+    assert eom_mlp / t_mlp < eom_plain / t_plain
+    tc = max(t_plain, t_mlp) + 0.05 / AU2FS
+    outs = []
+    for core, t in ((plain, t_plain), (assisted, t_mlp)):
+        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, tc, t, model.tout * 0.01)
+        outs.append(core.observables(tt))
+    assert abs(outs[0]["auto"] - outs[1]["auto"]) < 1e-6
+    assert np.abs(outs[0]["pop"] - outs[1]["pop"]).max() < 1e-5
