@@ -38,6 +38,7 @@ METRIC = "simulated fs/s & EOM evals/s vs plain FP64 GPU path at |dC(t)|<=1e-6"
 WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/state, CMF2+Lanczos"
 EPS_CMF = 1e-5
 PRE_FS = 1.0
+MFX_EPOCHS = 12
 ACC_FS = 0.5   # interval over which the split path is compared with the FP64 path
 REF_STEP_FS = 0.1   # CMF2 step length the reference arm times (steady-state steps are of this order)
 
@@ -200,14 +201,19 @@ def timed_steps(core, t, h, steps, l2, torch):
     return t, h, ms_total, fs_total, hdids
 
 
-def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile):
+def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mfx_net=None):
     from macaw_gb300.capi import GpuCore
     A0, psi0, A1, psi1 = state
     core = GpuCore(model, precision=precision)
     core.set_state(A0, psi0, as_start=True)
     core.set_state(A1, psi1, as_start=False)
+    warm = args.warmup
+    if mfx_net is not None:
+        # the extrapolator needs five accepted step starts of history
+        core.mfx_attach(*mfx_net, tol=model.eps_int)
+        warm = max(warm, 6)
     t, h = t0, h0
-    for _ in range(args.warmup):
+    for _ in range(warm):
         hdid, h, _ = core.step(INT_CMF2, t, h)
         t += hdid
     c0 = core.counters()
@@ -238,29 +244,43 @@ def run_gpu(args):
     # propagate 1 fs untimed with the FP64 path; both arms start from that state
     pre = GpuCore(model, precision=0)
     pre.set_state(A0, psi0, as_start=True)
+    pre.mfx_record(2)   # the untimed FP64 steps are the extrapolator's training data
     t1, h1, _, _, _ = pre.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
     A1, psi1 = pre.get_state()
+    from macaw_gb300 import mfx
+    tr0 = time.perf_counter()
+    X, R, ks = mfx.build_dataset(*pre.mfx_fetch())
+    net, fscale, tscale, tr_loss = mfx.train(X, R, steps=ks, epochs=MFX_EPOCHS)
+    train_s = time.perf_counter() - tr0
     pre.close()
     state = (A0, psi0, A1, psi1)
     with ClockSampler(torch.cuda.current_device()) as clk:
         ref_core, ref = run_arm(model, 0, state, t1, h1, args, l2, torch, tdist, profile=False)
         mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=True)
-    # accuracy of the split path against the plain FP64 path: both propagate the same
-    # state over the same output interval; C(t) and populations are compared there
+        mfx_core, mfxr = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=False,
+                                 mfx_net=(net, fscale, tscale))
+    # accuracy against the plain FP64 path: every arm propagates the same state over
+    # the same output interval; C(t) and populations are compared there
     cmp = {}
-    for name, core in (("fp64", ref_core), ("mixed", mix_core)):
+    for name, core in (("fp64", ref_core), ("mixed", mix_core), ("mfx", mfx_core)):
         core.set_state(A1, psi1, as_start=False)
         tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + ACC_FS / AU2FS, t1, h1)
         cmp[name] = core.observables(tt)
     dC = abs(cmp["mixed"]["auto"] - cmp["fp64"]["auto"])
     dpop = float(np.abs(cmp["mixed"]["pop"] - cmp["fp64"]["pop"]).max())
+    mfx_stats = mfx_core.mfx_stats()
     ms_total, fs_total = mix["ms"], mix["fs"]
     if tdist is not None:
         tt = torch.tensor([ms_total, ref["ms"]], device="cuda", dtype=torch.float64)
         tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
         ms_total, ref["ms"] = float(tt[0].item()), float(tt[1].item())
+    if tdist is not None:
+        tt = torch.tensor([mfxr["ms"]], device="cuda", dtype=torch.float64)
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        mfxr["ms"] = float(tt[0].item())
     value = ws * fs_total / (ms_total * 1e-3)
     fp64_value = ws * ref["fs"] / (ref["ms"] * 1e-3)
+    mfx_value = ws * mfxr["fs"] / (mfxr["ms"] * 1e-3)
 
     # e2e: the reference-facing host-buffer call (mctdh_cmf2) with pinned buffers,
     # host<->device copies of A and psi inside every step
@@ -311,6 +331,17 @@ def run_gpu(args):
                       "step_fs_mean": statistics.mean(ref["hdids"])},
         "speedup_vs_fp64_path": value / fp64_value,
         "accuracy_vs_fp64_path": {"dC": dC, "dpop": dpop, "over_fs": ACC_FS, "from_fs": t1 * AU2FS},
+        "mfx_path": {"value": mfx_value, "unit": "fs/s", "ms_per_step": mfxr["ms"] / args.steps,
+                     "step_fs_mean": statistics.mean(mfxr["hdids"]),
+                     "speedup_vs_fp64_path": mfx_value / fp64_value,
+                     "accuracy_vs_fp64_path": {
+                         "dC": abs(cmp["mfx"]["auto"] - cmp["fp64"]["auto"]),
+                         "dpop": float(np.abs(cmp["mfx"]["pop"] - cmp["fp64"]["pop"]).max())},
+                     "eom_per_s": mfxr["eom"] / (mfxr["ms"] * 1e-3),
+                     "extrapolated_steps": mfx_stats["mlp_steps"], "fallbacks": mfx_stats["fallbacks"],
+                     "training": {"rows": int(len(X)), "epochs": MFX_EPOCHS, "loss": tr_loss,
+                                  "seconds": train_s,
+                                  "data": f"the untimed FP64 CMF2 steps from 0 to {PRE_FS} fs"}},
         "eom_per_s": mix["eom"] / (ms_total * 1e-3), "hb_per_s": mix["hb"] / (ms_total * 1e-3),
         "e2e": {"value": e2e_fs / e2e_s, "unit": "fs/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
@@ -333,6 +364,7 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     ref_core.close()
     mix_core.close()
+    mfx_core.close()
     if tdist is not None:
         tdist.destroy_process_group()
     return 0

@@ -198,15 +198,23 @@ int64_t mctdh_mlp_train(mctdh_mlp_t *mlp, const float *X, const float *T, int64_
  * record: 1 start, 0 stop and clear, 2 clear and start; during plain CMF2 steps
  * each accepted step stores (t0, h, snapshot at t0, snapshot at t0 + h/2).
  * attach: with a trained network (NULL detaches) the half-step mean fields of
- * cmf2_base.f90:122-130 come from the network, and a step whose predicted
+ * cmf2_base.f90:122-130 come from the quartic extrapolation of the last five
+ * step-start snapshots plus the network's residual, and a step whose predicted
  * step-end snapshot differs from the recomputed one by more than tol (relative
- * 2-norm) is redone with the plain scheme.  tscale: the target scale the network
- * was trained with. */
+ * 2-norm) is redone with the plain scheme.  The network maps
+ * MCTDH_MFX_NFEAT inputs per entry (Newton increments of orders 1-4 through the
+ * last five step starts at the half step and the step end, Re/Im, divided by the
+ * RMS of the first-order step-end increment, then four step-length ratios; each
+ * column divided by fscale[j]) to MCTDH_MFX_NOUT outputs (Re/Im residual at the
+ * half step and the step end, in units of that RMS times tscale[j]). */
+#define MCTDH_MFX_NFEAT 20
+#define MCTDH_MFX_NOUT 4
 int64_t mctdh_mfx_size(mctdh_ctx_t *ctx, int64_t *E);
 int64_t mctdh_mfx_record(mctdh_ctx_t *ctx, int64_t enable);
 int64_t mctdh_mfx_fetch(mctdh_ctx_t *ctx, int64_t maxrec, double *t0, double *h, double *snap0, double *snaphalf,
                         int64_t *n);
-int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, double tscale, double tol);
+int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, const double *fscale, const double *tscale,
+                         double tol);
 int64_t mctdh_mfx_stats(mctdh_ctx_t *ctx, int64_t *mlp_steps, int64_t *fallbacks);
 
 /* Last error message of the context (or of the last failed create when ctx is NULL). */

@@ -97,7 +97,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_mfx_size.argtypes = [vp, I64P]
     lib.mctdh_mfx_record.argtypes = [vp, C.c_int64]
     lib.mctdh_mfx_fetch.argtypes = [vp, C.c_int64, DP, DP, DP, DP, I64P]
-    lib.mctdh_mfx_attach.argtypes = [vp, vp, C.c_double, C.c_double]
+    lib.mctdh_mfx_attach.argtypes = [vp, vp, DP, DP, C.c_double]
     lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P]
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats"):
         getattr(lib, name).restype = C.c_int64
@@ -128,7 +128,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats"]
 
 KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
-                  "spf_derivative", "elementwise"]
+                  "spf_derivative", "elementwise", "gaussian_block"]
 
 
 def _i64(a) -> np.ndarray:
@@ -193,6 +193,11 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
     gwpa = getattr(model, "gwpa", None)
     if gwpa is None or gwpa.size == 0:
         gwpa = np.zeros(1)
+    else:
+        # GWPa(maxdof, ns00max, nmodgwp): pad the DOF axis to maxdof
+        g = np.zeros((maxdof, max(int(model.ns00max), 1), gwpa.shape[2]))
+        g[:gwpa.shape[0], :gwpa.shape[1], :] = gwpa
+        gwpa = g
     s = Setup()
     s.nstates, s.nmodes, s.ndof, s.nham, s.maxdof = ns, nm, nd, model.nham, maxdof
     s.nspf = I(model.nspf.reshape(-1, order="F"))
@@ -386,8 +391,17 @@ class GpuCore:
             self._check(self.lib.mctdh_mfx_fetch(self.h, k, _ptr(t0), _ptr(h), _ptr(s0), _ptr(sh), C.byref(n)))
         return t0, h, s0, sh
 
-    def mfx_attach(self, mlp, tscale: float, tol: float):
-        self._check(self.lib.mctdh_mfx_attach(self.h, mlp.h if mlp is not None else None, tscale, tol))
+    def mfx_attach(self, mlp, fscale, tscale, tol: float):
+        """Attach a trained extrapolator (None detaches) with its input column scales
+        (20) and output column scales (4)."""
+        if mlp is None:
+            self._check(self.lib.mctdh_mfx_attach(self.h, None, None, None, tol))
+        else:
+            fs = np.ascontiguousarray(fscale, dtype=np.float64)
+            ts = np.ascontiguousarray(tscale, dtype=np.float64)
+            if fs.size != 20 or ts.size != 4:
+                raise ValueError("fscale needs 20 entries and tscale 4")
+            self._check(self.lib.mctdh_mfx_attach(self.h, mlp.h, fs.ctypes.data_as(DP), ts.ctypes.data_as(DP), tol))
         self._mlp_ref = mlp
 
     def mfx_stats(self):

@@ -211,6 +211,8 @@ struct HoleRef {
 struct OvlPlan {
   HoleBatch spf_holes;           // SPF overlap matrices
   RedBatch spf_red;
+  std::vector<GwpOvlDesc> gwp_h; // Gaussian-mode overlap matrices
+  GwpOvlDesc* gwp_d = nullptr;
   std::vector<ProdBatch> chain;  // one batch per mode step
   HoleBatch dots;
   RedBatch dot_red;
@@ -223,7 +225,7 @@ struct DotPlan {
   cplx* res = nullptr;
 };
 
-enum { KP_PROD, KP_HOLE, KP_RED, KP_H1, KP_REGINV, KP_TERMSUM, KP_SPF, KP_ELEM, KP_N };
+enum { KP_PROD, KP_HOLE, KP_RED, KP_H1, KP_REGINV, KP_TERMSUM, KP_SPF, KP_ELEM, KP_GWP, KP_N };
 struct KProf {
   double ms = 0, flops = 0, bytes = 0;
   long long launches = 0;
@@ -291,6 +293,7 @@ struct Ctx {
   std::vector<H1Desc> h1_h;
   H1Desc* h1_d = nullptr;
   size_t h1_smem = 0;
+  int h1_maxn2 = 0;
   std::vector<ProdBatch> chains;  // per depth
   HoleBatch holes;       // mean-field contractions of the general terms
   HoleBatch rho_holes;   // density matrices (FP64 always)
@@ -338,6 +341,31 @@ struct Ctx {
   std::vector<double> lan_evals, lan_evecs;
   cplx* d_coef = nullptr;
 
+  // Gaussian (G-MCTDH) modes
+  std::vector<int> modes_gwp;
+  std::vector<int> gwp_of;                            // mode -> index among Gaussian modes (-1: grid)
+  double* gwpa_d = nullptr;                           // GWPa(lda, ns00max, nmodgwp)
+  int gwp_lda = 0, ns00max = 0;
+  std::vector<std::vector<std::vector<cplx*>>> s00;   // [i][s1][s2] overlap matrices
+  std::vector<std::vector<cplx*>> s00m1;              // [i][s] Tikhonov inverses
+  std::vector<GwpOvlDesc> gs_h;
+  GwpOvlDesc* gs_d = nullptr;
+  std::vector<RegInvDesc> gsreg_h;
+  RegInvDesc* gsreg_d = nullptr;
+  std::vector<GwpH1Desc> gh1_h;
+  GwpH1Desc* gh1_d = nullptr;
+  std::vector<ProdBatch> gwp_rho_chain;               // S-weighted A for the density matrices
+  std::vector<GwpCYDesc> cy_h;
+  GwpCYDesc* cy_d = nullptr;
+  std::vector<GwpYOp> yop_h;
+  GwpYOp* yop_d = nullptr;
+  int cy_maxG = 0, cy_maxn = 0;
+  std::vector<std::vector<cplx*>> tau;                // [i][s]
+  cplx* d_adot = nullptr;                             // f * sum_t ae_t H_t A before the corrections
+  cplx* d_dA = nullptr;                               // dA after S^-1 and tau
+  std::vector<ProdBatch> gwp_sinv;                    // S^-1 products, one batch per Gaussian mode
+  std::vector<ProdBatch> gwp_tau;                     // -tau x_m A, one batch per Gaussian mode
+
   int m_of(int m, int s) const { return nspf[m + nmodes * s]; }
   std::vector<int> shape_of(int s) const {
     std::vector<int> v(nmodes);
@@ -369,8 +397,9 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
     c.multiset[m] = (int)s->multiset[m];
     c.is_gwp[m] = (int)s->is_gwp[m];
     for (int k = 0; k < c.nmodedof[m]; ++k) c.mode_dofs[m].push_back((int)s->idof[k + c.maxdof * m]);
-    if (c.is_gwp[m]) throw StatusError(MCTDH_EUNSUPPORTED, "Gaussian (GWP) modes are not supported by this build");
-    if (c.nmodedof[m] > MAXDOF_MODE) throw StatusError(MCTDH_EUNSUPPORTED, "too many DOFs in one DVR mode");
+    if (c.is_gwp[m] && c.nmodedof[m] > GWP_MAXDOF)
+      throw StatusError(MCTDH_EUNSUPPORTED, "too many DOFs in one Gaussian mode");
+    if (!c.is_gwp[m] && c.nmodedof[m] > MAXDOF_MODE) throw StatusError(MCTDH_EUNSUPPORTED, "too many DOFs in one DVR mode");
     for (int st = 0; st < c.nstates; ++st)
       if (c.m_of(m, st) > MAXN_SPF || c.m_of(m, st) < 1)
         throw StatusError(MCTDH_EUNSUPPORTED, "SPF count outside 1..32");
@@ -420,8 +449,13 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.ipsi.resize(c.nmodes * c.nstates);
   for (int i = 0; i < c.nmodes * c.nstates; ++i) c.ipsi[i] = s->ipsispf[i];
   c.gmode.assign(c.nmodes, 0);
+  c.gwp_of.assign(c.nmodes, -1);
   for (int m = 0; m < c.nmodes; ++m) {
-    if (c.is_gwp[m]) continue;
+    if (c.is_gwp[m]) {
+      c.gwp_of[m] = (int)c.modes_gwp.size();
+      c.modes_gwp.push_back(m);
+      continue;
+    }
     c.modes_dvr.push_back(m);
     int G = 1;
     for (int d : c.mode_dofs[m]) G *= c.ngp[d];
@@ -439,6 +473,26 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.int_type_psi = (int)s->int_type_psi;
   c.precision = (int)s->precision;
   if (c.precision < 0 || c.precision > 2) throw StatusError(MCTDH_EARG, "precision must be 0, 1 or 2");
+  if (!c.modes_gwp.empty()) {
+    // Gaussian widths GWPa(maxdof, ns00max, nmodgwp) (psidef: GWPa, init_calc.f90:1020-1068)
+    c.gwp_lda = c.maxdof;
+    c.ns00max = (int)s->ns00max;
+    if (!s->gwpa || c.ns00max < 1) throw StatusError(MCTDH_EARG, "Gaussian modes need gwpa and ns00max");
+    for (int m : c.modes_gwp)
+      for (int st = 0; st < c.nstates; ++st)
+        if (c.m_of(m, st) > c.ns00max) throw StatusError(MCTDH_EARG, "Gaussian SPF count above ns00max");
+    const size_t na = (size_t)c.gwp_lda * c.ns00max * c.modes_gwp.size();
+    c.gwpa_d = (double*)c.ar.alloc(sizeof(double) * na);
+    CK(cudaMemcpy(c.gwpa_d, s->gwpa, sizeof(double) * na, cudaMemcpyHostToDevice));
+    for (int m : c.modes_gwp)
+      for (int k = 0; k < c.noper[m]; ++k)
+        for (int q = 0; q < c.nmodedof[m]; ++q) {
+          const int code = c.oper[m][k][2 + q];
+          if (code < -3 || code > 20)
+            throw StatusError(MCTDH_EUNSUPPORTED, "primitive operator code " + std::to_string(code) +
+                                                      " has no Gaussian integral");
+        }
+  }
 
   // primitive DOF operator matrices (dense ones in the zlacrm-from-the-right form
   // with the +i factor of p and qp, hamilton.f90:455-461; diagonal q^k)
@@ -456,7 +510,7 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
         std::vector<cplx> v;
         int kind;
         if (code == -1 || code == -2 || code == -3) {
-          kind = 1;
+          kind = (code == -2) ? 1 : 3;   // d^2/dq^2 real; p and qp carry the factor i
           const double* src = code == -1 ? mats : (code == -2 ? mats + ng * ng : mats + 2 * ng * ng);
           v.resize(ng * ng);
           for (int i = 0; i < ng * ng; ++i) v[i] = (code == -2) ? mkc(src[i], 0.0) : mkc(0.0, src[i]);
@@ -475,8 +529,109 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
 }
 
 // ---------------------------------------------------------------------------
-// Planning of the EOM (Calc_Derivs for DVR models, derivatives.f90:39-156)
+// Gaussian modes: overlaps S00 and their Tikhonov inverses (Calc_S00,
+// gmctdh_objects.f90:323-381; Calc_S00m1, :385-404) and the h1mode matrices of
+// their operators (hamilton.f90:494-524), identity operators included (their
+// h1mode is S00, and the Hamiltonian chains do not skip them).
 // ---------------------------------------------------------------------------
+const cplx* psi_block(const Ctx& c, const cplx* y, int m, int s) {
+  return y + c.naconftot + c.ipsi[m + c.nmodes * s];
+}
+int set_of(const Ctx& c, int m, int s) { return c.multiset[m] ? s : 0; }
+
+void plan_gwp_setup(Ctx& c) {
+  const int f = c.nmodes;
+  const int ng = (int)c.modes_gwp.size();
+  c.s00.assign(ng, std::vector<std::vector<cplx*>>(c.nstates, std::vector<cplx*>(c.nstates, nullptr)));
+  c.s00m1.assign(ng, std::vector<cplx*>(c.nstates, nullptr));
+  for (int i = 0; i < ng; ++i) {
+    const int m = c.modes_gwp[i];
+    const double* a = c.gwpa_d + (size_t)c.gwp_lda * c.ns00max * i;
+    const int nsets = c.multiset[m] ? c.nstates : 1;
+    for (int s1 = 0; s1 < nsets; ++s1) {
+      for (int s2 = 0; s2 < nsets; ++s2) {
+        const int n1 = c.m_of(m, s1), n2 = c.m_of(m, s2);
+        c.s00[i][s1][s2] = c.ar.calloc_c((long long)n1 * n2);
+        GwpOvlDesc d;
+        memset(&d, 0, sizeof(d));
+        d.xi1 = psi_block(c, c.d_in, m, s1);
+        d.xi2 = psi_block(c, c.d_in, m, s2);
+        d.a = a;
+        d.out = c.s00[i][s1][s2];
+        d.nmd = c.nmodedof[m];
+        d.lda = c.gwp_lda;
+        d.n1 = n1;
+        d.n2 = n2;
+        d.kind = (s1 == s2) ? 0 : (s1 < s2 ? 1 : 2);
+        c.gs_h.push_back(d);
+      }
+      RegInvDesc rd;
+      memset(&rd, 0, sizeof(rd));
+      rd.A = c.s00[i][s1][s1];
+      rd.n = c.m_of(m, s1);
+      rd.regtype = 1;
+      rd.eps = c.eps_ovl;
+      c.s00m1[i][s1] = c.ar.calloc_c((long long)rd.n * rd.n);
+      rd.inv_out = c.s00m1[i][s1];
+      c.gsreg_h.push_back(rd);
+    }
+    // h1mode of every operator of the mode
+    c.hmat[m].assign(c.noper[m], nullptr);
+    c.ophi[m].assign(c.noper[m], nullptr);
+    c.mf[m].assign(c.noper[m], nullptr);
+    c.rhom1mf[m].assign(c.noper[m], nullptr);
+    for (int k = 0; k < c.noper[m]; ++k) {
+      const int l = c.oper[m][k][0], r = c.oper[m][k][1];
+      const int n1 = c.m_of(m, l), n2 = c.m_of(m, r);
+      c.hmat[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      if (!c.is_identity[m + f * k]) c.mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      GwpH1Desc hd;
+      memset(&hd, 0, sizeof(hd));
+      hd.xi1 = psi_block(c, c.d_in, m, l);
+      hd.xi2 = psi_block(c, c.d_in, m, r);
+      hd.a = a;
+      hd.S = c.s00[i][set_of(c, m, l)][set_of(c, m, r)];
+      hd.out = c.hmat[m][k];
+      hd.nmd = c.nmodedof[m];
+      hd.lda = c.gwp_lda;
+      hd.n1 = n1;
+      hd.n2 = n2;
+      hd.same_state = (l == r);
+      for (int q = 0; q < c.nmodedof[m]; ++q) hd.ops[q] = c.oper[m][k][2 + q];
+      c.gh1_h.push_back(hd);
+    }
+  }
+  c.gs_d = upload_vec(c.ar, c.gs_h);
+  c.gsreg_d = upload_vec(c.ar, c.gsreg_h);
+  c.gh1_d = upload_vec(c.ar, c.gh1_h);
+}
+
+// S-weighted coefficient tensors for the density matrices (Calc_rho1mode,
+// gmctdh_objects.f90:408-477): S00 applied on every Gaussian mode except `skip`,
+// in the order of the Gaussian modes.  Returns the tensor (A_s itself when no
+// product is needed).
+const cplx* plan_s_weighted(Ctx& c, int s, int skip) {
+  const cplx* cur = c.d_in + c.aoff[s];
+  std::vector<int> sh = c.shape_of(s);
+  int depth = 0;
+  for (int i = 0; i < (int)c.modes_gwp.size(); ++i) {
+    const int m = c.modes_gwp[i];
+    if (m == skip) continue;
+    if ((int)c.gwp_rho_chain.size() <= depth) c.gwp_rho_chain.emplace_back();
+    cplx* out = c.ar.calloc_c(c.naconf[s]);
+    const int n = sh[m];
+    c.gwp_rho_chain[depth].add(cur, out, c.s00[i][set_of(c, m, s)][set_of(c, m, s)], n, 0, sh, m, n, mkc(1, 0), 0);
+    cur = out;
+    ++depth;
+  }
+  return cur;
+}
+
+// ---------------------------------------------------------------------------
+// Planning of the EOM (Calc_Derivs, derivatives.f90:39-237)
+// ---------------------------------------------------------------------------
+void plan_gwp_derivs(Ctx& c);
+
 void plan_eom(Ctx& c) {
   const int f = c.nmodes;
   const int nsm = MAXN_SPF;
@@ -515,6 +670,7 @@ void plan_eom(Ctx& c) {
       hd.phi_l = c.d_in + c.naconftot + c.ipsi[m + f * l];
       hd.ophi = c.ophi[m][k];
       hd.h = c.hmat[m][k];
+      hd.X = c.ar.calloc_c((long long)n1 * n2);
       hd.G = G;
       hd.n1 = n1;
       hd.n2 = n2;
@@ -534,17 +690,22 @@ void plan_eom(Ctx& c) {
       }
       c.h1_of_mode[m].push_back((int)c.h1_h.size());
       c.h1_h.push_back(hd);
-      smem = std::max(smem, sizeof(cplx) * (size_t)(2 * G * n2 + MAXN_SPF * MAXN_SPF));
+      smem = std::max(smem, sizeof(cplx) * (size_t)(2 * G));
+      c.h1_maxn2 = std::max(c.h1_maxn2, n2);
     }
   }
   c.h1_smem = smem;
   c.h1_d = upload_vec(c.ar, c.h1_h);
+  if (!c.modes_gwp.empty()) plan_gwp_setup(c);
 
   // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
   std::vector<HoleRef> hrefs;       // mean-field contractions (c.holes)
   std::vector<HoleRef> rrefs;       // density-matrix contractions (c.rho_holes, FP64)
   std::vector<std::vector<int>> rho_hole(f, std::vector<int>(c.nstates, -1));
-  for (int m : c.modes_dvr) {
+  std::vector<int> rho_modes = c.modes_dvr;
+  rho_modes.insert(rho_modes.end(), c.modes_gwp.begin(), c.modes_gwp.end());
+  std::map<std::pair<int, int>, const cplx*> weighted;   // (state, skipped Gaussian mode or -1)
+  for (int m : rho_modes) {
     int ave_target = -1;
     if (!c.multiset[m]) {
       int n = c.m_of(m, 0);
@@ -555,7 +716,13 @@ void plan_eom(Ctx& c) {
       int n = c.m_of(m, s);
       c.rho[m][s] = c.ar.calloc_c((long long)n * n);
       std::vector<int> sh = c.shape_of(s);
-      int hidx = c.rho_holes.add(c.ar, c.d_in + c.aoff[s], c.d_in + c.aoff[s], prod_range(sh, 0, m),
+      const cplx* Y = c.d_in + c.aoff[s];
+      if (!c.modes_gwp.empty()) {
+        const auto key = std::make_pair(s, c.is_gwp[m] ? m : -1);
+        if (!weighted.count(key)) weighted[key] = plan_s_weighted(c, s, key.second);
+        Y = weighted[key];
+      }
+      int hidx = c.rho_holes.add(c.ar, Y, c.d_in + c.aoff[s], prod_range(sh, 0, m),
                                  prod_range(sh, m + 1, f), n, n);
       rho_hole[m][s] = hidx;
       int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
@@ -769,6 +936,91 @@ void plan_eom(Ctx& c) {
   }
   c.sum_d = upload_vec(c.ar, c.sum_h);
   c.src_d = upload_vec(c.ar, c.src_h);
+  for (auto& b : c.gwp_rho_chain) b.finalize(c.ar);
+  if (!c.modes_gwp.empty()) plan_gwp_derivs(c);
+}
+
+// Gaussian-parameter derivatives and the coefficient correction for Gaussian
+// modes (derivatives.f90:158-236): Calc_CY per (mode, state) block, the
+// Tikhonov solve, tau, then dA = S^-1 x_m (f H A) - tau x_m A over the Gaussian
+// modes.  All FP64.
+void plan_gwp_derivs(Ctx& c) {
+  const int f = c.nmodes;
+  const int ng = (int)c.modes_gwp.size();
+  c.tau.assign(ng, std::vector<cplx*>(c.nstates, nullptr));
+  for (int i = 0; i < ng; ++i) {
+    const int m = c.modes_gwp[i];
+    const double* a = c.gwpa_d + (size_t)c.gwp_lda * c.ns00max * i;
+    const int nsets = c.multiset[m] ? c.nstates : 1;
+    for (int s = 0; s < nsets; ++s) {
+      const int n = c.m_of(m, s), nmd = c.nmodedof[m];
+      const int nG = n * nmd;
+      GwpCYDesc d;
+      memset(&d, 0, sizeof(d));
+      d.xi = psi_block(c, c.d_in, m, s);
+      d.a = a;
+      d.S = c.s00[i][s][s];
+      d.Sm1 = c.s00m1[i][s];
+      d.rho = c.multiset[m] ? c.rho[m][s] : c.rho_ave[m];
+      d.Sa0 = c.ar.calloc_c((long long)nG * n);
+      d.Sa0Sm1 = c.ar.calloc_c((long long)nG * n);
+      d.M = c.ar.calloc_c(2LL * nG * (nG + 1));
+      d.R = c.ar.calloc_c((long long)nG * nG);
+      d.x = c.ar.calloc_c(nG);
+      d.dxi_offset = c.naconftot + c.ipsi[m + f * s];
+      c.tau[i][s] = c.ar.calloc_c((long long)n * n);
+      d.tau = c.tau[i][s];
+      d.nmd = nmd;
+      d.lda = c.gwp_lda;
+      d.n = n;
+      d.nG = nG;
+      d.eps = c.eps_C;
+      d.op_first = (int)c.yop_h.size();
+      for (int k = 0; k < c.noper[m]; ++k) {
+        if (c.is_identity[m + f * k]) continue;
+        const int l = c.oper[m][k][0], r = c.oper[m][k][1];
+        if (c.multiset[m] && l != s) continue;
+        GwpYOp op;
+        memset(&op, 0, sizeof(op));
+        op.xi2 = psi_block(c, c.d_in, m, r);
+        op.S12 = c.s00[i][s][set_of(c, m, r)];
+        op.h = c.hmat[m][k];
+        op.mf = c.mf[m][k];
+        op.n2 = c.m_of(m, r);
+        for (int q = 0; q < nmd; ++q) op.ops[q] = c.oper[m][k][2 + q];
+        c.yop_h.push_back(op);
+      }
+      d.op_count = (int)c.yop_h.size() - d.op_first;
+      c.cy_maxG = std::max(c.cy_maxG, nG);
+      c.cy_maxn = std::max(c.cy_maxn, n);
+      if (nG > 512) throw StatusError(MCTDH_EUNSUPPORTED, "Gaussian parameter system above 512 unknowns");
+      c.cy_h.push_back(d);
+    }
+  }
+  c.cy_d = upload_vec(c.ar, c.cy_h);
+  c.yop_d = upload_vec(c.ar, c.yop_h);
+  // dA = S^-1 (f H A) - tau A on the Gaussian modes
+  c.d_adot = c.ar.calloc_c(c.naconftot);
+  c.d_dA = c.ar.calloc_c(c.naconftot);
+  c.gwp_sinv.assign(ng, ProdBatch());
+  c.gwp_tau.assign(ng, ProdBatch());
+  for (int s = 0; s < c.nstates; ++s) {
+    std::vector<int> sh = c.shape_of(s);
+    const cplx* cur = c.d_adot + c.aoff[s];
+    for (int i = 0; i < ng; ++i) {
+      const int m = c.modes_gwp[i];
+      cplx* out = (i + 1 == ng) ? c.d_dA + c.aoff[s] : c.ar.calloc_c(c.naconf[s]);
+      c.gwp_sinv[i].add(cur, out, c.s00m1[i][set_of(c, m, s)], sh[m], 0, sh, m, sh[m], mkc(1, 0), 0);
+      cur = out;
+    }
+    for (int i = 0; i < ng; ++i) {
+      const int m = c.modes_gwp[i];
+      c.gwp_tau[i].add(c.d_in + c.aoff[s], c.d_dA + c.aoff[s], c.tau[i][set_of(c, m, s)], sh[m], 0, sh, m, sh[m],
+                       mkc(-1, 0), 1);
+    }
+  }
+  for (auto& b : c.gwp_sinv) b.finalize(c.ar);
+  for (auto& b : c.gwp_tau) b.finalize(c.ar);
 }
 
 // H_B * B for the CMF2 Lanczos (Calc_DHD_B, cmf2_derivatives.f90:1-80): chains over
@@ -853,10 +1105,48 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2) {
       S[m][s] = sm;
     }
   }
+  // Gaussian modes: normalised Gaussian overlaps; <1|1> and <2|2> from the upper
+  // triangle with unit diagonal (gmctdh_objects.f90:21-97), <1|2> in full (:101-180)
+  for (int m : c.modes_gwp) {
+    const int i = c.gwp_of[m];
+    const double* a = c.gwpa_d + (size_t)c.gwp_lda * c.ns00max * i;
+    for (int s = 0; s < c.nstates; ++s) {
+      if (!c.multiset[m] && s > 0) { S[m][s] = S[m][0]; continue; }
+      const int n = c.m_of(m, s);
+      Smat sm;
+      cplx* outs[3];
+      for (int q = 0; q < 3; ++q) outs[q] = c.ar.calloc_c((long long)n * n);
+      sm.s11 = outs[0];
+      sm.s22 = outs[1];
+      sm.s12 = outs[2];
+      const cplx* p1 = psi_block(c, y1, m, s);
+      const cplx* p2 = psi_block(c, y2, m, s);
+      const cplx* L[3] = {p1, p2, p1};
+      const cplx* Rr[3] = {p1, p2, p2};
+      for (int q = 0; q < 3; ++q) {
+        GwpOvlDesc d;
+        memset(&d, 0, sizeof(d));
+        d.xi1 = L[q];
+        d.xi2 = Rr[q];
+        d.a = a;
+        d.out = outs[q];
+        d.nmd = c.nmodedof[m];
+        d.lda = c.gwp_lda;
+        d.n1 = n;
+        d.n2 = n;
+        d.kind = (q < 2) ? 0 : 1;
+        P.gwp_h.push_back(d);
+      }
+      S[m][s] = sm;
+    }
+  }
+  P.gwp_d = upload_vec(c.ar, P.gwp_h);
   P.spf_holes.finalize(c.ar);
   for (auto& hr : hrefs) P.spf_red.add_term(hr.target, P.spf_holes.h[hr.hole], hr.alpha);
   P.spf_red.finalize(c.ar);
-  P.chain.assign(c.modes_dvr.size() + 1, ProdBatch());
+  std::vector<int> order = c.modes_dvr;
+  order.insert(order.end(), c.modes_gwp.begin(), c.modes_gwp.end());
+  P.chain.assign(order.size() + 1, ProdBatch());
   std::vector<HoleRef> drefs;
   int t11 = P.dot_red.add_target(P.d_result + 0, 1, 1, 1, 0);
   int t22 = P.dot_red.add_target(P.d_result + 1, 1, 1, 1, 0);
@@ -867,8 +1157,8 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2) {
     cplx* a1 = y1 + c.aoff[s];
     cplx* a2 = y2 + c.aoff[s];
     cplx* cur[3] = {a1, a2, a2};
-    for (size_t i = 0; i < c.modes_dvr.size(); ++i) {
-      const int m = c.modes_dvr[i];
+    for (size_t i = 0; i < order.size(); ++i) {
+      const int m = order[i];
       const int n = sh[m];
       cplx* mats[3] = {S[m][s].s11, S[m][s].s22, S[m][s].s12};
       for (int q = 0; q < 3; ++q) {
@@ -956,16 +1246,42 @@ void run_red(Ctx& c, const RedBatch& b) {
   c.count();
 }
 
+// Gaussian modes, first part of the EOM: S00, S00^-1 (tikh) and h1mode.
+void gwp_setup_run(Ctx& c) {
+  ProfScope ps(c, KP_GWP);
+  launch_gwp_ovl(c.gs_d, (int)c.gs_h.size(), c.st);
+  launch_reginv(c.gsreg_d, (int)c.gsreg_h.size(), c.mfop_d, c.d_status, c.st);
+  launch_gwp_h1(c.gh1_d, (int)c.gh1_h.size(), c.st);
+  c.count(3);
+}
+
+// Gaussian modes, last part: parameter derivatives into out's psi part and the
+// corrected dA into out's coefficient part (from d_adot).
+void gwp_derivs_run(Ctx& c, cplx* out) {
+  {
+    ProfScope ps(c, KP_GWP);
+    launch_gwp_cy(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.cy_maxn, c.yop_d, c.st);
+    launch_gwp_solve(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.der, out, c.d_status, c.st);
+    c.count(5 + (c.cy_maxG + GWP_QR_PW - 1) / GWP_QR_PW);
+  }
+  for (auto& b : c.gwp_sinv) run_prod(c, b);
+  for (auto& b : c.gwp_tau) run_prod(c, b);
+  CK(cudaMemcpyAsync(out, c.d_dA, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
+}
+
 // EOM on d_in -> out (full vector [dA | dpsi]).
 void eom(Ctx& c, cplx* out) {
+  const bool gwp = !c.modes_gwp.empty();
+  if (gwp) gwp_setup_run(c);
   {
     ProfScope ps(c, KP_H1);
-    launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
+    launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st);
     launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
-    c.count(2);
+    c.count(3);
   }
   for (size_t i = 1; i < c.chains.size(); ++i) run_prod(c, c.chains[i]);
   run_prod(c, c.gprods);
+  for (auto& b : c.gwp_rho_chain) run_prod(c, b);
   run_hole(c, c.rho_holes);
   run_hole(c, c.holes);
   run_red(c, c.red);
@@ -976,7 +1292,7 @@ void eom(Ctx& c, cplx* out) {
   }
   {
     ProfScope ps(c, KP_TERMSUM, 0.0, 16.0 * (double)c.src_h.size() * (double)c.naconftot / std::max(1, c.nstates));
-    launch_termsum(out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st);
+    launch_termsum(gwp ? c.d_adot : out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st);
     c.count();
   }
   {
@@ -984,6 +1300,7 @@ void eom(Ctx& c, cplx* out) {
     launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st);
     c.count(3);
   }
+  if (gwp) gwp_derivs_run(c, out);
   c.eom_count++;
 }
 
@@ -993,6 +1310,10 @@ void eom_from(Ctx& c, const cplx* y, cplx* out) {
 }
 
 void run_ovl(Ctx& c, OvlPlan& P) {
+  if (!P.gwp_h.empty()) {
+    launch_gwp_ovl(P.gwp_d, (int)P.gwp_h.size(), c.st);
+    c.count();
+  }
   run_hole(c, P.spf_holes);
   run_red(c, P.spf_red);
   for (auto& b : P.chain) run_prod(c, b);
@@ -1220,9 +1541,9 @@ void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
 // h1mode only (no mean fields) on the SPFs of y: used before the back-propagation.
 void h1_only(Ctx& c, const cplx* y) {
   copy_dev(c, c.d_in + c.naconftot, y + c.naconftot, c.dimpsi);
-  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_smem, c.st);
+  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st);
   launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
-  c.count(2);
+  c.count(3);
 }
 
 // SPF integration of all DVR modes with frozen mean fields, in lockstep: one
@@ -1268,7 +1589,7 @@ void stage_modes(Ctx& c, CmfState& S, cplx* out, const cplx* base, const double*
 void spf_eval_all(Ctx& c, CmfState& S, cplx* out) {
   {
     ProfScope ps(c, KP_H1);
-    launch_h1(S.h1_d, (int)S.h1.size(), c.h1_smem, c.st);
+    launch_h1(S.h1_d, (int)S.h1.size(), c.h1_maxn2, c.h1_smem, false, c.st);
   }
   {
     ProfScope ps(c, KP_SPF);
@@ -1323,9 +1644,13 @@ void plan_cmf(Ctx& c, CmfState& S) {
   S.planned = true;
 }
 
-// propagate_SPF for every DVR mode over dt_total, on the psi part of y.
+// propagate_SPF for every DVR mode over dt_total, on the psi part of y
+// (cmf2_base.f90:210-260): Cash-Karp (rk_SPF_ck, cmf2_integration.f90:105-253)
+// for int_type_psi 1, Dormand-Prince (rk_SPF_dp, :257-412) for 2.
 void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
-  if (c.int_type_psi != 1) throw StatusError(MCTDH_EUNSUPPORTED, "only Cash-Karp SPF integration is supported");
+  if (c.int_type_psi != 1 && c.int_type_psi != 2)
+    throw StatusError(MCTDH_EUNSUPPORTED, "SPF integrator must be rk45 (1) or dopri (2)");
+  const bool dp = c.int_type_psi == 2;
   const int f = c.nmodes;
   const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
   std::vector<double> done(f, 0.0), dtry(f, 0.0), dt_h(64, 0.0), err_h(64, 0.0);
@@ -1348,11 +1673,19 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
     copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
     spf_eval_all(c, S, c.d_k[0]);
     for (int st = 1; st < 6; ++st) {
-      stage_modes(c, S, c.d_in, y, CK_B[st], st);
+      stage_modes(c, S, c.d_in, y, dp ? DP_B[st] : CK_B[st], st);
       spf_eval_all(c, S, c.d_k[st]);
     }
-    stage_modes(c, S, c.d_tmp, y, CK_C, 6);
-    stage_modes(c, S, c.d_err, y, CK_D, 6);
+    if (dp) {
+      // the 7th stage is the derivative at the 5th-order solution (:386-393)
+      stage_modes(c, S, c.d_in, y, DP_C, 6);
+      spf_eval_all(c, S, c.d_k[6]);
+      stage_modes(c, S, c.d_tmp, y, DP_C, 6);
+      stage_modes(c, S, c.d_err, y, DP_D, 7);
+    } else {
+      stage_modes(c, S, c.d_tmp, y, CK_C, 6);
+      stage_modes(c, S, c.d_err, y, CK_D, 6);
+    }
     {
       StageArgs a;
       memset(&a, 0, sizeof(a));
@@ -1396,6 +1729,8 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
 }
 
 CmfState& cmf_state(Ctx& c) {
+  if (!c.modes_gwp.empty())
+    throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 with Gaussian modes (A_to_B / DD matrices) is not built; use RK");
   CmfState*& Sp = g_cmf[&c];
   if (!Sp) {
     Sp = new CmfState();
@@ -1420,12 +1755,13 @@ struct MfxState {
   long long E = 0;
   std::vector<SnapSeg> segs_h;
   SnapSeg* segs_d = nullptr;
-  cplx* hist[3] = {};
-  double thist[3] = {0, 0, 0};
+  cplx* hist[MFX_NHIST] = {};
+  double thist[MFX_NHIST] = {};
   int nhist = 0, head = 0;         // head: index of the newest entry
+  double* S = nullptr;             // device: feature scale of the current prediction
   cplx *half = nullptr, *pred_half = nullptr, *pred_full = nullptr, *now = nullptr, *backup = nullptr;
   mctdh_mlp* mlp = nullptr;
-  double tscale = 1.0, tol = 0.0;
+  double fscale[MFX_NFEAT] = {}, tscale[MFX_NOUT] = {}, tol = 0.0;
   bool recording = false;
   std::vector<double> rec_t0, rec_h;
   std::vector<cplx> rec_s0, rec_sh;
@@ -1468,6 +1804,7 @@ MfxState& mfx_state(Ctx& c) {
   M->diff = c.ar.calloc_c(off);
   M->backup = c.ar.calloc_c(c.ntot);
   M->dres = c.ar.calloc_c(2);
+  M->S = (double*)c.ar.alloc(sizeof(double) * 2);
   int h1 = M->dh.add(c.ar, M->diff, M->diff, off, 1, 1, 1);
   int h2 = M->dh.add(c.ar, M->now, M->now, off, 1, 1, 1);
   M->dh.finalize(c.ar);
@@ -1498,25 +1835,56 @@ double snap_rel_diff(Ctx& c, MfxState& M) {
   return sqrt(r[0].x / std::max(r[1].x, 1e-300));
 }
 
-// Predict the half-step and step-end snapshots from the history for step length h.
+// Lagrange weights at tau of the polynomial through the points ts[first..n-1]
+// (zero weight for the earlier points).
+static void lagrange_tail(const double* ts, int n, int first, double tau, double* w) {
+  for (int j = 0; j < n; ++j) {
+    w[j] = 0.0;
+    if (j < first) continue;
+    double p = 1.0;
+    for (int k = first; k < n; ++k)
+      if (k != j) p *= (tau - ts[k]) / (ts[j] - ts[k]);
+    w[j] = p;
+  }
+}
+
+// Predict the half-step and step-end snapshots from the history for step length h:
+// quartic extrapolation through the last five step starts plus the network's
+// residual, whose inputs are the Newton increments of orders 1-4
+// (mfx_features_kernel).
 void mfx_predict(Ctx& c, MfxState& M, double h) {
-  const int i2 = M.head, i1 = (M.head + 2) % 3, i0 = (M.head + 1) % 3;
-  const double t0 = M.thist[i0], t1 = M.thist[i1], t2 = M.thist[i2];
-  MfxWeights w;
-  const double th = t2 + 0.5 * h, tf = t2 + h;
-  auto lag = [&](double tau, double* o) {
-    o[0] = (tau - t1) * (tau - t2) / ((t0 - t1) * (t0 - t2));
-    o[1] = (tau - t0) * (tau - t2) / ((t1 - t0) * (t1 - t2));
-    o[2] = (tau - t0) * (tau - t1) / ((t2 - t0) * (t2 - t1));
-  };
-  lag(th, w.h);
-  lag(tf, w.f);
+  const int NH = MFX_NHIST;
+  MfxHist hz;
+  double ts[MFX_NHIST];
+  for (int j = 0; j < NH; ++j) {
+    const int idx = (M.head + 1 + j) % NH;   // oldest first
+    hz.z[j] = M.hist[idx];
+    ts[j] = M.thist[idx];
+  }
+  MfxCoef cf;
+  memset(&cf, 0, sizeof(cf));
+  const double taus[2] = {ts[NH - 1] + 0.5 * h, ts[NH - 1] + h};
+  for (int tau = 0; tau < 2; ++tau) {
+    double prev[MFX_NHIST] = {};
+    prev[NH - 1] = 1.0;   // P_0 = newest value
+    for (int o = 1; o < NH; ++o) {
+      double w[MFX_NHIST];
+      lagrange_tail(ts, NH, NH - 1 - o, taus[tau], w);
+      for (int j = 0; j < NH; ++j) cf.inc[tau][o - 1][j] = w[j] - prev[j];
+      memcpy(prev, w, sizeof(prev));
+    }
+    for (int j = 0; j < NH; ++j) cf.base[tau][j] = prev[j];
+  }
+  const double dlast = ts[NH - 1] - ts[NH - 2];
+  for (int j = 0; j < NH - 2; ++j) cf.ratio[j] = (ts[j + 1] - ts[j]) / dlast;
+  cf.ratio[NH - 2] = h / dlast;
+  memcpy(cf.fscale, M.fscale, sizeof(cf.fscale));
+  memcpy(cf.tscale, M.tscale, sizeof(cf.tscale));
   float* X = mlp_input_buffer(M.mlp, M.E);
-  launch_mfx_features(M.hist[i0], M.hist[i1], M.hist[i2], (float)((t1 - t0) / (t2 - t1)), (float)(h / (t2 - t1)),
-                      X, M.E, c.st);
+  launch_mfx_features(hz, cf, M.S, X, M.E, c.st);
   const float* Y = mlp_forward_on(M.mlp, M.E, c.st);
-  launch_mfx_combine(M.hist[i0], M.hist[i1], M.hist[i2], w, Y, M.tscale, M.pred_half, M.pred_full, M.E, c.st);
-  c.count(6);
+  launch_mfx_combine(hz, cf, Y, M.S, M.pred_half, M.pred_full, M.E, c.st);
+  c.count(7);
 }
 
 // One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
@@ -1585,20 +1953,28 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
   if (M) {
     // push the step-start snapshot into the history (once per accepted step start)
     if (M->nhist == 0 || M->thist[M->head] != t) {
-      M->head = (M->head + 1) % 3;
+      M->head = (M->head + 1) % MFX_NHIST;
       snap_gather(c, *M, M->hist[M->head]);
       M->thist[M->head] = t;
-      M->nhist = std::min(M->nhist + 1, 3);
+      M->nhist = std::min(M->nhist + 1, MFX_NHIST);
     }
   }
-  bool use_mlp = M && M->mlp && M->nhist == 3;
+  bool use_mlp = M && M->mlp && M->nhist == MFX_NHIST;
   if (use_mlp) copy_dev(c, M->backup, c.d_y, c.ntot);
   double hdid = htry;
   bool first = true;
   while (true) {
     ++*tries;
+    if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
     double error = cmf2_attempt(c, t, hdid, use_mlp, first);
     first = false;
+    if (error > 1.0 && use_mlp) {
+      // the extrapolated mean fields were trained for accepted steps: redo this
+      // step with the plain scheme instead of shrinking it
+      ++M->fallbacks;
+      use_mlp = false;
+      continue;
+    }
     if (error > 1.0) {
       hdid = hdid / sqrt(error) * 0.95;
       continue;
@@ -1950,13 +2326,22 @@ int64_t mctdh_mfx_fetch(mctdh_ctx_t* ctx, int64_t maxrec, double* t0, double* h,
   });
 }
 
-int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, double tscale, double tol) {
+int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, const double* fscale, const double* tscale, double tol) {
   if (!ctx) return MCTDH_EARG;
+  if (mlp && (!fscale || !tscale)) return MCTDH_EARG;
   Ctx* c = ctx->c;
   return guarded(c, [&] {
+    if (mlp && !mlp_has_shape(mlp, MFX_NFEAT, MFX_NOUT))
+      throw StatusError(MCTDH_EARG, "the network must map 20 inputs to 4 outputs");
     MfxState& M = mfx_state(*c);
     M.mlp = mlp;
-    M.tscale = tscale;
+    if (mlp) {
+      for (int j = 0; j < MFX_NFEAT; ++j) {
+        if (!(fscale[j] > 0.0)) throw StatusError(MCTDH_EARG, "input scales must be positive");
+        M.fscale[j] = fscale[j];
+      }
+      for (int j = 0; j < MFX_NOUT; ++j) M.tscale[j] = tscale[j];
+    }
     M.tol = tol;
   });
 }
@@ -2038,7 +2423,9 @@ int64_t mctdh_observables(mctdh_ctx_t* ctx, double t, double* energy, double* po
   return guarded(c, [&] {
     (void)t;
     eom_from(*c, c->d_y, c->d_out);
-    cplx e = dot_now(*c, c->d_y, c->d_out, c->naconftot);
+    // f * H A before the Gaussian-mode corrections (Calc_MeanField's energyMF)
+    const cplx* hA = c->modes_gwp.empty() ? c->d_out : c->d_adot;
+    cplx e = dot_now(*c, c->d_y, hA, c->naconftot);
     // energy = Re <A| H A> = Re( <A|dA> / der_factor )
     double dr = c->der.x, di = c->der.y, den = dr * dr + di * di;
     double en = (e.x * dr + e.y * di) / den;
@@ -2051,7 +2438,19 @@ int64_t mctdh_observables(mctdh_ctx_t* ctx, double t, double* energy, double* po
       CK(cudaMemcpyAsync(r.data(), c->rho[m0][s], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
       double tr = 0.0;
-      for (int j = 0; j < n; ++j) tr += r[j + n * j].x;
+      if (c->is_gwp[m0]) {
+        // Gaussian first mode: sum of rho o S00 from the upper triangle (output.f90:63-85)
+        std::vector<cplx> S(n * n);
+        const cplx* sp = c->s00[c->gwp_of[m0]][set_of(*c, m0, s)][set_of(*c, m0, s)];
+        CK(cudaMemcpyAsync(S.data(), sp, sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        for (int j2 = 0; j2 < n; ++j2) {
+          for (int j1 = 0; j1 < j2; ++j1) tr += 2.0 * cmul(r[j1 + n * j2], S[j1 + n * j2]).x;
+          tr += cmul(r[j2 + n * j2], S[j2 + n * j2]).x;
+        }
+      } else {
+        for (int j = 0; j < n; ++j) tr += r[j + n * j].x;
+      }
       p[s] = tr;
       tot += tr;
     }

@@ -325,15 +325,21 @@ void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaS
 // h1mode and operator-applied SPFs for DVR modes (Calc_h1mode, hamilton.f90:416-482;
 // MultTens / MultTensDiag, :577-629).  One block per (mode, operator).
 // ---------------------------------------------------------------------------
+// One block per (operator, SPF column j2): the primitive DOF operators act
+// within each SPF, so a column is transformed in shared memory on its own
+// (MultTens / MultTensDiag, hamilton.f90:577-629).  The DVR matrices of p, qp
+// (i x real) and d^2/dq^2 (real) are applied with real arithmetic.  Then, when
+// h1mode is wanted, the column j2 of phi_l^H (O phi_r), one warp per row j1.
 __global__ void __launch_bounds__(256) h1_kernel(const H1Desc* __restrict__ descs) {
   extern __shared__ cplx sm[];
   const H1Desc& d = descs[blockIdx.x];
-  const int G = d.G, n2 = d.n2, n1 = d.n1;
-  const int tot = G * n2;
+  const int j2 = blockIdx.y;
+  if (j2 >= d.n2) return;
+  const int G = d.G, n1 = d.n1;
   cplx* bufA = sm;
-  cplx* bufB = sm + tot;
-  cplx* X = sm + 2 * tot;   // n1*n2 scratch for the Hermitian part
-  for (int e = threadIdx.x; e < tot; e += blockDim.x) bufA[e] = d.phi_r[e];
+  cplx* bufB = sm + G;
+  const cplx* src = d.phi_r + (long long)G * j2;
+  for (int e = threadIdx.x; e < G; e += blockDim.x) bufA[e] = src[e];
   __syncthreads();
   int ll = 1;
   for (int k = 0; k < d.ndof; ++k) {
@@ -341,19 +347,33 @@ __global__ void __launch_bounds__(256) h1_kernel(const H1Desc* __restrict__ desc
     const int ot = d.optype[k];
     if (ot != 0) {
       const cplx* M = d.mat[k];
-      for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      for (int e = threadIdx.x; e < G; e += blockDim.x) {
         const int a = e % ll;
         const int gg = (e / ll) % ng;
         const int bidx = e / (ll * ng);
         cplx v;
-        if (ot == 1) {
+        if (ot == 2) {
+          v = cscale(bufA[e], M[gg].x);
+        } else {
           // psi(.., g, ..) <- sum_g' psi(.., g', ..) M(g', g)   (zlacrm from the right)
-          v = mkc(0, 0);
           const cplx* in = bufA + a + (long long)ll * ng * bidx;
           const cplx* mc = M + (long long)ng * gg;
-          for (int gp = 0; gp < ng; ++gp) cfma(v, mc[gp], in[(long long)ll * gp]);
-        } else {
-          v = cscale(bufA[e], M[gg].x);
+          double sx = 0.0, sy = 0.0;
+          if (ot == 1) {
+            for (int gp = 0; gp < ng; ++gp) {
+              const cplx x = in[(long long)ll * gp];
+              sx = fma(mc[gp].x, x.x, sx);
+              sy = fma(mc[gp].x, x.y, sy);
+            }
+            v = mkc(sx, sy);
+          } else {
+            for (int gp = 0; gp < ng; ++gp) {
+              const cplx x = in[(long long)ll * gp];
+              sx = fma(mc[gp].y, x.x, sx);
+              sy = fma(mc[gp].y, x.y, sy);
+            }
+            v = mkc(-sy, sx);   // i * (real matrix x column)
+          }
         }
         bufB[e] = v;
       }
@@ -362,116 +382,158 @@ __global__ void __launch_bounds__(256) h1_kernel(const H1Desc* __restrict__ desc
     }
     ll *= ng;
   }
-  for (int e = threadIdx.x; e < tot; e += blockDim.x) d.ophi[e] = bufA[e];
+  cplx* dst = d.ophi + (long long)G * j2;
+  for (int e = threadIdx.x; e < G; e += blockDim.x) dst[e] = bufA[e];
   if (d.h == nullptr) return;
-  for (int pr = threadIdx.x; pr < n1 * n2; pr += blockDim.x) {
-    const int j1 = pr % n1, j2 = pr / n1;
-    cplx s = mkc(0, 0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j1 = warp; j1 < n1; j1 += (int)(blockDim.x >> 5)) {
     const cplx* pl = d.phi_l + (long long)G * j1;
-    const cplx* po = bufA + (long long)G * j2;
-    for (int gg = 0; gg < G; ++gg) cfma_conj(s, pl[gg], po[gg]);
-    X[pr] = s;
-  }
-  __syncthreads();
-  for (int pr = threadIdx.x; pr < n1 * n2; pr += blockDim.x) {
-    const int j1 = pr % n1, j2 = pr / n1;
-    cplx v = X[pr];
-    if (d.same_state) v = cscale(cadd(v, cconj(X[j2 + n1 * j1])), 0.5);
-    d.h[pr] = v;
+    cplx s = mkc(0, 0);
+    for (int gg = lane; gg < G; gg += 32) cfma_conj(s, pl[gg], bufA[gg]);
+    for (int o = 16; o > 0; o >>= 1) {
+      s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) {
+      if (d.same_state) d.X[j1 + n1 * j2] = s;
+      else d.h[j1 + n1 * j2] = s;
+    }
   }
 }
 
-void launch_h1(const H1Desc* d_descs, int ndesc, size_t smem_bytes, cudaStream_t st) {
+// Same-state h1mode = (X + X^H) / 2 (the zher2k form, hamilton.f90:500-506).
+__global__ void h1_herm_kernel(const H1Desc* __restrict__ descs) {
+  const H1Desc& d = descs[blockIdx.x];
+  if (d.h == nullptr || !d.same_state) return;
+  const int n1 = d.n1;
+  for (int pr = threadIdx.x; pr < n1 * d.n2; pr += blockDim.x) {
+    const int j1 = pr % n1, j2 = pr / n1;
+    d.h[pr] = cscale(cadd(d.X[pr], cconj(d.X[j2 + n1 * j1])), 0.5);
+  }
+}
+
+void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, bool with_h, cudaStream_t st) {
   if (ndesc <= 0) return;
   static size_t configured = 0;
   if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
     cudaFuncSetAttribute(h1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     configured = smem_bytes;
   }
-  h1_kernel<<<ndesc, 256, smem_bytes, st>>>(d_descs);
+  h1_kernel<<<dim3(ndesc, maxn2), 256, smem_bytes, st>>>(d_descs);
+  if (with_h) h1_herm_kernel<<<ndesc, 128, 0, st>>>(d_descs);
 }
 
 // ---------------------------------------------------------------------------
-// Cyclic complex Jacobi eigen-decomposition of a Hermitian matrix held in shared
-// memory (the work zheev does inside StdRegInv, maths.f90:36).  Rotations are
-// computed by one thread and applied by all; the sweep count is capped.
-// A[i + ld*j], V likewise.  Returns through *ok whether the sweeps converged.
+// Parallel complex Jacobi eigen-decomposition of a Hermitian matrix (n <= 32)
+// held in shared memory, run by one warp: the work zheev does inside StdRegInv
+// (maths.f90:36).  Each round rotates the n/2 disjoint index pairs of a
+// round-robin schedule at once (column rotations A J, then row rotations J^H (A J);
+// rotations of disjoint pairs commute), so a sweep is n-1 rounds.  A pair is
+// rotated when |a_pq| > 1e-19 ||A||_F and |a_pq|^2 > 1e-32 |a_pp a_qq|; the
+// sweep count is capped.  A[i + ld*j], V likewise.  *ok: the sweeps converged.
 // ---------------------------------------------------------------------------
 #define JAC_MAX_SWEEPS 40
-__device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, volatile int* s_flag, volatile double* s_rot,
-                            bool* ok) {
-  const int tid = threadIdx.x;
-  for (int e = tid; e < n * n; e += blockDim.x) {
+struct JacRot {
+  double c, s, tm, app, aqq;
+  cplx u;
+  int p, q, rot;
+};
+
+__device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, JacRot* R, bool* ok) {
+  const int lane = threadIdx.x;   // blockDim.x == 32
+  for (int e = lane; e < n * n; e += 32) {
     int i = e % n, j = e / n;
     V[i + ld * j] = mkc(i == j ? 1.0 : 0.0, 0.0);
   }
-  __syncthreads();
+  __syncwarp();
   double fro2 = 0.0;
   for (int e = 0; e < n * n; ++e) { int i = e % n, j = e / n; fro2 += cabs2(A[i + ld * j]); }
   const double fro = sqrt(fro2);
-  bool converged = false;
-  for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep) {
-    if (tid == 0) s_flag[0] = 0;
-    __syncthreads();
-    for (int p = 0; p < n - 1; ++p) {
-      for (int q = p + 1; q < n; ++q) {
-        if (tid == 0) {
-          cplx apq = A[p + ld * q];
-          double mag = sqrt(cabs2(apq));
-          double app = A[p + ld * p].x, aqq = A[q + ld * q].x;
-          int rot = (mag > 1e-19 * fro) && (mag * mag > 1e-32 * fabs(app * aqq));
-          s_rot[0] = rot;
+  const int m = n + (n & 1);      // even count; index n is a dummy for odd n
+  const int npair = m / 2;
+  bool converged = (n <= 1);
+  for (int sweep = 0; sweep < JAC_MAX_SWEEPS && !converged; ++sweep) {
+    bool any = false;
+    for (int r = 0; r < m - 1; ++r) {
+      int rot = 0;
+      if (lane < npair) {
+        // circle schedule: (r, m-1) and ((r+j) mod (m-1), (r-j) mod (m-1))
+        int a = (lane == 0) ? r : (r + lane) % (m - 1);
+        int b = (lane == 0) ? m - 1 : (r - lane + (m - 1)) % (m - 1);
+        const int p = min(a, b), q = max(a, b);
+        JacRot& J = R[lane];
+        J.p = p;
+        J.q = q;
+        if (q < n) {
+          const cplx apq = A[p + ld * q];
+          const double mag = sqrt(cabs2(apq));
+          const double app = A[p + ld * p].x, aqq = A[q + ld * q].x;
+          rot = (mag > 1e-19 * fro) && (mag * mag > 1e-32 * fabs(app * aqq));
           if (rot) {
-            double ux = apq.x / mag, uy = apq.y / mag;
-            double tau = (aqq - app) / (2.0 * mag);
-            double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            double c = 1.0 / sqrt(1.0 + t * t);
-            double s = t * c;
-            s_rot[1] = c; s_rot[2] = s; s_rot[3] = ux; s_rot[4] = uy; s_rot[5] = t * mag;
-            s_flag[0] = 1;
+            const double tau = (aqq - app) / (2.0 * mag);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            J.c = 1.0 / sqrt(1.0 + t * t);
+            J.s = t * J.c;
+            J.u = mkc(apq.x / mag, apq.y / mag);
+            J.tm = t * mag;
+            J.app = app;
+            J.aqq = aqq;
           }
         }
-        __syncthreads();
-        if (s_rot[0] != 0.0) {
-          const double c = s_rot[1], s = s_rot[2];
-          const cplx u = mkc(s_rot[3], s_rot[4]);
-          const cplx uc = cconj(u);
-          for (int k = tid; k < n; k += blockDim.x) {
-            cplx vp = V[k + ld * p], vq = V[k + ld * q];
-            V[k + ld * p] = csub(cscale(vp, c), cscale(cmul(uc, vq), s));
-            V[k + ld * q] = cadd(cscale(cmul(u, vp), s), cscale(vq, c));
-            if (k == p || k == q) continue;
-            cplx akp = A[k + ld * p], akq = A[k + ld * q];
-            cplx nkp = csub(cscale(akp, c), cscale(cmul(uc, akq), s));
-            cplx nkq = cadd(cscale(cmul(u, akp), s), cscale(akq, c));
-            A[k + ld * p] = nkp; A[p + ld * k] = cconj(nkp);
-            A[k + ld * q] = nkq; A[q + ld * k] = cconj(nkq);
-          }
-          if (tid == 0) {
-            const double tm = s_rot[5];
-            A[p + ld * p] = mkc(A[p + ld * p].x - tm, 0.0);
-            A[q + ld * q] = mkc(A[q + ld * q].x + tm, 0.0);
-            A[p + ld * q] = mkc(0, 0);
-            A[q + ld * p] = mkc(0, 0);
-          }
-        }
-        __syncthreads();
+        J.rot = rot;
       }
+      const unsigned ballot = __ballot_sync(0xffffffffu, rot);
+      __syncwarp();
+      if (ballot == 0) continue;
+      any = true;
+      // column rotations: row `lane` of A and V
+      if (lane < n) {
+        for (int j = 0; j < npair; ++j) {
+          const JacRot& J = R[j];
+          if (!J.rot) continue;
+          const cplx uc = cconj(J.u);
+          cplx ap = A[lane + ld * J.p], aq = A[lane + ld * J.q];
+          A[lane + ld * J.p] = csub(cscale(ap, J.c), cscale(cmul(uc, aq), J.s));
+          A[lane + ld * J.q] = cadd(cscale(cmul(J.u, ap), J.s), cscale(aq, J.c));
+          cplx vp = V[lane + ld * J.p], vq = V[lane + ld * J.q];
+          V[lane + ld * J.p] = csub(cscale(vp, J.c), cscale(cmul(uc, vq), J.s));
+          V[lane + ld * J.q] = cadd(cscale(cmul(J.u, vp), J.s), cscale(vq, J.c));
+        }
+      }
+      __syncwarp();
+      // row rotations: column `lane` of A
+      if (lane < n) {
+        for (int j = 0; j < npair; ++j) {
+          const JacRot& J = R[j];
+          if (!J.rot) continue;
+          cplx ap = A[J.p + ld * lane], aq = A[J.q + ld * lane];
+          A[J.p + ld * lane] = csub(cscale(ap, J.c), cscale(cmul(J.u, aq), J.s));
+          A[J.q + ld * lane] = cadd(cscale(cmul(cconj(J.u), ap), J.s), cscale(aq, J.c));
+        }
+      }
+      __syncwarp();
+      // the rotated 2x2 blocks in closed form (other pairs never touch them)
+      if (lane < npair && rot) {
+        const JacRot& J = R[lane];
+        A[J.p + ld * J.p] = mkc(J.app - J.tm, 0.0);
+        A[J.q + ld * J.q] = mkc(J.aqq + J.tm, 0.0);
+        A[J.p + ld * J.q] = mkc(0, 0);
+        A[J.q + ld * J.p] = mkc(0, 0);
+      }
+      __syncwarp();
     }
-    if (s_flag[0] == 0) { converged = true; break; }
-    __syncthreads();
+    converged = !any;
   }
   *ok = converged;
 }
 
-__global__ void __launch_bounds__(64) reginv_kernel(const RegInvDesc* __restrict__ descs, const MFOp* __restrict__ ops,
+__global__ void __launch_bounds__(32) reginv_kernel(const RegInvDesc* __restrict__ descs, const MFOp* __restrict__ ops,
                                                     int* status) {
   __shared__ cplx A[MAXN_SPF * MAXN_SPF];
   __shared__ cplx V[MAXN_SPF * MAXN_SPF];
   __shared__ cplx Inv[MAXN_SPF * MAXN_SPF];
   __shared__ double w[MAXN_SPF];
-  __shared__ int s_flag[1];
-  __shared__ double s_rot[8];
+  __shared__ JacRot R[MAXN_SPF / 2];
   const RegInvDesc& d = descs[blockIdx.x];
   const int n = d.n, ld = MAXN_SPF;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -483,7 +545,7 @@ __global__ void __launch_bounds__(64) reginv_kernel(const RegInvDesc* __restrict
   }
   __syncthreads();
   bool ok;
-  jacobi_herm(A, V, n, ld, s_flag, s_rot, &ok);
+  jacobi_herm(A, V, n, ld, R, &ok);
   if (!ok && threadIdx.x == 0) atomicOr(status, DEVST_EIG_NOCONV);
   if (threadIdx.x < n) {
     double wv = A[threadIdx.x + ld * threadIdx.x].x;
@@ -522,7 +584,7 @@ __global__ void __launch_bounds__(64) reginv_kernel(const RegInvDesc* __restrict
 
 void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st) {
   if (ndesc <= 0) return;
-  reginv_kernel<<<ndesc, 64, 0, st>>>(d_descs, d_ops, d_status);
+  reginv_kernel<<<ndesc, 32, 0, st>>>(d_descs, d_ops, d_status);
 }
 
 // Tridiagonal eigenproblem of the Lanczos matrix (dstev, cmf2_integration.f90:85)
@@ -530,8 +592,7 @@ __global__ void tridiag_kernel(const double* alpha, const double* beta, int n, d
                                int* status) {
   __shared__ cplx A[MAXN_SPF * MAXN_SPF];
   __shared__ cplx V[MAXN_SPF * MAXN_SPF];
-  __shared__ int s_flag[1];
-  __shared__ double s_rot[8];
+  __shared__ JacRot R[MAXN_SPF / 2];
   const int ld = MAXN_SPF;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int i = e % n, j = e / n;
@@ -543,7 +604,7 @@ __global__ void tridiag_kernel(const double* alpha, const double* beta, int n, d
   }
   __syncthreads();
   bool ok;
-  jacobi_herm(A, V, n, ld, s_flag, s_rot, &ok);
+  jacobi_herm(A, V, n, ld, R, &ok);
   if (!ok && threadIdx.x == 0) atomicOr(status, DEVST_EIG_NOCONV);
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int i = e % n, j = e / n;
@@ -554,7 +615,7 @@ __global__ void tridiag_kernel(const double* alpha, const double* beta, int n, d
 
 void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, double* evals, double* evecs,
                            int* d_status, cudaStream_t st) {
-  tridiag_kernel<<<1, 64, 0, st>>>(alpha, beta, n, evals, evecs, d_status);
+  tridiag_kernel<<<1, 32, 0, st>>>(alpha, beta, n, evals, evecs, d_status);
 }
 
 // ---------------------------------------------------------------------------
@@ -950,47 +1011,102 @@ void launch_snap(const SnapSeg* segs, int nseg, cplx* flat, long long E, int sca
   snap_gather_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(segs, nseg, flat, E, scatter);
 }
 
-// Features of every entry from its three last values z0, z1, z2 (times t0<t1<t2):
-// z_i / s (s = max |z_i|), (t1-t0)/(t2-t1), h/(t2-t1).
-__global__ void mfx_features_kernel(const cplx* __restrict__ z0, const cplx* __restrict__ z1,
-                                    const cplx* __restrict__ z2, float r1, float r2, float* __restrict__ X,
+// Learned mean-field extrapolation.  Each entry z of the snapshot has its values
+// z_0..z_4 at the last five step starts.  Newton increments at tau:
+// inc_o(tau) = P_o(tau) - P_{o-1}(tau), P_o the Lagrange polynomial through the
+// last o+1 values (P_0 = z_4), with host-computed weights c.inc[tau][o-1][j].
+// The scale S is the RMS over all entries of |inc_1| at the step end.
+
+// S = sqrt(mean |inc_1(end)|^2): one block, fixed-order grid-stride sums.
+__global__ void __launch_bounds__(1024) mfx_scale_kernel(MfxHist hz, MfxCoef c, double* __restrict__ S,
+                                                         long long E) {
+  __shared__ double red[1024];
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < E; i += blockDim.x) {
+    cplx v = mkc(0, 0);
+#pragma unroll
+    for (int j = 0; j < MFX_NHIST; ++j) {
+      const cplx z = hz.z[j][i];
+      v.x += c.inc[1][0][j] * z.x;
+      v.y += c.inc[1][0][j] * z.y;
+    }
+    acc += cabs2(v);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) S[0] = fmax(sqrt(red[0] / (double)(E > 0 ? E : 1)), 1e-300);
+}
+
+// Network inputs per entry: Re/Im of inc_1..inc_4 at the half step and the step
+// end divided by S, then the step-length ratios; each divided by its column scale.
+__global__ void mfx_features_kernel(MfxHist hz, MfxCoef c, const double* __restrict__ S, float* __restrict__ X,
                                     long long E) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= E) return;
-  const cplx a = z0[i], b = z1[i], c = z2[i];
-  double s = fmax(sqrt(cabs2(a)), fmax(sqrt(cabs2(b)), sqrt(cabs2(c))));
-  s = fmax(s, 1e-300);
-  const double q = 1.0 / s;
-  float* x = X + 8 * i;
-  x[0] = (float)(a.x * q); x[1] = (float)(a.y * q);
-  x[2] = (float)(b.x * q); x[3] = (float)(b.y * q);
-  x[4] = (float)(c.x * q); x[5] = (float)(c.y * q);
-  x[6] = r1; x[7] = r2;
-}
-void launch_mfx_features(const cplx* z0, const cplx* z1, const cplx* z2, float r1, float r2, float* X, long long E,
-                         cudaStream_t st) {
-  if (E <= 0) return;
-  mfx_features_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(z0, z1, z2, r1, r2, X, E);
+  cplx z[MFX_NHIST];
+#pragma unroll
+  for (int j = 0; j < MFX_NHIST; ++j) z[j] = hz.z[j][i];
+  const double q = 1.0 / S[0];
+  float* x = X + (long long)MFX_NFEAT * i;
+  int col = 0;
+#pragma unroll
+  for (int tau = 0; tau < 2; ++tau) {
+#pragma unroll
+    for (int o = 0; o < MFX_NHIST - 1; ++o) {
+      cplx v = mkc(0, 0);
+#pragma unroll
+      for (int j = 0; j < MFX_NHIST; ++j) {
+        v.x += c.inc[tau][o][j] * z[j].x;
+        v.y += c.inc[tau][o][j] * z[j].y;
+      }
+      x[col] = (float)(v.x * q / c.fscale[col]);
+      ++col;
+      x[col] = (float)(v.y * q / c.fscale[col]);
+      ++col;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < MFX_NHIST - 1; ++r, ++col) x[col] = (float)(c.ratio[r] / c.fscale[col]);
 }
 
-// z(tau) = quadratic extrapolation + s * tscale * y for the half step and the step end
-__global__ void mfx_combine_kernel(const cplx* __restrict__ z0, const cplx* __restrict__ z1,
-                                   const cplx* __restrict__ z2, MfxWeights w, const float* __restrict__ Y,
-                                   double tscale, cplx* __restrict__ half, cplx* __restrict__ full, long long E) {
+// z(tau) = quartic extrapolation + S * tscale * y at the half step and the step end
+__global__ void mfx_combine_kernel(MfxHist hz, MfxCoef c, const float* __restrict__ Y, const double* __restrict__ S,
+                                   cplx* __restrict__ half, cplx* __restrict__ full, long long E) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= E) return;
-  const cplx a = z0[i], b = z1[i], c = z2[i];
-  double s = fmax(sqrt(cabs2(a)), fmax(sqrt(cabs2(b)), sqrt(cabs2(c))));
-  s = fmax(s, 1e-300);
-  const float* y = Y + 4 * i;
-  const double f = s * tscale;
-  half[i] = mkc(w.h[0] * a.x + w.h[1] * b.x + w.h[2] * c.x + f * y[0],
-                w.h[0] * a.y + w.h[1] * b.y + w.h[2] * c.y + f * y[1]);
-  full[i] = mkc(w.f[0] * a.x + w.f[1] * b.x + w.f[2] * c.x + f * y[2],
-                w.f[0] * a.y + w.f[1] * b.y + w.f[2] * c.y + f * y[3]);
+  cplx z[MFX_NHIST];
+#pragma unroll
+  for (int j = 0; j < MFX_NHIST; ++j) z[j] = hz.z[j][i];
+  const float* y = Y + (long long)MFX_NOUT * i;
+  const double s = S[0];
+  cplx out[2];
+#pragma unroll
+  for (int tau = 0; tau < 2; ++tau) {
+    cplx v = mkc(0, 0);
+#pragma unroll
+    for (int j = 0; j < MFX_NHIST; ++j) {
+      v.x += c.base[tau][j] * z[j].x;
+      v.y += c.base[tau][j] * z[j].y;
+    }
+    v.x += s * c.tscale[2 * tau] * (double)y[2 * tau];
+    v.y += s * c.tscale[2 * tau + 1] * (double)y[2 * tau + 1];
+    out[tau] = v;
+  }
+  half[i] = out[0];
+  full[i] = out[1];
 }
-void launch_mfx_combine(const cplx* z0, const cplx* z1, const cplx* z2, const MfxWeights& w, const float* Y,
-                        double tscale, cplx* half, cplx* full, long long E, cudaStream_t st) {
+
+void launch_mfx_features(const MfxHist& hz, const MfxCoef& c, double* S, float* X, long long E, cudaStream_t st) {
   if (E <= 0) return;
-  mfx_combine_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(z0, z1, z2, w, Y, tscale, half, full, E);
+  mfx_scale_kernel<<<1, 1024, 0, st>>>(hz, c, S, E);
+  mfx_features_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(hz, c, S, X, E);
+}
+void launch_mfx_combine(const MfxHist& hz, const MfxCoef& c, const float* Y, const double* S, cplx* half, cplx* full,
+                        long long E, cudaStream_t st) {
+  if (E <= 0) return;
+  mfx_combine_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(hz, c, Y, S, half, full, E);
 }

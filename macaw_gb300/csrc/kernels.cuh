@@ -63,11 +63,12 @@ struct H1Desc {
   const cplx* phi_l;
   cplx* ophi;              // G x n2, operator applied to phi_r
   cplx* h;                 // n1 x n2 (ld n1); nullptr: only ophi is produced
+  cplx* X;                 // n1 x n2 scratch: phi_l^H ophi before the Hermitian part
   int G, n1, n2;
   int same_state;
   int ndof;
   int ng[MAXDOF_MODE];
-  int optype[MAXDOF_MODE]; // 0 none, 1 dense (from the right), 2 diagonal
+  int optype[MAXDOF_MODE]; // 0 none, 1 dense real, 2 diagonal, 3 dense imaginary (i x real)
   const cplx* mat[MAXDOF_MODE];
 };
 
@@ -140,8 +141,21 @@ struct SnapSeg {
   cplx* ptr;               // matrix storage
   long long offset;        // first index in the flat snapshot
 };
-struct MfxWeights {
-  double h[3], f[3];       // Lagrange weights of t0, t1, t2 at the half step and the step end
+// Learned mean-field extrapolation: five step-start snapshots, 20 network inputs
+// (Newton increments of orders 1-4 at the half step and the step end, Re/Im, and
+// four step-length ratios), 4 outputs (Re/Im residual at the half step and end).
+#define MFX_NHIST 5
+#define MFX_NFEAT 20
+#define MFX_NOUT 4
+struct MfxHist {
+  const cplx* z[MFX_NHIST];  // oldest first
+};
+struct MfxCoef {
+  double inc[2][MFX_NHIST - 1][MFX_NHIST];  // [half, end][order-1][history point]
+  double base[2][MFX_NHIST];                // quartic extrapolation weights (all five points)
+  double ratio[MFX_NHIST - 1];              // (t1-t0, t2-t1, t3-t2, h) / (t4-t3)
+  double fscale[MFX_NFEAT];                 // input column scales
+  double tscale[MFX_NOUT];                  // output column scales
 };
 
 struct StageArgs {
@@ -155,7 +169,8 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
                  int prec = 0);
 void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec = 0);
 void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st);
-void launch_h1(const H1Desc* d_descs, int ndesc, size_t smem_bytes, cudaStream_t st);
+// with_h: also h1mode (second launch: the Hermitian part of same-state matrices)
+void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, bool with_h, cudaStream_t st);
 void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st);
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
                 cplx der_factor, int* d_status, cudaStream_t st);
@@ -178,12 +193,72 @@ void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_a
                      double* alpha_out, long long n, cudaStream_t st);
 void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st);
 void launch_snap(const SnapSeg* segs, int nseg, cplx* flat, long long E, int scatter, cudaStream_t st);
-void launch_mfx_features(const cplx* z0, const cplx* z1, const cplx* z2, float r1, float r2, float* X, long long E,
-                         cudaStream_t st);
-void launch_mfx_combine(const cplx* z0, const cplx* z1, const cplx* z2, const MfxWeights& w, const float* Y,
-                        double tscale, cplx* half, cplx* full, long long E, cudaStream_t st);
+void launch_mfx_features(const MfxHist& hz, const MfxCoef& c, double* S, float* X, long long E, cudaStream_t st);
+void launch_mfx_combine(const MfxHist& hz, const MfxCoef& c, const float* Y, const double* S, cplx* half, cplx* full,
+                        long long E, cudaStream_t st);
 // MLP forward on a given stream (mlp.cu): input buffer for M rows, then the output
 struct mctdh_mlp;
 float* mlp_input_buffer(mctdh_mlp* m, long long M);
 const float* mlp_forward_on(mctdh_mlp* m, long long M, cudaStream_t st);
+bool mlp_has_shape(const mctdh_mlp* m, int din, int dout);
 double measure_fp64_tflops();
+
+// ---------------------------------------------------------------------------
+// Gaussian (G-MCTDH) modes (gwp.cu).  A Gaussian SPF j of a mode with d DOFs is
+// g_j(x) = exp(sum_k a[k,j] x_k^2 + xi[k,j] x_k): widths a (real, fixed, GWPa
+// layout a[k + lda*j]) and complex parameters xi (the psi block, xi[k + d*j]).
+// ---------------------------------------------------------------------------
+#define GWP_MAXDOF 16    // DOFs of one Gaussian mode
+#define GWP_QR_PW 8      // panel width of the regularised least-squares QR
+
+struct GwpOvlDesc {      // S(j1, j2) = <g1_j1 | g2_j2> (normalised), n1 x n2 (ld n1)
+  const cplx* xi1;
+  const cplx* xi2;
+  const double* a;
+  cplx* out;
+  int nmd, lda, n1, n2;
+  int kind;              // 0: same parameter set (diagonal 1, lower = conj upper); 1: full;
+                         // 2: conjugate transpose of the full overlap with the sets swapped
+  int pad;
+};
+struct GwpH1Desc {       // h1mode of a Gaussian mode (hamilton.f90:494-524)
+  const cplx* xi1;
+  const cplx* xi2;
+  const double* a;
+  const cplx* S;         // overlap of the two parameter sets, n1 x n2
+  cplx* out;
+  int nmd, lda, n1, n2;
+  int same_state;        // 1: Hermitian from the upper triangle
+  int ops[GWP_MAXDOF];   // primitive operator code per DOF (0 = identity)
+};
+struct GwpYOp {          // one operator of the Y vector of Calc_CY (gmctdh_objects.f90:1285-1326)
+  const cplx* xi2;       // parameters of the right state
+  const cplx* S12;       // overlap (left state, right state), n x n2
+  const cplx* h;         // h1mode of the operator, n x n2
+  const cplx* mf;        // mean field of the operator, n x n2
+  int n2;
+  int ops[GWP_MAXDOF];
+};
+struct GwpCYDesc {       // one (Gaussian mode, state) block of Calc_CY and the parameter solve
+  const cplx* xi;        // parameters (d x n)
+  const double* a;
+  const cplx* S;         // S00 (n x n)
+  const cplx* Sm1;       // Tikhonov inverse of S00 (n x n)
+  const cplx* rho;       // density matrix of the mode (n x n)
+  cplx* Sa0;             // nG x n, nG = d * n
+  cplx* Sa0Sm1;          // nG x n
+  cplx* M;               // (2 nG) x (nG + 1) least-squares system [C, Y; eps I, 0], column-major
+  cplx* R;               // nG x nG: R factor entries of the panels
+  cplx* x;               // nG solution (parameter derivative before der_factor)
+  long long dxi_offset;  // where der_factor * x goes in the derivative vector
+  cplx* tau;             // n x n (derivatives.f90:201-234)
+  int nmd, lda, n, nG;
+  int op_first, op_count;
+  double eps;            // eps_C
+};
+void launch_gwp_ovl(const GwpOvlDesc* d, int nd, cudaStream_t st);
+void launch_gwp_h1(const GwpH1Desc* d, int nd, cudaStream_t st);
+// Calc_CY and the Tikhonov parameter solve (StdRegSol 'tikh', maths.f90:87-162)
+// for nd (mode, state) blocks; maxG = max nG.  Then dxi = der * x and tau.
+void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, const GwpYOp* ops, cudaStream_t st);
+void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out, int* status, cudaStream_t st);

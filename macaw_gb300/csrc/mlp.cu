@@ -514,3 +514,7 @@ const float* mlp_forward_on(mctdh_mlp* m, long long M, cudaStream_t st) {
   m->forward_on(M, st);
   return m->Y;
 }
+
+bool mlp_has_shape(const mctdh_mlp* m, int din, int dout) {
+  return !m->L.empty() && m->L[0].K == din && m->L.back().N == dout;
+}

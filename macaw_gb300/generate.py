@@ -146,7 +146,7 @@ def ensemble(count: int = 512, seed: int = SEED0 + 2, max_conf: int = 1 << 20) -
 
 
 def gmctdh16(seed: int = SEED0 + 3, ngwp: int = 32, gwp_dofs: int = 12, dvr_grid: int = 32,
-             dvr_nspf: int = 6) -> Model:
+             dvr_nspf: int = 6, tfinal_fs: float = 100.0, eps_int: float = 1e-6) -> Model:
     """2-state LVC over 16 DOFs: 4 HO DVR modes + one Gaussian mode of 12 DOFs."""
     rng = np.random.default_rng(seed)
     ndof = 4 + gwp_dofs
@@ -160,7 +160,7 @@ def gmctdh16(seed: int = SEED0 + 3, ngwp: int = 32, gwp_dofs: int = 12, dvr_grid
     model = Model(nstates=2, mode_dofs=mode_dofs, multiset=[True] * 5, nspf=nspf,
                   dvr_type=["HO"] * 4 + ["gwp"] * gwp_dofs, ngp=[dvr_grid] * 4 + [101] * gwp_dofs,
                   dvrpar=[(0.0, 1.0)] * 4 + [(-10.0, 10.0)] * gwp_dofs, terms=terms,
-                  tfinal=100.0 / AU2FS, tout=0.5 / AU2FS, eps_int=1e-6, eps_ovl=1e-8, eps_C=1e-8,
+                  tfinal=tfinal_fs / AU2FS, tout=0.5 / AU2FS, eps_int=eps_int, eps_ovl=1e-8, eps_C=1e-8,
                   int_type=INT_RK45, init_state=1, label="gmctdh16")
     for d in range(4, ndof):
         model.init_spf[d] = ("gwp", (0, 0.0, 0.0, 0.707107, 0.8, 0.9))

@@ -1,14 +1,21 @@
-"""Learned mean-field extrapolation for CMF2: data, training and use.
+"""Learned mean-field extrapolation for CMF2: data, training and evaluation.
 
 A snapshot is every density matrix and mean field of the grid modes at one
 time (``GpuCore.mfx_size()`` complex entries).  Plain CMF2 steps recorded with
 ``GpuCore.mfx_record`` give, per accepted step k, the snapshot at the step
 start t_k and at its half step t_k + h_k/2; the snapshot at the step end is
-the next step's start.  For every entry z the network sees its last three
-step-start values (z0, z1, z2 at t_{k-2}, t_{k-1}, t_k) scaled by
-s = max|z_i|, and the ratios (t1-t0)/(t2-t1) and h/(t2-t1); it predicts the
-correction to the quadratic extrapolation of z to t_k + h/2 and t_k + h, in
-units of s * tscale.  The same features are built on the device
+the next step's start.
+
+For a step of length h after the step starts t_0 < ... < t_4 (values z_0..z_4
+of every entry), P_o(tau) is the Lagrange polynomial through the last o+1
+values and inc_o = P_o - P_{o-1} (P_0 = z_4) its Newton increment.  The
+extrapolation without the network is P_4 (quartic through the five step
+starts).  The network sees, per entry, Re/Im of inc_1..inc_4 at the half
+step and at the step end divided by S (the RMS over all entries of |inc_1| at
+the step end), and the step-length ratios (t1-t0, t2-t1, t3-t2, h) / (t4-t3);
+every input column is divided by its scale ``fscale``.  It predicts the residual
+z(tau) - P_4(tau) at the half step and the step end in units of S times the
+output column scale ``tscale``.  The device builds the same inputs
 (mfx_features_kernel) when the trained network replaces the half-step mean
 fields inside CMF2 (cmf2_base.f90:122-130).
 """
@@ -18,70 +25,143 @@ from typing import Tuple
 
 import numpy as np
 
-WIDTHS = (8, 256, 256, 256, 4)
+NHIST = 5
+NFEAT = 20
+NOUT = 4
+WIDTHS = (NFEAT, 256, 256, 256, NOUT)
+GATE_GAIN = 0.9   # a correction column is kept when it removes >= 10 % of the validation residual
 
 
-def lagrange_weights(t0, t1, t2, tau):
-    return np.array([(tau - t1) * (tau - t2) / ((t0 - t1) * (t0 - t2)),
-                     (tau - t0) * (tau - t2) / ((t1 - t0) * (t1 - t2)),
-                     (tau - t0) * (tau - t1) / ((t2 - t0) * (t2 - t1))])
+def lagrange_tail(ts, first, tau):
+    """Weights at tau of the polynomial through ts[first:] (zero for earlier points)."""
+    n = len(ts)
+    w = np.zeros(n)
+    for j in range(first, n):
+        p = 1.0
+        for k in range(first, n):
+            if k != j:
+                p *= (tau - ts[k]) / (ts[j] - ts[k])
+        w[j] = p
+    return w
 
 
-def features(z0, z1, z2, t0, t1, t2, h):
-    s = np.maximum(np.maximum(np.abs(z0), np.abs(z1)), np.maximum(np.abs(z2), 1e-300))
-    X = np.empty((z0.size, 8), dtype=np.float32)
-    for j, z in enumerate((z0, z1, z2)):
-        X[:, 2 * j] = (z.real / s).astype(np.float32)
-        X[:, 2 * j + 1] = (z.imag / s).astype(np.float32)
-    X[:, 6] = np.float32((t1 - t0) / (t2 - t1))
-    X[:, 7] = np.float32(h / (t2 - t1))
-    return X, s
+def coefficients(ts, h):
+    """Increment weights inc[tau][o-1][j], quartic weights base[tau][j] and the ratios."""
+    n = len(ts)
+    inc = np.zeros((2, n - 1, n))
+    base = np.zeros((2, n))
+    for it, tau in enumerate((ts[-1] + 0.5 * h, ts[-1] + h)):
+        prev = np.zeros(n)
+        prev[-1] = 1.0
+        for o in range(1, n):
+            w = lagrange_tail(ts, n - 1 - o, tau)
+            inc[it, o - 1] = w - prev
+            prev = w
+        base[it] = prev
+    d = ts[-1] - ts[-2]
+    ratio = np.array([(ts[j + 1] - ts[j]) / d for j in range(n - 2)] + [h / d])
+    return inc, base, ratio
 
 
-def quadratic(z0, z1, z2, t0, t1, t2, tau):
-    w = lagrange_weights(t0, t1, t2, tau)
-    return w[0] * z0 + w[1] * z1 + w[2] * z2
+def features(Z, ts, h):
+    """Unscaled inputs (E, 20), the quartic extrapolations (2, E) and S for the
+    history Z (5, E) at times ts."""
+    inc, base, ratio = coefficients(ts, h)
+    incs = np.einsum("toj,je->toe", inc, Z)          # (2, 4, E)
+    S = max(float(np.sqrt(np.mean(np.abs(incs[1, 0]) ** 2))), 1e-300)
+    E = Z.shape[1]
+    X = np.empty((E, NFEAT))
+    col = 0
+    for it in range(2):
+        for o in range(NHIST - 1):
+            X[:, col] = incs[it, o].real / S
+            X[:, col + 1] = incs[it, o].imag / S
+            col += 2
+    X[:, col:] = ratio[None, :]
+    Q = base @ Z
+    return X, Q, S
 
 
 def build_dataset(t0, h, s0, sh) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
-    """Samples from consecutive recorded steps: features X, raw residual targets R
-    (in units of s; columns Re/Im at the half step, Re/Im at the step end), and the
-    step index of every row."""
+    """Samples of consecutive recorded steps: unscaled inputs X, residual targets R
+    of the quartic extrapolation (Re/Im at the half step, Re/Im at the step end,
+    in units of S) and the step index of every row."""
     Xs, Rs, ks = [], [], []
-    for k in range(2, len(t0) - 1):
-        if not np.isclose(t0[k + 1], t0[k] + h[k], rtol=0, atol=1e-9 * max(1.0, abs(t0[k]))):
+    for k in range(NHIST - 1, len(t0) - 1):
+        ok = all(np.isclose(t0[j + 1], t0[j] + h[j], rtol=0, atol=1e-9 * max(1.0, abs(t0[j])))
+                 for j in range(k - NHIST + 1, k + 1))
+        if not ok:
             continue
-        ta, tb, tc = t0[k - 2], t0[k - 1], t0[k]
-        z0, z1, z2 = s0[k - 2], s0[k - 1], s0[k]
-        X, s = features(z0, z1, z2, ta, tb, tc, h[k])
-        qh = quadratic(z0, z1, z2, ta, tb, tc, tc + 0.5 * h[k])
-        qf = quadratic(z0, z1, z2, ta, tb, tc, tc + h[k])
-        rh = (sh[k] - qh) / s
-        rf = (s0[k + 1] - qf) / s
-        R = np.stack([rh.real, rh.imag, rf.real, rf.imag], axis=1)
+        ts = t0[k - NHIST + 1:k + 1]
+        X, Q, S = features(s0[k - NHIST + 1:k + 1], ts, h[k])
+        rh = (sh[k] - Q[0]) / S
+        rf = (s0[k + 1] - Q[1]) / S
         Xs.append(X)
-        Rs.append(R)
+        Rs.append(np.stack([rh.real, rh.imag, rf.real, rf.imag], axis=1))
         ks.append(np.full(len(X), k))
     if not Xs:
         raise ValueError("not enough consecutive recorded steps")
     return np.concatenate(Xs), np.concatenate(Rs), np.concatenate(ks)
 
 
-def train(X, R, seed=1, epochs=20, batch=8192, lr=1e-3, widths=WIDTHS):
-    """Train the GPU network on residuals R scaled by their RMS; returns (net, tscale, loss)."""
+def train(X, R, steps=None, seed=1, epochs=20, batch=4096, lr=1e-3, widths=WIDTHS, val_frac=0.2):
+    """Train the GPU network; returns (net, fscale, tscale, loss).  Input columns
+    are scaled to an RMS of 1/4 (keeping tanh near its linear range), targets to 1.
+
+    The last `val_frac` of the steps (or of the rows, without `steps`) are held
+    back: per output column the network's correction is shrunk by the factor
+    beta in [0, 1] that minimises the residual on them (folded into tscale), and
+    switched off (beta = 0) unless it removes at least 10 % of that residual, so
+    a correction that does not generalise is not applied."""
     from .capi import Mlp
-    tscale = float(np.sqrt(np.mean(R ** 2))) or 1.0
+    if steps is not None:
+        cut = np.quantile(np.unique(steps), 1.0 - val_frac)
+        fit, val = steps <= cut, steps > cut
+    else:
+        n_fit = int(len(X) * (1.0 - val_frac))
+        fit = np.zeros(len(X), dtype=bool)
+        fit[:n_fit] = True
+        val = ~fit
+    fscale = 4.0 * np.sqrt(np.mean(X[fit] ** 2, axis=0))
+    fscale = np.where(fscale > 0, fscale, 1.0)
+    tscale = np.sqrt(np.mean(R[fit] ** 2, axis=0))
+    tscale = np.where(tscale > 0, tscale, 1.0)
     net = Mlp(widths, seed=seed)
     rng = np.random.default_rng(seed)
-    perm = rng.permutation(len(X))
-    loss = net.train(X[perm], (R[perm] / tscale).astype(np.float32), batch=batch, epochs=epochs, lr=lr)
-    return net, tscale, loss
+    idx = np.flatnonzero(fit)[rng.permutation(int(fit.sum()))]
+    loss = net.train((X[idx] / fscale).astype(np.float32), (R[idx] / tscale).astype(np.float32),
+                     batch=batch, epochs=epochs, lr=lr)
+    if val.any():
+        P = predict(net, fscale, tscale, X[val])
+        Rv = R[val]
+        beta = np.clip(np.sum(P * Rv, axis=0) / np.maximum(np.sum(P * P, axis=0), 1e-300), 0.0, 1.0)
+        before = np.sum(Rv ** 2, axis=0)
+        after = np.sum((Rv - beta * P) ** 2, axis=0)
+        beta = np.where(after < GATE_GAIN * before, beta, 0.0)   # keep only clear gains
+        tscale = tscale * beta
+    return net, fscale, tscale, loss
 
 
-def prediction_errors(net, tscale, X, R):
-    """RMS of the half-step / step-end residual left by the quadratic extrapolation
-    alone (R) and by quadratic + network (R - prediction), in units of s."""
-    P = net.predict(X).astype(np.float64) * tscale
+def predict(net, fscale, tscale, X):
+    return net.predict((X / fscale).astype(np.float32)).astype(np.float64) * tscale
+
+
+def poly_residual(X, R, order):
+    """Residual of the polynomial through the last order+1 step starts (1 <= order <= 4),
+    from the quartic residual R by adding back the increments above `order`."""
+    P = np.zeros_like(R)
+    for o in range(order + 1, NHIST):
+        P[:, 0] += X[:, 2 * (o - 1)]
+        P[:, 1] += X[:, 2 * (o - 1) + 1]
+        P[:, 2] += X[:, 8 + 2 * (o - 1)]
+        P[:, 3] += X[:, 8 + 2 * (o - 1) + 1]
+    return R + P
+
+
+def prediction_errors(net, fscale, tscale, X, R):
+    """RMS per output column of the residual left by the quartic extrapolation
+    alone (R) and by quartic + network, in units of S."""
+    P = predict(net, fscale, tscale, X)
     base = np.sqrt(np.mean(R ** 2, axis=0))
     left = np.sqrt(np.mean((R - P) ** 2, axis=0))
     return base, left

@@ -826,15 +826,17 @@ class Oracle:
             out.append(slice(o, o + n))
         return out
 
-    def rk_spf_ck(self, psi: np.ndarray, mode: int, htry: float):
-        """rk_SPF_ck, DVR branch (cmf2_integration.f90:105-253)."""
+    def rk_spf_ck(self, psi: np.ndarray, mode: int, htry: float, dopri: bool = False):
+        """rk_SPF_ck / rk_SPF_dp, DVR branch (cmf2_integration.f90:105-253, :257-412).
+        Dormand-Prince adds a 7th derivative at the 5th-order solution (:386-393)."""
         md = self.m
         sl = self._spf_slices(mode)
+        tab = DP if dopri else CK
         dt = htry
         while True:
             k = [self.calc_der_spf_dvr(psi, mode)]
             for st in range(1, 6):
-                b = CK["B"][st]
+                b = tab["B"][st]
                 pt = psi.copy()
                 for s_ in sl:
                     pt[s_] = psi[s_] + dt * sum(b[j] * k[j][s_] for j in range(len(b)))
@@ -842,11 +844,11 @@ class Oracle:
             ptemp = psi.copy()
             perr = psi.copy()
             for s_ in sl:
-                ptemp[s_] = psi[s_] + dt * (CK["C"][0] * k[0][s_] + CK["C"][2] * k[2][s_]
-                                            + CK["C"][3] * k[3][s_] + CK["C"][5] * k[5][s_])
-                perr[s_] = psi[s_] + dt * (CK["D"][0] * k[0][s_] + CK["D"][2] * k[2][s_]
-                                           + CK["D"][3] * k[3][s_] + CK["D"][4] * k[4][s_]
-                                           + CK["D"][5] * k[5][s_])
+                ptemp[s_] = psi[s_] + dt * sum(cj * k[j][s_] for j, cj in enumerate(tab["C"]) if cj != 0.0)
+            if dopri:
+                k.append(self.calc_der_spf_dvr(ptemp, mode))
+            for s_ in sl:
+                perr[s_] = psi[s_] + dt * sum(dj * k[j][s_] for j, dj in enumerate(tab["D"]) if dj != 0.0)
             error = self.calc_err_spf_dvr(ptemp, perr, mode) / md.eps_psi
             if error < 1.0:
                 break
@@ -861,14 +863,14 @@ class Oracle:
         return out, dt, hnext
 
     def propagate_spf(self, dt: float, mode: int, psi: np.ndarray) -> np.ndarray:
-        """propagate_SPF (cmf2_base.f90:210-260), Cash-Karp branch."""
+        """propagate_SPF (cmf2_base.f90:210-260): Cash-Karp (1) or Dormand-Prince (2)."""
         md = self.m
-        if md.int_type_psi != 1:
-            raise OracleError("only the Cash-Karp SPF integrator is restated")
+        if md.int_type_psi not in (1, 2):
+            raise OracleError("SPF integrator must be rk45 (1) or dopri (2)")
         done = 0.0
         step = dt
         while True:
-            psi, sdone, snext = self.rk_spf_ck(psi, mode, step)
+            psi, sdone, snext = self.rk_spf_ck(psi, mode, step, dopri=md.int_type_psi == 2)
             done += sdone
             if done >= dt:
                 break

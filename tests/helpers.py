@@ -1,7 +1,7 @@
 """Shared test helpers: small seeded models and random MCTDH states."""
 import numpy as np
 
-from macaw_gb300.generate import lvc5, qvc
+from macaw_gb300.generate import gmctdh16, lvc5, qvc
 from macaw_gb300.model import initial_wavefunction, INT_CMF2, INT_RK45
 
 
@@ -15,13 +15,29 @@ def small_qvc(nstates=3, ndof=4, grid=6, nspf=4, integrator=INT_CMF2, eps_int=1e
                eps_int=eps_int, eps_lanczos=1e-8, eps_spf=1e-7, tfinal_fs=tfinal_fs)
 
 
-def random_state(model, seed=0, spread=1.0):
+def small_gmctdh(tfinal_fs=1.0, eps_int=1e-6):
+    """2-state LVC: 4 HO DVR modes (6 points, 3 SPFs) + one Gaussian mode of 2 DOFs
+    with 4 Gaussians per state (the G-MCTDH model at small size)."""
+    return gmctdh16(ngwp=4, gwp_dofs=2, dvr_grid=6, dvr_nspf=3, tfinal_fs=tfinal_fs, eps_int=eps_int)
+
+
+def random_state(model, seed=0, spread=1.0, gwp_shift=0.1):
     """Random normalised A and SPF blocks with orthonormal columns (per mode and state)."""
     rng = np.random.default_rng(seed)
     A = rng.normal(size=model.naconftot) + 1j * rng.normal(size=model.naconftot)
     A *= spread
     psi = np.zeros(model.dimpsi, dtype=np.complex128)
+    if model.modes_gwp:
+        # Gaussian parameters: the initial ones, displaced at random
+        _, psi0 = initial_wavefunction(model)
+        for m in model.modes_gwp:
+            for s in range(model.nstates):
+                o = int(model.ipsispf[m, s])
+                n = int(model.nspf[m, s]) * len(model.mode_dofs[m])
+                psi[o:o + n] = psi0[o:o + n] + gwp_shift * (rng.normal(size=n) + 1j * rng.normal(size=n))
     for m in range(model.nmodes):
+        if model.is_gwp_mode[m]:
+            continue
         for s in range(model.nstates):
             if (not model.multiset[m]) and s > 0:
                 continue

@@ -159,8 +159,11 @@ def test_rk45_free_running(core_cls):
     _compare(outs, ref, 10 * model.eps_int)
 
 
-def test_cmf2_step(core_cls):
+@pytest.mark.parametrize("int_type_psi", [1, 2])
+def test_cmf2_step(core_cls, int_type_psi):
+    """One CMF2 step; the SPFs integrated with Cash-Karp (1) or Dormand-Prince (2)."""
     model = small_qvc()
+    model.int_type_psi = int_type_psi
     A, psi = initial_wavefunction(model)
     o = Oracle(model)
     rA, rp, rh, rn, tries = o.cmf2(A, psi, 0.0, 1.0)
