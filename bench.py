@@ -339,6 +339,7 @@ def run_gpu(args):
                          "dpop": float(np.abs(cmp["mfx"]["pop"] - cmp["fp64"]["pop"]).max())},
                      "eom_per_s": mfxr["eom"] / (mfxr["ms"] * 1e-3),
                      "extrapolated_steps": mfx_stats["mlp_steps"], "fallbacks": mfx_stats["fallbacks"],
+                     "rejected": mfx_stats["rejected"], "last_step_end_mismatch": mfx_stats["last_rel"],
                      "training": {"rows": int(len(X)), "epochs": MFX_EPOCHS, "loss": tr_loss,
                                   "seconds": train_s,
                                   "data": f"the untimed FP64 CMF2 steps from 0 to {PRE_FS} fs"}},

@@ -215,7 +215,19 @@ int64_t mctdh_mfx_fetch(mctdh_ctx_t *ctx, int64_t maxrec, double *t0, double *h,
                         int64_t *n);
 int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, const double *fscale, const double *tscale,
                          double tol);
-int64_t mctdh_mfx_stats(mctdh_ctx_t *ctx, int64_t *mlp_steps, int64_t *fallbacks);
+/* predict: run the attached extrapolator on a given history (5 x E complex
+ * snapshots, oldest first, at times ts[5]) for a step of length h; writes the
+ * half-step and step-end snapshots (E complex each) and clears the history. */
+int64_t mctdh_mfx_predict(mctdh_ctx_t *ctx, const double *hist, const double *ts, double h, double *half,
+                          double *full);
+/* log: one row per CMF2 attempt of a context with extrapolation state
+ * (t, h, error estimate / eps_int, extrapolated 0/1, step-end mismatch or -1). */
+int64_t mctdh_mfx_log(mctdh_ctx_t *ctx, int64_t maxrows, double *rows, int64_t *n);
+/* stats: steps taken with extrapolated mean fields, steps redone because the
+ * step-end check failed, steps redone because the CMF2 error estimate rejected
+ * the extrapolated attempt, and the last step-end mismatch (-1 before any). */
+int64_t mctdh_mfx_stats(mctdh_ctx_t *ctx, int64_t *mlp_steps, int64_t *fallbacks, int64_t *rejected,
+                        double *last_rel);
 
 /* Last error message of the context (or of the last failed create when ctx is NULL). */
 const char *mctdh_last_error(mctdh_ctx_t *ctx);

@@ -98,8 +98,11 @@ def load_library() -> C.CDLL:
     lib.mctdh_mfx_record.argtypes = [vp, C.c_int64]
     lib.mctdh_mfx_fetch.argtypes = [vp, C.c_int64, DP, DP, DP, DP, I64P]
     lib.mctdh_mfx_attach.argtypes = [vp, vp, DP, DP, C.c_double]
-    lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P]
-    for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats"):
+    lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P, I64P, DP]
+    lib.mctdh_mfx_predict.argtypes = [vp, DP, DP, C.c_double, DP, DP]
+    lib.mctdh_mfx_log.argtypes = [vp, C.c_int64, DP, I64P]
+    for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
+                 "mctdh_mfx_predict", "mctdh_mfx_log"):
         getattr(lib, name).restype = C.c_int64
     lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
                                                  C.c_int64, C.c_void_p]
@@ -125,7 +128,8 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
-            "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats"]
+            "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
+            "mctdh_mfx_predict", "mctdh_mfx_log"]
 
 KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
                   "spf_derivative", "elementwise", "gaussian_block"]
@@ -404,10 +408,30 @@ class GpuCore:
             self._check(self.lib.mctdh_mfx_attach(self.h, mlp.h, fs.ctypes.data_as(DP), ts.ctypes.data_as(DP), tol))
         self._mlp_ref = mlp
 
+    def mfx_predict(self, hist, ts, h):
+        """The attached extrapolator on a given history (5, E) at times ts: (half, full)."""
+        Hs = np.ascontiguousarray(hist, dtype=np.complex128)
+        T = np.ascontiguousarray(ts, dtype=np.float64)
+        E = Hs.shape[1]
+        half = np.zeros(E, dtype=np.complex128)
+        full = np.zeros(E, dtype=np.complex128)
+        self._check(self.lib.mctdh_mfx_predict(self.h, Hs.ctypes.data_as(DP), T.ctypes.data_as(DP), h,
+                                               half.ctypes.data_as(DP), full.ctypes.data_as(DP)))
+        return half, full
+
+    def mfx_log(self):
+        """One row per CMF2 attempt: t, h, error / eps_int, extrapolated, step-end mismatch."""
+        n = C.c_int64()
+        self._check(self.lib.mctdh_mfx_log(self.h, 0, None, C.byref(n)))
+        rows = np.zeros((n.value, 5))
+        if n.value:
+            self._check(self.lib.mctdh_mfx_log(self.h, n.value, rows.ctypes.data_as(DP), C.byref(n)))
+        return rows
+
     def mfx_stats(self):
-        a, b = C.c_int64(), C.c_int64()
-        self._check(self.lib.mctdh_mfx_stats(self.h, C.byref(a), C.byref(b)))
-        return dict(mlp_steps=a.value, fallbacks=b.value)
+        a, b, r, x = C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
+        self._check(self.lib.mctdh_mfx_stats(self.h, C.byref(a), C.byref(b), C.byref(r), C.byref(x)))
+        return dict(mlp_steps=a.value, fallbacks=b.value, rejected=r.value, last_rel=x.value)
 
     def launch_count(self) -> int:
         return int(self.lib.mctdh_launch_count(self.h))

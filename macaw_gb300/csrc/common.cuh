@@ -69,6 +69,22 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29)));
 }
 
+// Element i of a tensor in either storage format (TF_C64 / TF_SPLIT).
+__device__ __forceinline__ cplx load_c(const cplx* p, long long i, int fmt) {
+  if (!fmt) return p[i];
+  const float4 w = reinterpret_cast<const float4*>(p)[i];
+  return make_double2(f2d_exact(w.x) + f2d_exact(w.z), f2d_exact(w.y) + f2d_exact(w.w));
+}
+// ... as an FP32 (re hi, im hi, re lo, im lo) split
+__device__ __forceinline__ float4 load_split(const cplx* p, long long i, int fmt) {
+  if (fmt) return reinterpret_cast<const float4*>(p)[i];
+  const cplx v = p[i];
+  float4 w;
+  split_d2f(v.x, w.x, w.z);
+  split_d2f(v.y, w.y, w.w);
+  return w;
+}
+
 // Status codes returned through the C-ABI (negative = error).
 enum {
   MCTDH_OK = 0,

@@ -77,6 +77,7 @@ T* upload_vec(DevArena& ar, const std::vector<T>& v) {
 struct TRef {
   cplx* p = nullptr;
   std::vector<int> shape;
+  int fmt = TF_C64;   // storage format of the tensor
 };
 long long prod_range(const std::vector<int>& s, int a, int b) {
   long long r = 1;
@@ -92,9 +93,13 @@ struct ProdBatch {
   int prec = 0;                  // 0 FP64, 1 split FP32, 2 split FP32 compensated
   double flops = 0, bytes = 0;   // algorithmic work of one launch
   void add(const cplx* X, cplx* Y, const cplx* M, int ldm, int conjT, const std::vector<int>& shape, int mode,
-           int nout, cplx alpha, int accumulate) {
+           int nout, cplx alpha, int accumulate, int xfmt = TF_C64, int yfmt = TF_C64) {
+    if (yfmt != TF_C64 && (accumulate || alpha.x != 1.0 || alpha.y != 0.0))
+      throw StatusError(MCTDH_EARG, "split-format output needs alpha = 1 without accumulation");
     ProdDesc pd;
     memset(&pd, 0, sizeof(pd));
+    pd.xfmt = xfmt;
+    pd.yfmt = yfmt;
     pd.X = X;
     pd.Y = Y;
     pd.M = M;
@@ -131,11 +136,14 @@ struct HoleBatch {
   int prec = 0;                  // 0 FP64, 2 compensated split FP32
   double flops = 0, bytes = 0;
   // returns index of the hole
-  int add(DevArena& ar, const cplx* X, const cplx* Y, long long L, long long R, int n1, int n2) {
+  int add(DevArena& ar, const cplx* X, const cplx* Y, long long L, long long R, int n1, int n2,
+          int xfmt = TF_C64, int yfmt = TF_C64) {
     HoleDesc hd;
     memset(&hd, 0, sizeof(hd));
     hd.X = X;
     hd.Y = Y;
+    hd.xfmt = xfmt;
+    hd.yfmt = yfmt;
     hd.L = L;
     hd.R = R;
     hd.n1 = n1;
@@ -282,6 +290,7 @@ struct Ctx {
 
   // DVR operator matrices on device: (dof, code) -> pointer
   std::map<std::pair<int, int>, cplx*> dofmat;
+  std::map<std::pair<int, int>, float2*> dofmatf;   // real coefficients split into FP32 (hi, lo)
   std::map<std::pair<int, int>, int> dofkind;
 
   // per (mode, op) storage
@@ -523,6 +532,13 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
         }
         c.dofmat[key] = upload_vec(c.ar, v);
         c.dofkind[key] = kind;
+        std::vector<float2> vf(v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+          const double x = (kind == 3) ? v[i].y : v[i].x;
+          const float hi = (float)x;
+          vf[i] = make_float2(hi, (float)(x - (double)hi));
+        }
+        c.dofmatf[key] = upload_vec(c.ar, vf);
       }
     }
   }
@@ -686,6 +702,7 @@ void plan_eom(Ctx& c) {
           auto key = std::make_pair(d, code);
           hd.optype[q] = c.dofkind[key];
           hd.mat[q] = c.dofmat[key];
+          hd.matf[q] = c.dofmatf[key];
         }
       }
       c.h1_of_mode[m].push_back((int)c.h1_h.size());
@@ -740,6 +757,8 @@ void plan_eom(Ctx& c) {
   // reference's left/right chains.
   c.chains.assign(f + 1, ProdBatch());
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
+  // split-precision contexts keep chain intermediates in the split storage format
+  const int chain_fmt = c.precision ? TF_SPLIT : TF_C64;
   std::map<std::pair<int, int>, int> mf_target;   // (m,k) -> red target
   auto mf_tg = [&](int im, int k) {
     auto key = std::make_pair(im, k);
@@ -785,9 +804,11 @@ void plan_eom(Ctx& c) {
       std::vector<int> ns = R[i - 1].shape;
       ns[jm] = n1;
       cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
-      c.chains[i].add(R[i - 1].p, out, c.hmat[jm][k], n1, 0, R[i - 1].shape, jm, n1, mkc(1, 0), 0);
+      c.chains[i].add(R[i - 1].p, out, c.hmat[jm][k], n1, 0, R[i - 1].shape, jm, n1, mkc(1, 0), 0, R[i - 1].fmt,
+                      chain_fmt);
       R[i].p = out;
       R[i].shape = ns;
+      R[i].fmt = chain_fmt;
     }
     L[0].p = c.d_in + c.aoff[s1];
     L[0].shape = c.shape_of(s1);
@@ -799,11 +820,13 @@ void plan_eom(Ctx& c) {
       std::vector<int> ns = L[i - 1].shape;
       ns[im] = n2;
       cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
-      c.chains[i].add(L[i - 1].p, out, c.hmat[im][k], n1, 1, L[i - 1].shape, im, n2, mkc(1, 0), 0);
+      c.chains[i].add(L[i - 1].p, out, c.hmat[im][k], n1, 1, L[i - 1].shape, im, n2, mkc(1, 0), 0, L[i - 1].fmt,
+                      chain_fmt);
       L[i].p = out;
       L[i].shape = ns;
+      L[i].fmt = chain_fmt;
     }
-    srcs[s1].push_back(SumSrc{R[f].p, cmul(c.der, c.ae[t])});
+    srcs[s1].push_back(SumSrc{R[f].p, cmul(c.der, c.ae[t]), R[f].fmt});
     c.general_terms.push_back(t);
     for (int im = 0; im < f; ++im) {
       const int k = c.ioper[im + f * t];
@@ -811,7 +834,7 @@ void plan_eom(Ctx& c) {
       const TRef& X = L[im];
       const TRef& Y = R[f - 1 - im];
       long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, f);
-      int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im]);
+      int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im], X.fmt, Y.fmt);
       hrefs.push_back(HoleRef{hidx, mf_tg(im, k), c.ae[t]});
     }
   }
@@ -830,8 +853,8 @@ void plan_eom(Ctx& c) {
     c.gmat[kv.first] = md.out;
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
-    c.gprods.add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0);
-    srcs[s].push_back(SumSrc{out, c.der});
+    c.gprods.add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0, TF_C64, chain_fmt);
+    srcs[s].push_back(SumSrc{out, c.der, chain_fmt});
   }
   for (int s = 0; s < c.nstates; ++s)
     if (c0[s].x != 0.0 || c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_in + c.aoff[s], cmul(c.der, c0[s])});
@@ -1029,6 +1052,7 @@ void plan_hb(Ctx& c) {
   const int f = c.nmodes;
   c.hb_chains.assign(f + 1, ProdBatch());
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
+  const int chain_fmt = c.precision ? TF_SPLIT : TF_C64;
   for (int t : c.general_terms) {
     const int s1 = c.lhs[t], s2 = c.rhs[t];
     TRef cur;
@@ -1043,19 +1067,20 @@ void plan_hb(Ctx& c) {
       ns[m] = n1;
       cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
       ++depth;
-      c.hb_chains[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0);
+      c.hb_chains[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0, cur.fmt, chain_fmt);
       cur.p = out;
       cur.shape = ns;
+      cur.fmt = chain_fmt;
     }
-    srcs[s1].push_back(SumSrc{cur.p, c.ae[t]});
+    srcs[s1].push_back(SumSrc{cur.p, c.ae[t], cur.fmt});
   }
   for (auto& kv : c.gmat) {
     const int s = kv.first.first, m = kv.first.second;
     const int n = c.m_of(m, s);
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
-    c.hb_chains[1].add(c.d_hbin + c.aoff[s], out, kv.second, n, 0, sh, m, n, mkc(1, 0), 0);
-    srcs[s].push_back(SumSrc{out, mkc(1, 0)});
+    c.hb_chains[1].add(c.d_hbin + c.aoff[s], out, kv.second, n, 0, sh, m, n, mkc(1, 0), 0, TF_C64, chain_fmt);
+    srcs[s].push_back(SumSrc{out, mkc(1, 0), chain_fmt});
   }
   for (int s = 0; s < c.nstates; ++s)
     if (c.c0[s].x != 0.0 || c.c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_hbin + c.aoff[s], c.c0[s]});
@@ -1275,7 +1300,7 @@ void eom(Ctx& c, cplx* out) {
   if (gwp) gwp_setup_run(c);
   {
     ProfScope ps(c, KP_H1);
-    launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st);
+    launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, c.precision);
     launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
     c.count(3);
   }
@@ -1297,7 +1322,7 @@ void eom(Ctx& c, cplx* out) {
   }
   {
     ProfScope ps(c, KP_SPF);
-    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st);
+    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision);
     c.count(3);
   }
   if (gwp) gwp_derivs_run(c, out);
@@ -1541,7 +1566,7 @@ void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
 // h1mode only (no mean fields) on the SPFs of y: used before the back-propagation.
 void h1_only(Ctx& c, const cplx* y) {
   copy_dev(c, c.d_in + c.naconftot, y + c.naconftot, c.dimpsi);
-  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st);
+  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, c.precision);
   launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
   c.count(3);
 }
@@ -1589,11 +1614,11 @@ void stage_modes(Ctx& c, CmfState& S, cplx* out, const cplx* base, const double*
 void spf_eval_all(Ctx& c, CmfState& S, cplx* out) {
   {
     ProfScope ps(c, KP_H1);
-    launch_h1(S.h1_d, (int)S.h1.size(), c.h1_maxn2, c.h1_smem, false, c.st);
+    launch_h1(S.h1_d, (int)S.h1.size(), c.h1_maxn2, c.h1_smem, false, c.st, c.precision);
   }
   {
     ProfScope ps(c, KP_SPF);
-    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st);
+    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision);
   }
   c.count(4);
 }
@@ -1765,7 +1790,9 @@ struct MfxState {
   bool recording = false;
   std::vector<double> rec_t0, rec_h;
   std::vector<cplx> rec_s0, rec_sh;
-  long long mlp_steps = 0, fallbacks = 0;
+  long long mlp_steps = 0, fallbacks = 0, rejected = 0;
+  double last_rel = -1.0;          // relative step-end mismatch of the last validated prediction
+  std::vector<double> log;         // per CMF2 attempt: t, h, error, extrapolated (0/1), step-end mismatch
   HoleBatch dh;                     // ||now - pred_full||^2 and ||now||^2
   RedBatch dr;
   cplx* dres = nullptr;
@@ -1963,16 +1990,23 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
   if (use_mlp) copy_dev(c, M->backup, c.d_y, c.ntot);
   double hdid = htry;
   bool first = true;
+  int mlp_rejects = 0;
   while (true) {
     ++*tries;
     if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
     double error = cmf2_attempt(c, t, hdid, use_mlp, first);
     first = false;
+    if (M && M->log.size() < 5 * 100000) {
+      const double row[5] = {t, hdid, error, use_mlp ? 1.0 : 0.0, -1.0};
+      M->log.insert(M->log.end(), row, row + 5);
+    }
     if (error > 1.0 && use_mlp) {
-      // the extrapolated mean fields were trained for accepted steps: redo this
-      // step with the plain scheme instead of shrinking it
-      ++M->fallbacks;
-      use_mlp = false;
+      // rejected by the CMF2 error estimate like any attempt: shrink and retry
+      // with new extrapolated mean fields; after three rejections in a row the
+      // plain scheme takes over
+      ++M->rejected;
+      if (++mlp_rejects >= 3) use_mlp = false;
+      hdid = hdid / sqrt(error) * 0.95;
       continue;
     }
     if (error > 1.0) {
@@ -1985,12 +2019,13 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       operators_and_mf(c, c.d_y);
       snap_gather(c, *M, M->now);
       const double rel = snap_rel_diff(c, *M);
+      M->last_rel = rel;
+      if (!M->log.empty()) M->log.back() = rel;
       if (!(rel <= M->tol)) {
         ++M->fallbacks;
         copy_dev(c, c.d_y, M->backup, c.ntot);
         use_mlp = false;
         first = false;
-        hdid = htry;
         continue;
       }
       ++M->mlp_steps;
@@ -2346,13 +2381,48 @@ int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, const double* fscale,
   });
 }
 
-int64_t mctdh_mfx_stats(mctdh_ctx_t* ctx, int64_t* mlp_steps, int64_t* fallbacks) {
+int64_t mctdh_mfx_predict(mctdh_ctx_t* ctx, const double* hist, const double* ts, double h, double* half,
+                          double* full) {
+  if (!ctx || !hist || !ts || !half || !full) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    if (!M.mlp) throw StatusError(MCTDH_EARG, "no extrapolator attached");
+    for (int j = 0; j < MFX_NHIST; ++j) {
+      CK(cudaMemcpyAsync(M.hist[j], hist + 2 * M.E * j, sizeof(cplx) * M.E, cudaMemcpyHostToDevice, c->st));
+      M.thist[j] = ts[j];
+    }
+    M.head = MFX_NHIST - 1;
+    M.nhist = MFX_NHIST;
+    mfx_predict(*c, M, h);
+    CK(cudaMemcpyAsync(half, M.pred_half, sizeof(cplx) * M.E, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(full, M.pred_full, sizeof(cplx) * M.E, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    M.nhist = 0;
+  });
+}
+
+int64_t mctdh_mfx_log(mctdh_ctx_t* ctx, int64_t maxrows, double* rows, int64_t* n) {
+  if (!ctx || !n) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    const long long nr = (long long)M.log.size() / 5;
+    *n = nr;
+    if (rows) memcpy(rows, M.log.data(), sizeof(double) * 5 * std::min<long long>(nr, maxrows));
+  });
+}
+
+int64_t mctdh_mfx_stats(mctdh_ctx_t* ctx, int64_t* mlp_steps, int64_t* fallbacks, int64_t* rejected,
+                        double* last_rel) {
   if (!ctx) return MCTDH_EARG;
   Ctx* c = ctx->c;
   return guarded(c, [&] {
     MfxState& M = mfx_state(*c);
     if (mlp_steps) *mlp_steps = M.mlp_steps;
     if (fallbacks) *fallbacks = M.fallbacks;
+    if (rejected) *rejected = M.rejected;
+    if (last_rel) *last_rel = M.last_rel;
   });
 }
 

@@ -72,13 +72,13 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   const long long L = d.L;
   if (p >= L * d.R) return;
   const long long l = p % L, r = p / L;
-  const cplx* __restrict__ x0 = d.X + l + L * (long long)nin * r;
+  const long long xi0 = l + L * (long long)nin * r;
   cplx* y0 = d.Y + l + L * (long long)nout * r;
   const cplx alpha = d.alpha;
   if (PREC == 0) {
     cplx x[MAXN];
 #pragma unroll
-    for (int j = 0; j < MAXN; ++j) x[j] = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
+    for (int j = 0; j < MAXN; ++j) x[j] = (j < nin) ? load_c(d.X, xi0 + L * j, d.xfmt) : mkc(0.0, 0.0);
     for (int jo = 0; jo < nout; ++jo) {
       cplx acc = mkc(0.0, 0.0);
 #pragma unroll
@@ -92,14 +92,12 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
     cplxf xh[MAXN], xl[MAXN];
 #pragma unroll
     for (int j = 0; j < MAXN; ++j) {
-      cplx v = (j < nin) ? x0[L * j] : mkc(0.0, 0.0);
-      float hx, lx, hy, ly;
-      split_d2f(v.x, hx, lx);
-      split_d2f(v.y, hy, ly);
-      xh[j] = make_float2(hx, hy);
-      xl[j] = make_float2(lx, ly);
+      const float4 w = (j < nin) ? load_split(d.X, xi0 + L * j, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
+      xh[j] = make_float2(w.x, w.y);
+      xl[j] = make_float2(w.z, w.w);
     }
     const bool unit_alpha = (alpha.x == 1.0 && alpha.y == 0.0);
+    float4* y0f = reinterpret_cast<float4*>(y0);
     for (int jo = 0; jo < nout; ++jo) {
       cplx accd;
       if (PREC == 1) {
@@ -112,6 +110,10 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
             acc = cfmaf_(acc, mh, xl[j]);
             acc = cfmaf_(acc, ml, xh[j]);
           }
+        if (d.yfmt) {
+          y0f[L * jo] = make_float4(acc.x, acc.y, 0.f, 0.f);
+          continue;
+        }
         accd = mkc(f2d_exact(acc.x), f2d_exact(acc.y));
       } else {
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
@@ -125,6 +127,10 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
             df_fma(ih, il, mh.x, ml.x, xh[j].y, xl[j].y);
             df_fma(ih, il, mh.y, ml.y, xh[j].x, xl[j].x);
           }
+        if (d.yfmt) {
+          y0f[L * jo] = make_float4(rh, ih, rl, il);
+          continue;
+        }
         accd = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
       }
       cplx v = unit_alpha ? accd : cmul(alpha, accd);
@@ -162,7 +168,7 @@ __device__ void dot_block(const HoleDesc& d, int b, cplx* red) {
   const int tid = threadIdx.x;
   cplx acc = mkc(0, 0);
   for (long long i = (long long)b * HOLE_THREADS + tid; i < n; i += (long long)d.nblk * HOLE_THREADS)
-    cfma_conj(acc, d.X[i], d.Y[i]);
+    cfma_conj(acc, load_c(d.X, i, d.xfmt), load_c(d.Y, i, d.yfmt));
   red[tid] = acc;
   __syncthreads();
   for (int s = HOLE_THREADS / 2; s > 0; s >>= 1) {
@@ -205,29 +211,23 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
     for (int e = tid; e < HOLE_TILE * n1; e += HOLE_THREADS) {
       int q = e % HOLE_TILE, j = e / HOLE_TILE;
       long long p = p0 + q;
-      cplx v = mkc(0, 0);
-      if (p < nfib) { long long l = p % L, r = p / L; v = d.X[l + L * (j + (long long)n1 * r)]; }
+      long long idx = -1;
+      if (p < nfib) { long long l = p % L, r = p / L; idx = l + L * (j + (long long)n1 * r); }
       if (PREC == 0) {
-        Xs[q * MAXN_SPF + j] = v;
+        Xs[q * MAXN_SPF + j] = (idx >= 0) ? load_c(d.X, idx, d.xfmt) : mkc(0, 0);
       } else {
-        float4 w;
-        split_d2f(v.x, w.x, w.z);
-        split_d2f(v.y, w.y, w.w);
-        Xf[q * MAXN_SPF + j] = w;
+        Xf[q * MAXN_SPF + j] = (idx >= 0) ? load_split(d.X, idx, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
     for (int e = tid; e < HOLE_TILE * n2; e += HOLE_THREADS) {
       int q = e % HOLE_TILE, j = e / HOLE_TILE;
       long long p = p0 + q;
-      cplx v = mkc(0, 0);
-      if (p < nfib) { long long l = p % L, r = p / L; v = d.Y[l + L * (j + (long long)n2 * r)]; }
+      long long idx = -1;
+      if (p < nfib) { long long l = p % L, r = p / L; idx = l + L * (j + (long long)n2 * r); }
       if (PREC == 0) {
-        Ys[q * MAXN_SPF + j] = v;
+        Ys[q * MAXN_SPF + j] = (idx >= 0) ? load_c(d.Y, idx, d.yfmt) : mkc(0, 0);
       } else {
-        float4 w;
-        split_d2f(v.x, w.x, w.z);
-        split_d2f(v.y, w.y, w.w);
-        Yf[q * MAXN_SPF + j] = w;
+        Yf[q * MAXN_SPF + j] = (idx >= 0) ? load_split(d.Y, idx, d.yfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
     __syncthreads();
@@ -401,6 +401,93 @@ __global__ void __launch_bounds__(256) h1_kernel(const H1Desc* __restrict__ desc
   }
 }
 
+// Split-FP32 variant of h1_kernel (precision modes 1 and 2): the column is held
+// as FP32 (hi, lo) pairs, the DOF matrices come pre-split, every product is
+// accumulated as a compensated FP32 pair (df_fma, ~1e-13 relative).
+__global__ void __launch_bounds__(256) h1_split_kernel(const H1Desc* __restrict__ descs) {
+  extern __shared__ float4 smf[];
+  const H1Desc& d = descs[blockIdx.x];
+  const int j2 = blockIdx.y;
+  if (j2 >= d.n2) return;
+  const int G = d.G, n1 = d.n1;
+  float4* bufA = smf;
+  float4* bufB = smf + G;
+  const cplx* src = d.phi_r + (long long)G * j2;
+  for (int e = threadIdx.x; e < G; e += blockDim.x) {
+    const cplx v = src[e];
+    float hx, lx, hy, ly;
+    split_d2f(v.x, hx, lx);
+    split_d2f(v.y, hy, ly);
+    bufA[e] = make_float4(hx, hy, lx, ly);
+  }
+  __syncthreads();
+  int ll = 1;
+  for (int k = 0; k < d.ndof; ++k) {
+    const int ng = d.ng[k];
+    const int ot = d.optype[k];
+    if (ot != 0) {
+      const float2* Mf = d.matf[k];
+      for (int e = threadIdx.x; e < G; e += blockDim.x) {
+        const int a = e % ll;
+        const int gg = (e / ll) % ng;
+        const int bidx = e / (ll * ng);
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        if (ot == 2) {
+          const float4 x = bufA[e];
+          const float2 m = Mf[gg];
+          df_fma(rh, rl, m.x, m.y, x.x, x.z);
+          df_fma(ih, il, m.x, m.y, x.y, x.w);
+        } else {
+          const float4* in = bufA + a + (long long)ll * ng * bidx;
+          const float2* mc = Mf + (long long)ng * gg;
+          for (int gp = 0; gp < ng; ++gp) {
+            const float4 x = in[(long long)ll * gp];
+            const float2 m = mc[gp];
+            df_fma(rh, rl, m.x, m.y, x.x, x.z);
+            df_fma(ih, il, m.x, m.y, x.y, x.w);
+          }
+        }
+        bufB[e] = (ot == 3) ? make_float4(-ih, rh, -il, rl) : make_float4(rh, ih, rl, il);
+      }
+      __syncthreads();
+      float4* t = bufA; bufA = bufB; bufB = t;
+    }
+    ll *= ng;
+  }
+  cplx* dst = d.ophi + (long long)G * j2;
+  for (int e = threadIdx.x; e < G; e += blockDim.x) {
+    const float4 x = bufA[e];
+    dst[e] = mkc(f2d_exact(x.x) + f2d_exact(x.z), f2d_exact(x.y) + f2d_exact(x.w));
+  }
+  if (d.h == nullptr) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j1 = warp; j1 < n1; j1 += (int)(blockDim.x >> 5)) {
+    const cplx* pl = d.phi_l + (long long)G * j1;
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int gg = lane; gg < G; gg += 32) {
+      const cplx p = pl[gg];
+      float phx, plx, phy, ply;
+      split_d2f(p.x, phx, plx);
+      split_d2f(p.y, phy, ply);
+      const float4 x = bufA[gg];
+      // conj(p) * x
+      df_fma(rh, rl, phx, plx, x.x, x.z);
+      df_fma(rh, rl, phy, ply, x.y, x.w);
+      df_fma(ih, il, phx, plx, x.y, x.w);
+      df_fma(ih, il, -phy, -ply, x.x, x.z);
+    }
+    cplx s = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+    for (int o = 16; o > 0; o >>= 1) {
+      s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) {
+      if (d.same_state) d.X[j1 + n1 * j2] = s;
+      else d.h[j1 + n1 * j2] = s;
+    }
+  }
+}
+
 // Same-state h1mode = (X + X^H) / 2 (the zher2k form, hamilton.f90:500-506).
 __global__ void h1_herm_kernel(const H1Desc* __restrict__ descs) {
   const H1Desc& d = descs[blockIdx.x];
@@ -412,14 +499,17 @@ __global__ void h1_herm_kernel(const H1Desc* __restrict__ descs) {
   }
 }
 
-void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, bool with_h, cudaStream_t st) {
+void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, bool with_h, cudaStream_t st,
+               int prec) {
   if (ndesc <= 0) return;
   static size_t configured = 0;
   if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
     cudaFuncSetAttribute(h1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    cudaFuncSetAttribute(h1_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     configured = smem_bytes;
   }
-  h1_kernel<<<dim3(ndesc, maxn2), 256, smem_bytes, st>>>(d_descs);
+  if (prec > 0) h1_split_kernel<<<dim3(ndesc, maxn2), 256, smem_bytes, st>>>(d_descs);
+  else h1_kernel<<<dim3(ndesc, maxn2), 256, smem_bytes, st>>>(d_descs);
   if (with_h) h1_herm_kernel<<<ndesc, 128, 0, st>>>(d_descs);
 }
 
@@ -429,7 +519,7 @@ void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, b
 // (maths.f90:36).  Each round rotates the n/2 disjoint index pairs of a
 // round-robin schedule at once (column rotations A J, then row rotations J^H (A J);
 // rotations of disjoint pairs commute), so a sweep is n-1 rounds.  A pair is
-// rotated when |a_pq| > 1e-19 ||A||_F and |a_pq|^2 > 1e-32 |a_pp a_qq|; the
+// rotated when |a_pq|^2 > 1e-38 ||A||_F^2 and |a_pq|^2 > 1e-32 |a_pp a_qq|; the
 // sweep count is capped.  A[i + ld*j], V likewise.  *ok: the sweeps converged.
 // ---------------------------------------------------------------------------
 #define JAC_MAX_SWEEPS 40
@@ -448,7 +538,6 @@ __device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, JacRot* R, bool* ok
   __syncwarp();
   double fro2 = 0.0;
   for (int e = 0; e < n * n; ++e) { int i = e % n, j = e / n; fro2 += cabs2(A[i + ld * j]); }
-  const double fro = sqrt(fro2);
   const int m = n + (n & 1);      // even count; index n is a dummy for odd n
   const int npair = m / 2;
   bool converged = (n <= 1);
@@ -466,15 +555,18 @@ __device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, JacRot* R, bool* ok
         J.q = q;
         if (q < n) {
           const cplx apq = A[p + ld * q];
-          const double mag = sqrt(cabs2(apq));
+          const double m2 = cabs2(apq);
           const double app = A[p + ld * p].x, aqq = A[q + ld * q].x;
-          rot = (mag > 1e-19 * fro) && (mag * mag > 1e-32 * fabs(app * aqq));
+          rot = (m2 > 1e-38 * fro2) && (m2 > 1e-32 * fabs(app * aqq));
           if (rot) {
-            const double tau = (aqq - app) / (2.0 * mag);
+            // one reciprocal square root for |a_pq| (the FP64 pipe is the bottleneck here)
+            const double rm = rsqrt(m2);
+            const double mag = m2 * rm;
+            const double tau = (aqq - app) * 0.5 * rm;
             const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            J.c = 1.0 / sqrt(1.0 + t * t);
+            J.c = rsqrt(1.0 + t * t);
             J.s = t * J.c;
-            J.u = mkc(apq.x / mag, apq.y / mag);
+            J.u = mkc(apq.x * rm, apq.y * rm);
             J.tm = t * mag;
             J.app = app;
             J.aqq = aqq;
@@ -668,6 +760,94 @@ __global__ void __launch_bounds__(256) spf_tile_kernel(const SpfDesc* __restrict
   }
 }
 
+// Split-FP32 variant of spf_tile_kernel (precision modes 1 and 2): per operator,
+// the tile rows of ophi and the matrix rhom1MF are split once into FP32 hi/lo
+// pairs in shared memory, and every product is accumulated as a compensated
+// FP32 pair (df_fma, ~1e-13 relative), leaving the FP64 pipe one add per output.
+__global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __restrict__ descs, int ndesc,
+                                                             const SpfOp* __restrict__ ops, cplx* __restrict__ out,
+                                                             cplx der) {
+  __shared__ int s_di;
+  // operator phase: ophi tile and rhom1MF as (hx, hy, lx, ly); epilogue: phi and dphi rows
+  __shared__ __align__(16) cplx smem_u[2 * SPF_TILE * MAXN_SPF];
+  float4* ops_s = reinterpret_cast<float4*>(smem_u);
+  float4* rm_s = ops_s + SPF_TILE * MAXN_SPF;
+  cplx* phs = smem_u;
+  cplx* dps = smem_u + SPF_TILE * MAXN_SPF;
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const SpfDesc& d = descs[s_di];
+  const int t = (int)(blockIdx.x - d.block_start);
+  const int G = d.G, n = d.n;
+  const int g0 = t * SPF_TILE;
+  const int rows = min(SPF_TILE, G - g0);
+  cplx* o = out + d.out_offset;
+  // each thread owns up to 4 outputs (r, j1); SPF_TILE * MAXN_SPF <= 4 * 256
+  float ah[4][2], al[4][2];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) ah[u][0] = ah[u][1] = al[u][0] = al[u][1] = 0.f;
+  for (int q = 0; q < d.op_count; ++q) {
+    const SpfOp& op = ops[d.op_first + q];
+    const int n2 = op.n2;
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * n2; e += blockDim.x) {
+      const int r = e % rows, j2 = e / rows;
+      const cplx v = op.ophi[g0 + r + (long long)G * j2];
+      float hx, lx, hy, ly;
+      split_d2f(v.x, hx, lx);
+      split_d2f(v.y, hy, ly);
+      ops_s[r + SPF_TILE * j2] = make_float4(hx, hy, lx, ly);
+    }
+    for (int e = threadIdx.x; e < n * n2; e += blockDim.x) {
+      const cplx v = op.rm[e];
+      float hx, lx, hy, ly;
+      split_d2f(v.x, hx, lx);
+      split_d2f(v.y, hy, ly);
+      rm_s[e] = make_float4(hx, hy, lx, ly);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = threadIdx.x + u * blockDim.x;
+      if (e >= rows * n) continue;
+      const int r = e % rows, j1 = e / rows;
+      for (int j2 = 0; j2 < n2; ++j2) {
+        const float4 x = ops_s[r + SPF_TILE * j2];
+        const float4 m = rm_s[j1 + n * j2];
+        // (x.r + i x.i)(m.r + i m.i)
+        df_fma(ah[u][0], al[u][0], x.x, x.z, m.x, m.z);
+        df_fma(ah[u][0], al[u][0], -x.y, -x.w, m.y, m.w);
+        df_fma(ah[u][1], al[u][1], x.x, x.z, m.y, m.w);
+        df_fma(ah[u][1], al[u][1], x.y, x.w, m.x, m.z);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int e = threadIdx.x + u * blockDim.x;
+    if (e >= rows * n) continue;
+    const int r = e % rows, j1 = e / rows;
+    const int g = g0 + r;
+    const cplx acc = cmul(der, mkc(f2d_exact(ah[u][0]) + f2d_exact(al[u][0]),
+                                   f2d_exact(ah[u][1]) + f2d_exact(al[u][1])));
+    phs[r + SPF_TILE * j1] = d.phi[g + (long long)G * j1];
+    dps[r + SPF_TILE * j1] = acc;
+    o[g + (long long)G * j1] = acc;
+  }
+  __syncthreads();
+  cplx* part = d.partial + (long long)t * 2 * n * n;
+  for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
+    const int which = pr / (n * n), q = pr % (n * n);
+    const int j1 = q % n, j2 = q / n;
+    const cplx* a = phs + SPF_TILE * j1;
+    const cplx* b = (which == 0 ? phs : dps) + SPF_TILE * j2;
+    cplx s = mkc(0, 0);
+    for (int r = 0; r < rows; ++r) cfma_conj(s, a[r], b[r]);
+    part[pr] = s;
+  }
+}
+
 __global__ void spf_solve_kernel(const SpfDesc* __restrict__ descs, int* status) {
   __shared__ cplx S[MAXN_SPF * MAXN_SPF];
   __shared__ cplx O[MAXN_SPF * MAXN_SPF];
@@ -743,9 +923,10 @@ __global__ void __launch_bounds__(256) spf_proj_kernel(const SpfDesc* __restrict
 }
 
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
-                cplx der_factor, int* d_status, cudaStream_t st) {
+                cplx der_factor, int* d_status, cudaStream_t st, int prec) {
   if (ndesc <= 0) return;
-  spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  if (prec > 0) spf_tile_split_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  else spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   spf_solve_kernel<<<ndesc, 128, 0, st>>>(d_descs, d_status);
   spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
 }
@@ -765,7 +946,7 @@ __global__ void termsum_kernel(cplx* __restrict__ out, const SumRange* __restric
   cplx acc = mkc(0, 0);
   for (int k = 0; k < rg.count; ++k) {
     const SumSrc& s = srcs[rg.first + k];
-    cfma(acc, s.coeff, s.src[li]);
+    cfma(acc, s.coeff, load_c(s.src, li, s.fmt));
   }
   out[i] = acc;
 }

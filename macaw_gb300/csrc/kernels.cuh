@@ -14,6 +14,12 @@
 #define HOLE_THREADS 256
 
 // Y = alpha * (M_eff x_mode X) (+ Y when accumulate)
+// Tensor storage formats.  TF_C64: complex128 (re, im).  TF_SPLIT: the same 16
+// bytes per element as FP32 (re hi, im hi, re lo, im lo), re = hi + lo to
+// ~2^-48 relative: intermediates of the split-precision chains stay in this
+// form, so neither side of a chain step converts through the FP64 pipe.
+enum { TF_C64 = 0, TF_SPLIT = 1 };
+
 struct ProdDesc {
   const cplx* X;
   cplx* Y;
@@ -23,6 +29,7 @@ struct ProdDesc {
   int conjT;               // 0: M_eff(j',j) = M[j' + ldm*j];  1: M_eff(j',j) = conj(M[j + ldm*j'])
   cplx alpha;
   int accumulate;
+  int xfmt, yfmt;          // TF_*: TF_SPLIT output only with alpha = 1, no accumulation, PREC > 0
   int pad;
   long long block_start;
 };
@@ -36,6 +43,7 @@ struct HoleDesc {
   cplx* partial;           // [nblk][n1*n2]
   long long block_start;
   int nblk;
+  int xfmt, yfmt;          // TF_*
   int pad;
 };
 
@@ -70,6 +78,7 @@ struct H1Desc {
   int ng[MAXDOF_MODE];
   int optype[MAXDOF_MODE]; // 0 none, 1 dense real, 2 diagonal, 3 dense imaginary (i x real)
   const cplx* mat[MAXDOF_MODE];
+  const float2* matf[MAXDOF_MODE];  // the real coefficients split into FP32 (hi, lo)
 };
 
 // Regularised inverse of a Hermitian n x n matrix by Jacobi rotations
@@ -118,6 +127,8 @@ struct SumRange {
 struct SumSrc {
   const cplx* src;
   cplx coeff;
+  int fmt;                 // TF_*
+  int pad;
 };
 
 // out (n1 x n2, ld n1) = sum_k coeff_k * src_k  (operators pre-summed per state and mode)
@@ -169,11 +180,14 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
                  int prec = 0);
 void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec = 0);
 void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st);
-// with_h: also h1mode (second launch: the Hermitian part of same-state matrices)
-void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, bool with_h, cudaStream_t st);
+// with_h: also h1mode (second launch: the Hermitian part of same-state matrices);
+// prec > 0: the operator products and phi^H (O phi) in compensated split FP32
+void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, bool with_h, cudaStream_t st,
+               int prec);
 void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st);
+// prec > 0: the tile products in compensated split FP32 (spf_tile_split_kernel)
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
-                cplx der_factor, int* d_status, cudaStream_t st);
+                cplx der_factor, int* d_status, cudaStream_t st, int prec);
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
                     long long total, cudaStream_t st);
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st);
