@@ -1103,8 +1103,11 @@ void plan_hb(Ctx& c) {
 }
 
 // Overlap plan between states y1 and y2: o11 = <1|1>, o22 = <2|2>, o12 = <1|2>
-// (norm_wf / WF_Ovl / DeltaPsi, gmctdh_objects.f90:21-226).
-void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2) {
+// (norm_wf / WF_Ovl / DeltaPsi, gmctdh_objects.f90:21-226).  prec 2: the mode
+// products of the chains in compensated split FP32 (~1e-13 relative); used for
+// the step-error norm DeltaPsi of split-precision contexts, where 1 - Re<1|2>/..
+// is of order eps_int^2 / 2 >> 1e-13.  Norms and C(t) keep prec 0.
+void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
   const int f = c.nmodes;
   P.d_result = c.ar.calloc_c(3);
   struct Smat { cplx* s11; cplx* s22; cplx* s12; };
@@ -1182,21 +1185,27 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2) {
     cplx* a1 = y1 + c.aoff[s];
     cplx* a2 = y2 + c.aoff[s];
     cplx* cur[3] = {a1, a2, a2};
+    int curfmt[3] = {TF_C64, TF_C64, TF_C64};
+    const int cfmt = prec ? TF_SPLIT : TF_C64;
     for (size_t i = 0; i < order.size(); ++i) {
       const int m = order[i];
       const int n = sh[m];
       cplx* mats[3] = {S[m][s].s11, S[m][s].s22, S[m][s].s12};
       for (int q = 0; q < 3; ++q) {
         cplx* out = c.ar.calloc_c(N);
-        P.chain[i + 1].add(cur[q], out, mats[q], n, 0, sh, m, n, mkc(1, 0), 0);
+        P.chain[i + 1].add(cur[q], out, mats[q], n, 0, sh, m, n, mkc(1, 0), 0, curfmt[q], cfmt);
         cur[q] = out;
+        curfmt[q] = cfmt;
       }
     }
-    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[0], N, 1, 1, 1), t11, mkc(1, 0)});
-    drefs.push_back(HoleRef{P.dots.add(c.ar, a2, cur[1], N, 1, 1, 1), t22, mkc(1, 0)});
-    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[2], N, 1, 1, 1), t12, mkc(1, 0)});
+    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[0], N, 1, 1, 1, TF_C64, curfmt[0]), t11, mkc(1, 0)});
+    drefs.push_back(HoleRef{P.dots.add(c.ar, a2, cur[1], N, 1, 1, 1, TF_C64, curfmt[1]), t22, mkc(1, 0)});
+    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[2], N, 1, 1, 1, TF_C64, curfmt[2]), t12, mkc(1, 0)});
   }
-  for (auto& b : P.chain) b.finalize(c.ar);
+  for (auto& b : P.chain) {
+    b.prec = prec;
+    b.finalize(c.ar);
+  }
   P.dots.finalize(c.ar);
   for (auto& hr : drefs) P.dot_red.add_term(hr.target, P.dots.h[hr.hole], hr.alpha);
   P.dot_red.finalize(c.ar);
@@ -1294,8 +1303,10 @@ void gwp_derivs_run(Ctx& c, cplx* out) {
   CK(cudaMemcpyAsync(out, c.d_dA, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
 }
 
-// EOM on d_in -> out (full vector [dA | dpsi]).
-void eom(Ctx& c, cplx* out) {
+// EOM on d_in -> out (full vector [dA | dpsi]).  mf_only: only the operator
+// matrices, density matrices, mean fields and rho^-1 MF that CMF2 consumes
+// (cmf2_base.f90:78-87, 122-130); the coefficient and SPF derivatives are skipped.
+void eom(Ctx& c, cplx* out, bool mf_only = false) {
   const bool gwp = !c.modes_gwp.empty();
   if (gwp) gwp_setup_run(c);
   {
@@ -1304,8 +1315,10 @@ void eom(Ctx& c, cplx* out) {
     launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
     c.count(3);
   }
-  for (size_t i = 1; i < c.chains.size(); ++i) run_prod(c, c.chains[i]);
-  run_prod(c, c.gprods);
+  // the deepest level holds only the full products H_t A of the right chains (dA)
+  const size_t depth_end = mf_only ? c.chains.size() - 1 : c.chains.size();
+  for (size_t i = 1; i < depth_end; ++i) run_prod(c, c.chains[i]);
+  if (!mf_only) run_prod(c, c.gprods);
   for (auto& b : c.gwp_rho_chain) run_prod(c, b);
   run_hole(c, c.rho_holes);
   run_hole(c, c.holes);
@@ -1315,9 +1328,13 @@ void eom(Ctx& c, cplx* out) {
     launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
     c.count();
   }
+  if (mf_only) {
+    c.eom_count++;
+    return;
+  }
   {
     ProfScope ps(c, KP_TERMSUM, 0.0, 16.0 * (double)c.src_h.size() * (double)c.naconftot / std::max(1, c.nstates));
-    launch_termsum(gwp ? c.d_adot : out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st);
+    launch_termsum(gwp ? c.d_adot : out, c.sum_d, (int)c.sum_h.size(), c.src_d, c.naconftot, c.st, c.precision);
     c.count();
   }
   {
@@ -1452,7 +1469,7 @@ void rkqs(Ctx& c, double t, double htry, double* hdid, double* hnext, int method
 void hb(Ctx& c, const cplx* B, cplx* out) {
   if (B != c.d_hbin) CK(cudaMemcpyAsync(c.d_hbin, B, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
   for (size_t i = 1; i < c.hb_chains.size(); ++i) run_prod(c, c.hb_chains[i]);
-  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st);
+  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st, c.precision);
   c.count();
   c.hb_count++;
 }
@@ -1557,7 +1574,10 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
 
 // operators and mean fields on the state y (Calc_rho1mode, Calc_h1mode,
 // Calc_MeanField, Calc_rhom1MF): one EOM into d_out (the derivative is unused).
-void operators_and_mf(Ctx& c, const cplx* y) { eom_from(c, y, c.d_out); }
+void operators_and_mf(Ctx& c, const cplx* y) {
+  if (y != c.d_in) CK(cudaMemcpyAsync(c.d_in, y, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+  eom(c, c.d_out, true);
+}
 
 void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
   CK(cudaMemcpyAsync(dst, src, sizeof(cplx) * n, cudaMemcpyDeviceToDevice, c.st));
@@ -2078,9 +2098,9 @@ Ctx* create(const mctdh_setup_t* s) {
     c->d_coef = c->ar.calloc_c(NKRYLOV_MAX);
     plan_eom(*c);
     plan_hb(*c);
-    plan_ovl(*c, c->dpsi_plan, c->d_tmp, c->d_err);
-    plan_ovl(*c, c->auto_plan, c->d_y0, c->d_y);
-    plan_ovl(*c, c->io_plan, c->d_in, c->d_out);
+    plan_ovl(*c, c->dpsi_plan, c->d_tmp, c->d_err, c->precision ? 2 : 0);
+    plan_ovl(*c, c->auto_plan, c->d_y0, c->d_y, 0);
+    plan_ovl(*c, c->io_plan, c->d_in, c->d_out, 0);
     CK(cudaDeviceSynchronize());
   } catch (...) {
     if (c->st) cudaStreamDestroy(c->st);

@@ -951,10 +951,40 @@ __global__ void termsum_kernel(cplx* __restrict__ out, const SumRange* __restric
   out[i] = acc;
 }
 
+// Split-precision variant: every coeff * src product accumulated as a
+// compensated FP32 pair (df_fma, ~1e-13 relative); one FP64 add per output.
+__global__ void termsum_split_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges, int nr,
+                                     const SumSrc* __restrict__ srcs, long long total) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  int r = 0;
+  while (r + 1 < nr && i >= ranges[r + 1].offset) ++r;
+  const SumRange& rg = ranges[r];
+  const long long li = i - rg.offset;
+  if (li < 0 || li >= rg.n) return;
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  for (int k = 0; k < rg.count; ++k) {
+    const SumSrc& s = srcs[rg.first + k];
+    float ch, cl, dh, dl;
+    split_d2f(s.coeff.x, ch, cl);
+    split_d2f(s.coeff.y, dh, dl);
+    const float4 x = load_split(s.src, li, s.fmt);
+    // (c + i d)(xr + i xi)
+    df_fma(rh, rl, ch, cl, x.x, x.z);
+    df_fma(rh, rl, -dh, -dl, x.y, x.w);
+    df_fma(ih, il, ch, cl, x.y, x.w);
+    df_fma(ih, il, dh, dl, x.x, x.z);
+  }
+  out[i] = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+}
+
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs, long long total,
-                    cudaStream_t st) {
+                    cudaStream_t st, int prec) {
   if (total <= 0) return;
-  termsum_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total);
+  if (prec > 0)
+    termsum_split_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total);
+  else
+    termsum_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total);
 }
 
 __global__ void stage_kernel(cplx* __restrict__ out, const cplx* __restrict__ base, StageArgs a, double dt,

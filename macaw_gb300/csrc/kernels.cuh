@@ -188,8 +188,9 @@ void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int*
 // prec > 0: the tile products in compensated split FP32 (spf_tile_split_kernel)
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
                 cplx der_factor, int* d_status, cudaStream_t st, int prec);
+// prec > 0: compensated split-FP32 accumulation (termsum_split_kernel)
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
-                    long long total, cudaStream_t st);
+                    long long total, cudaStream_t st, int prec);
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st);
 void launch_copy_scale(cplx* out, const cplx* in, cplx s, long long n, cudaStream_t st);
 void launch_axpy(cplx* y, const cplx* x, cplx a, long long n, cudaStream_t st);
