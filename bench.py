@@ -31,7 +31,7 @@ if ROOT not in sys.path:
 
 import numpy as np  # noqa: E402
 
-from macaw_gb300.model import AU2FS, INT_CMF2, initial_wavefunction  # noqa: E402
+from macaw_gb300.model import AU2FS, INT_CMF2, INT_RK45, initial_wavefunction  # noqa: E402
 from macaw_gb300.generate import qvc12  # noqa: E402
 
 METRIC = "simulated fs/s & EOM evals/s vs plain FP64 GPU path at |dC(t)|<=1e-6"
@@ -389,6 +389,69 @@ def run_profile_case(args):
     return 0
 
 
+def run_ensemble(args):
+    """Batched-ensemble workload: ragged LVC members (2-4 states, 4-10 modes,
+    4-10 SPFs, 16-48 points per mode, configurations per state capped) advanced
+    together with lockstep RK45, against the same members propagated one context
+    at a time.  Unit: member-fs/s (simulated fs summed over members per second)."""
+    import torch
+    from macaw_gb300.capi import Ensemble, GpuCore
+    from macaw_gb300.generate import ensemble
+    torch.cuda.init()
+    models = ensemble(count=args.members, max_conf=args.max_conf)
+    starts = [initial_wavefunction(m) for m in models]
+    ens = Ensemble(models)
+    for i, (A, psi) in enumerate(starts):
+        ens.set_state(i, A, psi, as_start=True)
+    t = np.zeros(len(models))
+    step = np.array([m.tout * m.eps_int for m in models])
+    # untimed start-up transient (steps grow from tout * eps_int)
+    ens.propagate(INT_RK45, 0.1 / AU2FS, t, step)
+    t0 = t.copy()
+    es = torch.cuda.ExternalStream(ens.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0 = ens.counters()
+    torch.cuda.synchronize()
+    ev0.record(es)
+    rounds, neom = ens.propagate(INT_RK45, (0.1 + args.ens_fs) / AU2FS, t, step)
+    ev1.record(es)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    c1 = ens.counters()
+    fs_total = float(np.sum(t - t0)) * AU2FS
+    # the same members one context at a time (sequential), same interval
+    seq_ms = 0.0
+    nseq = min(len(models), args.seq_members)
+    seq_fs = 0.0
+    for i in range(nseq):
+        core = GpuCore(models[i])
+        A, psi = starts[i]
+        core.set_state(A, psi, as_start=True)
+        tt, ss, _, _, _ = core.propagate_interval(INT_RK45, 0.1 / AU2FS, 0.0, models[i].tout * models[i].eps_int)
+        torch.cuda.synchronize()
+        w = time.perf_counter()
+        tt2, _, _, _, _ = core.propagate_interval(INT_RK45, (0.1 + args.ens_fs) / AU2FS, tt, ss)
+        torch.cuda.synchronize()
+        seq_ms += 1e3 * (time.perf_counter() - w)
+        seq_fs += (tt2 - tt) * AU2FS
+        core.close()
+    sizes = [m.naconftot + m.dimpsi for m in models]
+    line = {"metric": "member-fs/s of a batched ensemble (lockstep RK45)", "value": fs_total / (ms * 1e-3),
+            "unit": "member-fs/s", "n_gpus": 1, "members": len(models), "ms": ms, "rounds": rounds,
+            "eom_member_evals_per_s": (c1["eom"] - c0["eom"]) * len(models) / (ms * 1e-3),
+            "launches": c1["launches"] - c0["launches"],
+            "sequential": {"members": nseq, "member_fs_per_s": seq_fs / (seq_ms * 1e-3) if seq_ms else None,
+                           "timing": "host wall clock around each member's propagate call"},
+            "config": {"workload": "ragged LVC ensemble", "interval_fs": args.ens_fs, "max_conf": args.max_conf,
+                       "coefficients_total": int(sum(sizes)), "largest_member": int(max(sizes)),
+                       "smallest_member": int(min(sizes))}}
+    if line["sequential"]["member_fs_per_s"]:
+        line["batched_over_sequential"] = line["value"] / line["sequential"]["member_fs_per_s"]
+    print(json.dumps(line), flush=True)
+    ens.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -398,11 +461,19 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
+    ap.add_argument("--workload", default="qvc12", choices=["qvc12", "ensemble"],
+                    help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement")
+    ap.add_argument("--members", type=int, default=128)
+    ap.add_argument("--max-conf", type=int, default=1 << 14)
+    ap.add_argument("--ens-fs", type=float, default=0.5)
+    ap.add_argument("--seq-members", type=int, default=16)
     ap.add_argument("--profile-case", action="store_true",
                     help="run a short fixed piece of the workload (for profiler captures) instead of the benchmark")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -229,6 +229,31 @@ int64_t mctdh_mfx_log(mctdh_ctx_t *ctx, int64_t maxrows, double *rows, int64_t *
 int64_t mctdh_mfx_stats(mctdh_ctx_t *ctx, int64_t *mlp_steps, int64_t *fallbacks, int64_t *rejected,
                         double *last_rel);
 
+/* Ensembles of independent wavepackets of uneven shape (no reference counterpart:
+ * the reference runs one wavepacket per process).  Each member is described by
+ * its own set-up record; every stage of the EOM is one launch over all members,
+ * and adaptive RK (int_type 1 Cash-Karp, 2 Dormand-Prince; rkqs,
+ * integrator.f90:36-91, per member) runs the members in lockstep.  Members are
+ * DVR models in one precision mode; CMF2 is not offered for ensembles.
+ * propagate: t[i] and step[i] (in/out) as propagate_wf keeps them
+ * (propagator.f90:110-134), every member advanced to tnext; nrounds counts the
+ * lockstep attempt rounds.  calc_derivs: the EOM of every member at its state
+ * (read with get_derivs).  stream: the CUDA stream the ensemble runs on. */
+typedef struct mctdh_ens mctdh_ens_t;
+int64_t mctdh_ens_create(const mctdh_setup_t *setups, int64_t n, mctdh_ens_t **ens);
+int64_t mctdh_ens_destroy(mctdh_ens_t *ens);
+int64_t mctdh_ens_set_state(mctdh_ens_t *ens, int64_t i, const double *A, const double *psi, int64_t as_start);
+int64_t mctdh_ens_get_state(mctdh_ens_t *ens, int64_t i, double *A, double *psi);
+int64_t mctdh_ens_calc_derivs(mctdh_ens_t *ens);
+int64_t mctdh_ens_get_derivs(mctdh_ens_t *ens, int64_t i, double *dA, double *dpsi);
+int64_t mctdh_ens_propagate(mctdh_ens_t *ens, int64_t int_type, double tnext, double *t, double *step,
+                            int64_t *nrounds, int64_t *neom);
+int64_t mctdh_ens_observables(mctdh_ens_t *ens, int64_t i, double *energy, double *pop, double *norm,
+                              double *auto_re, double *auto_im);
+int64_t mctdh_ens_counters(mctdh_ens_t *ens, int64_t *launches, int64_t *eom, int64_t *rounds);
+int64_t mctdh_ens_stream(mctdh_ens_t *ens, void **stream);
+const char *mctdh_ens_last_error(mctdh_ens_t *ens);
+
 /* Last error message of the context (or of the last failed create when ctx is NULL). */
 const char *mctdh_last_error(mctdh_ctx_t *ctx);
 

@@ -101,6 +101,22 @@ def load_library() -> C.CDLL:
     lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P, I64P, DP]
     lib.mctdh_mfx_predict.argtypes = [vp, DP, DP, C.c_double, DP, DP]
     lib.mctdh_mfx_log.argtypes = [vp, C.c_int64, DP, I64P]
+    lib.mctdh_ens_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
+    lib.mctdh_ens_destroy.argtypes = [vp]
+    lib.mctdh_ens_set_state.argtypes = [vp, C.c_int64, DP, DP, C.c_int64]
+    lib.mctdh_ens_get_state.argtypes = [vp, C.c_int64, DP, DP]
+    lib.mctdh_ens_calc_derivs.argtypes = [vp]
+    lib.mctdh_ens_get_derivs.argtypes = [vp, C.c_int64, DP, DP]
+    lib.mctdh_ens_propagate.argtypes = [vp, C.c_int64, C.c_double, DP, DP, I64P, I64P]
+    lib.mctdh_ens_observables.argtypes = [vp, C.c_int64, DP, DP, DP, DP, DP]
+    lib.mctdh_ens_counters.argtypes = [vp, I64P, I64P, I64P]
+    lib.mctdh_ens_stream.argtypes = [vp, C.POINTER(vp)]
+    lib.mctdh_ens_last_error.argtypes = [vp]
+    lib.mctdh_ens_last_error.restype = C.c_char_p
+    for name in ("mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
+                 "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
+                 "mctdh_ens_counters", "mctdh_ens_stream"):
+        getattr(lib, name).restype = C.c_int64
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
                  "mctdh_mfx_predict", "mctdh_mfx_log"):
         getattr(lib, name).restype = C.c_int64
@@ -129,7 +145,10 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
-            "mctdh_mfx_predict", "mctdh_mfx_log"]
+            "mctdh_mfx_predict", "mctdh_mfx_log",
+            "mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
+            "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
+            "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_last_error"]
 
 KERNEL_CLASSES = ["mode_product", "hole_contract", "reduce", "h1_spf_ops", "reg_inverse", "term_sum",
                   "spf_derivative", "elementwise", "gaussian_block"]
@@ -470,6 +489,94 @@ def fp64_peak_tflops() -> float:
 
 def _f32(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+
+
+class Ensemble:
+    """Independent wavepackets of uneven shape advanced together (mctdh_ens_*): one
+    launch per EOM stage over all members, lockstep adaptive RK."""
+
+    def __init__(self, models, precision: int = 0):
+        self.lib = load_library()
+        self.models = list(models)
+        built = [build_setup(m, precision) for m in self.models]
+        self._keep = [b[1] for b in built]
+        arr = (Setup * len(built))(*[b[0] for b in built])
+        self._arr = arr
+        h = C.c_void_p()
+        rc = self.lib.mctdh_ens_create(C.cast(arr, C.c_void_p), len(built), C.byref(h))
+        if rc != 0:
+            raise MctdhError(rc, self.lib.mctdh_ens_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mctdh_ens_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise MctdhError(rc, self.lib.mctdh_ens_last_error(self.h).decode())
+
+    def __len__(self):
+        return len(self.models)
+
+    def set_state(self, i: int, A, psi, as_start: bool = True):
+        A, psi = _cbuf(A), _cbuf(psi)
+        self._check(self.lib.mctdh_ens_set_state(self.h, i, _ptr(A), _ptr(psi), 1 if as_start else 0))
+
+    def get_state(self, i: int):
+        m = self.models[i]
+        A = np.empty(m.naconftot, dtype=np.complex128)
+        psi = np.empty(m.dimpsi, dtype=np.complex128)
+        self._check(self.lib.mctdh_ens_get_state(self.h, i, _ptr(A), _ptr(psi)))
+        return A, psi
+
+    def calc_derivs(self):
+        """EOM of every member at its resident state; returns [(dA, dpsi)]."""
+        self._check(self.lib.mctdh_ens_calc_derivs(self.h))
+        out = []
+        for i, m in enumerate(self.models):
+            dA = np.empty(m.naconftot, dtype=np.complex128)
+            dpsi = np.empty(m.dimpsi, dtype=np.complex128)
+            self._check(self.lib.mctdh_ens_get_derivs(self.h, i, _ptr(dA), _ptr(dpsi)))
+            out.append((dA, dpsi))
+        return out
+
+    def propagate(self, int_type: int, tnext: float, t, step):
+        """Advance every member to tnext; t and step (arrays, per member) are updated
+        in place.  Returns (lockstep rounds, EOM evaluations)."""
+        T = np.ascontiguousarray(t, dtype=np.float64)
+        S = np.ascontiguousarray(step, dtype=np.float64)
+        nr, ne = C.c_int64(), C.c_int64()
+        self._check(self.lib.mctdh_ens_propagate(self.h, int_type, tnext, T.ctypes.data_as(DP),
+                                                 S.ctypes.data_as(DP), C.byref(nr), C.byref(ne)))
+        t[:] = T
+        step[:] = S
+        return nr.value, ne.value
+
+    def observables(self, i: int, t: float = 0.0):
+        m = self.models[i]
+        e, nrm, ar, ai = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        pop = np.zeros(m.nstates)
+        self._check(self.lib.mctdh_ens_observables(self.h, i, C.byref(e), pop.ctypes.data_as(DP), C.byref(nrm),
+                                                   C.byref(ar), C.byref(ai)))
+        return dict(t=t, pop=pop, norm=nrm.value, energy=e.value, auto=complex(ar.value, ai.value))
+
+    def counters(self):
+        a, b, r = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.mctdh_ens_counters(self.h, C.byref(a), C.byref(b), C.byref(r)))
+        return dict(launches=a.value, eom=b.value, rounds=r.value)
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._check(self.lib.mctdh_ens_stream(self.h, C.byref(p)))
+        return p.value or 0
 
 
 class Mlp:

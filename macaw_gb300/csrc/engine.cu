@@ -42,11 +42,12 @@ struct DevArena {
   char* cur = nullptr;
   size_t left = 0;
   size_t total = 0;
+  size_t chunk = (size_t)64 << 20;   // smallest cudaMalloc
   void* alloc(size_t bytes) {
     bytes = (bytes + 255) & ~(size_t)255;
     if (bytes == 0) bytes = 256;
     if (bytes > left) {
-      size_t sz = std::max(bytes, (size_t)64 << 20);
+      size_t sz = std::max(bytes, chunk);
       void* p = nullptr;
       CK(cudaMalloc(&p, sz));
       chunks.push_back(p);
@@ -276,6 +277,8 @@ struct Ctx {
   long long eom_count = 0, hb_count = 0;
 
   cudaStream_t st = nullptr;
+  bool own_stream = true;   // false for ensemble members (the ensemble's stream)
+  bool member = false;      // ensemble member: RK only, state vectors owned by the ensemble
   DevArena ar;
   int* d_status = nullptr;
   cplx* d_y = nullptr;      // resident state [A | psi]
@@ -1681,6 +1684,7 @@ void plan_cmf(Ctx& c, CmfState& S) {
   S.err_holes.finalize(c.ar);
   for (auto& hr : hrefs) S.err_red.add_term(hr.target, S.err_holes.h[hr.hole], hr.alpha);
   S.err_red.finalize(c.ar);
+  if (S.errd_h.size() > 256) throw StatusError(MCTDH_EUNSUPPORTED, "more than 256 (mode, state) SPF blocks");
   S.errd_d = upload_vec(c.ar, S.errd_h);
   S.dt_mode = (double*)c.ar.alloc(sizeof(double) * 64);
   S.accept = (int*)c.ar.alloc(sizeof(int) * 64);
@@ -1774,6 +1778,7 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
 }
 
 CmfState& cmf_state(Ctx& c) {
+  if (c.member) throw StatusError(MCTDH_EUNSUPPORTED, "ensemble members integrate with RK");
   if (!c.modes_gwp.empty())
     throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 with Gaussian modes (A_to_B / DD matrices) is not built; use RK");
   CmfState*& Sp = g_cmf[&c];
@@ -2073,37 +2078,64 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
 // ---------------------------------------------------------------------------
 // Context creation
 // ---------------------------------------------------------------------------
-Ctx* create(const mctdh_setup_t* s) {
+// Vectors an ensemble provides to one of its members: views into the ensemble's
+// contiguous state, input, output, stage and error vectors, and its stream.
+struct MemberBufs {
+  cplx *y, *y0, *in, *out, *k[7], *tmp, *err;
+  cudaStream_t st;
+};
+
+Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     throw StatusError(MCTDH_ECUDA, "no CUDA device available (this core has no CPU fallback)");
   Ctx* c = new Ctx();
   try {
-    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    if (mb) {
+      c->st = mb->st;
+      c->own_stream = false;
+      c->member = true;
+      c->ar.chunk = (size_t)4 << 20;
+    } else {
+      CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    }
     load_setup(*c, s);
     c->d_status = (int*)c->ar.alloc(64);
     CK(cudaMemset(c->d_status, 0, 64));
-    c->d_y = c->ar.calloc_c(c->ntot);
-    c->d_y0 = c->ar.calloc_c(c->ntot);
-    c->d_in = c->ar.calloc_c(c->ntot);
-    c->d_out = c->ar.calloc_c(c->ntot);
-    for (int i = 0; i < 7; ++i) c->d_k[i] = c->ar.calloc_c(c->ntot);
-    c->d_tmp = c->ar.calloc_c(c->ntot);
-    c->d_err = c->ar.calloc_c(c->ntot);
-    c->d_hbin = c->ar.calloc_c(c->naconftot);
-    c->d_hb = c->ar.calloc_c(c->naconftot);
+    if (mb) {
+      c->d_y = mb->y;
+      c->d_y0 = mb->y0;
+      c->d_in = mb->in;
+      c->d_out = mb->out;
+      for (int i = 0; i < 7; ++i) c->d_k[i] = mb->k[i];
+      c->d_tmp = mb->tmp;
+      c->d_err = mb->err;
+    } else {
+      c->d_y = c->ar.calloc_c(c->ntot);
+      c->d_y0 = c->ar.calloc_c(c->ntot);
+      c->d_in = c->ar.calloc_c(c->ntot);
+      c->d_out = c->ar.calloc_c(c->ntot);
+      for (int i = 0; i < 7; ++i) c->d_k[i] = c->ar.calloc_c(c->ntot);
+      c->d_tmp = c->ar.calloc_c(c->ntot);
+      c->d_err = c->ar.calloc_c(c->ntot);
+    }
     c->d_scal = (double*)c->ar.alloc(4096);
-    c->d_krylov = c->ar.calloc_c(c->naconftot * (NKRYLOV_MAX + 1));
-    c->d_lan = (double*)c->ar.alloc(sizeof(double) * (3 * NKRYLOV_MAX + NKRYLOV_MAX * NKRYLOV_MAX));
-    c->d_coef = c->ar.calloc_c(NKRYLOV_MAX);
     plan_eom(*c);
-    plan_hb(*c);
+    if (!mb) {
+      // CMF2 / Lanczos buffers (ensemble members integrate with RK only)
+      c->d_hbin = c->ar.calloc_c(c->naconftot);
+      c->d_hb = c->ar.calloc_c(c->naconftot);
+      c->d_krylov = c->ar.calloc_c(c->naconftot * (NKRYLOV_MAX + 1));
+      c->d_lan = (double*)c->ar.alloc(sizeof(double) * (3 * NKRYLOV_MAX + NKRYLOV_MAX * NKRYLOV_MAX));
+      c->d_coef = c->ar.calloc_c(NKRYLOV_MAX);
+      plan_hb(*c);
+    }
     plan_ovl(*c, c->dpsi_plan, c->d_tmp, c->d_err, c->precision ? 2 : 0);
     plan_ovl(*c, c->auto_plan, c->d_y0, c->d_y, 0);
     plan_ovl(*c, c->io_plan, c->d_in, c->d_out, 0);
     CK(cudaDeviceSynchronize());
   } catch (...) {
-    if (c->st) cudaStreamDestroy(c->st);
+    if (c->st && c->own_stream) cudaStreamDestroy(c->st);
     delete c;
     throw;
   }
@@ -2139,6 +2171,372 @@ void download(Ctx& c, const cplx* src, double* A, double* psi) {
   CK(cudaStreamSynchronize(c.st));
 }
 
+
+// ---------------------------------------------------------------------------
+// Ensembles of independent wavepackets of uneven shape (different state, mode,
+// SPF and grid counts).  Every member is planned like a single context, on
+// views into the ensemble's contiguous vectors; the members' descriptors are
+// then concatenated, so each stage of the EOM (each chain depth, the
+// contractions, the reduction, the regularised inverses, the term sums, the
+// SPF derivatives) is ONE launch over all members.  Time stepping is adaptive
+// RK in lockstep: a round runs one attempt of every member still stepping, each
+// with its own step length, and the host applies each member's rkqs control
+// (integrator.f90:36-91) to the round's error norms.
+// ---------------------------------------------------------------------------
+struct Ens {
+  std::vector<Ctx*> m;
+  std::vector<long long> off;   // member offsets in the ensemble vectors (size n + 1)
+  long long total = 0;
+  cudaStream_t st = nullptr;
+  DevArena ar;
+  cplx *Y = nullptr, *Y0 = nullptr, *IN = nullptr, *OUT = nullptr, *K[7] = {}, *TMP = nullptr, *ERR = nullptr;
+  long long* off_d = nullptr;
+  double* dt_d = nullptr;
+  int* acc_d = nullptr;
+  int* status_d = nullptr;
+  cplx* res_d = nullptr;        // 3 per member: <1|1>, <2|2>, <1|2> of the error norm
+  int precision = 0;
+  cplx der = mkc(0, -1);
+  double min_stepsize = 0, writetime = 0;
+  // merged EOM plan
+  std::vector<ProdBatch> chains;
+  ProdBatch gprods;
+  HoleBatch rho_holes, holes;
+  RedBatch red;
+  std::vector<H1Desc> h1_h;
+  H1Desc* h1_d = nullptr;
+  int h1_maxn2 = 0;
+  size_t h1_smem = 0;
+  std::vector<MatSumDesc> msum_h;
+  std::vector<MatSumSrc> msum_src_h;
+  MatSumDesc* msum_d = nullptr;
+  MatSumSrc* msum_src_d = nullptr;
+  std::vector<RegInvDesc> reg_h;
+  std::vector<MFOp> mfop_h;
+  RegInvDesc* reg_d = nullptr;
+  MFOp* mfop_d = nullptr;
+  std::vector<SpfDesc> spf_h;
+  std::vector<SpfOp> spfop_h;
+  SpfDesc* spf_d = nullptr;
+  SpfOp* spfop_d = nullptr;
+  long long spf_tiles = 0;
+  std::vector<SumRange> sum_h;
+  std::vector<SumSrc> src_h;
+  SumRange* sum_d = nullptr;
+  SumSrc* src_d = nullptr;
+  // merged error-norm plan (DeltaPsi of every member)
+  HoleBatch ov_spf_holes, ov_dots;
+  RedBatch ov_spf_red, ov_dot_red;
+  std::vector<ProdBatch> ov_chain;
+  long long launches = 0, eom_count = 0, rounds = 0;
+  std::string last_error;
+};
+
+void merge_prod(ProdBatch& d, const ProdBatch& s) {
+  d.h.insert(d.h.end(), s.h.begin(), s.h.end());
+  d.prec = s.prec;
+}
+void merge_hole(HoleBatch& d, const HoleBatch& s) {
+  d.h.insert(d.h.end(), s.h.begin(), s.h.end());
+  d.prec = s.prec;
+}
+void merge_red(RedBatch& d, const RedBatch& s) {
+  d.tg.insert(d.tg.end(), s.tg.begin(), s.tg.end());
+  d.pending.insert(d.pending.end(), s.pending.begin(), s.pending.end());
+}
+
+Ens* ens_create(const mctdh_setup_t* setups, int n) {
+  if (n < 1) throw StatusError(MCTDH_EARG, "empty ensemble");
+  Ens* E = new Ens();
+  try {
+    CK(cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking));
+    // sizes first: the member layout fixes the ensemble vectors
+    E->off.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+      const mctdh_setup_t& s = setups[i];
+      long long na = 0;
+      for (int st = 0; st < s.nstates; ++st) {
+        long long q = 1;
+        for (int md = 0; md < s.nmodes; ++md) q *= s.nspf[md + s.nmodes * st];
+        na += q;
+      }
+      E->off[i + 1] = E->off[i] + na + s.dimpsi;
+    }
+    E->total = E->off[n];
+    E->Y = E->ar.calloc_c(E->total);
+    E->Y0 = E->ar.calloc_c(E->total);
+    E->IN = E->ar.calloc_c(E->total);
+    E->OUT = E->ar.calloc_c(E->total);
+    for (int j = 0; j < 7; ++j) E->K[j] = E->ar.calloc_c(E->total);
+    E->TMP = E->ar.calloc_c(E->total);
+    E->ERR = E->ar.calloc_c(E->total);
+    for (int i = 0; i < n; ++i) {
+      MemberBufs mb;
+      const long long o = E->off[i];
+      mb.y = E->Y + o;
+      mb.y0 = E->Y0 + o;
+      mb.in = E->IN + o;
+      mb.out = E->OUT + o;
+      for (int j = 0; j < 7; ++j) mb.k[j] = E->K[j] + o;
+      mb.tmp = E->TMP + o;
+      mb.err = E->ERR + o;
+      mb.st = E->st;
+      Ctx* c = create(&setups[i], &mb);
+      E->m.push_back(c);
+      if (c->ntot != E->off[i + 1] - o) throw StatusError(MCTDH_EARG, "member size mismatch");
+      if (!c->modes_gwp.empty()) throw StatusError(MCTDH_EUNSUPPORTED, "ensembles of Gaussian-mode models");
+      if (i == 0) {
+        E->precision = c->precision;
+        E->der = c->der;
+        E->min_stepsize = c->min_stepsize;
+        E->writetime = c->writetime;
+      } else if (c->precision != E->precision || c->der.x != E->der.x || c->der.y != E->der.y) {
+        throw StatusError(MCTDH_EARG, "ensemble members must share precision and der_factor");
+      }
+      // merge the EOM plan
+      if (E->chains.size() < c->chains.size()) E->chains.resize(c->chains.size());
+      for (size_t dd = 1; dd < c->chains.size(); ++dd) merge_prod(E->chains[dd], c->chains[dd]);
+      merge_prod(E->gprods, c->gprods);
+      merge_hole(E->rho_holes, c->rho_holes);
+      merge_hole(E->holes, c->holes);
+      merge_red(E->red, c->red);
+      E->h1_h.insert(E->h1_h.end(), c->h1_h.begin(), c->h1_h.end());
+      E->h1_maxn2 = std::max(E->h1_maxn2, c->h1_maxn2);
+      E->h1_smem = std::max(E->h1_smem, c->h1_smem);
+      for (MatSumDesc md : c->msum_h) {
+        md.first += (int)E->msum_src_h.size();
+        E->msum_h.push_back(md);
+      }
+      E->msum_src_h.insert(E->msum_src_h.end(), c->msum_src_h.begin(), c->msum_src_h.end());
+      for (RegInvDesc rd : c->reg_h) {
+        rd.op_first += (int)E->mfop_h.size();
+        E->reg_h.push_back(rd);
+      }
+      E->mfop_h.insert(E->mfop_h.end(), c->mfop_h.begin(), c->mfop_h.end());
+      for (SpfDesc sd : c->spf_h) {
+        sd.op_first += (int)E->spfop_h.size();
+        sd.out_offset += o;
+        sd.block_start = E->spf_tiles;
+        E->spf_tiles += sd.ntile;
+        E->spf_h.push_back(sd);
+      }
+      E->spfop_h.insert(E->spfop_h.end(), c->spfop_h.begin(), c->spfop_h.end());
+      for (SumRange r : c->sum_h) {
+        r.offset += o;
+        r.first += (int)E->src_h.size();
+        E->sum_h.push_back(r);
+      }
+      E->src_h.insert(E->src_h.end(), c->src_h.begin(), c->src_h.end());
+      // merge the error-norm plan; its three results land at res_d + 3 i
+      const OvlPlan& P = c->dpsi_plan;
+      merge_hole(E->ov_spf_holes, P.spf_holes);
+      merge_red(E->ov_spf_red, P.spf_red);
+      if (E->ov_chain.size() < P.chain.size()) E->ov_chain.resize(P.chain.size());
+      for (size_t dd = 1; dd < P.chain.size(); ++dd) merge_prod(E->ov_chain[dd], P.chain[dd]);
+      merge_hole(E->ov_dots, P.dots);
+      merge_red(E->ov_dot_red, P.dot_red);
+    }
+    E->res_d = E->ar.calloc_c(3LL * n);
+    for (int i = 0; i < n; ++i)
+      for (int q = 0; q < 3; ++q) E->ov_dot_red.tg[3 * i + q].out = E->res_d + 3 * i + q;
+    for (auto& b : E->chains) b.finalize(E->ar);
+    E->gprods.finalize(E->ar);
+    E->rho_holes.finalize(E->ar);
+    E->holes.finalize(E->ar);
+    E->red.finalize(E->ar);
+    E->h1_d = upload_vec(E->ar, E->h1_h);
+    E->msum_d = upload_vec(E->ar, E->msum_h);
+    E->msum_src_d = upload_vec(E->ar, E->msum_src_h);
+    E->reg_d = upload_vec(E->ar, E->reg_h);
+    E->mfop_d = upload_vec(E->ar, E->mfop_h);
+    E->spf_d = upload_vec(E->ar, E->spf_h);
+    E->spfop_d = upload_vec(E->ar, E->spfop_h);
+    E->sum_d = upload_vec(E->ar, E->sum_h);
+    E->src_d = upload_vec(E->ar, E->src_h);
+    E->ov_spf_holes.finalize(E->ar);
+    E->ov_spf_red.finalize(E->ar);
+    for (auto& b : E->ov_chain) b.finalize(E->ar);
+    E->ov_dots.finalize(E->ar);
+    E->ov_dot_red.finalize(E->ar);
+    E->off_d = upload_vec(E->ar, E->off);
+    E->dt_d = (double*)E->ar.alloc(sizeof(double) * n);
+    E->acc_d = (int*)E->ar.alloc(sizeof(int) * n);
+    E->status_d = (int*)E->ar.alloc(64);
+    CK(cudaMemset(E->status_d, 0, 64));
+    if (E->h1_smem > 48 * 1024) throw StatusError(MCTDH_EUNSUPPORTED, "grid of a mode too large for the h1 kernel");
+    CK(cudaDeviceSynchronize());
+  } catch (...) {
+    for (Ctx* c : E->m) delete c;
+    if (E->st) cudaStreamDestroy(E->st);
+    delete E;
+    throw;
+  }
+  return E;
+}
+
+void ens_destroy(Ens* E) {
+  cudaStreamSynchronize(E->st);
+  for (Ctx* c : E->m) {
+    for (auto& kv : c->dots) delete kv.second;
+    for (auto e : c->evpool) cudaEventDestroy(e);
+    delete c;
+  }
+  cudaStreamDestroy(E->st);
+  delete E;
+}
+
+void ens_run_prod(Ens& E, const ProdBatch& b) {
+  if (b.h.empty()) return;
+  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec);
+  ++E.launches;
+}
+void ens_run_hole(Ens& E, const HoleBatch& b) {
+  if (b.h.empty()) return;
+  launch_hole(b.d, (int)b.h.size(), b.nblocks, E.st, b.prec);
+  ++E.launches;
+}
+void ens_run_red(Ens& E, const RedBatch& b) {
+  if (b.tg.empty()) return;
+  launch_reduce(b.d_tg, (int)b.tg.size(), b.d_terms, E.st);
+  ++E.launches;
+}
+
+// EOM of every member: IN -> out (same layout as the ensemble vectors).
+void ens_eom(Ens& E, cplx* out) {
+  launch_h1(E.h1_d, (int)E.h1_h.size(), E.h1_maxn2, E.h1_smem, true, E.st, E.precision);
+  launch_matsum(E.msum_d, (int)E.msum_h.size(), E.msum_src_d, E.st);
+  E.launches += 3;
+  for (size_t i = 1; i < E.chains.size(); ++i) ens_run_prod(E, E.chains[i]);
+  ens_run_prod(E, E.gprods);
+  ens_run_hole(E, E.rho_holes);
+  ens_run_hole(E, E.holes);
+  ens_run_red(E, E.red);
+  launch_reginv(E.reg_d, (int)E.reg_h.size(), E.mfop_d, E.status_d, E.st);
+  launch_termsum(out, E.sum_d, (int)E.sum_h.size(), E.src_d, E.total, E.st, E.precision);
+  launch_spf(E.spf_d, (int)E.spf_h.size(), E.spf_tiles, E.spfop_d, out, E.der, E.status_d, E.st, E.precision);
+  E.launches += 5;
+  E.eom_count++;
+}
+
+void ens_stage(Ens& E, cplx* out, const cplx* base, const double* coef, int nk) {
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  int n = 0;
+  for (int j = 0; j < nk; ++j) {
+    if (coef[j] == 0.0) continue;
+    a.k[n] = E.K[j];
+    a.c[n] = coef[j];
+    ++n;
+  }
+  a.nk = n;
+  launch_ens_stage(out, base, a, E.dt_d, E.off_d, (int)E.m.size(), E.total, E.st);
+  ++E.launches;
+}
+
+void ens_check_status(Ens& E) {
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, E.status_d, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+  CK(cudaStreamSynchronize(E.st));
+  if (st != 0) {
+    CK(cudaMemsetAsync(E.status_d, 0, sizeof(int), E.st));
+    if (st & DEVST_EIG_NOCONV) throw StatusError(MCTDH_EEIG, "Jacobi eigensolver did not converge");
+    if (st & DEVST_CHOL_FAIL) throw StatusError(MCTDH_EEIG, "SPF overlap matrix is not positive definite");
+    throw StatusError(MCTDH_ENONFINITE, "device status " + std::to_string(st));
+  }
+}
+
+// Every member from its time t[i] to tnext with adaptive RK (int_type 1 Cash-Karp,
+// 2 Dormand-Prince); step[i]: the trial step, updated like propagate_wf's
+// (propagator.f90:110-134).  Dormand-Prince re-evaluates the first stage at each
+// step start instead of carrying it (the same numbers: the EOM is deterministic).
+void ens_propagate(Ens& E, int method, double tnext, double* t, double* step) {
+  const int n = (int)E.m.size();
+  const bool dp = (method == 2);
+  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
+  std::vector<int> done(n, 0), acc(n, 0);
+  std::vector<double> dt(n, 0.0), hn(n, 0.0);
+  std::vector<cplx> res(3 * (size_t)n);
+  for (int i = 0; i < n; ++i) done[i] = (t[i] >= tnext - E.m[i]->min_stepsize);
+  for (long long guard = 0;; ++guard) {
+    bool any = false;
+    for (int i = 0; i < n; ++i) any = any || !done[i];
+    if (!any) break;
+    if (guard > 1000000) throw StatusError(MCTDH_ESTEP, "ensemble propagation did not finish");
+    // the derivative at every member's step start
+    CK(cudaMemcpyAsync(E.IN, E.Y, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
+    ens_eom(E, E.K[0]);
+    std::vector<int> pending(n, 0);
+    for (int i = 0; i < n; ++i) {
+      pending[i] = !done[i];
+      dt[i] = pending[i] ? step[i] : 0.0;
+    }
+    while (true) {
+      bool anyp = false;
+      for (int i = 0; i < n; ++i) anyp = anyp || pending[i];
+      if (!anyp) break;
+      ++E.rounds;
+      std::vector<double> dth(n);
+      for (int i = 0; i < n; ++i) dth[i] = pending[i] ? dt[i] : 0.0;
+      CK(cudaMemcpyAsync(E.dt_d, dth.data(), sizeof(double) * n, cudaMemcpyHostToDevice, E.st));
+      for (int sg = 1; sg < 6; ++sg) {
+        ens_stage(E, E.IN, E.Y, dp ? DP_B[sg] : CK_B[sg], sg);
+        ens_eom(E, E.K[sg]);
+      }
+      ens_stage(E, E.TMP, E.Y, dp ? DP_C : CK_C, 6);
+      if (dp) {
+        CK(cudaMemcpyAsync(E.IN, E.TMP, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
+        ens_eom(E, E.K[6]);
+        ens_stage(E, E.ERR, E.Y, DP_D, 7);
+      } else {
+        ens_stage(E, E.ERR, E.Y, CK_D, 6);
+      }
+      // DeltaPsi (gmctdh_objects.f90:206-226) of every member
+      ens_run_hole(E, E.ov_spf_holes);
+      ens_run_red(E, E.ov_spf_red);
+      for (size_t d = 1; d < E.ov_chain.size(); ++d) ens_run_prod(E, E.ov_chain[d]);
+      ens_run_hole(E, E.ov_dots);
+      ens_run_red(E, E.ov_dot_red);
+      CK(cudaMemcpyAsync(res.data(), E.res_d, sizeof(cplx) * 3 * n, cudaMemcpyDeviceToHost, E.st));
+      ens_check_status(E);
+      for (int i = 0; i < n; ++i) {
+        acc[i] = 0;
+        if (!pending[i]) continue;
+        const Ctx& c = *E.m[i];
+        const double o11 = res[3 * i].x, o22 = res[3 * i + 1].x, o12 = res[3 * i + 2].x;
+        const double errmax = sqrt(fabs(2.0 * (1.0 - o12 / sqrt(o11 * o22)))) / c.eps_int;
+        if (!std::isfinite(errmax)) throw StatusError(MCTDH_ENONFINITE, "non-finite RK error estimate");
+        if (errmax < 1.0 || dt[i] <= c.min_stepsize) {   // rkqs accept (integrator.f90:63)
+          double h = (errmax > errcon) ? RK_SAFETY * dt[i] * pow(errmax, RK_PGROW) : dt[i] * RK_MAXSCAL;
+          h = std::max(h, c.min_stepsize);
+          hn[i] = std::min(h, c.writetime);
+          acc[i] = 1;
+          pending[i] = 0;
+        } else {
+          double d = std::max(RK_MINSCAL * dt[i], RK_SAFETY * dt[i] * pow(errmax, RK_PSHRNK));
+          dt[i] = std::max(d, c.min_stepsize);
+        }
+      }
+      CK(cudaMemcpyAsync(E.acc_d, acc.data(), sizeof(int) * n, cudaMemcpyHostToDevice, E.st));
+      launch_ens_accept(E.Y, E.TMP, E.acc_d, E.off_d, n, E.total, E.st);
+      ++E.launches;
+      for (int i = 0; i < n; ++i) {
+        if (!acc[i]) continue;
+        const Ctx& c = *E.m[i];
+        t[i] += dt[i];
+        if (t[i] >= tnext - c.min_stepsize) {
+          done[i] = 1;
+          continue;
+        }
+        const long long q = (long long)((tnext - t[i]) / hn[i]);   // propagator.f90:124-126
+        step[i] = (q == 0) ? (tnext - t[i]) : (tnext - t[i]) / (double)(q + 1);
+      }
+    }
+  }
+  CK(cudaStreamSynchronize(E.st));
+}
+
+void observables(Ctx& c, double* energy, double* pop, double* norm, double* auto_re, double* auto_im);
+
 }  // namespace
 
 struct mctdh_ctx {
@@ -2147,6 +2545,76 @@ struct mctdh_ctx {
 
 // Error text for calls that run without a context (read with mctdh_last_error(NULL)).
 void mctdh_set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+
+namespace {
+// WriteOutput quantities (output.f90:35-87, 144-150) of the resident state.
+void observables(Ctx& c, double* energy, double* pop, double* norm, double* auto_re, double* auto_im) {
+  {
+    eom_from(c, c.d_y, c.d_out);
+    // f * H A before the Gaussian-mode corrections (Calc_MeanField's energyMF)
+    const cplx* hA = c.modes_gwp.empty() ? c.d_out : c.d_adot;
+    cplx e = dot_now(c, c.d_y, hA, c.naconftot);
+    // energy = Re <A| H A> = Re( <A|dA> / der_factor )
+    double dr = c.der.x, di = c.der.y, den = dr * dr + di * di;
+    double en = (e.x * dr + e.y * di) / den;
+    std::vector<double> p(c.nstates);
+    double tot = 0.0;
+    const int m0 = 0;
+    for (int s = 0; s < c.nstates; ++s) {
+      int n = c.m_of(m0, s);
+      std::vector<cplx> r(n * n);
+      CK(cudaMemcpyAsync(r.data(), c.rho[m0][s], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c.st));
+      CK(cudaStreamSynchronize(c.st));
+      double tr = 0.0;
+      if (c.is_gwp[m0]) {
+        // Gaussian first mode: sum of rho o S00 from the upper triangle (output.f90:63-85)
+        std::vector<cplx> S(n * n);
+        const cplx* sp = c.s00[c.gwp_of[m0]][set_of(c, m0, s)][set_of(c, m0, s)];
+        CK(cudaMemcpyAsync(S.data(), sp, sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c.st));
+        CK(cudaStreamSynchronize(c.st));
+        for (int j2 = 0; j2 < n; ++j2) {
+          for (int j1 = 0; j1 < j2; ++j1) tr += 2.0 * cmul(r[j1 + n * j2], S[j1 + n * j2]).x;
+          tr += cmul(r[j2 + n * j2], S[j2 + n * j2]).x;
+        }
+      } else {
+        for (int j = 0; j < n; ++j) tr += r[j + n * j].x;
+      }
+      p[s] = tr;
+      tot += tr;
+    }
+    run_ovl(c, c.auto_plan);
+    cplx o[3];
+    read_ovl(c, c.auto_plan, o);
+    check_status(c);
+    if (energy) *energy = en / tot;
+    if (pop) for (int s = 0; s < c.nstates; ++s) pop[s] = p[s];
+    if (norm) *norm = tot;
+    if (auto_re) *auto_re = o[2].x;
+    if (auto_im) *auto_im = o[2].y;
+  }
+}
+}  // namespace
+
+struct mctdh_ens {
+  Ens* e;
+};
+
+template <typename F>
+int64_t ens_guarded(mctdh_ens* h, F&& fn) {
+  try {
+    fn();
+    return MCTDH_OK;
+  } catch (const StatusError& e) {
+    h->e->last_error = e.what();
+    return e.code;
+  } catch (const CudaError& e) {
+    h->e->last_error = e.what();
+    return MCTDH_ECUDA;
+  } catch (const std::exception& e) {
+    h->e->last_error = e.what();
+    return MCTDH_EARG;
+  }
+}
 
 extern "C" {
 
@@ -2185,7 +2653,7 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
   drain_profile(*c);
   for (auto e : c->evpool) cudaEventDestroy(e);
   for (auto e : c->user_ev) if (e) cudaEventDestroy(e);
-  cudaStreamDestroy(c->st);
+  if (c->own_stream) cudaStreamDestroy(c->st);
   delete c;
   delete ctx;
   return MCTDH_OK;
@@ -2510,50 +2978,8 @@ int64_t mctdh_observables(mctdh_ctx_t* ctx, double t, double* energy, double* po
                           double* auto_re, double* auto_im) {
   if (!ctx) return MCTDH_EARG;
   Ctx* c = ctx->c;
-  return guarded(c, [&] {
-    (void)t;
-    eom_from(*c, c->d_y, c->d_out);
-    // f * H A before the Gaussian-mode corrections (Calc_MeanField's energyMF)
-    const cplx* hA = c->modes_gwp.empty() ? c->d_out : c->d_adot;
-    cplx e = dot_now(*c, c->d_y, hA, c->naconftot);
-    // energy = Re <A| H A> = Re( <A|dA> / der_factor )
-    double dr = c->der.x, di = c->der.y, den = dr * dr + di * di;
-    double en = (e.x * dr + e.y * di) / den;
-    std::vector<double> p(c->nstates);
-    double tot = 0.0;
-    const int m0 = 0;
-    for (int s = 0; s < c->nstates; ++s) {
-      int n = c->m_of(m0, s);
-      std::vector<cplx> r(n * n);
-      CK(cudaMemcpyAsync(r.data(), c->rho[m0][s], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c->st));
-      CK(cudaStreamSynchronize(c->st));
-      double tr = 0.0;
-      if (c->is_gwp[m0]) {
-        // Gaussian first mode: sum of rho o S00 from the upper triangle (output.f90:63-85)
-        std::vector<cplx> S(n * n);
-        const cplx* sp = c->s00[c->gwp_of[m0]][set_of(*c, m0, s)][set_of(*c, m0, s)];
-        CK(cudaMemcpyAsync(S.data(), sp, sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        for (int j2 = 0; j2 < n; ++j2) {
-          for (int j1 = 0; j1 < j2; ++j1) tr += 2.0 * cmul(r[j1 + n * j2], S[j1 + n * j2]).x;
-          tr += cmul(r[j2 + n * j2], S[j2 + n * j2]).x;
-        }
-      } else {
-        for (int j = 0; j < n; ++j) tr += r[j + n * j].x;
-      }
-      p[s] = tr;
-      tot += tr;
-    }
-    run_ovl(*c, c->auto_plan);
-    cplx o[3];
-    read_ovl(*c, c->auto_plan, o);
-    check_status(*c);
-    if (energy) *energy = en / tot;
-    if (pop) for (int s = 0; s < c->nstates; ++s) pop[s] = p[s];
-    if (norm) *norm = tot;
-    if (auto_re) *auto_re = o[2].x;
-    if (auto_im) *auto_im = o[2].y;
-  });
+  (void)t;
+  return guarded(c, [&] { observables(*c, energy, pop, norm, auto_re, auto_im); });
 }
 
 int64_t mctdh_norm_wf(mctdh_ctx_t* ctx, const double* A, const double* psi, double* norm) {
@@ -2582,6 +3008,111 @@ int64_t mctdh_wf_ovl(mctdh_ctx_t* ctx, const double* A1, const double* psi1, con
     *re = o[2].x;
     *im = o[2].y;
   });
+}
+
+
+// ---------------------------------------------------------------------------
+// Ensembles
+// ---------------------------------------------------------------------------
+int64_t mctdh_ens_create(const mctdh_setup_t* setups, int64_t n, mctdh_ens_t** out) {
+  if (!setups || !out || n < 1) return MCTDH_EARG;
+  *out = nullptr;
+  try {
+    Ens* e = ens_create(setups, (int)n);
+    *out = new mctdh_ens{e};
+    g_create_error.clear();
+    return MCTDH_OK;
+  } catch (const StatusError& e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const CudaError& e) {
+    g_create_error = e.what();
+    return MCTDH_ECUDA;
+  } catch (const std::exception& e) {
+    g_create_error = e.what();
+    return MCTDH_EARG;
+  }
+}
+
+int64_t mctdh_ens_destroy(mctdh_ens_t* ens) {
+  if (!ens) return MCTDH_EARG;
+  ens_destroy(ens->e);
+  delete ens;
+  return MCTDH_OK;
+}
+
+int64_t mctdh_ens_set_state(mctdh_ens_t* ens, int64_t i, const double* A, const double* psi, int64_t as_start) {
+  if (!ens || !A || !psi || i < 0 || i >= (int64_t)ens->e->m.size()) return MCTDH_EARG;
+  return ens_guarded(ens, [&] {
+    Ctx& c = *ens->e->m[i];
+    upload(c, c.d_y, A, psi);
+    if (as_start) copy_dev(c, c.d_y0, c.d_y, c.ntot);
+    CK(cudaStreamSynchronize(c.st));
+  });
+}
+
+int64_t mctdh_ens_get_state(mctdh_ens_t* ens, int64_t i, double* A, double* psi) {
+  if (!ens || !A || !psi || i < 0 || i >= (int64_t)ens->e->m.size()) return MCTDH_EARG;
+  return ens_guarded(ens, [&] {
+    Ctx& c = *ens->e->m[i];
+    download(c, c.d_y, A, psi);
+  });
+}
+
+int64_t mctdh_ens_calc_derivs(mctdh_ens_t* ens) {
+  if (!ens) return MCTDH_EARG;
+  return ens_guarded(ens, [&] {
+    Ens& E = *ens->e;
+    CK(cudaMemcpyAsync(E.IN, E.Y, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
+    ens_eom(E, E.OUT);
+    ens_check_status(E);
+  });
+}
+
+int64_t mctdh_ens_get_derivs(mctdh_ens_t* ens, int64_t i, double* dA, double* dpsi) {
+  if (!ens || !dA || !dpsi || i < 0 || i >= (int64_t)ens->e->m.size()) return MCTDH_EARG;
+  return ens_guarded(ens, [&] {
+    Ctx& c = *ens->e->m[i];
+    download(c, c.d_out, dA, dpsi);
+  });
+}
+
+int64_t mctdh_ens_propagate(mctdh_ens_t* ens, int64_t int_type, double tnext, double* t, double* step,
+                            int64_t* nrounds, int64_t* neom) {
+  if (!ens || !t || !step) return MCTDH_EARG;
+  if (int_type != 1 && int_type != 2) return MCTDH_EUNSUPPORTED;
+  return ens_guarded(ens, [&] {
+    Ens& E = *ens->e;
+    const long long r0 = E.rounds, e0 = E.eom_count;
+    ens_propagate(E, (int)int_type, tnext, t, step);
+    if (nrounds) *nrounds = E.rounds - r0;
+    if (neom) *neom = E.eom_count - e0;
+  });
+}
+
+int64_t mctdh_ens_observables(mctdh_ens_t* ens, int64_t i, double* energy, double* pop, double* norm,
+                              double* auto_re, double* auto_im) {
+  if (!ens || i < 0 || i >= (int64_t)ens->e->m.size()) return MCTDH_EARG;
+  return ens_guarded(ens, [&] { observables(*ens->e->m[i], energy, pop, norm, auto_re, auto_im); });
+}
+
+int64_t mctdh_ens_counters(mctdh_ens_t* ens, int64_t* launches, int64_t* eom, int64_t* rounds) {
+  if (!ens) return MCTDH_EARG;
+  if (launches) *launches = ens->e->launches;
+  if (eom) *eom = ens->e->eom_count;
+  if (rounds) *rounds = ens->e->rounds;
+  return MCTDH_OK;
+}
+
+int64_t mctdh_ens_stream(mctdh_ens_t* ens, void** stream) {
+  if (!ens || !stream) return MCTDH_EARG;
+  *stream = (void*)ens->e->st;
+  return MCTDH_OK;
+}
+
+const char* mctdh_ens_last_error(mctdh_ens_t* ens) {
+  if (!ens) return g_create_error.c_str();
+  return ens->e->last_error.c_str();
 }
 
 }  // extern "C"

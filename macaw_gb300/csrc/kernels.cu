@@ -5,6 +5,8 @@
 // each fibre of a tensor is read once into registers (mode products), fibre tiles
 // are staged in shared memory for the single-hole contractions, and reductions
 // are two-stage with a fixed summation order so reruns are bitwise identical.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include <stdio.h>
 
@@ -882,16 +884,19 @@ __global__ void spf_solve_kernel(const SpfDesc* __restrict__ descs, int* status)
     }
     __syncthreads();
   }
+  __shared__ double invd[MAXN_SPF];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) invd[i] = 1.0 / S[i + ld * i].x;
+  __syncthreads();
   for (int cidx = threadIdx.x; cidx < n; cidx += blockDim.x) {
     for (int i = 0; i < n; ++i) {
       cplx v = O[i + ld * cidx];
       for (int k = 0; k < i; ++k) v = csub(v, cmul(cconj(S[k + ld * i]), O[k + ld * cidx]));
-      O[i + ld * cidx] = cscale(v, 1.0 / S[i + ld * i].x);
+      O[i + ld * cidx] = cscale(v, invd[i]);
     }
     for (int i = n - 1; i >= 0; --i) {
       cplx v = O[i + ld * cidx];
       for (int k = i + 1; k < n; ++k) v = csub(v, cmul(S[i + ld * k], O[k + ld * cidx]));
-      O[i + ld * cidx] = cscale(v, 1.0 / S[i + ld * i].x);
+      O[i + ld * cidx] = cscale(v, invd[i]);
     }
   }
   if (threadIdx.x == 0 && s_fail) atomicOr(status, DEVST_CHOL_FAIL);
@@ -938,9 +943,12 @@ __global__ void termsum_kernel(cplx* __restrict__ out, const SumRange* __restric
                                const SumSrc* __restrict__ srcs, long long total) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
-  int r = 0;
-  while (r + 1 < nr && i >= ranges[r + 1].offset) ++r;
-  const SumRange& rg = ranges[r];
+  int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
+  }
+  const SumRange& rg = ranges[lo];
   const long long li = i - rg.offset;
   if (li < 0 || li >= rg.n) return;
   cplx acc = mkc(0, 0);
@@ -957,9 +965,12 @@ __global__ void termsum_split_kernel(cplx* __restrict__ out, const SumRange* __r
                                      const SumSrc* __restrict__ srcs, long long total) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
-  int r = 0;
-  while (r + 1 < nr && i >= ranges[r + 1].offset) ++r;
-  const SumRange& rg = ranges[r];
+  int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
+  }
+  const SumRange& rg = ranges[lo];
   const long long li = i - rg.offset;
   if (li < 0 || li >= rg.n) return;
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
@@ -999,6 +1010,47 @@ __global__ void stage_kernel(cplx* __restrict__ out, const cplx* __restrict__ ba
   }
   cplx b = base[i];
   out[i] = mkc(fma(dt, s.x, b.x), fma(dt, s.y, b.y));
+}
+
+// Ensemble stage: every member m (elements off[m] .. off[m+1]) with its own dt.
+__device__ __forceinline__ int member_of(const long long* __restrict__ off, int nm, long long i) {
+  int lo = 0, hi = nm - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void ens_stage_kernel(cplx* __restrict__ out, const cplx* __restrict__ base, StageArgs a,
+                                 const double* __restrict__ dt, const long long* __restrict__ off, int nm,
+                                 long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double h = dt[member_of(off, nm, i)];
+  cplx s = mkc(0, 0);
+  for (int k = 0; k < a.nk; ++k) {
+    cplx v = a.k[k][i];
+    s.x = fma(a.c[k], v.x, s.x);
+    s.y = fma(a.c[k], v.y, s.y);
+  }
+  cplx b = base[i];
+  out[i] = mkc(fma(h, s.x, b.x), fma(h, s.y, b.y));
+}
+void launch_ens_stage(cplx* out, const cplx* base, const StageArgs& a, const double* dt, const long long* off, int nm,
+                      long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  ens_stage_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, base, a, dt, off, nm, n);
+}
+__global__ void ens_accept_kernel(cplx* __restrict__ y, const cplx* __restrict__ src, const int* __restrict__ accept,
+                                  const long long* __restrict__ off, int nm, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (accept[member_of(off, nm, i)]) y[i] = src[i];
+}
+void launch_ens_accept(cplx* y, const cplx* src, const int* accept, const long long* off, int nm, long long n,
+                       cudaStream_t st) {
+  if (n <= 0) return;
+  ens_accept_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, src, accept, off, nm, n);
 }
 
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st) {
@@ -1135,30 +1187,44 @@ void launch_masked_copy(cplx* y, const cplx* src, const unsigned char* elem_mode
 
 // Calc_Err_SPF (cmf2_derivatives.f90:239-283): err_m = sqrt|sum_blocks Tr(rho dS)| with
 // the reference's upper-triangle evaluation; one thread per mode.
-__global__ void spf_err_kernel(const SpfErrDesc* __restrict__ d, int nd, double* err_mode, int nmodes) {
+// err_m = sqrt|sum over the mode's blocks of Tr(rho . dS)| (Calc_Err_SPF,
+// cmf2_derivatives.f90:239-338): one warp per block (lane-strided entries,
+// shuffle sum), then one thread per mode adds its blocks in descriptor order.
+__global__ void __launch_bounds__(1024) spf_err_kernel(const SpfErrDesc* __restrict__ d, int nd, double* err_mode,
+                                                       int nmodes) {
+  __shared__ double part[256];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int q = warp; q < nd && q < 256; q += nw) {
+    const int n = d[q].n;
+    const cplx* r = d[q].rho;
+    const cplx* o = d[q].ds;
+    double e = 0.0;
+    for (int pr = lane; pr < n * n; pr += 32) {
+      const int j1 = pr % n, j2 = pr / n;
+      if (j1 > j2) continue;
+      const cplx rv = r[pr], ov = o[pr];
+      e += (j1 < j2) ? 2.0 * (rv.x * ov.x + rv.y * ov.y) : (rv.x * ov.x - rv.y * ov.y);
+    }
+    for (int off = 16; off > 0; off >>= 1) e += __shfl_down_sync(0xffffffffu, e, off);
+    if (lane == 0) part[q] = e;
+  }
+  __syncthreads();
   const int m = threadIdx.x;
   if (m >= nmodes) return;
   double e = 0.0;
   bool any = false;
-  for (int q = 0; q < nd; ++q) {
+  for (int q = 0; q < nd && q < 256; ++q) {
     if (d[q].mode != m) continue;
     any = true;
-    const int n = d[q].n;
-    const cplx* r = d[q].rho;
-    const cplx* o = d[q].ds;
-    for (int j2 = 0; j2 < n; ++j2) {
-      for (int j1 = 0; j1 < j2; ++j1) {
-        cplx rv = r[j1 + n * j2], ov = o[j1 + n * j2];
-        e += 2.0 * (rv.x * ov.x + rv.y * ov.y);
-      }
-      cplx rv = r[j2 + n * j2], ov = o[j2 + n * j2];
-      e += rv.x * ov.x - rv.y * ov.y;
-    }
+    e += part[q];
   }
   err_mode[m] = any ? sqrt(fabs(e)) : 0.0;
 }
 void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, cudaStream_t st) {
-  spf_err_kernel<<<1, 64, 0, st>>>(d, nd, err_mode, nmodes);
+  // nd <= 256 blocks (checked when the plan is built), nmodes <= 64
+  const int warps = std::max(std::min(nd, 32), (nmodes + 31) / 32);
+  spf_err_kernel<<<1, 32 * warps, 0, st>>>(d, nd, err_mode, nmodes);
 }
 
 // ---------------------------------------------------------------------------
@@ -1187,18 +1253,23 @@ void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_a
   lan_axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Kn, Kj, Kp, dot_alpha, beta_prev, alpha_out, n);
 }
 
+// Grid-stride: the norm and its reciprocal once per thread (FP64 square roots and
+// divisions are expensive on this GPU), then one multiply per component.
 __global__ void lan_normalize_kernel(cplx* __restrict__ out, const cplx* __restrict__ in, const cplx* __restrict__ nrm2,
                                      double* beta_out, long long n) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const double beta = sqrt(nrm2->x);
-  if (i == 0 && beta_out) *beta_out = beta;
-  if (i >= n) return;
+  if (i0 == 0 && beta_out) *beta_out = beta;
   const double s = 1.0 / beta;
-  cplx v = in[i];
-  out[i] = mkc(v.x * s, v.y * s);
+  for (long long i = i0; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const cplx v = in[i];
+    out[i] = mkc(v.x * s, v.y * s);
+  }
 }
 void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st) {
-  lan_normalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, in, nrm2, beta_out, n);
+  const long long want = (n + 255) / 256;
+  const unsigned nb = (unsigned)std::max<long long>(1, std::min<long long>(want, 152 * 4));
+  lan_normalize_kernel<<<nb, 256, 0, st>>>(out, in, nrm2, beta_out, n);
 }
 
 // ---------------------------------------------------------------------------

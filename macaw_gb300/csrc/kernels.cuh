@@ -192,6 +192,11 @@ void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
                     long long total, cudaStream_t st, int prec);
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st);
+// ensembles: member m owns elements off[m] .. off[m+1] of the vectors
+void launch_ens_stage(cplx* out, const cplx* base, const StageArgs& a, const double* dt, const long long* off, int nm,
+                      long long n, cudaStream_t st);
+void launch_ens_accept(cplx* y, const cplx* src, const int* accept, const long long* off, int nm, long long n,
+                       cudaStream_t st);
 void launch_copy_scale(cplx* out, const cplx* in, cplx s, long long n, cudaStream_t st);
 void launch_axpy(cplx* y, const cplx* x, cplx a, long long n, cudaStream_t st);
 void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* coef, int ncol, long long n,
