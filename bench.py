@@ -39,6 +39,7 @@ WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/
 EPS_CMF = 1e-5
 PRE_FS = 1.0
 MFX_EPOCHS = 12
+TRAFFIC_PER_ALG_BYTE = 0.43   # ncu DRAM bytes per algorithmic byte, mode products of this model
 ACC_FS = 0.5   # interval over which the split path is compared with the FP64 path
 REF_STEP_FS = 0.1   # CMF2 step length the reference arm times (steady-state steps are of this order)
 
@@ -217,17 +218,30 @@ def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mf
         hdid, h, _ = core.step(INT_CMF2, t, h)
         t += hdid
     c0 = core.counters()
-    if profile:
-        core.profile(2)
     barrier(tdist)
     torch.cuda.synchronize()
     t, h, ms, fs, hdids = timed_steps(core, t, h, args.steps, l2, torch)
     torch.cuda.synchronize()
     barrier(tdist)
-    prof = core.profile_read() if profile else None
-    core.profile(0)
     c1 = core.counters()
-    return core, dict(t=t, h=h, ms=ms, fs=fs, hdids=hdids, prof=prof,
+    prof, prof_ms = None, None
+    if profile:
+        # per-kernel-class CUDA events on the same number of further steps (a
+        # separate pass: the events and the launches without graphs it needs
+        # stay out of the timed region above)
+        core.profile(2)
+        torch.cuda.synchronize()
+        core.event_record(0)
+        tp, hp = t, h
+        for _ in range(args.steps):
+            hdid, hp, _ = core.step(INT_CMF2, tp, hp)
+            tp += hdid
+        core.event_record(1)
+        torch.cuda.synchronize()
+        prof_ms = core.event_elapsed(0, 1)
+        prof = core.profile_read()
+        core.profile(0)
+    return core, dict(t=t, h=h, ms=ms, fs=fs, hdids=hdids, prof=prof, prof_ms=prof_ms,
                       eom=c1["eom"] - c0["eom"], hb=c1["hb"] - c0["hb"], launches=c1["launches"] - c0["launches"])
 
 
@@ -348,15 +362,21 @@ def run_gpu(args):
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": mix["launches"],
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                     "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
+                     "traffic": by_launch * TRAFFIC_PER_ALG_BYTE if dname == "mode_product" else None,
+                     "traffic_source": "ncu DRAM bytes / algorithmic bytes of three mode-product launches of "
+                                       "this model (profiles/qvc12_cmf2_split32_ncu.md), times the "
+                                       "algorithmic bytes per launch",
                      "peak_source": peak_src},
-        "fp64_roofline": {"kernel": dname, "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
-                          "frac": achieved_tf / fp64_peak if fp64_peak > 0 else None,
-                          "peak_source": "measured FP64 FMA chain on this GPU"},
+        "compute": ({"kernel": dname, "achieved": achieved_tf, "unit": "TFLOP/s (complex MAC = 8 flop)",
+                     "fp64_peak": fp64_peak, "frac_of_fp64_peak": achieved_tf / fp64_peak if fp64_peak > 0 else None,
+                     "peak_source": "measured FP64 FMA chain on this GPU"} if args.precision == 0 else
+                    {"kernel": dname, "achieved": achieved_tf, "unit": "TFLOP/s (complex MAC = 8 flop)",
+                     "note": "split-FP32 arithmetic: FP32-issue-bound in ncu (FMA pipe 55-60 %, issue 68-74 %)"}),
         "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                                "share": round(v["ms"] / tot_ms, 4)}
                            for k, v in prof.items() if v["launches"]},
-        "gpu_busy_frac": tot_ms / ms_total,
+        "gpu_busy_frac_profiled_pass": tot_ms / mix["prof_ms"] if mix["prof_ms"] else None,
         "clocks": clocks,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

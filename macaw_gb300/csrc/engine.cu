@@ -249,6 +249,14 @@ struct Ctx {
   bool ops_fresh = false;    // operators/mean fields at d_y are in place (time ops_fresh_t)
   double ops_fresh_t = -1.0;
   bool profiling = false;
+  // CUDA graphs of launch sequences that repeat with the same buffers: (kind, key
+  // buffer) -> (executable graph, kernel launches it holds)
+  struct GraphRec {
+    cudaGraphExec_t exec;
+    long long launches, eoms;   // what one replay accounts for
+  };
+  std::map<std::pair<int, const void*>, GraphRec> graphs;
+  bool graphs_off = false;
   KProf prof[KP_N];
   std::vector<PendingEv> pending;
   std::vector<cudaEvent_t> evpool;
@@ -1264,6 +1272,53 @@ void drain_profile(Ctx& c) {
   c.pending.clear();
 }
 
+// Run `body` (a launch sequence without host synchronisation) through a CUDA
+// graph captured on its first use for this (kind, key); if capture is not
+// possible the sequence is launched directly from then on.
+template <typename F>
+void run_graphed(Ctx& c, int kind, const void* key, F&& body) {
+  if (c.profiling || c.graphs_off) {
+    body();
+    return;
+  }
+  auto k = std::make_pair(kind, key);
+  auto it = c.graphs.find(k);
+  if (it == c.graphs.end()) {
+    const long long l0 = c.launches, e0 = c.eom_count;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      c.graphs_off = true;
+      body();
+      return;
+    }
+    bool ok = true;
+    try {
+      body();
+    } catch (...) {
+      ok = false;
+    }
+    cudaError_t e = cudaStreamEndCapture(c.st, &g);
+    cudaGraphExec_t ge = nullptr;
+    if (ok && e == cudaSuccess && g) ok = (cudaGraphInstantiate(&ge, g, 0) == cudaSuccess);
+    else ok = false;
+    if (g) cudaGraphDestroy(g);
+    const long long nl = c.launches - l0, ne = c.eom_count - e0;
+    c.launches = l0;
+    c.eom_count = e0;
+    if (!ok) {
+      cudaGetLastError();
+      c.graphs_off = true;
+      body();
+      return;
+    }
+    it = c.graphs.emplace(k, Ctx::GraphRec{ge, nl, ne}).first;
+  }
+  CK(cudaGraphLaunch(it->second.exec, c.st));
+  c.launches += it->second.launches;
+  c.eom_count += it->second.eoms;
+}
+
 void run_prod(Ctx& c, const ProdBatch& b) {
   if (b.h.empty()) return;
   ProfScope ps(c, KP_PROD, b.flops, b.bytes);
@@ -1578,8 +1633,10 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
 // operators and mean fields on the state y (Calc_rho1mode, Calc_h1mode,
 // Calc_MeanField, Calc_rhom1MF): one EOM into d_out (the derivative is unused).
 void operators_and_mf(Ctx& c, const cplx* y) {
-  if (y != c.d_in) CK(cudaMemcpyAsync(c.d_in, y, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
-  eom(c, c.d_out, true);
+  run_graphed(c, 2, y, [&] {
+    if (y != c.d_in) CK(cudaMemcpyAsync(c.d_in, y, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+    eom(c, c.d_out, true);
+  });
 }
 
 void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
@@ -1719,23 +1776,25 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
     if (iter > 100000) throw StatusError(MCTDH_ESTEP, "SPF integration did not finish");
     ++S.rk_iters;
     CK(cudaMemcpyAsync(S.dt_mode, dt_h.data(), sizeof(double) * 64, cudaMemcpyHostToDevice, c.st));
-    copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
-    spf_eval_all(c, S, c.d_k[0]);
-    for (int st = 1; st < 6; ++st) {
-      stage_modes(c, S, c.d_in, y, dp ? DP_B[st] : CK_B[st], st);
-      spf_eval_all(c, S, c.d_k[st]);
-    }
-    if (dp) {
-      // the 7th stage is the derivative at the 5th-order solution (:386-393)
-      stage_modes(c, S, c.d_in, y, DP_C, 6);
-      spf_eval_all(c, S, c.d_k[6]);
-      stage_modes(c, S, c.d_tmp, y, DP_C, 6);
-      stage_modes(c, S, c.d_err, y, DP_D, 7);
-    } else {
-      stage_modes(c, S, c.d_tmp, y, CK_C, 6);
-      stage_modes(c, S, c.d_err, y, CK_D, 6);
-    }
-    {
+    // one RK attempt of every mode: the same launches on the same buffers each
+    // iteration (the step lengths live in S.dt_mode), so it runs as a CUDA graph
+    run_graphed(c, 1, y, [&] {
+      copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
+      spf_eval_all(c, S, c.d_k[0]);
+      for (int st = 1; st < 6; ++st) {
+        stage_modes(c, S, c.d_in, y, dp ? DP_B[st] : CK_B[st], st);
+        spf_eval_all(c, S, c.d_k[st]);
+      }
+      if (dp) {
+        // the 7th stage is the derivative at the 5th-order solution (:386-393)
+        stage_modes(c, S, c.d_in, y, DP_C, 6);
+        spf_eval_all(c, S, c.d_k[6]);
+        stage_modes(c, S, c.d_tmp, y, DP_C, 6);
+        stage_modes(c, S, c.d_err, y, DP_D, 7);
+      } else {
+        stage_modes(c, S, c.d_tmp, y, CK_C, 6);
+        stage_modes(c, S, c.d_err, y, CK_D, 6);
+      }
       StageArgs a;
       memset(&a, 0, sizeof(a));
       a.k[0] = c.d_err + nA;
@@ -1743,11 +1802,11 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
       a.nk = 1;
       launch_stage(S.ytmp + nA, c.d_tmp + nA, a, 1.0, c.dimpsi, c.st);
       c.count();
-    }
-    run_hole(c, S.err_holes);
-    run_red(c, S.err_red);
-    launch_spf_err(S.errd_d, (int)S.errd_h.size(), S.err_mode, f, c.st);
-    c.count();
+      run_hole(c, S.err_holes);
+      run_red(c, S.err_red);
+      launch_spf_err(S.errd_d, (int)S.errd_h.size(), S.err_mode, f, c.st);
+      c.count();
+    });
     CK(cudaMemcpyAsync(err_h.data(), S.err_mode, sizeof(double) * f, cudaMemcpyDeviceToHost, c.st));
     CK(cudaStreamSynchronize(c.st));
     for (int m = 0; m < f; ++m) {
@@ -2650,6 +2709,7 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
     g_mfx.erase(mi);
   }
   for (auto& kv : c->dots) delete kv.second;
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
   drain_profile(*c);
   for (auto e : c->evpool) cudaEventDestroy(e);
   for (auto e : c->user_ev) if (e) cudaEventDestroy(e);
