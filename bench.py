@@ -472,6 +472,50 @@ def run_ensemble(args):
     return 0
 
 
+def run_rk_workload(args):
+    """RK configurations: lvc5 (2-state LVC over 5 HO modes, Cash-Karp, eps 1e-8)
+    and gmctdh16 (2-state LVC, 4 HO modes + one 12-DOF Gaussian mode with 32
+    Gaussians per state).  After 0.2 fs untimed, `--rk-fs` fs timed with CUDA
+    events on the library's stream; C(t) against the FP64 path when the
+    precision is split."""
+    import torch
+    from macaw_gb300.capi import GpuCore
+    from macaw_gb300.generate import lvc5, gmctdh16
+    torch.cuda.init()
+    model = lvc5() if args.workload == "lvc5" else gmctdh16()
+    A0, psi0 = initial_wavefunction(model)
+    out = {}
+    for prec in sorted({0, args.precision}):
+        core = GpuCore(model, precision=prec)
+        core.set_state(A0, psi0, as_start=True)
+        t, h, _, _, _ = core.propagate_interval(INT_RK45, 0.2 / AU2FS, 0.0, model.tout * model.eps_int)
+        torch.cuda.synchronize()
+        e0 = core.counters()["eom"]
+        core.event_record(0)
+        t1, h1, nsteps, natt, _ = core.propagate_interval(INT_RK45, t + args.rk_fs / AU2FS, t, h)
+        core.event_record(1)
+        torch.cuda.synchronize()
+        ms = core.event_elapsed(0, 1)
+        ob = core.observables(t1)
+        out[prec] = dict(fs_per_s=(t1 - t) * AU2FS / (ms * 1e-3), ms=ms, steps=nsteps, attempts=natt,
+                         eom_per_s=(core.counters()["eom"] - e0) / (ms * 1e-3), auto=ob["auto"], pop=ob["pop"])
+        core.close()
+    line = {"metric": f"simulated fs/s ({args.workload}, RK45)", "value": out[args.precision]["fs_per_s"],
+            "unit": "fs/s", "n_gpus": 1, "precision": args.precision,
+            "fp64_fs_per_s": out[0]["fs_per_s"], "eom_per_s": out[args.precision]["eom_per_s"],
+            "steps": out[args.precision]["steps"], "attempts": out[args.precision]["attempts"],
+            "ms": out[args.precision]["ms"],
+            "config": {"workload": args.workload, "interval_fs": args.rk_fs, "from_fs": 0.2,
+                       "coefficients": int(model.naconftot), "dimpsi": int(model.dimpsi),
+                       "eps_int": model.eps_int}}
+    if args.precision != 0:
+        line["accuracy_vs_fp64_path"] = {
+            "dC": abs(out[args.precision]["auto"] - out[0]["auto"]),
+            "dpop": float(np.abs(out[args.precision]["pop"] - out[0]["pop"]).max())}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -481,8 +525,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
-    ap.add_argument("--workload", default="qvc12", choices=["qvc12", "ensemble"],
-                    help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement")
+    ap.add_argument("--workload", default="qvc12", choices=["qvc12", "ensemble", "lvc5", "gmctdh16"],
+                    help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement; "
+                         "lvc5 / gmctdh16: RK configurations")
+    ap.add_argument("--rk-fs", type=float, default=0.5)
     ap.add_argument("--members", type=int, default=128)
     ap.add_argument("--max-conf", type=int, default=1 << 14)
     ap.add_argument("--ens-fs", type=float, default=0.5)
@@ -494,6 +540,8 @@ def main():
         return run_profile_case(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload in ("lvc5", "gmctdh16"):
+        return run_rk_workload(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
