@@ -60,6 +60,7 @@ typedef struct mctdh_setup {
   double der_factor_re, der_factor_im;  /* -i for propagation, -1 for relaxation */
   int64_t int_type_psi;                 /* 1 = Cash-Karp for the CMF2 SPF sweeps  */
   int64_t precision;                    /* 0 = FP64, 1 = split-FP32 contractions  */
+  int64_t int_order, int_par1;          /* Adams PECE order and extra EC iterations (abm<order><par1>) */
 } mctdh_setup_t;
 
 /* Build the device context: uploads the operators, plans the batched kernels
@@ -67,6 +68,11 @@ typedef struct mctdh_setup {
  * init_calc.f90:1-226 (alloc_h1mode, alloc_MeanField, alloc_rho, alloc_AVec). */
 int64_t mctdh_create(const mctdh_setup_t *setup, mctdh_ctx_t **ctx);
 int64_t mctdh_destroy(mctdh_ctx_t *ctx);
+
+/* Integrator codes of mctdh_step / mctdh_propagate: 1 Cash-Karp RK, 2 Dormand-Prince
+ * RK, 3 Adams PECE of order int_order with int_par1 extra EC iterations (the first
+ * int_order steps of a propagation with Cash-Karp, propagator.f90:156-181;
+ * integrator.f90:244-380), 10 CMF2. */
 
 /* Equation of motion (A, psi, t) -> (dA, dpsi) on host buffers.
  * Replaces Calc_Derivs(A0, psi0, dA, dpsi, tt) -- derivatives.f90:39. */

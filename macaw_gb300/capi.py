@@ -47,6 +47,7 @@ class Setup(C.Structure):
         ("eps_A", C.c_double), ("eps_psi", C.c_double), ("min_stepsize", C.c_double),
         ("writetime", C.c_double), ("der_factor_re", C.c_double), ("der_factor_im", C.c_double),
         ("int_type_psi", C.c_int64), ("precision", C.c_int64),
+        ("int_order", C.c_int64), ("int_par1", C.c_int64),
     ]
 
 
@@ -252,6 +253,8 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
     s.der_factor_re, s.der_factor_im = model.der_factor.real, model.der_factor.imag
     s.int_type_psi = model.int_type_psi
     s.precision = precision
+    s.int_order = getattr(model, "int_order", 4)
+    s.int_par1 = getattr(model, "int_par1", 0)
     return s, keep
 
 

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <map>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -253,9 +254,10 @@ struct Ctx {
   // buffer) -> (executable graph, kernel launches it holds)
   struct GraphRec {
     cudaGraphExec_t exec;
-    long long launches, eoms;   // what one replay accounts for
+    long long launches, eoms, hbs;   // what one replay accounts for
   };
   std::map<std::pair<int, const void*>, GraphRec> graphs;
+  std::set<std::pair<int, const void*>> graph_seen;   // run once directly before capture
   bool graphs_off = false;
   KProf prof[KP_N];
   std::vector<PendingEv> pending;
@@ -263,6 +265,15 @@ struct Ctx {
   cudaEvent_t user_ev[16] = {};
   std::map<std::pair<const void*, const void*>, DotPlan*> dots;
   bool fsal_valid = false;   // Dormand-Prince derivative carried between steps
+  // Adams PECE (integrator.f90:227-380)
+  int int_order = 4, int_par1 = 0;
+  bool ad_planned = false, ad_valid = false;
+  int ad_iprop = 0;                  // bootstrap steps done (propagator.f90:156-181)
+  std::vector<cplx*> ad_hist;        // dA_prev(:, 1..order): derivatives at x_(n-1), x_(n-2), ...
+  std::vector<double> ad_hprev;      // h_prev(1..order)
+  cplx *ad_dcur = nullptr, *ad_temp = nullptr, *ad_new = nullptr, *ad_new1 = nullptr, *ad_dnew = nullptr,
+       *ad_d1 = nullptr;
+  OvlPlan ad_plan;                   // DeltaPsi(ANew, ANew1)
   // model
   int nstates = 0, nmodes = 0, ndof = 0, nham = 0, maxdof = 0, nopermax = 0;
   std::vector<int> nspf;  // [m + nmodes*s]
@@ -297,7 +308,9 @@ struct Ctx {
   cplx* d_tmp = nullptr;
   cplx* d_err = nullptr;
   cplx* d_hb = nullptr;     // H*B output
-  double* d_scal = nullptr; // small scalars
+  double* d_scal = nullptr; // small scalars: [0] the RK step of the current attempt
+  double* h_scal = nullptr; // pinned host staging for d_scal
+  long long* d_off1 = nullptr;   // {0, ntot}: the whole vector as one segment
 
   // DVR operator matrices on device: (dof, code) -> pointer
   std::map<std::pair<int, int>, cplx*> dofmat;
@@ -386,6 +399,10 @@ struct Ctx {
   std::vector<ProdBatch> gwp_sinv;                    // S^-1 products, one batch per Gaussian mode
   std::vector<ProdBatch> gwp_tau;                     // -tau x_m A, one batch per Gaussian mode
 
+  ~Ctx() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+    if (h_scal) cudaFreeHost(h_scal);
+  }
   int m_of(int m, int s) const { return nspf[m + nmodes * s]; }
   std::vector<int> shape_of(int s) const {
     std::vector<int> v(nmodes);
@@ -491,6 +508,8 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.writetime = s->writetime;
   c.der = mkc(s->der_factor_re, s->der_factor_im);
   c.int_type_psi = (int)s->int_type_psi;
+  c.int_order = (int)s->int_order;
+  c.int_par1 = (int)s->int_par1;
   c.precision = (int)s->precision;
   if (c.precision < 0 || c.precision > 2) throw StatusError(MCTDH_EARG, "precision must be 0, 1 or 2");
   if (!c.modes_gwp.empty()) {
@@ -1284,7 +1303,13 @@ void run_graphed(Ctx& c, int kind, const void* key, F&& body) {
   auto k = std::make_pair(kind, key);
   auto it = c.graphs.find(k);
   if (it == c.graphs.end()) {
-    const long long l0 = c.launches, e0 = c.eom_count;
+    if (!c.graph_seen.count(k)) {
+      // first use runs directly: lazily built plans allocate then, never under capture
+      c.graph_seen.insert(k);
+      body();
+      return;
+    }
+    const long long l0 = c.launches, e0 = c.eom_count, h0 = c.hb_count;
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       cudaGetLastError();
@@ -1303,20 +1328,22 @@ void run_graphed(Ctx& c, int kind, const void* key, F&& body) {
     if (ok && e == cudaSuccess && g) ok = (cudaGraphInstantiate(&ge, g, 0) == cudaSuccess);
     else ok = false;
     if (g) cudaGraphDestroy(g);
-    const long long nl = c.launches - l0, ne = c.eom_count - e0;
+    const long long nl = c.launches - l0, ne = c.eom_count - e0, nh = c.hb_count - h0;
     c.launches = l0;
     c.eom_count = e0;
+    c.hb_count = h0;
     if (!ok) {
       cudaGetLastError();
       c.graphs_off = true;
       body();
       return;
     }
-    it = c.graphs.emplace(k, Ctx::GraphRec{ge, nl, ne}).first;
+    it = c.graphs.emplace(k, Ctx::GraphRec{ge, nl, ne, nh}).first;
   }
   CK(cudaGraphLaunch(it->second.exec, c.st));
   c.launches += it->second.launches;
   c.eom_count += it->second.eoms;
+  c.hb_count += it->second.hbs;
 }
 
 void run_prod(Ctx& c, const ProdBatch& b) {
@@ -1459,7 +1486,9 @@ const double DP_D[7] = {5179.0 / 57600.0, 0.0, 7571.0 / 16695.0, 393.0 / 640.0, 
                         187.0 / 2100.0, 0.025};
 const double RK_SAFETY = 0.9, RK_PGROW = -0.2, RK_PSHRNK = -0.25, RK_MINSCAL = 0.1, RK_MAXSCAL = 5.0;
 
-void stage(Ctx& c, cplx* out, const cplx* base, const double* coef, int nk, int kofs, double dt) {
+// RK stage combination out = base + dt * sum_j coef_j k_j, with dt read from the
+// device (c.d_scal[0]) so that a whole attempt can replay as one CUDA graph.
+void stage(Ctx& c, cplx* out, const cplx* base, const double* coef, int nk, int kofs) {
   StageArgs a;
   memset(&a, 0, sizeof(a));
   int n = 0;
@@ -1470,27 +1499,33 @@ void stage(Ctx& c, cplx* out, const cplx* base, const double* coef, int nk, int 
     ++n;
   }
   a.nk = n;
-  launch_stage(out, base, a, dt, c.ntot, c.st);
+  launch_ens_stage(out, base, a, c.d_scal, c.d_off1, 1, c.ntot, c.st);
   c.count();
 }
 
 // One rkck/rkdp attempt from d_y with k1 in d_k[0]; leaves the 5th-order state in
 // d_tmp, the embedded state in d_err; returns errmax / eps (DeltaPsi).
 double rk_attempt(Ctx& c, double t, double dt, int method) {
+  (void)t;
   const bool dp = (method == 2);
-  for (int st = 1; st < 6; ++st) {
-    stage(c, c.d_in, c.d_y, dp ? DP_B[st] : CK_B[st], st, 0, dt);
-    eom(c, c.d_k[st]);
-  }
-  stage(c, c.d_tmp, c.d_y, dp ? DP_C : CK_C, 6, 0, dt);
-  if (dp) {
-    CK(cudaMemcpyAsync(c.d_in, c.d_tmp, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
-    eom(c, c.d_k[6]);
-    stage(c, c.d_err, c.d_y, DP_D, 7, 0, dt);
-  } else {
-    stage(c, c.d_err, c.d_y, CK_D, 6, 0, dt);
-  }
-  run_ovl(c, c.dpsi_plan);
+  c.h_scal[0] = dt;
+  CK(cudaMemcpyAsync(c.d_scal, c.h_scal, sizeof(double), cudaMemcpyHostToDevice, c.st));
+  // the attempt is the same launch sequence every time: one CUDA graph per method
+  run_graphed(c, 10 + method, nullptr, [&] {
+    for (int st = 1; st < 6; ++st) {
+      stage(c, c.d_in, c.d_y, dp ? DP_B[st] : CK_B[st], st, 0);
+      eom(c, c.d_k[st]);
+    }
+    stage(c, c.d_tmp, c.d_y, dp ? DP_C : CK_C, 6, 0);
+    if (dp) {
+      CK(cudaMemcpyAsync(c.d_in, c.d_tmp, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+      eom(c, c.d_k[6]);
+      stage(c, c.d_err, c.d_y, DP_D, 7, 0);
+    } else {
+      stage(c, c.d_err, c.d_y, CK_D, 6, 0);
+    }
+    run_ovl(c, c.dpsi_plan);
+  });
   cplx o[3];
   read_ovl(c, c.dpsi_plan, o);
   check_status(c);
@@ -1519,6 +1554,187 @@ void rkqs(Ctx& c, double t, double htry, double* hdid, double* hnext, int method
   CK(cudaMemcpyAsync(c.d_y, c.d_tmp, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
   if (method == 2)
     CK(cudaMemcpyAsync(c.d_k[0], c.d_k[6], sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+}
+
+// ---------------------------------------------------------------------------
+// Adams PECE with variable step size (Adams, integrator.f90:244-380), on the
+// resident state; the derivative at the current point is kept in ad_dcur.
+// ---------------------------------------------------------------------------
+void adams_plan(Ctx& c) {
+  if (c.ad_planned) return;
+  const int k = c.int_order;
+  if (k < 1 || k > 6) throw StatusError(MCTDH_EUNSUPPORTED, "Adams order must be 1..6");
+  for (int i = 0; i < k; ++i) c.ad_hist.push_back(c.ar.calloc_c(c.ntot));
+  c.ad_hprev.assign(k, 0.0);
+  c.ad_dcur = c.ar.calloc_c(c.ntot);
+  c.ad_temp = c.ar.calloc_c(c.ntot);
+  c.ad_new = c.ar.calloc_c(c.ntot);
+  c.ad_new1 = c.ar.calloc_c(c.ntot);
+  c.ad_dnew = c.ar.calloc_c(c.ntot);
+  c.ad_d1 = c.ar.calloc_c(c.ntot);
+  plan_ovl(c, c.ad_plan, c.ad_new, c.ad_new1, c.precision ? 2 : 0);
+  c.ad_planned = true;
+}
+
+// Solve the n x n system M x = b (column-major, leading dimension ld) by Gaussian
+// elimination with partial pivoting (the work of dgesv).
+void small_solve(std::vector<double> M, int n, int ld, std::vector<double>& b) {
+  for (int col = 0; col < n; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < n; ++r)
+      if (fabs(M[r + ld * col]) > fabs(M[piv + ld * col])) piv = r;
+    if (M[piv + ld * col] == 0.0) throw StatusError(MCTDH_ESTEP, "singular Adams system");
+    if (piv != col) {
+      for (int j = 0; j < n; ++j) std::swap(M[col + ld * j], M[piv + ld * j]);
+      std::swap(b[col], b[piv]);
+    }
+    for (int r = col + 1; r < n; ++r) {
+      const double f = M[r + ld * col] / M[col + ld * col];
+      for (int j = col; j < n; ++j) M[r + ld * j] -= f * M[col + ld * j];
+      b[r] -= f * b[col];
+    }
+  }
+  for (int r = n - 1; r >= 0; --r) {
+    double v = b[r];
+    for (int j = r + 1; j < n; ++j) v -= M[r + ld * j] * b[j];
+    b[r] = v / M[r + ld * r];
+  }
+}
+
+// out = base + w[0] dcur + sum_{i=1..nprev} w[i] hist[i-1]
+void adams_combine(Ctx& c, cplx* out, const double* w, int nprev) {
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  a.k[0] = c.ad_dcur;
+  a.c[0] = w[0];
+  for (int i = 1; i <= nprev; ++i) {
+    a.k[i] = c.ad_hist[i - 1];
+    a.c[i] = w[i];
+  }
+  a.nk = nprev + 1;
+  launch_stage(out, c.d_y, a, 1.0, c.ntot, c.st);
+  c.count();
+}
+// out = base + w * d
+void adams_axpy(Ctx& c, cplx* out, const cplx* base, const cplx* d, double w) {
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  a.k[0] = d;
+  a.c[0] = w;
+  a.nk = 1;
+  launch_stage(out, base, a, 1.0, c.ntot, c.st);
+  c.count();
+}
+
+void adams_step(Ctx& c, double t, double htry, double* hdid, double* hnext, long long* attempts) {
+  const int k = c.int_order;
+  const double minscal = 0.3, maxscal = 4.0, safety = 0.95;
+  const double pow_shrink = -1.0 / (double)(k + 1);
+  const int ld = k + 2;
+  // M(j, i) = (x_(n-i) - x_n)^j for the columns i >= 1 (:259-268); column -1 per step size
+  std::vector<double> M((size_t)ld * ld, 0.0);   // column index i + 1 for i = -1..k
+  for (int i = 0; i < ld; ++i) M[0 + ld * i] = 1.0;
+  double hsum = 0.0;
+  for (int i = 1; i <= k; ++i) {
+    hsum -= c.ad_hprev[i - 1];
+    double d = hsum;
+    for (int j = 1; j <= k + 1; ++j) {
+      M[j + ld * (i + 1)] = d;
+      d *= hsum;
+    }
+  }
+  double dt = htry, errmax = 0.0;
+  while (true) {
+    ++*attempts;
+    std::vector<double> B(ld);
+    B[0] = dt;
+    double d = dt;
+    for (int j = 1; j <= k + 1; ++j) {
+      M[j + ld * 0] = d;
+      d *= dt;
+      B[j] = d / (double)(j + 1);
+    }
+    // predictor (order k): columns 0..k-1
+    std::vector<double> P((size_t)ld * ld, 0.0), xp(B.begin(), B.begin() + k);
+    for (int j = 0; j < k; ++j)
+      for (int i = 0; i < k; ++i) P[j + ld * i] = M[j + ld * (i + 1)];
+    small_solve(P, k, ld, xp);
+    // correctors: order k+1 (columns -1..k-1) and order k+2 (columns -1..k)
+    std::vector<double> x1(B.begin(), B.begin() + k + 1), x2(B.begin(), B.begin() + k + 2);
+    std::vector<double> C1((size_t)ld * ld, 0.0), C2((size_t)ld * ld, 0.0);
+    for (int j = 0; j < k + 1; ++j)
+      for (int i = 0; i < k + 1; ++i) C1[j + ld * i] = M[j + ld * i];
+    for (int j = 0; j < k + 2; ++j)
+      for (int i = 0; i < k + 2; ++i) C2[j + ld * i] = M[j + ld * i];
+    small_solve(C1, k + 1, ld, x1);
+    small_solve(C2, k + 2, ld, x2);
+    // P: Atemp = y + XX(0) dy + sum XX(i) dy_(n-i); E: derivative at t + dt
+    adams_combine(c, c.ad_temp, xp.data(), k - 1);
+    eom_from(c, c.ad_temp, c.ad_dnew);
+    // C (order k+1) with int_par1 further EC iterations
+    adams_combine(c, c.ad_temp, x1.data() + 1, k - 1);
+    adams_axpy(c, c.ad_new, c.ad_temp, c.ad_dnew, x1[0]);
+    for (int it = 0; it < c.int_par1; ++it) {
+      eom_from(c, c.ad_new, c.ad_d1);
+      adams_axpy(c, c.ad_new, c.ad_temp, c.ad_d1, x1[0]);
+    }
+    // C (order k+2)
+    adams_combine(c, c.ad_temp, x2.data() + 1, k);
+    adams_axpy(c, c.ad_new1, c.ad_temp, c.ad_dnew, x2[0]);
+    for (int it = 0; it < c.int_par1; ++it) {
+      eom_from(c, c.ad_new1, c.ad_d1);
+      adams_axpy(c, c.ad_new1, c.ad_temp, c.ad_d1, x2[0]);
+    }
+    run_ovl(c, c.ad_plan);
+    cplx o[3];
+    read_ovl(c, c.ad_plan, o);
+    check_status(c);
+    errmax = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x)))) / c.eps_int;
+    if (!std::isfinite(errmax)) throw StatusError(MCTDH_ENONFINITE, "non-finite Adams error estimate");
+    if (errmax < 1.0) break;
+    dt = std::max(minscal * dt, safety * dt * pow(errmax, pow_shrink));
+    if (dt < c.min_stepsize) throw StatusError(MCTDH_ESTEP, "The stepsize has become too small");
+  }
+  // errmax ** pow_shrink is +Infinity for errmax = 0 (IEEE), leaving maxscal * dt
+  const double grow = (errmax > 0.0) ? pow(errmax, pow_shrink) : INFINITY;
+  *hnext = std::min(std::min(maxscal * dt, dt * grow), c.writetime);
+  *hdid = dt;
+  // shift the history: dA_prev(:,1) = derivative at the old point (:366-373)
+  cplx* oldest = c.ad_hist[k - 1];
+  for (int i = k - 1; i > 0; --i) {
+    c.ad_hist[i] = c.ad_hist[i - 1];
+    c.ad_hprev[i] = c.ad_hprev[i - 1];
+  }
+  c.ad_hist[0] = c.ad_dcur;
+  c.ad_hprev[0] = dt;
+  c.ad_dcur = oldest;
+  CK(cudaMemcpyAsync(c.d_y, c.ad_new1, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+  eom_from(c, c.d_y, c.ad_dcur);   // Calc_Derivs at tt + hdid
+}
+
+// One step of the Adams propagation on the resident state, bootstrapping with
+// Cash-Karp for the first int_order steps (propagator.f90:156-198).  Returns
+// whether the step was a bootstrap step.
+bool adams_or_boot_step(Ctx& c, double t, double htry, double* hdid, double* hnext, long long* att) {
+  adams_plan(c);
+  const int k = c.int_order;
+  if (!c.ad_valid) {
+    eom_from(c, c.d_y, c.ad_dcur);   // propagator.f90:151
+    c.ad_iprop = 0;
+    c.ad_valid = true;
+  }
+  if (c.ad_iprop < k) {
+    CK(cudaMemcpyAsync(c.ad_hist[k - 1 - c.ad_iprop], c.ad_dcur, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice,
+                       c.st));
+    CK(cudaMemcpyAsync(c.d_k[0], c.ad_dcur, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+    rkqs(c, t, htry, hdid, hnext, 1, att);
+    eom_from(c, c.d_y, c.ad_dcur);
+    c.ad_hprev[k - 1 - c.ad_iprop] = *hdid;
+    c.ad_iprop++;
+    return true;
+  }
+  adams_step(c, t, htry, hdid, hnext, att);
+  return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -1572,13 +1788,16 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
     // comes back for the stopping rule: one host synchronisation per Krylov vector
     double* d_alpha = c.d_lan;
     double* d_beta = c.d_lan + NKRYLOV_MAX;
-    launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st);
-    c.count();
+    // each Krylov step is a fixed launch sequence on fixed buffers: CUDA graphs
+    run_graphed(c, 4, B0, [&] {
+      launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st);
+      c.count();
+      hb(c, K, K + n);
+      launch_lan_axpy(K + n, K, nullptr, dot_dev(c, K, K + n, n), nullptr, d_alpha, n, c.st);
+      launch_lan_normalize(K + n, K + n, dot_dev(c, K + n, K + n, n), d_beta, n, c.st);
+      c.count(2);
+    });
     double beta[NKRYLOV_MAX] = {0};
-    hb(c, K, K + n);
-    launch_lan_axpy(K + n, K, nullptr, dot_dev(c, K, K + n, n), nullptr, d_alpha, n, c.st);
-    launch_lan_normalize(K + n, K + n, dot_dev(c, K + n, K + n, n), d_beta, n, c.st);
-    c.count(2);
     CK(cudaMemcpyAsync(&beta[0], d_beta, sizeof(double), cudaMemcpyDeviceToHost, c.st));
     CK(cudaStreamSynchronize(c.st));
     double error = beta[0] * fabs(dt);
@@ -1588,10 +1807,12 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
       cplx* Kj = K + (long long)(j - 1) * n;
       cplx* Kn = K + (long long)j * n;
       cplx* Kp = K + (long long)(j - 2) * n;
-      hb(c, Kj, Kn);
-      launch_lan_axpy(Kn, Kj, Kp, dot_dev(c, Kj, Kn, n), d_beta + (j - 2), d_alpha + (j - 1), n, c.st);
-      launch_lan_normalize(Kn, Kn, dot_dev(c, Kn, Kn, n), d_beta + (j - 1), n, c.st);
-      c.count(2);
+      run_graphed(c, 3, Kn, [&] {
+        hb(c, Kj, Kn);
+        launch_lan_axpy(Kn, Kj, Kp, dot_dev(c, Kj, Kn, n), d_beta + (j - 2), d_alpha + (j - 1), n, c.st);
+        launch_lan_normalize(Kn, Kn, dot_dev(c, Kn, Kn, n), d_beta + (j - 1), n, c.st);
+        c.count(2);
+      });
       CK(cudaMemcpyAsync(&beta[j - 1], d_beta + (j - 1), sizeof(double), cudaMemcpyDeviceToHost, c.st));
       CK(cudaStreamSynchronize(c.st));
       error = error * beta[j - 1] / (double)j * fabs(dt);
@@ -2179,6 +2400,12 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       c->d_err = c->ar.calloc_c(c->ntot);
     }
     c->d_scal = (double*)c->ar.alloc(4096);
+    CK(cudaMallocHost(&c->h_scal, 4096));
+    {
+      const long long offs[2] = {0, c->ntot};
+      c->d_off1 = (long long*)c->ar.alloc(sizeof(offs));
+      CK(cudaMemcpy(c->d_off1, offs, sizeof(offs), cudaMemcpyHostToDevice));
+    }
     plan_eom(*c);
     if (!mb) {
       // CMF2 / Lanczos buffers (ensemble members integrate with RK only)
@@ -2709,7 +2936,6 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
     g_mfx.erase(mi);
   }
   for (auto& kv : c->dots) delete kv.second;
-  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
   drain_profile(*c);
   for (auto e : c->evpool) cudaEventDestroy(e);
   for (auto e : c->user_ev) if (e) cudaEventDestroy(e);
@@ -2745,6 +2971,7 @@ int64_t mctdh_set_state(mctdh_ctx_t* ctx, const double* A, const double* psi, in
   return guarded(c, [&] {
     upload(*c, c->d_y, A, psi);
     c->fsal_valid = false;
+    c->ad_valid = false;
     c->ops_fresh = false;
     auto mi = g_mfx.find(c);
     if (mi != g_mfx.end()) mi->second->nhist = 0;
@@ -2822,6 +3049,20 @@ int64_t mctdh_propagate(mctdh_ctx_t* ctx, int64_t int_type, double tnext, double
     double time = *t, stepsize = *step;
     while (true) {
       double sdone, snext;
+      if (int_type == 3) {
+        const bool boot = adams_or_boot_step(*c, time, stepsize, &sdone, &snext, &att);
+        ++steps;
+        time += sdone;
+        if (boot) {
+          if (time >= tnext - c->min_stepsize) break;
+          long long q = (long long)((tnext - time) / snext);
+          stepsize = (q == 0) ? (tnext - time) : (tnext - time) / (double)(q + 1);
+        } else {
+          if (time >= tnext) break;   // propagator.f90:191-193
+          stepsize = std::min((tnext - time) / (double)((long long)((tnext - time) / snext) + 1), tnext - time);
+        }
+        continue;
+      }
       if (int_type == 10) {
         cmf2(*c, time, stepsize, &sdone, &snext, &att);
       } else if (int_type == 1 || int_type == 2) {
@@ -2857,7 +3098,9 @@ int64_t mctdh_step(mctdh_ctx_t* ctx, int64_t int_type, double t, double htry, do
   Ctx* c = ctx->c;
   return guarded(c, [&] {
     long long att = 0;
-    if (int_type == 10) {
+    if (int_type == 3) {
+      adams_or_boot_step(*c, t, htry, hdid, hnext, &att);
+    } else if (int_type == 10) {
       cmf2(*c, t, htry, hdid, hnext, &att);
     } else if (int_type == 1 || int_type == 2) {
       if (int_type == 1 || !c->fsal_valid) eom_from(*c, c->d_y, c->d_k[0]);

@@ -39,6 +39,7 @@ OP_SINM2 = -4    # sin^-2 (Legendre DVR only)
 
 INT_RK45 = 1     # Cash-Karp (input.f90:280-282)
 INT_DOPRI = 2    # Dormand-Prince (input.f90:283-285)
+INT_ABM = 3      # Adams PECE, 'abm<order><par1>' (input.f90:286-292)
 INT_CMF2 = 10    # constant mean field (input.f90:295-331)
 
 
@@ -179,6 +180,8 @@ class Model:
     eps_psi: float = 1e-8
     min_stepsize: float = 1e-9 / AU2FS
     int_type: int = INT_RK45
+    int_order: int = 4                      # Adams PECE order (input.f90:75, 299)
+    int_par1: int = 0                       # extra EC iterations of Adams (input.f90:300-304)
     int_type_A: int = 5                     # Lanczos
     int_type_psi: int = 1                   # rk45 (Cash-Karp) for the SPFs
     relaxation: bool = False
@@ -671,6 +674,10 @@ def parse_input(path: str) -> Model:
         model.int_type = INT_RK45
     elif integ == "dopri":
         model.int_type = INT_DOPRI
+    elif integ.startswith("abm"):
+        model.int_type = INT_ABM
+        model.int_order = int(integ[3:5])
+        model.int_par1 = int(integ[5:]) if integ[5:].strip() else 0
     elif integ.startswith("cmf2"):
         model.int_type = INT_CMF2
         a_name, a_eps = cmf_lines[0].split()[:2]

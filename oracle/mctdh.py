@@ -42,7 +42,7 @@ from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
-from macaw_gb300.model import Model, AU2FS, INT_RK45, INT_DOPRI, INT_CMF2
+from macaw_gb300.model import Model, AU2FS, INT_RK45, INT_DOPRI, INT_ABM, INT_CMF2
 
 _EPS = np.finfo(np.float64).eps
 
@@ -715,6 +715,78 @@ class Oracle:
             dA, dpsi = a7, p7
         return At, pt, dA, dpsi, dt, hnext, attempts
 
+    # ---------------- Adams PECE ----------------
+    @staticmethod
+    def adams_weights(h_prev, dt, k):
+        """Weights of Adams (integrator.f90:259-341): the predictor XX(0:k-1) and the
+        correctors of order k+1 (XX(-1:k-1)) and k+2 (XX(-1:k)) from the matrix
+        M(j,i) = (x_(n-i) - x_n)^j (column -1: dt^j) and B(j) = dt^(j+1)/(j+1)."""
+        M = np.zeros((k + 2, k + 2))   # rows j = 0..k+1, columns i = -1..k (index i + 1)
+        M[0, :] = 1.0
+        hsum = 0.0
+        for i in range(1, k + 1):
+            hsum -= h_prev[i - 1]
+            d = hsum
+            for j in range(1, k + 2):
+                M[j, i + 1] = d
+                d *= hsum
+        B = np.zeros(k + 2)
+        B[0] = dt
+        d = dt
+        for j in range(1, k + 2):
+            M[j, 0] = d
+            d *= dt
+            B[j] = d / (j + 1)
+        pred = np.linalg.solve(M[0:k, 1:k + 1], B[0:k])           # XX(0..k-1)
+        corr1 = np.linalg.solve(M[0:k + 1, 0:k + 1], B[0:k + 1])  # XX(-1..k-1)
+        corr2 = np.linalg.solve(M[0:k + 2, 0:k + 2], B[0:k + 2])  # XX(-1..k)
+        return pred, corr1, corr2
+
+    def adams(self, A, psi, dA, dpsi, hist, h_prev, t, htry):
+        """Adams (integrator.f90:244-380).  hist[i] = (dA, dpsi) at x_(n-1-i); h_prev[i] =
+        x_(n-i) - x_(n-1-i).  Returns (A, psi, dA, dpsi, hist, h_prev, hdid, hnext)."""
+        md = self.m
+        k = md.int_order
+        minscal, maxscal, safety = 0.3, 4.0, 0.95
+        pow_shrink = -1.0 / (k + 1)
+        dt = htry
+        while True:
+            pred, c1, c2 = self.adams_weights(h_prev, dt, k)
+
+            def combine(w, nprev):
+                At = A + w[0] * dA
+                pt = psi + w[0] * dpsi
+                for i in range(1, nprev + 1):
+                    At = At + w[i] * hist[i - 1][0]
+                    pt = pt + w[i] * hist[i - 1][1]
+                return At, pt
+            At, pt = combine(pred, k - 1)
+            dAn, dpn = self.calc_derivs(At, pt, t + dt)
+            At, pt = combine(c1[1:], k - 1)
+            An, pn = dAn * c1[0] + At, dpn * c1[0] + pt
+            for _ in range(md.int_par1):
+                dA1, dp1 = self.calc_derivs(An, pn, t + dt)
+                An, pn = dA1 * c1[0] + At, dp1 * c1[0] + pt
+            At, pt = combine(c2[1:], k)
+            An1, pn1 = dAn * c2[0] + At, dpn * c2[0] + pt
+            for _ in range(md.int_par1):
+                dA1, dp1 = self.calc_derivs(An1, pn1, t + dt)
+                An1, pn1 = dA1 * c2[0] + At, dp1 * c2[0] + pt
+            errmax = self.delta_psi(An, pn, An1, pn1) / md.eps_int
+            if errmax < 1.0:
+                break
+            dt = max(minscal * dt, safety * dt * errmax ** pow_shrink)
+            if dt < md.min_stepsize:
+                raise OracleError("Adams step size too small")
+        # errmax ** pow_shrink is +Infinity for errmax = 0 in the reference's IEEE arithmetic
+        grow = errmax ** pow_shrink if errmax > 0.0 else math.inf
+        hnext = min(maxscal * dt, dt * grow)
+        hnext = min(hnext, md.tout)
+        hist = [(dA, dpsi)] + hist[:-1]
+        h_prev = [dt] + h_prev[:-1]
+        dA2, dpsi2 = self.calc_derivs(An1, pn1, t + dt)
+        return An1, pn1, dA2, dpsi2, hist, h_prev, dt, hnext
+
     # ---------------- CMF2 ----------------
     def calc_dhd_b(self, B: np.ndarray) -> np.ndarray:
         """Calc_DHD_B (cmf2_derivatives.f90:1-80): H_B * B (no der_factor)."""
@@ -967,6 +1039,8 @@ class Oracle:
         outputs = []
         steps = []
         nsteps = 0
+        if md.int_type == INT_ABM:
+            return self._propagate_adams(A, psi, A0, psi0, t, step, maxtime, record_steps)
         while t < maxtime:
             outputs.append(self.observables(A, psi, A0, psi0, t))
             tnext = t + md.tout
@@ -985,8 +1059,47 @@ class Oracle:
                 nsteps += 1
                 if max_steps is not None and nsteps >= max_steps:
                     return outputs, steps, (A, psi, t)
+
                 if t >= tnext - md.min_stepsize:
                     break
                 q = int((tnext - t) / snext)
                 step = (tnext - t) if q == 0 else (tnext - t) / (q + 1)
+        return outputs, steps, (A, psi, t)
+
+    def _propagate_adams(self, A, psi, A0, psi0, t, step, maxtime, record_steps):
+        """propagate_wf with Adams (propagator.f90:150-198): the first int_order steps
+        with Cash-Karp rkqs, storing the derivatives and step lengths."""
+        md = self.m
+        k = md.int_order
+        hist = [None] * k
+        h_prev = [0.0] * k
+        dA, dpsi = self.calc_derivs(A, psi, t)
+        iprop = 0
+        outputs, steps = [], []
+        while t < maxtime:
+            outputs.append(self.observables(A, psi, A0, psi0, t))
+            tnext = t + md.tout
+            while True:
+                if iprop < k:
+                    hist[k - 1 - iprop] = (dA, dpsi)
+                    A, psi, _, _, sdone, snext, tries = self.rkqs(A, psi, dA, dpsi, t, step, INT_RK45)
+                    dA, dpsi = self.calc_derivs(A, psi, t)
+                    h_prev[k - 1 - iprop] = sdone
+                    iprop += 1
+                    if record_steps:
+                        steps.append((t, step, sdone, snext, tries))
+                    t = t + sdone
+                    if t >= tnext - md.min_stepsize:
+                        break
+                    q = int((tnext - t) / snext)
+                    step = (tnext - t) if q == 0 else (tnext - t) / (q + 1)
+                    continue
+                A, psi, dA, dpsi, hist, h_prev, sdone, snext = self.adams(A, psi, dA, dpsi, hist, h_prev, t, step)
+                if record_steps:
+                    steps.append((t, step, sdone, snext, 1))
+                t = t + sdone
+                if t >= tnext:
+                    break
+                step = (tnext - t) / (int((tnext - t) / snext) + 1)
+                step = min(step, tnext - t)
         return outputs, steps, (A, psi, t)

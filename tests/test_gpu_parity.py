@@ -226,3 +226,20 @@ def test_gpu_stays_usable_after_error(core_cls):
         gpu.rkqs(A, psi, A * 0, psi * 0, 0.0, 1.0, method=7)
     dA, _ = gpu.calc_derivs(A, psi)
     assert np.all(np.isfinite(dA))
+
+
+@pytest.mark.parametrize("order,par1", [(4, 0), (3, 1)])
+def test_adams_free_running(core_cls, order, par1):
+    """Adams PECE ('abm<order><par1>', integrator.f90:244-380) after the Cash-Karp
+    bootstrap of propagate_wf (propagator.f90:156-181), free running against the
+    oracle's restatement: the step control sees DeltaPsi's rounding noise, so the
+    bound is the integrator tolerance."""
+    from macaw_gb300.model import INT_ABM
+    model = small_lvc(tfinal_fs=1.0)
+    model.int_type = INT_ABM
+    model.int_order = order
+    model.int_par1 = par1
+    A, psi = initial_wavefunction(model)
+    ref, _, _ = Oracle(model).propagate(A, psi)
+    outs = core_cls(model).propagate(A, psi)
+    _compare(outs, ref, 10 * model.eps_int)
