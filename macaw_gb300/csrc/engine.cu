@@ -392,7 +392,8 @@ struct Ctx {
   GwpCYDesc* cy_d = nullptr;
   std::vector<GwpYOp> yop_h;
   GwpYOp* yop_d = nullptr;
-  int cy_maxG = 0, cy_maxn = 0;
+  int cy_maxG = 0, cy_maxn = 0, cy_maxops = 0;
+  cplx* cy_part = nullptr;                            // per-operator partial sums of Y
   std::vector<std::vector<cplx*>> tau;                // [i][s]
   cplx* d_adot = nullptr;                             // f * sum_t ae_t H_t A before the corrections
   cplx* d_dA = nullptr;                               // dA after S^-1 and tau
@@ -1044,6 +1045,7 @@ void plan_gwp_derivs(Ctx& c) {
         c.yop_h.push_back(op);
       }
       d.op_count = (int)c.yop_h.size() - d.op_first;
+      c.cy_maxops = std::max(c.cy_maxops, d.op_count);
       c.cy_maxG = std::max(c.cy_maxG, nG);
       c.cy_maxn = std::max(c.cy_maxn, n);
       if (nG > 512) throw StatusError(MCTDH_EUNSUPPORTED, "Gaussian parameter system above 512 unknowns");
@@ -1052,6 +1054,7 @@ void plan_gwp_derivs(Ctx& c) {
   }
   c.cy_d = upload_vec(c.ar, c.cy_h);
   c.yop_d = upload_vec(c.ar, c.yop_h);
+  c.cy_part = c.ar.calloc_c((long long)c.cy_h.size() * c.cy_maxG * std::max(c.cy_maxops, 1));
   // dA = S^-1 (f H A) - tau A on the Gaussian modes
   c.d_adot = c.ar.calloc_c(c.naconftot);
   c.d_dA = c.ar.calloc_c(c.naconftot);
@@ -1379,9 +1382,9 @@ void gwp_setup_run(Ctx& c) {
 void gwp_derivs_run(Ctx& c, cplx* out) {
   {
     ProfScope ps(c, KP_GWP);
-    launch_gwp_cy(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.cy_maxn, c.yop_d, c.st);
+    launch_gwp_cy(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.cy_maxn, c.cy_maxops, c.yop_d, c.cy_part, c.st);
     launch_gwp_solve(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.der, out, c.d_status, c.st);
-    c.count(5 + (c.cy_maxG + GWP_QR_PW - 1) / GWP_QR_PW);
+    c.count(6 + (c.cy_maxG + GWP_QR_PW - 1) / GWP_QR_PW);
   }
   for (auto& b : c.gwp_sinv) run_prod(c, b);
   for (auto& b : c.gwp_tau) run_prod(c, b);
@@ -1572,7 +1575,7 @@ void adams_plan(Ctx& c) {
   c.ad_new1 = c.ar.calloc_c(c.ntot);
   c.ad_dnew = c.ar.calloc_c(c.ntot);
   c.ad_d1 = c.ar.calloc_c(c.ntot);
-  plan_ovl(c, c.ad_plan, c.ad_new, c.ad_new1, c.precision ? 2 : 0);
+  plan_ovl(c, c.ad_plan, c.ad_new, c.ad_new1, (c.precision && c.eps_int >= 1e-5) ? 2 : 0);
   c.ad_planned = true;
 }
 
@@ -2416,7 +2419,9 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       c->d_coef = c->ar.calloc_c(NKRYLOV_MAX);
       plan_hb(*c);
     }
-    plan_ovl(*c, c->dpsi_plan, c->d_tmp, c->d_err, c->precision ? 2 : 0);
+    // the compensated products of DeltaPsi (~1e-13) resolve 1 - Re<1|2>/.. ~ eps_int^2 / 2
+    // only for loose tolerances; tight ones keep FP64
+    plan_ovl(*c, c->dpsi_plan, c->d_tmp, c->d_err, (c->precision && c->eps_int >= 1e-5) ? 2 : 0);
     plan_ovl(*c, c->auto_plan, c->d_y0, c->d_y, 0);
     plan_ovl(*c, c->io_plan, c->d_in, c->d_out, 0);
     CK(cudaDeviceSynchronize());

@@ -264,31 +264,52 @@ __global__ void gwp_c_kernel(const GwpCYDesc* __restrict__ descs) {
 
 // Y (gmctdh_objects.f90:1285-1326): per entry r = j1*nmd + k,
 // sum over operators and j2 of MF(j1,j2) (Ha0 - Sa0Sm1 h)(r, j2).
-__global__ void gwp_y_kernel(const GwpCYDesc* __restrict__ descs, const GwpYOp* __restrict__ ops) {
+// Stage 1: one thread per (j1, operator) sums over j2 for all k of that j1 (the
+// nmd one-dimensional integrals of a (j1, j2) pair are computed once and shared
+// by the k entries through prefix/suffix products) into part[(r, op)].
+// Stage 2: one thread per r adds its operators' partial sums in operator order.
+__global__ void gwp_y_part_kernel(const GwpCYDesc* __restrict__ descs, const GwpYOp* __restrict__ ops,
+                                  cplx* __restrict__ part, long long part_ld) {
+  const GwpCYDesc& d = descs[blockIdx.y];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n * d.op_count) return;
+  const int j1 = e % d.n, o = e / d.n;
+  const GwpYOp& op = ops[d.op_first + o];
+  const int nmd = d.nmd;
+  const double* a = d.a;
+  cplx acc[GWP_MAXDOF];
+  for (int k = 0; k < nmd; ++k) acc[k] = mkc(0.0, 0.0);
+  for (int j2 = 0; j2 < op.n2; ++j2) {
+    cplx g[GWP_MAXDOF], pre[GWP_MAXDOF + 1];
+    for (int q = 0; q < nmd; ++q)
+      g[q] = gau_int_1d(a[q + d.lda * j1], a[q + d.lda * j2], d.xi[q + d.nmd * j1], op.xi2[q + d.nmd * j2], op.ops[q]);
+    pre[0] = mkc(1.0, 0.0);
+    for (int q = 0; q < nmd; ++q) pre[q + 1] = cmul(pre[q], g[q]);
+    const cplx s12 = op.S12[j1 + d.n * j2];
+    const cplx mf = op.mf[j1 + d.n * j2];
+    for (int k = 0; k < nmd; ++k) {
+      // right = prod_{q > k} g[q], in order (as np.prod over gi[k+1:])
+      cplx right = mkc(1.0, 0.0);
+      for (int q = k + 1; q < nmd; ++q) right = cmul(right, g[q]);
+      const cplx g10 = gau10_int_1d(a[k + d.lda * j1], a[k + d.lda * j2], d.xi[k + d.nmd * j1],
+                                    op.xi2[k + d.nmd * j2], op.ops[k]);
+      const cplx ha0 = cmul(cmul(s12, cmul(pre[k], right)), g10);
+      const int r = j1 * nmd + k;
+      cplx sh = mkc(0.0, 0.0);
+      for (int j = 0; j < d.n; ++j) cfma(sh, d.Sa0Sm1[r + d.nG * j], op.h[j + d.n * j2]);
+      cfma(acc[k], mf, csub(ha0, sh));
+    }
+  }
+  for (int k = 0; k < nmd; ++k) part[(long long)blockIdx.y * part_ld + (long long)(j1 * nmd + k) + (long long)d.nG * o] = acc[k];
+}
+
+__global__ void gwp_y_sum_kernel(const GwpCYDesc* __restrict__ descs, const cplx* __restrict__ part,
+                                 long long part_ld) {
   const GwpCYDesc& d = descs[blockIdx.y];
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= d.nG) return;
-  const int j1 = r / d.nmd, k = r % d.nmd;
-  const double* a = d.a;
   cplx acc = mkc(0.0, 0.0);
-  for (int o = 0; o < d.op_count; ++o) {
-    const GwpYOp& op = ops[d.op_first + o];
-    for (int j2 = 0; j2 < op.n2; ++j2) {
-      cplx left = mkc(1.0, 0.0), right = mkc(1.0, 0.0);
-      for (int q = 0; q < d.nmd; ++q) {
-        if (q == k) continue;
-        const cplx g = gau_int_1d(a[q + d.lda * j1], a[q + d.lda * j2], d.xi[q + d.nmd * j1], op.xi2[q + d.nmd * j2],
-                                  op.ops[q]);
-        if (q < k) left = cmul(left, g); else right = cmul(right, g);
-      }
-      const cplx g10 = gau10_int_1d(a[k + d.lda * j1], a[k + d.lda * j2], d.xi[k + d.nmd * j1],
-                                    op.xi2[k + d.nmd * j2], op.ops[k]);
-      cplx ha0 = cmul(cmul(op.S12[j1 + d.n * j2], cmul(left, right)), g10);
-      cplx sh = mkc(0.0, 0.0);
-      for (int j = 0; j < d.n; ++j) cfma(sh, d.Sa0Sm1[r + d.nG * j], op.h[j + d.n * j2]);
-      cfma(acc, op.mf[j1 + d.n * j2], csub(ha0, sh));
-    }
-  }
+  for (int o = 0; o < d.op_count; ++o) acc = cadd(acc, part[(long long)blockIdx.y * part_ld + r + (long long)d.nG * o]);
   const long long ld = 2LL * d.nG;
   d.M[r + ld * d.nG] = acc;
   d.M[d.nG + r + ld * d.nG] = mkc(0.0, 0.0);
@@ -465,14 +486,17 @@ void launch_gwp_h1(const GwpH1Desc* d, int nd, cudaStream_t st) {
   gwp_h1_kernel<<<nd, 256, 0, st>>>(d);
 }
 
-void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, const GwpYOp* ops, cudaStream_t st) {
+void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, int maxops, const GwpYOp* ops, cplx* part,
+                   cudaStream_t st) {
   if (nd <= 0) return;
   const unsigned ne = (unsigned)((maxG * maxn + 255) / 256);
   gwp_sa0_kernel<<<dim3(ne, nd), 256, 0, st>>>(d);
   gwp_sa0sm1_kernel<<<dim3(ne, nd), 256, 0, st>>>(d);
   const unsigned nt = (unsigned)((maxG + 15) / 16);
   gwp_c_kernel<<<dim3(nt, nt, nd), dim3(16, 16), 0, st>>>(d);
-  gwp_y_kernel<<<dim3((maxG + 127) / 128, nd), 128, 0, st>>>(d, ops);
+  const long long part_ld = (long long)maxG * std::max(maxops, 1);
+  gwp_y_part_kernel<<<dim3((unsigned)((maxn * std::max(maxops, 1) + 63) / 64), nd), 64, 0, st>>>(d, ops, part, part_ld);
+  gwp_y_sum_kernel<<<dim3((maxG + 127) / 128, nd), 128, 0, st>>>(d, part, part_ld);
 }
 
 void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out, int* status, cudaStream_t st) {

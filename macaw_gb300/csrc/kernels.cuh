@@ -280,5 +280,7 @@ void launch_gwp_ovl(const GwpOvlDesc* d, int nd, cudaStream_t st);
 void launch_gwp_h1(const GwpH1Desc* d, int nd, cudaStream_t st);
 // Calc_CY and the Tikhonov parameter solve (StdRegSol 'tikh', maths.f90:87-162)
 // for nd (mode, state) blocks; maxG = max nG.  Then dxi = der * x and tau.
-void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, const GwpYOp* ops, cudaStream_t st);
+// part: scratch of nd * maxG * maxops complex (per-operator partial sums of Y)
+void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, int maxops, const GwpYOp* ops, cplx* part,
+                   cudaStream_t st);
 void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out, int* status, cudaStream_t st);
