@@ -1054,7 +1054,7 @@ void plan_gwp_derivs(Ctx& c) {
   }
   c.cy_d = upload_vec(c.ar, c.cy_h);
   c.yop_d = upload_vec(c.ar, c.yop_h);
-  c.cy_part = c.ar.calloc_c((long long)c.cy_h.size() * c.cy_maxG * std::max(c.cy_maxops, 1));
+  c.cy_part = c.ar.calloc_c((long long)c.cy_h.size() * c.cy_maxG * c.cy_maxn * std::max(c.cy_maxops, 1));
   // dA = S^-1 (f H A) - tau A on the Gaussian modes
   c.d_adot = c.ar.calloc_c(c.naconftot);
   c.d_dA = c.ar.calloc_c(c.naconftot);
@@ -1372,7 +1372,7 @@ void run_red(Ctx& c, const RedBatch& b) {
 void gwp_setup_run(Ctx& c) {
   ProfScope ps(c, KP_GWP);
   launch_gwp_ovl(c.gs_d, (int)c.gs_h.size(), c.st);
-  launch_reginv(c.gsreg_d, (int)c.gsreg_h.size(), c.mfop_d, c.d_status, c.st);
+  launch_tikh_inv(c.gsreg_d, (int)c.gsreg_h.size(), c.st);
   launch_gwp_h1(c.gh1_d, (int)c.gh1_h.size(), c.st);
   c.count(3);
 }

@@ -263,53 +263,55 @@ __global__ void gwp_c_kernel(const GwpCYDesc* __restrict__ descs) {
 }
 
 // Y (gmctdh_objects.f90:1285-1326): per entry r = j1*nmd + k,
-// sum over operators and j2 of MF(j1,j2) (Ha0 - Sa0Sm1 h)(r, j2).
-// Stage 1: one thread per (j1, operator) sums over j2 for all k of that j1 (the
-// nmd one-dimensional integrals of a (j1, j2) pair are computed once and shared
-// by the k entries through prefix/suffix products) into part[(r, op)].
-// Stage 2: one thread per r adds its operators' partial sums in operator order.
+// sum over operators (outer) and j2 (inner) of MF(j1,j2) (Ha0 - Sa0Sm1 h)(r, j2).
+// Stage 1: one thread per (j1, j2, operator) computes the nmd one-dimensional
+// integrals of the pair once, shares them between the k entries through
+// prefix/suffix products, and writes the nmd terms to part[((o*n2 + j2)*nG + r)].
+// Stage 2: one thread per r adds its terms in the reference's order.
 __global__ void gwp_y_part_kernel(const GwpCYDesc* __restrict__ descs, const GwpYOp* __restrict__ ops,
-                                  cplx* __restrict__ part, long long part_ld) {
+                                  cplx* __restrict__ part, long long part_ld, int maxn2) {
   const GwpCYDesc& d = descs[blockIdx.y];
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= d.n * d.op_count) return;
-  const int j1 = e % d.n, o = e / d.n;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)d.n * maxn2 * d.op_count) return;
+  const int j1 = (int)(e % d.n);
+  const int j2 = (int)((e / d.n) % maxn2);
+  const int o = (int)(e / ((long long)d.n * maxn2));
   const GwpYOp& op = ops[d.op_first + o];
+  if (j2 >= op.n2) return;
   const int nmd = d.nmd;
   const double* a = d.a;
-  cplx acc[GWP_MAXDOF];
-  for (int k = 0; k < nmd; ++k) acc[k] = mkc(0.0, 0.0);
-  for (int j2 = 0; j2 < op.n2; ++j2) {
-    cplx g[GWP_MAXDOF], pre[GWP_MAXDOF + 1];
-    for (int q = 0; q < nmd; ++q)
-      g[q] = gau_int_1d(a[q + d.lda * j1], a[q + d.lda * j2], d.xi[q + d.nmd * j1], op.xi2[q + d.nmd * j2], op.ops[q]);
-    pre[0] = mkc(1.0, 0.0);
-    for (int q = 0; q < nmd; ++q) pre[q + 1] = cmul(pre[q], g[q]);
-    const cplx s12 = op.S12[j1 + d.n * j2];
-    const cplx mf = op.mf[j1 + d.n * j2];
-    for (int k = 0; k < nmd; ++k) {
-      // right = prod_{q > k} g[q], in order (as np.prod over gi[k+1:])
-      cplx right = mkc(1.0, 0.0);
-      for (int q = k + 1; q < nmd; ++q) right = cmul(right, g[q]);
-      const cplx g10 = gau10_int_1d(a[k + d.lda * j1], a[k + d.lda * j2], d.xi[k + d.nmd * j1],
-                                    op.xi2[k + d.nmd * j2], op.ops[k]);
-      const cplx ha0 = cmul(cmul(s12, cmul(pre[k], right)), g10);
-      const int r = j1 * nmd + k;
-      cplx sh = mkc(0.0, 0.0);
-      for (int j = 0; j < d.n; ++j) cfma(sh, d.Sa0Sm1[r + d.nG * j], op.h[j + d.n * j2]);
-      cfma(acc[k], mf, csub(ha0, sh));
-    }
+  cplx g[GWP_MAXDOF], pre[GWP_MAXDOF + 1];
+  for (int q = 0; q < nmd; ++q)
+    g[q] = gau_int_1d(a[q + d.lda * j1], a[q + d.lda * j2], d.xi[q + d.nmd * j1], op.xi2[q + d.nmd * j2], op.ops[q]);
+  pre[0] = mkc(1.0, 0.0);
+  for (int q = 0; q < nmd; ++q) pre[q + 1] = cmul(pre[q], g[q]);
+  const cplx s12 = op.S12[j1 + d.n * j2];
+  const cplx mf = op.mf[j1 + d.n * j2];
+  cplx* out = part + (long long)blockIdx.y * part_ld + ((long long)o * maxn2 + j2) * d.nG;
+  for (int k = 0; k < nmd; ++k) {
+    cplx right = mkc(1.0, 0.0);   // prod_{q > k} g[q] in order (np.prod over gi[k+1:])
+    for (int q = k + 1; q < nmd; ++q) right = cmul(right, g[q]);
+    const cplx g10 = gau10_int_1d(a[k + d.lda * j1], a[k + d.lda * j2], d.xi[k + d.nmd * j1],
+                                  op.xi2[k + d.nmd * j2], op.ops[k]);
+    const cplx ha0 = cmul(cmul(s12, cmul(pre[k], right)), g10);
+    const int r = j1 * nmd + k;
+    cplx sh = mkc(0.0, 0.0);
+    for (int j = 0; j < d.n; ++j) cfma(sh, d.Sa0Sm1[r + d.nG * j], op.h[j + d.n * j2]);
+    out[r] = cmul(mf, csub(ha0, sh));
   }
-  for (int k = 0; k < nmd; ++k) part[(long long)blockIdx.y * part_ld + (long long)(j1 * nmd + k) + (long long)d.nG * o] = acc[k];
 }
 
-__global__ void gwp_y_sum_kernel(const GwpCYDesc* __restrict__ descs, const cplx* __restrict__ part,
-                                 long long part_ld) {
+__global__ void gwp_y_sum_kernel(const GwpCYDesc* __restrict__ descs, const GwpYOp* __restrict__ ops,
+                                 const cplx* __restrict__ part, long long part_ld, int maxn2) {
   const GwpCYDesc& d = descs[blockIdx.y];
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= d.nG) return;
+  const cplx* base = part + (long long)blockIdx.y * part_ld;
   cplx acc = mkc(0.0, 0.0);
-  for (int o = 0; o < d.op_count; ++o) acc = cadd(acc, part[(long long)blockIdx.y * part_ld + r + (long long)d.nG * o]);
+  for (int o = 0; o < d.op_count; ++o) {
+    const int n2 = ops[d.op_first + o].n2;
+    for (int j2 = 0; j2 < n2; ++j2) acc = cadd(acc, base[((long long)o * maxn2 + j2) * d.nG + r]);
+  }
   const long long ld = 2LL * d.nG;
   d.M[r + ld * d.nG] = acc;
   d.M[d.nG + r + ld * d.nG] = mkc(0.0, 0.0);
@@ -365,8 +367,11 @@ __global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __re
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int jj = 0; jj < pw; ++jj) {
     cplx* col = P + (long long)rows * jj;
+    // reflector j0+jj has no support below row nG + j0 + jj: the eps I block below C
+    // only fills in down to that row (panel-relative: nG + jj)
+    const int rend = min(rows, nG + jj + 1);
     double part = 0.0;
-    for (int rr = jj + threadIdx.x; rr < rows; rr += blockDim.x) part += cabs2(col[rr]);
+    for (int rr = jj + threadIdx.x; rr < rend; rr += blockDim.x) part += cabs2(col[rr]);
     const double nrm2 = block_sum(part, red);
     if (threadIdx.x == 0) {
       const double nrm = sqrt(nrm2);
@@ -389,10 +394,10 @@ __global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __re
     if (c < pw && s_tau[jj] != 0.0) {
       cplx* y = P + (long long)rows * c;
       cplx w = mkc(0.0, 0.0);
-      for (int rr = jj + lane; rr < rows; rr += 32) cfma_conj(w, col[rr], y[rr]);
+      for (int rr = jj + lane; rr < rend; rr += 32) cfma_conj(w, col[rr], y[rr]);
       w = warp_sum(w);
       const cplx f = cscale(w, s_tau[jj]);
-      for (int rr = jj + lane; rr < rows; rr += 32) y[rr] = csub(y[rr], cmul(col[rr], f));
+      for (int rr = jj + lane; rr < rend; rr += 32) y[rr] = csub(y[rr], cmul(col[rr], f));
     }
     __syncthreads();
   }
@@ -404,10 +409,11 @@ __global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __re
       if (s_tau[jj] == 0.0) continue;
       const cplx* v = P + (long long)rows * jj;
       cplx w = mkc(0.0, 0.0);
-      for (int rr = jj + lane; rr < rows; rr += 32) cfma_conj(w, v[rr], y[j0 + rr]);
+      const int rend = min(rows, nG + jj + 1);
+      for (int rr = jj + lane; rr < rend; rr += 32) cfma_conj(w, v[rr], y[j0 + rr]);
       w = warp_sum(w);
       const cplx f = cscale(w, s_tau[jj]);
-      for (int rr = jj + lane; rr < rows; rr += 32) y[j0 + rr] = csub(y[j0 + rr], cmul(v[rr], f));
+      for (int rr = jj + lane; rr < rend; rr += 32) y[j0 + rr] = csub(y[j0 + rr], cmul(v[rr], f));
       __syncwarp();
     }
   }
@@ -474,7 +480,102 @@ __global__ void __launch_bounds__(256) gwp_backsub_kernel(const GwpCYDesc* __res
   }
 }
 
+// Tikhonov-regularised inverse of a Hermitian n x n matrix (n <= 32) as the
+// least-squares solution of [A; eps I] X = [I; 0]: X = (A^2 + eps^2)^-1 A, the
+// matrix StdRegInv 'tikh' (maths.f90:8-83) builds from the eigen-decomposition
+// U w/(w^2 + eps^2) U^H.  Householder QR of the 2n x n stack in shared memory
+// with the 2n x n right-hand side carried along, one warp per column.
+__global__ void __launch_bounds__(256) tikh_inv_kernel(const RegInvDesc* __restrict__ descs) {
+  extern __shared__ cplx smq[];
+  const RegInvDesc& d = descs[blockIdx.x];
+  const int n = d.n, m = 2 * n, ld = 2 * MAXN_SPF;
+  cplx* A = smq;                       // m x n (ld)
+  cplx* B = smq + (size_t)ld * MAXN_SPF;  // m x n (ld)
+  __shared__ cplx s_alpha[MAXN_SPF];
+  __shared__ double s_tau[MAXN_SPF];
+  for (int e = threadIdx.x; e < m * n; e += blockDim.x) {
+    const int i = e % m, j = e / m;
+    cplx a, b;
+    if (i < n) {
+      // the upper triangle is authoritative (zheev 'U'): mirror it, real diagonal
+      a = (i <= j) ? d.A[i + n * j] : cconj(d.A[j + n * i]);
+      if (i == j) a.y = 0.0;
+      b = mkc(i == j ? 1.0 : 0.0, 0.0);
+    } else {
+      a = mkc((i - n) == j ? d.eps : 0.0, 0.0);
+      b = mkc(0.0, 0.0);
+    }
+    A[i + ld * j] = a;
+    B[i + ld * j] = b;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int j = 0; j < n; ++j) {
+    cplx* col = A + ld * j;
+    if (warp == 0) {
+      double part = 0.0;
+      for (int r = j + lane; r < m; r += 32) part += cabs2(col[r]);
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+      if (lane == 0) {
+        const double nrm = sqrt(part);
+        const cplx x0 = col[j];
+        const double ax0 = sqrt(cabs2(x0));
+        if (nrm == 0.0) {
+          s_alpha[j] = mkc(0.0, 0.0);
+          s_tau[j] = 0.0;
+        } else {
+          const cplx ph = (ax0 > 0.0) ? mkc(x0.x / ax0, x0.y / ax0) : mkc(1.0, 0.0);
+          const cplx alpha = cscale(ph, -nrm);
+          col[j] = csub(x0, alpha);
+          s_alpha[j] = alpha;
+          s_tau[j] = 2.0 / (2.0 * part + 2.0 * nrm * ax0);
+        }
+      }
+    }
+    __syncthreads();
+    const double tau = s_tau[j];
+    if (tau != 0.0) {
+      // columns j+1..n-1 of A, then all n columns of B
+      for (int c = warp; c < (n - j - 1) + n; c += nw) {
+        cplx* y = (c < n - j - 1) ? A + ld * (j + 1 + c) : B + ld * (c - (n - j - 1));
+        cplx w = mkc(0.0, 0.0);
+        for (int r = j + lane; r < m; r += 32) cfma_conj(w, col[r], y[r]);
+        w = warp_sum(w);
+        const cplx f = cscale(w, tau);
+        for (int r = j + lane; r < m; r += 32) y[r] = csub(y[r], cmul(col[r], f));
+      }
+    }
+    __syncthreads();
+  }
+  // back substitution R X = (Q^H [I; 0])[0:n], one thread per right-hand side
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    cplx* x = B + ld * c;
+    for (int i = n - 1; i >= 0; --i) {
+      cplx v = x[i];
+      for (int k = i + 1; k < n; ++k) v = csub(v, cmul(A[i + ld * k], x[k]));
+      x[i] = cdiv(v, s_alpha[i]);
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e % n, j = e / n;
+    d.inv_out[i + n * j] = B[i + ld * j];
+  }
+}
+
 }  // namespace
+
+void launch_tikh_inv(const RegInvDesc* d, int nd, cudaStream_t st) {
+  if (nd <= 0) return;
+  const size_t smem = sizeof(cplx) * 2 * (size_t)(2 * MAXN_SPF) * MAXN_SPF;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(tikh_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  tikh_inv_kernel<<<nd, 256, smem, st>>>(d);
+}
 
 void launch_gwp_ovl(const GwpOvlDesc* d, int nd, cudaStream_t st) {
   if (nd <= 0) return;
@@ -494,9 +595,10 @@ void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, int maxops, c
   gwp_sa0sm1_kernel<<<dim3(ne, nd), 256, 0, st>>>(d);
   const unsigned nt = (unsigned)((maxG + 15) / 16);
   gwp_c_kernel<<<dim3(nt, nt, nd), dim3(16, 16), 0, st>>>(d);
-  const long long part_ld = (long long)maxG * std::max(maxops, 1);
-  gwp_y_part_kernel<<<dim3((unsigned)((maxn * std::max(maxops, 1) + 63) / 64), nd), 64, 0, st>>>(d, ops, part, part_ld);
-  gwp_y_sum_kernel<<<dim3((maxG + 127) / 128, nd), 128, 0, st>>>(d, part, part_ld);
+  const long long part_ld = (long long)maxG * maxn * std::max(maxops, 1);
+  const long long nthr = (long long)maxn * maxn * std::max(maxops, 1);
+  gwp_y_part_kernel<<<dim3((unsigned)((nthr + 127) / 128), nd), 128, 0, st>>>(d, ops, part, part_ld, maxn);
+  gwp_y_sum_kernel<<<dim3((maxG + 127) / 128, nd), 128, 0, st>>>(d, ops, part, part_ld, maxn);
 }
 
 void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out, int* status, cudaStream_t st) {

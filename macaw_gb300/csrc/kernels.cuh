@@ -277,10 +277,12 @@ struct GwpCYDesc {       // one (Gaussian mode, state) block of Calc_CY and the 
   double eps;            // eps_C
 };
 void launch_gwp_ovl(const GwpOvlDesc* d, int nd, cudaStream_t st);
+// Tikhonov inverses (regtype 'tikh') of n <= 32 Hermitian matrices into inv_out, by QR
+void launch_tikh_inv(const RegInvDesc* d, int nd, cudaStream_t st);
 void launch_gwp_h1(const GwpH1Desc* d, int nd, cudaStream_t st);
 // Calc_CY and the Tikhonov parameter solve (StdRegSol 'tikh', maths.f90:87-162)
 // for nd (mode, state) blocks; maxG = max nG.  Then dxi = der * x and tau.
-// part: scratch of nd * maxG * maxops complex (per-operator partial sums of Y)
+// part: scratch of nd * maxG * maxn * maxops complex (the terms of Y)
 void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, int maxops, const GwpYOp* ops, cplx* part,
                    cudaStream_t st);
 void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out, int* status, cudaStream_t st);
