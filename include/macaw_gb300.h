@@ -72,7 +72,7 @@ int64_t mctdh_destroy(mctdh_ctx_t *ctx);
 /* Integrator codes of mctdh_step / mctdh_propagate: 1 Cash-Karp RK, 2 Dormand-Prince
  * RK, 3 Adams PECE of order int_order with int_par1 extra EC iterations (the first
  * int_order steps of a propagation with Cash-Karp, propagator.f90:156-181;
- * integrator.f90:244-380), 10 CMF2. */
+ * integrator.f90:244-380), 4 Bulirsch-Stoer (bsstep, integrator.f90:418-608), 10 CMF2. */
 
 /* Equation of motion (A, psi, t) -> (dA, dpsi) on host buffers.
  * Replaces Calc_Derivs(A0, psi0, dA, dpsi, tt) -- derivatives.f90:39. */

@@ -274,6 +274,16 @@ struct Ctx {
   cplx *ad_dcur = nullptr, *ad_temp = nullptr, *ad_new = nullptr, *ad_new1 = nullptr, *ad_dnew = nullptr,
        *ad_d1 = nullptr;
   OvlPlan ad_plan;                   // DeltaPsi(ANew, ANew1)
+  // Bulirsch-Stoer (integrator.f90:384-608)
+  bool bs_planned = false, bs_first = true;
+  int bs_kmax = 0, bs_kopt = 0;
+  double bs_tnew = -1e16, bs_hnext = -1e15;
+  double bs_Ak[10] = {}, bs_tstore[10] = {};
+  double bs_alf[9][9] = {};
+  cplx *bs_save = nullptr, *bs_d0 = nullptr, *bs_am = nullptr, *bs_an = nullptr, *bs_sw = nullptr, *bs_d = nullptr,
+       *bs_seq = nullptr, *bs_a0 = nullptr, *bs_a1 = nullptr;
+  cplx* bs_q[10] = {};
+  OvlPlan bs_plan;                   // DeltaPsi(A0, A1) of the extrapolation
   // model
   int nstates = 0, nmodes = 0, ndof = 0, nham = 0, maxdof = 0, nopermax = 0;
   std::vector<int> nspf;  // [m + nmodes*s]
@@ -1741,6 +1751,174 @@ bool adams_or_boot_step(Ctx& c, double t, double htry, double* hdid, double* hne
 }
 
 // ---------------------------------------------------------------------------
+// Bulirsch-Stoer (bsstep, mmid, pzextr, SetupBS; integrator.f90:384-608) on the
+// resident state: modified midpoint sequences nSeq = 2, 4, .., 18, polynomial
+// extrapolation to zero step, order window kOpt with the work model Ak.
+// ---------------------------------------------------------------------------
+const int BS_KMAXX = 8;
+const int BS_NSEQ[9] = {2, 4, 6, 8, 10, 12, 14, 16, 18};
+const double BS_SAFE1 = 0.25, BS_SAFE2 = 0.7, BS_REDMAX = 1e-5, BS_REDMIN = 0.7, BS_SCALMAX = 0.1;
+
+void bs_plan(Ctx& c) {
+  if (c.bs_planned) return;
+  c.bs_Ak[1] = BS_NSEQ[0] + 1.0;
+  for (int k = 1; k <= BS_KMAXX; ++k) c.bs_Ak[k + 1] = c.bs_Ak[k] + BS_NSEQ[k];
+  for (int iq = 2; iq <= BS_KMAXX; ++iq)
+    for (int k = 1; k < iq; ++k)
+      c.bs_alf[k][iq] = pow(BS_SAFE1 * c.eps_int, (c.bs_Ak[k + 1] - c.bs_Ak[iq + 1]) /
+                                                      ((c.bs_Ak[iq + 1] - c.bs_Ak[1] + 1.0) * (double)(2 * k + 1)));
+  int kopt = BS_KMAXX;
+  for (int ko = 2; ko < BS_KMAXX; ++ko)
+    if (c.bs_Ak[ko + 1] > c.bs_Ak[ko] * c.bs_alf[ko - 1][ko]) {
+      kopt = ko;
+      break;
+    }
+  c.bs_kmax = kopt;
+  c.bs_kopt = kopt;
+  cplx** bufs[] = {&c.bs_save, &c.bs_d0, &c.bs_am, &c.bs_an, &c.bs_sw, &c.bs_d, &c.bs_seq, &c.bs_a0, &c.bs_a1};
+  for (cplx** b : bufs) *b = c.ar.calloc_c(c.ntot);
+  for (int q = 1; q <= BS_KMAXX + 1; ++q) c.bs_q[q] = c.ar.calloc_c(c.ntot);
+  plan_ovl(c, c.bs_plan, c.bs_a0, c.bs_a1, (c.precision && c.eps_int >= 1e-5) ? 2 : 0);
+  c.bs_planned = true;
+}
+
+// mmid: AOut (bs_seq) after nstep modified-midpoint steps of htot from bs_save
+void bs_mmid(Ctx& c, double htot, int nstep) {
+  const double dt = htot / nstep;
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  a.k[0] = c.bs_d0;
+  a.c[0] = 1.0;
+  a.nk = 1;
+  CK(cudaMemcpyAsync(c.bs_am, c.bs_save, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+  launch_stage(c.bs_an, c.bs_save, a, dt, c.ntot, c.st);   // An = A0 + dt dA
+  c.count();
+  eom_from(c, c.bs_an, c.bs_d);
+  cplx *am = c.bs_am, *an = c.bs_an, *sw = c.bs_sw;
+  for (int n = 2; n <= nstep; ++n) {
+    a.k[0] = c.bs_d;
+    launch_stage(sw, am, a, 2.0 * dt, c.ntot, c.st);   // Aswap = Am + 2 dt D
+    c.count();
+    cplx* t = am;
+    am = an;
+    an = sw;
+    sw = t;
+    eom_from(c, an, c.bs_d);
+  }
+  launch_bs_final(c.bs_seq, am, an, c.bs_d, dt, c.ntot, c.st);
+  c.count();
+}
+
+void bs_pzextr(Ctx& c, int iest, double test) {
+  c.bs_tstore[iest] = test;
+  BsExtr e;
+  memset(&e, 0, sizeof(e));
+  for (int q = 1; q <= BS_KMAXX + 1; ++q) e.q[q] = c.bs_q[q];
+  e.iest = iest;
+  for (int k1 = 1; k1 < iest; ++k1) {
+    const double delta = 1.0 / (c.bs_tstore[iest - k1] - test);
+    e.f1[k1] = test * delta;
+    e.f2[k1] = c.bs_tstore[iest - k1] * delta;
+  }
+  launch_bs_extr(e, c.bs_seq, c.bs_a0, c.bs_a1, c.ntot, c.st);
+  c.count();
+}
+
+// bsstep from d_y with its derivative in bs_d0; the accepted state lands in d_y.
+void bsstep(Ctx& c, double t, double htry, double* hdid, double* hnext) {
+  double dt = htry;
+  CK(cudaMemcpyAsync(c.bs_save, c.d_y, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+  if (dt != c.bs_hnext || t != c.bs_tnew) {   // :428-431
+    c.bs_first = true;
+    c.bs_kopt = c.bs_kmax;
+  }
+  bool reduct = false, converged = false;
+  double error[BS_KMAXX + 2] = {};
+  const int kmax = c.bs_kmax;
+  int k = 1;
+  for (int guard = 0;; ++guard) {
+    if (guard > 1000) throw StatusError(MCTDH_ESTEP, "Bulirsch-Stoer step not accepted");
+    double red = BS_REDMIN;
+    double errmax = 0.0;
+    for (k = 1; k <= kmax; ++k) {
+      c.bs_tnew = t + dt;
+      bs_mmid(c, dt, BS_NSEQ[k - 1]);
+      const double test = (dt / BS_NSEQ[k - 1]) * (dt / BS_NSEQ[k - 1]);
+      bs_pzextr(c, k, test);
+      if (k != 1) {
+        run_ovl(c, c.bs_plan);
+        cplx o[3];
+        read_ovl(c, c.bs_plan, o);
+        check_status(c);
+        errmax = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x)))) / c.eps_int;
+        if (!std::isfinite(errmax)) throw StatusError(MCTDH_ENONFINITE, "non-finite Bulirsch-Stoer error estimate");
+        error[k - 1] = pow(errmax / BS_SAFE1, 1.0 / (double)(2 * k - 1));
+      }
+      const int kopt = c.bs_kopt;
+      if (k != 1 && (k >= kopt - 1 || c.bs_first)) {
+        if (errmax < 1.0) {
+          converged = true;
+          break;
+        }
+        if (k == kmax || k == kopt + 1) {
+          red = BS_SAFE2 / error[k - 1];
+          break;
+        } else if (k == kopt) {
+          if (c.bs_alf[kopt - 1][kopt] < error[k - 1]) {
+            red = 1.0 / error[k - 1];
+            break;
+          }
+        } else if (kopt == kmax) {
+          if (c.bs_alf[k - 1][kmax - 1] < error[k - 1]) {
+            red = c.bs_alf[k - 1][kmax - 1] * BS_SAFE2 / error[k - 1];
+            break;
+          }
+        } else if (c.bs_alf[k - 1][kopt] < error[k - 1]) {
+          red = c.bs_alf[k - 1][kopt - 1] / error[k - 1];
+          break;
+        }
+      }
+    }
+    if (converged) break;
+    red = std::max(std::min(red, BS_REDMIN), BS_REDMAX);
+    dt *= red;
+    reduct = true;
+  }
+  *hdid = dt;
+  c.bs_first = false;
+  double workmin = 1e16, scal = 1.0;
+  for (int kk = 1; kk <= k - 1; ++kk) {
+    const double fact = std::max(error[kk], BS_SCALMAX);
+    const double work = fact * c.bs_Ak[kk + 1];
+    if (work < workmin) {
+      scal = fact;
+      workmin = work;
+      c.bs_kopt = kk + 1;
+    }
+  }
+  double hn = dt / scal;
+  const int kopt = c.bs_kopt;
+  if (kopt >= k && kopt != kmax && !reduct) {
+    const double fact = std::max(scal / c.bs_alf[kopt - 1][kopt], BS_SCALMAX);
+    if (c.bs_Ak[kopt + 1] * fact <= workmin) {
+      hn = dt / fact;
+      c.bs_kopt = kopt + 1;
+    }
+  }
+  *hnext = hn;
+  c.bs_hnext = hn;
+  CK(cudaMemcpyAsync(c.d_y, c.bs_a0, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
+}
+
+// One Bulirsch-Stoer step of propagate_wf (propagator.f90:216-222): the
+// derivative at the step start, then bsstep.
+void bs_step(Ctx& c, double t, double htry, double* hdid, double* hnext) {
+  bs_plan(c);
+  eom_from(c, c.d_y, c.bs_d0);
+  bsstep(c, t, htry, hdid, hnext);
+}
+
+// ---------------------------------------------------------------------------
 // CMF2 (cmf2_base.f90:47-206) for DVR models
 // ---------------------------------------------------------------------------
 void hb(Ctx& c, const cplx* B, cplx* out) {
@@ -2977,6 +3155,8 @@ int64_t mctdh_set_state(mctdh_ctx_t* ctx, const double* A, const double* psi, in
     upload(*c, c->d_y, A, psi);
     c->fsal_valid = false;
     c->ad_valid = false;
+    c->bs_tnew = -1e16;   // SetupBS and propagator.f90:213: a new propagation
+    c->bs_hnext = -1e15;
     c->ops_fresh = false;
     auto mi = g_mfx.find(c);
     if (mi != g_mfx.end()) mi->second->nhist = 0;
@@ -3054,6 +3234,16 @@ int64_t mctdh_propagate(mctdh_ctx_t* ctx, int64_t int_type, double tnext, double
     double time = *t, stepsize = *step;
     while (true) {
       double sdone, snext;
+      if (int_type == 4) {
+        bs_step(*c, time, stepsize, &sdone, &snext);
+        ++att;
+        ++steps;
+        time += sdone;
+        if (time >= tnext - c->min_stepsize) break;
+        long long q = (long long)((tnext - time) / snext);
+        stepsize = (q == 0) ? (tnext - time) : (tnext - time) / (double)(q + 1);
+        continue;
+      }
       if (int_type == 3) {
         const bool boot = adams_or_boot_step(*c, time, stepsize, &sdone, &snext, &att);
         ++steps;
@@ -3105,6 +3295,9 @@ int64_t mctdh_step(mctdh_ctx_t* ctx, int64_t int_type, double t, double htry, do
     long long att = 0;
     if (int_type == 3) {
       adams_or_boot_step(*c, t, htry, hdid, hnext, &att);
+    } else if (int_type == 4) {
+      bs_step(*c, t, htry, hdid, hnext);
+      att = 1;
     } else if (int_type == 10) {
       cmf2(*c, t, htry, hdid, hnext, &att);
     } else if (int_type == 1 || int_type == 2) {

@@ -1053,6 +1053,46 @@ void launch_ens_accept(cplx* y, const cplx* src, const int* accept, const long l
   ens_accept_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, src, accept, off, nm, n);
 }
 
+__global__ void bs_final_kernel(cplx* __restrict__ out, const cplx* __restrict__ am, const cplx* __restrict__ an,
+                                const cplx* __restrict__ d, double dt, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cplx a = am[i], b = an[i], g = d[i];
+  out[i] = mkc(0.5 * ((a.x + b.x) + dt * g.x), 0.5 * ((a.y + b.y) + dt * g.y));
+}
+void launch_bs_final(cplx* out, const cplx* am, const cplx* an, const cplx* d, double dt, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  bs_final_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, am, an, d, dt, n);
+}
+__global__ void bs_extr_kernel(BsExtr e, const cplx* __restrict__ est, cplx* __restrict__ a0, cplx* __restrict__ a1,
+                               long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cplx x = est[i];
+  if (e.iest == 1) {
+    e.q[1][i] = x;
+    a0[i] = x;
+    a1[i] = x;
+    return;
+  }
+  cplx A0 = x, A1 = x, At = x;
+  for (int k1 = 1; k1 < e.iest; ++k1) {
+    const cplx cd = e.q[k1][i];
+    e.q[k1][i] = A1;
+    const cplx del = csub(At, cd);
+    A1 = cscale(del, e.f1[k1]);
+    At = cscale(del, e.f2[k1]);
+    A0 = cadd(A0, A1);
+  }
+  e.q[e.iest][i] = A1;
+  a0[i] = A0;
+  a1[i] = cadd(A0, A1);
+}
+void launch_bs_extr(const BsExtr& e, const cplx* est, cplx* a0, cplx* a1, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  bs_extr_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e, est, a0, a1, n);
+}
+
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st) {
   if (n <= 0) return;
   stage_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, base, a, dt, n);

@@ -192,6 +192,16 @@ void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
                     long long total, cudaStream_t st, int prec);
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st);
+// Bulirsch-Stoer: the last modified-midpoint stage 0.5 (am + an + dt d) (mmid,
+// integrator.f90:550-551) and one polynomial-extrapolation column (pzextr, :559-608)
+struct BsExtr {
+  cplx* q[10];             // qA(:, 1..iEst) (index 0 unused)
+  double f1[10], f2[10];   // per k1 = 1..iEst-1
+  int iest;
+  int pad;
+};
+void launch_bs_final(cplx* out, const cplx* am, const cplx* an, const cplx* d, double dt, long long n, cudaStream_t st);
+void launch_bs_extr(const BsExtr& e, const cplx* est, cplx* a0, cplx* a1, long long n, cudaStream_t st);
 // ensembles: member m owns elements off[m] .. off[m+1] of the vectors
 void launch_ens_stage(cplx* out, const cplx* base, const StageArgs& a, const double* dt, const long long* off, int nm,
                       long long n, cudaStream_t st);

@@ -40,6 +40,7 @@ OP_SINM2 = -4    # sin^-2 (Legendre DVR only)
 INT_RK45 = 1     # Cash-Karp (input.f90:280-282)
 INT_DOPRI = 2    # Dormand-Prince (input.f90:283-285)
 INT_ABM = 3      # Adams PECE, 'abm<order><par1>' (input.f90:286-292)
+INT_BS = 4       # Bulirsch-Stoer, 'bs' (input.f90:293-294)
 INT_CMF2 = 10    # constant mean field (input.f90:295-331)
 
 
@@ -674,6 +675,8 @@ def parse_input(path: str) -> Model:
         model.int_type = INT_RK45
     elif integ == "dopri":
         model.int_type = INT_DOPRI
+    elif integ.startswith("bs"):
+        model.int_type = INT_BS
     elif integ.startswith("abm"):
         model.int_type = INT_ABM
         model.int_order = int(integ[3:5])

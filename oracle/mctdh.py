@@ -42,7 +42,7 @@ from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
-from macaw_gb300.model import Model, AU2FS, INT_RK45, INT_DOPRI, INT_ABM, INT_CMF2
+from macaw_gb300.model import Model, AU2FS, INT_RK45, INT_DOPRI, INT_ABM, INT_BS, INT_CMF2
 
 _EPS = np.finfo(np.float64).eps
 
@@ -787,6 +787,162 @@ class Oracle:
         dA2, dpsi2 = self.calc_derivs(An1, pn1, t + dt)
         return An1, pn1, dA2, dpsi2, hist, h_prev, dt, hnext
 
+    # ---------------- Bulirsch-Stoer ----------------
+    BS_KMAXX = 8
+    BS_NSEQ = (2, 4, 6, 8, 10, 12, 14, 16, 18)
+    BS_SAFE1, BS_SAFE2 = 0.25, 0.7
+    BS_REDMAX, BS_REDMIN, BS_SCALMAX = 1e-5, 0.7, 0.1
+
+    def bs_setup(self):
+        """SetupBS (integrator.f90:387-414): work coefficients Ak, the tableau alf(k, q)
+        and the row kMax; tNew and hnext start at impossible values."""
+        kmaxx = self.BS_KMAXX
+        Ak = [0.0] * (kmaxx + 2)   # 1-based: Ak[1..iMax]
+        Ak[1] = self.BS_NSEQ[0] + 1.0
+        for k in range(1, kmaxx + 1):
+            Ak[k + 1] = Ak[k] + self.BS_NSEQ[k]
+        alf = np.zeros((kmaxx + 1, kmaxx + 1))
+        for iq in range(2, kmaxx + 1):
+            for k in range(1, iq):
+                alf[k, iq] = (self.BS_SAFE1 * self.m.eps_int) ** (
+                    (Ak[k + 1] - Ak[iq + 1]) / ((Ak[iq + 1] - Ak[1] + 1.0) * (2 * k + 1)))
+        kopt = kmaxx
+        for ko in range(2, kmaxx):
+            if Ak[ko + 1] > Ak[ko] * alf[ko - 1, ko]:
+                kopt = ko
+                break
+        self.bs = dict(Ak=Ak, alf=alf, kmax=kopt, kopt=kopt, tnew=-1e16, first=True,
+                       tstore=[0.0] * (kmaxx + 2), qA=[None] * (kmaxx + 2), qpsi=[None] * (kmaxx + 2))
+
+    def bs_mmid(self, A0, psi0, dA, dpsi, t, htot, nstep):
+        """mmid (integrator.f90:522-555): modified midpoint rule."""
+        dt = htot / nstep
+        Am, pm = A0, psi0
+        An, pn = A0 + dt * dA, psi0 + dt * dpsi
+        tx = t + dt
+        dAo, dpo = self.calc_derivs(An, pn, tx)
+        dt2 = dt * 2
+        for _ in range(2, nstep + 1):
+            As, ps = Am + dt2 * dAo, pm + dt2 * dpo
+            Am, pm = An, pn
+            An, pn = As, ps
+            tx = tx + dt
+            dAo, dpo = self.calc_derivs(An, pn, tx)
+        return 0.5 * (Am + An + dt * dAo), 0.5 * (pm + pn + dt * dpo)
+
+    def bs_pzextr(self, iest, test, Aest, pest):
+        """pzextr (integrator.f90:559-608): polynomial extrapolation to zero step."""
+        b = self.bs
+        b["tstore"][iest] = test
+        A0, p0 = Aest.copy(), pest.copy()
+        A1, p1 = Aest.copy(), pest.copy()
+        if iest == 1:
+            b["qA"][1], b["qpsi"][1] = Aest.copy(), pest.copy()
+            return A0, p0, A1, p1
+        At, pt = Aest.copy(), pest.copy()
+        for k1 in range(1, iest):
+            delta = 1.0 / (b["tstore"][iest - k1] - test)
+            f1 = test * delta
+            f2 = b["tstore"][iest - k1] * delta
+            qa, qp = b["qA"][k1], b["qpsi"][k1]
+            b["qA"][k1], b["qpsi"][k1] = A1.copy(), p1.copy()
+            cda, cdp = At - qa, pt - qp
+            A1, p1 = f1 * cda, f1 * cdp
+            At, pt = f2 * cda, f2 * cdp
+            A0, p0 = A0 + A1, p0 + p1
+        b["qA"][iest], b["qpsi"][iest] = A1.copy(), p1.copy()
+        return A0, p0, A0 + A1, p0 + p1
+
+    def bsstep(self, A, psi, dA, dpsi, t, htry, hnext_prev):
+        """bsstep (integrator.f90:418-518).  Returns (A, psi, hdid, hnext)."""
+        b = self.bs
+        md = self.m
+        dt = htry
+        Asave, psave = A.copy(), psi.copy()
+        if dt != hnext_prev or t != b["tnew"]:
+            b["first"] = True
+            b["kopt"] = b["kmax"]
+        reduct = False
+        converged = False
+        error = [0.0] * (self.BS_KMAXX + 2)
+        Ak, alf, kmax = b["Ak"], b["alf"], b["kmax"]
+        while True:
+            red = None
+            k = 1
+            while k <= kmax:
+                b["tnew"] = t + dt
+                As, ps = self.bs_mmid(Asave, psave, dA, dpsi, t, dt, self.BS_NSEQ[k - 1])
+                test = (dt / self.BS_NSEQ[k - 1]) ** 2
+                A0, p0, A1, p1 = self.bs_pzextr(k, test, As, ps)
+                if k != 1:
+                    errmax = self.delta_psi(A0, p0, A1, p1) / md.eps_int
+                    error[k - 1] = (errmax / self.BS_SAFE1) ** (1.0 / (2 * k - 1))
+                kopt = b["kopt"]
+                if k != 1 and (k >= kopt - 1 or b["first"]):
+                    if errmax < 1.0:
+                        converged = True
+                        break
+                    if k == kmax or k == kopt + 1:
+                        red = self.BS_SAFE2 / error[k - 1]
+                        break
+                    elif k == kopt:
+                        if alf[kopt - 1, kopt] < error[k - 1]:
+                            red = 1.0 / error[k - 1]
+                            break
+                    elif kopt == kmax:
+                        if alf[k - 1, kmax - 1] < error[k - 1]:
+                            red = alf[k - 1, kmax - 1] * self.BS_SAFE2 / error[k - 1]
+                            break
+                    elif alf[k - 1, kopt] < error[k - 1]:
+                        red = alf[k - 1, kopt - 1] / error[k - 1]
+                        break
+                k += 1
+            if converged:
+                break
+            red = max(min(red, self.BS_REDMIN), self.BS_REDMAX)
+            dt = dt * red
+            reduct = True
+        hdid = dt
+        b["first"] = False
+        workmin = 1e16
+        scal = None
+        for kk in range(1, k):
+            fact = max(error[kk], self.BS_SCALMAX)
+            work = fact * Ak[kk + 1]
+            if work < workmin:
+                scal = fact
+                workmin = work
+                b["kopt"] = kk + 1
+        hnext = dt / scal
+        kopt = b["kopt"]
+        if kopt >= k and kopt != kmax and not reduct:
+            fact = max(scal / alf[kopt - 1, kopt], self.BS_SCALMAX)
+            if Ak[kopt + 1] * fact <= workmin:
+                hnext = dt / fact
+                b["kopt"] = kopt + 1
+        return A0, p0, hdid, hnext
+
+    def _propagate_bs(self, A, psi, A0, psi0, t, step, maxtime, record_steps):
+        """propagate_wf with Bulirsch-Stoer (propagator.f90:210-248)."""
+        md = self.m
+        self.bs_setup()
+        snext = -1e15
+        outputs, steps = [], []
+        while t < maxtime:
+            outputs.append(self.observables(A, psi, A0, psi0, t))
+            tnext = t + md.tout
+            while True:
+                dA, dpsi = self.calc_derivs(A, psi, t)
+                A, psi, sdone, snext = self.bsstep(A, psi, dA, dpsi, t, step, snext)
+                if record_steps:
+                    steps.append((t, step, sdone, snext, 1))
+                t = t + sdone
+                if t >= tnext - md.min_stepsize:
+                    break
+                q = int((tnext - t) / snext)
+                step = (tnext - t) if q == 0 else (tnext - t) / (q + 1)
+        return outputs, steps, (A, psi, t)
+
     # ---------------- CMF2 ----------------
     def calc_dhd_b(self, B: np.ndarray) -> np.ndarray:
         """Calc_DHD_B (cmf2_derivatives.f90:1-80): H_B * B (no der_factor)."""
@@ -1041,6 +1197,8 @@ class Oracle:
         nsteps = 0
         if md.int_type == INT_ABM:
             return self._propagate_adams(A, psi, A0, psi0, t, step, maxtime, record_steps)
+        if md.int_type == INT_BS:
+            return self._propagate_bs(A, psi, A0, psi0, t, step, maxtime, record_steps)
         while t < maxtime:
             outputs.append(self.observables(A, psi, A0, psi0, t))
             tnext = t + md.tout

@@ -243,3 +243,15 @@ def test_adams_free_running(core_cls, order, par1):
     ref, _, _ = Oracle(model).propagate(A, psi)
     outs = core_cls(model).propagate(A, psi)
     _compare(outs, ref, 10 * model.eps_int)
+
+
+def test_bulirsch_stoer_free_running(core_cls):
+    """Bulirsch-Stoer ('bs', integrator.f90:384-608; propagate_wf :210-248) free
+    running against the oracle's restatement, bounded by the integrator tolerance."""
+    from macaw_gb300.model import INT_BS
+    model = small_lvc(tfinal_fs=1.0)
+    model.int_type = INT_BS
+    A, psi = initial_wavefunction(model)
+    ref, _, _ = Oracle(model).propagate(A, psi)
+    outs = core_cls(model).propagate(A, psi)
+    _compare(outs, ref, 10 * model.eps_int)
