@@ -393,8 +393,21 @@ def run_gpu(args):
 
 def run_profile_case(args):
     """A short, fixed piece of the workload for profiler captures: three CMF2 steps
-    of 1e-3 fs from the initial state of the qvc12 model (about 1,700 launches)."""
+    of 1e-3 fs from the initial state of the qvc12 model (about 1,700 launches), or
+    with `--workload gmctdh16` three EOM evaluations of the Gaussian model."""
     from macaw_gb300.capi import GpuCore
+    if args.workload == "gmctdh16":
+        # three EOM evaluations of the Gaussian model on its initial state
+        from macaw_gb300.generate import gmctdh16
+        model = gmctdh16()
+        A0, psi0 = initial_wavefunction(model)
+        core = GpuCore(model, precision=args.precision)
+        for _ in range(3):
+            core.calc_derivs(A0, psi0, 0.0)
+        print(json.dumps({"profile_case": "gmctdh16", "precision": args.precision,
+                          "launches": core.launch_count()}), flush=True)
+        core.close()
+        return 0
     model = make_model()
     A0, psi0 = initial_wavefunction(model)
     core = GpuCore(model, precision=args.precision)
