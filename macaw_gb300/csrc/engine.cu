@@ -405,6 +405,7 @@ struct Ctx {
   int cy_maxG = 0, cy_maxn = 0, cy_maxops = 0;
   cplx* cy_part = nullptr;                            // per-operator partial sums of Y
   std::vector<std::vector<cplx*>> tau;                // [i][s]
+  std::vector<std::vector<cplx*>> dhd;                // [i][k] D^H h D of the CMF2 Lanczos (Calc_DHD)
   cplx* d_adot = nullptr;                             // f * sum_t ae_t H_t A before the corrections
   cplx* d_dA = nullptr;                               // dA after S^-1 and tau
   std::vector<ProdBatch> gwp_sinv;                    // S^-1 products, one batch per Gaussian mode
@@ -1090,10 +1091,20 @@ void plan_gwp_derivs(Ctx& c) {
 }
 
 // H_B * B for the CMF2 Lanczos (Calc_DHD_B, cmf2_derivatives.f90:1-80): chains over
-// the non-identity operators of each term, no der_factor.
+// the non-identity operators of each term (grid modes, then Gaussian modes with
+// D^H h D), no der_factor.
 void plan_hb(Ctx& c) {
   const int f = c.nmodes;
   c.hb_chains.assign(f + 1, ProdBatch());
+  c.dhd.assign(c.modes_gwp.size(), {});
+  for (size_t i = 0; i < c.modes_gwp.size(); ++i) {
+    const int m = c.modes_gwp[i];
+    c.dhd[i].assign(c.noper[m], nullptr);
+    for (int k = 0; k < c.noper[m]; ++k) {
+      if (c.is_identity[m + f * k]) continue;
+      c.dhd[i][k] = c.ar.calloc_c((long long)c.m_of(m, c.oper[m][k][0]) * c.m_of(m, c.oper[m][k][1]));
+    }
+  }
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
   const int chain_fmt = c.precision ? TF_SPLIT : TF_C64;
   for (int t : c.general_terms) {
@@ -1111,6 +1122,21 @@ void plan_hb(Ctx& c) {
       cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
       ++depth;
       c.hb_chains[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0, cur.fmt, chain_fmt);
+      cur.p = out;
+      cur.shape = ns;
+      cur.fmt = chain_fmt;
+    }
+    // Gaussian modes act through D^H h D; their identity is skipped (D^H S D = 1)
+    for (size_t i = 0; i < c.modes_gwp.size(); ++i) {
+      const int m = c.modes_gwp[i];
+      const int k = c.ioper[m + f * t];
+      if (c.is_identity[m + f * k]) continue;
+      const int n1 = c.m_of(m, s1);
+      std::vector<int> ns = cur.shape;
+      ns[m] = n1;
+      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+      ++depth;
+      c.hb_chains[depth].add(cur.p, out, c.dhd[i][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0, cur.fmt, chain_fmt);
       cur.p = out;
       cur.shape = ns;
       cur.fmt = chain_fmt;
@@ -1389,13 +1415,16 @@ void gwp_setup_run(Ctx& c) {
 
 // Gaussian modes, last part: parameter derivatives into out's psi part and the
 // corrected dA into out's coefficient part (from d_adot).
+// Calc_CY and the Tikhonov parameter solve: der_factor * x into out's psi part, tau
+void gwp_solve_run(Ctx& c, cplx* out) {
+  ProfScope ps(c, KP_GWP);
+  launch_gwp_cy(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.cy_maxn, c.cy_maxops, c.yop_d, c.cy_part, c.st);
+  launch_gwp_solve(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.der, out, c.d_status, c.st);
+  c.count(6 + (c.cy_maxG + GWP_QR_PW - 1) / GWP_QR_PW);
+}
+
 void gwp_derivs_run(Ctx& c, cplx* out) {
-  {
-    ProfScope ps(c, KP_GWP);
-    launch_gwp_cy(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.cy_maxn, c.cy_maxops, c.yop_d, c.cy_part, c.st);
-    launch_gwp_solve(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.der, out, c.d_status, c.st);
-    c.count(6 + (c.cy_maxG + GWP_QR_PW - 1) / GWP_QR_PW);
-  }
+  gwp_solve_run(c, out);
   for (auto& b : c.gwp_sinv) run_prod(c, b);
   for (auto& b : c.gwp_tau) run_prod(c, b);
   CK(cudaMemcpyAsync(out, c.d_dA, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
@@ -2048,6 +2077,12 @@ void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
 // h1mode only (no mean fields) on the SPFs of y: used before the back-propagation.
 void h1_only(Ctx& c, const cplx* y) {
   copy_dev(c, c.d_in + c.naconftot, y + c.naconftot, c.dimpsi);
+  if (!c.modes_gwp.empty()) {
+    // Calc_S00 and Calc_h1mode of the Gaussian modes (cmf2_base.f90:158-163)
+    launch_gwp_ovl(c.gs_d, (int)c.gs_h.size(), c.st);
+    launch_gwp_h1(c.gh1_d, (int)c.gh1_h.size(), c.st);
+    c.count(2);
+  }
   launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, c.precision);
   launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
   c.count(3);
@@ -2074,6 +2109,23 @@ struct CmfState {
   std::vector<SpfErrDesc> errd_h;
   SpfErrDesc* errd_d = nullptr;
   long long rk_iters = 0;
+  // Gaussian modes (cmf2_base.f90): the D matrices of every (mode, set) block,
+  // concatenated into one vector per role; B = D^H S A is the propagated vector
+  bool gwp = false;
+  long long nD = 0;
+  cplx *DD0 = nullptr, *DDHalf = nullptr, *DDHalf2 = nullptr;   // DD0, DDHalf, DDHalf2 of cmf2
+  cplx *Din = nullptr, *Dtmp = nullptr, *DhS = nullptr;         // stage input, 5th-order result, D^H S
+  cplx* Dk[7] = {};                                             // stage derivatives dDD
+  unsigned char* d_elem_mode = nullptr;                         // mode of every D element
+  std::vector<GwpIsqrtDesc> isq_h;
+  GwpIsqrtDesc* isq_d = nullptr;
+  std::vector<GwpDhdDesc> dhd0_h, dhd2_h;                       // D^H h D with DD0 / DDHalf2
+  GwpDhdDesc *dhd0_d = nullptr, *dhd2_d = nullptr;
+  std::vector<GwpDDerivDesc> dder_h;
+  GwpDDerivDesc* dder_d = nullptr;
+  std::vector<GwpOvlDesc> gerr_h;                               // Calc_Err_SPF overlaps
+  GwpOvlDesc* gerr_d = nullptr;
+  std::vector<ProdBatch> a2b, b2a_half, b2a_end;                // A_to_B, B_to_A chains
 };
 std::map<const Ctx*, CmfState*> g_cmf;
 
@@ -2093,16 +2145,162 @@ void stage_modes(Ctx& c, CmfState& S, cplx* out, const cplx* base, const double*
   c.count();
 }
 
-void spf_eval_all(Ctx& c, CmfState& S, cplx* out) {
-  {
-    ProfScope ps(c, KP_H1);
-    launch_h1(S.h1_d, (int)S.h1.size(), c.h1_maxn2, c.h1_smem, false, c.st, c.precision);
+// the same combination on the D vectors of the Gaussian modes (rk_SPF_ck DDtemp)
+void stage_D(Ctx& c, CmfState& S, cplx* out, const cplx* base, const double* coef, int nk) {
+  if (!S.gwp) return;
+  StageArgs a;
+  memset(&a, 0, sizeof(a));
+  int n = 0;
+  for (int j = 0; j < nk; ++j) {
+    if (coef[j] == 0.0) continue;
+    a.k[n] = S.Dk[j];
+    a.c[n] = coef[j];
+    ++n;
   }
-  {
-    ProfScope ps(c, KP_SPF);
-    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision);
+  a.nk = n;
+  ProfScope ps(c, KP_ELEM);
+  launch_stage_modes(out, base, a, S.dt_mode, S.d_elem_mode, 0, S.nD, c.st);
+  c.count();
+}
+
+// Calc_Der_SPF (cmf2_derivatives.f90:84-235) of every mode on the SPFs in d_in
+// (and the D matrices in S.Din) with frozen mean fields: grid modes through the
+// h1 and SPF-tile kernels; Gaussian modes through S00, its Tikhonov inverse,
+// h1mode, C and Y with the frozen density matrices and mean fields, the
+// Tikhonov solve (der_factor * x into out) and dD = -tau D into Dout.
+void spf_eval_all(Ctx& c, CmfState& S, cplx* out, cplx* Dout) {
+  if (!c.modes_dvr.empty()) {
+    {
+      ProfScope ps(c, KP_H1);
+      launch_h1(S.h1_d, (int)S.h1.size(), c.h1_maxn2, c.h1_smem, false, c.st, c.precision);
+    }
+    {
+      ProfScope ps(c, KP_SPF);
+      launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision);
+    }
+    c.count(4);
   }
-  c.count(4);
+  if (S.gwp) {
+    gwp_setup_run(c);
+    gwp_solve_run(c, out);
+    ProfScope ps(c, KP_GWP);
+    launch_gwp_dderiv(S.dder_d, (int)S.dder_h.size(), S.Din, Dout, c.st);
+    c.count();
+  }
+}
+
+// Per state, mode products over the Gaussian modes with mat(i, set), src -> dst:
+// one batch per Gaussian mode (A_to_B / B_to_A, cmf2_base.f90:264-345).
+template <typename F>
+void plan_gwp_chain(Ctx& c, std::vector<ProdBatch>& B, const cplx* src, cplx* dst, F mat) {
+  const int ng = (int)c.modes_gwp.size();
+  B.assign(ng, ProdBatch());
+  for (int s = 0; s < c.nstates; ++s) {
+    std::vector<int> sh = c.shape_of(s);
+    const cplx* cur = src + c.aoff[s];
+    for (int i = 0; i < ng; ++i) {
+      const int m = c.modes_gwp[i];
+      cplx* out = (i + 1 == ng) ? dst + c.aoff[s] : c.ar.calloc_c(c.naconf[s]);
+      B[i].add(cur, out, mat(i, set_of(c, m, s)), sh[m], 0, sh, m, sh[m], mkc(1, 0), 0);
+      cur = out;
+    }
+  }
+  for (auto& b : B) b.finalize(c.ar);
+}
+
+// CMF2 buffers and plans of the Gaussian modes: D vectors, S^-1/2 by Cholesky,
+// D^H h D, dD = -tau D, the SPF error overlaps, A_to_B and B_to_A.
+void plan_cmf_gwp(Ctx& c, CmfState& S, std::vector<unsigned char>& em) {
+  const int f = c.nmodes;
+  const int ng = (int)c.modes_gwp.size();
+  S.gwp = true;
+  std::vector<std::vector<long long>> doff(ng, std::vector<long long>(c.nstates, 0));
+  std::vector<unsigned char> dem;
+  for (int i = 0; i < ng; ++i) {
+    const int m = c.modes_gwp[i];
+    const int nsets = c.multiset[m] ? c.nstates : 1;
+    for (int s = 0; s < nsets; ++s) {
+      const int n = c.m_of(m, s);
+      doff[i][s] = S.nD;
+      S.nD += (long long)n * n;
+      dem.insert(dem.end(), (size_t)n * n, (unsigned char)m);
+      const long long o = c.ipsi[m + f * s], len = (long long)c.nmodedof[m] * n;
+      for (long long q = 0; q < len; ++q) em[o + q] = (unsigned char)m;
+    }
+  }
+  S.DD0 = c.ar.calloc_c(S.nD);
+  S.DDHalf = c.ar.calloc_c(S.nD);
+  S.DDHalf2 = c.ar.calloc_c(S.nD);
+  S.Din = c.ar.calloc_c(S.nD);
+  S.Dtmp = c.ar.calloc_c(S.nD);
+  S.DhS = c.ar.calloc_c(S.nD);
+  for (int j = 0; j < 7; ++j) S.Dk[j] = c.ar.calloc_c(S.nD);
+  S.d_elem_mode = upload_vec(c.ar, dem);
+  for (int i = 0; i < ng; ++i) {
+    const int m = c.modes_gwp[i];
+    const double* a = c.gwpa_d + (size_t)c.gwp_lda * c.ns00max * i;
+    const int nsets = c.multiset[m] ? c.nstates : 1;
+    for (int s = 0; s < nsets; ++s) {
+      const int n = c.m_of(m, s);
+      GwpIsqrtDesc q;
+      memset(&q, 0, sizeof(q));
+      q.S = c.s00[i][s][s];
+      q.D = S.DD0 + doff[i][s];
+      q.DhS = S.DhS + doff[i][s];
+      q.n = n;
+      S.isq_h.push_back(q);
+      GwpDDerivDesc dd;
+      memset(&dd, 0, sizeof(dd));
+      dd.tau = c.tau[i][s];
+      dd.off = doff[i][s];
+      dd.n = n;
+      S.dder_h.push_back(dd);
+      cplx* mat = c.ar.calloc_c((long long)n * n);
+      GwpOvlDesc g;
+      memset(&g, 0, sizeof(g));
+      g.xi1 = psi_block(c, c.d_tmp, m, s);
+      g.xi2 = psi_block(c, c.d_err, m, s);
+      g.a = a;
+      g.out = mat;
+      g.nmd = c.nmodedof[m];
+      g.lda = c.gwp_lda;
+      g.n1 = n;
+      g.n2 = n;
+      g.kind = 3;
+      S.gerr_h.push_back(g);
+      SpfErrDesc ed;
+      ed.ds = mat;
+      ed.rho = c.multiset[m] ? c.rho[m][s] : c.rho_ave[m];
+      ed.n = n;
+      ed.mode = m;
+      S.errd_h.push_back(ed);
+    }
+    for (int k = 0; k < c.noper[m]; ++k) {
+      if (c.is_identity[m + f * k]) continue;
+      const int l = c.oper[m][k][0], r = c.oper[m][k][1];
+      GwpDhdDesc d;
+      memset(&d, 0, sizeof(d));
+      d.h = c.hmat[m][k];
+      d.out = c.dhd[i][k];
+      d.n1 = c.m_of(m, l);
+      d.n2 = c.m_of(m, r);
+      d.same_state = (l == r);
+      d.D1 = S.DD0 + doff[i][set_of(c, m, l)];
+      d.D2 = S.DD0 + doff[i][set_of(c, m, r)];
+      S.dhd0_h.push_back(d);
+      d.D1 = S.DDHalf2 + doff[i][set_of(c, m, l)];
+      d.D2 = S.DDHalf2 + doff[i][set_of(c, m, r)];
+      S.dhd2_h.push_back(d);
+    }
+  }
+  S.isq_d = upload_vec(c.ar, S.isq_h);
+  S.dder_d = upload_vec(c.ar, S.dder_h);
+  S.gerr_d = upload_vec(c.ar, S.gerr_h);
+  S.dhd0_d = upload_vec(c.ar, S.dhd0_h);
+  S.dhd2_d = upload_vec(c.ar, S.dhd2_h);
+  plan_gwp_chain(c, S.a2b, c.d_y, S.B0, [&](int i, int s) { return (const cplx*)(S.DhS + doff[i][s]); });
+  plan_gwp_chain(c, S.b2a_half, S.BHalf, S.AHalf, [&](int i, int s) { return (const cplx*)(S.DDHalf + doff[i][s]); });
+  plan_gwp_chain(c, S.b2a_end, S.B02, c.d_y, [&](int i, int s) { return (const cplx*)(S.DDHalf2 + doff[i][s]); });
 }
 
 void plan_cmf(Ctx& c, CmfState& S) {
@@ -2139,6 +2337,7 @@ void plan_cmf(Ctx& c, CmfState& S) {
       S.errd_h.push_back(ed);
     }
   }
+  if (!c.modes_gwp.empty()) plan_cmf_gwp(c, S, em);
   S.elem_mode = upload_vec(c.ar, em);
   S.err_holes.finalize(c.ar);
   for (auto& hr : hrefs) S.err_red.add_term(hr.target, S.err_holes.h[hr.hole], hr.alpha);
@@ -2152,10 +2351,11 @@ void plan_cmf(Ctx& c, CmfState& S) {
   S.planned = true;
 }
 
-// propagate_SPF for every DVR mode over dt_total, on the psi part of y
-// (cmf2_base.f90:210-260): Cash-Karp (rk_SPF_ck, cmf2_integration.f90:105-253)
-// for int_type_psi 1, Dormand-Prince (rk_SPF_dp, :257-412) for 2.
-void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
+// propagate_SPF for every mode over dt_total, on the psi part of y and, for
+// Gaussian modes, the D matrices in Dy (cmf2_base.f90:210-260): Cash-Karp
+// (rk_SPF_ck, cmf2_integration.f90:105-253) for int_type_psi 1, Dormand-Prince
+// (rk_SPF_dp, :257-412) for 2.
+void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y, cplx* Dy) {
   if (c.int_type_psi != 1 && c.int_type_psi != 2)
     throw StatusError(MCTDH_EUNSUPPORTED, "SPF integrator must be rk45 (1) or dopri (2)");
   const bool dp = c.int_type_psi == 2;
@@ -2164,6 +2364,10 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
   std::vector<double> done(f, 0.0), dtry(f, 0.0), dt_h(64, 0.0), err_h(64, 0.0);
   std::vector<int> active(f, 0), acc_h(64, 0);
   for (int m : c.modes_dvr) {
+    active[m] = 1;
+    dtry[m] = dt_total;
+  }
+  for (int m : c.modes_gwp) {
     active[m] = 1;
     dtry[m] = dt_total;
   }
@@ -2182,19 +2386,24 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
     // iteration (the step lengths live in S.dt_mode), so it runs as a CUDA graph
     run_graphed(c, 1, y, [&] {
       copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
-      spf_eval_all(c, S, c.d_k[0]);
+      if (S.gwp) copy_dev(c, S.Din, Dy, S.nD);
+      spf_eval_all(c, S, c.d_k[0], S.Dk[0]);
       for (int st = 1; st < 6; ++st) {
         stage_modes(c, S, c.d_in, y, dp ? DP_B[st] : CK_B[st], st);
-        spf_eval_all(c, S, c.d_k[st]);
+        stage_D(c, S, S.Din, Dy, dp ? DP_B[st] : CK_B[st], st);
+        spf_eval_all(c, S, c.d_k[st], S.Dk[st]);
       }
       if (dp) {
         // the 7th stage is the derivative at the 5th-order solution (:386-393)
         stage_modes(c, S, c.d_in, y, DP_C, 6);
-        spf_eval_all(c, S, c.d_k[6]);
+        stage_D(c, S, S.Din, Dy, DP_C, 6);
+        spf_eval_all(c, S, c.d_k[6], S.Dk[6]);
         stage_modes(c, S, c.d_tmp, y, DP_C, 6);
+        stage_D(c, S, S.Dtmp, Dy, DP_C, 6);
         stage_modes(c, S, c.d_err, y, DP_D, 7);
       } else {
         stage_modes(c, S, c.d_tmp, y, CK_C, 6);
+        stage_D(c, S, S.Dtmp, Dy, CK_C, 6);
         stage_modes(c, S, c.d_err, y, CK_D, 6);
       }
       StageArgs a;
@@ -2206,6 +2415,10 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
       c.count();
       run_hole(c, S.err_holes);
       run_red(c, S.err_red);
+      if (S.gwp) {
+        launch_gwp_ovl(S.gerr_d, (int)S.gerr_h.size(), c.st);
+        c.count();
+      }
       launch_spf_err(S.errd_d, (int)S.errd_h.size(), S.err_mode, f, c.st);
       c.count();
     });
@@ -2235,13 +2448,16 @@ void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y) {
     CK(cudaMemcpyAsync(S.accept, acc_h.data(), sizeof(int) * 64, cudaMemcpyHostToDevice, c.st));
     launch_masked_copy(y, c.d_tmp, S.elem_mode, S.accept, nA, c.dimpsi, c.st);
     c.count();
+    if (S.gwp) {
+      launch_masked_copy(Dy, S.Dtmp, S.d_elem_mode, S.accept, 0, S.nD, c.st);
+      c.count();
+    }
   }
+  if (S.gwp) check_status(c);
 }
 
 CmfState& cmf_state(Ctx& c) {
   if (c.member) throw StatusError(MCTDH_EUNSUPPORTED, "ensemble members integrate with RK");
-  if (!c.modes_gwp.empty())
-    throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 with Gaussian modes (A_to_B / DD matrices) is not built; use RK");
   CmfState*& Sp = g_cmf[&c];
   if (!Sp) {
     Sp = new CmfState();
@@ -2407,11 +2623,25 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh)
   CmfState& S = cmf_state(c);
   const long long nA = c.naconftot;
   if (!ops_fresh) operators_and_mf(c, c.d_y);       // cmf2_base.f90:78-87
-  copy_dev(c, S.B0, c.d_y, nA);                     // A_to_B (DVR only)
+  if (S.gwp) {
+    // D0 = S^-1/2 (InverseSquareRootU, :63-73), Calc_DHD(DD0) (:87), B0 = D^H S A (:92)
+    ProfScope ps(c, KP_GWP);
+    launch_gwp_isqrt(S.isq_d, (int)S.isq_h.size(), c.d_status, c.st);
+    launch_gwp_dhd(S.dhd0_d, (int)S.dhd0_h.size(), c.st);
+    c.count(2);
+    for (auto& b : S.a2b) run_prod(c, b);
+  } else {
+    copy_dev(c, S.B0, c.d_y, nA);                   // A_to_B: B = A without Gaussian modes
+  }
   lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);      // :97
   copy_dev(c, S.psiHalf, c.d_y, c.ntot);
-  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf);   // :109-115
-  copy_dev(c, S.AHalf, S.BHalf, nA);                // B_to_A  :120
+  if (S.gwp) copy_dev(c, S.DDHalf, S.DD0, S.nD);
+  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf, S.DDHalf);   // :109-115
+  if (S.gwp) {
+    for (auto& b : S.b2a_half) run_prod(c, b);      // B_to_A(AHalf, BHalf, DDHalf)  :120
+  } else {
+    copy_dev(c, S.AHalf, S.BHalf, nA);
+  }
   copy_dev(c, S.AHalf + nA, S.psiHalf + nA, c.dimpsi);
   MfxState* M = nullptr;
   auto it = g_mfx.find(&c);
@@ -2427,7 +2657,8 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh)
     if (M && M->recording) snap_gather(c, *M, M->half);
   }
   copy_dev(c, S.psiHalf2, c.d_y, c.ntot);
-  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2);  // :132-141
+  if (S.gwp) copy_dev(c, S.DDHalf2, S.DD0, S.nD);
+  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2, S.DDHalf2);  // :132-141
   // err_psi = DeltaPsi(AHalf, psiHalf, AHalf, psiHalf2)  (:143)
   copy_dev(c, c.d_tmp, S.AHalf, c.ntot);
   copy_dev(c, c.d_err, S.AHalf, nA);
@@ -2436,8 +2667,12 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh)
   cplx o[3];
   read_ovl(c, c.dpsi_plan, o);
   double err_psi = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x))));
-  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2);  // :148-154
-  h1_only(c, S.psiHalf2);                           // :158-165
+  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2, S.DDHalf2);  // :148-154
+  h1_only(c, S.psiHalf2);                           // :158-163
+  if (S.gwp) {
+    launch_gwp_dhd(S.dhd2_d, (int)S.dhd2_h.size(), c.st);   // Calc_DHD(DDHalf2)  :164
+    c.count();
+  }
   lanczos(c, S.BHalf, S.B02, -0.5 * hdid, true);    // :169
   launch_axpy(S.B02, S.B0, mkc(-1, 0), nA, c.st);
   c.count();
@@ -2451,7 +2686,12 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh)
 // Accept: finish the coefficients with the reused Krylov space (:189) and update.
 void cmf2_accept(Ctx& c, double hdid) {
   CmfState& S = cmf_state(c);
-  lanczos(c, S.BHalf, c.d_y, 0.5 * hdid, false);
+  if (S.gwp) {
+    lanczos(c, S.BHalf, S.B02, 0.5 * hdid, false);
+    for (auto& b : S.b2a_end) run_prod(c, b);       // B_to_A(A0, B0, DDHalf2)  :195
+  } else {
+    lanczos(c, S.BHalf, c.d_y, 0.5 * hdid, false);
+  }
   copy_dev(c, c.d_y + c.naconftot, S.psiHalf2 + c.naconftot, c.dimpsi);
 }
 
@@ -3357,6 +3597,8 @@ int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, const double* fscale,
   return guarded(c, [&] {
     if (mlp && !mlp_has_shape(mlp, MFX_NFEAT, MFX_NOUT))
       throw StatusError(MCTDH_EARG, "the network must map 20 inputs to 4 outputs");
+    if (mlp && !c->modes_gwp.empty())
+      throw StatusError(MCTDH_EUNSUPPORTED, "the mean-field extrapolator covers grid-mode models only");
     MfxState& M = mfx_state(*c);
     M.mlp = mlp;
     if (mlp) {

@@ -167,7 +167,24 @@ __global__ void gwp_ovl_kernel(const GwpOvlDesc* __restrict__ descs) {
   for (int e = threadIdx.x; e < d.n1 * d.n2; e += blockDim.x) {
     const int j1 = e % d.n1, j2 = e / d.n1;
     cplx v;
-    if (d.kind == 0 && j1 == j2) {
+    if (d.kind == 3) {
+      // Calc_Err_SPF (cmf2_derivatives.f90:301-315): 2 - 2 Re<g(x)|g(y)> on the
+      // diagonal, S(x,x) + S(y,y) - S(x,y) - S(y,x) above it
+      if (j1 > j2) continue;
+      const double* a1 = d.a + d.lda * j1;
+      const double* a2 = d.a + d.lda * j2;
+      const cplx* x1 = d.xi1 + d.nmd * j1;
+      const cplx* x2 = d.xi1 + d.nmd * j2;
+      const cplx* y1 = d.xi2 + d.nmd * j1;
+      const cplx* y2 = d.xi2 + d.nmd * j2;
+      if (j1 == j2) {
+        v = mkc(2.0 - 2.0 * gau_ovl(a1, a1, x1, y1, d.nmd).x, 0.0);
+      } else {
+        v = cadd(gau_ovl(a1, a2, x1, x2, d.nmd), gau_ovl(a1, a2, y1, y2, d.nmd));
+        v = csub(v, gau_ovl(a1, a2, x1, y2, d.nmd));
+        v = csub(v, gau_ovl(a1, a2, y1, x2, d.nmd));
+      }
+    } else if (d.kind == 0 && j1 == j2) {
       v = mkc(1.0, 0.0);
     } else if (d.kind == 0 && j1 > j2) {
       v = cconj(gau_ovl(d.a + d.lda * j2, d.a + d.lda * j1, d.xi1 + d.nmd * j2, d.xi2 + d.nmd * j1, d.nmd));
@@ -575,6 +592,160 @@ void launch_tikh_inv(const RegInvDesc* d, int nd, cudaStream_t st) {
     configured = true;
   }
   tikh_inv_kernel<<<nd, 256, smem, st>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// CMF2 with Gaussian modes
+// ---------------------------------------------------------------------------
+// D = S^-1/2 in the Cholesky form of InverseSquareRootU (maths.f90:621-644):
+// S = U^H U (zpotrf 'U', column by column as the unblocked zpotf2), D = U^-1
+// (ztrtri 'U','N', columns from the already inverted leading block as ztrti2),
+// zeros below the diagonal; and DhS = D^H S, the matrix of A_to_B
+// (cmf2_base.f90:288-292, B = (S D)^H A).  One block per (mode, set), n <= 32.
+__global__ void __launch_bounds__(1024) gwp_isqrt_kernel(const GwpIsqrtDesc* __restrict__ descs, int* status) {
+  const GwpIsqrtDesc& d = descs[blockIdx.x];
+  const int n = d.n;
+  __shared__ cplx U[MAXN_SPF][MAXN_SPF + 1];   // U[row][col]
+  __shared__ cplx X[MAXN_SPF][MAXN_SPF + 1];   // U^-1
+  __shared__ int bad;
+  const int tid = threadIdx.x;
+  if (tid == 0) bad = 0;
+  for (int e = tid; e < MAXN_SPF * MAXN_SPF; e += blockDim.x) {
+    const int r = e % MAXN_SPF, col = e / MAXN_SPF;
+    U[r][col] = (r < n && col < n && r <= col) ? d.S[r + n * col] : mkc(0.0, 0.0);
+    X[r][col] = mkc(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (tid < 32) {
+      // U(j,j) = sqrt(S(j,j) - sum_{q<j} |U(q,j)|^2)
+      double part = 0.0;
+      for (int q = tid; q < j; q += 32) part += U[q][j].x * U[q][j].x + U[q][j].y * U[q][j].y;
+      for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
+      if (tid == 0) {
+        const double ajj = U[j][j].x - part;
+        if (!(ajj > 0.0)) bad = 1;
+        U[j][j] = mkc(sqrt(fabs(ajj)), 0.0);
+      }
+    }
+    __syncthreads();
+    // row j right of the diagonal: (S(j,k) - sum_{q<j} conj(U(q,j)) U(q,k)) / U(j,j)
+    const double rinv = 1.0 / U[j][j].x;
+    for (int k = j + 1 + tid; k < n; k += blockDim.x) {
+      cplx v = U[j][k];
+      for (int q = 0; q < j; ++q) v = csub(v, cmul(cconj(U[q][j]), U[q][k]));
+      U[j][k] = cscale(v, rinv);
+    }
+    __syncthreads();
+  }
+  for (int j = tid; j < n; j += blockDim.x) X[j][j] = mkc(1.0 / U[j][j].x, 0.0);
+  __syncthreads();
+  for (int j = 1; j < n; ++j) {
+    // X(0:j-1, j) = -X(0:j-1, 0:j-1) U(0:j-1, j) X(j,j)
+    for (int i = tid; i < j; i += blockDim.x) {
+      cplx v = mkc(0.0, 0.0);
+      for (int q = i; q < j; ++q) v = cadd(v, cmul(X[i][q], U[q][j]));
+      X[i][j] = cscale(v, -X[j][j].x);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int r = e % n, col = e / n;
+    d.D[e] = X[r][col];
+    // (D^H S)(r, col) = sum_q conj(D(q, r)) S(q, col), S Hermitian from its upper triangle
+    cplx v = mkc(0.0, 0.0);
+    for (int q = 0; q <= r; ++q) {
+      const cplx sq = (q <= col) ? d.S[q + n * col] : cconj(d.S[col + n * q]);
+      v = cadd(v, cmul(cconj(X[q][r]), sq));
+    }
+    d.DhS[e] = v;
+  }
+  if (tid == 0 && bad) atomicOr(status, DEVST_CHOL_FAIL);
+}
+
+// Calc_DHD (hamilton.f90:535-574): same state, 1/2 (D^H (h D) + (h D)^H D) with h
+// Hermitian from its upper triangle (zhemm + zher2k), real diagonal; across
+// states (D1^H h) D2.  Entries of modulus <= DBL_EPSILON become zero (the
+// reference's clean-up, on the upper triangle for the Hermitian case, which is
+// then mirrored into the full matrix the mode products use).
+__global__ void __launch_bounds__(1024) gwp_dhd_kernel(const GwpDhdDesc* __restrict__ descs) {
+  const GwpDhdDesc& d = descs[blockIdx.x];
+  const int n1 = d.n1, n2 = d.n2;
+  __shared__ cplx aux[MAXN_SPF][MAXN_SPF + 1];
+  __shared__ cplx res[MAXN_SPF][MAXN_SPF + 1];
+  const int tid = threadIdx.x;
+  if (d.same_state) {
+    for (int e = tid; e < n1 * n2; e += blockDim.x) {   // aux = h D
+      const int a = e % n1, b = e / n1;
+      cplx v = mkc(0.0, 0.0);
+      for (int q = 0; q < n1; ++q) {
+        const cplx hq = (a <= q) ? d.h[a + n1 * q] : cconj(d.h[q + n1 * a]);
+        v = cadd(v, cmul(hq, d.D2[q + n2 * b]));
+      }
+      aux[a][b] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < n1 * n2; e += blockDim.x) {
+      const int a = e % n1, b = e / n1;
+      if (a > b) continue;
+      cplx v = mkc(0.0, 0.0);
+      for (int q = 0; q < n1; ++q) {
+        v = cadd(v, cmul(cconj(d.D1[q + n1 * a]), aux[q][b]));
+        v = cadd(v, cmul(cconj(aux[q][a]), d.D1[q + n1 * b]));
+      }
+      v = cscale(v, 0.5);
+      if (a == b) v.y = 0.0;
+      if (!(sqrt(v.x * v.x + v.y * v.y) > DBL_EPSILON)) v = mkc(0.0, 0.0);
+      res[a][b] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < n1 * n2; e += blockDim.x) {
+      const int a = e % n1, b = e / n1;
+      d.out[e] = (a <= b) ? res[a][b] : cconj(res[b][a]);
+    }
+  } else {
+    for (int e = tid; e < n1 * n2; e += blockDim.x) {   // aux = D1^H h
+      const int a = e % n1, b = e / n1;
+      cplx v = mkc(0.0, 0.0);
+      for (int q = 0; q < n1; ++q) v = cadd(v, cmul(cconj(d.D1[q + n1 * a]), d.h[q + n1 * b]));
+      aux[a][b] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < n1 * n2; e += blockDim.x) {
+      const int a = e % n1, b = e / n1;
+      cplx v = mkc(0.0, 0.0);
+      for (int q = 0; q < n2; ++q) v = cadd(v, cmul(aux[a][q], d.D2[q + n2 * b]));
+      if (!(sqrt(v.x * v.x + v.y * v.y) > DBL_EPSILON)) v = mkc(0.0, 0.0);
+      d.out[e] = v;
+    }
+  }
+}
+
+// dD = -tau D per (mode, set) block of the D vectors (cmf2_derivatives.f90:228)
+__global__ void gwp_dderiv_kernel(const GwpDDerivDesc* __restrict__ descs, const cplx* __restrict__ Din,
+                                  cplx* __restrict__ Dout) {
+  const GwpDDerivDesc& d = descs[blockIdx.x];
+  const int n = d.n;
+  const cplx* D = Din + d.off;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int a = e % n, b = e / n;
+    cplx v = mkc(0.0, 0.0);
+    for (int q = 0; q < n; ++q) v = cadd(v, cmul(d.tau[a + n * q], D[q + n * b]));
+    Dout[d.off + e] = mkc(-v.x, -v.y);
+  }
+}
+
+void launch_gwp_isqrt(const GwpIsqrtDesc* d, int nd, int* status, cudaStream_t st) {
+  if (nd <= 0) return;
+  gwp_isqrt_kernel<<<nd, 1024, 0, st>>>(d, status);
+}
+void launch_gwp_dhd(const GwpDhdDesc* d, int nd, cudaStream_t st) {
+  if (nd <= 0) return;
+  gwp_dhd_kernel<<<nd, 1024, 0, st>>>(d);
+}
+void launch_gwp_dderiv(const GwpDDerivDesc* d, int nd, const cplx* Din, cplx* Dout, cudaStream_t st) {
+  if (nd <= 0) return;
+  gwp_dderiv_kernel<<<nd, 256, 0, st>>>(d, Din, Dout);
 }
 
 void launch_gwp_ovl(const GwpOvlDesc* d, int nd, cudaStream_t st) {

@@ -248,7 +248,9 @@ struct GwpOvlDesc {      // S(j1, j2) = <g1_j1 | g2_j2> (normalised), n1 x n2 (l
   cplx* out;
   int nmd, lda, n1, n2;
   int kind;              // 0: same parameter set (diagonal 1, lower = conj upper); 1: full;
-                         // 2: conjugate transpose of the full overlap with the sets swapped
+                         // 2: conjugate transpose of the full overlap with the sets swapped;
+                         // 3: overlap of the difference of two parameter sets xi1 - xi2 (upper
+                         //    triangle, Calc_Err_SPF, cmf2_derivatives.f90:294-315)
   int pad;
 };
 struct GwpH1Desc {       // h1mode of a Gaussian mode (hamilton.f90:494-524)
@@ -296,3 +298,26 @@ void launch_gwp_h1(const GwpH1Desc* d, int nd, cudaStream_t st);
 void launch_gwp_cy(const GwpCYDesc* d, int nd, int maxG, int maxn, int maxops, const GwpYOp* ops, cplx* part,
                    cudaStream_t st);
 void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out, int* status, cudaStream_t st);
+
+// CMF2 with Gaussian modes (cmf2_base.f90, cmf2_derivatives.f90)
+struct GwpIsqrtDesc {    // D = U^-1 with S = U^H U (InverseSquareRootU, maths.f90:621-644), DhS = D^H S
+  const cplx* S;         // n x n, upper triangle authoritative
+  cplx* D;
+  cplx* DhS;
+  int n, pad;
+};
+struct GwpDhdDesc {      // D1^H h D2 for one operator of a Gaussian mode (Calc_DHD, hamilton.f90:535-574)
+  const cplx* h;         // n1 x n2 (full)
+  const cplx* D1;        // n1 x n1
+  const cplx* D2;        // n2 x n2
+  cplx* out;             // n1 x n2 (full; Hermitian when same_state)
+  int n1, n2, same_state, pad;
+};
+struct GwpDDerivDesc {   // dD = -tau D for one (Gaussian mode, set) block (cmf2_derivatives.f90:228)
+  const cplx* tau;
+  long long off;         // offset of the block in the D vectors
+  int n, pad;
+};
+void launch_gwp_isqrt(const GwpIsqrtDesc* d, int nd, int* status, cudaStream_t st);
+void launch_gwp_dhd(const GwpDhdDesc* d, int nd, cudaStream_t st);
+void launch_gwp_dderiv(const GwpDDerivDesc* d, int nd, const cplx* Din, cplx* Dout, cudaStream_t st);

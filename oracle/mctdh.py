@@ -591,19 +591,10 @@ class Oracle:
                 js = s if md.multiset[mode] else 0
                 nmd = len(md.mode_dofs[mode])
                 ns = int(md.nspf[mode, s])
-                Sa0Sm1 = self.Sa0Sm1[(i, js)]
                 op = int(md.ipsispf[mode, s])
                 dxi = dpsi[op:op + nmd * ns].reshape((nmd, ns), order="F")
                 xi = psi[op:op + nmd * ns].reshape((nmd, ns), order="F")
-                tau = np.zeros((ns, ns), dtype=np.complex128)
-                for j2 in range(ns):
-                    for j1 in range(ns):
-                        tau[j1, j2] = np.vdot(Sa0Sm1[j2 * nmd:(j2 + 1) * nmd, j1], dxi[:, j2])
-                for j2 in range(ns):
-                    dd = 0.0
-                    for k in range(nmd):
-                        dd += xi[k, j2].real * dxi[k, j2].real / md.gwpa[k, j2, i]
-                    tau[j2, j2] += dd * 0.5
+                tau = self._gwp_tau(i, js, xi, dxi)
                 X = X - mode_product(tau, A0, mode)
             dA[o:o + n] = X.reshape(-1, order="F")
         return dA, dpsi
@@ -1028,6 +1019,20 @@ class Oracle:
         self.dvr_spf_derivative(psi, mode, dpsi)
         return dpsi
 
+    @staticmethod
+    def _trace_rho(rho: np.ndarray, ovl: np.ndarray) -> float:
+        """Tr(rho . ovl) over the upper triangle (cmf2_derivatives.f90:278-291)."""
+        err = 0.0
+        n = ovl.shape[0]
+        for j2 in range(n):
+            for j1 in range(j2):
+                err += 2 * float((rho[j1, j2] * np.conj(ovl[j1, j2])).real)
+            err += float((rho[j2, j2] * ovl[j2, j2]).real)
+        return err
+
+    def _rho_of(self, mode: int, s: int) -> np.ndarray:
+        return self.rho[(mode, s)] if self.m.multiset[mode] else self.rho_ave[mode]
+
     def calc_err_spf_dvr(self, psi1, psi2, mode) -> float:
         """Calc_Err_SPF, DVR branch (cmf2_derivatives.f90:239-283)."""
         md = self.m
@@ -1035,49 +1040,133 @@ class Oracle:
         states = range(md.nstates) if md.multiset[mode] else [0]
         for s in states:
             d = md.spf_block(psi1, mode, s) - md.spf_block(psi2, mode, s)
-            ovl = d.conj().T @ d
-            rho = self.rho[(mode, s)] if md.multiset[mode] else self.rho_ave[mode]
-            n = ovl.shape[0]
-            for j2 in range(n):
-                for j1 in range(j2):
-                    err += 2 * float((rho[j1, j2] * np.conj(ovl[j1, j2])).real)
-                err += float((rho[j2, j2] * ovl[j2, j2]).real)
+            err += self._trace_rho(self._rho_of(mode, s), d.conj().T @ d)
         return math.sqrt(abs(err))
+
+    def calc_err_spf_gwp(self, psi1, psi2, i) -> float:
+        """Calc_Err_SPF, Gaussian branch (cmf2_derivatives.f90:294-332): the
+        overlap of the parameter difference from Gaussian overlaps."""
+        md = self.m
+        mode = md.modes_gwp[i]
+        err = 0.0
+        states = range(md.nstates) if md.multiset[mode] else [0]
+        for s in states:
+            x, a = self.gwp_params(psi1, i, s)
+            y, _ = self.gwp_params(psi2, i, s)
+            ns = x.shape[1]
+            ovl = np.zeros((ns, ns), dtype=np.complex128)
+            for j in range(ns):
+                ovl[j, j] = 2.0 - 2.0 * gau_ovl_multid(a[:, j], a[:, j], x[:, j], y[:, j]).real
+            for j2 in range(ns):
+                for j1 in range(j2):
+                    g = lambda u, v: gau_ovl_multid(a[:, j1], a[:, j2], u, v)
+                    ovl[j1, j2] = g(x[:, j1], x[:, j2]) + g(y[:, j1], y[:, j2]) \
+                        - g(x[:, j1], y[:, j2]) - g(y[:, j1], x[:, j2])
+            err += self._trace_rho(self._rho_of(mode, s), ovl)
+        return math.sqrt(abs(err))
+
+    def _gwp_tau(self, i: int, s: int, xi: np.ndarray, dxi: np.ndarray) -> np.ndarray:
+        """tau = (Sa0 S^-1)^H dxi per Gaussian plus the phase term
+        1/2 sum_k Re xi Re dxi / a on the diagonal (derivatives.f90:201-234,
+        cmf2_derivatives.f90:207-226)."""
+        md = self.m
+        mode = md.modes_gwp[i]
+        nmd = len(md.mode_dofs[mode])
+        ns = xi.shape[1]
+        Sa0Sm1 = self.Sa0Sm1[(i, s)]
+        tau = np.zeros((ns, ns), dtype=np.complex128)
+        for j2 in range(ns):
+            for j1 in range(ns):
+                tau[j1, j2] = np.vdot(Sa0Sm1[j2 * nmd:(j2 + 1) * nmd, j1], dxi[:, j2])
+        for j2 in range(ns):
+            dd = 0.0
+            for k in range(nmd):
+                dd += xi[k, j2].real * dxi[k, j2].real / md.gwpa[k, j2, i]
+            tau[j2, j2] += dd * 0.5
+        return tau
+
+    def calc_der_spf_gwp(self, psi: np.ndarray, DD: Dict, i: int):
+        """Calc_Der_SPF, Gaussian branch (cmf2_derivatives.f90:175-232): S00, its
+        Tikhonov inverse, h1mode and C, Y on the current parameters with the
+        frozen density matrices and mean fields; the Tikhonov solve times
+        der_factor; dD = -tau D."""
+        md = self.m
+        mode = md.modes_gwp[i]
+        self.calc_s00(psi, i)
+        self.calc_s00m1(i)
+        self.calc_h1mode(psi, mode)
+        self.calc_cy(psi, i)
+        nmd = len(md.mode_dofs[mode])
+        dpsi = np.zeros(md.dimpsi, dtype=np.complex128)
+        dDD = {}
+        states = range(md.nstates) if md.multiset[mode] else [0]
+        for s in states:
+            ns = int(md.nspf[mode, s])
+            x = md.der_factor * std_reg_sol(self.Cmat[(i, s)], self.Yvec[(i, s)], md.eps_C, "tikh")
+            o = int(md.ipsispf[mode, s])
+            dpsi[o:o + len(x)] = x
+            xi = psi[o:o + nmd * ns].reshape((nmd, ns), order="F")
+            tau = self._gwp_tau(i, s, xi, x.reshape((nmd, ns), order="F"))
+            dDD[(i, s)] = -tau @ DD[(i, s)]
+        return dpsi, dDD
 
     def _spf_slices(self, mode):
         md = self.m
         states = range(md.nstates) if md.multiset[mode] else [0]
+        rows = len(md.mode_dofs[mode]) if md.is_gwp_mode[mode] else md.ngpm[mode]
         out = []
         for s in states:
             o = int(md.ipsispf[mode, s])
-            n = int(md.nspf[mode, s]) * md.ngpm[mode]
+            n = int(md.nspf[mode, s]) * rows
             out.append(slice(o, o + n))
         return out
 
-    def rk_spf_ck(self, psi: np.ndarray, mode: int, htry: float, dopri: bool = False):
-        """rk_SPF_ck / rk_SPF_dp, DVR branch (cmf2_integration.f90:105-253, :257-412).
-        Dormand-Prince adds a 7th derivative at the 5th-order solution (:386-393)."""
+    def rk_spf_ck(self, psi: np.ndarray, mode: int, htry: float, dopri: bool = False, DD: Optional[Dict] = None):
+        """rk_SPF_ck / rk_SPF_dp (cmf2_integration.f90:105-253, :257-412).
+        Dormand-Prince adds a 7th derivative at the 5th-order solution (:386-393).
+        Gaussian modes carry their D matrices along (DDtemp, dDD)."""
         md = self.m
         sl = self._spf_slices(mode)
         tab = DP if dopri else CK
+        gwp = md.is_gwp_mode[mode]
+        i = md.modes_gwp.index(mode) if gwp else -1
+        keys = [(i, s) for s in (range(md.nstates) if md.multiset[mode] else [0])] if gwp else []
+
+        def der(p, D):
+            if gwp:
+                return self.calc_der_spf_gwp(p, D, i)
+            return self.calc_der_spf_dvr(p, mode), {}
+
+        def comb(p0, D0, coef, kp, kd):
+            p = p0.copy()
+            for s_ in sl:
+                p[s_] = p0[s_] + dt * sum(cj * kp[j][s_] for j, cj in enumerate(coef) if cj != 0.0)
+            D = dict(D0) if D0 is not None else None
+            for key in keys:
+                D[key] = D0[key] + dt * sum(cj * kd[j][key] for j, cj in enumerate(coef) if cj != 0.0)
+            return p, D
+
         dt = htry
         while True:
-            k = [self.calc_der_spf_dvr(psi, mode)]
+            kp, kd = [], []
+            d1, d2 = der(psi, DD)
+            kp.append(d1)
+            kd.append(d2)
             for st in range(1, 6):
-                b = tab["B"][st]
-                pt = psi.copy()
-                for s_ in sl:
-                    pt[s_] = psi[s_] + dt * sum(b[j] * k[j][s_] for j in range(len(b)))
-                k.append(self.calc_der_spf_dvr(pt, mode))
-            ptemp = psi.copy()
-            perr = psi.copy()
-            for s_ in sl:
-                ptemp[s_] = psi[s_] + dt * sum(cj * k[j][s_] for j, cj in enumerate(tab["C"]) if cj != 0.0)
+                pt, Dt = comb(psi, DD, tab["B"][st], kp, kd)
+                d1, d2 = der(pt, Dt)
+                kp.append(d1)
+                kd.append(d2)
+            ptemp, Dtemp = comb(psi, DD, tab["C"], kp, kd)
             if dopri:
-                k.append(self.calc_der_spf_dvr(ptemp, mode))
-            for s_ in sl:
-                perr[s_] = psi[s_] + dt * sum(dj * k[j][s_] for j, dj in enumerate(tab["D"]) if dj != 0.0)
-            error = self.calc_err_spf_dvr(ptemp, perr, mode) / md.eps_psi
+                d1, d2 = der(ptemp, Dtemp)
+                kp.append(d1)
+                kd.append(d2)
+            perr, _ = comb(psi, DD, tab["D"], kp, kd)
+            if gwp:
+                error = self.calc_err_spf_gwp(ptemp, perr, i) / md.eps_psi
+            else:
+                error = self.calc_err_spf_dvr(ptemp, perr, mode) / md.eps_psi
             if error < 1.0:
                 break
             dt = max(RK_MINSCAL * dt, RK_SAFETY * dt * error ** RK_PSHRNK)
@@ -1088,24 +1177,69 @@ class Oracle:
         out = psi.copy()
         for s_ in sl:
             out[s_] = ptemp[s_]
-        return out, dt, hnext
+        if gwp:
+            DD = dict(DD)
+            for key in keys:
+                DD[key] = Dtemp[key]
+        return out, dt, hnext, DD
 
-    def propagate_spf(self, dt: float, mode: int, psi: np.ndarray) -> np.ndarray:
-        """propagate_SPF (cmf2_base.f90:210-260): Cash-Karp (1) or Dormand-Prince (2)."""
+    def propagate_spf(self, dt: float, mode: int, psi: np.ndarray, DD: Optional[Dict] = None):
+        """propagate_SPF (cmf2_base.f90:210-260): Cash-Karp (1) or Dormand-Prince (2).
+        Returns psi, or (psi, DD) when D matrices are given."""
         md = self.m
         if md.int_type_psi not in (1, 2):
             raise OracleError("SPF integrator must be rk45 (1) or dopri (2)")
         done = 0.0
         step = dt
         while True:
-            psi, sdone, snext = self.rk_spf_ck(psi, mode, step, dopri=md.int_type_psi == 2)
+            psi, sdone, snext, DD = self.rk_spf_ck(psi, mode, step, dopri=md.int_type_psi == 2, DD=DD)
             done += sdone
             if done >= dt:
                 break
             snext = max(snext, md.min_stepsize * 2)
             step = (dt - done) / (int((dt - done) / snext) + 1)
             step = min(step, dt - done)
-        return psi
+        return psi if DD is None else (psi, DD)
+
+    def _propagate_spf_all(self, dt, psi, DD):
+        """DVR modes, then Gaussian modes (cmf2_base.f90:108-115)."""
+        md = self.m
+        for mode in md.modes_dvr:
+            psi = self.propagate_spf(dt, mode, psi)
+        for mode in md.modes_gwp:
+            psi, DD = self.propagate_spf(dt, mode, psi, DD)
+        return psi, DD
+
+    def _gwp_chain(self, X: np.ndarray, mats: Dict) -> np.ndarray:
+        """Per state, mode products with mats[(i, set)] on the Gaussian modes."""
+        md = self.m
+        out = X.copy()
+        for s in range(md.nstates):
+            o = int(md.astate_offset[s])
+            T = md.a_state(X, s)
+            for i, mode in enumerate(md.modes_gwp):
+                T = mode_product(mats[(i, s if md.multiset[mode] else 0)], T, mode)
+            out[o:o + int(md.naconf[s])] = T.reshape(-1, order="F")
+        return out
+
+    def a_to_b(self, A: np.ndarray, DD: Dict) -> np.ndarray:
+        """A_to_B (cmf2_base.f90:264-305): B = D^H S A on the Gaussian modes."""
+        mats = {key: D.conj().T @ self.s00(key[0], key[1], key[1]) for key, D in DD.items()}
+        return self._gwp_chain(A, mats)
+
+    def b_to_a(self, B: np.ndarray, DD: Dict) -> np.ndarray:
+        """B_to_A (cmf2_base.f90:309-345): A = D B on the Gaussian modes."""
+        return self._gwp_chain(B, DD)
+
+    def _inverse_sqrt_s00(self) -> Dict:
+        """D = S^-1/2 by Cholesky (InverseSquareRootU) per Gaussian mode and set
+        (cmf2_base.f90:63-73)."""
+        md = self.m
+        DD = {}
+        for i, mode in enumerate(md.modes_gwp):
+            for s in (range(md.nstates) if md.multiset[mode] else [0]):
+                DD[(i, s)] = inverse_square_root_u(np.triu(self.S00[i][(s, s)]))
+        return DD
 
     def _operators_and_mf(self, A, psi, t):
         self._prepare(A, psi)
@@ -1117,44 +1251,56 @@ class Oracle:
         return self.cmf2(A, psi, t, h, fixed=True)
 
     def cmf2(self, A, psi, t, htry, fixed=False):
-        """cmf2 (cmf2_base.f90:47-206) for DVR-only models.  Returns (A, psi, hdid, hnext, tries);
-        with fixed=True one attempt of length htry is completed: (A, psi, error)."""
+        """cmf2 (cmf2_base.f90:47-206).  Returns (A, psi, hdid, hnext, tries);
+        with fixed=True one attempt of length htry is completed: (A, psi, error).
+        Gaussian modes propagate in the orthonormalised coefficients B = D^H S A
+        with D = S^-1/2 recomputed at the step start."""
         md = self.m
-        if md.modes_gwp:
-            raise OracleError("CMF2 with GWP modes is not restated")
+        gwp = bool(md.modes_gwp)
+        DD0 = {}
+        if gwp:
+            self.S00 = {}
+            for i in range(len(md.modes_gwp)):
+                self.calc_s00(psi, i)
+            DD0 = self._inverse_sqrt_s00()
         hdid = htry
         tries = 0
         while True:
             tries += 1
             self._operators_and_mf(A, psi, t)
-            B0 = A.copy()
+            if gwp:
+                self.calc_dhd(DD0)
+                B0 = self.a_to_b(A, DD0)
+            else:
+                B0 = A.copy()
             BHalf = self.lanczos(B0, 0.5 * hdid, True)
-            psiHalf = psi.copy()
-            for mode in md.modes_dvr:
-                psiHalf = self.propagate_spf(0.5 * hdid, mode, psiHalf)
-            AHalf = BHalf.copy()
+            psiHalf, DDHalf = self._propagate_spf_all(0.5 * hdid, psi.copy(), dict(DD0))
+            AHalf = self.b_to_a(BHalf, DDHalf) if gwp else BHalf.copy()
             self._operators_and_mf(AHalf, psiHalf, t + 0.5 * hdid)
-            psiHalf2 = psi.copy()
-            for mode in md.modes_dvr:
-                psiHalf2 = self.propagate_spf(0.5 * hdid, mode, psiHalf2)
+            psiHalf2, DDHalf2 = self._propagate_spf_all(0.5 * hdid, psi.copy(), dict(DD0))
             err_psi = self.delta_psi(AHalf, psiHalf, AHalf, psiHalf2)
-            for mode in md.modes_dvr:
-                psiHalf2 = self.propagate_spf(0.5 * hdid, mode, psiHalf2)
+            psiHalf2, DDHalf2 = self._propagate_spf_all(0.5 * hdid, psiHalf2, DDHalf2)
+            if gwp:
+                for i in range(len(md.modes_gwp)):
+                    self.calc_s00(psiHalf2, i)
             self.h1mode = {}
             for mode in range(md.nmodes):
                 self.calc_h1mode(psiHalf2, mode)
+            if gwp:
+                self.calc_dhd(DDHalf2)
             B02 = self.lanczos(BHalf, -0.5 * hdid, True)
             err_A = np.linalg.norm(B02 - B0) * 0.5
             error = max(err_A, err_psi) / md.eps_int
             if fixed:
-                return self.lanczos(BHalf, 0.5 * hdid, False), psiHalf2, error
+                Bend = self.lanczos(BHalf, 0.5 * hdid, False)
+                return (self.b_to_a(Bend, DDHalf2) if gwp else Bend), psiHalf2, error
             if error > 1.0:
                 hdid = hdid / math.sqrt(error) * 0.95
                 continue
             Bend = self.lanczos(BHalf, 0.5 * hdid, False)
             hnext = min(hdid / math.sqrt(error), hdid * 1.5) if error > 0 else hdid * 1.5
             hnext = min(hnext, md.tout)
-            return Bend, psiHalf2, hdid, hnext, tries
+            return (self.b_to_a(Bend, DDHalf2) if gwp else Bend), psiHalf2, hdid, hnext, tries
 
     # ---------------- observables and driver ----------------
     def observables(self, A, psi, A0, psi0, t):

@@ -90,14 +90,39 @@ def test_gwp_rk45_free_running(core_cls):
     _compare(outs, ref, 10 * model.eps_int)
 
 
-def test_gwp_cmf2_is_refused(core_cls):
-    """CMF2 with Gaussian modes needs the D-matrix transformation (A_to_B), which
-    this build does not have: the call fails with -1 instead of running."""
-    from macaw_gb300.capi import MctdhError
-    model = small_gmctdh()
+def _cmf2_model(tfinal_fs=1.0):
+    model = small_gmctdh(tfinal_fs=tfinal_fs)
+    model.int_type = INT_CMF2
+    return model
+
+
+@pytest.mark.parametrize("int_type_psi", [1, 2])
+def test_gwp_cmf2_step(core_cls, int_type_psi):
+    """One CMF2 step of the Gaussian model (cmf2_base.f90:47-206): D = S^-1/2 by
+    Cholesky, B = D^H S A, Lanczos with D^H h D, the Gaussian parameters and D
+    integrated with Cash-Karp (1) or Dormand-Prince (2), A = D B at the end."""
+    model = _cmf2_model()
+    model.int_type_psi = int_type_psi
+    A, psi = random_state(model, seed=7, gwp_shift=0.05)
+    rA, rp, rh, rn, tries = Oracle(model).cmf2(A, psi, 0.0, 0.2)
+    gA, gp, gh, gn = core_cls(model).cmf2(A, psi, 0.0, 0.2)
+    assert gh == rh
+    assert abs(gn - rn) <= 1e-4 * rn   # hnext uses err_psi = DeltaPsi (rounding-floor noise)
+    assert np.abs(gA - rA).max() < 1e-10
+    assert np.abs(gp - rp).max() < 1e-10
+
+
+def test_gwp_cmf2_propagation(core_cls):
+    """CMF2 over 0.5 fs from the single-configuration start: on the oracle's step
+    sequence within 1e-10, free running within 10 eps_int."""
+    model = _cmf2_model(tfinal_fs=0.5)
     A, psi = initial_wavefunction(model)
-    core = core_cls(model)
-    core.set_state(A, psi, as_start=True)
-    with pytest.raises(MctdhError) as e:
-        core.step(INT_CMF2, 0.0, 1.0)
-    assert e.value.code == -1
+    ref, steps, _ = Oracle(model).propagate(A, psi, record_steps=True)
+    gpu = core_cls(model)
+    outs, errs = _replay(gpu, model, A, psi, steps, lambda A, psi, t, h: gpu.cmf2_attempt(A, psi, t, h))
+    # err_psi = sqrt(2 (1 - Re<1|2>/..)) with 1 - Re<1|2> ~ eps_int^2: FP64 rounding
+    # of the overlaps (1e-16) moves the accepted steps' error by up to ~1e-4 relative
+    assert max(errs) <= 1.0 + 1e-3
+    _compare(outs, ref, 1e-10)
+    outs = core_cls(model).propagate(A, psi)
+    _compare(outs, ref, 10 * model.eps_int)
