@@ -61,6 +61,15 @@ typedef struct mctdh_setup {
   int64_t int_type_psi;                 /* 1 = Cash-Karp for the CMF2 SPF sweeps  */
   int64_t precision;                    /* 0 = FP64, 1 = split-FP32 contractions  */
   int64_t int_order, int_par1;          /* Adams PECE order and extra EC iterations (abm<order><par1>) */
+  /* Operators whose expectation values are written (the 'expect' keyword,
+   * input.f90:196-216, terms read by Read_Operators, input.f90:516-748).  Their
+   * mode operators are entries of oper after the Hamiltonian's (hamilton.f90:139-161). */
+  int64_t nexpect;
+  const int64_t *expect_nterms;  /* nOpTerms(nexpect)                                    */
+  const double *expect_ae;       /* aeExtra, the terms of all operators concatenated, complex */
+  const int64_t *expect_lhs;     /* lhs_elExtra, 0-based, concatenated                   */
+  const int64_t *expect_rhs;     /* rhs_elExtra                                          */
+  const int64_t *expect_ioper;   /* iOperExtra(nmodes, total terms), 0-based             */
 } mctdh_setup_t;
 
 /* Build the device context: uploads the operators, plans the batched kernels
@@ -149,6 +158,19 @@ int64_t mctdh_profile_read(mctdh_ctx_t *ctx, int64_t kid, double *ms, int64_t *l
  * norm = sum(pop), and C(t) = <Psi(0)|Psi(t)>. */
 int64_t mctdh_observables(mctdh_ctx_t *ctx, double t, double *energy, double *pop, double *norm,
                           double *auto_re, double *auto_im);
+
+/* The rest of WriteOutput for the resident state, computed on the device (only
+ * the results are copied back):
+ * - mctdh_expect: Expectation (output.f90:449-500), values[i] = sum_t ae_t <A_l| prod_m h_m |A_r>
+ *   of expectation operator i (nexpect interleaved complex values);
+ * - mctdh_natpop: natural populations natpop(nspfmax, nmodes, nstates), decreasing, with
+ *   nspfmax = max nSPF; for Gaussian modes the gross Gaussian populations and the population
+ *   errors ggp, poperr(ns00max, nmodgwp, nstates) (output.f90:88-140); ggp/poperr may be NULL;
+ * - mctdh_densmat: the reduced density matrix rho(mode, state) as written to the densmat
+ *   file (output.f90:276-300), n x n interleaved complex, both triangles filled. */
+int64_t mctdh_expect(mctdh_ctx_t *ctx, double *values);
+int64_t mctdh_natpop(mctdh_ctx_t *ctx, double *natpop, double *ggp, double *poperr);
+int64_t mctdh_densmat(mctdh_ctx_t *ctx, int64_t mode, int64_t state, double *rho);
 
 /* norm_wf (gmctdh_objects.f90:21) and WF_Ovl (gmctdh_objects.f90:101) on host buffers. */
 int64_t mctdh_norm_wf(mctdh_ctx_t *ctx, const double *A, const double *psi, double *norm);

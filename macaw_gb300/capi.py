@@ -48,6 +48,8 @@ class Setup(C.Structure):
         ("writetime", C.c_double), ("der_factor_re", C.c_double), ("der_factor_im", C.c_double),
         ("int_type_psi", C.c_int64), ("precision", C.c_int64),
         ("int_order", C.c_int64), ("int_par1", C.c_int64),
+        ("nexpect", C.c_int64), ("expect_nterms", I64P), ("expect_ae", DP), ("expect_lhs", I64P),
+        ("expect_rhs", I64P), ("expect_ioper", I64P),
     ]
 
 
@@ -75,6 +77,9 @@ def load_library() -> C.CDLL:
     lib.mctdh_propagate.argtypes = [vp, C.c_int64, C.c_double, DP, DP, I64P, I64P, I64P]
     lib.mctdh_observables.argtypes = [vp, C.c_double, DP, DP, DP, DP, DP]
     lib.mctdh_norm_wf.argtypes = [vp, DP, DP, DP]
+    lib.mctdh_expect.argtypes = [vp, DP]
+    lib.mctdh_natpop.argtypes = [vp, DP, DP, DP]
+    lib.mctdh_densmat.argtypes = [vp, C.c_int64, C.c_int64, DP]
     lib.mctdh_wf_ovl.argtypes = [vp, DP, DP, DP, DP, DP, DP]
     lib.mctdh_launch_count.argtypes = [vp]
     lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
@@ -130,7 +135,7 @@ def load_library() -> C.CDLL:
                  "mctdh_rk_attempt", "mctdh_cmf2_attempt",
                  "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
                  "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_step",
-                 "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
+                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
                  "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"):
         getattr(lib, name).restype = C.c_int64
     _lib = lib
@@ -141,6 +146,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_rk_attempt", "mctdh_cmf2_attempt",
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
+            "mctdh_expect", "mctdh_natpop", "mctdh_densmat",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
@@ -255,6 +261,18 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
     s.precision = precision
     s.int_order = getattr(model, "int_order", 4)
     s.int_par1 = getattr(model, "int_par1", 0)
+    expect = getattr(model, "expect", [])
+    s.nexpect = len(expect)
+    if expect:
+        terms = [t for op in expect for t in op]
+        eae = np.empty(2 * len(terms))
+        eae[0::2] = [t.coeff.real for t in terms]
+        eae[1::2] = [complex(t.coeff).imag for t in terms]
+        s.expect_nterms = I([len(op) for op in expect])
+        s.expect_ae = F(eae)
+        s.expect_lhs = I([t.lhs for t in terms])
+        s.expect_rhs = I([t.rhs for t in terms])
+        s.expect_ioper = I(np.concatenate(model.ioper_expect, axis=1).reshape(-1, order="F"))
     return s, keep
 
 
@@ -356,6 +374,31 @@ class GpuCore:
         self._check(self.lib.mctdh_observables(self.h, t, C.byref(e), _ptr(pop), C.byref(nrm),
                                                C.byref(ar), C.byref(ai)))
         return dict(t=t, pop=pop, norm=nrm.value, energy=e.value, auto=complex(ar.value, ai.value))
+
+    def expect(self) -> np.ndarray:
+        """Expectation values of the model's expectation operators for the resident
+        state (Expectation, output.f90:449-500)."""
+        out = np.zeros(max(len(getattr(self.model, "expect", [])), 1), dtype=np.complex128)
+        self._check(self.lib.mctdh_expect(self.h, out.ctypes.data_as(DP)))
+        return out[:len(getattr(self.model, "expect", []))]
+
+    def natpop(self):
+        """Natural populations (nspfmax, nmodes, nstates), decreasing; gross Gaussian
+        populations and population errors (ns00max, nmodgwp, nstates) (output.f90:88-140)."""
+        m = self.model
+        nat = np.zeros((int(m.nspf.max()), m.nmodes, m.nstates), order="F")
+        shape = (max(int(m.ns00max), 1), len(m.modes_gwp), m.nstates)
+        ggp, perr = np.zeros(shape, order="F"), np.zeros(shape, order="F")
+        self._check(self.lib.mctdh_natpop(self.h, nat.ctypes.data_as(DP), ggp.ctypes.data_as(DP),
+                                          perr.ctypes.data_as(DP)))
+        return nat, ggp, perr
+
+    def densmat(self, mode: int, state: int) -> np.ndarray:
+        """rho(mode, state) of the resident state (the densmat file, output.f90:276-300)."""
+        n = int(self.model.nspf[mode, state])
+        rho = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._check(self.lib.mctdh_densmat(self.h, mode, state, rho.ctypes.data_as(DP)))
+        return rho
 
     def propagate_interval(self, int_type: int, tnext: float, t: float, step: float):
         tt, ss = C.c_double(t), C.c_double(step)

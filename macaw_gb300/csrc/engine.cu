@@ -406,6 +406,15 @@ struct Ctx {
   cplx* cy_part = nullptr;                            // per-operator partial sums of Y
   std::vector<std::vector<cplx*>> tau;                // [i][s]
   std::vector<std::vector<cplx*>> dhd;                // [i][k] D^H h D of the CMF2 Lanczos (Calc_DHD)
+  // expectation operators (Expectation, output.f90:449-500)
+  int nexpect = 0;
+  std::vector<int> exp_nterms, exp_lhs, exp_rhs, exp_ioper;   // exp_ioper[m + nmodes * term]
+  std::vector<cplx> exp_ae;
+  std::vector<std::vector<char>> ham_op;              // [m][k]: the operator of some Hamiltonian term
+  std::vector<H1Desc> xh1_h;                          // grid-mode operators of expectation operators only
+  H1Desc* xh1_d = nullptr;
+  std::vector<GwpH1Desc> xgh1_h;                      // Gaussian-mode ones
+  GwpH1Desc* xgh1_d = nullptr;
   cplx* d_adot = nullptr;                             // f * sum_t ae_t H_t A before the corrections
   cplx* d_dA = nullptr;                               // dA after S^-1 and tau
   std::vector<ProdBatch> gwp_sinv;                    // S^-1 products, one batch per Gaussian mode
@@ -482,6 +491,41 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   }
   c.is_identity.resize(c.nmodes * c.nopermax);
   for (int i = 0; i < c.nmodes * c.nopermax; ++i) c.is_identity[i] = (int)s->is_identity[i];
+  // Operators no Hamiltonian term uses (those of expectation operators only) get no
+  // mean field and stay out of the EOM; the reference carries them with zero mean
+  // fields, which add exact zeros to its sums.
+  c.ham_op.assign(c.nmodes, std::vector<char>(c.nopermax, 0));
+  for (int t = 0; t < c.nham; ++t)
+    for (int m = 0; m < c.nmodes; ++m) {
+      const int k = c.ioper[m + c.nmodes * t];
+      if (k < 0 || k >= c.noper[m]) throw StatusError(MCTDH_EARG, "iOper out of range");
+      c.ham_op[m][k] = 1;
+    }
+  c.nexpect = (int)s->nexpect;
+  if (c.nexpect < 0) throw StatusError(MCTDH_EARG, "nexpect < 0");
+  if (c.nexpect > 0) {
+    if (!s->expect_nterms || !s->expect_ae || !s->expect_lhs || !s->expect_rhs || !s->expect_ioper)
+      throw StatusError(MCTDH_EARG, "expectation operators need their term arrays");
+    int tot = 0;
+    for (int i = 0; i < c.nexpect; ++i) {
+      c.exp_nterms.push_back((int)s->expect_nterms[i]);
+      if (c.exp_nterms.back() < 0) throw StatusError(MCTDH_EARG, "negative term count");
+      tot += c.exp_nterms.back();
+    }
+    for (int g = 0; g < tot; ++g) {
+      c.exp_ae.push_back(mkc(s->expect_ae[2 * g], s->expect_ae[2 * g + 1]));
+      c.exp_lhs.push_back((int)s->expect_lhs[g]);
+      c.exp_rhs.push_back((int)s->expect_rhs[g]);
+      if (c.exp_lhs.back() < 0 || c.exp_lhs.back() >= c.nstates || c.exp_rhs.back() < 0 ||
+          c.exp_rhs.back() >= c.nstates)
+        throw StatusError(MCTDH_EARG, "electronic label of an expectation term out of range");
+      for (int m = 0; m < c.nmodes; ++m) {
+        const int k = (int)s->expect_ioper[m + (long long)c.nmodes * g];
+        if (k < 0 || k >= c.noper[m]) throw StatusError(MCTDH_EARG, "iOperExtra out of range");
+        c.exp_ioper.push_back(k);
+      }
+    }
+  }
   c.naconf.resize(c.nstates);
   c.aoff.resize(c.nstates);
   long long off = 0;
@@ -642,7 +686,7 @@ void plan_gwp_setup(Ctx& c) {
       const int l = c.oper[m][k][0], r = c.oper[m][k][1];
       const int n1 = c.m_of(m, l), n2 = c.m_of(m, r);
       c.hmat[m][k] = c.ar.calloc_c((long long)n1 * n2);
-      if (!c.is_identity[m + f * k]) c.mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      if (!c.is_identity[m + f * k] && c.ham_op[m][k]) c.mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
       GwpH1Desc hd;
       memset(&hd, 0, sizeof(hd));
       hd.xi1 = psi_block(c, c.d_in, m, l);
@@ -656,12 +700,14 @@ void plan_gwp_setup(Ctx& c) {
       hd.n2 = n2;
       hd.same_state = (l == r);
       for (int q = 0; q < c.nmodedof[m]; ++q) hd.ops[q] = c.oper[m][k][2 + q];
-      c.gh1_h.push_back(hd);
+      if (c.ham_op[m][k]) c.gh1_h.push_back(hd);
+      else c.xgh1_h.push_back(hd);
     }
   }
   c.gs_d = upload_vec(c.ar, c.gs_h);
   c.gsreg_d = upload_vec(c.ar, c.gsreg_h);
   c.gh1_d = upload_vec(c.ar, c.gh1_h);
+  c.xgh1_d = upload_vec(c.ar, c.xgh1_h);
 }
 
 // S-weighted coefficient tensors for the density matrices (Calc_rho1mode,
@@ -719,9 +765,12 @@ void plan_eom(Ctx& c) {
         CK(cudaMemcpy(c.hmat[m][k], I.data(), sizeof(cplx) * I.size(), cudaMemcpyHostToDevice));
         continue;
       }
+      const bool ham = c.ham_op[m][k];
       c.ophi[m][k] = c.ar.calloc_c((long long)G * n2);
-      c.mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
-      c.rhom1mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      if (ham) {
+        c.mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+        c.rhom1mf[m][k] = c.ar.calloc_c((long long)n1 * n2);
+      }
       H1Desc hd;
       memset(&hd, 0, sizeof(hd));
       hd.phi_r = c.d_in + c.naconftot + c.ipsi[m + f * r];
@@ -747,14 +796,19 @@ void plan_eom(Ctx& c) {
           hd.matf[q] = c.dofmatf[key];
         }
       }
-      c.h1_of_mode[m].push_back((int)c.h1_h.size());
-      c.h1_h.push_back(hd);
+      if (ham) {
+        c.h1_of_mode[m].push_back((int)c.h1_h.size());
+        c.h1_h.push_back(hd);
+      } else {
+        c.xh1_h.push_back(hd);
+      }
       smem = std::max(smem, sizeof(cplx) * (size_t)(2 * G));
       c.h1_maxn2 = std::max(c.h1_maxn2, n2);
     }
   }
   c.h1_smem = smem;
   c.h1_d = upload_vec(c.ar, c.h1_h);
+  c.xh1_d = upload_vec(c.ar, c.xh1_h);
   if (!c.modes_gwp.empty()) plan_gwp_setup(c);
 
   // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
@@ -935,7 +989,7 @@ void plan_eom(Ctx& c) {
       rd.eps = c.eps_rho;
       rd.op_first = (int)c.mfop_h.size();
       for (int k = 0; k < c.noper[m]; ++k) {
-        if (c.is_identity[m + f * k]) continue;
+        if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
         if (c.multiset[m] && c.oper[m][k][0] != s) continue;
         MFOp op;
         memset(&op, 0, sizeof(op));
@@ -966,7 +1020,7 @@ void plan_eom(Ctx& c) {
       sd.n = c.m_of(m, s);
       sd.op_first = (int)c.spfop_h.size();
       for (int k = 0; k < c.noper[m]; ++k) {
-        if (c.is_identity[m + f * k]) continue;
+        if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
         if (c.multiset[m] && c.oper[m][k][0] != s) continue;
         SpfOp op;
         memset(&op, 0, sizeof(op));
@@ -1042,7 +1096,7 @@ void plan_gwp_derivs(Ctx& c) {
       d.eps = c.eps_C;
       d.op_first = (int)c.yop_h.size();
       for (int k = 0; k < c.noper[m]; ++k) {
-        if (c.is_identity[m + f * k]) continue;
+        if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
         const int l = c.oper[m][k][0], r = c.oper[m][k][1];
         if (c.multiset[m] && l != s) continue;
         GwpYOp op;
@@ -1101,7 +1155,7 @@ void plan_hb(Ctx& c) {
     const int m = c.modes_gwp[i];
     c.dhd[i].assign(c.noper[m], nullptr);
     for (int k = 0; k < c.noper[m]; ++k) {
-      if (c.is_identity[m + f * k]) continue;
+      if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
       c.dhd[i][k] = c.ar.calloc_c((long long)c.m_of(m, c.oper[m][k][0]) * c.m_of(m, c.oper[m][k][1]));
     }
   }
@@ -2276,7 +2330,7 @@ void plan_cmf_gwp(Ctx& c, CmfState& S, std::vector<unsigned char>& em) {
       S.errd_h.push_back(ed);
     }
     for (int k = 0; k < c.noper[m]; ++k) {
-      if (c.is_identity[m + f * k]) continue;
+      if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
       const int l = c.oper[m][k][0], r = c.oper[m][k][1];
       GwpDhdDesc d;
       memset(&d, 0, sizeof(d));
@@ -2518,7 +2572,7 @@ MfxState& mfx_state(Ctx& c) {
       off += (long long)c.m_of(m, 0) * c.m_of(m, 0);
     }
     for (int k = 0; k < c.noper[m]; ++k) {
-      if (c.is_identity[m + f * k]) continue;
+      if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
       M->segs_h.push_back(SnapSeg{c.mf[m][k], off});
       off += (long long)c.m_of(m, c.oper[m][k][0]) * c.m_of(m, c.oper[m][k][1]);
     }
@@ -3302,6 +3356,143 @@ void observables(Ctx& c, double* energy, double* pop, double* norm, double* auto
     if (auto_im) *auto_im = o[2].y;
   }
 }
+
+// ---------------------------------------------------------------------------
+// The rest of WriteOutput on the device: expectation values, natural
+// populations, density matrices of the resident state (output.f90:88-140,
+// 276-300, 449-500).
+// ---------------------------------------------------------------------------
+struct WriterPlan {
+  bool expect_planned = false;
+  std::vector<ProdBatch> chain;   // per term: prod_m h_m A_r, one batch per product depth
+  HoleBatch dots;                 // <A_l | .>
+  RedBatch red;                   // sum_t ae_t <..> per operator
+  cplx* res = nullptr;
+  std::vector<NatpopDesc> np_h;
+  NatpopDesc* np_d = nullptr;
+  double* np_out = nullptr;       // natpop | ggp | poperr
+  long long np_len = 0, ggp_off = 0, perr_off = 0;
+  int nspfmax = 0;
+};
+std::map<const Ctx*, WriterPlan*> g_writer;
+
+WriterPlan& writer_plan(Ctx& c) {
+  WriterPlan*& W = g_writer[&c];
+  if (!W) W = new WriterPlan();
+  return *W;
+}
+
+// Expectation (output.f90:449-500): every mode's h1mode in mode order on A_r
+// (identity matrices of grid modes are skipped, they change nothing; the
+// Gaussian identity is S00), then <A_l| . > times ae_t summed per operator.
+void plan_expect(Ctx& c, WriterPlan& W) {
+  const int f = c.nmodes;
+  W.res = c.ar.calloc_c(std::max(c.nexpect, 1));
+  W.chain.assign(f + 1, ProdBatch());
+  std::vector<HoleRef> refs;
+  int g = 0;
+  for (int i = 0; i < c.nexpect; ++i) {
+    const int tg = W.red.add_target(W.res + i, 1, 1, 1, 0);
+    for (int t = 0; t < c.exp_nterms[i]; ++t, ++g) {
+      const int s1 = c.exp_lhs[g], s2 = c.exp_rhs[g];
+      TRef cur;
+      cur.p = c.d_in + c.aoff[s2];
+      cur.shape = c.shape_of(s2);
+      int depth = 0;
+      for (int m = 0; m < f; ++m) {
+        const int k = c.exp_ioper[m + f * g];
+        if (!c.is_gwp[m] && c.is_identity[m + f * k]) continue;
+        const int n1 = c.m_of(m, s1);
+        std::vector<int> ns = cur.shape;
+        ns[m] = n1;
+        cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+        ++depth;
+        W.chain[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0);
+        cur.p = out;
+        cur.shape = ns;
+      }
+      if (prod_range(cur.shape, 0, f) != c.naconf[s1])
+        throw StatusError(MCTDH_EARG, "expectation term does not map state r onto state l");
+      const int h = W.dots.add(c.ar, c.d_in + c.aoff[s1], cur.p, c.naconf[s1], 1, 1, 1);
+      refs.push_back(HoleRef{h, tg, c.exp_ae[g]});
+    }
+  }
+  for (auto& b : W.chain) b.finalize(c.ar);
+  W.dots.finalize(c.ar);
+  for (auto& r : refs) W.red.add_term(r.target, W.dots.h[r.hole], r.alpha);
+  W.red.finalize(c.ar);
+  W.expect_planned = true;
+}
+
+void expectation(Ctx& c, cplx* values) {
+  WriterPlan& W = writer_plan(c);
+  if (!W.expect_planned) plan_expect(c, W);
+  copy_dev(c, c.d_in, c.d_y, c.ntot);
+  // h1mode of every operator on the resident SPFs, FP64 (Calc_h1mode before
+  // WriteOutput, output.f90:35-41)
+  if (!c.modes_gwp.empty()) {
+    launch_gwp_ovl(c.gs_d, (int)c.gs_h.size(), c.st);
+    launch_gwp_h1(c.gh1_d, (int)c.gh1_h.size(), c.st);
+    launch_gwp_h1(c.xgh1_d, (int)c.xgh1_h.size(), c.st);
+    c.count(3);
+  }
+  launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, 0);
+  launch_h1(c.xh1_d, (int)c.xh1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, 0);
+  c.count(2);
+  for (size_t i = 1; i < W.chain.size(); ++i) run_prod(c, W.chain[i]);
+  run_hole(c, W.dots);
+  run_red(c, W.red);
+  CK(cudaMemcpyAsync(values, W.res, sizeof(cplx) * c.nexpect, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  check_status(c);
+}
+
+void plan_natpop(Ctx& c, WriterPlan& W) {
+  const int f = c.nmodes, ng = (int)c.modes_gwp.size();
+  for (int m = 0; m < f; ++m)
+    for (int s = 0; s < c.nstates; ++s) W.nspfmax = std::max(W.nspfmax, c.m_of(m, s));
+  const long long nnat = (long long)W.nspfmax * f * c.nstates;
+  const long long ngg = (long long)std::max(c.ns00max, 1) * ng * c.nstates;
+  W.ggp_off = nnat;
+  W.perr_off = nnat + ngg;
+  W.np_len = nnat + 2 * ngg;
+  W.np_out = (double*)c.ar.alloc(sizeof(double) * std::max(W.np_len, 1LL));
+  for (int s = 0; s < c.nstates; ++s) {
+    for (int m = 0; m < f; ++m) {
+      NatpopDesc d;
+      memset(&d, 0, sizeof(d));
+      d.n = c.m_of(m, s);
+      d.rho = c.rho[m][s];
+      d.natpop = W.np_out + (long long)W.nspfmax * (m + f * s);
+      if (c.is_gwp[m]) {
+        const int i = c.gwp_of[m];
+        d.S = c.s00[i][set_of(c, m, s)][set_of(c, m, s)];
+        d.work = c.ar.calloc_c(2LL * d.n * d.n);
+        d.ggp = W.np_out + W.ggp_off + (long long)c.ns00max * (i + ng * s);
+        d.poperr = W.np_out + W.perr_off + (long long)c.ns00max * (i + ng * s);
+      }
+      W.np_h.push_back(d);
+    }
+  }
+  W.np_d = upload_vec(c.ar, W.np_h);
+}
+
+void natpop(Ctx& c, double* nat, double* ggp, double* poperr) {
+  WriterPlan& W = writer_plan(c);
+  if (!W.np_d) plan_natpop(c, W);
+  operators_and_mf(c, c.d_y);   // rho and S00 of the resident state (output.f90:35-41)
+  CK(cudaMemsetAsync(W.np_out, 0, sizeof(double) * W.np_len, c.st));
+  launch_natpop(W.np_d, (int)W.np_h.size(), c.d_status, c.st);
+  c.count();
+  const long long nnat = W.ggp_off, ngg = W.perr_off - W.ggp_off;
+  CK(cudaMemcpyAsync(nat, W.np_out, sizeof(double) * nnat, cudaMemcpyDeviceToHost, c.st));
+  if (ggp && ngg > 0 && !c.modes_gwp.empty())
+    CK(cudaMemcpyAsync(ggp, W.np_out + W.ggp_off, sizeof(double) * ngg, cudaMemcpyDeviceToHost, c.st));
+  if (poperr && ngg > 0 && !c.modes_gwp.empty())
+    CK(cudaMemcpyAsync(poperr, W.np_out + W.perr_off, sizeof(double) * ngg, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  check_status(c);
+}
 }  // namespace
 
 struct mctdh_ens {
@@ -3357,6 +3548,11 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
   if (mi != g_mfx.end()) {
     delete mi->second;
     g_mfx.erase(mi);
+  }
+  auto wi = g_writer.find(c);
+  if (wi != g_writer.end()) {
+    delete wi->second;
+    g_writer.erase(wi);
   }
   for (auto& kv : c->dots) delete kv.second;
   drain_profile(*c);
@@ -3723,6 +3919,34 @@ int64_t mctdh_observables(mctdh_ctx_t* ctx, double t, double* energy, double* po
   Ctx* c = ctx->c;
   (void)t;
   return guarded(c, [&] { observables(*c, energy, pop, norm, auto_re, auto_im); });
+}
+
+int64_t mctdh_expect(mctdh_ctx_t* ctx, double* values) {
+  if (!ctx) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  if (c->nexpect > 0 && !values) return MCTDH_EARG;
+  return guarded(c, [&] {
+    if (c->nexpect > 0) expectation(*c, (cplx*)values);
+  });
+}
+
+int64_t mctdh_natpop(mctdh_ctx_t* ctx, double* nat, double* ggp, double* poperr) {
+  if (!ctx || !nat) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] { natpop(*c, nat, ggp, poperr); });
+}
+
+int64_t mctdh_densmat(mctdh_ctx_t* ctx, int64_t mode, int64_t state, double* rho) {
+  if (!ctx || !rho) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  if (mode < 0 || mode >= c->nmodes || state < 0 || state >= c->nstates) return MCTDH_EARG;
+  return guarded(c, [&] {
+    operators_and_mf(*c, c->d_y);
+    const int n = c->m_of((int)mode, (int)state);
+    CK(cudaMemcpyAsync(rho, c->rho[mode][state], sizeof(cplx) * n * n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    check_status(*c);
+  });
 }
 
 int64_t mctdh_norm_wf(mctdh_ctx_t* ctx, const double* A, const double* psi, double* norm) {

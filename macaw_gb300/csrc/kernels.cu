@@ -681,6 +681,107 @@ void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int*
   reginv_kernel<<<ndesc, 32, 0, st>>>(d_descs, d_ops, d_status);
 }
 
+// ---------------------------------------------------------------------------
+// Natural populations (output.f90:88-140), one warp per (mode, state) block:
+// eigenvalues of rho (zheev on the upper triangle) in decreasing order; for a
+// Gaussian mode of conj(S^1/2) rho conj(S^1/2) with S^1/2 = sum_j sqrt(w_j) u_j u_j^H
+// (SquareRoot, maths.f90:556-585; zlacgv; two zhemm 'R' on upper triangles), the
+// gross Gaussian populations sum_j2 Re(rho S)(j1, j2) and the population errors
+// |sum_j2 2 Re(rho S)(j1, j2) - rho(j1, j1)| (decreasing), all from upper triangles.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ cplx herm_up(const cplx* X, int n, int i, int j) {
+  cplx v = (i <= j) ? X[i + n * j] : cconj(X[j + n * i]);
+  if (i == j) v.y = 0.0;
+  return v;
+}
+
+// position of v[i] in decreasing order (ties keep their index order)
+__device__ __forceinline__ int rank_desc(const double* v, int n, int i) {
+  int r = 0;
+  for (int j = 0; j < n; ++j) r += (v[j] > v[i]) || (v[j] == v[i] && j < i);
+  return r;
+}
+
+__global__ void __launch_bounds__(32) natpop_kernel(const NatpopDesc* __restrict__ descs, int* status) {
+  __shared__ cplx A[MAXN_SPF * MAXN_SPF];
+  __shared__ cplx V[MAXN_SPF * MAXN_SPF];
+  __shared__ double w[MAXN_SPF];
+  __shared__ JacRot R[MAXN_SPF / 2];
+  const NatpopDesc& d = descs[blockIdx.x];
+  const int n = d.n, ld = MAXN_SPF, lane = threadIdx.x;
+  bool ok = true, ok2 = true;
+  if (d.S) {
+    for (int e = lane; e < n * n; e += 32) A[e % n + ld * (e / n)] = herm_up(d.S, n, e % n, e / n);
+    __syncwarp();
+    jacobi_herm(A, V, n, ld, R, &ok);
+    if (lane < n) w[lane] = sqrt(A[lane + ld * lane].x);
+    __syncwarp();
+    cplx* S12 = d.work;
+    cplx* T = d.work + n * n;
+    for (int e = lane; e < n * n; e += 32) {
+      const int i = e % n, j = e / n;
+      cplx v = mkc(0.0, 0.0);
+      for (int k = 0; k < n; ++k) v = cadd(v, cscale(cmul(V[i + ld * k], cconj(V[j + ld * k])), w[k]));
+      S12[e] = cconj(v);
+    }
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) {   // T = S12 rho
+      const int i = e % n, j = e / n;
+      cplx v = mkc(0.0, 0.0);
+      for (int q = 0; q < n; ++q) v = cadd(v, cmul(S12[i + n * q], herm_up(d.rho, n, q, j)));
+      T[e] = v;
+    }
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) {   // M = T S12, S12 Hermitian from its upper triangle
+      const int i = e % n, j = e / n;
+      cplx v = mkc(0.0, 0.0);
+      for (int q = 0; q < n; ++q) v = cadd(v, cmul(T[i + n * q], herm_up(S12, n, q, j)));
+      A[i + ld * j] = v;
+    }
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) {   // zheev reads the upper triangle
+      const int i = e % n, j = e / n;
+      if (i > j) A[i + ld * j] = cconj(A[j + ld * i]);
+      if (i == j) A[i + ld * j].y = 0.0;
+    }
+  } else {
+    for (int e = lane; e < n * n; e += 32) A[e % n + ld * (e / n)] = herm_up(d.rho, n, e % n, e / n);
+  }
+  __syncwarp();
+  jacobi_herm(A, V, n, ld, R, &ok2);
+  if (lane < n) w[lane] = A[lane + ld * lane].x;
+  __syncwarp();
+  if (lane < n) d.natpop[rank_desc(w, n, lane)] = w[lane];
+  __syncwarp();
+  if (d.S) {
+    double g = 0.0, e = 0.0;
+    if (lane < n) {
+      const int j1 = lane;
+      for (int j2 = 0; j2 < j1; ++j2) {
+        const double v = cmul(d.rho[j2 + n * j1], d.S[j2 + n * j1]).x;
+        g += v;
+        e += 2.0 * v;
+      }
+      e -= d.rho[j1 + n * j1].x;
+      for (int j2 = j1; j2 < n; ++j2) {
+        const double v = cmul(d.rho[j1 + n * j2], d.S[j1 + n * j2]).x;
+        g += v;
+        e += 2.0 * v;
+      }
+      e = fabs(e);
+      d.ggp[j1] = g;
+      w[lane] = e;
+    }
+    __syncwarp();
+    if (lane < n) d.poperr[rank_desc(w, n, lane)] = e;
+  }
+  if (lane == 0 && !(ok && ok2)) atomicOr(status, DEVST_EIG_NOCONV);
+}
+void launch_natpop(const NatpopDesc* d, int nd, int* status, cudaStream_t st) {
+  if (nd <= 0) return;
+  natpop_kernel<<<nd, 32, 0, st>>>(d, status);
+}
+
 // Tridiagonal eigenproblem of the Lanczos matrix (dstev, cmf2_integration.f90:85)
 __global__ void tridiag_kernel(const double* alpha, const double* beta, int n, double* evals, double* evecs,
                                int* status) {

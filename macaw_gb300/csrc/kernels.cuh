@@ -148,6 +148,17 @@ struct SpfErrDesc {
   int n, mode;
 };
 
+struct NatpopDesc {       // one (mode, state) block of the natural populations (output.f90:88-140)
+  const cplx* rho;         // n x n density matrix (upper triangle authoritative)
+  const cplx* S;           // Gaussian modes: S00 of the set (n x n), else null
+  cplx* work;              // Gaussian modes: 2 n^2 scratch
+  double* natpop;          // n, decreasing
+  double* ggp;             // Gaussian modes: gross Gaussian populations (n)
+  double* poperr;          // Gaussian modes: population errors (n, decreasing)
+  int n, pad;
+};
+void launch_natpop(const NatpopDesc* d, int nd, int* status, cudaStream_t st);
+
 struct SnapSeg {
   cplx* ptr;               // matrix storage
   long long offset;        // first index in the flat snapshot

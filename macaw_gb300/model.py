@@ -190,6 +190,8 @@ class Model:
     init_state: int = 0                     # populated electronic state (0-based)
     init_spf: Dict[int, Tuple[str, tuple]] = dataclasses.field(default_factory=dict)
     label: str = "model"
+    # operators whose expectation values are written (the 'expect' keyword, input.f90:196-216)
+    expect: List[List[Term]] = dataclasses.field(default_factory=list)
 
     # ---- derived (filled by finalize) ----
     def finalize(self) -> "Model":
@@ -234,7 +236,8 @@ class Model:
         for m in self.modes_dvr:
             self.ngpm[m] = int(np.prod([self.ngp[d] for d in self.mode_dofs[m]]))
 
-    # hamilton.f90:91-167 (operator dedup), :353-374 (IsIdentity), :377-399 (SkipTerm)
+    # hamilton.f90:91-167 (operator dedup, the extra operators after the
+    # Hamiltonian's), :353-374 (IsIdentity), :377-399 (SkipTerm)
     def _build_operators(self):
         nham = len(self.terms)
         self.nham = nham
@@ -244,20 +247,28 @@ class Model:
                 self.iopdof[d, t] = op
         self.oper: List[List[Tuple[int, int, Tuple[int, ...]]]] = []
         self.ioper = np.zeros((self.nmodes, nham), dtype=np.int64)
+        # iOperExtra: (nmodes, nterms) per expectation operator
+        self.ioper_expect = [np.zeros((self.nmodes, len(op)), dtype=np.int64) for op in self.expect]
+
+        def vec_of(m, term):
+            el = (term.lhs, term.rhs) if self.multiset[m] else (0, 0)
+            return (el[0], el[1], tuple(int(term.dof_ops.get(d, 0)) for d in self.mode_dofs[m]))
+
         for m in range(self.nmodes):
             ops: List[Tuple[int, int, Tuple[int, ...]]] = []
-            for t, term in enumerate(self.terms):
-                if self.multiset[m]:
-                    el = (term.lhs, term.rhs)
-                else:
-                    el = (0, 0)
-                vec = (el[0], el[1], tuple(int(self.iopdof[d, t]) for d in self.mode_dofs[m]))
+
+            def index_of(vec):
                 try:
-                    k = ops.index(vec)
+                    return ops.index(vec)
                 except ValueError:
                     ops.append(vec)
-                    k = len(ops) - 1
-                self.ioper[m, t] = k
+                    return len(ops) - 1
+
+            for t, term in enumerate(self.terms):
+                self.ioper[m, t] = index_of(vec_of(m, term))
+            for i, op in enumerate(self.expect):
+                for t, term in enumerate(op):
+                    self.ioper_expect[i][m, t] = index_of(vec_of(m, term))
             self.oper.append(ops)
         self.nopermax = max(len(o) for o in self.oper)
         self.is_identity = np.zeros((self.nmodes, self.nopermax), dtype=bool)
@@ -273,10 +284,15 @@ class Model:
         self.ae = np.array([term.coeff for term in self.terms], dtype=np.complex128)
         self.lhs_el = np.array([term.lhs for term in self.terms], dtype=np.int64)
         self.rhs_el = np.array([term.rhs for term in self.terms], dtype=np.int64)
+        codes = {d: set(int(c) for c in self.iopdof[d]) for d in range(self.ndof)}
+        for op in self.expect:
+            for term in op:
+                for d, c in term.dof_ops.items():
+                    codes[d].add(int(c))
         for d in range(self.ndof):
             if self.dvr_type[d] == "gwp":
                 continue
-            for code in set(int(c) for c in self.iopdof[d]):
+            for code in codes[d]:
                 if code in (OP_ID, OP_P, OP_DQ2, OP_QP) or 1 <= code <= 20:
                     continue
                 raise ModelError(f"primitive operator code {code} on dof {d + 1} is not supported")
@@ -567,6 +583,7 @@ def parse_input(path: str) -> Model:
     nstates, ndof, nmodes = 1, -1, 0
     i = 0
     flags = set()
+    expect_files: List[str] = []
     while i < len(lines):
         line = lines[i].split("#", 1)[0]
         i += 1
@@ -611,7 +628,9 @@ def parse_input(path: str) -> Model:
         elif name in ("hamiltonian", "tinit", "tfinal", "tout", "eps_rho", "eps_c", "eps_int",
                       "eps_s", "eps_pop", "minstep", "normalize", "psi", "npackets"):
             kw[name] = val
-        elif name in ("expect", "densmat"):
+        elif name == "expect":
+            expect_files.append(val)
+        elif name == "densmat":
             continue
         else:
             raise ModelError(f"Input instruction: {s} cannot be understood")
@@ -650,9 +669,16 @@ def parse_input(path: str) -> Model:
         raise ModelError(f"Operator file, {hfile} not found")
     with open(hpath) as fh:
         terms = parse_operator_file(fh.read(), nstates)
+    expect: List[List[Term]] = []
+    for ef in expect_files:
+        epath = os.path.join(base, ef)
+        if not os.path.exists(epath):
+            raise ModelError(f"Operator file, {ef} not found")
+        with open(epath) as fh:
+            expect.append(parse_operator_file(fh.read(), nstates))
     model = Model(nstates=nstates, mode_dofs=mode_dofs, multiset=multiset, nspf=nspf,
                   dvr_type=dvr_type, ngp=ngp, dvrpar=dvrpar, terms=terms,
-                  label=os.path.basename(path))
+                  label=os.path.basename(path), expect=expect)
     if "tinit" in kw:
         model.tinit = _read_float(kw["tinit"]) / AU2FS
     if "tfinal" in kw:

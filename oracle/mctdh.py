@@ -1326,6 +1326,59 @@ class Oracle:
         auto = self.wf_ovl(A0, psi0, A, psi)
         return dict(t=t, pop=pop, norm=float(pop.sum()), energy=self.energyMF / pop.sum(), auto=auto)
 
+    def expectation(self, A, psi) -> np.ndarray:
+        """Expectation (output.f90:449-500): for each expectation operator
+        sum_t ae_t <A_l| prod_m h_m |A_r> with h1mode on every mode (identity
+        matrices on grid modes, S00 on Gaussian modes), as written (the
+        conjugate of the accumulated zdotu)."""
+        md = self.m
+        self._prepare(A, psi)
+        out = np.zeros(len(md.expect), dtype=np.complex128)
+        for i, op in enumerate(md.expect):
+            for t, term in enumerate(op):
+                X = md.a_state(A, term.rhs)
+                for mode in range(md.nmodes):
+                    X = mode_product(self.h1mode[mode][int(md.ioper_expect[i][mode, t])], X, mode)
+                out[i] += term.coeff * np.vdot(md.a_state(A, term.lhs), X)
+        return out
+
+    def natpop(self, A, psi):
+        """Natural populations (eigenvalues of rho, decreasing; Gaussian modes:
+        of conj(S^1/2) rho conj(S^1/2)), gross Gaussian populations and the
+        population errors of neglecting one Gaussian, decreasing
+        (output.f90:88-140).  Dicts keyed (mode, state)."""
+        md = self.m
+        self._prepare(A, psi)
+        nat, ggp, perr = {}, {}, {}
+        for mode in md.modes_dvr:
+            for s in range(md.nstates):
+                nat[(mode, s)] = np.linalg.eigvalsh(herm_from_upper(np.triu(self.rho[(mode, s)])))[::-1]
+        for i, mode in enumerate(md.modes_gwp):
+            for s in range(md.nstates):
+                js = s if md.multiset[mode] else 0
+                S = self.s00(i, js, js)
+                w, U = np.linalg.eigh(herm_from_upper(np.triu(S)))         # SquareRoot (maths.f90:556-585)
+                S12 = ((U * np.sqrt(w)) @ U.conj().T).conj()                 # zlacgv
+                r = self.rho[(mode, s)]
+                M = S12 @ herm_from_upper(np.triu(r)) @ S12                  # two zhemm 'R'
+                nat[(mode, s)] = np.linalg.eigvalsh(herm_from_upper(np.triu(M)))[::-1]
+                n = S.shape[0]
+                g, e = np.zeros(n), np.zeros(n)
+                for j1 in range(n):
+                    for j2 in range(j1):
+                        v = float((r[j2, j1] * S[j2, j1]).real)
+                        g[j1] += v
+                        e[j1] += 2 * v
+                    e[j1] -= float(r[j1, j1].real)
+                    for j2 in range(j1, n):
+                        v = float((r[j1, j2] * S[j1, j2]).real)
+                        g[j1] += v
+                        e[j1] += 2 * v
+                    e[j1] = abs(e[j1])
+                ggp[(mode, s)] = g
+                perr[(mode, s)] = np.sort(e)[::-1]
+        return nat, ggp, perr
+
     def propagate(self, A, psi, tfinal: Optional[float] = None, max_steps: Optional[int] = None,
                   record_steps: bool = False):
         """propagate_wf (propagator.f90:87-146 RK, :257-306 CMF2).  Returns the list

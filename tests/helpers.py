@@ -50,3 +50,22 @@ def random_state(model, seed=0, spread=1.0, gwp_shift=0.1):
     from oracle.mctdh import Oracle
     nrm = Oracle(model).norm_wf(A, psi)
     return A / np.sqrt(nrm), psi
+
+
+def with_expect(model):
+    """The model with expectation operators (the 'expect' keyword): the identity
+    (= the norm), the projector on state 1, q of dof 1 on every state, and the
+    one-sided coherence |1><2| q of dof 2 (complex in general)."""
+    from macaw_gb300.model import Term
+    ns = model.nstates
+    model.expect = [
+        [Term(1.0, s, s, {}) for s in range(ns)],
+        [Term(1.0, 0, 0, {})],
+        [Term(1.0, s, s, {0: 1}) for s in range(ns)],
+        [Term(0.5, 0, 1, {1: 1})],
+    ]
+    gwpa = getattr(model, "gwpa", None)
+    model.finalize()
+    if gwpa is not None:
+        model.gwpa = gwpa
+    return model

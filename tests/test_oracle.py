@@ -174,3 +174,46 @@ def test_golden_fixtures(name):
     cur = compute(name)
     for key in g.files:
         assert np.allclose(cur[key], g[key], rtol=1e-11, atol=1e-13), key
+
+
+@pytest.mark.parametrize("builder", ["lvc", "gmctdh"])
+def test_writer_quantities_oracle(builder):
+    """Natural populations of every mode sum to the state population (the trace of
+    rho, of rho S for Gaussian modes), population errors are sorted and
+    non-negative, and <1> equals the norm (output.f90:88-140, 449-500)."""
+    from tests.helpers import small_lvc, small_gmctdh, random_state, with_expect
+    model = small_lvc() if builder == "lvc" else small_gmctdh()
+    if builder == "gmctdh":
+        initial_wavefunction(model)
+    model = with_expect(model)
+    A, psi = random_state(model, seed=11)
+    o = Oracle(model)
+    ev = o.expectation(A, psi)
+    obs = o.observables(A, psi, A, psi, 0.0)
+    assert abs(ev[0] - obs["norm"]) < 1e-12
+    assert abs(ev[1] - obs["pop"][0]) < 1e-12
+    assert abs(ev[2].imag) < 1e-12          # q is Hermitian
+    nat, ggp, perr = o.natpop(A, psi)
+    for (mode, s), w in nat.items():
+        assert np.all(np.diff(w) <= 1e-14)
+        assert abs(w.sum() - obs["pop"][s]) < 1e-10
+    for key, e in perr.items():
+        assert np.all(e >= 0) and np.all(np.diff(e) <= 0)
+        assert abs(ggp[key].sum() - obs["pop"][key[1]]) < 1e-10
+
+
+def test_expect_keyword_is_parsed(tmp_path):
+    model = lvc5(grid=[12, 10, 11, 9, 10], nspf=3, eps_int=1e-7)
+    path = write_inputs(model, str(tmp_path), "lvc")
+    with open(os.path.join(str(tmp_path), "q1.op"), "w") as fh:
+        fh.write("# position of dof 1\n1.0 | 1 | 1 q\n")
+    with open(path) as fh:
+        text = fh.read()
+    with open(path, "w") as fh:
+        fh.write("expect = q1.op\n" + text)
+    m2 = parse_input(path)
+    assert len(m2.expect) == 1 and len(m2.expect[0]) == m2.nstates
+    assert all(t.dof_ops == {0: 1} and t.lhs == t.rhs for t in m2.expect[0])
+    # the expectation operator's mode operators follow the Hamiltonian's
+    assert m2.nham == model.nham
+    assert np.array_equal(m2.ioper, model.ioper)
