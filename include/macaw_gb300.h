@@ -171,6 +171,14 @@ int64_t mctdh_observables(mctdh_ctx_t *ctx, double t, double *energy, double *po
 int64_t mctdh_expect(mctdh_ctx_t *ctx, double *values);
 int64_t mctdh_natpop(mctdh_ctx_t *ctx, double *natpop, double *ggp, double *poperr);
 int64_t mctdh_densmat(mctdh_ctx_t *ctx, int64_t mode, int64_t state, double *rho);
+/* Calc_Density (output.f90:332-445) along DOF `dof` (0-based) for every state:
+ * density(ngp, nstates).  Grid DOFs: the diagonal of the DOF's density matrix in
+ * the DVR, and with trafo = trafoDVR of the DOF (basis x grid, leading dimension
+ * ldt) density_pop(ngp, nstates), the populations of the basis functions
+ * underlying the DVR (trafo or density_pop NULL skips them).  Gaussian DOFs: the
+ * density on ngp equidistant points of [xmin, xmax] = dvrpar(1:2, dof). */
+int64_t mctdh_density(mctdh_ctx_t *ctx, int64_t dof, const double *trafo, int64_t ldt, double xmin,
+                      double xmax, double *density, double *density_pop);
 
 /* norm_wf (gmctdh_objects.f90:21) and WF_Ovl (gmctdh_objects.f90:101) on host buffers. */
 int64_t mctdh_norm_wf(mctdh_ctx_t *ctx, const double *A, const double *psi, double *norm);

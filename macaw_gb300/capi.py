@@ -80,6 +80,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_expect.argtypes = [vp, DP]
     lib.mctdh_natpop.argtypes = [vp, DP, DP, DP]
     lib.mctdh_densmat.argtypes = [vp, C.c_int64, C.c_int64, DP]
+    lib.mctdh_density.argtypes = [vp, C.c_int64, DP, C.c_int64, C.c_double, C.c_double, DP, DP]
     lib.mctdh_wf_ovl.argtypes = [vp, DP, DP, DP, DP, DP, DP]
     lib.mctdh_launch_count.argtypes = [vp]
     lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
@@ -135,7 +136,8 @@ def load_library() -> C.CDLL:
                  "mctdh_rk_attempt", "mctdh_cmf2_attempt",
                  "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
                  "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_step",
-                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
+                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density",
+                 "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
                  "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"):
         getattr(lib, name).restype = C.c_int64
     _lib = lib
@@ -146,7 +148,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_rk_attempt", "mctdh_cmf2_attempt",
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
-            "mctdh_expect", "mctdh_natpop", "mctdh_densmat",
+            "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
@@ -399,6 +401,22 @@ class GpuCore:
         rho = np.zeros((n, n), dtype=np.complex128, order="F")
         self._check(self.lib.mctdh_densmat(self.h, mode, state, rho.ctypes.data_as(DP)))
         return rho
+
+    def density(self, dof: int):
+        """Calc_Density (output.f90:332-445) along dof: (density, basis populations),
+        each (ngp, nstates); the populations are zero for Gaussian DOFs."""
+        m = self.model
+        ng = m.ngp[dof]
+        dens = np.zeros((ng, m.nstates), order="F")
+        pop = np.zeros((ng, m.nstates), order="F")
+        if m.dvr_type[dof] == "gwp":
+            x0, x1 = m.dvrpar[dof]
+            self._check(self.lib.mctdh_density(self.h, dof, None, 0, x0, x1, dens.ctypes.data_as(DP), None))
+        else:
+            tr = np.asfortranarray(m.trafo[dof])
+            self._check(self.lib.mctdh_density(self.h, dof, tr.ctypes.data_as(DP), ng, 0.0, 0.0,
+                                               dens.ctypes.data_as(DP), pop.ctypes.data_as(DP)))
+        return dens, pop
 
     def propagate_interval(self, int_type: int, tnext: float, t: float, step: float):
         tt, ss = C.c_double(t), C.c_double(step)

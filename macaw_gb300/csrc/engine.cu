@@ -3373,6 +3373,8 @@ struct WriterPlan {
   double* np_out = nullptr;       // natpop | ggp | poperr
   long long np_len = 0, ggp_off = 0, perr_off = 0;
   int nspfmax = 0;
+  std::map<int, cplx*> dens_scratch;     // dof -> Y (G x n) | DM (nG x nG)
+  std::map<int, double*> dens_out;       // dof -> density | pop | trafo (per state: 2 nG, then nG^2)
 };
 std::map<const Ctx*, WriterPlan*> g_writer;
 
@@ -3443,6 +3445,85 @@ void expectation(Ctx& c, cplx* values) {
   run_hole(c, W.dots);
   run_red(c, W.red);
   CK(cudaMemcpyAsync(values, W.res, sizeof(cplx) * c.nexpect, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  check_status(c);
+}
+
+// Calc_Density (output.f90:332-445) along one DOF for every state.
+void density(Ctx& c, int dof, const double* trafo, int ldt, double xmin, double xmax, double* dens, double* pop) {
+  WriterPlan& W = writer_plan(c);
+  int mode = -1, k = -1;
+  for (int m = 0; m < c.nmodes && mode < 0; ++m)
+    for (int q = 0; q < c.nmodedof[m]; ++q)
+      if (c.mode_dofs[m][q] == dof) { mode = m; k = q; }
+  if (mode < 0) throw StatusError(MCTDH_EARG, "dof not in any mode");
+  const int nG = c.ngp[dof];
+  if (nG < 2) throw StatusError(MCTDH_EARG, "density needs at least two grid points");
+  const bool gwp = c.is_gwp[mode];
+  if (!W.dens_out.count(dof)) {
+    W.dens_out[dof] = (double*)c.ar.alloc(sizeof(double) * (2LL * nG * c.nstates + (long long)nG * nG));
+    if (!gwp) {
+      int nmax = 0;
+      for (int s = 0; s < c.nstates; ++s) nmax = std::max(nmax, c.m_of(mode, s));
+      W.dens_scratch[dof] = c.ar.calloc_c((long long)c.gmode[mode] * nmax + (long long)nG * nG);
+    }
+  }
+  double* out = W.dens_out[dof];
+  double* d_trafo = out + 2LL * nG * c.nstates;
+  const bool with_pop = !gwp && trafo && pop;
+  if (with_pop) {
+    if (ldt < nG) throw StatusError(MCTDH_EARG, "trafo leading dimension below ngp");
+    for (int b = 0; b < nG; ++b)
+      CK(cudaMemcpyAsync(d_trafo + (long long)nG * b, trafo + (long long)ldt * b, sizeof(double) * nG,
+                         cudaMemcpyHostToDevice, c.st));
+  }
+  operators_and_mf(c, c.d_y);   // rho of the resident state (output.f90:35-41)
+  for (int s = 0; s < c.nstates; ++s) {
+    const int n = c.m_of(mode, s);
+    double* ds = out + (long long)nG * s;
+    double* ps = out + (long long)nG * (c.nstates + s);
+    if (gwp) {
+      const int i = c.gwp_of[mode];
+      DensGwpArgs a;
+      memset(&a, 0, sizeof(a));
+      a.xi = psi_block(c, c.d_y, mode, s);
+      a.a = c.gwpa_d + (size_t)c.gwp_lda * c.ns00max * i;
+      a.rho = c.rho[mode][s];
+      a.dens = ds;
+      a.x0 = xmin;
+      a.delta = (xmax - xmin) / (double)(nG - 1);
+      a.n = n;
+      a.nmd = c.nmodedof[mode];
+      a.lda = c.gwp_lda;
+      a.k = k;
+      a.nG = nG;
+      launch_density_gwp(a, c.st);
+    } else {
+      DensGridArgs a;
+      memset(&a, 0, sizeof(a));
+      int ll = 1, nl = 1;
+      for (int q = 0; q < k; ++q) ll *= c.ngp[c.mode_dofs[mode][q]];
+      for (int q = k + 1; q < c.nmodedof[mode]; ++q) nl *= c.ngp[c.mode_dofs[mode][q]];
+      a.phi = psi_block(c, c.d_y, mode, s);
+      a.rho = c.rho[mode][s];
+      a.Y = W.dens_scratch[dof];
+      a.DM = W.dens_scratch[dof] + (long long)c.gmode[mode] * n;
+      a.trafo = with_pop ? d_trafo : nullptr;
+      a.ldt = nG;
+      a.dens = ds;
+      a.pop = ps;
+      a.n = n;
+      a.nG = nG;
+      a.ll = ll;
+      a.nl = nl;
+      launch_density_grid(a, c.st);
+    }
+    c.count();
+  }
+  CK(cudaMemcpyAsync(dens, out, sizeof(double) * nG * c.nstates, cudaMemcpyDeviceToHost, c.st));
+  if (with_pop)
+    CK(cudaMemcpyAsync(pop, out + (long long)nG * c.nstates, sizeof(double) * nG * c.nstates,
+                       cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
   check_status(c);
 }
@@ -3934,6 +4015,14 @@ int64_t mctdh_natpop(mctdh_ctx_t* ctx, double* nat, double* ggp, double* poperr)
   if (!ctx || !nat) return MCTDH_EARG;
   Ctx* c = ctx->c;
   return guarded(c, [&] { natpop(*c, nat, ggp, poperr); });
+}
+
+int64_t mctdh_density(mctdh_ctx_t* ctx, int64_t dof, const double* trafo, int64_t ldt, double xmin, double xmax,
+                      double* dens, double* pop) {
+  if (!ctx || !dens) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  if (dof < 0 || dof >= c->ndof) return MCTDH_EARG;
+  return guarded(c, [&] { density(*c, (int)dof, trafo, (int)ldt, xmin, xmax, dens, pop); });
 }
 
 int64_t mctdh_densmat(mctdh_ctx_t* ctx, int64_t mode, int64_t state, double* rho) {

@@ -748,6 +748,101 @@ void launch_gwp_dderiv(const GwpDDerivDesc* d, int nd, const cplx* Din, cplx* Do
   gwp_dderiv_kernel<<<nd, 256, 0, st>>>(d, Din, Dout);
 }
 
+// ---------------------------------------------------------------------------
+// Calc_Density (output.f90:332-445)
+// ---------------------------------------------------------------------------
+// GauOvl1D (gmctdh_objects.f90:1476-1493): <g1|g2> of normalised 1D Gaussians
+__device__ cplx gau_ovl_1d(double a1, double a2, cplx xi1, cplx xi2) {
+  const cplx s = cadd(cconj(xi1), xi2);
+  cplx c = mkc(xi1.x * xi1.x / a1 + xi2.x * xi2.x / a2, 0.0);
+  c = csub(c, cdivr(cmul(s, s), a1 + a2));
+  const double a12 = a1 + a2;
+  return cscale(cexp_(cscale(c, 0.25)), sqrt(sqrt(4.0 * a1 * a2 / (a12 * a12))));
+}
+
+__device__ __forceinline__ cplx herm_el(const cplx* X, int n, int i, int j) {
+  cplx v = (i <= j) ? X[i + n * j] : cconj(X[j + n * i]);
+  if (i == j) v.y = 0.0;
+  return v;
+}
+
+// Grid DOF: Y_j = sum_j' rho(j, j') phi_j' (rho Hermitian from its upper
+// triangle), DM(kg1, kg2) = sum_r sum_j conj(phi_j(r, kg2)) Y_j(r, kg1) with r the
+// other DOFs of the mode (MatricisePsi, hamilton.f90:664-699), density = Re DM(kg, kg),
+// basis populations Re sum_ab T(kg, a) DM(a, b) T(kg, b).  One block.
+__global__ void __launch_bounds__(256) density_grid_kernel(DensGridArgs a) {
+  const int n = a.n, nG = a.nG, ll = a.ll, nl = a.nl;
+  const long long G = (long long)ll * nG * nl;
+  for (long long e = threadIdx.x; e < G * n; e += blockDim.x) {
+    const long long g = e % G;
+    const int j = (int)(e / G);
+    cplx v = mkc(0.0, 0.0);
+    for (int q = 0; q < n; ++q) v = cadd(v, cmul(herm_el(a.rho, n, j, q), a.phi[g + G * q]));
+    a.Y[e] = v;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nG * nG; e += blockDim.x) {
+    const int k1 = e % nG, k2 = e / nG;
+    cplx v = mkc(0.0, 0.0);
+    for (int j = 0; j < n; ++j)
+      for (int ro = 0; ro < nl; ++ro)
+        for (int ri = 0; ri < ll; ++ri) {
+          const long long b = ri + (long long)ll * nG * ro + G * j;
+          v = cadd(v, cmul(cconj(a.phi[b + (long long)ll * k2]), a.Y[b + (long long)ll * k1]));
+        }
+    a.DM[e] = v;
+  }
+  __syncthreads();
+  for (int kg = threadIdx.x; kg < nG; kg += blockDim.x) {
+    a.dens[kg] = a.DM[kg + nG * kg].x;
+    if (a.trafo) {
+      double p = 0.0;
+      for (int q = 0; q < nG; ++q) {
+        cplx v = mkc(0.0, 0.0);
+        for (int b = 0; b < nG; ++b) v = cadd(v, cscale(a.DM[q + nG * b], a.trafo[kg + a.ldt * b]));
+        p += a.trafo[kg + a.ldt * q] * v.x;
+      }
+      a.pop[kg] = p;
+    }
+  }
+}
+
+// Gaussian DOF k: density(x) = delta Re sum_{j1,j2} c(j1,j2) exp(x^2 (a1 + a2) + x (conj xi1 + xi2))
+// with c = rho(j1,j2) (4/pi^2 a1 a2 exp(Re xi1^2/a1 + Re xi2^2/a2))^(1/4) times the 1D
+// overlaps of the other DOFs (rho Hermitian from its upper triangle).  One block.
+__global__ void __launch_bounds__(256) density_gwp_kernel(DensGwpArgs a) {
+  __shared__ cplx cf[MAXN_SPF * MAXN_SPF];
+  const int n = a.n, k = a.k;
+  const double pi24 = 1.0 / (asin(1.0) * asin(1.0));
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int j1 = e % n, j2 = e / n;
+    const double a1 = a.a[k + a.lda * j1], a2 = a.a[k + a.lda * j2];
+    const cplx x1 = a.xi[k + a.nmd * j1], x2 = a.xi[k + a.nmd * j2];
+    cplx c = cscale(herm_el(a.rho, n, j1, j2), pow(pi24 * a1 * a2 * exp(x1.x * x1.x / a1 + x2.x * x2.x / a2), 0.25));
+    for (int q = 0; q < a.nmd; ++q) {
+      if (q == k) continue;
+      c = cmul(c, gau_ovl_1d(a.a[q + a.lda * j1], a.a[q + a.lda * j2], a.xi[q + a.nmd * j1], a.xi[q + a.nmd * j2]));
+    }
+    cf[e] = c;
+  }
+  __syncthreads();
+  for (int kg = threadIdx.x; kg < a.nG; kg += blockDim.x) {
+    const double x = a.x0 + a.delta * kg;
+    double d = 0.0;
+    for (int j2 = 0; j2 < n; ++j2)
+      for (int j1 = 0; j1 < n; ++j1) {
+        const double a12 = a.a[k + a.lda * j1] + a.a[k + a.lda * j2];
+        const cplx xs = cadd(cconj(a.xi[k + a.nmd * j1]), a.xi[k + a.nmd * j2]);
+        const cplx ex = cexp_(mkc(x * x * a12 + x * xs.x, x * xs.y));
+        d += cmul(cf[j1 + n * j2], ex).x;
+      }
+    a.dens[kg] = d * a.delta;
+  }
+}
+
+void launch_density_grid(const DensGridArgs& a, cudaStream_t st) { density_grid_kernel<<<1, 256, 0, st>>>(a); }
+void launch_density_gwp(const DensGwpArgs& a, cudaStream_t st) { density_gwp_kernel<<<1, 256, 0, st>>>(a); }
+
 void launch_gwp_ovl(const GwpOvlDesc* d, int nd, cudaStream_t st) {
   if (nd <= 0) return;
   gwp_ovl_kernel<<<nd, 256, 0, st>>>(d);

@@ -159,6 +159,28 @@ struct NatpopDesc {       // one (mode, state) block of the natural populations 
 };
 void launch_natpop(const NatpopDesc* d, int nd, int* status, cudaStream_t st);
 
+// Calc_Density (output.f90:332-445) of one state along one DOF
+struct DensGridArgs {      // grid DOF: SPFs phi(ll, nG, nl, n) of the mode, DOF in the middle
+  const cplx* phi;
+  const cplx* rho;         // n x n (upper triangle authoritative)
+  cplx* Y;                 // scratch G x n (rho applied to the SPFs)
+  cplx* DM;                // scratch nG x nG (density matrix of the DOF)
+  const double* trafo;     // basis x grid (ld ldt), or null
+  double* dens;            // nG
+  double* pop;             // nG (basis populations), with trafo
+  int n, nG, ll, nl, ldt, pad;
+};
+struct DensGwpArgs {       // Gaussian DOF k of a mode with nmd DOFs
+  const cplx* xi;          // parameters (nmd x n)
+  const double* a;         // widths (lda x n)
+  const cplx* rho;         // n x n
+  double* dens;            // nG
+  double x0, delta;
+  int n, nmd, lda, k, nG, pad;
+};
+void launch_density_grid(const DensGridArgs& a, cudaStream_t st);
+void launch_density_gwp(const DensGwpArgs& a, cudaStream_t st);
+
 struct SnapSeg {
   cplx* ptr;               // matrix storage
   long long offset;        // first index in the flat snapshot

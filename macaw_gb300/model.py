@@ -52,12 +52,13 @@ class ModelError(ValueError):
 # Primitive DVRs
 # ----------------------------------------------------------------------------
 
-def harm_dvr(n: int, x0: float, mw: float):
+def harm_dvr(n: int, x0: float, mw: float, with_trafo: bool = False):
     """Harmonic-oscillator DVR (dvr.f90:263-357).
 
     Returns grid, weights, d1 (d/dq), d2 (d^2/dq^2), xd1 (x d/dx + d/dx x)
-    as float64 arrays.  Eigenvector signs are fixed by making the first row
-    of the transformation non-negative, as the reference does (dvr.f90:287).
+    as float64 arrays, and with_trafo the DVR-to-FBR transformation trafoDVR
+    (basis x grid).  Eigenvector signs are fixed by making the first row of the
+    transformation non-negative, as the reference does (dvr.f90:287).
     """
     if n < 2:
         raise ModelError("too few grid points selected for a DVR")
@@ -101,11 +102,13 @@ def harm_dvr(n: int, x0: float, mw: float):
         aux[i + 1, i - 1] = aux[i - 1, i + 1]
     d2 = 0.5 * mw * (trafo.T @ (aux @ trafo))
     d2 = np.triu(d2) + np.triu(d2, 1).T
+    if with_trafo:
+        return grid, w, d1, d2, xd1, trafo
     return grid, w, d1, d2, xd1
 
 
-def sin_dvr(n: int, xi: float, xf: float):
-    """Sine (particle-in-a-box) DVR (dvr.f90:107-186)."""
+def sin_dvr(n: int, xi: float, xf: float, with_trafo: bool = False):
+    """Sine (particle-in-a-box) DVR (dvr.f90:107-186); with_trafo also trafoDVR."""
     if n < 2:
         raise ModelError("too few grid points selected for a DVR")
     dx = (xf - xi) / (n - 1)
@@ -142,6 +145,8 @@ def sin_dvr(n: int, xi: float, xf: float):
     fac = 0.5 * (math.pi / (xf - xi + 2 * dx)) ** 2
     d2 = -np.triu(d2) * fac
     d2 = d2 + np.triu(d2, 1).T
+    if with_trafo:
+        return grid, w, d1, d2, xd1, trafo
     return grid, w, d1, d2, xd1
 
 
@@ -221,17 +226,19 @@ class Model:
         self.d1: Dict[int, np.ndarray] = {}
         self.d2: Dict[int, np.ndarray] = {}
         self.xd1: Dict[int, np.ndarray] = {}
+        self.trafo: Dict[int, np.ndarray] = {}     # trafoDVR (basis x grid)
         for d in range(self.ndof):
             t = self.dvr_type[d]
             if t == "HO":
-                g, w, d1, d2, xd1 = harm_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1])
+                g, w, d1, d2, xd1, tr = harm_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1], True)
             elif t == "sin":
-                g, w, d1, d2, xd1 = sin_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1])
+                g, w, d1, d2, xd1, tr = sin_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1], True)
             elif t == "gwp":
                 continue
             else:
                 raise ModelError(f"DVR type {t!r} is not supported by this core")
             self.grid[d], self.wgrid[d], self.d1[d], self.d2[d], self.xd1[d] = g, w, d1, d2, xd1
+            self.trafo[d] = tr
         self.ngpm = {}
         for m in self.modes_dvr:
             self.ngpm[m] = int(np.prod([self.ngp[d] for d in self.mode_dofs[m]]))

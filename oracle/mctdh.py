@@ -215,6 +215,12 @@ def gau10_int_1d(a1: float, a2: float, xi1: complex, xi2: complex, iop: int) -> 
     raise OracleError(f"Gau10Int1D operator {iop} not restated")
 
 
+def gau_ovl_1d(a1: float, a2: float, xi1: complex, xi2: complex) -> complex:
+    """GauOvl1D (gmctdh_objects.f90:1476-1493): <g1|g2> of normalised 1D Gaussians."""
+    c = xi1.real ** 2 / a1 + xi2.real ** 2 / a2 - (np.conj(xi1) + xi2) ** 2 / (a1 + a2)
+    return np.exp(0.25 * c) * math.sqrt(math.sqrt(4 * a1 * a2 / (a1 + a2) ** 2))
+
+
 def gau_ovl_multid(a1: np.ndarray, a2: np.ndarray, xi1: np.ndarray, xi2: np.ndarray) -> complex:
     """Overlap of normalised multi-D Gaussians (GauOvlMultiD, gmctdh_objects.f90:1497-1519)."""
     if np.all(np.abs(a1 - a2) < _EPS):
@@ -1378,6 +1384,53 @@ class Oracle:
                 ggp[(mode, s)] = g
                 perr[(mode, s)] = np.sort(e)[::-1]
         return nat, ggp, perr
+
+    def density(self, A, psi, dof: int, trafo: Optional[np.ndarray] = None,
+                xrange: Optional[Tuple[float, float]] = None):
+        """Calc_Density (output.f90:332-445) along one DOF, per state.  Grid DOFs:
+        the density matrix in the coordinate representation of the DOF from rho and
+        the SPFs matricised along it (MatricisePsi, hamilton.f90:664-699), its
+        diagonal, and the populations of the basis functions trafo(kg, :) DM trafo(kg, :).
+        Gaussian DOFs: the density on ngp equidistant points of xrange from rho, the
+        Gaussian parameters and the 1D overlaps of the other DOFs of the mode."""
+        md = self.m
+        self._prepare(A, psi)
+        mode = next(m for m in range(md.nmodes) if dof in md.mode_dofs[m])
+        k = md.mode_dofs[mode].index(dof)
+        nG = md.ngp[dof]
+        dens = np.zeros((nG, md.nstates))
+        pop = np.zeros((nG, md.nstates))
+        if md.is_gwp_mode[mode]:
+            i = md.modes_gwp.index(mode)
+            delta = (xrange[1] - xrange[0]) / (nG - 1)
+            x = xrange[0] + delta * np.arange(nG)
+            nmd = len(md.mode_dofs[mode])
+            pi24 = 1.0 / math.asin(1.0) ** 2
+            for s in range(md.nstates):
+                xi, a = self.gwp_params(psi, i, s)
+                R = herm_from_upper(np.triu(self.rho[(mode, s)]))
+                ns = xi.shape[1]
+                for j1 in range(ns):
+                    for j2 in range(ns):
+                        a1, a2 = a[k, j1], a[k, j2]
+                        c = R[j1, j2] * (pi24 * a1 * a2 * math.exp(xi[k, j1].real ** 2 / a1
+                                                                   + xi[k, j2].real ** 2 / a2)) ** 0.25
+                        for kg in range(nmd):
+                            if kg != k:
+                                c *= gau_ovl_1d(a[kg, j1], a[kg, j2], xi[kg, j1], xi[kg, j2])
+                        dens[:, s] += (c * np.exp(x ** 2 * (a1 + a2) + x * (np.conj(xi[k, j1]) + xi[k, j2]))).real
+            return dens * delta, pop
+        ngs = [md.ngp[d] for d in md.mode_dofs[mode]]
+        for s in range(md.nstates):
+            phi = md.spf_block(psi, mode, s)
+            n = phi.shape[1]
+            P = np.moveaxis(phi.reshape(ngs + [n], order="F"), k, -2).reshape(-1, nG, n)
+            R = herm_from_upper(np.triu(self.rho[(mode, s)]))
+            DM = np.einsum("rbj,jq,raq->ab", P.conj(), R, P)
+            dens[:, s] = DM.diagonal().real
+            if trafo is not None:
+                pop[:, s] = np.einsum("ka,ab,kb->k", trafo, DM, trafo).real
+        return dens, pop
 
     def propagate(self, A, psi, tfinal: Optional[float] = None, max_steps: Optional[int] = None,
                   record_steps: bool = False):

@@ -65,3 +65,22 @@ def test_expectation_operators_leave_the_eom_unchanged(core_cls):
     dA, dpsi = core_cls(model).calc_derivs(A, psi, 0.0)
     assert np.linalg.norm(dA - ref_dA) < 1e-10 * np.linalg.norm(ref_dA)
     assert np.linalg.norm(dpsi - ref_dpsi) < 1e-10 * np.linalg.norm(ref_dpsi)
+
+
+@pytest.mark.parametrize("name,seed", [("qvc", 35), ("gmctdh", 36)])
+def test_density(core_cls, name, seed):
+    """Calc_Density along every DOF: grid DOFs (inner and outer DOF of two-DOF
+    modes) with the basis populations, and Gaussian DOFs."""
+    model = _model(name)
+    A, psi = random_state(model, seed=seed)
+    o = Oracle(model)
+    core = core_cls(model)
+    core.set_state(A, psi, as_start=True)
+    for dof in range(model.ndof):
+        dens, pop = core.density(dof)
+        if model.dvr_type[dof] == "gwp":
+            rd, _ = o.density(A, psi, dof, xrange=model.dvrpar[dof])
+        else:
+            rd, rp = o.density(A, psi, dof, trafo=model.trafo[dof])
+            assert np.abs(pop - rp).max() < TOL
+        assert np.abs(dens - rd).max() < TOL

@@ -217,3 +217,25 @@ def test_expect_keyword_is_parsed(tmp_path):
     # the expectation operator's mode operators follow the Hamiltonian's
     assert m2.nham == model.nham
     assert np.array_equal(m2.ioper, model.ioper)
+
+
+@pytest.mark.parametrize("builder", ["qvc", "gmctdh"])
+def test_density_oracle(builder):
+    """Calc_Density: on a grid DOF the density and the basis populations both sum to
+    the state population; on a Gaussian DOF the Riemann sum of the density over the
+    plotting range approaches it."""
+    from tests.helpers import small_qvc, small_gmctdh, random_state
+    model = small_qvc() if builder == "qvc" else small_gmctdh()
+    if builder == "gmctdh":
+        initial_wavefunction(model)
+    A, psi = random_state(model, seed=12)
+    o = Oracle(model)
+    pop = o.observables(A, psi, A, psi, 0.0)["pop"]
+    for dof in range(model.ndof):
+        if model.dvr_type[dof] == "gwp":
+            dens, _ = o.density(A, psi, dof, xrange=model.dvrpar[dof])
+            assert np.abs(dens.sum(axis=0) - pop).max() < 1e-3
+        else:
+            dens, bpop = o.density(A, psi, dof, trafo=model.trafo[dof])
+            assert np.abs(dens.sum(axis=0) - pop).max() < 1e-10
+            assert np.abs(bpop.sum(axis=0) - pop).max() < 1e-10
