@@ -230,9 +230,9 @@ struct OvlPlan {
 };
 
 struct DotPlan {
-  HoleBatch hb;
-  RedBatch red;
   cplx* res = nullptr;
+  cplx* partial = nullptr;     // DOT_BLOCKS block sums
+  unsigned* counter = nullptr; // blocks done (reset by the last one)
 };
 
 enum { KP_PROD, KP_HOLE, KP_RED, KP_H1, KP_REGINV, KP_TERMSUM, KP_SPF, KP_ELEM, KP_GWP, KP_N };
@@ -2020,15 +2020,16 @@ cplx* dot_dev(Ctx& c, const cplx* a, const cplx* b, long long n) {
   if (!P) {
     P = new DotPlan();
     P->res = c.ar.calloc_c(1);
-    int h = P->hb.add(c.ar, a, b, n, 1, 1, 1);
-    P->hb.finalize(c.ar);
-    int tg = P->red.add_target(P->res, 1, 1, 1, 0);
-    P->red.add_term(tg, P->hb.h[h], mkc(1, 0));
-    P->red.finalize(c.ar);
+    P->partial = c.ar.calloc_c(DOT_BLOCKS);
+    P->counter = (unsigned*)c.ar.alloc(sizeof(unsigned));
+    CK(cudaMemset(P->counter, 0, sizeof(unsigned)));
     c.dots[key] = P;
   }
-  run_hole(c, P->hb);
-  run_red(c, P->red);
+  {
+    ProfScope ps(c, KP_HOLE, 8.0 * (double)n, 32.0 * (double)n);
+    launch_dot(a, b, n, P->partial, P->counter, P->res, c.st);
+    c.count();
+  }
   return P->res;
 }
 

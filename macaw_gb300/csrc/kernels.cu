@@ -580,30 +580,29 @@ __device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, JacRot* R, bool* ok
       __syncwarp();
       if (ballot == 0) continue;
       any = true;
-      // column rotations: row `lane` of A and V
-      if (lane < n) {
-        for (int j = 0; j < npair; ++j) {
-          const JacRot& J = R[j];
-          if (!J.rot) continue;
-          const cplx uc = cconj(J.u);
-          cplx ap = A[lane + ld * J.p], aq = A[lane + ld * J.q];
-          A[lane + ld * J.p] = csub(cscale(ap, J.c), cscale(cmul(uc, aq), J.s));
-          A[lane + ld * J.q] = cadd(cscale(cmul(J.u, ap), J.s), cscale(aq, J.c));
-          cplx vp = V[lane + ld * J.p], vq = V[lane + ld * J.q];
-          V[lane + ld * J.p] = csub(cscale(vp, J.c), cscale(cmul(uc, vq), J.s));
-          V[lane + ld * J.q] = cadd(cscale(cmul(J.u, vp), J.s), cscale(vq, J.c));
-        }
+      // column rotations: work items (row, pair) spread over the lanes (one item per
+      // lane for n <= 8); pairs are disjoint, so items never share an element
+      for (int it = lane; it < n * npair; it += 32) {
+        const int row = it % n;
+        const JacRot& J = R[it / n];
+        if (!J.rot) continue;
+        const cplx uc = cconj(J.u);
+        cplx ap = A[row + ld * J.p], aq = A[row + ld * J.q];
+        A[row + ld * J.p] = csub(cscale(ap, J.c), cscale(cmul(uc, aq), J.s));
+        A[row + ld * J.q] = cadd(cscale(cmul(J.u, ap), J.s), cscale(aq, J.c));
+        cplx vp = V[row + ld * J.p], vq = V[row + ld * J.q];
+        V[row + ld * J.p] = csub(cscale(vp, J.c), cscale(cmul(uc, vq), J.s));
+        V[row + ld * J.q] = cadd(cscale(cmul(J.u, vp), J.s), cscale(vq, J.c));
       }
       __syncwarp();
-      // row rotations: column `lane` of A
-      if (lane < n) {
-        for (int j = 0; j < npair; ++j) {
-          const JacRot& J = R[j];
-          if (!J.rot) continue;
-          cplx ap = A[J.p + ld * lane], aq = A[J.q + ld * lane];
-          A[J.p + ld * lane] = csub(cscale(ap, J.c), cscale(cmul(J.u, aq), J.s));
-          A[J.q + ld * lane] = cadd(cscale(cmul(cconj(J.u), ap), J.s), cscale(aq, J.c));
-        }
+      // row rotations: items (column, pair)
+      for (int it = lane; it < n * npair; it += 32) {
+        const int col = it % n;
+        const JacRot& J = R[it / n];
+        if (!J.rot) continue;
+        cplx ap = A[J.p + ld * col], aq = A[J.q + ld * col];
+        A[J.p + ld * col] = csub(cscale(ap, J.c), cscale(cmul(J.u, aq), J.s));
+        A[J.q + ld * col] = cadd(cscale(cmul(cconj(J.u), ap), J.s), cscale(aq, J.c));
       }
       __syncwarp();
       // the rotated 2x2 blocks in closed form (other pairs never touch them)
@@ -782,6 +781,62 @@ void launch_natpop(const NatpopDesc* d, int nd, int* status, cudaStream_t st) {
   natpop_kernel<<<nd, 32, 0, st>>>(d, status);
 }
 
+// ---------------------------------------------------------------------------
+// <a|b> over a whole vector in FP64 (zdotc): each of DOT_BLOCKS blocks sums a
+// grid-stride range (warp shuffles, then warps in order), and the last block to
+// finish adds the block sums in block order, so the result does not depend on
+// the blocks' timing.  The counter is reset for the next launch (graph replays).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ cplx warp_sum_c(cplx v) {
+  for (int off = 16; off > 0; off >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(256) dot_kernel(const cplx* __restrict__ a, const cplx* __restrict__ b,
+                                                  long long n, cplx* partial, unsigned* counter, cplx* out) {
+  __shared__ cplx ws[8];
+  __shared__ bool last;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  cplx s = mkc(0.0, 0.0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + tid; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const cplx x = a[i], y = b[i];
+    s.x = fma(x.x, y.x, fma(x.y, y.y, s.x));
+    s.y = fma(x.x, y.y, fma(-x.y, y.x, s.y));
+  }
+  s = warp_sum_c(s);
+  if (lane == 0) ws[warp] = s;
+  __syncthreads();
+  if (tid == 0) {
+    cplx t = ws[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t = cadd(t, ws[w]);
+    partial[blockIdx.x] = t;
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (warp == 0) {
+    cplx t = mkc(0.0, 0.0);
+    for (int q = lane; q < (int)gridDim.x; q += 32) {
+      const volatile double* pv = (const volatile double*)partial;
+      t = cadd(t, mkc(pv[2 * q], pv[2 * q + 1]));
+    }
+    t = warp_sum_c(t);
+    if (lane == 0) {
+      *out = t;
+      *counter = 0u;
+    }
+  }
+}
+void launch_dot(const cplx* a, const cplx* b, long long n, cplx* partial, unsigned* counter, cplx* out,
+                cudaStream_t st) {
+  dot_kernel<<<DOT_BLOCKS, 256, 0, st>>>(a, b, n, partial, counter, out);
+}
+
 // Tridiagonal eigenproblem of the Lanczos matrix (dstev, cmf2_integration.f90:85)
 __global__ void tridiag_kernel(const double* alpha, const double* beta, int n, double* evals, double* evecs,
                                int* status) {
@@ -951,58 +1006,46 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
   }
 }
 
-__global__ void spf_solve_kernel(const SpfDesc* __restrict__ descs, int* status) {
-  __shared__ cplx S[MAXN_SPF * MAXN_SPF];
-  __shared__ cplx O[MAXN_SPF * MAXN_SPF];
+// (phi^H phi) X = phi^H dphi (zposv 'U') by Gauss-Jordan elimination of [S | O]
+// without pivoting, which is stable for the Hermitian positive definite S: each of
+// the n steps is one pivot reciprocal, then one scale and one update per element
+// across all threads (a short dependent path, unlike the column-serial Cholesky
+// and the per-right-hand-side triangular solves).  A non-positive pivot is the
+// zposv failure (DEVST_CHOL_FAIL).
+__global__ void __launch_bounds__(256) spf_solve_kernel(const SpfDesc* __restrict__ descs, int* status) {
+  __shared__ cplx M[MAXN_SPF * 2 * MAXN_SPF];   // M[i + ld * c], c < n: S, c >= n: O
+  __shared__ cplx s_pinv;
+  __shared__ int s_fail;
   const SpfDesc& d = descs[blockIdx.x];
   const int n = d.n, ld = MAXN_SPF;
+  if (threadIdx.x == 0) s_fail = 0;
   for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
     const int which = pr / (n * n), q = pr % (n * n);
     const int j1 = q % n, j2 = q / n;
     cplx s = mkc(0, 0);
     for (int t = 0; t < d.ntile; ++t) s = cadd(s, d.partial[(long long)t * 2 * n * n + pr]);
-    if (which == 0) S[j1 + ld * j2] = s; else O[j1 + ld * j2] = s;
+    M[j1 + ld * (j2 + which * n)] = s;
   }
   __syncthreads();
-  // zposv('U'): S = U^H U by columns (row j of U finished by all threads), then
-  // one thread per right-hand side for the two triangular solves
-  __shared__ int s_fail;
-  if (threadIdx.x == 0) s_fail = 0;
-  __syncthreads();
-  for (int j = 0; j < n; ++j) {
+  for (int k = 0; k < n; ++k) {
     if (threadIdx.x == 0) {
-      double djj = S[j + ld * j].x;
-      for (int k = 0; k < j; ++k) djj -= cabs2(S[k + ld * j]);
-      if (!(djj > 0.0)) { s_fail = 1; djj = 1e-300; }
-      S[j + ld * j] = mkc(sqrt(djj), 0.0);
+      const cplx p = M[k + ld * k];
+      if (!(p.x > 0.0)) s_fail = 1;
+      const double den = p.x * p.x + p.y * p.y;
+      s_pinv = (den > 0.0) ? mkc(p.x / den, -p.y / den) : mkc(0.0, 0.0);
     }
     __syncthreads();
-    const double inv = 1.0 / S[j + ld * j].x;
-    for (int i = j + 1 + (int)threadIdx.x; i < n; i += blockDim.x) {
-      cplx sji = S[j + ld * i];
-      for (int k = 0; k < j; ++k) sji = csub(sji, cmul(cconj(S[k + ld * j]), S[k + ld * i]));
-      S[j + ld * i] = cscale(sji, inv);
+    for (int c = k + 1 + (int)threadIdx.x; c < 2 * n; c += blockDim.x) M[k + ld * c] = cmul(s_pinv, M[k + ld * c]);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * 2 * n; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      if (i == k || c <= k) continue;
+      M[i + ld * c] = csub(M[i + ld * c], cmul(M[i + ld * k], M[k + ld * c]));
     }
     __syncthreads();
-  }
-  __shared__ double invd[MAXN_SPF];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) invd[i] = 1.0 / S[i + ld * i].x;
-  __syncthreads();
-  for (int cidx = threadIdx.x; cidx < n; cidx += blockDim.x) {
-    for (int i = 0; i < n; ++i) {
-      cplx v = O[i + ld * cidx];
-      for (int k = 0; k < i; ++k) v = csub(v, cmul(cconj(S[k + ld * i]), O[k + ld * cidx]));
-      O[i + ld * cidx] = cscale(v, invd[i]);
-    }
-    for (int i = n - 1; i >= 0; --i) {
-      cplx v = O[i + ld * cidx];
-      for (int k = i + 1; k < n; ++k) v = csub(v, cmul(S[i + ld * k], O[k + ld * cidx]));
-      O[i + ld * cidx] = cscale(v, invd[i]);
-    }
   }
   if (threadIdx.x == 0 && s_fail) atomicOr(status, DEVST_CHOL_FAIL);
-  __syncthreads();
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) d.X[e] = O[(e % n) + ld * (e / n)];
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) d.X[e] = M[(e % n) + ld * (n + e / n)];
 }
 
 __global__ void __launch_bounds__(256) spf_proj_kernel(const SpfDesc* __restrict__ descs, int ndesc,
@@ -1033,7 +1076,7 @@ void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp
   if (ndesc <= 0) return;
   if (prec > 0) spf_tile_split_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   else spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
-  spf_solve_kernel<<<ndesc, 128, 0, st>>>(d_descs, d_status);
+  spf_solve_kernel<<<ndesc, 256, 0, st>>>(d_descs, d_status);
   spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
 }
 

@@ -255,6 +255,11 @@ void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, c
 void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
                      double* alpha_out, long long n, cudaStream_t st);
 void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st);
+// <a|b> = sum_i conj(a_i) b_i in FP64 into *out, one launch, fixed summation order.
+// partial: DOT_BLOCKS complex scratch; counter: one zero-initialised unsigned.
+#define DOT_BLOCKS 304
+void launch_dot(const cplx* a, const cplx* b, long long n, cplx* partial, unsigned* counter, cplx* out,
+                cudaStream_t st);
 void launch_snap(const SnapSeg* segs, int nseg, cplx* flat, long long E, int scatter, cudaStream_t st);
 void launch_mfx_features(const MfxHist& hz, const MfxCoef& c, double* S, float* X, long long E, cudaStream_t st);
 void launch_mfx_combine(const MfxHist& hz, const MfxCoef& c, const float* Y, const double* S, cplx* half, cplx* full,
