@@ -69,14 +69,23 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29)));
 }
 
-// Element i of a tensor in either storage format (TF_C64 / TF_SPLIT).
+// Element i of a tensor in any storage format: 0 complex128, 1 FP32 split pairs
+// (re hi, im hi, re lo, im lo) in 16 bytes, 2 complex FP32 (re, im) in 8 bytes.
 __device__ __forceinline__ cplx load_c(const cplx* p, long long i, int fmt) {
   if (!fmt) return p[i];
+  if (fmt == 2) {
+    const float2 v = reinterpret_cast<const float2*>(p)[i];
+    return make_double2(f2d_exact(v.x), f2d_exact(v.y));
+  }
   const float4 w = reinterpret_cast<const float4*>(p)[i];
   return make_double2(f2d_exact(w.x) + f2d_exact(w.z), f2d_exact(w.y) + f2d_exact(w.w));
 }
 // ... as an FP32 (re hi, im hi, re lo, im lo) split
 __device__ __forceinline__ float4 load_split(const cplx* p, long long i, int fmt) {
+  if (fmt == 2) {
+    const float2 v = reinterpret_cast<const float2*>(p)[i];
+    return make_float4(v.x, v.y, 0.f, 0.f);
+  }
   if (fmt) return reinterpret_cast<const float4*>(p)[i];
   const cplx v = p[i];
   float4 w;

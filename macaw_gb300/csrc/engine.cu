@@ -12,6 +12,7 @@
 #include <set>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/macaw_gb300.h"
@@ -949,8 +950,9 @@ void plan_eom(Ctx& c) {
     c.gmat[kv.first] = md.out;
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
-    c.gprods.add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0, TF_C64, chain_fmt);
-    srcs[s].push_back(SumSrc{out, c.der, chain_fmt});
+    const int gfmt = c.precision == 1 ? TF_F32 : chain_fmt;   // FP32 products in precision 1
+    c.gprods.add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0, TF_C64, gfmt);
+    srcs[s].push_back(SumSrc{out, c.der, gfmt});
   }
   for (int s = 0; s < c.nstates; ++s)
     if (c0[s].x != 0.0 || c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_in + c.aoff[s], cmul(c.der, c0[s])});
@@ -1160,42 +1162,69 @@ void plan_hb(Ctx& c) {
     }
   }
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
-  const int chain_fmt = c.precision ? TF_SPLIT : TF_C64;
-  for (int t : c.general_terms) {
-    const int s1 = c.lhs[t], s2 = c.rhs[t];
-    TRef cur;
-    cur.p = c.d_hbin + c.aoff[s2];
-    cur.shape = c.shape_of(s2);
-    int depth = 0;
-    for (int m : c.modes_dvr) {
-      const int k = c.ioper[m + f * t];
-      if (c.is_identity[m + f * k]) continue;
-      const int n1 = c.m_of(m, s1);
-      std::vector<int> ns = cur.shape;
-      ns[m] = n1;
-      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
-      ++depth;
-      c.hb_chains[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0, cur.fmt, chain_fmt);
-      cur.p = out;
-      cur.shape = ns;
-      cur.fmt = chain_fmt;
+  // FP32 products (precision 1) keep complex FP32 intermediates; compensated ones the split pairs
+  const int chain_fmt = c.precision == 1 ? TF_F32 : (c.precision ? TF_SPLIT : TF_C64);
+  // The general terms of one state pair share products: each pair's chains form a
+  // prefix tree over the modes, with the modes on which all of the pair's terms
+  // carry the same matrix first (the SPF overlaps between two state sets, for
+  // example), so a product common to several terms is computed once.  The order
+  // of the mode products changes only the rounding; a pair with one term keeps the
+  // reference order (grid modes, then Gaussian modes with D^H h D).
+  std::vector<int> base_order = c.modes_dvr;
+  base_order.insert(base_order.end(), c.modes_gwp.begin(), c.modes_gwp.end());
+  auto hb_mat = [&](int t, int m) -> const cplx* {
+    const int k = c.ioper[m + f * t];
+    if (c.is_identity[m + f * k]) return nullptr;   // identity; D^H S D = 1 on Gaussian modes
+    return c.is_gwp[m] ? c.dhd[c.gwp_of[m]][k] : c.hmat[m][k];
+  };
+  std::map<std::pair<int, int>, std::vector<int>> pair_terms;
+  for (int t : c.general_terms) pair_terms[std::make_pair(c.lhs[t], c.rhs[t])].push_back(t);
+  for (auto& pt : pair_terms) {
+    const int s1 = pt.first.first, s2 = pt.first.second;
+    const std::vector<int>& terms = pt.second;
+    std::vector<int> order = base_order;
+    std::vector<int> distinct(f, 0);
+    for (int m : order) {
+      std::set<const cplx*> mats;
+      for (int t : terms) mats.insert(hb_mat(t, m));
+      distinct[m] = (int)mats.size();
     }
-    // Gaussian modes act through D^H h D; their identity is skipped (D^H S D = 1)
-    for (size_t i = 0; i < c.modes_gwp.size(); ++i) {
-      const int m = c.modes_gwp[i];
-      const int k = c.ioper[m + f * t];
-      if (c.is_identity[m + f * k]) continue;
-      const int n1 = c.m_of(m, s1);
-      std::vector<int> ns = cur.shape;
-      ns[m] = n1;
-      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
-      ++depth;
-      c.hb_chains[depth].add(cur.p, out, c.dhd[i][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0, cur.fmt, chain_fmt);
-      cur.p = out;
-      cur.shape = ns;
-      cur.fmt = chain_fmt;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return distinct[a] < distinct[b]; });
+    struct Node {
+      TRef ref;
+      int depth;
+    };
+    std::vector<Node> nodes(1);
+    nodes[0].ref.p = c.d_hbin + c.aoff[s2];
+    nodes[0].ref.shape = c.shape_of(s2);
+    nodes[0].depth = 0;
+    std::map<std::tuple<int, int, const cplx*>, int> child;   // (node, mode, matrix) -> node
+    for (int t : terms) {
+      int cur = 0;
+      for (int m : order) {
+        const cplx* mat = hb_mat(t, m);
+        if (!mat) continue;
+        const auto key = std::make_tuple(cur, m, mat);
+        auto it = child.find(key);
+        if (it != child.end()) {
+          cur = it->second;
+          continue;
+        }
+        const int n1 = c.m_of(m, s1);
+        Node nd;
+        nd.ref.shape = nodes[cur].ref.shape;
+        nd.ref.shape[m] = n1;
+        nd.ref.p = c.ar.calloc_c(prod_range(nd.ref.shape, 0, f));
+        nd.ref.fmt = chain_fmt;
+        nd.depth = nodes[cur].depth + 1;
+        c.hb_chains[nd.depth].add(nodes[cur].ref.p, nd.ref.p, mat, n1, 0, nodes[cur].ref.shape, m, n1, mkc(1, 0), 0,
+                                  nodes[cur].ref.fmt, chain_fmt);
+        nodes.push_back(nd);
+        child[key] = (int)nodes.size() - 1;
+        cur = (int)nodes.size() - 1;
+      }
+      srcs[s1].push_back(SumSrc{nodes[cur].ref.p, c.ae[t], nodes[cur].ref.fmt});
     }
-    srcs[s1].push_back(SumSrc{cur.p, c.ae[t], cur.fmt});
   }
   for (auto& kv : c.gmat) {
     const int s = kv.first.first, m = kv.first.second;

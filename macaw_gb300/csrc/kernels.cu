@@ -43,8 +43,10 @@ __device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al,
   sl += t + e;
 }
 
-// PREC 0: FP64.  PREC 1: split FP32 -- x and M are split into hi + lo FP32 parts
-// and x*M = xh*Mh + xh*Ml + xl*Mh is accumulated in FP32.  PREC 2: the same split
+// PREC 0: FP64.  PREC 1: FP32 -- the products of the FP32-rounded x and M are
+// accumulated in FP32 (~1e-7 relative; the split's correction products would sit
+// at the accumulation's own rounding level), outputs complex FP32 (TF_F32) or
+// FP64.  PREC 2: x and M split into hi + lo FP32 parts, x*M = xh*Mh + xh*Ml + xl*Mh
 // with the sum carried as an FP32 hi/lo pair (compensated), ~1e-13 relative.
 template <int MAXN, int PREC>
 __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
@@ -106,12 +108,11 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
         cplxf acc = make_float2(0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < MAXN; ++j)
-          if (j < nin) {
-            const cplxf mh = Mh[jo + MAXN * j], ml = Ml[jo + MAXN * j];
-            acc = cfmaf_(acc, mh, xh[j]);
-            acc = cfmaf_(acc, mh, xl[j]);
-            acc = cfmaf_(acc, ml, xh[j]);
-          }
+          if (j < nin) acc = cfmaf_(acc, Mh[jo + MAXN * j], xh[j]);
+        if (d.yfmt == TF_F32) {   // 8-byte elements: index from the tensor's base
+          reinterpret_cast<float2*>(d.Y)[l + L * ((long long)nout * r + jo)] = acc;
+          continue;
+        }
         if (d.yfmt) {
           y0f[L * jo] = make_float4(acc.x, acc.y, 0.f, 0.f);
           continue;

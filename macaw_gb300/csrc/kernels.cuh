@@ -18,7 +18,7 @@
 // bytes per element as FP32 (re hi, im hi, re lo, im lo), re = hi + lo to
 // ~2^-48 relative: intermediates of the split-precision chains stay in this
 // form, so neither side of a chain step converts through the FP64 pipe.
-enum { TF_C64 = 0, TF_SPLIT = 1 };
+enum { TF_C64 = 0, TF_SPLIT = 1, TF_F32 = 2 };
 
 struct ProdDesc {
   const cplx* X;
