@@ -368,6 +368,9 @@ struct Ctx {
   ProdBatch gprods;                            // G_{s,m} x_m A_s
   // H_B * B plan for CMF2 (Calc_DHD_B): reads d_hbin, writes d_hb
   cplx* d_hbin = nullptr;
+  cplx* d_hbin32 = nullptr;   // precision 1: d_hbin as complex FP32, the input of the H_B products
+  FusedDot hb_dot{nullptr, nullptr, nullptr, nullptr};    // <d_hbin | H_B d_hbin> in the term sum
+  FusedDot lan_nrm{nullptr, nullptr, nullptr, nullptr};   // ||Kn||^2 in the Lanczos axpy
   std::vector<ProdBatch> hb_chains;
   std::vector<SumSrc> hbsrc_h;
   SumSrc* hbsrc_d = nullptr;
@@ -854,8 +857,8 @@ void plan_eom(Ctx& c) {
   // reference's left/right chains.
   c.chains.assign(f + 1, ProdBatch());
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
-  // split-precision contexts keep chain intermediates in the split storage format
-  const int chain_fmt = c.precision ? TF_SPLIT : TF_C64;
+  // chain intermediates: complex FP32 in precision 1, FP32 split pairs in precision 2
+  const int chain_fmt = c.precision == 1 ? TF_F32 : (c.precision ? TF_SPLIT : TF_C64);
   std::map<std::pair<int, int>, int> mf_target;   // (m,k) -> red target
   auto mf_tg = [&](int im, int k) {
     auto key = std::make_pair(im, k);
@@ -959,19 +962,20 @@ void plan_eom(Ctx& c) {
   c.c0 = c0;
   c.msum_d = upload_vec(c.ar, c.msum_h);
   c.msum_src_d = upload_vec(c.ar, c.msum_src_h);
-  // Precision: the pre-summed products feed only dA and run in the context's
-  // precision.  The chains and contractions of the mean fields use the
-  // compensated split (about 1e-13 relative) whenever a split mode is chosen,
-  // because the regularised inverse of rho scales mean-field errors by up to
-  // 1/eps_rho.  The density matrices themselves stay FP64.
+  // Precision: the chain products run in the context's precision (FP32 in
+  // precision 1).  The contractions of the mean fields and density matrices use
+  // the compensated split (about 1e-13 relative) whenever a split mode is chosen:
+  // the regularised inverse of rho scales mean-field errors by up to 1/eps_rho.
   for (auto& b : c.chains) {
-    b.prec = c.precision ? 2 : 0;
+    b.prec = c.precision;
     b.finalize(c.ar);
   }
   c.gprods.prec = c.precision;
   c.gprods.finalize(c.ar);
   c.holes.prec = c.precision ? 2 : 0;
   c.holes.finalize(c.ar);
+  // density matrices: compensated split FP32 (~1e-13 relative) in the split modes
+  c.rho_holes.prec = c.precision ? 2 : 0;
   c.rho_holes.finalize(c.ar);
   for (auto& hr : rrefs) c.red.add_term(hr.target, c.rho_holes.h[hr.hole], hr.alpha);
   for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha);
@@ -1056,6 +1060,7 @@ void plan_eom(Ctx& c) {
     c.sum_h.push_back(r);
   }
   c.sum_d = upload_vec(c.ar, c.sum_h);
+  split_coeffs(c.src_h);
   c.src_d = upload_vec(c.ar, c.src_h);
   for (auto& b : c.gwp_rho_chain) b.finalize(c.ar);
   if (!c.modes_gwp.empty()) plan_gwp_derivs(c);
@@ -1164,6 +1169,13 @@ void plan_hb(Ctx& c) {
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
   // FP32 products (precision 1) keep complex FP32 intermediates; compensated ones the split pairs
   const int chain_fmt = c.precision == 1 ? TF_F32 : (c.precision ? TF_SPLIT : TF_C64);
+  // precision 1 reads the Krylov vector once converted to complex FP32 (8-byte
+  // elements: state offsets count float2)
+  const int hb_in_fmt = c.precision == 1 ? TF_F32 : TF_C64;
+  auto hb_in_at = [&](int s) -> cplx* {
+    if (hb_in_fmt == TF_F32) return reinterpret_cast<cplx*>(reinterpret_cast<float2*>(c.d_hbin32) + c.aoff[s]);
+    return c.d_hbin + c.aoff[s];
+  };
   // The general terms of one state pair share products: each pair's chains form a
   // prefix tree over the modes, with the modes on which all of the pair's terms
   // carry the same matrix first (the SPF overlaps between two state sets, for
@@ -1195,7 +1207,8 @@ void plan_hb(Ctx& c) {
       int depth;
     };
     std::vector<Node> nodes(1);
-    nodes[0].ref.p = c.d_hbin + c.aoff[s2];
+    nodes[0].ref.p = hb_in_at(s2);
+    nodes[0].ref.fmt = hb_in_fmt;
     nodes[0].ref.shape = c.shape_of(s2);
     nodes[0].depth = 0;
     std::map<std::tuple<int, int, const cplx*>, int> child;   // (node, mode, matrix) -> node
@@ -1231,7 +1244,7 @@ void plan_hb(Ctx& c) {
     const int n = c.m_of(m, s);
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
-    c.hb_chains[1].add(c.d_hbin + c.aoff[s], out, kv.second, n, 0, sh, m, n, mkc(1, 0), 0, TF_C64, chain_fmt);
+    c.hb_chains[1].add(hb_in_at(s), out, kv.second, n, 0, sh, m, n, mkc(1, 0), 0, hb_in_fmt, chain_fmt);
     srcs[s].push_back(SumSrc{out, mkc(1, 0), chain_fmt});
   }
   for (int s = 0; s < c.nstates; ++s)
@@ -1251,6 +1264,7 @@ void plan_hb(Ctx& c) {
     ranges.push_back(r);
   }
   c.hbsum_d = upload_vec(c.ar, ranges);
+  split_coeffs(c.hbsrc_h);
   c.hbsrc_d = upload_vec(c.ar, c.hbsrc_h);
 }
 
@@ -2033,10 +2047,15 @@ void bs_step(Ctx& c, double t, double htry, double* hdid, double* hnext) {
 // ---------------------------------------------------------------------------
 // CMF2 (cmf2_base.f90:47-206) for DVR models
 // ---------------------------------------------------------------------------
-void hb(Ctx& c, const cplx* B, cplx* out) {
+void hb(Ctx& c, const cplx* B, cplx* out, bool with_dot = false) {
   if (B != c.d_hbin) CK(cudaMemcpyAsync(c.d_hbin, B, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
+  if (c.d_hbin32) {
+    launch_to_f32(c.d_hbin32, c.d_hbin, c.naconftot, c.st);
+    c.count();
+  }
   for (size_t i = 1; i < c.hb_chains.size(); ++i) run_prod(c, c.hb_chains[i]);
-  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st, c.precision);
+  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st, c.precision,
+                 with_dot ? c.hb_dot : FusedDot{nullptr, nullptr, nullptr, nullptr});
   c.count();
   c.hb_count++;
 }
@@ -2086,9 +2105,10 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
     run_graphed(c, 4, B0, [&] {
       launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st);
       c.count();
-      hb(c, K, K + n);
-      launch_lan_axpy(K + n, K, nullptr, dot_dev(c, K, K + n, n), nullptr, d_alpha, n, c.st);
-      launch_lan_normalize(K + n, K + n, dot_dev(c, K + n, K + n, n), d_beta, n, c.st);
+      // alpha = <K|H_B K> in the term sum, ||K'||^2 in the axpy
+      hb(c, K, K + n, true);
+      launch_lan_axpy(K + n, K, nullptr, c.hb_dot.res, nullptr, d_alpha, n, c.st, c.lan_nrm);
+      launch_lan_normalize(K + n, K + n, c.lan_nrm.res, d_beta, n, c.st);
       c.count(2);
     });
     double beta[NKRYLOV_MAX] = {0};
@@ -2102,9 +2122,9 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
       cplx* Kn = K + (long long)j * n;
       cplx* Kp = K + (long long)(j - 2) * n;
       run_graphed(c, 3, Kn, [&] {
-        hb(c, Kj, Kn);
-        launch_lan_axpy(Kn, Kj, Kp, dot_dev(c, Kj, Kn, n), d_beta + (j - 2), d_alpha + (j - 1), n, c.st);
-        launch_lan_normalize(Kn, Kn, dot_dev(c, Kn, Kn, n), d_beta + (j - 1), n, c.st);
+        hb(c, Kj, Kn, true);
+        launch_lan_axpy(Kn, Kj, Kp, c.hb_dot.res, d_beta + (j - 2), d_alpha + (j - 1), n, c.st, c.lan_nrm);
+        launch_lan_normalize(Kn, Kn, c.lan_nrm.res, d_beta + (j - 1), n, c.st);
         c.count(2);
       });
       CK(cudaMemcpyAsync(&beta[j - 1], d_beta + (j - 1), sizeof(double), cudaMemcpyDeviceToHost, c.st));
@@ -2915,6 +2935,19 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
     if (!mb) {
       // CMF2 / Lanczos buffers (ensemble members integrate with RK only)
       c->d_hbin = c->ar.calloc_c(c->naconftot);
+      if (c->precision == 1) c->d_hbin32 = c->ar.calloc_c((c->naconftot + 1) / 2);
+      {
+        // block sums of the fused Lanczos dots (one per block of the 256-thread launches)
+        const long long nb = (c->naconftot + 255) / 256;
+        for (FusedDot* fd : {&c->hb_dot, &c->lan_nrm}) {
+          fd->partial = c->ar.calloc_c(nb);
+          fd->counter = (unsigned*)c->ar.alloc(sizeof(unsigned));
+          CK(cudaMemset(fd->counter, 0, sizeof(unsigned)));
+          fd->res = c->ar.calloc_c(1);
+        }
+        c->hb_dot.v = c->d_hbin;
+        c->lan_nrm.v = c->d_hbin;   // any non-null vector requests the norm
+      }
       c->d_hb = c->ar.calloc_c(c->naconftot);
       c->d_krylov = c->ar.calloc_c(c->naconftot * (NKRYLOV_MAX + 1));
       c->d_lan = (double*)c->ar.alloc(sizeof(double) * (3 * NKRYLOV_MAX + NKRYLOV_MAX * NKRYLOV_MAX));
@@ -3145,6 +3178,7 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
     E->spf_d = upload_vec(E->ar, E->spf_h);
     E->spfop_d = upload_vec(E->ar, E->spfop_h);
     E->sum_d = upload_vec(E->ar, E->sum_h);
+    split_coeffs(E->src_h);
     E->src_d = upload_vec(E->ar, E->src_h);
     E->ov_spf_holes.finalize(E->ar);
     E->ov_spf_red.finalize(E->ar);

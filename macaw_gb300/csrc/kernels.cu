@@ -67,8 +67,12 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
       float hx, lx, hy, ly;
       split_d2f(v.x, hx, lx);
       split_d2f(v.y, hy, ly);
-      Mh[jo + MAXN * ji] = make_float2(hx, hy);
-      Ml[jo + MAXN * ji] = make_float2(lx, ly);
+      if (PREC == 1) {
+        Mh[jo + MAXN * ji] = make_float2(hx + lx, hy + ly);   // rounded to nearest
+      } else {
+        Mh[jo + MAXN * ji] = make_float2(hx, hy);
+        Ml[jo + MAXN * ji] = make_float2(lx, ly);
+      }
     }
   }
   __syncthreads();
@@ -97,14 +101,19 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
 #pragma unroll
     for (int j = 0; j < MAXN; ++j) {
       const float4 w = (j < nin) ? load_split(d.X, xi0 + L * j, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
-      xh[j] = make_float2(w.x, w.y);
-      xl[j] = make_float2(w.z, w.w);
+      if (PREC == 1) {
+        xh[j] = make_float2(w.x + w.z, w.y + w.w);   // rounded to nearest
+      } else {
+        xh[j] = make_float2(w.x, w.y);
+        xl[j] = make_float2(w.z, w.w);
+      }
     }
     const bool unit_alpha = (alpha.x == 1.0 && alpha.y == 0.0);
     float4* y0f = reinterpret_cast<float4*>(y0);
     for (int jo = 0; jo < nout; ++jo) {
       cplx accd;
       if (PREC == 1) {
+        // FP32 values rounded to nearest: hi + lo of the split, added in FP32
         cplxf acc = make_float2(0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < MAXN; ++j)
@@ -1084,63 +1093,120 @@ void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp
 // ---------------------------------------------------------------------------
 // Elementwise helpers
 // ---------------------------------------------------------------------------
+// The launch-wide sum of one complex value per thread, in a fixed order: warps,
+// then the block's warps into partial[blockIdx.x]; the last block to finish adds
+// the block sums in block order into *out and resets the counter (graph replays).
+// Every thread of every block calls it (no early returns before it).
+__device__ __forceinline__ cplx warp_sum_cd(cplx v) {
+  for (int off = 16; off > 0; off >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+  }
+  return v;
+}
+__device__ void grid_sum_c(cplx v, cplx* partial, unsigned* counter, cplx* out) {
+  __shared__ cplx ws[32];
+  __shared__ bool last;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum_cd(v);
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  if (tid == 0) {
+    cplx t = ws[0];
+    for (int w = 1; w < nw; ++w) t = cadd(t, ws[w]);
+    partial[blockIdx.x] = t;
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const volatile double* pv = (const volatile double*)partial;
+  cplx t = mkc(0.0, 0.0);
+  for (int q = tid; q < (int)gridDim.x; q += blockDim.x) t = cadd(t, mkc(pv[2 * q], pv[2 * q + 1]));
+  t = warp_sum_cd(t);
+  __syncthreads();
+  if (lane == 0) ws[warp] = t;
+  __syncthreads();
+  if (tid == 0) {
+    cplx r = ws[0];
+    for (int w = 1; w < nw; ++w) r = cadd(r, ws[w]);
+    *out = r;
+    *counter = 0u;
+  }
+}
+
+// out = sum of coeff * src per state range; with dotv also the launch-wide
+// <dotv|out> (FP64 products of the values written) into dot->res.
+// Grid-stride over the elements (a capped grid keeps the fused sum's block count,
+// and with it the counter's atomics, small).
 __global__ void termsum_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges, int nr,
-                               const SumSrc* __restrict__ srcs, long long total) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
+                               const SumSrc* __restrict__ srcs, long long total, FusedDot dot) {
+  cplx d = mkc(0, 0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
+    }
+    const SumRange& rg = ranges[lo];
+    const long long li = i - rg.offset;
+    if (li < 0 || li >= rg.n) continue;
+    cplx acc = mkc(0, 0);
+    for (int k = 0; k < rg.count; ++k) {
+      const SumSrc& s = srcs[rg.first + k];
+      cfma(acc, s.coeff, load_c(s.src, li, s.fmt));
+    }
+    out[i] = acc;
+    if (dot.v) cfma_conj(d, dot.v[i], acc);
   }
-  const SumRange& rg = ranges[lo];
-  const long long li = i - rg.offset;
-  if (li < 0 || li >= rg.n) return;
-  cplx acc = mkc(0, 0);
-  for (int k = 0; k < rg.count; ++k) {
-    const SumSrc& s = srcs[rg.first + k];
-    cfma(acc, s.coeff, load_c(s.src, li, s.fmt));
-  }
-  out[i] = acc;
+  if (dot.v) grid_sum_c(d, dot.partial, dot.counter, dot.res);
 }
 
 // Split-precision variant: every coeff * src product accumulated as a
 // compensated FP32 pair (df_fma, ~1e-13 relative); one FP64 add per output.
 __global__ void termsum_split_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges, int nr,
-                                     const SumSrc* __restrict__ srcs, long long total) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
+                                     const SumSrc* __restrict__ srcs, long long total, FusedDot dot) {
+  cplx d = mkc(0, 0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
+    }
+    const SumRange& rg = ranges[lo];
+    const long long li = i - rg.offset;
+    if (li < 0 || li >= rg.n) continue;
+    {
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      for (int k = 0; k < rg.count; ++k) {
+        const SumSrc& s = srcs[rg.first + k];
+        const float ch = s.cs[0], cl = s.cs[1], dh = s.cs[2], dl = s.cs[3];
+        const float4 x = load_split(s.src, li, s.fmt);
+        // (c + i d)(xr + i xi)
+        df_fma(rh, rl, ch, cl, x.x, x.z);
+        df_fma(rh, rl, -dh, -dl, x.y, x.w);
+        df_fma(ih, il, ch, cl, x.y, x.w);
+        df_fma(ih, il, dh, dl, x.x, x.z);
+      }
+      const cplx val = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+      out[i] = val;
+      if (dot.v) cfma_conj(d, dot.v[i], val);
+    }
   }
-  const SumRange& rg = ranges[lo];
-  const long long li = i - rg.offset;
-  if (li < 0 || li >= rg.n) return;
-  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-  for (int k = 0; k < rg.count; ++k) {
-    const SumSrc& s = srcs[rg.first + k];
-    float ch, cl, dh, dl;
-    split_d2f(s.coeff.x, ch, cl);
-    split_d2f(s.coeff.y, dh, dl);
-    const float4 x = load_split(s.src, li, s.fmt);
-    // (c + i d)(xr + i xi)
-    df_fma(rh, rl, ch, cl, x.x, x.z);
-    df_fma(rh, rl, -dh, -dl, x.y, x.w);
-    df_fma(ih, il, ch, cl, x.y, x.w);
-    df_fma(ih, il, dh, dl, x.x, x.z);
-  }
-  out[i] = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+  if (dot.v) grid_sum_c(d, dot.partial, dot.counter, dot.res);
 }
 
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs, long long total,
-                    cudaStream_t st, int prec) {
+                    cudaStream_t st, int prec, FusedDot dot) {
   if (total <= 0) return;
+  const unsigned nb = (unsigned)std::min<long long>((total + 255) / 256, FUSED_BLOCKS);
   if (prec > 0)
-    termsum_split_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total);
+    termsum_split_kernel<<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
   else
-    termsum_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total);
+    termsum_kernel<<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
 }
 
 __global__ void stage_kernel(cplx* __restrict__ out, const cplx* __restrict__ base, StageArgs a, double dt,
@@ -1256,6 +1322,21 @@ __global__ void axpy_kernel(cplx* y, const cplx* x, cplx a, long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) { cplx v = y[i]; cfma(v, a, x[i]); y[i] = v; }
 }
+// complex FP64 -> complex FP32 rounded to nearest (the FP64 pipe stays idle)
+__global__ void to_f32_kernel(float2* __restrict__ out, const cplx* __restrict__ in, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cplx v = in[i];
+  float hx, lx, hy, ly;
+  split_d2f(v.x, hx, lx);
+  split_d2f(v.y, hy, ly);
+  out[i] = make_float2(hx + lx, hy + ly);
+}
+void launch_to_f32(cplx* out, const cplx* in, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<float2*>(out), in, n);
+}
+
 void launch_axpy(cplx* y, const cplx* x, cplx a, long long n, cudaStream_t st) {
   if (n <= 0) return;
   axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, x, a, n);
@@ -1417,25 +1498,32 @@ void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, c
 // Kn <- (Kn - beta_prev * Kp) - alpha * Kj, alpha = Re <Kj|Kn> (two zaxpy in the
 // reference order), then Kn <- Kn / ||Kn||.
 // ---------------------------------------------------------------------------
+// ... and with nrm.res the launch-wide ||Kn||^2 of the new Kn (the next normalisation)
 __global__ void lan_axpy_kernel(cplx* __restrict__ Kn, const cplx* __restrict__ Kj, const cplx* __restrict__ Kp,
                                 const cplx* __restrict__ dot_alpha, const double* __restrict__ beta_prev,
-                                double* alpha_out, long long n) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+                                double* alpha_out, long long n, FusedDot nrm) {
+  const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const double alpha = dot_alpha->x;
-  if (i == 0) *alpha_out = alpha;
-  if (i >= n) return;
-  cplx v = Kn[i];
-  if (Kp) {
-    const double b = *beta_prev;
-    cplx p = Kp[i];
-    v = mkc(fma(-b, p.x, v.x), fma(-b, p.y, v.y));
+  if (i0 == 0) *alpha_out = alpha;
+  const double b = Kp ? *beta_prev : 0.0;
+  double s2 = 0.0;
+  for (long long i = i0; i < n; i += (long long)gridDim.x * blockDim.x) {
+    cplx v = Kn[i];
+    if (Kp) {
+      cplx p = Kp[i];
+      v = mkc(fma(-b, p.x, v.x), fma(-b, p.y, v.y));
+    }
+    cplx q = Kj[i];
+    const cplx w = mkc(fma(-alpha, q.x, v.x), fma(-alpha, q.y, v.y));
+    Kn[i] = w;
+    s2 = fma(w.x, w.x, fma(w.y, w.y, s2));
   }
-  cplx q = Kj[i];
-  Kn[i] = mkc(fma(-alpha, q.x, v.x), fma(-alpha, q.y, v.y));
+  if (nrm.res) grid_sum_c(mkc(s2, 0.0), nrm.partial, nrm.counter, nrm.res);
 }
 void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
-                     double* alpha_out, long long n, cudaStream_t st) {
-  lan_axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Kn, Kj, Kp, dot_alpha, beta_prev, alpha_out, n);
+                     double* alpha_out, long long n, cudaStream_t st, FusedDot nrm) {
+  const unsigned nb = (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, FUSED_BLOCKS));
+  lan_axpy_kernel<<<nb, 256, 0, st>>>(Kn, Kj, Kp, dot_alpha, beta_prev, alpha_out, n, nrm);
 }
 
 // Grid-stride: the norm and its reciprocal once per thread (FP64 square roots and

@@ -7,6 +7,7 @@
 // touched, element (l, j, r) sits at l + L*(j + n*r), with L = prod of the
 // sizes of the faster modes and R = prod of the sizes of the slower modes.
 #pragma once
+#include <vector>
 #include "common.cuh"
 
 #define MAXDOF_MODE 4     // primitive DOFs combined in one DVR logical mode
@@ -129,7 +130,18 @@ struct SumSrc {
   cplx coeff;
   int fmt;                 // TF_*
   int pad;
+  float cs[4];             // coeff split into FP32 pairs (re hi, re lo, im hi, im lo), set by split_coeffs
 };
+// Fill SumSrc::cs from coeff for the compensated term sums (host, before upload).
+inline void split_coeffs(std::vector<SumSrc>& v) {
+  for (auto& s : v) {
+    const float rh = (float)s.coeff.x, ih = (float)s.coeff.y;
+    s.cs[0] = rh;
+    s.cs[1] = (float)(s.coeff.x - (double)rh);
+    s.cs[2] = ih;
+    s.cs[3] = (float)(s.coeff.y - (double)ih);
+  }
+}
 
 // out (n1 x n2, ld n1) = sum_k coeff_k * src_k  (operators pre-summed per state and mode)
 struct MatSumDesc {
@@ -222,8 +234,19 @@ void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int*
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
                 cplx der_factor, int* d_status, cudaStream_t st, int prec);
 // prec > 0: compensated split-FP32 accumulation (termsum_split_kernel)
+// A sum over a whole launch fused into a streaming kernel: v the vector to dot
+// with (termsum: <v|out>; Lanczos axpy: any non-null v requests ||Kn||^2), partial
+// one complex per block of the launch, counter zero-initialised, result in res.
+#define FUSED_BLOCKS 608   // grid of the streaming kernels that carry a fused sum (4 per SM)
+struct FusedDot {
+  const cplx* v;
+  cplx* partial;
+  unsigned* counter;
+  cplx* res;
+};
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
-                    long long total, cudaStream_t st, int prec);
+                    long long total, cudaStream_t st, int prec,
+                    FusedDot dot = FusedDot{nullptr, nullptr, nullptr, nullptr});
 void launch_stage(cplx* out, const cplx* base, const StageArgs& a, double dt, long long n, cudaStream_t st);
 // Bulirsch-Stoer: the last modified-midpoint stage 0.5 (am + an + dt d) (mmid,
 // integrator.f90:550-551) and one polynomial-extrapolation column (pzextr, :559-608)
@@ -242,6 +265,8 @@ void launch_ens_accept(cplx* y, const cplx* src, const int* accept, const long l
                        cudaStream_t st);
 void launch_copy_scale(cplx* out, const cplx* in, cplx s, long long n, cudaStream_t st);
 void launch_axpy(cplx* y, const cplx* x, cplx a, long long n, cudaStream_t st);
+// out (complex FP32, TF_F32 storage) = in rounded to nearest
+void launch_to_f32(cplx* out, const cplx* in, long long n, cudaStream_t st);
 void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* coef, int ncol, long long n,
                       cudaStream_t st);
 void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, double* evals, double* evecs,
@@ -253,7 +278,8 @@ void launch_masked_copy(cplx* y, const cplx* src, const unsigned char* elem_mode
                         long long n, cudaStream_t st);
 void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, cudaStream_t st);
 void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
-                     double* alpha_out, long long n, cudaStream_t st);
+                     double* alpha_out, long long n, cudaStream_t st,
+                     FusedDot nrm = FusedDot{nullptr, nullptr, nullptr, nullptr});
 void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st);
 // <a|b> = sum_i conj(a_i) b_i in FP64 into *out, one launch, fixed summation order.
 // partial: DOT_BLOCKS complex scratch; counter: one zero-initialised unsigned.
