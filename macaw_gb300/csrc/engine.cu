@@ -308,6 +308,9 @@ struct Ctx {
 
   cudaStream_t st = nullptr;
   bool own_stream = true;   // false for ensemble members (the ensemble's stream)
+  // a second stream for CMF2 work that runs beside the Lanczos build (own contexts only)
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool member = false;      // ensemble member: RK only, state vectors owned by the ensemble
   DevArena ar;
   int* d_status = nullptr;
@@ -427,6 +430,9 @@ struct Ctx {
   ~Ctx() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     if (h_scal) cudaFreeHost(h_scal);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (st2) cudaStreamDestroy(st2);
   }
   int m_of(int m, int s) const { return nspf[m + nmodes * s]; }
   std::vector<int> shape_of(int s) const {
@@ -1482,6 +1488,15 @@ void run_graphed(Ctx& c, int kind, const void* key, F&& body) {
   c.hb_count += it->second.hbs;
 }
 
+// Issue the enclosed launches on another stream of the context (the launch
+// helpers all use c.st).
+struct StreamSwap {
+  Ctx& c;
+  cudaStream_t old;
+  StreamSwap(Ctx& ctx, cudaStream_t s) : c(ctx), old(ctx.st) { c.st = s; }
+  ~StreamSwap() { c.st = old; }
+};
+
 void run_prod(Ctx& c, const ProdBatch& b) {
   if (b.h.empty()) return;
   ProfScope ps(c, KP_PROD, b.flops, b.bytes);
@@ -1530,7 +1545,13 @@ void gwp_derivs_run(Ctx& c, cplx* out) {
 // EOM on d_in -> out (full vector [dA | dpsi]).  mf_only: only the operator
 // matrices, density matrices, mean fields and rho^-1 MF that CMF2 consumes
 // (cmf2_base.f90:78-87, 122-130); the coefficient and SPF derivatives are skipped.
-void eom(Ctx& c, cplx* out, bool mf_only = false) {
+void run_reginv(Ctx& c) {
+  ProfScope ps(c, KP_REGINV);
+  launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
+  c.count();
+}
+
+void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   const bool gwp = !c.modes_gwp.empty();
   if (gwp) gwp_setup_run(c);
   {
@@ -1547,11 +1568,7 @@ void eom(Ctx& c, cplx* out, bool mf_only = false) {
   run_hole(c, c.rho_holes);
   run_hole(c, c.holes);
   run_red(c, c.red);
-  {
-    ProfScope ps(c, KP_REGINV);
-    launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
-    c.count();
-  }
+  if (reginv || !mf_only) run_reginv(c);
   if (mf_only) {
     c.eom_count++;
     return;
@@ -2092,16 +2109,29 @@ cplx dot_now(Ctx& c, const cplx* a, const cplx* b, long long n) {
 const double EPS_B = 1e-8;  // cmf2_integration.f90:13
 const int NKRYLOV_MAX = 20; // cmf2_integration.f90:11
 
-// Lanczos (cmf2_integration.f90:30-103) from B0 (device, naconftot) into BT.
-void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
+// Lanczos (cmf2_integration.f90:30-103) as issue / check steps, so that the
+// Krylov build can run on one stream while other work runs on another: lan_issue
+// launches the next Krylov step (one CUDA graph) and the copy of its beta into
+// pinned memory, lan_check applies the stopping rule once the stream is idle,
+// lan_finish diagonalises the tridiagonal matrix and forms BT.  alpha_j, beta_j
+// stay on the device (d_lan[0..19], d_lan[20..39]).
+struct LanRun {
+  const cplx* B0 = nullptr;
+  double dt = 0.0, error = 0.0;
+  int j = 0;          // 0 before the first step; then the index of the next Krylov vector
+  int nk = 0;
+  bool done = false;
+};
+
+void lan_issue(Ctx& c, LanRun& R) {
   const long long n = c.naconftot;
   cplx* K = c.d_krylov;
-  if (build) {
-    // alpha_j, beta_j stay on the device (d_lan[0..19], d_lan[20..39]); only beta_j
-    // comes back for the stopping rule: one host synchronisation per Krylov vector
-    double* d_alpha = c.d_lan;
-    double* d_beta = c.d_lan + NKRYLOV_MAX;
+  double* d_alpha = c.d_lan;
+  double* d_beta = c.d_lan + NKRYLOV_MAX;
+  double* h_beta = c.h_scal + 64;   // pinned
+  if (R.j == 0) {
     // each Krylov step is a fixed launch sequence on fixed buffers: CUDA graphs
+    const cplx* B0 = R.B0;
     run_graphed(c, 4, B0, [&] {
       launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st);
       c.count();
@@ -2111,43 +2141,60 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
       launch_lan_normalize(K + n, K + n, c.lan_nrm.res, d_beta, n, c.st);
       c.count(2);
     });
-    double beta[NKRYLOV_MAX] = {0};
-    CK(cudaMemcpyAsync(&beta[0], d_beta, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-    CK(cudaStreamSynchronize(c.st));
-    double error = beta[0] * fabs(dt);
-    int j = 2;
-    while (true) {
-      if (j == NKRYLOV_MAX) throw StatusError(MCTDH_EKRYLOV, "Maximum number of Krylov vectors reached");
-      cplx* Kj = K + (long long)(j - 1) * n;
-      cplx* Kn = K + (long long)j * n;
-      cplx* Kp = K + (long long)(j - 2) * n;
-      run_graphed(c, 3, Kn, [&] {
-        hb(c, Kj, Kn, true);
-        launch_lan_axpy(Kn, Kj, Kp, c.hb_dot.res, d_beta + (j - 2), d_alpha + (j - 1), n, c.st, c.lan_nrm);
-        launch_lan_normalize(Kn, Kn, c.lan_nrm.res, d_beta + (j - 1), n, c.st);
-        c.count(2);
-      });
-      CK(cudaMemcpyAsync(&beta[j - 1], d_beta + (j - 1), sizeof(double), cudaMemcpyDeviceToHost, c.st));
-      CK(cudaStreamSynchronize(c.st));
-      error = error * beta[j - 1] / (double)j * fabs(dt);
-      if (error < EPS_B) break;
-      ++j;
-    }
-    const int nk = j;
-    launch_jacobi_tridiag(c.d_lan, c.d_lan + NKRYLOV_MAX, nk, c.d_lan + 2 * NKRYLOV_MAX,
-                          c.d_lan + 3 * NKRYLOV_MAX, c.d_status, c.st);
-    c.count();
-    c.lan_evals.assign(nk, 0.0);
-    c.lan_evecs.assign(nk * nk, 0.0);
-    CK(cudaMemcpyAsync(c.lan_evals.data(), c.d_lan + 2 * NKRYLOV_MAX, sizeof(double) * nk, cudaMemcpyDeviceToHost, c.st));
-    CK(cudaMemcpyAsync(c.lan_evecs.data(), c.d_lan + 3 * NKRYLOV_MAX, sizeof(double) * nk * nk,
-                       cudaMemcpyDeviceToHost, c.st));
-    CK(cudaStreamSynchronize(c.st));
-    check_status(c);
-    c.lan_nk = nk;
+    CK(cudaMemcpyAsync(h_beta, d_beta, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    return;
   }
+  const int j = R.j;
+  if (j == NKRYLOV_MAX) throw StatusError(MCTDH_EKRYLOV, "Maximum number of Krylov vectors reached");
+  cplx* Kj = K + (long long)(j - 1) * n;
+  cplx* Kn = K + (long long)j * n;
+  cplx* Kp = K + (long long)(j - 2) * n;
+  run_graphed(c, 3, Kn, [&] {
+    hb(c, Kj, Kn, true);
+    launch_lan_axpy(Kn, Kj, Kp, c.hb_dot.res, d_beta + (j - 2), d_alpha + (j - 1), n, c.st, c.lan_nrm);
+    launch_lan_normalize(Kn, Kn, c.lan_nrm.res, d_beta + (j - 1), n, c.st);
+    c.count(2);
+  });
+  CK(cudaMemcpyAsync(h_beta + (j - 1), d_beta + (j - 1), sizeof(double), cudaMemcpyDeviceToHost, c.st));
+}
+
+// after the stream is idle: error = beta_1 |dt|, then error * beta_j / j * |dt| < eps_B
+// (cmf2_integration.f90:64-80)
+void lan_check(Ctx& c, LanRun& R) {
+  const double* h_beta = c.h_scal + 64;
+  if (R.j == 0) {
+    R.error = h_beta[0] * fabs(R.dt);
+    R.j = 2;
+    return;
+  }
+  R.error = R.error * h_beta[R.j - 1] / (double)R.j * fabs(R.dt);
+  if (R.error < EPS_B) {
+    R.done = true;
+    R.nk = R.j;
+  } else {
+    ++R.j;
+  }
+}
+
+void lan_finish(Ctx& c, LanRun& R) {
+  const int nk = R.nk;
+  launch_jacobi_tridiag(c.d_lan, c.d_lan + NKRYLOV_MAX, nk, c.d_lan + 2 * NKRYLOV_MAX,
+                        c.d_lan + 3 * NKRYLOV_MAX, c.d_status, c.st);
+  c.count();
+  c.lan_evals.assign(nk, 0.0);
+  c.lan_evecs.assign(nk * nk, 0.0);
+  CK(cudaMemcpyAsync(c.lan_evals.data(), c.d_lan + 2 * NKRYLOV_MAX, sizeof(double) * nk, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaMemcpyAsync(c.lan_evecs.data(), c.d_lan + 3 * NKRYLOV_MAX, sizeof(double) * nk * nk,
+                     cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  check_status(c);
+  c.lan_nk = nk;
+}
+
+// BT = sum_j BK_j * (sum_r U_jr U_1r exp(f alpha_r dt)), renormalised (:85-99)
+void lan_combine(Ctx& c, cplx* BT, double dt) {
+  const long long n = c.naconftot;
   const int nk = c.lan_nk;
-  // BT = sum_j BK_j * (sum_r U_jr U_1r exp(f alpha_r dt))
   std::vector<cplx> coef(nk, mkc(0, 0));
   for (int r = 0; r < nk; ++r) {
     double u1 = c.lan_evecs[0 + nk * r];
@@ -2160,17 +2207,34 @@ void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
     }
   }
   CK(cudaMemcpyAsync(c.d_coef, coef.data(), sizeof(cplx) * nk, cudaMemcpyHostToDevice, c.st));
-  launch_gemv_cols(BT, K, n, c.d_coef, nk, n, c.st);
+  launch_gemv_cols(BT, c.d_krylov, n, c.d_coef, nk, n, c.st);
   launch_lan_normalize(BT, BT, dot_dev(c, BT, BT, n), nullptr, n, c.st);
   c.count(2);
 }
 
+// Lanczos from B0 (device, naconftot) into BT on the context's stream; build =
+// false reuses the last Krylov space (cmf2_base.f90:189).
+void lanczos(Ctx& c, const cplx* B0, cplx* BT, double dt, bool build) {
+  if (build) {
+    LanRun R;
+    R.B0 = B0;
+    R.dt = dt;
+    while (!R.done) {
+      lan_issue(c, R);
+      CK(cudaStreamSynchronize(c.st));
+      lan_check(c, R);
+    }
+    lan_finish(c, R);
+  }
+  lan_combine(c, BT, dt);
+}
+
 // operators and mean fields on the state y (Calc_rho1mode, Calc_h1mode,
 // Calc_MeanField, Calc_rhom1MF): one EOM into d_out (the derivative is unused).
-void operators_and_mf(Ctx& c, const cplx* y) {
-  run_graphed(c, 2, y, [&] {
+void operators_and_mf(Ctx& c, const cplx* y, bool reginv = true) {
+  run_graphed(c, reginv ? 2 : 5, y, [&] {
     if (y != c.d_in) CK(cudaMemcpyAsync(c.d_in, y, sizeof(cplx) * c.ntot, cudaMemcpyDeviceToDevice, c.st));
-    eom(c, c.d_out, true);
+    eom(c, c.d_out, true, reginv);
   });
 }
 
@@ -2230,6 +2294,14 @@ struct CmfState {
   std::vector<GwpOvlDesc> gerr_h;                               // Calc_Err_SPF overlaps
   GwpOvlDesc* gerr_d = nullptr;
   std::vector<ProdBatch> a2b, b2a_half, b2a_end;                // A_to_B, B_to_A chains
+  double* h_dt = nullptr;    // pinned host copies: per-mode step lengths, errors, accept flags
+  double* h_err = nullptr;
+  int* h_acc = nullptr;
+  ~CmfState() {
+    if (h_dt) cudaFreeHost(h_dt);
+    if (h_err) cudaFreeHost(h_err);
+    if (h_acc) cudaFreeHost(h_acc);
+  }
 };
 std::map<const Ctx*, CmfState*> g_cmf;
 
@@ -2451,8 +2523,142 @@ void plan_cmf(Ctx& c, CmfState& S) {
   S.dt_mode = (double*)c.ar.alloc(sizeof(double) * 64);
   S.accept = (int*)c.ar.alloc(sizeof(int) * 64);
   S.err_mode = (double*)c.ar.alloc(sizeof(double) * 64);
+  CK(cudaMallocHost(&S.h_dt, sizeof(double) * 64));
+  CK(cudaMallocHost(&S.h_err, sizeof(double) * 64));
+  CK(cudaMallocHost(&S.h_acc, sizeof(int) * 64));
   if (f > 64) throw StatusError(MCTDH_EUNSUPPORTED, "more than 64 modes");
   S.planned = true;
+}
+
+// The SPF integration of one CMF2 half step as issue / check steps (like LanRun),
+// so it can run on a second stream while the Lanczos build runs on the first.
+struct SpfRun {
+  double dt_total = 0.0;
+  cplx* y = nullptr;
+  cplx* Dy = nullptr;
+  bool dp = false, finished = false;
+  int iter = 0;
+  std::vector<double> done, dtry;
+  std::vector<int> active;
+};
+
+void spf_begin(Ctx& c, SpfRun& R, double dt_total, cplx* y, cplx* Dy) {
+  if (c.int_type_psi != 1 && c.int_type_psi != 2)
+    throw StatusError(MCTDH_EUNSUPPORTED, "SPF integrator must be rk45 (1) or dopri (2)");
+  const int f = c.nmodes;
+  R.dt_total = dt_total;
+  R.y = y;
+  R.Dy = Dy;
+  R.dp = c.int_type_psi == 2;
+  R.done.assign(f, 0.0);
+  R.dtry.assign(f, 0.0);
+  R.active.assign(f, 0);
+  for (int m : c.modes_dvr) {
+    R.active[m] = 1;
+    R.dtry[m] = dt_total;
+  }
+  for (int m : c.modes_gwp) {
+    R.active[m] = 1;
+    R.dtry[m] = dt_total;
+  }
+  R.finished = false;
+  for (int m = 0; m < f; ++m) R.finished = R.finished || R.active[m];
+  R.finished = !R.finished;
+}
+
+// one RK attempt of every active mode on the context's stream, and the copy of
+// the per-mode errors into pinned memory
+void spf_issue(Ctx& c, CmfState& S, SpfRun& R) {
+  const int f = c.nmodes;
+  const bool dp = R.dp;
+  cplx* y = R.y;
+  cplx* Dy = R.Dy;
+  const long long nA = c.naconftot;
+  if (R.iter > 100000) throw StatusError(MCTDH_ESTEP, "SPF integration did not finish");
+  ++R.iter;
+  ++S.rk_iters;
+  for (int m = 0; m < 64; ++m) S.h_dt[m] = (m < f && R.active[m]) ? R.dtry[m] : 0.0;
+  CK(cudaMemcpyAsync(S.dt_mode, S.h_dt, sizeof(double) * 64, cudaMemcpyHostToDevice, c.st));
+  // one RK attempt of every mode: the same launches on the same buffers each
+  // iteration (the step lengths live in S.dt_mode), so it runs as a CUDA graph
+  run_graphed(c, 1, y, [&] {
+    copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
+    if (S.gwp) copy_dev(c, S.Din, Dy, S.nD);
+    spf_eval_all(c, S, c.d_k[0], S.Dk[0]);
+    for (int st = 1; st < 6; ++st) {
+      stage_modes(c, S, c.d_in, y, dp ? DP_B[st] : CK_B[st], st);
+      stage_D(c, S, S.Din, Dy, dp ? DP_B[st] : CK_B[st], st);
+      spf_eval_all(c, S, c.d_k[st], S.Dk[st]);
+    }
+    if (dp) {
+      // the 7th stage is the derivative at the 5th-order solution (:386-393)
+      stage_modes(c, S, c.d_in, y, DP_C, 6);
+      stage_D(c, S, S.Din, Dy, DP_C, 6);
+      spf_eval_all(c, S, c.d_k[6], S.Dk[6]);
+      stage_modes(c, S, c.d_tmp, y, DP_C, 6);
+      stage_D(c, S, S.Dtmp, Dy, DP_C, 6);
+      stage_modes(c, S, c.d_err, y, DP_D, 7);
+    } else {
+      stage_modes(c, S, c.d_tmp, y, CK_C, 6);
+      stage_D(c, S, S.Dtmp, Dy, CK_C, 6);
+      stage_modes(c, S, c.d_err, y, CK_D, 6);
+    }
+    StageArgs a;
+    memset(&a, 0, sizeof(a));
+    a.k[0] = c.d_err + nA;
+    a.c[0] = -1.0;
+    a.nk = 1;
+    launch_stage(S.ytmp + nA, c.d_tmp + nA, a, 1.0, c.dimpsi, c.st);
+    c.count();
+    run_hole(c, S.err_holes);
+    run_red(c, S.err_red);
+    if (S.gwp) {
+      launch_gwp_ovl(S.gerr_d, (int)S.gerr_h.size(), c.st);
+      c.count();
+    }
+    launch_spf_err(S.errd_d, (int)S.errd_h.size(), S.err_mode, f, c.st);
+    c.count();
+  });
+  CK(cudaMemcpyAsync(S.h_err, S.err_mode, sizeof(double) * f, cudaMemcpyDeviceToHost, c.st));
+}
+
+// after the stream is idle: each mode's rk_SPF_ck / propagate_SPF control
+// (cmf2_integration.f90:231-248, cmf2_base.f90:225-237), then the accepted modes'
+// SPFs (and D matrices) copied into y on the context's stream
+void spf_check(Ctx& c, CmfState& S, SpfRun& R) {
+  const int f = c.nmodes;
+  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
+  for (int m = 0; m < 64; ++m) S.h_acc[m] = 0;
+  for (int m = 0; m < f; ++m) {
+    if (!R.active[m]) continue;
+    const double error = S.h_err[m] / c.eps_psi;
+    if (!std::isfinite(error)) throw StatusError(MCTDH_ENONFINITE, "non-finite SPF error estimate");
+    if (error >= 1.0) {   // retry with a shorter step (rk_SPF_ck :231)
+      R.dtry[m] = std::max(RK_MINSCAL * R.dtry[m], RK_SAFETY * R.dtry[m] * pow(error, RK_PSHRNK));
+      continue;
+    }
+    S.h_acc[m] = 1;
+    const double hdid = R.dtry[m];
+    double hnext = (error > errcon) ? RK_SAFETY * hdid * pow(error, RK_PGROW) : hdid * RK_MAXSCAL;
+    R.done[m] += hdid;
+    if (R.done[m] >= R.dt_total) {   // propagate_SPF :229
+      R.active[m] = 0;
+      continue;
+    }
+    hnext = std::max(hnext, c.min_stepsize * 2);
+    double step = (R.dt_total - R.done[m]) / ((double)(long long)((R.dt_total - R.done[m]) / hnext) + 1);
+    R.dtry[m] = std::min(step, R.dt_total - R.done[m]);
+  }
+  CK(cudaMemcpyAsync(S.accept, S.h_acc, sizeof(int) * 64, cudaMemcpyHostToDevice, c.st));
+  launch_masked_copy(R.y, c.d_tmp, S.elem_mode, S.accept, c.naconftot, c.dimpsi, c.st);
+  c.count();
+  if (S.gwp) {
+    launch_masked_copy(R.Dy, S.Dtmp, S.d_elem_mode, S.accept, 0, S.nD, c.st);
+    c.count();
+  }
+  bool any = false;
+  for (int m = 0; m < f; ++m) any = any || R.active[m];
+  R.finished = !any;
 }
 
 // propagate_SPF for every mode over dt_total, on the psi part of y and, for
@@ -2460,102 +2666,12 @@ void plan_cmf(Ctx& c, CmfState& S) {
 // (rk_SPF_ck, cmf2_integration.f90:105-253) for int_type_psi 1, Dormand-Prince
 // (rk_SPF_dp, :257-412) for 2.
 void propagate_spf_all(Ctx& c, CmfState& S, double dt_total, cplx* y, cplx* Dy) {
-  if (c.int_type_psi != 1 && c.int_type_psi != 2)
-    throw StatusError(MCTDH_EUNSUPPORTED, "SPF integrator must be rk45 (1) or dopri (2)");
-  const bool dp = c.int_type_psi == 2;
-  const int f = c.nmodes;
-  const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
-  std::vector<double> done(f, 0.0), dtry(f, 0.0), dt_h(64, 0.0), err_h(64, 0.0);
-  std::vector<int> active(f, 0), acc_h(64, 0);
-  for (int m : c.modes_dvr) {
-    active[m] = 1;
-    dtry[m] = dt_total;
-  }
-  for (int m : c.modes_gwp) {
-    active[m] = 1;
-    dtry[m] = dt_total;
-  }
-  const long long nA = c.naconftot;
-  for (int iter = 0;; ++iter) {
-    bool any = false;
-    for (int m = 0; m < f; ++m) {
-      dt_h[m] = active[m] ? dtry[m] : 0.0;
-      any = any || active[m];
-    }
-    if (!any) break;
-    if (iter > 100000) throw StatusError(MCTDH_ESTEP, "SPF integration did not finish");
-    ++S.rk_iters;
-    CK(cudaMemcpyAsync(S.dt_mode, dt_h.data(), sizeof(double) * 64, cudaMemcpyHostToDevice, c.st));
-    // one RK attempt of every mode: the same launches on the same buffers each
-    // iteration (the step lengths live in S.dt_mode), so it runs as a CUDA graph
-    run_graphed(c, 1, y, [&] {
-      copy_dev(c, c.d_in + nA, y + nA, c.dimpsi);
-      if (S.gwp) copy_dev(c, S.Din, Dy, S.nD);
-      spf_eval_all(c, S, c.d_k[0], S.Dk[0]);
-      for (int st = 1; st < 6; ++st) {
-        stage_modes(c, S, c.d_in, y, dp ? DP_B[st] : CK_B[st], st);
-        stage_D(c, S, S.Din, Dy, dp ? DP_B[st] : CK_B[st], st);
-        spf_eval_all(c, S, c.d_k[st], S.Dk[st]);
-      }
-      if (dp) {
-        // the 7th stage is the derivative at the 5th-order solution (:386-393)
-        stage_modes(c, S, c.d_in, y, DP_C, 6);
-        stage_D(c, S, S.Din, Dy, DP_C, 6);
-        spf_eval_all(c, S, c.d_k[6], S.Dk[6]);
-        stage_modes(c, S, c.d_tmp, y, DP_C, 6);
-        stage_D(c, S, S.Dtmp, Dy, DP_C, 6);
-        stage_modes(c, S, c.d_err, y, DP_D, 7);
-      } else {
-        stage_modes(c, S, c.d_tmp, y, CK_C, 6);
-        stage_D(c, S, S.Dtmp, Dy, CK_C, 6);
-        stage_modes(c, S, c.d_err, y, CK_D, 6);
-      }
-      StageArgs a;
-      memset(&a, 0, sizeof(a));
-      a.k[0] = c.d_err + nA;
-      a.c[0] = -1.0;
-      a.nk = 1;
-      launch_stage(S.ytmp + nA, c.d_tmp + nA, a, 1.0, c.dimpsi, c.st);
-      c.count();
-      run_hole(c, S.err_holes);
-      run_red(c, S.err_red);
-      if (S.gwp) {
-        launch_gwp_ovl(S.gerr_d, (int)S.gerr_h.size(), c.st);
-        c.count();
-      }
-      launch_spf_err(S.errd_d, (int)S.errd_h.size(), S.err_mode, f, c.st);
-      c.count();
-    });
-    CK(cudaMemcpyAsync(err_h.data(), S.err_mode, sizeof(double) * f, cudaMemcpyDeviceToHost, c.st));
+  SpfRun R;
+  spf_begin(c, R, dt_total, y, Dy);
+  while (!R.finished) {
+    spf_issue(c, S, R);
     CK(cudaStreamSynchronize(c.st));
-    for (int m = 0; m < f; ++m) {
-      acc_h[m] = 0;
-      if (!active[m]) continue;
-      const double error = err_h[m] / c.eps_psi;
-      if (!std::isfinite(error)) throw StatusError(MCTDH_ENONFINITE, "non-finite SPF error estimate");
-      if (error >= 1.0) {   // retry with a shorter step (rk_SPF_ck :231)
-        dtry[m] = std::max(RK_MINSCAL * dtry[m], RK_SAFETY * dtry[m] * pow(error, RK_PSHRNK));
-        continue;
-      }
-      acc_h[m] = 1;
-      const double hdid = dtry[m];
-      double hnext = (error > errcon) ? RK_SAFETY * hdid * pow(error, RK_PGROW) : hdid * RK_MAXSCAL;
-      done[m] += hdid;
-      if (done[m] >= dt_total) {   // propagate_SPF :229
-        active[m] = 0;
-        continue;
-      }
-      hnext = std::max(hnext, c.min_stepsize * 2);
-      double step = (dt_total - done[m]) / ((double)(long long)((dt_total - done[m]) / hnext) + 1);
-      dtry[m] = std::min(step, dt_total - done[m]);
-    }
-    CK(cudaMemcpyAsync(S.accept, acc_h.data(), sizeof(int) * 64, cudaMemcpyHostToDevice, c.st));
-    launch_masked_copy(y, c.d_tmp, S.elem_mode, S.accept, nA, c.dimpsi, c.st);
-    c.count();
-    if (S.gwp) {
-      launch_masked_copy(Dy, S.Dtmp, S.d_elem_mode, S.accept, 0, S.nD, c.st);
-      c.count();
-    }
+    spf_check(c, S, R);
   }
   if (S.gwp) check_status(c);
 }
@@ -2723,10 +2839,16 @@ void mfx_predict(Ctx& c, MfxState& M, double h) {
 // One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
 // ops_fresh: the operators and mean fields at d_y are already in place.
-double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh) {
+double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh, bool reginv_done) {
   CmfState& S = cmf_state(c);
   const long long nA = c.naconftot;
-  if (!ops_fresh) operators_and_mf(c, c.d_y);       // cmf2_base.f90:78-87
+  // With a second stream the regularised inverse of rho and the SPF half step
+  // (which needs it) run beside the Lanczos build (which needs only h1mode).
+  const bool overlap = c.st2 != nullptr;
+  if (!ops_fresh) {
+    operators_and_mf(c, c.d_y, !overlap);           // cmf2_base.f90:78-87
+    reginv_done = !overlap;
+  }
   if (S.gwp) {
     // D0 = S^-1/2 (InverseSquareRootU, :63-73), Calc_DHD(DD0) (:87), B0 = D^H S A (:92)
     ProfScope ps(c, KP_GWP);
@@ -2737,10 +2859,61 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh)
   } else {
     copy_dev(c, S.B0, c.d_y, nA);                   // A_to_B: B = A without Gaussian modes
   }
-  lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);      // :97
   copy_dev(c, S.psiHalf, c.d_y, c.ntot);
   if (S.gwp) copy_dev(c, S.DDHalf, S.DD0, S.nD);
-  propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf, S.DDHalf);   // :109-115
+  if (!overlap) {
+    if (!reginv_done) run_reginv(c);
+    lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);    // :97
+    propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf, S.DDHalf);   // :109-115
+  } else {
+    // the Krylov build on c.st, the SPF integration (:109-115) on st2, in
+    // lockstep: issue one step of each, wait for both, apply both controls
+    CK(cudaEventRecord(c.ev_fork, c.st));
+    CK(cudaStreamWaitEvent(c.st2, c.ev_fork, 0));
+    LanRun L;
+    L.B0 = S.B0;
+    L.dt = 0.5 * hdid;
+    SpfRun P;
+    {
+      StreamSwap sw(c, c.st2);
+      if (!reginv_done) run_reginv(c);
+      spf_begin(c, P, 0.5 * hdid, S.psiHalf, S.DDHalf);
+    }
+    lan_issue(c, L);
+    bool lan_pending = true, spf_pending = false;
+    if (!P.finished) {
+      StreamSwap sw(c, c.st2);
+      spf_issue(c, S, P);
+      spf_pending = true;
+    }
+    while (lan_pending || spf_pending) {
+      if (lan_pending) CK(cudaStreamSynchronize(c.st));
+      if (spf_pending) CK(cudaStreamSynchronize(c.st2));
+      if (lan_pending) {
+        lan_check(c, L);
+        lan_pending = false;
+        if (!L.done) {
+          lan_issue(c, L);
+          lan_pending = true;
+        }
+      }
+      if (spf_pending) {
+        StreamSwap sw(c, c.st2);
+        spf_check(c, S, P);
+        spf_pending = false;
+        if (!P.finished) {
+          spf_issue(c, S, P);
+          spf_pending = true;
+        }
+      }
+    }
+    lan_finish(c, L);
+    lan_combine(c, S.BHalf, 0.5 * hdid);            // :97
+    // the last SPF control's copies were issued on st2 after the last wait
+    CK(cudaEventRecord(c.ev_join, c.st2));
+    CK(cudaStreamWaitEvent(c.st, c.ev_join, 0));
+    if (S.gwp) check_status(c);
+  }
   if (S.gwp) {
     for (auto& b : S.b2a_half) run_prod(c, b);      // B_to_A(AHalf, BHalf, DDHalf)  :120
   } else {
@@ -2805,7 +2978,10 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
   if (it != g_mfx.end()) M = it->second;
   // the operators at the step start: recomputed unless the last step's validation left them
   bool fresh = c.ops_fresh_t == t && c.ops_fresh;
-  if (!fresh) operators_and_mf(c, c.d_y);
+  // (the extrapolator's validation leaves the full operators, rho^-1 MF included)
+  const bool overlap = c.st2 != nullptr;
+  if (!fresh) operators_and_mf(c, c.d_y, !overlap);
+  const bool reginv_first = fresh || !overlap;
   c.ops_fresh = false;
   if (M) {
     // push the step-start snapshot into the history (once per accepted step start)
@@ -2824,7 +3000,7 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
   while (true) {
     ++*tries;
     if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
-    double error = cmf2_attempt(c, t, hdid, use_mlp, first);
+    double error = cmf2_attempt(c, t, hdid, use_mlp, first, first && reginv_first);
     first = false;
     if (M && M->log.size() < 5 * 100000) {
       const double row[5] = {t, hdid, error, use_mlp ? 1.0 : 0.0, -1.0};
@@ -2903,6 +3079,9 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       c->ar.chunk = (size_t)4 << 20;
     } else {
       CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+      CK(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     }
     load_setup(*c, s);
     c->d_status = (int*)c->ar.alloc(64);
@@ -3684,6 +3863,7 @@ int64_t mctdh_destroy(mctdh_ctx_t* ctx) {
   if (!ctx) return MCTDH_EARG;
   Ctx* c = ctx->c;
   cudaStreamSynchronize(c->st);
+  if (c->st2) cudaStreamSynchronize(c->st2);
   auto it = g_cmf.find(c);
   if (it != g_cmf.end()) {
     delete it->second;
@@ -3787,7 +3967,7 @@ int64_t mctdh_cmf2_attempt(mctdh_ctx_t* ctx, double* A, double* psi, double t, d
   return guarded(c, [&] {
     upload(*c, c->d_y, A, psi);
     c->ops_fresh = false;
-    *error = cmf2_attempt(*c, t, h, false, false);
+    *error = cmf2_attempt(*c, t, h, false, false, false);
     cmf2_accept(*c, h);
     download(*c, c->d_y, A, psi);
   });

@@ -932,6 +932,10 @@ __global__ void __launch_bounds__(256) spf_tile_kernel(const SpfDesc* __restrict
 // the tile rows of ophi and the matrix rhom1MF are split once into FP32 hi/lo
 // pairs in shared memory, and every product is accumulated as a compensated
 // FP32 pair (df_fma, ~1e-13 relative), leaving the FP64 pipe one add per output.
+// PREC 1: the products of FP32-rounded operands accumulated in FP32 (~1e-7
+// relative); PREC 2: compensated pairs.  The tile's shares of phi^H phi and
+// phi^H dphi are compensated FP32 sums in both.
+template <int PREC>
 __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __restrict__ descs, int ndesc,
                                                              const SpfOp* __restrict__ ops, cplx* __restrict__ out,
                                                              cplx der) {
@@ -940,8 +944,8 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
   __shared__ __align__(16) cplx smem_u[2 * SPF_TILE * MAXN_SPF];
   float4* ops_s = reinterpret_cast<float4*>(smem_u);
   float4* rm_s = ops_s + SPF_TILE * MAXN_SPF;
-  cplx* phs = smem_u;
-  cplx* dps = smem_u + SPF_TILE * MAXN_SPF;
+  float4* phf = reinterpret_cast<float4*>(smem_u);                    // epilogue: phi rows, split
+  float4* dpf = reinterpret_cast<float4*>(smem_u) + SPF_TILE * MAXN_SPF; // epilogue: dphi rows, split
   if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
   __syncthreads();
   const SpfDesc& d = descs[s_di];
@@ -964,14 +968,14 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
       float hx, lx, hy, ly;
       split_d2f(v.x, hx, lx);
       split_d2f(v.y, hy, ly);
-      ops_s[r + SPF_TILE * j2] = make_float4(hx, hy, lx, ly);
+      ops_s[r + SPF_TILE * j2] = (PREC == 1) ? make_float4(hx + lx, hy + ly, 0.f, 0.f) : make_float4(hx, hy, lx, ly);
     }
     for (int e = threadIdx.x; e < n * n2; e += blockDim.x) {
       const cplx v = op.rm[e];
       float hx, lx, hy, ly;
       split_d2f(v.x, hx, lx);
       split_d2f(v.y, hy, ly);
-      rm_s[e] = make_float4(hx, hy, lx, ly);
+      rm_s[e] = (PREC == 1) ? make_float4(hx + lx, hy + ly, 0.f, 0.f) : make_float4(hx, hy, lx, ly);
     }
     __syncthreads();
 #pragma unroll
@@ -983,10 +987,15 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
         const float4 x = ops_s[r + SPF_TILE * j2];
         const float4 m = rm_s[j1 + n * j2];
         // (x.r + i x.i)(m.r + i m.i)
-        df_fma(ah[u][0], al[u][0], x.x, x.z, m.x, m.z);
-        df_fma(ah[u][0], al[u][0], -x.y, -x.w, m.y, m.w);
-        df_fma(ah[u][1], al[u][1], x.x, x.z, m.y, m.w);
-        df_fma(ah[u][1], al[u][1], x.y, x.w, m.x, m.z);
+        if (PREC == 1) {
+          ah[u][0] = fmaf(x.x, m.x, fmaf(-x.y, m.y, ah[u][0]));
+          ah[u][1] = fmaf(x.x, m.y, fmaf(x.y, m.x, ah[u][1]));
+        } else {
+          df_fma(ah[u][0], al[u][0], x.x, x.z, m.x, m.z);
+          df_fma(ah[u][0], al[u][0], -x.y, -x.w, m.y, m.w);
+          df_fma(ah[u][1], al[u][1], x.x, x.z, m.y, m.w);
+          df_fma(ah[u][1], al[u][1], x.y, x.w, m.x, m.z);
+        }
       }
     }
   }
@@ -999,8 +1008,14 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
     const int g = g0 + r;
     const cplx acc = cmul(der, mkc(f2d_exact(ah[u][0]) + f2d_exact(al[u][0]),
                                    f2d_exact(ah[u][1]) + f2d_exact(al[u][1])));
-    phs[r + SPF_TILE * j1] = d.phi[g + (long long)G * j1];
-    dps[r + SPF_TILE * j1] = acc;
+    const cplx ph = d.phi[g + (long long)G * j1];
+    float4 w;
+    split_d2f(ph.x, w.x, w.z);
+    split_d2f(ph.y, w.y, w.w);
+    phf[r + SPF_TILE * j1] = w;
+    split_d2f(acc.x, w.x, w.z);
+    split_d2f(acc.y, w.y, w.w);
+    dpf[r + SPF_TILE * j1] = w;
     o[g + (long long)G * j1] = acc;
   }
   __syncthreads();
@@ -1008,11 +1023,18 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
   for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
     const int which = pr / (n * n), q = pr % (n * n);
     const int j1 = q % n, j2 = q / n;
-    const cplx* a = phs + SPF_TILE * j1;
-    const cplx* b = (which == 0 ? phs : dps) + SPF_TILE * j2;
-    cplx s = mkc(0, 0);
-    for (int r = 0; r < rows; ++r) cfma_conj(s, a[r], b[r]);
-    part[pr] = s;
+    const float4* a = phf + SPF_TILE * j1;
+    const float4* b = (which == 0 ? phf : dpf) + SPF_TILE * j2;
+    // conj(a) b as compensated FP32 pairs on the pre-split rows (the FP64 pipe is ~64x slower)
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int r = 0; r < rows; ++r) {
+      const float4 x = a[r], y = b[r];
+      df_fma(rh, rl, x.x, x.z, y.x, y.z);
+      df_fma(rh, rl, x.y, x.w, y.y, y.w);
+      df_fma(ih, il, x.x, x.z, y.y, y.w);
+      df_fma(ih, il, -x.y, -x.w, y.x, y.z);
+    }
+    part[pr] = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
   }
 }
 
@@ -1084,7 +1106,9 @@ __global__ void __launch_bounds__(256) spf_proj_kernel(const SpfDesc* __restrict
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
                 cplx der_factor, int* d_status, cudaStream_t st, int prec) {
   if (ndesc <= 0) return;
-  if (prec > 0) spf_tile_split_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  // both split modes: compensated (FP32 accumulation here makes the SPF error
+  // estimate noisier and the adaptive SPF integration take more steps)
+  if (prec > 0) spf_tile_split_kernel<2><<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   else spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   spf_solve_kernel<<<ndesc, 256, 0, st>>>(d_descs, d_status);
   spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
@@ -1136,65 +1160,82 @@ __device__ void grid_sum_c(cplx v, cplx* partial, unsigned* counter, cplx* out) 
   }
 }
 
-// out = sum of coeff * src per state range; with dotv also the launch-wide
-// <dotv|out> (FP64 products of the values written) into dot->res.
-// Grid-stride over the elements (a capped grid keeps the fused sum's block count,
-// and with it the counter's atomics, small).
-__global__ void termsum_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges, int nr,
-                               const SumSrc* __restrict__ srcs, long long total, FusedDot dot) {
+// out[i] = sum_k coeff_k src_k[i - offset] over the sources of the state range
+// holding i; with dot.v also the launch-wide <dot.v|out> (FP64 products of the
+// values written) into dot.res.  Each block streams a contiguous chunk of the
+// elements with the current range's source descriptors cached in shared memory.
+// PREC 0: FP64.  PREC 1: FP32 coefficients times FP32-rounded sources accumulated
+// in FP32 (the sources are FP32 products there).  PREC 2: compensated FP32 pairs
+// (df_fma, ~1e-13 relative).
+#define TERMSUM_CACHE 64
+template <int PREC>
+__global__ void __launch_bounds__(256) termsum_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges,
+                                                      int nr, const SumSrc* __restrict__ srcs, long long total,
+                                                      FusedDot dot) {
+  __shared__ SumSrc ss[TERMSUM_CACHE];
+  __shared__ int s_rg;
+  const long long chunk = (total + gridDim.x - 1) / gridDim.x;
+  const long long start = (long long)blockIdx.x * chunk, end = min(total, start + chunk);
   cplx d = mkc(0, 0);
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
-    }
-    const SumRange& rg = ranges[lo];
-    const long long li = i - rg.offset;
-    if (li < 0 || li >= rg.n) continue;
-    cplx acc = mkc(0, 0);
-    for (int k = 0; k < rg.count; ++k) {
-      const SumSrc& s = srcs[rg.first + k];
-      cfma(acc, s.coeff, load_c(s.src, li, s.fmt));
-    }
-    out[i] = acc;
-    if (dot.v) cfma_conj(d, dot.v[i], acc);
-  }
-  if (dot.v) grid_sum_c(d, dot.partial, dot.counter, dot.res);
-}
-
-// Split-precision variant: every coeff * src product accumulated as a
-// compensated FP32 pair (df_fma, ~1e-13 relative); one FP64 add per output.
-__global__ void termsum_split_kernel(cplx* __restrict__ out, const SumRange* __restrict__ ranges, int nr,
-                                     const SumSrc* __restrict__ srcs, long long total, FusedDot dot) {
-  cplx d = mkc(0, 0);
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nr - 1;   // last range starting at or before i (ranges sorted by offset)
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (ranges[mid].offset <= i) lo = mid; else hi = mid - 1;
-    }
-    const SumRange& rg = ranges[lo];
-    const long long li = i - rg.offset;
-    if (li < 0 || li >= rg.n) continue;
-    {
-      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-      for (int k = 0; k < rg.count; ++k) {
-        const SumSrc& s = srcs[rg.first + k];
-        const float ch = s.cs[0], cl = s.cs[1], dh = s.cs[2], dl = s.cs[3];
-        const float4 x = load_split(s.src, li, s.fmt);
-        // (c + i d)(xr + i xi)
-        df_fma(rh, rl, ch, cl, x.x, x.z);
-        df_fma(rh, rl, -dh, -dl, x.y, x.w);
-        df_fma(ih, il, ch, cl, x.y, x.w);
-        df_fma(ih, il, dh, dl, x.x, x.z);
+  long long base = start;
+  while (base < end) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = nr - 1;   // last range starting at or before base (ranges sorted by offset)
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ranges[mid].offset <= base) lo = mid; else hi = mid - 1;
       }
-      const cplx val = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+      s_rg = lo;
+    }
+    __syncthreads();
+    const SumRange rg = ranges[s_rg];
+    long long seg_end = min(end, rg.offset + rg.n);
+    if (base < rg.offset || base >= rg.offset + rg.n) {
+      // outside every range: skip to the next range start
+      seg_end = (s_rg + 1 < nr) ? min(end, ranges[s_rg + 1].offset) : end;
+      __syncthreads();
+      base = max(seg_end, base + 1);
+      continue;
+    }
+    const bool cached = rg.count <= TERMSUM_CACHE;
+    if (cached)
+      for (int k = threadIdx.x; k < rg.count; k += blockDim.x) ss[k] = srcs[rg.first + k];
+    __syncthreads();
+    const SumSrc* sp = cached ? ss : srcs + rg.first;
+    for (long long i = base + threadIdx.x; i < seg_end; i += blockDim.x) {
+      const long long li = i - rg.offset;
+      cplx val;
+      if (PREC == 0) {
+        val = mkc(0, 0);
+        for (int k = 0; k < rg.count; ++k) cfma(val, sp[k].coeff, load_c(sp[k].src, li, sp[k].fmt));
+      } else if (PREC == 1) {
+        float ar = 0.f, ai = 0.f;
+        for (int k = 0; k < rg.count; ++k) {
+          const float cr = sp[k].cs[0] + sp[k].cs[1], ci = sp[k].cs[2] + sp[k].cs[3];
+          const float4 x = load_split(sp[k].src, li, sp[k].fmt);
+          const float xr = x.x + x.z, xi = x.y + x.w;
+          ar = fmaf(cr, xr, fmaf(-ci, xi, ar));
+          ai = fmaf(cr, xi, fmaf(ci, xr, ai));
+        }
+        val = mkc(f2d_exact(ar), f2d_exact(ai));
+      } else {
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        for (int k = 0; k < rg.count; ++k) {
+          const float ch = sp[k].cs[0], cl = sp[k].cs[1], dh = sp[k].cs[2], dl = sp[k].cs[3];
+          const float4 x = load_split(sp[k].src, li, sp[k].fmt);
+          // (c + i d)(xr + i xi)
+          df_fma(rh, rl, ch, cl, x.x, x.z);
+          df_fma(rh, rl, -dh, -dl, x.y, x.w);
+          df_fma(ih, il, ch, cl, x.y, x.w);
+          df_fma(ih, il, dh, dl, x.x, x.z);
+        }
+        val = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+      }
       out[i] = val;
       if (dot.v) cfma_conj(d, dot.v[i], val);
     }
+    __syncthreads();
+    base = seg_end;
   }
   if (dot.v) grid_sum_c(d, dot.partial, dot.counter, dot.res);
 }
@@ -1203,10 +1244,12 @@ void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumS
                     cudaStream_t st, int prec, FusedDot dot) {
   if (total <= 0) return;
   const unsigned nb = (unsigned)std::min<long long>((total + 255) / 256, FUSED_BLOCKS);
-  if (prec > 0)
-    termsum_split_kernel<<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
+  if (prec == 1)
+    termsum_kernel<1><<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
+  else if (prec > 1)
+    termsum_kernel<2><<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
   else
-    termsum_kernel<<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
+    termsum_kernel<0><<<nb, 256, 0, st>>>(out, d_ranges, nranges, d_srcs, total, dot);
 }
 
 __global__ void stage_kernel(cplx* __restrict__ out, const cplx* __restrict__ base, StageArgs a, double dt,
