@@ -82,6 +82,9 @@ struct TRef {
   std::vector<int> shape;
   int fmt = TF_C64;   // storage format of the tensor
 };
+// bytes of one tensor element in a storage format (TF_F32: complex FP32)
+inline double elem_bytes(int fmt) { return fmt == TF_F32 ? 8.0 : 16.0; }
+
 long long prod_range(const std::vector<int>& s, int a, int b) {
   long long r = 1;
   for (int i = a; i < b; ++i) r *= s[i];
@@ -110,6 +113,8 @@ struct ProdBatch {
     pd.conjT = conjT;
     pd.L = prod_range(shape, 0, mode);
     pd.R = prod_range(shape, mode + 1, (int)shape.size());
+    if (pd.L * pd.R >= (1LL << 31))
+      throw StatusError(MCTDH_EUNSUPPORTED, "more than 2^31 fibres in one mode product");
     pd.nin = shape[mode];
     pd.nout = nout;
     pd.alpha = alpha;
@@ -126,7 +131,7 @@ struct ProdBatch {
       maxn = std::max(maxn, std::max(pd.nin, pd.nout));
       const double fib = (double)pd.L * (double)pd.R;
       flops += 8.0 * pd.nin * pd.nout * fib;
-      bytes += 16.0 * (pd.nin + pd.nout * (pd.accumulate ? 2 : 1)) * fib;
+      bytes += (elem_bytes(pd.xfmt) * pd.nin + elem_bytes(pd.yfmt) * pd.nout * (pd.accumulate ? 2 : 1)) * fib;
     }
     d = upload_vec(ar, h);
   }
@@ -149,6 +154,7 @@ struct HoleBatch {
     hd.yfmt = yfmt;
     hd.L = L;
     hd.R = R;
+    if (L * R >= (1LL << 31)) throw StatusError(MCTDH_EUNSUPPORTED, "more than 2^31 fibres in one contraction");
     hd.n1 = n1;
     hd.n2 = n2;
     long long ntiles = (L * R + HOLE_TILE - 1) / HOLE_TILE;
@@ -165,7 +171,7 @@ struct HoleBatch {
       nblocks += hd.nblk;
       const double fib = (double)hd.L * (double)hd.R;
       flops += 8.0 * hd.n1 * hd.n2 * fib;
-      bytes += 16.0 * (hd.n1 + (hd.X == hd.Y ? 0 : hd.n2)) * fib;
+      bytes += (elem_bytes(hd.xfmt) * hd.n1 + (hd.X == hd.Y ? 0.0 : elem_bytes(hd.yfmt) * hd.n2)) * fib;
     }
     d = upload_vec(ar, h);
   }
@@ -190,12 +196,13 @@ struct RedBatch {
     pending.emplace_back();
     return (int)tg.size() - 1;
   }
-  void add_term(int target, const HoleDesc& hd, cplx alpha) {
+  void add_term(int target, const HoleDesc& hd, cplx alpha, int conjT = 0) {
     RedTerm rt;
     memset(&rt, 0, sizeof(rt));
     rt.partial = hd.partial;
     rt.nblk = hd.nblk;
     rt.alpha = alpha;
+    rt.conjT = conjT;
     pending[target].push_back(rt);
   }
   void finalize(DevArena& ar) {
@@ -216,6 +223,7 @@ struct HoleRef {
   int hole;
   int target;
   cplx alpha;
+  int conjT = 0;   // add the hole's matrix conjugate-transposed
 };
 
 // Plan of one overlap evaluation <Psi1|Psi2> / norms (norm_wf, WF_Ovl, DeltaPsi).
@@ -342,6 +350,7 @@ struct Ctx {
   size_t h1_smem = 0;
   int h1_maxn2 = 0;
   std::vector<ProdBatch> chains;  // per depth
+  std::vector<ProdBatch> chains_full;   // per depth: right chains needed only for dA (adjoint partners)
   HoleBatch holes;       // mean-field contractions of the general terms
   HoleBatch rho_holes;   // density matrices (FP64 always)
   RedBatch red;
@@ -372,6 +381,7 @@ struct Ctx {
   // H_B * B plan for CMF2 (Calc_DHD_B): reads d_hbin, writes d_hb
   cplx* d_hbin = nullptr;
   cplx* d_hbin32 = nullptr;   // precision 1: d_hbin as complex FP32, the input of the H_B products
+  cplx* d_in32 = nullptr;     // precision 1: the coefficients of d_in as complex FP32 (chain inputs)
   FusedDot hb_dot{nullptr, nullptr, nullptr, nullptr};    // <d_hbin | H_B d_hbin> in the term sum
   FusedDot lan_nrm{nullptr, nullptr, nullptr, nullptr};   // ||Kn||^2 in the Lanczos axpy
   std::vector<ProdBatch> hb_chains;
@@ -865,6 +875,15 @@ void plan_eom(Ctx& c) {
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
   // chain intermediates: complex FP32 in precision 1, FP32 split pairs in precision 2
   const int chain_fmt = c.precision == 1 ? TF_F32 : (c.precision ? TF_SPLIT : TF_C64);
+  // precision 1: the products read the coefficients converted once to complex FP32
+  // (the contractions keep the FP64 coefficients)
+  if (c.precision == 1 && !c.member) c.d_in32 = c.ar.calloc_c((c.naconftot + 1) / 2);
+  auto prod_in = [&](const TRef& X, int s) -> std::pair<const cplx*, int> {
+    if (c.d_in32 && X.p == c.d_in + c.aoff[s])   // 8-byte elements: offsets count float2
+      return std::make_pair(reinterpret_cast<const cplx*>(reinterpret_cast<float2*>(c.d_in32) + c.aoff[s]),
+                            (int)TF_F32);
+    return std::make_pair((const cplx*)X.p, X.fmt);
+  };
   std::map<std::pair<int, int>, int> mf_target;   // (m,k) -> red target
   auto mf_tg = [&](int im, int k) {
     auto key = std::make_pair(im, k);
@@ -878,6 +897,47 @@ void plan_eom(Ctx& c) {
   std::vector<cplx> c0(c.nstates, mkc(0, 0));
   std::map<std::pair<int, int>, std::vector<MatSumSrc>> gsum;  // (s, m) -> sum_t ae_t h_t
   c.term_single.assign(c.nham, -2);
+  // Hermitian-conjugate partners among the cross-state terms: t2 acts from s2 to s1
+  // with the same primitive operators as t1 on every mode and the conjugate
+  // coefficient.  Every primitive DOF operator is Hermitian (q^k, i d/dq, d^2/dq^2,
+  // i (q d/dq + d/dq q), sin^-2, projectors), so on every mode t2's matrix is the
+  // adjoint of t1's and each single-hole mean field of t2 is t1's conjugate-
+  // transposed: only t1's contractions are computed, and t2's right chain is
+  // needed only for its contribution to dA (c.chains_full).
+  c.chains_full.assign(f + 1, ProdBatch());
+  std::vector<int> leader_of(c.nham, -1), is_general(c.nham, 0);
+  {
+    for (int t = 0; t < c.nham; ++t) {
+      int nact = 0, mact = -1;
+      for (int m = 0; m < f; ++m)
+        if (!c.skip_term[m + f * t]) { ++nact; mact = m; }
+      is_general[t] = !(c.lhs[t] == c.rhs[t] && nact <= 1 && (mact < 0 || !c.is_gwp[mact]));
+    }
+    std::vector<char> taken(c.nham, 0);
+    for (int t2 = 0; t2 < c.nham; ++t2) {
+      if (!is_general[t2] || c.lhs[t2] == c.rhs[t2]) continue;
+      for (int t1 = 0; t1 < t2; ++t1) {
+        if (!is_general[t1] || taken[t1] || leader_of[t1] >= 0) continue;
+        if (c.lhs[t1] != c.rhs[t2] || c.rhs[t1] != c.lhs[t2]) continue;
+        const cplx a1 = c.ae[t1], a2 = c.ae[t2];
+        const double da = hypot(a2.x - a1.x, a2.y + a1.y), ma = hypot(a1.x, a1.y);
+        if (!(da <= 1e-14 * ma)) continue;
+        bool same = true;
+        for (int m = 0; m < f && same; ++m) {
+          if (c.skip_term[m + f * t1] != c.skip_term[m + f * t2]) { same = false; break; }
+          const std::vector<int>& o1 = c.oper[m][c.ioper[m + f * t1]];
+          const std::vector<int>& o2 = c.oper[m][c.ioper[m + f * t2]];
+          const bool el = c.multiset[m] ? (o2[0] == o1[1] && o2[1] == o1[0]) : (o2[0] == o1[0] && o2[1] == o1[1]);
+          same = el && std::equal(o1.begin() + 2, o1.end(), o2.begin() + 2);
+        }
+        if (!same) continue;
+        leader_of[t2] = t1;
+        taken[t1] = 1;
+        break;
+      }
+    }
+  }
+  std::map<std::pair<int, int>, int> term_hole;   // (leader term, mode) -> contraction
   for (int t = 0; t < c.nham; ++t) {
     const int s1 = c.lhs[t], s2 = c.rhs[t];
     int nact = 0, mact = -1;
@@ -895,10 +955,14 @@ void plan_eom(Ctx& c) {
       continue;
     }
     // general term: right chain always reaches R_f; the left chain stops at the
-    // last mode whose mean field is needed
+    // last mode whose mean field is needed (an adjoint partner has neither left
+    // chain nor contractions, and its right chain serves dA only)
+    const int leader = leader_of[t];
+    std::vector<ProdBatch>& rchains = leader >= 0 ? c.chains_full : c.chains;
     int lmax = 0;
     for (int im = 0; im < f; ++im)
       if (!c.is_identity[im + f * c.ioper[im + f * t]]) lmax = im;
+    if (leader >= 0) lmax = 0;
     std::vector<TRef> R(f + 1), L(f);
     R[0].p = c.d_in + c.aoff[s2];
     R[0].shape = c.shape_of(s2);
@@ -910,8 +974,9 @@ void plan_eom(Ctx& c) {
       std::vector<int> ns = R[i - 1].shape;
       ns[jm] = n1;
       cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
-      c.chains[i].add(R[i - 1].p, out, c.hmat[jm][k], n1, 0, R[i - 1].shape, jm, n1, mkc(1, 0), 0, R[i - 1].fmt,
-                      chain_fmt);
+      const auto in = prod_in(R[i - 1], s2);
+      rchains[i].add(in.first, out, c.hmat[jm][k], n1, 0, R[i - 1].shape, jm, n1, mkc(1, 0), 0, in.second,
+                     chain_fmt);
       R[i].p = out;
       R[i].shape = ns;
       R[i].fmt = chain_fmt;
@@ -926,7 +991,8 @@ void plan_eom(Ctx& c) {
       std::vector<int> ns = L[i - 1].shape;
       ns[im] = n2;
       cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
-      c.chains[i].add(L[i - 1].p, out, c.hmat[im][k], n1, 1, L[i - 1].shape, im, n2, mkc(1, 0), 0, L[i - 1].fmt,
+      const auto in = prod_in(L[i - 1], s1);
+      c.chains[i].add(in.first, out, c.hmat[im][k], n1, 1, L[i - 1].shape, im, n2, mkc(1, 0), 0, in.second,
                       chain_fmt);
       L[i].p = out;
       L[i].shape = ns;
@@ -937,10 +1003,15 @@ void plan_eom(Ctx& c) {
     for (int im = 0; im < f; ++im) {
       const int k = c.ioper[im + f * t];
       if (c.is_identity[im + f * k]) continue;
+      if (leader >= 0) {
+        hrefs.push_back(HoleRef{term_hole.at(std::make_pair(leader, im)), mf_tg(im, k), c.ae[t], 1});
+        continue;
+      }
       const TRef& X = L[im];
       const TRef& Y = R[f - 1 - im];
       long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, f);
       int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im], X.fmt, Y.fmt);
+      term_hole[std::make_pair(t, im)] = hidx;
       hrefs.push_back(HoleRef{hidx, mf_tg(im, k), c.ae[t]});
     }
   }
@@ -960,7 +1031,10 @@ void plan_eom(Ctx& c) {
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
     const int gfmt = c.precision == 1 ? TF_F32 : chain_fmt;   // FP32 products in precision 1
-    c.gprods.add(c.d_in + c.aoff[s], out, md.out, n, 0, sh, m, n, mkc(1, 0), 0, TF_C64, gfmt);
+    TRef root;
+    root.p = c.d_in + c.aoff[s];
+    const auto in = prod_in(root, s);
+    c.gprods.add(in.first, out, md.out, n, 0, sh, m, n, mkc(1, 0), 0, in.second, gfmt);
     srcs[s].push_back(SumSrc{out, c.der, gfmt});
   }
   for (int s = 0; s < c.nstates; ++s)
@@ -972,6 +1046,10 @@ void plan_eom(Ctx& c) {
   // precision 1).  The contractions of the mean fields and density matrices use
   // the compensated split (about 1e-13 relative) whenever a split mode is chosen:
   // the regularised inverse of rho scales mean-field errors by up to 1/eps_rho.
+  for (auto& b : c.chains_full) {
+    b.prec = c.precision;
+    b.finalize(c.ar);
+  }
   for (auto& b : c.chains) {
     b.prec = c.precision;
     b.finalize(c.ar);
@@ -984,7 +1062,7 @@ void plan_eom(Ctx& c) {
   c.rho_holes.prec = c.precision ? 2 : 0;
   c.rho_holes.finalize(c.ar);
   for (auto& hr : rrefs) c.red.add_term(hr.target, c.rho_holes.h[hr.hole], hr.alpha);
-  for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha);
+  for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha, hr.conjT);
   c.red.finalize(c.ar);
 
   // regularised inverse of rho times the mean fields (Calc_rhom1MF, gmctdh_objects.f90:1147-1194)
@@ -1554,6 +1632,10 @@ void run_reginv(Ctx& c) {
 void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   const bool gwp = !c.modes_gwp.empty();
   if (gwp) gwp_setup_run(c);
+  if (c.d_in32) {
+    launch_to_f32(c.d_in32, c.d_in, c.naconftot, c.st);
+    c.count();
+  }
   {
     ProfScope ps(c, KP_H1);
     launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, c.precision);
@@ -1563,6 +1645,8 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   // the deepest level holds only the full products H_t A of the right chains (dA)
   const size_t depth_end = mf_only ? c.chains.size() - 1 : c.chains.size();
   for (size_t i = 1; i < depth_end; ++i) run_prod(c, c.chains[i]);
+  if (!mf_only)
+    for (size_t i = 1; i < c.chains_full.size(); ++i) run_prod(c, c.chains_full[i]);
   if (!mf_only) run_prod(c, c.gprods);
   for (auto& b : c.gwp_rho_chain) run_prod(c, b);
   run_hole(c, c.rho_holes);
@@ -3204,7 +3288,7 @@ struct Ens {
   cplx der = mkc(0, -1);
   double min_stepsize = 0, writetime = 0;
   // merged EOM plan
-  std::vector<ProdBatch> chains;
+  std::vector<ProdBatch> chains, chains_full;
   ProdBatch gprods;
   HoleBatch rho_holes, holes;
   RedBatch red;
@@ -3301,6 +3385,8 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
       // merge the EOM plan
       if (E->chains.size() < c->chains.size()) E->chains.resize(c->chains.size());
       for (size_t dd = 1; dd < c->chains.size(); ++dd) merge_prod(E->chains[dd], c->chains[dd]);
+      if (E->chains_full.size() < c->chains_full.size()) E->chains_full.resize(c->chains_full.size());
+      for (size_t dd = 1; dd < c->chains_full.size(); ++dd) merge_prod(E->chains_full[dd], c->chains_full[dd]);
       merge_prod(E->gprods, c->gprods);
       merge_hole(E->rho_holes, c->rho_holes);
       merge_hole(E->holes, c->holes);
@@ -3345,6 +3431,7 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
     for (int i = 0; i < n; ++i)
       for (int q = 0; q < 3; ++q) E->ov_dot_red.tg[3 * i + q].out = E->res_d + 3 * i + q;
     for (auto& b : E->chains) b.finalize(E->ar);
+    for (auto& b : E->chains_full) b.finalize(E->ar);
     E->gprods.finalize(E->ar);
     E->rho_holes.finalize(E->ar);
     E->holes.finalize(E->ar);
@@ -3413,6 +3500,7 @@ void ens_eom(Ens& E, cplx* out) {
   launch_matsum(E.msum_d, (int)E.msum_h.size(), E.msum_src_d, E.st);
   E.launches += 3;
   for (size_t i = 1; i < E.chains.size(); ++i) ens_run_prod(E, E.chains[i]);
+  for (size_t i = 1; i < E.chains_full.size(); ++i) ens_run_prod(E, E.chains_full[i]);
   ens_run_prod(E, E.gprods);
   ens_run_hole(E, E.rho_holes);
   ens_run_hole(E, E.holes);

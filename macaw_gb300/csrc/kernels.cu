@@ -311,13 +311,19 @@ __global__ void reduce_kernel(const RedTarget* __restrict__ tg, const RedTerm* _
   for (int pr = threadIdx.x; pr < npairs; pr += blockDim.x) {
     const int j1 = pr % t.n1, j2 = pr / t.n1;
     const int prT = j2 + t.n1 * j1;
+    const int prC = j2 + t.n2 * j1;   // element (j2, j1) of an n2 x n1 source (conjT terms)
     cplx s = mkc(0, 0), sT = mkc(0, 0);
     for (int k = 0; k < t.count; ++k) {
       const RedTerm& rt = terms[t.first + k];
       cplx a = mkc(0, 0), aT = mkc(0, 0);
       for (int bb = 0; bb < rt.nblk; ++bb) {
-        a = cadd(a, rt.partial[(long long)bb * npairs + pr]);
-        if (t.hermitize) aT = cadd(aT, rt.partial[(long long)bb * npairs + prT]);
+        if (rt.conjT) {
+          a = cadd(a, cconj(rt.partial[(long long)bb * npairs + prC]));
+          if (t.hermitize) aT = cadd(aT, cconj(rt.partial[(long long)bb * npairs + pr]));
+        } else {
+          a = cadd(a, rt.partial[(long long)bb * npairs + pr]);
+          if (t.hermitize) aT = cadd(aT, rt.partial[(long long)bb * npairs + prT]);
+        }
       }
       s = cadd(s, cmul(rt.alpha, a));
       if (t.hermitize) sT = cadd(sT, cmul(rt.alpha, aT));

@@ -60,7 +60,7 @@ struct RedTarget {
 struct RedTerm {
   const cplx* partial;
   int nblk;
-  int pad;
+  int conjT;               // 1: the term adds alpha * (its partials' matrix)^H (n2 x n1 source)
   cplx alpha;
 };
 
