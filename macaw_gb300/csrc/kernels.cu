@@ -305,38 +305,65 @@ void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStre
 // ---------------------------------------------------------------------------
 // Second stage: deterministic sum of partials into the target matrices.
 // ---------------------------------------------------------------------------
-__global__ void reduce_kernel(const RedTarget* __restrict__ tg, const RedTerm* __restrict__ terms) {
+// One block per target; the partial blocks of every term are spread over G thread
+// groups (G = blockDim / (n1 n2) when that is > 1), each group sums its share in a
+// fixed order, then the groups are added in group order (deterministic).
+__global__ void __launch_bounds__(256) reduce_kernel(const RedTarget* __restrict__ tg,
+                                                     const RedTerm* __restrict__ terms) {
+  __shared__ cplx red[256], redT[256];
   const RedTarget& t = tg[blockIdx.x];
   const int npairs = t.n1 * t.n2;
-  for (int pr = threadIdx.x; pr < npairs; pr += blockDim.x) {
-    const int j1 = pr % t.n1, j2 = pr / t.n1;
-    const int prT = j2 + t.n1 * j1;
-    const int prC = j2 + t.n2 * j1;   // element (j2, j1) of an n2 x n1 source (conjT terms)
+  const int G = (npairs <= (int)blockDim.x / 2) ? (int)blockDim.x / npairs : 1;
+  const int g = (G > 1) ? (int)threadIdx.x / npairs : 0;
+  const int p0 = (G > 1) ? (int)threadIdx.x % npairs : (int)threadIdx.x;
+  for (int base = 0; base < npairs; base += (G > 1 ? npairs : (int)blockDim.x)) {
+    const int pr = base + p0;
+    const bool act = (G > 1) ? (g < G) : (pr < npairs);
     cplx s = mkc(0, 0), sT = mkc(0, 0);
-    for (int k = 0; k < t.count; ++k) {
-      const RedTerm& rt = terms[t.first + k];
-      cplx a = mkc(0, 0), aT = mkc(0, 0);
-      for (int bb = 0; bb < rt.nblk; ++bb) {
-        if (rt.conjT) {
-          a = cadd(a, cconj(rt.partial[(long long)bb * npairs + prC]));
-          if (t.hermitize) aT = cadd(aT, cconj(rt.partial[(long long)bb * npairs + pr]));
-        } else {
-          a = cadd(a, rt.partial[(long long)bb * npairs + pr]);
-          if (t.hermitize) aT = cadd(aT, rt.partial[(long long)bb * npairs + prT]);
+    if (act) {
+      const int j1 = pr % t.n1, j2 = pr / t.n1;
+      const int prT = j2 + t.n1 * j1;
+      const int prC = j2 + t.n2 * j1;   // element (j2, j1) of an n2 x n1 source (conjT terms)
+      for (int k = 0; k < t.count; ++k) {
+        const RedTerm& rt = terms[t.first + k];
+        cplx a = mkc(0, 0), aT = mkc(0, 0);
+        for (int bb = g; bb < rt.nblk; bb += G) {
+          if (rt.conjT) {
+            a = cadd(a, cconj(rt.partial[(long long)bb * npairs + prC]));
+            if (t.hermitize) aT = cadd(aT, cconj(rt.partial[(long long)bb * npairs + pr]));
+          } else {
+            a = cadd(a, rt.partial[(long long)bb * npairs + pr]);
+            if (t.hermitize) aT = cadd(aT, rt.partial[(long long)bb * npairs + prT]);
+          }
+        }
+        s = cadd(s, cmul(rt.alpha, a));
+        if (t.hermitize) sT = cadd(sT, cmul(rt.alpha, aT));
+      }
+    }
+    if (G > 1) {
+      red[threadIdx.x] = s;
+      redT[threadIdx.x] = sT;
+      __syncthreads();
+      if (g == 0) {
+        for (int q = 1; q < G; ++q) {
+          s = cadd(s, red[q * npairs + p0]);
+          sT = cadd(sT, redT[q * npairs + p0]);
         }
       }
-      s = cadd(s, cmul(rt.alpha, a));
-      if (t.hermitize) sT = cadd(sT, cmul(rt.alpha, aT));
+      __syncthreads();
     }
-    if (t.hermitize) s = cscale(cadd(s, cconj(sT)), 0.5);
-    cplx* o = t.out + j1 + (long long)t.ld * j2;
-    *o = t.accumulate ? cadd(*o, s) : s;
+    if (act && g == 0) {
+      const int j1 = pr % t.n1, j2 = pr / t.n1;
+      if (t.hermitize) s = cscale(cadd(s, cconj(sT)), 0.5);
+      cplx* o = t.out + j1 + (long long)t.ld * j2;
+      *o = t.accumulate ? cadd(*o, s) : s;
+    }
   }
 }
 
 void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st) {
   if (ntg <= 0) return;
-  reduce_kernel<<<ntg, 128, 0, st>>>(d_tg, d_terms);
+  reduce_kernel<<<ntg, 256, 0, st>>>(d_tg, d_terms);
 }
 
 // ---------------------------------------------------------------------------
