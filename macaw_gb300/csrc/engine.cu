@@ -2148,11 +2148,15 @@ void bs_step(Ctx& c, double t, double htry, double* hdid, double* hnext) {
 // ---------------------------------------------------------------------------
 // CMF2 (cmf2_base.f90:47-206) for DVR models
 // ---------------------------------------------------------------------------
-void hb(Ctx& c, const cplx* B, cplx* out, bool with_dot = false) {
-  if (B != c.d_hbin) CK(cudaMemcpyAsync(c.d_hbin, B, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
-  if (c.d_hbin32) {
-    launch_to_f32(c.d_hbin32, c.d_hbin, c.naconftot, c.st);
-    c.count();
+// H_B B (Calc_DHD_B) into out; input_ready: B is already in d_hbin (and d_hbin32),
+// written there by the Lanczos normalisation that produced it.
+void hb(Ctx& c, const cplx* B, cplx* out, bool with_dot = false, bool input_ready = false) {
+  if (!input_ready) {
+    if (B != c.d_hbin) CK(cudaMemcpyAsync(c.d_hbin, B, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToDevice, c.st));
+    if (c.d_hbin32) {
+      launch_to_f32(c.d_hbin32, c.d_hbin, c.naconftot, c.st);
+      c.count();
+    }
   }
   for (size_t i = 1; i < c.hb_chains.size(); ++i) run_prod(c, c.hb_chains[i]);
   launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st, c.precision,
@@ -2217,12 +2221,13 @@ void lan_issue(Ctx& c, LanRun& R) {
     // each Krylov step is a fixed launch sequence on fixed buffers: CUDA graphs
     const cplx* B0 = R.B0;
     run_graphed(c, 4, B0, [&] {
-      launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st);
+      // every normalisation also writes the next H_B input (d_hbin, d_hbin32)
+      launch_lan_normalize(K, B0, dot_dev(c, B0, B0, n), nullptr, n, c.st, c.d_hbin, c.d_hbin32);
       c.count();
       // alpha = <K|H_B K> in the term sum, ||K'||^2 in the axpy
-      hb(c, K, K + n, true);
+      hb(c, K, K + n, true, true);
       launch_lan_axpy(K + n, K, nullptr, c.hb_dot.res, nullptr, d_alpha, n, c.st, c.lan_nrm);
-      launch_lan_normalize(K + n, K + n, c.lan_nrm.res, d_beta, n, c.st);
+      launch_lan_normalize(K + n, K + n, c.lan_nrm.res, d_beta, n, c.st, c.d_hbin, c.d_hbin32);
       c.count(2);
     });
     CK(cudaMemcpyAsync(h_beta, d_beta, sizeof(double), cudaMemcpyDeviceToHost, c.st));
@@ -2234,9 +2239,9 @@ void lan_issue(Ctx& c, LanRun& R) {
   cplx* Kn = K + (long long)j * n;
   cplx* Kp = K + (long long)(j - 2) * n;
   run_graphed(c, 3, Kn, [&] {
-    hb(c, Kj, Kn, true);
+    hb(c, Kj, Kn, true, true);   // Kj is in d_hbin: the previous step's normalisation wrote it
     launch_lan_axpy(Kn, Kj, Kp, c.hb_dot.res, d_beta + (j - 2), d_alpha + (j - 1), n, c.st, c.lan_nrm);
-    launch_lan_normalize(Kn, Kn, c.lan_nrm.res, d_beta + (j - 1), n, c.st);
+    launch_lan_normalize(Kn, Kn, c.lan_nrm.res, d_beta + (j - 1), n, c.st, c.d_hbin, c.d_hbin32);
     c.count(2);
   });
   CK(cudaMemcpyAsync(h_beta + (j - 1), d_beta + (j - 1), sizeof(double), cudaMemcpyDeviceToHost, c.st));

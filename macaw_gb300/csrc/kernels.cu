@@ -1235,22 +1235,44 @@ __global__ void __launch_bounds__(256) termsum_kernel(cplx* __restrict__ out, co
       for (int k = threadIdx.x; k < rg.count; k += blockDim.x) ss[k] = srcs[rg.first + k];
     __syncthreads();
     const SumSrc* sp = cached ? ss : srcs + rg.first;
+    if (PREC == 1) {
+      // four elements per thread in flight: per source, four independent loads
+      const long long stride = (long long)blockDim.x;
+      for (long long i0 = base + threadIdx.x; i0 < seg_end; i0 += 4 * stride) {
+        float ar[4] = {0.f, 0.f, 0.f, 0.f}, ai[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < rg.count; ++k) {
+          const float cr = sp[k].cs[0] + sp[k].cs[1], ci = sp[k].cs[2] + sp[k].cs[3];
+          const cplx* src = sp[k].src;
+          const int fmt = sp[k].fmt;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const long long i = i0 + e * stride;
+            if (i >= seg_end) break;
+            const float4 x = load_split(src, i - rg.offset, fmt);
+            const float xr = x.x + x.z, xi = x.y + x.w;
+            ar[e] = fmaf(cr, xr, fmaf(-ci, xi, ar[e]));
+            ai[e] = fmaf(cr, xi, fmaf(ci, xr, ai[e]));
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const long long i = i0 + e * stride;
+          if (i >= seg_end) break;
+          const cplx val = mkc(f2d_exact(ar[e]), f2d_exact(ai[e]));
+          out[i] = val;
+          if (dot.v) cfma_conj(d, dot.v[i], val);
+        }
+      }
+      __syncthreads();
+      base = seg_end;
+      continue;
+    }
     for (long long i = base + threadIdx.x; i < seg_end; i += blockDim.x) {
       const long long li = i - rg.offset;
       cplx val;
       if (PREC == 0) {
         val = mkc(0, 0);
         for (int k = 0; k < rg.count; ++k) cfma(val, sp[k].coeff, load_c(sp[k].src, li, sp[k].fmt));
-      } else if (PREC == 1) {
-        float ar = 0.f, ai = 0.f;
-        for (int k = 0; k < rg.count; ++k) {
-          const float cr = sp[k].cs[0] + sp[k].cs[1], ci = sp[k].cs[2] + sp[k].cs[3];
-          const float4 x = load_split(sp[k].src, li, sp[k].fmt);
-          const float xr = x.x + x.z, xi = x.y + x.w;
-          ar = fmaf(cr, xr, fmaf(-ci, xi, ar));
-          ai = fmaf(cr, xi, fmaf(ci, xr, ai));
-        }
-        val = mkc(f2d_exact(ar), f2d_exact(ai));
       } else {
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
         for (int k = 0; k < rg.count; ++k) {
@@ -1604,21 +1626,33 @@ void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_a
 
 // Grid-stride: the norm and its reciprocal once per thread (FP64 square roots and
 // divisions are expensive on this GPU), then one multiply per component.
+// ... optionally also into copy (FP64) and f32 (complex FP32 rounded to nearest):
+// the input of the next H_B application, written in the same pass.
 __global__ void lan_normalize_kernel(cplx* __restrict__ out, const cplx* __restrict__ in, const cplx* __restrict__ nrm2,
-                                     double* beta_out, long long n) {
+                                     double* beta_out, long long n, cplx* __restrict__ copy,
+                                     float2* __restrict__ f32) {
   const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const double beta = sqrt(nrm2->x);
   if (i0 == 0 && beta_out) *beta_out = beta;
   const double s = 1.0 / beta;
   for (long long i = i0; i < n; i += (long long)gridDim.x * blockDim.x) {
     const cplx v = in[i];
-    out[i] = mkc(v.x * s, v.y * s);
+    const cplx w = mkc(v.x * s, v.y * s);
+    out[i] = w;
+    if (copy) copy[i] = w;
+    if (f32) {
+      float hx, lx, hy, ly;
+      split_d2f(w.x, hx, lx);
+      split_d2f(w.y, hy, ly);
+      f32[i] = make_float2(hx + lx, hy + ly);
+    }
   }
 }
-void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st) {
+void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st,
+                          cplx* copy, cplx* f32) {
   const long long want = (n + 255) / 256;
   const unsigned nb = (unsigned)std::max<long long>(1, std::min<long long>(want, 152 * 4));
-  lan_normalize_kernel<<<nb, 256, 0, st>>>(out, in, nrm2, beta_out, n);
+  lan_normalize_kernel<<<nb, 256, 0, st>>>(out, in, nrm2, beta_out, n, copy, reinterpret_cast<float2*>(f32));
 }
 
 // ---------------------------------------------------------------------------

@@ -280,7 +280,8 @@ void launch_spf_err(const SpfErrDesc* d, int nd, double* err_mode, int nmodes, c
 void launch_lan_axpy(cplx* Kn, const cplx* Kj, const cplx* Kp, const cplx* dot_alpha, const double* beta_prev,
                      double* alpha_out, long long n, cudaStream_t st,
                      FusedDot nrm = FusedDot{nullptr, nullptr, nullptr, nullptr});
-void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st);
+void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* beta_out, long long n, cudaStream_t st,
+                          cplx* copy = nullptr, cplx* f32 = nullptr);
 // <a|b> = sum_i conj(a_i) b_i in FP64 into *out, one launch, fixed summation order.
 // partial: DOT_BLOCKS complex scratch; counter: one zero-initialised unsigned.
 #define DOT_BLOCKS 304
