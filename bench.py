@@ -39,7 +39,7 @@ WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/
 EPS_CMF = 1e-5
 PRE_FS = 1.0
 MFX_EPOCHS = 12
-TRAFFIC_PER_ALG_BYTE = 0.43   # ncu DRAM bytes per algorithmic byte, mode products of this model
+TRAFFIC_PER_ALG_BYTE = 0.51   # ncu DRAM bytes per algorithmic byte, mode products of this model
 ACC_FS = 0.5   # interval over which the split path is compared with the FP64 path
 REF_STEP_FS = 0.1   # CMF2 step length the reference arm times (steady-state steps are of this order)
 
@@ -364,7 +364,7 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
                      "traffic": by_launch * TRAFFIC_PER_ALG_BYTE if dname == "mode_product" else None,
-                     "traffic_source": "ncu DRAM bytes / algorithmic bytes of three mode-product launches of "
+                     "traffic_source": "ncu DRAM bytes / algorithmic bytes of the mean-field chain product launches of "
                                        "this model (profiles/qvc12_cmf2_split32_ncu.md), times the "
                                        "algorithmic bytes per launch",
                      "peak_source": peak_src},
@@ -372,7 +372,7 @@ def run_gpu(args):
                      "fp64_peak": fp64_peak, "frac_of_fp64_peak": achieved_tf / fp64_peak if fp64_peak > 0 else None,
                      "peak_source": "measured FP64 FMA chain on this GPU"} if args.precision == 0 else
                     {"kernel": dname, "achieved": achieved_tf, "unit": "TFLOP/s (complex MAC = 8 flop)",
-                     "note": "split-FP32 arithmetic: FP32-issue-bound in ncu (FMA pipe 55-60 %, issue 68-74 %)"}),
+                     "note": "FP32 mode products: issue-bound in ncu (issue 52-68 %, FMA pipe 27-32 %)"}),
         "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                                "share": round(v["ms"] / tot_ms, 4)}
                            for k, v in prof.items() if v["launches"]},
