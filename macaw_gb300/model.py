@@ -197,6 +197,16 @@ class Model:
     label: str = "model"
     # operators whose expectation values are written (the 'expect' keyword, input.f90:196-216)
     expect: List[List[Term]] = dataclasses.field(default_factory=list)
+    # statistical mixtures (the 'npackets' and 'eps_pop' keywords, input.f90:156, 262)
+    npackets: int = 1
+    eps_pop: float = 1e-6
+    # dissipative operators (the 'dissipation' keyword, input.f90:216-229, 596-616):
+    # (type 1 or 2, global coefficient as read, terms); type 1 is alpha V rho V^+
+    # with aeD1 = alpha / 2, type 2 is beta (W rho + rho W^+) with aeD2 = beta
+    dissipation: List[Tuple[int, float, List[Term]]] = dataclasses.field(default_factory=list)
+    # explicit mixture states of the INIT-WF 'packets' block (init_calc.f90:527-540):
+    # (state, 0-based SPF index per mode, coefficient) per packet
+    init_packets: Optional[List[Tuple[int, Tuple[int, ...], complex]]] = None
 
     # ---- derived (filled by finalize) ----
     def finalize(self) -> "Model":
@@ -256,6 +266,7 @@ class Model:
         self.ioper = np.zeros((self.nmodes, nham), dtype=np.int64)
         # iOperExtra: (nmodes, nterms) per expectation operator
         self.ioper_expect = [np.zeros((self.nmodes, len(op)), dtype=np.int64) for op in self.expect]
+        self.ioper_diss = [np.zeros((self.nmodes, len(d[2])), dtype=np.int64) for d in self.dissipation]
 
         def vec_of(m, term):
             el = (term.lhs, term.rhs) if self.multiset[m] else (0, 0)
@@ -276,6 +287,9 @@ class Model:
             for i, op in enumerate(self.expect):
                 for t, term in enumerate(op):
                     self.ioper_expect[i][m, t] = index_of(vec_of(m, term))
+            for i, (_, _, dterms) in enumerate(self.dissipation):
+                for t, term in enumerate(dterms):
+                    self.ioper_diss[i][m, t] = index_of(vec_of(m, term))
             self.oper.append(ops)
         self.nopermax = max(len(o) for o in self.oper)
         self.is_identity = np.zeros((self.nmodes, self.nopermax), dtype=bool)
@@ -288,11 +302,33 @@ class Model:
             for m in range(self.nmodes):
                 if (not self.is_gwp_mode[m]) and self.is_identity[m, self.ioper[m, t]]:
                     self.skip_term[m, t] = True
+        # SkipTerm of the dissipative terms: the identity on a DVR mode is not applied
+        # (gmctdh_objects.f90:632, 773)
+        self.skip_diss = []
+        for i, (_, _, dterms) in enumerate(self.dissipation):
+            sk = np.zeros((self.nmodes, len(dterms)), dtype=bool)
+            for t in range(len(dterms)):
+                for m in range(self.nmodes):
+                    sk[m, t] = (not self.is_gwp_mode[m]) and self.is_identity[m, self.ioper_diss[i][m, t]]
+            self.skip_diss.append(sk)
+        self.aeD1 = [0.5 * c for (ty, c, _) in self.dissipation if ty == 1]   # input.f90:607
+        self.aeD2 = [c for (ty, c, _) in self.dissipation if ty == 2]         # input.f90:612
+        self.diss1 = [i for i, d in enumerate(self.dissipation) if d[0] == 1]
+        self.diss2 = [i for i, d in enumerate(self.dissipation) if d[0] == 2]
+        for ty, _, dterms in self.dissipation:
+            if ty not in (1, 2):
+                raise ModelError(f"dissipation type {ty} is not supported (1: V rho V^+, 2: W rho + rho W^+)")
+            if ty == 1 and any(term.lhs != term.rhs for term in dterms):
+                raise ModelError("type-1 dissipative terms must act within one electronic state")
+        if self.npackets < 1:
+            raise ModelError("npackets must be at least 1")
+        if self.npackets > 1 and self.modes_gwp:
+            raise ModelError("statistical mixtures with Gaussian modes are not supported by this core")
         self.ae = np.array([term.coeff for term in self.terms], dtype=np.complex128)
         self.lhs_el = np.array([term.lhs for term in self.terms], dtype=np.int64)
         self.rhs_el = np.array([term.rhs for term in self.terms], dtype=np.int64)
         codes = {d: set(int(c) for c in self.iopdof[d]) for d in range(self.ndof)}
-        for op in self.expect:
+        for op in self.expect + [d[2] for d in self.dissipation]:
             for term in op:
                 for d, c in term.dof_ops.items():
                     codes[d].add(int(c))
@@ -372,8 +408,6 @@ def initial_wavefunction(model: Model) -> Tuple[np.ndarray, np.ndarray]:
     built by SetSPF (DVR: product Gaussian, then q-multiplied virtual SPFs,
     Gram-Schmidt + QR; GWP: lattice of Gaussians).  Returns (A, psi) with the
     normalisation of init_calc.f90:208-221 applied."""
-    A = np.zeros(model.naconftot, dtype=np.complex128)
-    A[int(model.astate_offset[model.init_state])] = 1.0
     psi = np.zeros(model.dimpsi, dtype=np.complex128)
     phi: Dict[int, np.ndarray] = {}
     gwp_par: Dict[int, tuple] = {}
@@ -506,7 +540,58 @@ def initial_wavefunction(model: Model) -> Tuple[np.ndarray, np.ndarray]:
             o = int(model.ipsispf[m, s])
             n = int(model.nspf[m, s])
             psi[o:o + nmd * n] = psi_t[:, :n].reshape(-1, order="F")
-    return A, psi
+    return initial_coefficients(model, psi), psi
+
+
+def initial_coefficients(model: Model, psi: np.ndarray) -> np.ndarray:
+    """Coefficients of the initial mixture, packet-major (APacketOffset(W) =
+    W * nAConftot).  'el' line (init_calc.f90:490-500): packet W (0-based) has the
+    single coefficient 1 (W = 0) or sqrt(eps_pop (W + 1)) on configuration W of the
+    initial state; 'packets' block (:527-540): one given coefficient per packet.
+    With more than one packet the packets are then rotated into the eigenvectors of
+    their overlap matrix (OrthoWP, init_calc.f90:1093-1126, eigenvalues ascending)
+    and the mixture is normalised to unit trace (trace_wf, init_calc.f90:212-219)."""
+    P = model.npackets
+    n = model.naconftot
+    A = np.zeros(n * P, dtype=np.complex128)
+    if model.init_packets is None:
+        s = model.init_state
+        o = int(model.astate_offset[s])
+        if P > int(model.naconf[s]):
+            raise ModelError("the number of wave packets is larger than the configurations of the initial state")
+        for W in range(P):
+            A[W * n + o + W] = 1.0 if W == 0 else math.sqrt(model.eps_pop * (W + 1))
+    else:
+        if len(model.init_packets) != P:
+            raise ModelError("the 'packets' block needs one line per wave packet")
+        for W, (s, jspf, coef) in enumerate(model.init_packets):
+            idx, stride = 0, 1
+            for m in range(model.nmodes):
+                if not 0 <= jspf[m] < int(model.nspf[m, s]):
+                    raise ModelError("SPF index of a 'packets' line out of range")
+                idx += jspf[m] * stride
+                stride *= int(model.nspf[m, s])
+            A[W * n + int(model.astate_offset[s]) + idx] = coef
+    if P == 1:
+        return A
+    # SPF overlap matrices (DVR modes): <A_i|A_j> = sum_s A_i,s^H (x_m S_m) A_j,s
+    Amat = A.reshape((n, P), order="F")
+    ovl = np.zeros((P, P), dtype=np.complex128)
+    for s in range(model.nstates):
+        o, ns = int(model.astate_offset[s]), int(model.naconf[s])
+        shape = tuple(int(x) for x in model.nspf[:, s])
+        for j in range(P):
+            Y = Amat[o:o + ns, j].reshape(shape, order="F")
+            for m in range(model.nmodes):
+                phi = model.spf_block(psi, m, s)
+                Y = np.moveaxis(np.tensordot(phi.conj().T @ phi, Y, axes=([1], [m])), 0, m)
+            y = Y.reshape(-1, order="F")
+            for i in range(P):
+                ovl[i, j] += np.vdot(Amat[o:o + ns, i], y)
+    _, V = np.linalg.eigh(ovl, UPLO="U")
+    Amat = Amat @ V
+    trace = float(np.real(np.trace(V.conj().T @ ovl @ V)))
+    return (Amat / math.sqrt(trace)).reshape(-1, order="F")
 
 
 # ----------------------------------------------------------------------------
@@ -591,6 +676,7 @@ def parse_input(path: str) -> Model:
     i = 0
     flags = set()
     expect_files: List[str] = []
+    diss_files: List[str] = []
     while i < len(lines):
         line = lines[i].split("#", 1)[0]
         i += 1
@@ -637,12 +723,14 @@ def parse_input(path: str) -> Model:
             kw[name] = val
         elif name == "expect":
             expect_files.append(val)
+        elif name == "dissipation":
+            diss_files.append(val)
+        elif name == "lcharmbathpt":
+            raise ModelError("the perturbative harmonic bath (lcharmbathpt) is not supported by this core")
         elif name == "densmat":
             continue
         else:
             raise ModelError(f"Input instruction: {s} cannot be understood")
-    if int(kw.get("npackets", "1")) != 1:
-        raise ModelError("npackets > 1 is not supported by this core")
     mode_dofs: List[List[int]] = []
     multiset: List[bool] = []
     nspf = np.zeros((nmodes, nstates), dtype=np.int64)
@@ -683,9 +771,28 @@ def parse_input(path: str) -> Model:
             raise ModelError(f"Operator file, {ef} not found")
         with open(epath) as fh:
             expect.append(parse_operator_file(fh.read(), nstates))
+    dissipation: List[Tuple[int, float, List[Term]]] = []
+    for df in diss_files:
+        dpath = os.path.join(base, df)
+        if not os.path.exists(dpath):
+            raise ModelError(f"Operator file, {df} not found")
+        with open(dpath) as fh:
+            dtext = fh.read().splitlines()
+        # the first line holds the type and the global coefficient (input.f90:221, 602)
+        first = 0
+        while first < len(dtext) and not dtext[first].split("#", 1)[0].strip():
+            first += 1
+        if first == len(dtext):
+            raise ModelError(f"dissipation file {df} is empty")
+        head = dtext[first].split("#", 1)[0].replace(",", " ").split()
+        dissipation.append((int(head[0]), _read_float(head[1]),
+                            parse_operator_file("\n".join(dtext[first + 1:]), nstates)))
     model = Model(nstates=nstates, mode_dofs=mode_dofs, multiset=multiset, nspf=nspf,
                   dvr_type=dvr_type, ngp=ngp, dvrpar=dvrpar, terms=terms,
-                  label=os.path.basename(path), expect=expect)
+                  label=os.path.basename(path), expect=expect, dissipation=dissipation,
+                  npackets=int(kw.get("npackets", "1")))
+    if "eps_pop" in kw:
+        model.eps_pop = _read_float(kw["eps_pop"])
     if "tinit" in kw:
         model.tinit = _read_float(kw["tinit"]) / AU2FS
     if "tfinal" in kw:
@@ -728,11 +835,25 @@ def parse_input(path: str) -> Model:
     # INIT-WF single-conf
     if not init_lines or init_lines[0] != "single-conf":
         raise ModelError("only the single-conf INIT-WF block is supported")
-    mm = re.match(r"el\s+(\d+)", init_lines[1])
-    if not mm:
-        raise ModelError("INIT-WF: expecting 'el <state>'")
-    model.init_state = int(mm.group(1)) - 1
-    for ln in init_lines[2:]:
+    spf_start = 2
+    if init_lines[1].strip().lower() == "packets":
+        # one line per packet: state, SPF index per mode, Re, Im (init_calc.f90:527-540)
+        packets = []
+        for W in range(model.npackets):
+            toks = init_lines[2 + W].replace(",", " ").split()
+            st = int(toks[0]) - 1
+            jspf = tuple(int(v) - 1 for v in toks[1:1 + nmodes])
+            cr, ci = _read_float(toks[1 + nmodes]), _read_float(toks[2 + nmodes])
+            packets.append((st, jspf, complex(cr, ci)))
+        model.init_packets = packets
+        model.init_state = packets[0][0]
+        spf_start = 2 + model.npackets
+    else:
+        mm = re.match(r"el\s+(\d+)", init_lines[1])
+        if not mm:
+            raise ModelError("INIT-WF: expecting 'el <state>' or 'packets'")
+        model.init_state = int(mm.group(1)) - 1
+    for ln in init_lines[spf_start:]:
         if "gauss" in ln:
             k, rest = ln.split("gauss", 1)
             x0, p0, dx = [_read_float(v) for v in rest.split()[:3]]

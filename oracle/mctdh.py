@@ -243,6 +243,7 @@ class Oracle:
         self.m = model
         self.eom_calls = 0
         self.hb_calls = 0
+        self.wppop = [1.0] * model.npackets
 
     # ---------------- SPF-side objects ----------------
     def apply_oper(self, mode: int, k: int, phi: np.ndarray) -> np.ndarray:
@@ -359,17 +360,25 @@ class Oracle:
                 hm[k] = herm_from_upper(H) if l == r else H
 
     # ---------------- A-side objects ----------------
+    def packets(self, A: np.ndarray) -> List[np.ndarray]:
+        """The packets of a mixture: A(APacketOffset(W) + 1 : ...) with
+        APacketOffset(W) = W * nAConftot (init_calc.f90:50-53)."""
+        n = self.m.naconftot
+        return [A[W * n:(W + 1) * n] for W in range(self.m.npackets)]
+
     def calc_rho1mode(self, mode: int, A: np.ndarray):
-        """Calc_rho1mode (gmctdh_objects.f90:408-477)."""
+        """Calc_rho1mode (gmctdh_objects.f90:408-477), summed over the packets."""
         md = self.m
         for s in range(md.nstates):
-            X = md.a_state(A, s)
-            Y = X
-            for i, m2 in enumerate(md.modes_gwp):
-                if m2 == mode:
-                    continue
-                Y = mode_product(self.s00(i, s, s), Y, m2)
-            R = hole_contract(Y, X, mode)
+            R = 0
+            for AW in self.packets(A):
+                X = md.a_state(AW, s)
+                Y = X
+                for i, m2 in enumerate(md.modes_gwp):
+                    if m2 == mode:
+                        continue
+                    Y = mode_product(self.s00(i, s, s), Y, m2)
+                R = R + hole_contract(Y, X, mode)
             self.rho[(mode, s)] = 0.5 * (R + R.conj().T)
         if not md.multiset[mode]:
             ra = self.rho[(mode, 0)].copy()
@@ -377,50 +386,153 @@ class Oracle:
                 ra = ra + self.rho[(mode, s)]
             self.rho_ave[mode] = ra
 
-    def calc_meanfield(self, A: np.ndarray, t: float):
-        """Hamiltonian part of Calc_MeanField (gmctdh_objects.f90:513-604).
+    def _right_chain(self, X: np.ndarray, ioper: np.ndarray, skip: np.ndarray) -> List[np.ndarray]:
+        """H_f x X, H_(f-1) x H_f x X, ... (gmctdh_objects.f90:527-550)."""
+        f = self.m.nmodes
+        R = [X]
+        for im in range(f):
+            jm = f - 1 - im
+            if skip[jm]:
+                R.append(R[-1])
+                continue
+            R.append(mode_product(self.h1mode[jm][int(ioper[jm])], R[-1], jm))
+        return R
 
-        Returns Adot = f * H A (the reference stores its complex conjugate in
-        Adot_tmp) and sets self.MF[(mode, op)] and self.energyMF."""
+    def _left_chain(self, X: np.ndarray, ioper: np.ndarray, skip: np.ndarray) -> List[np.ndarray]:
+        """X x H_1, X x H_1 x H_2, ... (gmctdh_objects.f90:552-573)."""
+        f = self.m.nmodes
+        L = [X]
+        for im in range(f - 1):
+            if skip[im]:
+                L.append(L[-1])
+                continue
+            L.append(mode_product(self.h1mode[im][int(ioper[im])].conj().T, L[-1], im))
+        return L
+
+    def _add_mf(self, im: int, k: int, M: np.ndarray):
+        key = (im, k)
+        self.MF[key] = self.MF.get(key, 0) + M
+
+    def calc_meanfield(self, A: np.ndarray, t: float):
+        """Calc_MeanField (gmctdh_objects.f90:481-1141): Hamiltonian terms per
+        packet (:513-604), type-1 dissipation alpha V rho V^+ (:606-745), type-2
+        dissipation beta (W rho + rho W^+) (:747-845) and the Lagrange multipliers
+        that conserve the total population and the packets' orthogonality
+        (:612-620, 1128-1137).  The perturbative harmonic bath is not covered.
+
+        Returns Adot (the reference stores its complex conjugate in Adot_tmp), sets
+        self.MF[(mode, op)], self.energyMF, self.mult_diag and self.mult_lag (lower
+        triangle)."""
         md = self.m
         f = md.nmodes
+        n = md.naconftot
+        P = md.npackets
+        pk = self.packets(A)
         self.MF = {}
-        adot = np.zeros(md.naconftot, dtype=np.complex128)
+        adot = np.zeros(n * P, dtype=np.complex128)
         energy = 0.0
+
+        def seg(W, s):
+            o = W * n + int(md.astate_offset[s])
+            return slice(o, o + int(md.naconf[s]))
+
         for t_ in range(md.nham):
             s1, s2 = int(md.lhs_el[t_]), int(md.rhs_el[t_])
             ae = md.ae[t_]
-            # right chain: H_f x A, H_(f-1) x H_f x A, ...   (:527-550)
-            R = [md.a_state(A, s2)]
-            for im in range(f):
-                jm = f - 1 - im
-                if md.skip_term[jm, t_]:
-                    R.append(R[-1])
-                    continue
-                h = self.h1mode[jm][int(md.ioper[jm, t_])]
-                R.append(mode_product(h, R[-1], jm))
-            # left chain: A x H_1, A x H_1 x H_2, ...   (:552-573)
-            L = [md.a_state(A, s1)]
-            for im in range(f - 1):
-                if md.skip_term[im, t_]:
-                    L.append(L[-1])
-                    continue
-                h = self.h1mode[im][int(md.ioper[im, t_])]
-                L.append(mode_product(h.conj().T, L[-1], im))
-            o1 = int(md.astate_offset[s1])
-            n1 = int(md.naconf[s1])
-            Rf = R[f].reshape(-1, order="F")
-            adot[o1:o1 + n1] += md.der_factor * ae * Rf                      # :578
-            energy += float((ae * np.vdot(A[o1:o1 + n1], Rf)).real)          # :580
-            for im in range(f):                                               # :582-601
-                k = int(md.ioper[im, t_])
-                if md.is_identity[im, k]:
-                    continue
-                C = hole_contract(L[im], R[f - 1 - im], im)
-                key = (im, k)
-                self.MF[key] = self.MF.get(key, 0) + ae * C
+            for W, AW in enumerate(pk):
+                R = self._right_chain(md.a_state(AW, s2), md.ioper[:, t_], md.skip_term[:, t_])
+                L = self._left_chain(md.a_state(AW, s1), md.ioper[:, t_], md.skip_term[:, t_])
+                Rf = R[f].reshape(-1, order="F")
+                adot[seg(W, s1)] += md.der_factor * ae * Rf                             # :578
+                energy += float((ae * np.vdot(A[seg(W, s1)], Rf)).real)                # :580
+                for im in range(f):                                                     # :582-601
+                    k = int(md.ioper[im, t_])
+                    if md.is_identity[im, k]:
+                        continue
+                    self._add_mf(im, k, ae * hole_contract(L[im], R[f - 1 - im], im))
         self.energyMF = energy
+        # dissipative terms
+        self.mult_diag = 0.0
+        self.mult_lag = np.zeros((P, P), dtype=np.complex128)
+        pop = np.asarray(self.wppop, dtype=float)
+        reg = md.eps_pop * np.exp(-(pop / md.eps_pop) ** 2)
+        wpm1 = pop / (pop ** 2 + reg ** 2)                                              # :616-619
+        Amat = A.reshape((n, P), order="F")
+        for kd, idx in enumerate(md.diss1):                                             # :606-745
+            aeD1 = md.aeD1[kd]
+            dterms = md.dissipation[idx][2]
+            iop, sk = md.ioper_diss[idx], md.skip_diss[idx]
+            VA = np.zeros(n * P, dtype=np.complex128)
+            for t_, term in enumerate(dterms):
+                s1, s2 = term.lhs, term.rhs
+                for W, AW in enumerate(pk):
+                    X = md.a_state(AW, s2)
+                    for im in range(f):                                                 # :630-646
+                        if sk[im, t_]:
+                            continue
+                        X = mode_product(self.h1mode[im][int(iop[im, t_])], X, im)
+                    VA[seg(W, s1)] += term.coeff * X.reshape(-1, order="F")            # :648
+            VAm = VA.reshape((n, P), order="F")
+            AVA = Amat.conj().T @ VAm                                                   # :661-662, <A_i|V A_j>
+            self.mult_diag += aeD1 * -float(np.sum((np.abs(AVA) ** 2) * wpm1[:, None]))   # :664-672
+            AVAAVpA = aeD1 * (AVA @ AVA.conj().T)                                       # :674
+            for i in range(P):
+                for j in range(i):
+                    self.mult_lag[i, j] += AVAAVpA[i, j] * (wpm1[i] + wpm1[j])         # :675-676
+            adot += (aeD1 * (VAm @ AVA.conj().T) * wpm1[None, :]).reshape(-1, order="F")  # :678-684
+            AuxA = (1j * aeD1 * (Amat @ AVA.conj().T)) * wpm1[None, :]                # :686-692
+            auxp = [AuxA[:, W] for W in range(P)]
+            for t_, term in enumerate(dterms):                                          # :696-744
+                s1, s2 = term.lhs, term.rhs
+                for im in range(f):
+                    k = int(iop[im, t_])
+                    if md.is_identity[im, k]:
+                        continue
+                    for W, AW in enumerate(pk):
+                        X = md.a_state(AW, s2)
+                        for im2 in range(f):
+                            if im2 == im or sk[im2, t_]:
+                                continue
+                            X = mode_product(self.h1mode[im2][int(iop[im2, t_])], X, im2)
+                        self._add_mf(im, k, term.coeff * hole_contract(X, md.a_state(auxp[W], s1), im))
+        for kd, idx in enumerate(md.diss2):                                             # :747-845
+            dterms = md.dissipation[idx][2]
+            iop, sk = md.ioper_diss[idx], md.skip_diss[idx]
+            for t_, term in enumerate(dterms):
+                aet = md.aeD2[kd] * term.coeff
+                cd = md.der_factor * 1j * aet
+                s1, s2 = term.lhs, term.rhs
+                for W, AW in enumerate(pk):
+                    R = self._right_chain(md.a_state(AW, s2), iop[:, t_], sk[:, t_])
+                    L = self._left_chain(md.a_state(AW, s1), iop[:, t_], sk[:, t_])
+                    Rf = R[f].reshape(-1, order="F")
+                    adot[seg(W, s1)] += cd * Rf                                        # :805-806
+                    self.mult_diag += -float((cd * np.vdot(A[seg(W, s1)], Rf)).real)  # :807-808
+                    for W2 in range(W):                                                 # :809-813
+                        self.mult_lag[W, W2] += np.conj(cd) * np.vdot(Rf, A[seg(W2, s1)])
+                    for W2 in range(W + 1, P):                                          # :814-818
+                        self.mult_lag[W2, W] += cd * np.conj(np.vdot(Rf, A[seg(W2, s1)]))
+                    for im in range(f):                                                 # :820-840
+                        k = int(iop[im, t_])
+                        if md.is_identity[im, k]:
+                            continue
+                        self._add_mf(im, k, 1j * aet * hole_contract(L[im], R[f - 1 - im], im))
+        for j in range(P):                                                              # :1128-1137
+            for i in range(j + 1, P):
+                dw = pop[i] - pop[j]
+                r = md.eps_pop * math.exp(-(dw / md.eps_pop) ** 2)
+                self.mult_lag[i, j] *= 1j * dw / (dw ** 2 + r ** 2)
         return adot
+
+    def apply_multipliers(self, A: np.ndarray, dA: np.ndarray) -> np.ndarray:
+        """dA += multLagDiag A + i A multLag with multLag Hermitian from its
+        lower triangle and a zero diagonal (derivatives.f90:238-242)."""
+        md = self.m
+        P = md.npackets
+        M = np.tril(self.mult_lag, -1)
+        M = M + M.conj().T
+        Amat = A.reshape((md.naconftot, P), order="F")
+        return dA + self.mult_diag * A + (1j * (Amat @ M)).reshape(-1, order="F")
 
     def calc_rhom1mf(self):
         """Calc_rhom1MF (gmctdh_objects.f90:1147-1194) with 'poly' regularisation."""
@@ -566,6 +678,9 @@ class Oracle:
         md = self.m
         self.eom_calls += 1
         self._prepare(A, psi)
+        # packet populations (derivatives.f90:70-83); one packet keeps the unit
+        # population that WriteOutput leaves in WPpop (output.f90:47-53)
+        self.wppop = [self.norm_wf(AW, psi) for AW in self.packets(A)] if md.npackets > 1 else [1.0]
         adot = self.calc_meanfield(A, t)
         self.calc_rhom1mf()
         for i in range(len(md.modes_gwp)):
@@ -574,6 +689,8 @@ class Oracle:
         for mode in md.modes_dvr:
             self.dvr_spf_derivative(psi, mode, dpsi)
         if not md.modes_gwp:
+            if md.npackets > 1:
+                adot = self.apply_multipliers(A, adot)
             return adot, dpsi
         # Gaussian parameter derivatives (derivatives.f90:158-173)
         for i, mode in enumerate(md.modes_gwp):
@@ -649,7 +766,18 @@ class Oracle:
         return tot
 
     def delta_psi(self, A1, psi1, A2, psi2) -> float:
-        """DeltaPsi (gmctdh_objects.f90:206-226), npackets = 1."""
+        """DeltaPsi (gmctdh_objects.f90:206-248): for a mixture
+        sqrt(2 sum_W |sqrt(o11 o22) - Re o12| / sum_W sqrt(o11 o22)) over the packets."""
+        if self.m.npackets > 1:
+            num = pop = 0.0
+            for B1, B2 in zip(self.packets(A1), self.packets(A2)):
+                o11 = self.norm_wf(B1, psi1)
+                o22 = self.norm_wf(B2, psi2)
+                o12 = self.wf_ovl(B1, psi1, B2, psi2)
+                d = math.sqrt(o11 * o22)
+                pop += d
+                num += abs(d - o12.real)
+            return math.sqrt(2.0 * num / pop)
         o11 = self.norm_wf(A1, psi1)
         o22 = self.norm_wf(A2, psi2)
         o12 = self.wf_ovl(A1, psi1, A2, psi2)
@@ -1329,8 +1457,12 @@ class Oracle:
                 pop[s] = v
             else:
                 pop[s] = float(np.trace(r).real)
-        auto = self.wf_ovl(A0, psi0, A, psi)
-        return dict(t=t, pop=pop, norm=float(pop.sum()), energy=self.energyMF / pop.sum(), auto=auto)
+        auto = sum(self.wf_ovl(B0, psi0, B, psi) for B0, B in zip(self.packets(A0), self.packets(A)))  # :143-149
+        wp = np.array([self.norm_wf(B, psi) for B in self.packets(A)])                    # :46-60
+        wp = wp / wp.sum()
+        ent = -sum(w * math.log(w) for w in wp if w >= 1e-8) / math.log(md.npackets) if md.npackets > 1 else 0.0
+        return dict(t=t, pop=pop, norm=float(pop.sum()), energy=self.energyMF / pop.sum(), auto=auto,
+                    wppop=np.sort(wp)[::-1], entropy=ent)
 
     def expectation(self, A, psi) -> np.ndarray:
         """Expectation (output.f90:449-500): for each expectation operator
@@ -1340,12 +1472,13 @@ class Oracle:
         md = self.m
         self._prepare(A, psi)
         out = np.zeros(len(md.expect), dtype=np.complex128)
-        for i, op in enumerate(md.expect):
-            for t, term in enumerate(op):
-                X = md.a_state(A, term.rhs)
-                for mode in range(md.nmodes):
-                    X = mode_product(self.h1mode[mode][int(md.ioper_expect[i][mode, t])], X, mode)
-                out[i] += term.coeff * np.vdot(md.a_state(A, term.lhs), X)
+        for AW in self.packets(A):                       # summed over the packets (:461)
+            for i, op in enumerate(md.expect):
+                for t, term in enumerate(op):
+                    X = md.a_state(AW, term.rhs)
+                    for mode in range(md.nmodes):
+                        X = mode_product(self.h1mode[mode][int(md.ioper_expect[i][mode, t])], X, mode)
+                    out[i] += term.coeff * np.vdot(md.a_state(AW, term.lhs), X)
         return out
 
     def natpop(self, A, psi):

@@ -69,3 +69,39 @@ def with_expect(model):
     if gwpa is not None:
         model.gwpa = gwpa
     return model
+
+
+def with_mixture(model, npackets=3, diss=True, eps_pop=1e-6):
+    """The model as a statistical mixture of `npackets` packets, with (diss=True)
+    a type-1 operator V = 0.4 q_1 on every state plus 0.3 q_2^2 on state 1 and
+    coefficient 0.02 (aeD1 = 0.01), and a type-2 operator W = -0.5 q_1^2 on
+    every state plus the coupling 0.2 (|1><2| + |2><1|) q_3 with coefficient 0.03."""
+    from macaw_gb300.model import Term
+    ns = model.nstates
+    model.npackets = npackets
+    model.eps_pop = eps_pop
+    model.dissipation = []
+    if diss:
+        v = [Term(0.4, s, s, {0: 1}) for s in range(ns)] + [Term(0.3, 0, 0, {1: 2})]
+        w = [Term(-0.5, s, s, {0: 2}) for s in range(ns)]
+        if ns > 1:
+            w += [Term(0.2, 0, 1, {2: 1}), Term(0.2, 1, 0, {2: 1})]
+        model.dissipation = [(1, 0.02, v), (2, 0.03, w)]
+    return model.finalize()
+
+
+def random_mixture(model, seed=0, pops=None):
+    """Random SPFs and P mutually orthogonal packets with distinct populations
+    (default 0.6, 0.3, 0.1, ... normalised to unit trace), packet-major."""
+    rng = np.random.default_rng(seed)
+    P = model.npackets
+    A1, psi = random_state(model, seed=seed)
+    n = model.naconftot
+    X = rng.normal(size=(n, P)) + 1j * rng.normal(size=(n, P))
+    q, _ = np.linalg.qr(X)
+    if pops is None:
+        pops = np.array([0.6 / 2 ** k for k in range(P)])
+    pops = np.asarray(pops, dtype=float)
+    pops = pops / pops.sum()
+    A = (q * np.sqrt(pops)[None, :]).reshape(-1, order="F")
+    return A, psi
