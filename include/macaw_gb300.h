@@ -70,6 +70,23 @@ typedef struct mctdh_setup {
   const int64_t *expect_lhs;     /* lhs_elExtra, 0-based, concatenated                   */
   const int64_t *expect_rhs;     /* rhs_elExtra                                          */
   const int64_t *expect_ioper;   /* iOperExtra(nmodes, total terms), 0-based             */
+  /* Statistical mixtures and dissipation (input.f90:156, 216-229, 262, 596-616;
+   * gmctdh_objects.f90:481-1141; derivatives.f90:70-83, 238-242).  Every coefficient
+   * array that crosses the boundary holds the npackets packets one after the other
+   * (APacketOffset(W) = W * nAConftot, init_calc.f90:50-53).  Dissipative terms
+   * follow the Hamiltonian's terms in ae/lhs_el/rhs_el/ioper/skip_term (nham counts
+   * them) with term_kind 1 for a term of a type-1 operator alpha V rho V^+ (ae =
+   * aeExtra, term_diss1 = its operator, diss1_ae = aeD1 = alpha / 2) and 2 for a term
+   * of a type-2 operator beta (W rho + rho W^+) (ae = i aeD2 aeExtra, aeD2 = beta).
+   * term_kind NULL: every term is Hamiltonian.  Mixtures (up to 16 packets) and
+   * dissipation (up to 4 type-1 operators, state-diagonal terms) run on DVR models
+   * with the derivative-based integrators; CMF2 returns -1 for them. */
+  int64_t npackets;              /* npackets, 0 or 1 for a single wave packet            */
+  double eps_pop;                /* eps_pop (0: the reference's default 1e-6)            */
+  const int64_t *term_kind;      /* (nham) 0 Hamiltonian, 1 type-1, 2 type-2, or NULL    */
+  const int64_t *term_diss1;     /* (nham) type-1 operator of a kind-1 term (0-based)    */
+  int64_t ndiss1;                /* number of type-1 operators                           */
+  const double *diss1_ae;        /* aeD1(ndiss1)                                         */
 } mctdh_setup_t;
 
 /* Build the device context: uploads the operators, plans the batched kernels
@@ -168,6 +185,12 @@ int64_t mctdh_observables(mctdh_ctx_t *ctx, double t, double *energy, double *po
  *   errors ggp, poperr(ns00max, nmodgwp, nstates) (output.f90:88-140); ggp/poperr may be NULL;
  * - mctdh_densmat: the reduced density matrix rho(mode, state) as written to the densmat
  *   file (output.f90:276-300), n x n interleaved complex, both triangles filled. */
+/* Packet populations of the resident mixture as written by WriteOutput
+ * (output.f90:44-60): WPpop normalised to unit sum and sorted decreasing
+ * (npackets values), and the entropy -sum p ln p / ln npackets over p >= 1e-8
+ * (0 for a single packet). */
+int64_t mctdh_packets(mctdh_ctx_t *ctx, double *wppop, double *entropy);
+
 int64_t mctdh_expect(mctdh_ctx_t *ctx, double *values);
 int64_t mctdh_natpop(mctdh_ctx_t *ctx, double *natpop, double *ggp, double *poperr);
 int64_t mctdh_densmat(mctdh_ctx_t *ctx, int64_t mode, int64_t state, double *rho);

@@ -50,6 +50,8 @@ class Setup(C.Structure):
         ("int_order", C.c_int64), ("int_par1", C.c_int64),
         ("nexpect", C.c_int64), ("expect_nterms", I64P), ("expect_ae", DP), ("expect_lhs", I64P),
         ("expect_rhs", I64P), ("expect_ioper", I64P),
+        ("npackets", C.c_int64), ("eps_pop", C.c_double), ("term_kind", I64P), ("term_diss1", I64P),
+        ("ndiss1", C.c_int64), ("diss1_ae", DP),
     ]
 
 
@@ -78,6 +80,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_observables.argtypes = [vp, C.c_double, DP, DP, DP, DP, DP]
     lib.mctdh_norm_wf.argtypes = [vp, DP, DP, DP]
     lib.mctdh_expect.argtypes = [vp, DP]
+    lib.mctdh_packets.argtypes = [vp, DP, DP]
     lib.mctdh_natpop.argtypes = [vp, DP, DP, DP]
     lib.mctdh_densmat.argtypes = [vp, C.c_int64, C.c_int64, DP]
     lib.mctdh_density.argtypes = [vp, C.c_int64, DP, C.c_int64, C.c_double, C.c_double, DP, DP]
@@ -136,7 +139,7 @@ def load_library() -> C.CDLL:
                  "mctdh_rk_attempt", "mctdh_cmf2_attempt",
                  "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
                  "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_step",
-                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density",
+                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets",
                  "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
                  "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"):
         getattr(lib, name).restype = C.c_int64
@@ -148,7 +151,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_rk_attempt", "mctdh_cmf2_attempt",
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
-            "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density",
+            "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
@@ -219,9 +222,29 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
             oper[0, k, m] = l
             oper[1, k, m] = r
             oper[2:2 + len(dops), k, m] = dops
-    ae = np.empty(2 * model.nham)
-    ae[0::2] = model.ae.real
-    ae[1::2] = model.ae.imag
+    # dissipative terms follow the Hamiltonian's: kind 1 (aeExtra, its type-1
+    # operator), kind 2 (i aeD2 aeExtra)
+    kinds = [0] * model.nham
+    diss1_of = [-1] * model.nham
+    coeffs = list(model.ae)
+    lhs, rhs = list(model.lhs_el), list(model.rhs_el)
+    iop_cols, skip_cols = [model.ioper], [model.skip_term]
+    dissipation = getattr(model, "dissipation", [])
+    for ty in (1, 2):
+        for j, idx in enumerate(model.diss1 if ty == 1 else model.diss2):
+            for term in dissipation[idx][2]:
+                kinds.append(ty)
+                diss1_of.append(j if ty == 1 else -1)
+                coeffs.append(complex(term.coeff) if ty == 1 else 1j * model.aeD2[j] * complex(term.coeff))
+                lhs.append(term.lhs)
+                rhs.append(term.rhs)
+            iop_cols.append(model.ioper_diss[idx])
+            skip_cols.append(model.skip_diss[idx])
+    nterm = len(kinds)
+    coeffs = np.asarray(coeffs, dtype=np.complex128)
+    ae = np.empty(2 * nterm)
+    ae[0::2] = coeffs.real
+    ae[1::2] = coeffs.imag
     gwpa = getattr(model, "gwpa", None)
     if gwpa is None or gwpa.size == 0:
         gwpa = np.zeros(1)
@@ -231,7 +254,7 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
         g[:gwpa.shape[0], :gwpa.shape[1], :] = gwpa
         gwpa = g
     s = Setup()
-    s.nstates, s.nmodes, s.ndof, s.nham, s.maxdof = ns, nm, nd, model.nham, maxdof
+    s.nstates, s.nmodes, s.ndof, s.nham, s.maxdof = ns, nm, nd, nterm, maxdof
     s.nspf = I(model.nspf.reshape(-1, order="F"))
     s.nmodedof = I([len(d) for d in model.mode_dofs])
     s.idof = I(idof.reshape(-1, order="F"))
@@ -243,14 +266,14 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
     s.dvr_mats = F(mats)
     s.dvr_mat_off = I(mat_off)
     s.ae = F(ae)
-    s.lhs_el = I(model.lhs_el)
-    s.rhs_el = I(model.rhs_el)
+    s.lhs_el = I(lhs)
+    s.rhs_el = I(rhs)
     s.nopermax = model.nopermax
     s.noper = I([len(o) for o in model.oper])
     s.oper = I(oper.reshape(-1, order="F"))
-    s.ioper = I(model.ioper.reshape(-1, order="F"))
+    s.ioper = I(np.concatenate(iop_cols, axis=1).reshape(-1, order="F"))
     s.is_identity = I(model.is_identity.astype(np.int64).reshape(-1, order="F"))
-    s.skip_term = I(model.skip_term.astype(np.int64).reshape(-1, order="F"))
+    s.skip_term = I(np.concatenate(skip_cols, axis=1).astype(np.int64).reshape(-1, order="F"))
     s.ipsispf = I(model.ipsispf.reshape(-1, order="F"))
     s.dimpsi = model.dimpsi
     s.gwpa = F(np.asarray(gwpa).reshape(-1, order="F"))
@@ -275,6 +298,13 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
         s.expect_lhs = I([t.lhs for t in terms])
         s.expect_rhs = I([t.rhs for t in terms])
         s.expect_ioper = I(np.concatenate(model.ioper_expect, axis=1).reshape(-1, order="F"))
+    s.npackets = getattr(model, "npackets", 1)
+    s.eps_pop = getattr(model, "eps_pop", 1e-6)
+    if nterm > model.nham:
+        s.term_kind = I(kinds)
+        s.term_diss1 = I(diss1_of)
+        s.ndiss1 = len(model.diss1)
+        s.diss1_ae = F(model.aeD1 if model.aeD1 else [0.0])
     return s, keep
 
 
@@ -364,8 +394,16 @@ class GpuCore:
         A, psi = _cbuf(A), _cbuf(psi)
         self._check(self.lib.mctdh_set_state(self.h, _ptr(A), _ptr(psi), 1 if as_start else 0))
 
+    def packets(self):
+        """Packet populations (normalised, decreasing) and the entropy of the
+        resident mixture (output.f90:44-60)."""
+        w = np.empty(max(1, getattr(self.model, "npackets", 1)))
+        e = C.c_double()
+        self._check(self.lib.mctdh_packets(self.h, w.ctypes.data_as(DP), C.byref(e)))
+        return w, e.value
+
     def get_state(self):
-        A = np.empty(self.model.naconftot, dtype=np.complex128)
+        A = np.empty(self.model.naconftot * getattr(self.model, "npackets", 1), dtype=np.complex128)
         psi = np.empty(self.model.dimpsi, dtype=np.complex128)
         self._check(self.lib.mctdh_get_state(self.h, _ptr(A), _ptr(psi)))
         return A, psi

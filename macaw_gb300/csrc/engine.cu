@@ -235,7 +235,8 @@ struct OvlPlan {
   std::vector<ProdBatch> chain;  // one batch per mode step
   HoleBatch dots;
   RedBatch dot_red;
-  cplx* d_result = nullptr;      // [3] o11, o22, o12
+  cplx* d_result = nullptr;      // [3 npk] o11, o22, o12 per packet
+  int npk = 1;
 };
 
 struct DotPlan {
@@ -303,6 +304,41 @@ struct Ctx {
   std::vector<std::vector<std::vector<int>>> oper;  // [m][k] -> {l, r, codes...}
   std::vector<long long> naconf, aoff, ipsi;
   long long naconftot = 0, dimpsi = 0, ntot = 0;
+  // statistical mixture: npk packets stored packet-minor per state (state s holds
+  // naconf[s] = npk * n1[s] coefficients, packet W at aoff[s] + W * n1[s]); the
+  // host arrays are packet-major (APacketOffset(W) = W * nAConftot, aoff1)
+  int npk = 1;
+  double eps_pop = 1e-6;
+  std::vector<long long> n1, aoff1;
+  long long n1tot = 0;
+  // term kinds: 0 Hamiltonian, 1 type-1 dissipative (operator diss1_of[t]), 2 type-2
+  std::vector<int> kind, diss1_of;
+  int ndiss1 = 0, ndiss2_terms = 0;
+  std::vector<double> aeD1;
+  bool mixture = false;       // several packets or dissipation: derivative-based integrators only
+  bool skip_mult = false;     // observables: the EOM without the Lagrange multipliers
+  // packet stage (plan_packets)
+  struct SumPlan {
+    SumRange* ranges = nullptr;
+    SumSrc* srcs = nullptr;
+    int n = 0, nsrc = 0;
+  };
+  SumPlan pk_sum2;                      // X A (type-2 terms)
+  std::vector<SumPlan> pk_sum1;         // V_k A per type-1 operator
+  cplx *pk_xa = nullptr, *pk_va = nullptr, *pk_aux = nullptr, *pk_vmix = nullptr;
+  PkState* pk_st = nullptr;
+  PkGramPair* pk_pairs = nullptr;
+  int pk_npairs = 0, pk_nmix = 0;
+  cplx* pk_partial = nullptr;
+  cplx* pk_coef_buf = nullptr;
+  PkCoefArgs pk_args;
+  PkMix* pk_mix = nullptr;
+  std::vector<PkMix> pk_mult_h;
+  PkMix* pk_mult = nullptr;
+  cplx* pk_mult_out = nullptr;          // output the uploaded multiplier descriptor points at
+  std::vector<ProdBatch> aux_chains;    // right chains on AuxA_k (type-1 mean fields)
+  HoleBatch aux_holes;
+  RedBatch aux_red;
   std::vector<int> modes_dvr;
   std::vector<int> gmode;  // grid size G of DVR modes
   double eps_rho = 1e-8, eps_ovl = 1e-8, eps_C = 1e-8, eps_int = 1e-8, eps_A = 1e-8, eps_psi = 1e-8;
@@ -445,9 +481,11 @@ struct Ctx {
     if (st2) cudaStreamDestroy(st2);
   }
   int m_of(int m, int s) const { return nspf[m + nmodes * s]; }
+  // tensor shape of state s; a mixture adds the packet index as the slowest dimension
   std::vector<int> shape_of(int s) const {
     std::vector<int> v(nmodes);
     for (int m = 0; m < nmodes; ++m) v[m] = m_of(m, s);
+    if (npk > 1) v.push_back(npk);
     return v;
   }
   void count(int n = 1) { launches += n; }
@@ -546,15 +584,46 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
       }
     }
   }
+  // statistical mixtures and dissipation (input.f90:156, 216-229, 262, 596-616)
+  c.npk = s->npackets > 1 ? (int)s->npackets : 1;
+  if (c.npk > MAX_PACKETS) throw StatusError(MCTDH_EUNSUPPORTED, "more than 16 wave packets");
+  c.eps_pop = s->eps_pop > 0.0 ? s->eps_pop : 1e-6;
+  c.kind.assign(c.nham, 0);
+  c.diss1_of.assign(c.nham, -1);
+  c.ndiss1 = s->term_kind ? (int)s->ndiss1 : 0;
+  if (c.ndiss1 < 0 || c.ndiss1 > MAX_DISS1) throw StatusError(MCTDH_EUNSUPPORTED, "0..4 type-1 dissipative operators");
+  if (c.ndiss1 > 0 && !s->diss1_ae) throw StatusError(MCTDH_EARG, "type-1 operators need diss1_ae");
+  for (int k = 0; k < c.ndiss1; ++k) c.aeD1.push_back(s->diss1_ae[k]);
+  if (s->term_kind) {
+    for (int t = 0; t < c.nham; ++t) {
+      const int kd = (int)s->term_kind[t];
+      if (kd < 0 || kd > 2) throw StatusError(MCTDH_EARG, "term_kind outside 0..2");
+      c.kind[t] = kd;
+      if (kd == 2) ++c.ndiss2_terms;
+      if (kd == 1) {
+        const int k = s->term_diss1 ? (int)s->term_diss1[t] : -1;
+        if (k < 0 || k >= c.ndiss1) throw StatusError(MCTDH_EARG, "term_diss1 out of range");
+        if (c.lhs[t] != c.rhs[t])
+          throw StatusError(MCTDH_EUNSUPPORTED, "type-1 dissipative terms must act within one electronic state");
+        c.diss1_of[t] = k;
+      }
+    }
+  }
+  c.mixture = c.npk > 1 || c.ndiss1 > 0 || c.ndiss2_terms > 0;
   c.naconf.resize(c.nstates);
   c.aoff.resize(c.nstates);
+  c.n1.resize(c.nstates);
+  c.aoff1.resize(c.nstates);
   long long off = 0;
   for (int st = 0; st < c.nstates; ++st) {
     long long n = 1;
     for (int m = 0; m < c.nmodes; ++m) n *= c.m_of(m, st);
-    c.naconf[st] = n;
+    c.n1[st] = n;
+    c.aoff1[st] = c.n1tot;
+    c.n1tot += n;
+    c.naconf[st] = n * c.npk;
     c.aoff[st] = off;
-    off += n;
+    off += n * c.npk;
   }
   c.naconftot = off;
   c.dimpsi = s->dimpsi;
@@ -574,6 +643,8 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
     for (int d : c.mode_dofs[m]) G *= c.ngp[d];
     c.gmode[m] = G;
   }
+  if (c.mixture && !c.modes_gwp.empty())
+    throw StatusError(MCTDH_EUNSUPPORTED, "mixtures and dissipation need DVR modes only");
   c.eps_rho = s->eps_rho;
   c.eps_ovl = s->eps_ovl;
   c.eps_C = s->eps_C;
@@ -756,8 +827,121 @@ const cplx* plan_s_weighted(Ctx& c, int s, int skip) {
 // ---------------------------------------------------------------------------
 void plan_gwp_derivs(Ctx& c);
 
+// type-1 mean-field contribution: contraction of L_im(A) with the right chain on AuxA
+struct AuxRef {
+  int hole, im, k;
+  cplx ae;
+};
+
+// Statistical mixtures and dissipation (gmctdh_objects.f90:606-845, 1128-1137;
+// derivatives.f90:70-83, 238-242).  After the mean-field reduction of every EOM:
+//   X A = sum_t f i aeD2 ae_t W_t A (type-2 terms)   and   V_k A = sum_t ae_t V_t A,
+//   the packet norms, G = <A_i|X A_j> and <A_i|V_k A_j> (pk_gram), the populations,
+//   multipliers and mixing matrices (pk_coef), D = sum_k V_k A C1_k and
+//   AuxA_k = A C2_k (pk_mix), the right chains on AuxA_k and their contractions with
+//   the left chains on A, added to the mean fields.  D and X A join the term sum of
+//   dA; the multipliers dA += A (multLagDiag I + i multLag) close the EOM.
+void plan_packets(Ctx& c, std::vector<std::vector<SumSrc>>& srcs, std::vector<std::vector<SumSrc>>& srcs2,
+                  std::vector<std::vector<std::vector<SumSrc>>>& srcs1,
+                  const std::map<std::pair<int, int>, int>& mf_target, const std::vector<AuxRef>& arefs) {
+  const int P = c.npk;
+  const bool has2 = c.ndiss2_terms > 0;
+  std::vector<PkState> st(c.nstates);
+  for (int s = 0; s < c.nstates; ++s) st[s] = PkState{c.aoff[s], c.n1[s]};
+  c.pk_st = upload_vec(c.ar, st);
+  auto sum_plan = [&](std::vector<std::vector<SumSrc>>& v, Ctx::SumPlan& sp) {
+    std::vector<SumRange> rr;
+    std::vector<SumSrc> ss;
+    for (int s = 0; s < c.nstates; ++s) {
+      SumRange r;
+      r.offset = c.aoff[s];
+      r.n = c.naconf[s];
+      r.first = (int)ss.size();
+      r.count = (int)v[s].size();
+      for (auto& x : v[s]) ss.push_back(x);
+      rr.push_back(r);
+    }
+    split_coeffs(ss);
+    sp.n = (int)rr.size();
+    sp.nsrc = (int)ss.size();
+    sp.ranges = upload_vec(c.ar, rr);
+    sp.srcs = upload_vec(c.ar, ss);
+  };
+  std::vector<PkGramPair> pairs;
+  for (int w = 0; w < P; ++w) pairs.push_back(PkGramPair{c.d_in, c.d_in, w, w});
+  if (has2) {
+    c.pk_xa = c.ar.calloc_c(c.naconftot);
+    sum_plan(srcs2, c.pk_sum2);
+    for (int j = 0; j < P; ++j)
+      for (int i = 0; i < P; ++i) pairs.push_back(PkGramPair{c.d_in, c.pk_xa, i, j});
+    for (int s = 0; s < c.nstates; ++s) srcs[s].push_back(SumSrc{c.pk_xa + c.aoff[s], mkc(1, 0)});
+  }
+  c.pk_sum1.resize(c.ndiss1);
+  for (int k = 0; k < c.ndiss1; ++k) {
+    sum_plan(srcs1[k], c.pk_sum1[k]);
+    for (int j = 0; j < P; ++j)
+      for (int i = 0; i < P; ++i) pairs.push_back(PkGramPair{c.d_in, c.pk_va + (long long)k * c.naconftot, i, j});
+  }
+  c.pk_npairs = (int)pairs.size();
+  c.pk_pairs = upload_vec(c.ar, pairs);
+  c.pk_partial = c.ar.calloc_c((long long)c.pk_npairs * PK_GRAM_BLOCKS);
+  c.pk_coef_buf = c.ar.calloc_c((long long)(2 * c.ndiss1 + 1) * P * P + P);
+  PkCoefArgs& a = c.pk_args;
+  memset(&a, 0, sizeof(a));
+  a.P = P;
+  a.ndiss1 = c.ndiss1;
+  a.has2 = has2;
+  a.npairs = c.pk_npairs;
+  a.eps_pop = c.eps_pop;
+  for (int k = 0; k < c.ndiss1; ++k) a.aeD1[k] = c.aeD1[k];
+  a.partial = c.pk_partial;
+  a.C1 = c.pk_coef_buf;
+  a.C2 = c.pk_coef_buf + (long long)c.ndiss1 * P * P;
+  a.ML = c.pk_coef_buf + (long long)2 * c.ndiss1 * P * P;
+  a.pop = reinterpret_cast<double*>(a.ML + P * P);
+  std::vector<PkMix> mix;
+  if (c.ndiss1 > 0) {
+    c.pk_vmix = c.ar.calloc_c(c.naconftot);
+    for (int k = 0; k < c.ndiss1; ++k)
+      mix.push_back(PkMix{c.pk_va + (long long)k * c.naconftot, a.C1 + (long long)k * P * P, c.pk_vmix, k > 0});
+    for (int k = 0; k < c.ndiss1; ++k)
+      mix.push_back(PkMix{c.d_in, a.C2 + (long long)k * P * P, c.pk_aux + (long long)k * c.naconftot, 0});
+    for (int s = 0; s < c.nstates; ++s) srcs[s].push_back(SumSrc{c.pk_vmix + c.aoff[s], mkc(1, 0)});
+  }
+  c.pk_nmix = (int)mix.size();
+  if (!mix.empty()) c.pk_mix = upload_vec(c.ar, mix);
+  // type-1 mean fields: added to the reduction's targets, or written where no other
+  // term has a mean field for the operator
+  for (auto& b : c.aux_chains) {
+    b.prec = c.precision;
+    b.finalize(c.ar);
+  }
+  c.aux_holes.prec = c.precision ? 2 : 0;
+  c.aux_holes.finalize(c.ar);
+  std::map<std::pair<int, int>, int> tg;
+  for (const AuxRef& r : arefs) {
+    const auto key = std::make_pair(r.im, r.k);
+    if (!tg.count(key)) {
+      const int l = c.oper[r.im][r.k][0], rr = c.oper[r.im][r.k][1];
+      const int n1 = c.m_of(r.im, l), n2 = c.m_of(r.im, rr);
+      tg[key] = c.aux_red.add_target(c.mf[r.im][r.k], n1, n2, n1, 0, mf_target.count(key) ? 1 : 0);
+    }
+    c.aux_red.add_term(tg[key], c.aux_holes.h[r.hole], r.ae);
+  }
+  c.aux_red.finalize(c.ar);
+  if (P > 1) {
+    std::vector<PkMix> mult{PkMix{c.d_in, a.ML, nullptr, 1}};   // output set at run time
+    c.pk_mult_h = mult;
+    c.pk_mult = upload_vec(c.ar, mult);
+  }
+}
+
 void plan_eom(Ctx& c) {
   const int f = c.nmodes;
+  if (c.mixture) {
+    c.pk_va = c.ndiss1 ? c.ar.calloc_c((long long)c.ndiss1 * c.naconftot) : nullptr;
+    c.pk_aux = c.ndiss1 ? c.ar.calloc_c((long long)c.ndiss1 * c.naconftot) : nullptr;
+  }
   const int nsm = MAXN_SPF;
   (void)nsm;
   c.hmat.assign(f, {});
@@ -856,7 +1040,7 @@ void plan_eom(Ctx& c) {
         Y = weighted[key];
       }
       int hidx = c.rho_holes.add(c.ar, Y, c.d_in + c.aoff[s], prod_range(sh, 0, m),
-                                 prod_range(sh, m + 1, f), n, n);
+                                 prod_range(sh, m + 1, (int)sh.size()), n, n);
       rho_hole[m][s] = hidx;
       int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
       rrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
@@ -894,8 +1078,17 @@ void plan_eom(Ctx& c) {
     }
     return mf_target[key];
   };
-  std::vector<cplx> c0(c.nstates, mkc(0, 0));
-  std::map<std::pair<int, int>, std::vector<MatSumSrc>> gsum;  // (s, m) -> sum_t ae_t h_t
+  // per term kind: 0 Hamiltonian (dA), 2 type-2 dissipation (its own sum X A, needed
+  // alone for the Lagrange multipliers)
+  std::vector<cplx> c0k[3] = {std::vector<cplx>(c.nstates, mkc(0, 0)), {}, std::vector<cplx>(c.nstates, mkc(0, 0))};
+  std::vector<cplx>& c0 = c0k[0];
+  std::map<std::pair<int, int>, std::vector<MatSumSrc>> gsumk[3];  // (s, m) -> sum_t ae_t h_t
+  std::vector<std::vector<SumSrc>> srcs2(c.nstates);
+  std::vector<std::vector<std::vector<SumSrc>>> srcs1(c.ndiss1, std::vector<std::vector<SumSrc>>(c.nstates));
+  auto srcs_of = [&](int t) -> std::vector<std::vector<SumSrc>>& {
+    return c.kind[t] == 2 ? srcs2 : (c.kind[t] == 1 ? srcs1[c.diss1_of[t]] : srcs);
+  };
+  std::vector<AuxRef> arefs;
   c.term_single.assign(c.nham, -2);
   // Hermitian-conjugate partners among the cross-state terms: t2 acts from s2 to s1
   // with the same primitive operators as t1 on every mode and the conjugate
@@ -911,13 +1104,14 @@ void plan_eom(Ctx& c) {
       int nact = 0, mact = -1;
       for (int m = 0; m < f; ++m)
         if (!c.skip_term[m + f * t]) { ++nact; mact = m; }
-      is_general[t] = !(c.lhs[t] == c.rhs[t] && nact <= 1 && (mact < 0 || !c.is_gwp[mact]));
+      is_general[t] = c.kind[t] == 1 || !(c.lhs[t] == c.rhs[t] && nact <= 1 && (mact < 0 || !c.is_gwp[mact]));
     }
     std::vector<char> taken(c.nham, 0);
     for (int t2 = 0; t2 < c.nham; ++t2) {
       if (!is_general[t2] || c.lhs[t2] == c.rhs[t2]) continue;
       for (int t1 = 0; t1 < t2; ++t1) {
         if (!is_general[t1] || taken[t1] || leader_of[t1] >= 0) continue;
+        if (c.kind[t1] != c.kind[t2] || c.kind[t1] == 1) continue;
         if (c.lhs[t1] != c.rhs[t2] || c.rhs[t1] != c.lhs[t2]) continue;
         const cplx a1 = c.ae[t1], a2 = c.ae[t2];
         const double da = hypot(a2.x - a1.x, a2.y + a1.y), ma = hypot(a1.x, a1.y);
@@ -943,14 +1137,14 @@ void plan_eom(Ctx& c) {
     int nact = 0, mact = -1;
     for (int m = 0; m < f; ++m)
       if (!c.skip_term[m + f * t]) { ++nact; mact = m; }
-    if (s1 == s2 && nact <= 1 && (mact < 0 || !c.is_gwp[mact])) {
-      c.term_single[t] = mact;
+    if (c.kind[t] != 1 && s1 == s2 && nact <= 1 && (mact < 0 || !c.is_gwp[mact])) {
+      c.term_single[t] = c.kind[t] == 0 ? mact : -2;
       if (mact < 0) {
-        c0[s1] = cadd(c0[s1], c.ae[t]);
+        c0k[c.kind[t]][s1] = cadd(c0k[c.kind[t]][s1], c.ae[t]);
         continue;
       }
       const int k = c.ioper[mact + f * t];
-      gsum[std::make_pair(s1, mact)].push_back(MatSumSrc{c.hmat[mact][k], c.ae[t]});
+      gsumk[c.kind[t]][std::make_pair(s1, mact)].push_back(MatSumSrc{c.hmat[mact][k], c.ae[t]});
       if (!c.is_identity[mact + f * k]) rrefs.push_back(HoleRef{rho_hole[mact][s1], mf_tg(mact, k), c.ae[t]});
       continue;
     }
@@ -958,7 +1152,9 @@ void plan_eom(Ctx& c) {
     // last mode whose mean field is needed (an adjoint partner has neither left
     // chain nor contractions, and its right chain serves dA only)
     const int leader = leader_of[t];
-    std::vector<ProdBatch>& rchains = leader >= 0 ? c.chains_full : c.chains;
+    // type-1 terms: the right chain on A serves V A only (gmctdh_objects.f90:628-649);
+    // their mean fields contract the left chain with a right chain on AuxA (below)
+    std::vector<ProdBatch>& rchains = (leader >= 0 || c.kind[t] == 1) ? c.chains_full : c.chains;
     int lmax = 0;
     for (int im = 0; im < f; ++im)
       if (!c.is_identity[im + f * c.ioper[im + f * t]]) lmax = im;
@@ -973,7 +1169,7 @@ void plan_eom(Ctx& c) {
       const int n1 = c.m_of(jm, s1);
       std::vector<int> ns = R[i - 1].shape;
       ns[jm] = n1;
-      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+      cplx* out = c.ar.calloc_c(prod_range(ns, 0, (int)ns.size()));
       const auto in = prod_in(R[i - 1], s2);
       rchains[i].add(in.first, out, c.hmat[jm][k], n1, 0, R[i - 1].shape, jm, n1, mkc(1, 0), 0, in.second,
                      chain_fmt);
@@ -990,7 +1186,7 @@ void plan_eom(Ctx& c) {
       const int n1 = c.m_of(im, s1), n2 = c.m_of(im, s2);
       std::vector<int> ns = L[i - 1].shape;
       ns[im] = n2;
-      cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+      cplx* out = c.ar.calloc_c(prod_range(ns, 0, (int)ns.size()));
       const auto in = prod_in(L[i - 1], s1);
       c.chains[i].add(in.first, out, c.hmat[im][k], n1, 1, L[i - 1].shape, im, n2, mkc(1, 0), 0, in.second,
                       chain_fmt);
@@ -998,7 +1194,43 @@ void plan_eom(Ctx& c) {
       L[i].shape = ns;
       L[i].fmt = chain_fmt;
     }
-    srcs[s1].push_back(SumSrc{R[f].p, cmul(c.der, c.ae[t]), R[f].fmt});
+    if (c.kind[t] == 1) {
+      // V_k A = sum_t ae_t V_t A (no der_factor) and the mean fields
+      // ae_t <A| V_t^(not im) AuxA_k> (gmctdh_objects.f90:694-744, every h1mode of a
+      // same-state term being Hermitian)
+      const int k1 = c.diss1_of[t];
+      srcs1[k1][s1].push_back(SumSrc{R[f].p, c.ae[t], R[f].fmt});
+      int imin = f;
+      for (int im = 0; im < f; ++im)
+        if (!c.is_identity[im + f * c.ioper[im + f * t]]) imin = std::min(imin, im);
+      std::vector<TRef> Q(f);
+      Q[0].p = c.pk_aux + (long long)k1 * c.naconftot + c.aoff[s2];
+      Q[0].shape = c.shape_of(s2);
+      for (int i = 1; i <= f - 1 - imin; ++i) {
+        const int jm = f - i;
+        if (c.skip_term[jm + f * t]) { Q[i] = Q[i - 1]; continue; }
+        const int k = c.ioper[jm + f * t];
+        std::vector<int> ns = Q[i - 1].shape;
+        cplx* out = c.ar.calloc_c(prod_range(ns, 0, (int)ns.size()));
+        if ((int)c.aux_chains.size() <= i) c.aux_chains.resize(i + 1);
+        c.aux_chains[i].add(Q[i - 1].p, out, c.hmat[jm][k], ns[jm], 0, Q[i - 1].shape, jm, ns[jm], mkc(1, 0), 0,
+                            Q[i - 1].fmt, chain_fmt);
+        Q[i].p = out;
+        Q[i].shape = ns;
+        Q[i].fmt = chain_fmt;
+      }
+      for (int im = 0; im < f; ++im) {
+        const int k = c.ioper[im + f * t];
+        if (c.is_identity[im + f * k]) continue;
+        const TRef& X = L[im];
+        const TRef& Y = Q[f - 1 - im];
+        long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, (int)X.shape.size());
+        int hidx = c.aux_holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im], X.fmt, Y.fmt);
+        arefs.push_back(AuxRef{hidx, im, k, c.ae[t]});
+      }
+      continue;
+    }
+    srcs_of(t)[s1].push_back(SumSrc{R[f].p, cmul(c.der, c.ae[t]), R[f].fmt});
     c.general_terms.push_back(t);
     for (int im = 0; im < f; ++im) {
       const int k = c.ioper[im + f * t];
@@ -1009,14 +1241,15 @@ void plan_eom(Ctx& c) {
       }
       const TRef& X = L[im];
       const TRef& Y = R[f - 1 - im];
-      long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, f);
+      long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, (int)X.shape.size());
       int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im], X.fmt, Y.fmt);
       term_hole[std::make_pair(t, im)] = hidx;
       hrefs.push_back(HoleRef{hidx, mf_tg(im, k), c.ae[t]});
     }
   }
   // pre-summed single-mode operators and their products with A
-  for (auto& kv : gsum) {
+  for (int kd : {0, 2})
+  for (auto& kv : gsumk[kd]) {
     const int s = kv.first.first, m = kv.first.second;
     const int n = c.m_of(m, s);
     MatSumDesc md;
@@ -1029,16 +1262,21 @@ void plan_eom(Ctx& c) {
     c.msum_h.push_back(md);
     c.gmat[kv.first] = md.out;
     std::vector<int> sh = c.shape_of(s);
-    cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
+    cplx* out = c.ar.calloc_c(prod_range(sh, 0, (int)sh.size()));
     const int gfmt = c.precision == 1 ? TF_F32 : chain_fmt;   // FP32 products in precision 1
     TRef root;
     root.p = c.d_in + c.aoff[s];
     const auto in = prod_in(root, s);
     c.gprods.add(in.first, out, md.out, n, 0, sh, m, n, mkc(1, 0), 0, in.second, gfmt);
-    srcs[s].push_back(SumSrc{out, c.der, gfmt});
+    (kd == 2 ? srcs2 : srcs)[s].push_back(SumSrc{out, c.der, gfmt});
   }
-  for (int s = 0; s < c.nstates; ++s)
+  for (int s = 0; s < c.nstates; ++s) {
     if (c0[s].x != 0.0 || c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_in + c.aoff[s], cmul(c.der, c0[s])});
+    const cplx c2 = c0k[2][s];
+    if (c2.x != 0.0 || c2.y != 0.0) srcs2[s].push_back(SumSrc{c.d_in + c.aoff[s], cmul(c.der, c2)});
+  }
+  // without dissipation the multipliers vanish and the packets need no extra stage
+  if (c.ndiss1 > 0 || c.ndiss2_terms > 0) plan_packets(c, srcs, srcs2, srcs1, mf_target, arefs);
   c.c0 = c0;
   c.msum_d = upload_vec(c.ar, c.msum_h);
   c.msum_src_d = upload_vec(c.ar, c.msum_src_h);
@@ -1311,7 +1549,7 @@ void plan_hb(Ctx& c) {
         Node nd;
         nd.ref.shape = nodes[cur].ref.shape;
         nd.ref.shape[m] = n1;
-        nd.ref.p = c.ar.calloc_c(prod_range(nd.ref.shape, 0, f));
+        nd.ref.p = c.ar.calloc_c(prod_range(nd.ref.shape, 0, (int)nd.ref.shape.size()));
         nd.ref.fmt = chain_fmt;
         nd.depth = nodes[cur].depth + 1;
         c.hb_chains[nd.depth].add(nodes[cur].ref.p, nd.ref.p, mat, n1, 0, nodes[cur].ref.shape, m, n1, mkc(1, 0), 0,
@@ -1327,7 +1565,7 @@ void plan_hb(Ctx& c) {
     const int s = kv.first.first, m = kv.first.second;
     const int n = c.m_of(m, s);
     std::vector<int> sh = c.shape_of(s);
-    cplx* out = c.ar.calloc_c(prod_range(sh, 0, f));
+    cplx* out = c.ar.calloc_c(prod_range(sh, 0, (int)sh.size()));
     c.hb_chains[1].add(hb_in_at(s), out, kv.second, n, 0, sh, m, n, mkc(1, 0), 0, hb_in_fmt, chain_fmt);
     srcs[s].push_back(SumSrc{out, mkc(1, 0), chain_fmt});
   }
@@ -1359,7 +1597,8 @@ void plan_hb(Ctx& c) {
 // is of order eps_int^2 / 2 >> 1e-13.  Norms and C(t) keep prec 0.
 void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
   const int f = c.nmodes;
-  P.d_result = c.ar.calloc_c(3);
+  P.npk = c.npk;
+  P.d_result = c.ar.calloc_c(3 * c.npk);
   struct Smat { cplx* s11; cplx* s22; cplx* s12; };
   std::vector<std::vector<Smat>> S(f, std::vector<Smat>(c.nstates));
   std::vector<HoleRef> hrefs;
@@ -1426,9 +1665,9 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
   order.insert(order.end(), c.modes_gwp.begin(), c.modes_gwp.end());
   P.chain.assign(order.size() + 1, ProdBatch());
   std::vector<HoleRef> drefs;
-  int t11 = P.dot_red.add_target(P.d_result + 0, 1, 1, 1, 0);
-  int t22 = P.dot_red.add_target(P.d_result + 1, 1, 1, 1, 0);
-  int t12 = P.dot_red.add_target(P.d_result + 2, 1, 1, 1, 0);
+  // per packet W: results 3W + {0, 1, 2}
+  std::vector<int> tgt(3 * c.npk);
+  for (int q = 0; q < 3 * c.npk; ++q) tgt[q] = P.dot_red.add_target(P.d_result + q, 1, 1, 1, 0);
   for (int s = 0; s < c.nstates; ++s) {
     std::vector<int> sh = c.shape_of(s);
     const long long N = c.naconf[s];
@@ -1448,9 +1687,16 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
         curfmt[q] = cfmt;
       }
     }
-    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[0], N, 1, 1, 1, TF_C64, curfmt[0]), t11, mkc(1, 0)});
-    drefs.push_back(HoleRef{P.dots.add(c.ar, a2, cur[1], N, 1, 1, 1, TF_C64, curfmt[1]), t22, mkc(1, 0)});
-    drefs.push_back(HoleRef{P.dots.add(c.ar, a1, cur[2], N, 1, 1, 1, TF_C64, curfmt[2]), t12, mkc(1, 0)});
+    const long long n1 = c.n1[s];
+    for (int w = 0; w < c.npk; ++w) {
+      const long long o = n1 * w;
+      drefs.push_back(HoleRef{P.dots.add(c.ar, a1 + o, cur[0] + o, n1, 1, 1, 1, TF_C64, curfmt[0]), tgt[3 * w],
+                              mkc(1, 0)});
+      drefs.push_back(HoleRef{P.dots.add(c.ar, a2 + o, cur[1] + o, n1, 1, 1, 1, TF_C64, curfmt[1]), tgt[3 * w + 1],
+                              mkc(1, 0)});
+      drefs.push_back(HoleRef{P.dots.add(c.ar, a1 + o, cur[2] + o, n1, 1, 1, 1, TF_C64, curfmt[2]), tgt[3 * w + 2],
+                              mkc(1, 0)});
+    }
   }
   for (auto& b : P.chain) {
     b.prec = prec;
@@ -1629,6 +1875,30 @@ void run_reginv(Ctx& c) {
   c.count();
 }
 
+// The packet stage of the EOM (plan_packets).
+void run_packets(Ctx& c) {
+  ProfScope ps(c, KP_TERMSUM);
+  if (c.pk_sum2.n) {
+    launch_termsum(c.pk_xa, c.pk_sum2.ranges, c.pk_sum2.n, c.pk_sum2.srcs, c.naconftot, c.st, c.precision);
+    c.count();
+  }
+  for (int k = 0; k < c.ndiss1; ++k) {
+    const Ctx::SumPlan& sp = c.pk_sum1[k];
+    launch_termsum(c.pk_va + (long long)k * c.naconftot, sp.ranges, sp.n, sp.srcs, c.naconftot, c.st, c.precision);
+    c.count();
+  }
+  launch_pk_gram(c.pk_pairs, c.pk_npairs, c.pk_st, c.nstates, c.pk_partial, c.st);
+  launch_pk_coef(c.pk_args, c.st);
+  c.count(2);
+  if (c.pk_nmix) {
+    launch_pk_mix(c.pk_mix, c.pk_nmix, c.pk_st, c.nstates, c.n1tot, c.npk, nullptr, c.st);
+    c.count();
+  }
+  for (auto& b : c.aux_chains) run_prod(c, b);
+  run_hole(c, c.aux_holes);
+  run_red(c, c.aux_red);
+}
+
 void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   const bool gwp = !c.modes_gwp.empty();
   if (gwp) gwp_setup_run(c);
@@ -1652,6 +1922,7 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   run_hole(c, c.rho_holes);
   run_hole(c, c.holes);
   run_red(c, c.red);
+  if (c.pk_pairs) run_packets(c);
   if (reginv || !mf_only) run_reginv(c);
   if (mf_only) {
     c.eom_count++;
@@ -1668,6 +1939,11 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
     c.count(3);
   }
   if (gwp) gwp_derivs_run(c, out);
+  // Lagrange multipliers: dA += A (multLagDiag I + i multLag) (derivatives.f90:238-242)
+  if (c.pk_mult && !c.skip_mult) {
+    launch_pk_mix(c.pk_mult, 1, c.pk_st, c.nstates, c.n1tot, c.npk, out, c.st);
+    c.count();
+  }
   c.eom_count++;
 }
 
@@ -1700,9 +1976,31 @@ void check_status(Ctx& c) {
   }
 }
 
+// o11, o22, o12 summed over the packets (trace_wf, the autocorrelation of output.f90:143-149)
 void read_ovl(Ctx& c, OvlPlan& P, cplx out[3]) {
-  CK(cudaMemcpyAsync(out, P.d_result, sizeof(cplx) * 3, cudaMemcpyDeviceToHost, c.st));
+  std::vector<cplx> v(3 * P.npk);
+  CK(cudaMemcpyAsync(v.data(), P.d_result, sizeof(cplx) * v.size(), cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
+  for (int q = 0; q < 3; ++q) {
+    out[q] = mkc(0, 0);
+    for (int w = 0; w < P.npk; ++w) out[q] = cadd(out[q], v[3 * w + q]);
+  }
+}
+
+// DeltaPsi (gmctdh_objects.f90:206-248): sqrt|2 (1 - Re o12 / sqrt(o11 o22))| for one
+// packet; sqrt(2 sum_W |sqrt(o11 o22) - Re o12| / sum_W sqrt(o11 o22)) for a mixture.
+double ovl_delta(Ctx& c, OvlPlan& P) {
+  std::vector<cplx> v(3 * P.npk);
+  CK(cudaMemcpyAsync(v.data(), P.d_result, sizeof(cplx) * v.size(), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  if (P.npk == 1) return sqrt(fabs(2.0 * (1.0 - v[2].x / sqrt(v[0].x * v[1].x))));
+  double num = 0.0, pop = 0.0;
+  for (int w = 0; w < P.npk; ++w) {
+    const double d = sqrt(v[3 * w].x * v[3 * w + 1].x);
+    pop += d;
+    num += fabs(d - v[3 * w + 2].x);
+  }
+  return sqrt(2.0 * num / pop);
 }
 
 // Cash-Karp and Dormand-Prince tableaux (integrator.f90:107-121, :171-185)
@@ -1766,11 +2064,8 @@ double rk_attempt(Ctx& c, double t, double dt, int method) {
     }
     run_ovl(c, c.dpsi_plan);
   });
-  cplx o[3];
-  read_ovl(c, c.dpsi_plan, o);
+  const double delta = ovl_delta(c, c.dpsi_plan);
   check_status(c);
-  double o11 = o[0].x, o22 = o[1].x, o12 = o[2].x;
-  double delta = sqrt(fabs(2.0 * (1.0 - o12 / sqrt(o11 * o22))));
   if (!std::isfinite(delta)) throw StatusError(MCTDH_ENONFINITE, "non-finite RK error estimate");
   return delta / c.eps_int;
 }
@@ -1926,10 +2221,8 @@ void adams_step(Ctx& c, double t, double htry, double* hdid, double* hnext, long
       adams_axpy(c, c.ad_new1, c.ad_temp, c.ad_d1, x2[0]);
     }
     run_ovl(c, c.ad_plan);
-    cplx o[3];
-    read_ovl(c, c.ad_plan, o);
+    errmax = ovl_delta(c, c.ad_plan) / c.eps_int;
     check_status(c);
-    errmax = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x)))) / c.eps_int;
     if (!std::isfinite(errmax)) throw StatusError(MCTDH_ENONFINITE, "non-finite Adams error estimate");
     if (errmax < 1.0) break;
     dt = std::max(minscal * dt, safety * dt * pow(errmax, pow_shrink));
@@ -2074,10 +2367,8 @@ void bsstep(Ctx& c, double t, double htry, double* hdid, double* hnext) {
       bs_pzextr(c, k, test);
       if (k != 1) {
         run_ovl(c, c.bs_plan);
-        cplx o[3];
-        read_ovl(c, c.bs_plan, o);
+        errmax = ovl_delta(c, c.bs_plan) / c.eps_int;
         check_status(c);
-        errmax = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x)))) / c.eps_int;
         if (!std::isfinite(errmax)) throw StatusError(MCTDH_ENONFINITE, "non-finite Bulirsch-Stoer error estimate");
         error[k - 1] = pow(errmax / BS_SAFE1, 1.0 / (double)(2 * k - 1));
       }
@@ -2929,6 +3220,8 @@ void mfx_predict(Ctx& c, MfxState& M, double h) {
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
 // ops_fresh: the operators and mean fields at d_y are already in place.
 double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh, bool reginv_done) {
+  if (c.mixture)
+    throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 covers a single wave packet without dissipation (use rk45, dopri, abm or bs)");
   CmfState& S = cmf_state(c);
   const long long nA = c.naconftot;
   // With a second stream the regularised inverse of rho and the SPF half step
@@ -3062,6 +3355,8 @@ void cmf2_accept(Ctx& c, double hdid) {
 }
 
 void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, long long* tries) {
+  if (c.mixture)
+    throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 covers a single wave packet without dissipation (use rk45, dopri, abm or bs)");
   MfxState* M = nullptr;
   auto it = g_mfx.find(&c);
   if (it != g_mfx.end()) M = it->second;
@@ -3173,6 +3468,7 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     }
     load_setup(*c, s);
+    if (mb && c->mixture) throw StatusError(MCTDH_EUNSUPPORTED, "ensemble members are single wave packets without dissipation");
     c->d_status = (int*)c->ar.alloc(64);
     CK(cudaMemset(c->d_status, 0, 64));
     if (mb) {
@@ -3200,8 +3496,9 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       CK(cudaMemcpy(c->d_off1, offs, sizeof(offs), cudaMemcpyHostToDevice));
     }
     plan_eom(*c);
-    if (!mb) {
-      // CMF2 / Lanczos buffers (ensemble members integrate with RK only)
+    if (!mb && !c->mixture) {
+      // CMF2 / Lanczos buffers (ensemble members, mixtures and dissipation integrate
+      // with the derivative-based integrators only)
       c->d_hbin = c->ar.calloc_c(c->naconftot);
       if (c->precision == 1) c->d_hbin32 = c->ar.calloc_c((c->naconftot + 1) / 2);
       {
@@ -3253,13 +3550,27 @@ int64_t guarded(Ctx* c, F&& fn) {
   }
 }
 
+// Host coefficient arrays are packet-major (APacketOffset(W) = W * nAConftot); the
+// device keeps every state's packets together (one strided copy per state).
 void upload(Ctx& c, cplx* dst, const double* A, const double* psi) {
-  CK(cudaMemcpyAsync(dst, A, sizeof(cplx) * c.naconftot, cudaMemcpyHostToDevice, c.st));
+  if (c.npk == 1) {
+    CK(cudaMemcpyAsync(dst, A, sizeof(cplx) * c.naconftot, cudaMemcpyHostToDevice, c.st));
+  } else {
+    for (int s = 0; s < c.nstates; ++s)
+      CK(cudaMemcpy2DAsync(dst + c.aoff[s], sizeof(cplx) * c.n1[s], reinterpret_cast<const cplx*>(A) + c.aoff1[s],
+                           sizeof(cplx) * c.n1tot, sizeof(cplx) * c.n1[s], c.npk, cudaMemcpyHostToDevice, c.st));
+  }
   if (c.dimpsi > 0)
     CK(cudaMemcpyAsync(dst + c.naconftot, psi, sizeof(cplx) * c.dimpsi, cudaMemcpyHostToDevice, c.st));
 }
 void download(Ctx& c, const cplx* src, double* A, double* psi) {
-  CK(cudaMemcpyAsync(A, src, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToHost, c.st));
+  if (c.npk == 1) {
+    CK(cudaMemcpyAsync(A, src, sizeof(cplx) * c.naconftot, cudaMemcpyDeviceToHost, c.st));
+  } else {
+    for (int s = 0; s < c.nstates; ++s)
+      CK(cudaMemcpy2DAsync(reinterpret_cast<cplx*>(A) + c.aoff1[s], sizeof(cplx) * c.n1tot, src + c.aoff[s],
+                           sizeof(cplx) * c.n1[s], sizeof(cplx) * c.n1[s], c.npk, cudaMemcpyDeviceToHost, c.st));
+  }
   if (c.dimpsi > 0)
     CK(cudaMemcpyAsync(psi, src + c.naconftot, sizeof(cplx) * c.dimpsi, cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
@@ -3649,10 +3960,20 @@ namespace {
 // WriteOutput quantities (output.f90:35-87, 144-150) of the resident state.
 void observables(Ctx& c, double* energy, double* pop, double* norm, double* auto_re, double* auto_im) {
   {
-    eom_from(c, c.d_y, c.d_out);
-    // f * H A before the Gaussian-mode corrections (Calc_MeanField's energyMF)
+    c.skip_mult = true;
+    try {
+      eom_from(c, c.d_y, c.d_out);
+    } catch (...) {
+      c.skip_mult = false;
+      throw;
+    }
+    c.skip_mult = false;
+    // f * H A before the Gaussian-mode corrections (Calc_MeanField's energyMF); the
+    // dissipative parts of the term sum are not energy
     const cplx* hA = c.modes_gwp.empty() ? c.d_out : c.d_adot;
     cplx e = dot_now(c, c.d_y, hA, c.naconftot);
+    if (c.pk_xa) e = csub(e, dot_now(c, c.d_y, c.pk_xa, c.naconftot));
+    if (c.pk_vmix) e = csub(e, dot_now(c, c.d_y, c.pk_vmix, c.naconftot));
     // energy = Re <A| H A> = Re( <A|dA> / der_factor )
     double dr = c.der.x, di = c.der.y, den = dr * dr + di * di;
     double en = (e.x * dr + e.y * di) / den;
@@ -3743,13 +4064,13 @@ void plan_expect(Ctx& c, WriterPlan& W) {
         const int n1 = c.m_of(m, s1);
         std::vector<int> ns = cur.shape;
         ns[m] = n1;
-        cplx* out = c.ar.calloc_c(prod_range(ns, 0, f));
+        cplx* out = c.ar.calloc_c(prod_range(ns, 0, (int)ns.size()));
         ++depth;
         W.chain[depth].add(cur.p, out, c.hmat[m][k], n1, 0, cur.shape, m, n1, mkc(1, 0), 0);
         cur.p = out;
         cur.shape = ns;
       }
-      if (prod_range(cur.shape, 0, f) != c.naconf[s1])
+      if (prod_range(cur.shape, 0, (int)cur.shape.size()) != c.naconf[s1])
         throw StatusError(MCTDH_EARG, "expectation term does not map state r onto state l");
       const int h = W.dots.add(c.ar, c.d_in + c.aoff[s1], cur.p, c.naconf[s1], 1, 1, 1);
       refs.push_back(HoleRef{h, tg, c.exp_ae[g]});
@@ -4385,6 +4706,30 @@ int64_t mctdh_norm_wf(mctdh_ctx_t* ctx, const double* A, const double* psi, doub
     cplx o[3];
     read_ovl(*c, c->io_plan, o);
     *norm = o[0].x;
+  });
+}
+
+int64_t mctdh_packets(mctdh_ctx_t* ctx, double* wppop, double* entropy) {
+  if (!ctx || !wppop) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    copy_dev(*c, c->d_in, c->d_y, c->ntot);
+    copy_dev(*c, c->d_out, c->d_y, c->ntot);
+    run_ovl(*c, c->io_plan);
+    std::vector<cplx> v(3 * c->npk);
+    CK(cudaMemcpyAsync(v.data(), c->io_plan.d_result, sizeof(cplx) * v.size(), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    std::vector<double> w(c->npk);
+    double tot = 0.0;
+    for (int i = 0; i < c->npk; ++i) tot += (w[i] = v[3 * i].x);
+    double ent = 0.0;
+    for (int i = 0; i < c->npk; ++i) {
+      w[i] /= tot;
+      if (w[i] >= 1e-8) ent -= w[i] * log(w[i]);
+    }
+    std::sort(w.begin(), w.end(), [](double a, double b) { return a > b; });
+    for (int i = 0; i < c->npk; ++i) wppop[i] = w[i];
+    if (entropy) *entropy = c->npk > 1 ? ent / log((double)c->npk) : 0.0;
   });
 }
 

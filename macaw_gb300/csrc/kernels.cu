@@ -1775,3 +1775,183 @@ void launch_mfx_combine(const MfxHist& hz, const MfxCoef& c, const float* Y, con
   if (E <= 0) return;
   mfx_combine_kernel<<<(unsigned)((E + 255) / 256), 256, 0, st>>>(hz, c, Y, S, half, full, E);
 }
+
+// ---------------------------------------------------------------------------
+// Statistical mixtures and dissipation
+// ---------------------------------------------------------------------------
+
+// Partial sums of <X_i|Y_j> (one row of PK_GRAM_BLOCKS blocks per pair).
+__global__ void __launch_bounds__(256) pk_gram_kernel(const PkGramPair* __restrict__ pairs,
+                                                      const PkState* __restrict__ st, int nstates,
+                                                      cplx* __restrict__ partial) {
+  const PkGramPair pr = pairs[blockIdx.y];
+  double re = 0.0, im = 0.0;
+  for (int s = 0; s < nstates; ++s) {
+    const PkState q = st[s];
+    const cplx* x = pr.X + q.off + (long long)pr.i * q.n;
+    const cplx* y = pr.Y + q.off + (long long)pr.j * q.n;
+    for (long long c = blockIdx.x * 256LL + threadIdx.x; c < q.n; c += 256LL * gridDim.x) {
+      const cplx a = x[c], b = y[c];
+      re = fma(a.x, b.x, fma(a.y, b.y, re));
+      im = fma(a.x, b.y, fma(-a.y, b.x, im));
+    }
+  }
+  __shared__ double sr[8], si[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_down_sync(0xffffffffu, re, o);
+    im += __shfl_down_sync(0xffffffffu, im, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sr[w] = re; si[w] = im; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0, i2 = 0.0;
+    for (int k = 0; k < 8; ++k) { r += sr[k]; i2 += si[k]; }
+    partial[(long long)blockIdx.y * PK_GRAM_BLOCKS + blockIdx.x] = make_double2(r, i2);
+  }
+}
+
+void launch_pk_gram(const PkGramPair* d_pairs, int npairs, const PkState* d_st, int nstates, cplx* partial,
+                    cudaStream_t st) {
+  if (npairs <= 0) return;
+  pk_gram_kernel<<<dim3(PK_GRAM_BLOCKS, npairs), 256, 0, st>>>(d_pairs, d_st, nstates, partial);
+}
+
+__device__ __forceinline__ cplx pk_mul(cplx a, cplx b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ cplx pk_conj(cplx a) { return make_double2(a.x, -a.y); }
+
+// Packet populations, Lagrange multipliers and mixing matrices (one block).
+// WPpopm1 = p / (p^2 + (eps exp(-(p/eps)^2))^2) (gmctdh_objects.f90:616-619);
+// type 1 (:661-692): AVA = <A_i|V A_j>, multLagDiag -= aeD1 sum |AVA_ij|^2 WPpopm1_i,
+// multLag_ij += aeD1 (AVA AVA^H)_ij (WPpopm1_i + WPpopm1_j) for i > j, D_W += aeD1 WPpopm1_W
+// sum_j V A_j conj(AVA_Wj), AuxA_W = i aeD1 WPpopm1_W sum_j A_j conj(AVA_Wj);
+// type 2 (:805-818) with G_ij = <A_i|X A_j>, X = sum_t f i aeD2 ae_t W_t:
+// multLagDiag -= Re sum_W G_WW, multLag_ij += G_ij + conj(G_ji) for i > j;
+// then multLag_ij *= i dw / (dw^2 + (eps exp(-(dw/eps)^2))^2), dw = p_i - p_j (:1128-1137).
+__global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
+  extern __shared__ cplx g[];   // [npairs]
+  for (int p = threadIdx.x; p < a.npairs; p += blockDim.x) {
+    double r = 0.0, i2 = 0.0;
+    for (int b = 0; b < PK_GRAM_BLOCKS; ++b) {
+      const cplx v = a.partial[(long long)p * PK_GRAM_BLOCKS + b];
+      r += v.x;
+      i2 += v.y;
+    }
+    g[p] = make_double2(r, i2);
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int P = a.P;
+  double pop[MAX_PACKETS], wpm1[MAX_PACKETS];
+  for (int w = 0; w < P; ++w) {
+    pop[w] = P > 1 ? g[w].x : 1.0;
+    const double r = a.eps_pop * exp(-(pop[w] / a.eps_pop) * (pop[w] / a.eps_pop));
+    wpm1[w] = pop[w] / (pop[w] * pop[w] + r * r);
+    a.pop[w] = pop[w];
+  }
+  double mdiag = 0.0;
+  cplx M[MAX_PACKETS * MAX_PACKETS];
+  for (int q = 0; q < P * P; ++q) M[q] = make_double2(0.0, 0.0);
+  int base = P + (a.has2 ? P * P : 0);
+  for (int k = 0; k < a.ndiss1; ++k, base += P * P) {
+    const cplx* V = g + base;   // V[i + P j] = <A_i|V_k A_j>
+    const double ae = a.aeD1[k];
+    double s = 0.0;
+    for (int j = 0; j < P; ++j)
+      for (int i = 0; i < P; ++i) {
+        const cplx v = V[i + P * j];
+        s -= (v.x * v.x + v.y * v.y) * wpm1[i];
+      }
+    mdiag += s * ae;
+    for (int j = 0; j < P; ++j)
+      for (int i = j + 1; i < P; ++i) {
+        cplx h = make_double2(0.0, 0.0);
+        for (int l = 0; l < P; ++l) {
+          const cplx t = pk_mul(V[i + P * l], pk_conj(V[j + P * l]));
+          h.x += t.x;
+          h.y += t.y;
+        }
+        const double f = ae * (wpm1[i] + wpm1[j]);
+        M[i + P * j].x += h.x * f;
+        M[i + P * j].y += h.y * f;
+      }
+    cplx* C1 = a.C1 + (long long)k * P * P;
+    cplx* C2 = a.C2 + (long long)k * P * P;
+    for (int w = 0; w < P; ++w)
+      for (int j = 0; j < P; ++j) {
+        const cplx v = pk_conj(V[w + P * j]);
+        const double f = ae * wpm1[w];
+        C1[j + P * w] = make_double2(v.x * f, v.y * f);
+        C2[j + P * w] = make_double2(-v.y * f, v.x * f);
+      }
+  }
+  if (a.has2) {
+    const cplx* G = g + P;
+    for (int w = 0; w < P; ++w) mdiag -= G[w + P * w].x;
+    for (int j = 0; j < P; ++j)
+      for (int i = j + 1; i < P; ++i) {
+        M[i + P * j].x += G[i + P * j].x + G[j + P * i].x;
+        M[i + P * j].y += G[i + P * j].y - G[j + P * i].y;
+      }
+  }
+  for (int j = 0; j < P; ++j)
+    for (int i = j + 1; i < P; ++i) {
+      const double dw = pop[i] - pop[j];
+      const double r = a.eps_pop * exp(-(dw / a.eps_pop) * (dw / a.eps_pop));
+      const double f = dw / (dw * dw + r * r);
+      const cplx m = M[i + P * j];
+      M[i + P * j] = make_double2(-m.y * f, m.x * f);   // times i f
+    }
+  // ML = multLagDiag I + i H, H Hermitian from the lower triangle with a zero diagonal
+  for (int j = 0; j < P; ++j)
+    for (int i = 0; i < P; ++i) {
+      cplx h = i > j ? M[i + P * j] : (i < j ? pk_conj(M[j + P * i]) : make_double2(0.0, 0.0));
+      a.ML[i + P * j] = make_double2(-h.y + (i == j ? mdiag : 0.0), h.x);
+    }
+}
+
+void launch_pk_coef(const PkCoefArgs& a, cudaStream_t st) {
+  pk_coef_kernel<<<1, 256, sizeof(cplx) * a.npairs, st>>>(a);
+}
+
+__global__ void __launch_bounds__(256) pk_mix_kernel(const PkMix* __restrict__ mix, int nmix,
+                                                     const PkState* __restrict__ st, int nstates,
+                                                     long long n1tot, int P, cplx* out0) {
+  extern __shared__ cplx cm[];   // [nmix][P][P]
+  for (int q = threadIdx.x; q < nmix * P * P; q += blockDim.x) cm[q] = mix[q / (P * P)].C[q % (P * P)];
+  __syncthreads();
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n1tot; e += 256LL * gridDim.x) {
+    long long c = e;
+    int s = 0;
+    while (s + 1 < nstates && c >= st[s].n) c -= st[s++].n;
+    const long long off = st[s].off + c, n = st[s].n;
+    for (int d = 0; d < nmix; ++d) {
+      const cplx* in = mix[d].in + off;
+      cplx* out = (out0 ? out0 : mix[d].out) + off;
+      const cplx* C = cm + d * P * P;
+      cplx x[MAX_PACKETS];
+      for (int j = 0; j < P; ++j) x[j] = in[j * n];
+      for (int w = 0; w < P; ++w) {
+        double re = 0.0, im = 0.0;
+        for (int j = 0; j < P; ++j) {
+          const cplx cc = C[j + P * w];
+          re = fma(x[j].x, cc.x, fma(-x[j].y, cc.y, re));
+          im = fma(x[j].x, cc.y, fma(x[j].y, cc.x, im));
+        }
+        if (mix[d].accumulate) {
+          const cplx o = out[w * n];
+          re += o.x;
+          im += o.y;
+        }
+        out[w * n] = make_double2(re, im);
+      }
+    }
+  }
+}
+
+void launch_pk_mix(const PkMix* d_mix, int nmix, const PkState* d_st, int nstates, long long n1tot, int P,
+                   cplx* out0, cudaStream_t st) {
+  if (nmix <= 0 || n1tot <= 0) return;
+  const long long nb = std::min<long long>((n1tot + 255) / 256, FUSED_BLOCKS);
+  pk_mix_kernel<<<(int)nb, 256, sizeof(cplx) * nmix * P * P, st>>>(d_mix, nmix, d_st, nstates, n1tot, P, out0);
+}

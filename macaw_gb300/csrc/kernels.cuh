@@ -244,6 +244,50 @@ struct FusedDot {
   unsigned* counter;
   cplx* res;
 };
+// ---------------------------------------------------------------------------
+// Statistical mixtures and dissipation (gmctdh_objects.f90:481-1141,
+// derivatives.f90:70-83, 238-242).  The coefficients of every state are stored
+// packet-minor: state s occupies [off, off + P n) with packet W at off + W n.
+// ---------------------------------------------------------------------------
+#define MAX_PACKETS 16
+#define MAX_DISS1 4
+#define PK_GRAM_BLOCKS 32
+struct PkState {
+  long long off, n;        // storage offset of the state's block, configurations per packet
+};
+// <X_i | Y_j> summed over the states
+struct PkGramPair {
+  const cplx* X;
+  const cplx* Y;
+  int i, j;
+};
+// Pair order: [0, P) the packet norms <A_W|A_W>; then (has2) P^2 pairs
+// <A_i | (sum_t f ae_t W_t) A_j> at P + i + P j; then per type-1 operator k the P^2
+// pairs <A_i | V_k A_j>.
+struct PkCoefArgs {
+  int P, ndiss1, has2, npairs;
+  double eps_pop;
+  double aeD1[MAX_DISS1];
+  const cplx* partial;     // [npairs][PK_GRAM_BLOCKS]
+  double* pop;             // [P] WPpop (1 for a single packet)
+  cplx* C1;                // [ndiss1][P][P]: D_W += sum_j (V_k A)_j C1[j + P W]
+  cplx* C2;                // [ndiss1][P][P]: AuxA_k,W = sum_j A_j C2[j + P W]
+  cplx* ML;                // [P][P]: dA_W += sum_j A_j ML[j + P W]  (multLagDiag I + i multLag)
+};
+// out[s][W] (+)= sum_j in[s][j] C[j + P W] for every state s and packet W (out0, if
+// not null, replaces every descriptor's out)
+struct PkMix {
+  const cplx* in;
+  const cplx* C;
+  cplx* out;
+  int accumulate;
+};
+void launch_pk_gram(const PkGramPair* d_pairs, int npairs, const PkState* d_st, int nstates, cplx* partial,
+                    cudaStream_t st);
+void launch_pk_coef(const PkCoefArgs& a, cudaStream_t st);
+void launch_pk_mix(const PkMix* d_mix, int nmix, const PkState* d_st, int nstates, long long n1tot, int P,
+                   cplx* out0, cudaStream_t st);
+
 void launch_termsum(cplx* out, const SumRange* d_ranges, int nranges, const SumSrc* d_srcs,
                     long long total, cudaStream_t st, int prec,
                     FusedDot dot = FusedDot{nullptr, nullptr, nullptr, nullptr});
