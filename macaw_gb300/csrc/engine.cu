@@ -328,6 +328,7 @@ struct Ctx {
   cplx *pk_xa = nullptr, *pk_va = nullptr, *pk_aux = nullptr, *pk_vmix = nullptr;
   PkState* pk_st = nullptr;
   PkGramPair* pk_pairs = nullptr;
+  bool pk_on = false;
   int pk_npairs = 0, pk_nmix = 0;
   cplx* pk_partial = nullptr;
   cplx* pk_coef_buf = nullptr;
@@ -428,6 +429,7 @@ struct Ctx {
   std::vector<std::vector<int>> h1_of_mode;  // indices into h1_h per DVR mode
   // overlap plans
   OvlPlan dpsi_plan;   // d_tmp vs d_err
+  OvlPlan pk_norm;     // packet norms of d_in (mixtures with dissipation)
   OvlPlan auto_plan;   // d_y0 vs d_y (o12), d_y norm (o22)
   OvlPlan io_plan;     // d_in vs d_out (host API norm/ovl)
   // CMF2 / Lanczos
@@ -827,6 +829,9 @@ const cplx* plan_s_weighted(Ctx& c, int s, int skip) {
 // ---------------------------------------------------------------------------
 void plan_gwp_derivs(Ctx& c);
 
+void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only = false);
+void run_ovl(Ctx& c, OvlPlan& P);
+
 // type-1 mean-field contribution: contraction of L_im(A) with the right chain on AuxA
 struct AuxRef {
   int hole, im, k;
@@ -868,7 +873,9 @@ void plan_packets(Ctx& c, std::vector<std::vector<SumSrc>>& srcs, std::vector<st
     sp.srcs = upload_vec(c.ar, ss);
   };
   std::vector<PkGramPair> pairs;
-  for (int w = 0; w < P; ++w) pairs.push_back(PkGramPair{c.d_in, c.d_in, w, w});
+  // WPpop = norm_wf(A_W, psi) with the SPF overlaps (derivatives.f90:70-76): the
+  // intermediate states of an integrator step have non-orthonormal SPFs
+  if (P > 1) plan_ovl(c, c.pk_norm, c.d_in, c.d_in, 0, true);
   if (has2) {
     c.pk_xa = c.ar.calloc_c(c.naconftot);
     sum_plan(srcs2, c.pk_sum2);
@@ -882,6 +889,7 @@ void plan_packets(Ctx& c, std::vector<std::vector<SumSrc>>& srcs, std::vector<st
     for (int j = 0; j < P; ++j)
       for (int i = 0; i < P; ++i) pairs.push_back(PkGramPair{c.d_in, c.pk_va + (long long)k * c.naconftot, i, j});
   }
+  c.pk_on = true;
   c.pk_npairs = (int)pairs.size();
   c.pk_pairs = upload_vec(c.ar, pairs);
   c.pk_partial = c.ar.calloc_c((long long)c.pk_npairs * PK_GRAM_BLOCKS);
@@ -895,6 +903,7 @@ void plan_packets(Ctx& c, std::vector<std::vector<SumSrc>>& srcs, std::vector<st
   a.eps_pop = c.eps_pop;
   for (int k = 0; k < c.ndiss1; ++k) a.aeD1[k] = c.aeD1[k];
   a.partial = c.pk_partial;
+  a.norms = c.pk_norm.d_result;
   a.C1 = c.pk_coef_buf;
   a.C2 = c.pk_coef_buf + (long long)c.ndiss1 * P * P;
   a.ML = c.pk_coef_buf + (long long)2 * c.ndiss1 * P * P;
@@ -1595,7 +1604,7 @@ void plan_hb(Ctx& c) {
 // products of the chains in compensated split FP32 (~1e-13 relative); used for
 // the step-error norm DeltaPsi of split-precision contexts, where 1 - Re<1|2>/..
 // is of order eps_int^2 / 2 >> 1e-13.  Norms and C(t) keep prec 0.
-void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
+void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only) {
   const int f = c.nmodes;
   P.npk = c.npk;
   P.d_result = c.ar.calloc_c(3 * c.npk);
@@ -1680,7 +1689,7 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
       const int m = order[i];
       const int n = sh[m];
       cplx* mats[3] = {S[m][s].s11, S[m][s].s22, S[m][s].s12};
-      for (int q = 0; q < 3; ++q) {
+      for (int q = 0; q < (norm_only ? 1 : 3); ++q) {
         cplx* out = c.ar.calloc_c(N);
         P.chain[i + 1].add(cur[q], out, mats[q], n, 0, sh, m, n, mkc(1, 0), 0, curfmt[q], cfmt);
         cur[q] = out;
@@ -1692,6 +1701,7 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec) {
       const long long o = n1 * w;
       drefs.push_back(HoleRef{P.dots.add(c.ar, a1 + o, cur[0] + o, n1, 1, 1, 1, TF_C64, curfmt[0]), tgt[3 * w],
                               mkc(1, 0)});
+      if (norm_only) continue;
       drefs.push_back(HoleRef{P.dots.add(c.ar, a2 + o, cur[1] + o, n1, 1, 1, 1, TF_C64, curfmt[1]), tgt[3 * w + 1],
                               mkc(1, 0)});
       drefs.push_back(HoleRef{P.dots.add(c.ar, a1 + o, cur[2] + o, n1, 1, 1, 1, TF_C64, curfmt[2]), tgt[3 * w + 2],
@@ -1887,6 +1897,7 @@ void run_packets(Ctx& c) {
     launch_termsum(c.pk_va + (long long)k * c.naconftot, sp.ranges, sp.n, sp.srcs, c.naconftot, c.st, c.precision);
     c.count();
   }
+  if (c.npk > 1) run_ovl(c, c.pk_norm);
   launch_pk_gram(c.pk_pairs, c.pk_npairs, c.pk_st, c.nstates, c.pk_partial, c.st);
   launch_pk_coef(c.pk_args, c.st);
   c.count(2);
@@ -1922,7 +1933,7 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   run_hole(c, c.rho_holes);
   run_hole(c, c.holes);
   run_red(c, c.red);
-  if (c.pk_pairs) run_packets(c);
+  if (c.pk_on) run_packets(c);
   if (reginv || !mf_only) run_reginv(c);
   if (mf_only) {
     c.eom_count++;

@@ -1829,7 +1829,7 @@ __device__ __forceinline__ cplx pk_conj(cplx a) { return make_double2(a.x, -a.y)
 // multLagDiag -= Re sum_W G_WW, multLag_ij += G_ij + conj(G_ji) for i > j;
 // then multLag_ij *= i dw / (dw^2 + (eps exp(-(dw/eps)^2))^2), dw = p_i - p_j (:1128-1137).
 __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
-  extern __shared__ cplx g[];   // [npairs]
+  extern __shared__ cplx g[];   // [npairs + 1]
   for (int p = threadIdx.x; p < a.npairs; p += blockDim.x) {
     double r = 0.0, i2 = 0.0;
     for (int b = 0; b < PK_GRAM_BLOCKS; ++b) {
@@ -1844,7 +1844,7 @@ __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
   const int P = a.P;
   double pop[MAX_PACKETS], wpm1[MAX_PACKETS];
   for (int w = 0; w < P; ++w) {
-    pop[w] = P > 1 ? g[w].x : 1.0;
+    pop[w] = P > 1 ? a.norms[3 * w].x : 1.0;
     const double r = a.eps_pop * exp(-(pop[w] / a.eps_pop) * (pop[w] / a.eps_pop));
     wpm1[w] = pop[w] / (pop[w] * pop[w] + r * r);
     a.pop[w] = pop[w];
@@ -1852,7 +1852,7 @@ __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
   double mdiag = 0.0;
   cplx M[MAX_PACKETS * MAX_PACKETS];
   for (int q = 0; q < P * P; ++q) M[q] = make_double2(0.0, 0.0);
-  int base = P + (a.has2 ? P * P : 0);
+  int base = a.has2 ? P * P : 0;
   for (int k = 0; k < a.ndiss1; ++k, base += P * P) {
     const cplx* V = g + base;   // V[i + P j] = <A_i|V_k A_j>
     const double ae = a.aeD1[k];
@@ -1886,7 +1886,7 @@ __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
       }
   }
   if (a.has2) {
-    const cplx* G = g + P;
+    const cplx* G = g;
     for (int w = 0; w < P; ++w) mdiag -= G[w + P * w].x;
     for (int j = 0; j < P; ++j)
       for (int i = j + 1; i < P; ++i) {
@@ -1911,7 +1911,7 @@ __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
 }
 
 void launch_pk_coef(const PkCoefArgs& a, cudaStream_t st) {
-  pk_coef_kernel<<<1, 256, sizeof(cplx) * a.npairs, st>>>(a);
+  pk_coef_kernel<<<1, 256, sizeof(cplx) * (a.npairs + 1), st>>>(a);
 }
 
 __global__ void __launch_bounds__(256) pk_mix_kernel(const PkMix* __restrict__ mix, int nmix,

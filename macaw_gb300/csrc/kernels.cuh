@@ -261,14 +261,16 @@ struct PkGramPair {
   const cplx* Y;
   int i, j;
 };
-// Pair order: [0, P) the packet norms <A_W|A_W>; then (has2) P^2 pairs
-// <A_i | (sum_t f ae_t W_t) A_j> at P + i + P j; then per type-1 operator k the P^2
-// pairs <A_i | V_k A_j>.
+// Pair order: (has2) P^2 pairs <A_i | (sum_t f ae_t W_t) A_j> at i + P j; then per
+// type-1 operator k the P^2 pairs <A_i | V_k A_j> (plain coefficient dots, as the
+// reference's zdotu / zgemm).  The packet norms WPpop = norm_wf(A_W) carry the SPF
+// overlaps and come from an overlap plan (norms[3 W]).
 struct PkCoefArgs {
   int P, ndiss1, has2, npairs;
   double eps_pop;
   double aeD1[MAX_DISS1];
   const cplx* partial;     // [npairs][PK_GRAM_BLOCKS]
+  const cplx* norms;       // [3 P]: <A_W|A_W> with the SPF metric at 3 W
   double* pop;             // [P] WPpop (1 for a single packet)
   cplx* C1;                // [ndiss1][P][P]: D_W += sum_j (V_k A)_j C1[j + P W]
   cplx* C2;                // [ndiss1][P][P]: AuxA_k,W = sum_j A_j C2[j + P W]

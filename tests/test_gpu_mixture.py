@@ -48,6 +48,22 @@ def test_mixture_derivs(core_cls, P, which):
     assert _rel(dpsi, rp) < EOM_RTOL
 
 
+def test_mixture_derivs_nonorthonormal_spfs(core_cls):
+    """Intermediate states of a step have non-orthonormal SPFs: the packet
+    populations WPpop are norm_wf values with the SPF overlaps (derivatives.f90:74)."""
+    model = _model(3, "both")
+    model.eps_pop = 1e-3
+    model.finalize()
+    A, psi = initial_wavefunction(model)
+    orc = Oracle(model)
+    dA, dpsi = orc.calc_derivs(A, psi, 0.0)
+    A2, p2 = A + 0.04 * dA, psi + 0.04 * dpsi
+    rA, rp = orc.calc_derivs(A2, p2, 0.0)
+    gA, gp = core_cls(model).calc_derivs(A2, p2, 0.0)
+    assert _rel(gA, rA) < EOM_RTOL
+    assert _rel(gp, rp) < EOM_RTOL
+
+
 @pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-10)])
 def test_mixture_split_precision(core_cls, prec, tol):
     model = _model(3, "both")
@@ -76,8 +92,8 @@ def test_mixture_rk_attempt(core_cls, method):
 def test_mixture_propagation(core_cls):
     """Free-running RK45 of a mixture with both dissipation types: observables,
     packet populations and entropy against the oracle; the total population stays 1."""
-    model = _model(3, "both", tfinal_fs=0.5, eps_int=1e-7)
-    model.tout = 0.25 / 41.341373335
+    model = _model(3, "both", tfinal_fs=0.2, eps_int=1e-7)
+    model.tout = 0.1 / 41.341373335
     model.eps_pop = 1e-3
     model.finalize()
     A, psi = initial_wavefunction(model)
