@@ -10,7 +10,7 @@ by the rounding noise of DeltaPsi).
 import numpy as np
 import pytest
 
-from macaw_gb300.model import initial_wavefunction, INT_RK45, INT_DOPRI, INT_CMF2
+from macaw_gb300.model import initial_wavefunction, AU2FS, INT_RK45, INT_DOPRI, INT_CMF2
 from oracle.mctdh import Oracle
 from tests.helpers import small_lvc, with_mixture, random_mixture
 
@@ -92,8 +92,8 @@ def test_mixture_rk_attempt(core_cls, method):
 def test_mixture_propagation(core_cls):
     """Free-running RK45 of a mixture with both dissipation types: observables,
     packet populations and entropy against the oracle; the total population stays 1."""
-    model = _model(3, "both", tfinal_fs=0.2, eps_int=1e-7)
-    model.tout = 0.1 / 41.341373335
+    model = _model(3, "both", tfinal_fs=0.5, eps_int=1e-7)
+    model.tout = 0.25 / AU2FS
     model.eps_pop = 1e-3
     model.finalize()
     A, psi = initial_wavefunction(model)
