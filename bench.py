@@ -500,14 +500,15 @@ def run_ensemble(args):
 def run_rk_workload(args):
     """RK configurations: lvc5 (2-state LVC over 5 HO modes, Cash-Karp, eps 1e-8)
     and gmctdh16 (2-state LVC, 4 HO modes + one 12-DOF Gaussian mode with 32
-    Gaussians per state).  After 0.2 fs untimed, `--rk-fs` fs timed with CUDA
+    Gaussians per state) and lvc5mix (lvc5 as a 4-packet mixture under Lindblad
+    dephasing of mode 1: type-1 and type-2 dissipation).  After 0.2 fs untimed, `--rk-fs` fs timed with CUDA
     events on the library's stream; C(t) against the FP64 path when the
     precision is split."""
     import torch
     from macaw_gb300.capi import GpuCore
-    from macaw_gb300.generate import lvc5, gmctdh16
+    from macaw_gb300.generate import lvc5, gmctdh16, lvc5_mixture
     torch.cuda.init()
-    model = lvc5() if args.workload == "lvc5" else gmctdh16()
+    model = {"lvc5": lvc5, "gmctdh16": gmctdh16, "lvc5mix": lvc5_mixture}[args.workload]()
     A0, psi0 = initial_wavefunction(model)
     out = {}
     for prec in sorted({0, args.precision}):
@@ -531,7 +532,8 @@ def run_rk_workload(args):
             "steps": out[args.precision]["steps"], "attempts": out[args.precision]["attempts"],
             "ms": out[args.precision]["ms"],
             "config": {"workload": args.workload, "interval_fs": args.rk_fs, "from_fs": 0.2,
-                       "coefficients": int(model.naconftot), "dimpsi": int(model.dimpsi),
+                       "coefficients": int(model.naconftot * model.npackets), "dimpsi": int(model.dimpsi),
+                       "npackets": int(model.npackets), "dissipative_operators": len(model.dissipation),
                        "eps_int": model.eps_int}}
     if args.precision != 0:
         line["accuracy_vs_fp64_path"] = {
@@ -550,7 +552,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
-    ap.add_argument("--workload", default="qvc12", choices=["qvc12", "ensemble", "lvc5", "gmctdh16"],
+    ap.add_argument("--workload", default="qvc12", choices=["qvc12", "ensemble", "lvc5", "gmctdh16", "lvc5mix"],
                     help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement; "
                          "lvc5 / gmctdh16: RK configurations")
     ap.add_argument("--rk-fs", type=float, default=0.5)
@@ -567,7 +569,7 @@ def main():
         return run_profile_case(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
-    if args.workload in ("lvc5", "gmctdh16"):
+    if args.workload in ("lvc5", "gmctdh16", "lvc5mix"):
         return run_rk_workload(args)
     if args.impl == "reference":
         return run_reference(args)

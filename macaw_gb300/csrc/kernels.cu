@@ -1829,42 +1829,46 @@ __device__ __forceinline__ cplx pk_conj(cplx a) { return make_double2(a.x, -a.y)
 // multLagDiag -= Re sum_W G_WW, multLag_ij += G_ij + conj(G_ji) for i > j;
 // then multLag_ij *= i dw / (dw^2 + (eps exp(-(dw/eps)^2))^2), dw = p_i - p_j (:1128-1137).
 __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
-  extern __shared__ cplx g[];   // [npairs + 1]
-  for (int p = threadIdx.x; p < a.npairs; p += blockDim.x) {
-    double r = 0.0, i2 = 0.0;
-    for (int b = 0; b < PK_GRAM_BLOCKS; ++b) {
-      const cplx v = a.partial[(long long)p * PK_GRAM_BLOCKS + b];
-      r += v.x;
-      i2 += v.y;
+  extern __shared__ cplx g[];   // [npairs]
+  __shared__ double pop[MAX_PACKETS], wpm1[MAX_PACKETS];
+  __shared__ cplx M[MAX_PACKETS * MAX_PACKETS];
+  __shared__ double dterm[MAX_PACKETS * MAX_PACKETS];
+  // one warp per pair: the PK_GRAM_BLOCKS (= 32) block sums, one per lane, added by
+  // a fixed shuffle tree
+  const int lane = threadIdx.x & 31, tid = threadIdx.x;
+  for (int p = tid >> 5; p < a.npairs; p += blockDim.x >> 5) {
+    const cplx v = a.partial[(long long)p * PK_GRAM_BLOCKS + lane];
+    double r = v.x, i2 = v.y;
+    for (int o = 16; o > 0; o >>= 1) {
+      r += __shfl_down_sync(0xffffffffu, r, o);
+      i2 += __shfl_down_sync(0xffffffffu, i2, o);
     }
-    g[p] = make_double2(r, i2);
+    if (lane == 0) g[p] = make_double2(r, i2);
+  }
+  const int P = a.P, PP = P * P;
+  if (tid < P) {
+    const double p = P > 1 ? a.norms[3 * tid].x : 1.0;
+    const double r = a.eps_pop * exp(-(p / a.eps_pop) * (p / a.eps_pop));
+    pop[tid] = p;
+    wpm1[tid] = p / (p * p + r * r);
+    a.pop[tid] = p;
+  }
+  // thread (i, j) = (tid % P, tid / P) owns M[i + P j] and its share of multLagDiag
+  const int i = tid % P, j = tid / P;
+  const bool own = tid < PP;
+  if (own) {
+    M[tid] = make_double2(0.0, 0.0);
+    dterm[tid] = 0.0;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  const int P = a.P;
-  double pop[MAX_PACKETS], wpm1[MAX_PACKETS];
-  for (int w = 0; w < P; ++w) {
-    pop[w] = P > 1 ? a.norms[3 * w].x : 1.0;
-    const double r = a.eps_pop * exp(-(pop[w] / a.eps_pop) * (pop[w] / a.eps_pop));
-    wpm1[w] = pop[w] / (pop[w] * pop[w] + r * r);
-    a.pop[w] = pop[w];
-  }
-  double mdiag = 0.0;
-  cplx M[MAX_PACKETS * MAX_PACKETS];
-  for (int q = 0; q < P * P; ++q) M[q] = make_double2(0.0, 0.0);
-  int base = a.has2 ? P * P : 0;
-  for (int k = 0; k < a.ndiss1; ++k, base += P * P) {
+  int base = a.has2 ? PP : 0;
+  for (int k = 0; k < a.ndiss1; ++k, base += PP) {
     const cplx* V = g + base;   // V[i + P j] = <A_i|V_k A_j>
     const double ae = a.aeD1[k];
-    double s = 0.0;
-    for (int j = 0; j < P; ++j)
-      for (int i = 0; i < P; ++i) {
-        const cplx v = V[i + P * j];
-        s -= (v.x * v.x + v.y * v.y) * wpm1[i];
-      }
-    mdiag += s * ae;
-    for (int j = 0; j < P; ++j)
-      for (int i = j + 1; i < P; ++i) {
+    if (own) {
+      const cplx v = V[tid];
+      dterm[tid] -= ae * (v.x * v.x + v.y * v.y) * wpm1[i];
+      if (i > j) {
         cplx h = make_double2(0.0, 0.0);
         for (int l = 0; l < P; ++l) {
           const cplx t = pk_mul(V[i + P * l], pk_conj(V[j + P * l]));
@@ -1872,42 +1876,41 @@ __global__ void __launch_bounds__(256) pk_coef_kernel(PkCoefArgs a) {
           h.y += t.y;
         }
         const double f = ae * (wpm1[i] + wpm1[j]);
-        M[i + P * j].x += h.x * f;
-        M[i + P * j].y += h.y * f;
+        M[tid].x += h.x * f;
+        M[tid].y += h.y * f;
       }
-    cplx* C1 = a.C1 + (long long)k * P * P;
-    cplx* C2 = a.C2 + (long long)k * P * P;
-    for (int w = 0; w < P; ++w)
-      for (int j = 0; j < P; ++j) {
-        const cplx v = pk_conj(V[w + P * j]);
-        const double f = ae * wpm1[w];
-        C1[j + P * w] = make_double2(v.x * f, v.y * f);
-        C2[j + P * w] = make_double2(-v.y * f, v.x * f);
-      }
+      // C[j' + P w] with (j', w) = (i, j): conj(V[w + P j']) scaled by aeD1 WPpopm1_w
+      const cplx v2 = pk_conj(V[j + P * i]);
+      const double f = ae * wpm1[j];
+      a.C1[(long long)k * PP + tid] = make_double2(v2.x * f, v2.y * f);
+      a.C2[(long long)k * PP + tid] = make_double2(-v2.y * f, v2.x * f);
+    }
   }
-  if (a.has2) {
+  if (a.has2 && own) {
     const cplx* G = g;
-    for (int w = 0; w < P; ++w) mdiag -= G[w + P * w].x;
-    for (int j = 0; j < P; ++j)
-      for (int i = j + 1; i < P; ++i) {
-        M[i + P * j].x += G[i + P * j].x + G[j + P * i].x;
-        M[i + P * j].y += G[i + P * j].y - G[j + P * i].y;
-      }
+    if (i == j) dterm[tid] -= G[tid].x;
+    if (i > j) {
+      M[tid].x += G[i + P * j].x + G[j + P * i].x;
+      M[tid].y += G[i + P * j].y - G[j + P * i].y;
+    }
   }
-  for (int j = 0; j < P; ++j)
-    for (int i = j + 1; i < P; ++i) {
-      const double dw = pop[i] - pop[j];
-      const double r = a.eps_pop * exp(-(dw / a.eps_pop) * (dw / a.eps_pop));
-      const double f = dw / (dw * dw + r * r);
-      const cplx m = M[i + P * j];
-      M[i + P * j] = make_double2(-m.y * f, m.x * f);   // times i f
-    }
-  // ML = multLagDiag I + i H, H Hermitian from the lower triangle with a zero diagonal
-  for (int j = 0; j < P; ++j)
-    for (int i = 0; i < P; ++i) {
-      cplx h = i > j ? M[i + P * j] : (i < j ? pk_conj(M[j + P * i]) : make_double2(0.0, 0.0));
-      a.ML[i + P * j] = make_double2(-h.y + (i == j ? mdiag : 0.0), h.x);
-    }
+  if (own && i > j) {
+    const double dw = pop[i] - pop[j];
+    const double r = a.eps_pop * exp(-(dw / a.eps_pop) * (dw / a.eps_pop));
+    const double f = dw / (dw * dw + r * r);
+    const cplx m = M[tid];
+    M[tid] = make_double2(-m.y * f, m.x * f);   // times i f
+  }
+  __syncthreads();
+  if (own) {
+    // multLagDiag: the owners' shares added in a fixed order
+    double mdiag = 0.0;
+    if (i == j)
+      for (int q = 0; q < PP; ++q) mdiag += dterm[q];
+    // ML = multLagDiag I + i H, H Hermitian from the lower triangle with a zero diagonal
+    const cplx h = i > j ? M[tid] : (i < j ? pk_conj(M[j + P * i]) : make_double2(0.0, 0.0));
+    a.ML[tid] = make_double2(-h.y + (i == j ? mdiag : 0.0), h.x);
+  }
 }
 
 void launch_pk_coef(const PkCoefArgs& a, cudaStream_t st) {

@@ -251,7 +251,7 @@ struct FusedDot {
 // ---------------------------------------------------------------------------
 #define MAX_PACKETS 16
 #define MAX_DISS1 4
-#define PK_GRAM_BLOCKS 32
+#define PK_GRAM_BLOCKS 32   // one warp lane per block sum in pk_coef_kernel
 struct PkState {
   long long off, n;        // storage offset of the state's block, configurations per packet
 };

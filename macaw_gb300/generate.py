@@ -240,3 +240,20 @@ def write_inputs(model: Model, directory: str, name: str = "model") -> str:
 
 
 BUILDERS = {"lvc5": lvc5, "qvc12": qvc12, "gmctdh16": gmctdh16, "qvc24": qvc24}
+
+
+def lvc5_mixture(npackets: int = 4, gamma: float = 2e-3, eps_int: float = 1e-8, tfinal_fs: float = 100.0,
+                 eps_pop: float = 1e-6) -> Model:
+    """lvc5 as a statistical mixture of `npackets` packets (initialised from the
+    'el' line) under Lindblad dephasing of mode 1 with L = sqrt(gamma) q:
+    D[L] rho = gamma (q rho q - 1/2 {q^2, rho}), i.e. a type-1 operator V = q with
+    alpha = gamma and a type-2 operator W = q^2 with beta = -gamma / 2, on every
+    electronic state (input.f90:216-229, 596-616)."""
+    model = lvc5(eps_int=eps_int, tfinal_fs=tfinal_fs)
+    ns = model.nstates
+    model.npackets = npackets
+    model.eps_pop = eps_pop
+    model.dissipation = [(1, gamma, [Term(1.0, s, s, {0: 1}) for s in range(ns)]),
+                         (2, -0.5 * gamma, [Term(1.0, s, s, {0: 2}) for s in range(ns)])]
+    model.label = "lvc5-mixture"
+    return model.finalize()
