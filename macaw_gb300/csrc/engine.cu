@@ -429,6 +429,9 @@ struct Ctx {
   std::vector<std::vector<int>> h1_of_mode;  // indices into h1_h per DVR mode
   // overlap plans
   OvlPlan dpsi_plan;   // d_tmp vs d_err
+  OvlPlan cmf_ovl;     // CMF2's SPF error: d_ovl1 vs d_ovl2 (own buffers: it runs beside the SPF sweep)
+  cplx* d_ovl1 = nullptr;
+  cplx* d_ovl2 = nullptr;
   OvlPlan pk_norm;     // packet norms of d_in (mixtures with dissipation)
   OvlPlan auto_plan;   // d_y0 vs d_y (o12), d_y norm (o22)
   OvlPlan io_plan;     // d_in vs d_out (host API norm/ovl)
@@ -3329,14 +3332,19 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh,
   copy_dev(c, S.psiHalf2, c.d_y, c.ntot);
   if (S.gwp) copy_dev(c, S.DDHalf2, S.DD0, S.nD);
   propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2, S.DDHalf2);  // :132-141
-  // err_psi = DeltaPsi(AHalf, psiHalf, AHalf, psiHalf2)  (:143)
-  copy_dev(c, c.d_tmp, S.AHalf, c.ntot);
-  copy_dev(c, c.d_err, S.AHalf, nA);
-  copy_dev(c, c.d_err + nA, S.psiHalf2 + nA, c.dimpsi);
-  run_ovl(c, c.dpsi_plan);
-  cplx o[3];
-  read_ovl(c, c.dpsi_plan, o);
-  double err_psi = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x))));
+  // err_psi = DeltaPsi(AHalf, psiHalf, AHalf, psiHalf2)  (:143): copies of both
+  // states, then the overlaps on st2 beside the SPF sweep of :148-154 (read at the end)
+  copy_dev(c, c.d_ovl1, S.AHalf, c.ntot);
+  copy_dev(c, c.d_ovl2, S.AHalf, nA);
+  copy_dev(c, c.d_ovl2 + nA, S.psiHalf2 + nA, c.dimpsi);
+  if (overlap) {
+    CK(cudaEventRecord(c.ev_fork, c.st));
+    CK(cudaStreamWaitEvent(c.st2, c.ev_fork, 0));
+    StreamSwap sw(c, c.st2);
+    run_ovl(c, c.cmf_ovl);
+  } else {
+    run_ovl(c, c.cmf_ovl);
+  }
   propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2, S.DDHalf2);  // :148-154
   h1_only(c, S.psiHalf2);                           // :158-163
   if (S.gwp) {
@@ -3347,6 +3355,12 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh,
   launch_axpy(S.B02, S.B0, mkc(-1, 0), nA, c.st);
   c.count();
   double err_A = sqrt(dot_now(c, S.B02, S.B02, nA).x) * 0.5;
+  cplx o[3];
+  {
+    StreamSwap sw(c, overlap ? c.st2 : c.st);
+    read_ovl(c, c.cmf_ovl, o);
+  }
+  const double err_psi = sqrt(fabs(2.0 * (1.0 - o[2].x / sqrt(o[0].x * o[1].x))));
   check_status(c);
   double error = std::max(err_A, err_psi) / c.eps_int;
   if (!std::isfinite(error)) throw StatusError(MCTDH_ENONFINITE, "non-finite CMF2 error estimate");
@@ -3529,6 +3543,9 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       c->d_lan = (double*)c->ar.alloc(sizeof(double) * (3 * NKRYLOV_MAX + NKRYLOV_MAX * NKRYLOV_MAX));
       c->d_coef = c->ar.calloc_c(NKRYLOV_MAX);
       plan_hb(*c);
+      c->d_ovl1 = c->ar.calloc_c(c->ntot);
+      c->d_ovl2 = c->ar.calloc_c(c->ntot);
+      plan_ovl(*c, c->cmf_ovl, c->d_ovl1, c->d_ovl2, (c->precision && c->eps_int >= 1e-5) ? 2 : 0);
     }
     // the compensated products of DeltaPsi (~1e-13) resolve 1 - Re<1|2>/.. ~ eps_int^2 / 2
     // only for loose tolerances; tight ones keep FP64
