@@ -125,3 +125,43 @@ def test_cmf2_rejects_mixtures(core_cls):
     # the context stays usable
     dA, _ = gpu.calc_derivs(A, psi, 0.0)
     assert np.isfinite(dA).all()
+
+
+def _free_running(core_cls, model, atol_scale=10.0):
+    A, psi = initial_wavefunction(model)
+    ref, _, _ = Oracle(model).propagate(A, psi)
+    outs = core_cls(model).propagate(A, psi)
+    assert len(outs) == len(ref)
+    for g, r in zip(outs, ref):
+        assert abs(g["auto"] - r["auto"]) < atol_scale * model.eps_int
+        assert np.abs(g["pop"] - r["pop"]).max() < atol_scale * model.eps_int
+        assert abs(g["energy"] - r["energy"]) < atol_scale * model.eps_int
+    return outs
+
+
+@pytest.mark.parametrize("integrator", ["abm40", "bs"])
+def test_mixture_adams_and_bulirsch_stoer(core_cls, integrator):
+    """Adams PECE and Bulirsch-Stoer on a dissipative mixture: both error norms are
+    the packet DeltaPsi (integrator.f90:360-371, 540-548)."""
+    from macaw_gb300.model import INT_ABM, INT_BS
+    model = _model(3, "both", tfinal_fs=0.5, eps_int=1e-7)
+    model.tout = 0.25 / AU2FS
+    model.eps_pop = 1e-3
+    if integrator == "bs":
+        model.int_type = INT_BS
+    else:
+        model.int_type, model.int_order, model.int_par1 = INT_ABM, 4, 0
+    model.finalize()
+    _free_running(core_cls, model)
+
+
+def test_mixture_relaxation_and_packets_block(core_cls):
+    """Relaxation (der_factor = -1) of a dissipative mixture started from an explicit
+    'packets' block (init_calc.f90:527-540): the dissipative terms carry der_factor
+    exactly as the reference's (gmctdh_objects.f90:805)."""
+    model = _model(2, "both", tfinal_fs=0.5, eps_int=1e-7)
+    model.tout = 0.25 / AU2FS
+    model.relaxation = True
+    model.init_packets = [(1, (0, 0, 0, 0, 0), 0.8 + 0.0j), (0, (1, 0, 0, 0, 0), 0.6j)]
+    model.finalize()
+    _free_running(core_cls, model)
