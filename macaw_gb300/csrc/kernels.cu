@@ -1136,6 +1136,48 @@ __global__ void __launch_bounds__(256) spf_proj_kernel(const SpfDesc* __restrict
   }
 }
 
+// Split modes: dphi -= phi X with the products as compensated FP32 pairs on split
+// operands (~1e-13 relative) and one FP64 subtraction per element.
+__global__ void __launch_bounds__(256) spf_proj_split_kernel(const SpfDesc* __restrict__ descs, int ndesc,
+                                                             cplx* __restrict__ out) {
+  __shared__ int s_di;
+  __shared__ float4 Xs[MAXN_SPF * MAXN_SPF];
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const SpfDesc& d = descs[s_di];
+  const int n = d.n, G = d.G;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const cplx v = d.X[e];
+    float4 w4;
+    split_d2f(v.x, w4.x, w4.z);
+    split_d2f(v.y, w4.y, w4.w);
+    Xs[e] = w4;
+  }
+  __syncthreads();
+  const int t = (int)(blockIdx.x - d.block_start);
+  const int g0 = t * SPF_TILE;
+  const int rows = min(SPF_TILE, G - g0);
+  cplx* o = out + d.out_offset;
+  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
+    const int r = e % rows, j = e / rows;
+    const int g = g0 + r;
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int k = 0; k < n; ++k) {
+      const cplx ph = d.phi[g + (long long)G * k];
+      float xh, xl, yh, yl;
+      split_d2f(ph.x, xh, xl);
+      split_d2f(ph.y, yh, yl);
+      const float4 m = Xs[k + n * j];
+      df_fma(rh, rl, xh, xl, m.x, m.z);
+      df_fma(rh, rl, -yh, -yl, m.y, m.w);
+      df_fma(ih, il, xh, xl, m.y, m.w);
+      df_fma(ih, il, yh, yl, m.x, m.z);
+    }
+    const cplx v = o[g + (long long)G * j];
+    o[g + (long long)G * j] = mkc(v.x - (f2d_exact(rh) + f2d_exact(rl)), v.y - (f2d_exact(ih) + f2d_exact(il)));
+  }
+}
+
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
                 cplx der_factor, int* d_status, cudaStream_t st, int prec) {
   if (ndesc <= 0) return;
@@ -1144,7 +1186,8 @@ void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp
   if (prec > 0) spf_tile_split_kernel<2><<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   else spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   spf_solve_kernel<<<ndesc, 256, 0, st>>>(d_descs, d_status);
-  spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
+  if (prec > 0) spf_proj_split_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
+  else spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
 }
 
 // ---------------------------------------------------------------------------
