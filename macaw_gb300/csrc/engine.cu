@@ -401,6 +401,7 @@ struct Ctx {
   SpfOp* spfop_d = nullptr;
   size_t spf_smem = 0;
   long long spf_tiles = 0;
+  int spf_nf = 0;          // largest SPF count of the SPF derivative blocks and their operators
   std::vector<SumRange> sum_h;
   std::vector<SumSrc> src_h;
   SumRange* sum_d = nullptr;
@@ -1381,6 +1382,8 @@ void plan_eom(Ctx& c) {
   }
   c.spf_smem = ssmem;
   c.spf_d = upload_vec(c.ar, c.spf_h);
+  for (auto& x : c.spf_h) c.spf_nf = std::max(c.spf_nf, x.n);
+  for (auto& x : c.spfop_h) c.spf_nf = std::max(c.spf_nf, x.n2);
   c.spfop_d = upload_vec(c.ar, c.spfop_h);
 
   // dA = f * sum_t ae_t * (H_t A)   (conjugate of Adot_tmp, gmctdh_objects.f90:578; derivatives.f90:155-156)
@@ -1949,7 +1952,7 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   }
   {
     ProfScope ps(c, KP_SPF);
-    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision);
+    launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision, c.spf_nf);
     c.count(3);
   }
   if (gwp) gwp_derivs_run(c, out);
@@ -2746,7 +2749,7 @@ void spf_eval_all(Ctx& c, CmfState& S, cplx* out, cplx* Dout) {
     }
     {
       ProfScope ps(c, KP_SPF);
-      launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision);
+      launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision, c.spf_nf);
     }
     c.count(4);
   }
@@ -3653,6 +3656,7 @@ struct Ens {
   SpfDesc* spf_d = nullptr;
   SpfOp* spfop_d = nullptr;
   long long spf_tiles = 0;
+  int spf_nf = 0;          // largest SPF count of the SPF derivative blocks and their operators
   std::vector<SumRange> sum_h;
   std::vector<SumSrc> src_h;
   SumRange* sum_d = nullptr;
@@ -3786,6 +3790,8 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
     E->reg_d = upload_vec(E->ar, E->reg_h);
     E->mfop_d = upload_vec(E->ar, E->mfop_h);
     E->spf_d = upload_vec(E->ar, E->spf_h);
+    for (auto& x : E->spf_h) E->spf_nf = std::max(E->spf_nf, x.n);
+    for (auto& x : E->spfop_h) E->spf_nf = std::max(E->spf_nf, x.n2);
     E->spfop_d = upload_vec(E->ar, E->spfop_h);
     E->sum_d = upload_vec(E->ar, E->sum_h);
     split_coeffs(E->src_h);
@@ -3851,7 +3857,7 @@ void ens_eom(Ens& E, cplx* out) {
   ens_run_red(E, E.red);
   launch_reginv(E.reg_d, (int)E.reg_h.size(), E.mfop_d, E.status_d, E.st);
   launch_termsum(out, E.sum_d, (int)E.sum_h.size(), E.src_d, E.total, E.st, E.precision);
-  launch_spf(E.spf_d, (int)E.spf_h.size(), E.spf_tiles, E.spfop_d, out, E.der, E.status_d, E.st, E.precision);
+  launch_spf(E.spf_d, (int)E.spf_h.size(), E.spf_tiles, E.spfop_d, out, E.der, E.status_d, E.st, E.precision, E.spf_nf);
   E.launches += 5;
   E.eom_count++;
 }

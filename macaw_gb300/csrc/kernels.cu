@@ -1071,6 +1071,129 @@ __global__ void __launch_bounds__(256) spf_tile_split_kernel(const SpfDesc* __re
   }
 }
 
+// spf_tile_split_kernel<2> with the operator sum split between two groups of 256
+// threads (operators 0, 2, 4, .. and 1, 3, 5, ..; both groups pass every barrier),
+// for n <= 16: twice the warps per tile, the same compensated arithmetic; the
+// second group's (hi, lo) sums are added to the first's at the end.
+#define SPF_G2_N 16
+__global__ void __launch_bounds__(512) spf_tile_split2_kernel(const SpfDesc* __restrict__ descs, int ndesc,
+                                                              const SpfOp* __restrict__ ops,
+                                                              cplx* __restrict__ out, cplx der) {
+  __shared__ int s_di;
+  // per group: ophi tile [SPF_TILE][16] and rhom1MF [16][16], split; epilogue: phi and
+  // dphi rows alias them; red: the second group's sums
+  __shared__ __align__(16) float4 buf[2 * (SPF_TILE * SPF_G2_N + SPF_G2_N * SPF_G2_N)];
+  __shared__ __align__(16) float4 red[2 * 256];
+  const int grp = threadIdx.x >> 8, loc = threadIdx.x & 255;
+  float4* ops_s = buf + grp * (SPF_TILE * SPF_G2_N + SPF_G2_N * SPF_G2_N);
+  float4* rm_s = ops_s + SPF_TILE * SPF_G2_N;
+  float4* phf = buf;
+  float4* dpf = buf + SPF_TILE * SPF_G2_N;
+  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  __syncthreads();
+  const SpfDesc& d = descs[s_di];
+  const int t = (int)(blockIdx.x - d.block_start);
+  const int G = d.G, n = d.n;
+  const int g0 = t * SPF_TILE;
+  const int rows = min(SPF_TILE, G - g0);
+  cplx* o = out + d.out_offset;
+  // each thread owns up to 2 outputs (r, j1) = loc, loc + 256 of its group
+  float ah[2][2], al[2][2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) ah[u][0] = ah[u][1] = al[u][0] = al[u][1] = 0.f;
+  const int iters = (d.op_count + 1) / 2;
+  for (int it = 0; it < iters; ++it) {
+    const int q = 2 * it + grp;
+    const bool act = q < d.op_count;
+    const SpfOp* op = act ? &ops[d.op_first + q] : nullptr;
+    const int n2 = act ? op->n2 : 0;
+    __syncthreads();
+    for (int e = loc; e < rows * n2; e += 256) {
+      const int r = e % rows, j2 = e / rows;
+      const cplx v = op->ophi[g0 + r + (long long)G * j2];
+      float hx, lx, hy, ly;
+      split_d2f(v.x, hx, lx);
+      split_d2f(v.y, hy, ly);
+      ops_s[r + SPF_TILE * j2] = make_float4(hx, hy, lx, ly);
+    }
+    for (int e = loc; e < n * n2; e += 256) {
+      const cplx v = op->rm[e];
+      float hx, lx, hy, ly;
+      split_d2f(v.x, hx, lx);
+      split_d2f(v.y, hy, ly);
+      rm_s[e] = make_float4(hx, hy, lx, ly);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int e = loc + u * 256;
+      if (e >= rows * n) continue;
+      const int r = e % rows, j1 = e / rows;
+      for (int j2 = 0; j2 < n2; ++j2) {
+        const float4 x = ops_s[r + SPF_TILE * j2];
+        const float4 m = rm_s[j1 + n * j2];
+        df_fma(ah[u][0], al[u][0], x.x, x.z, m.x, m.z);
+        df_fma(ah[u][0], al[u][0], -x.y, -x.w, m.y, m.w);
+        df_fma(ah[u][1], al[u][1], x.x, x.z, m.y, m.w);
+        df_fma(ah[u][1], al[u][1], x.y, x.w, m.x, m.z);
+      }
+    }
+  }
+  if (grp == 1) {
+#pragma unroll
+    for (int u = 0; u < 2; ++u) red[loc + 256 * u] = make_float4(ah[u][0], ah[u][1], al[u][0], al[u][1]);
+  }
+  __syncthreads();   // the operator tiles are dead; red holds the second group's sums
+  if (grp == 0) {
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int e = loc + u * 256;
+      if (e >= rows * n) continue;
+      const float4 b = red[e];
+      float sh = ah[u][0], sl = al[u][0], th = ah[u][1], tl = al[u][1];
+      {
+        const float x = sh + b.x, bp = x - sh;
+        sl += ((sh - (x - bp)) + (b.x - bp)) + b.z;
+        sh = x;
+      }
+      {
+        const float x = th + b.y, bp = x - th;
+        tl += ((th - (x - bp)) + (b.y - bp)) + b.w;
+        th = x;
+      }
+      const int r = e % rows, j1 = e / rows;
+      const int g = g0 + r;
+      const cplx acc = cmul(der, mkc(f2d_exact(sh) + f2d_exact(sl), f2d_exact(th) + f2d_exact(tl)));
+      const cplx ph = d.phi[g + (long long)G * j1];
+      float4 w;
+      split_d2f(ph.x, w.x, w.z);
+      split_d2f(ph.y, w.y, w.w);
+      phf[r + SPF_TILE * j1] = w;
+      split_d2f(acc.x, w.x, w.z);
+      split_d2f(acc.y, w.y, w.w);
+      dpf[r + SPF_TILE * j1] = w;
+      o[g + (long long)G * j1] = acc;
+    }
+  }
+  __syncthreads();
+  cplx* part = d.partial + (long long)t * 2 * n * n;
+  for (int pr = threadIdx.x; pr < 2 * n * n; pr += blockDim.x) {
+    const int which = pr / (n * n), qq = pr % (n * n);
+    const int j1 = qq % n, j2 = qq / n;
+    const float4* a = phf + SPF_TILE * j1;
+    const float4* b = (which == 0 ? phf : dpf) + SPF_TILE * j2;
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int r = 0; r < rows; ++r) {
+      const float4 x = a[r], y = b[r];
+      df_fma(rh, rl, x.x, x.z, y.x, y.z);
+      df_fma(rh, rl, x.y, x.w, y.y, y.w);
+      df_fma(ih, il, x.x, x.z, y.y, y.w);
+      df_fma(ih, il, -x.y, -x.w, y.x, y.z);
+    }
+    part[pr] = mkc(f2d_exact(rh) + f2d_exact(rl), f2d_exact(ih) + f2d_exact(il));
+  }
+}
+
 // (phi^H phi) X = phi^H dphi (zposv 'U') by Gauss-Jordan elimination of [S | O]
 // without pivoting, which is stable for the Hermitian positive definite S: each of
 // the n steps is one pivot reciprocal, then one scale and one update per element
@@ -1179,12 +1302,16 @@ __global__ void __launch_bounds__(256) spf_proj_split_kernel(const SpfDesc* __re
 }
 
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
-                cplx der_factor, int* d_status, cudaStream_t st, int prec) {
+                cplx der_factor, int* d_status, cudaStream_t st, int prec, int nf) {
   if (ndesc <= 0) return;
   // both split modes: compensated (FP32 accumulation here makes the SPF error
   // estimate noisier and the adaptive SPF integration take more steps)
-  if (prec > 0) spf_tile_split_kernel<2><<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
-  else spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  if (prec > 0 && nf > 0 && nf <= SPF_G2_N)
+    spf_tile_split2_kernel<<<(unsigned)ntiles, 512, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  else if (prec > 0)
+    spf_tile_split_kernel<2><<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
+  else
+    spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   spf_solve_kernel<<<ndesc, 256, 0, st>>>(d_descs, d_status);
   if (prec > 0) spf_proj_split_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
   else spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);

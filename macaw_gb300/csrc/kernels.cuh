@@ -231,8 +231,10 @@ void launch_h1(const H1Desc* d_descs, int ndesc, int maxn2, size_t smem_bytes, b
                int prec);
 void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st);
 // prec > 0: the tile products in compensated split FP32 (spf_tile_split_kernel)
+// nf: the largest SPF count of the descriptors and their operators (<= 16: the
+// two-group split tile kernel)
 void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp* d_ops, cplx* out,
-                cplx der_factor, int* d_status, cudaStream_t st, int prec);
+                cplx der_factor, int* d_status, cudaStream_t st, int prec, int nf = 0);
 // prec > 0: compensated split-FP32 accumulation (termsum_split_kernel)
 // A sum over a whole launch fused into a streaming kernel: v the vector to dot
 // with (termsum: <v|out>; Lanczos axpy: any non-null v requests ||Kn||^2), partial
