@@ -649,8 +649,6 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
     for (int d : c.mode_dofs[m]) G *= c.ngp[d];
     c.gmode[m] = G;
   }
-  if (c.mixture && !c.modes_gwp.empty())
-    throw StatusError(MCTDH_EUNSUPPORTED, "mixtures and dissipation need DVR modes only");
   c.eps_rho = s->eps_rho;
   c.eps_ovl = s->eps_ovl;
   c.eps_C = s->eps_C;

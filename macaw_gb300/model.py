@@ -322,8 +322,6 @@ class Model:
                 raise ModelError("type-1 dissipative terms must act within one electronic state")
         if self.npackets < 1:
             raise ModelError("npackets must be at least 1")
-        if self.npackets > 1 and self.modes_gwp:
-            raise ModelError("statistical mixtures with Gaussian modes are not supported by this core")
         self.ae = np.array([term.coeff for term in self.terms], dtype=np.complex128)
         self.lhs_el = np.array([term.lhs for term in self.terms], dtype=np.int64)
         self.rhs_el = np.array([term.rhs for term in self.terms], dtype=np.int64)
@@ -543,6 +541,32 @@ def initial_wavefunction(model: Model) -> Tuple[np.ndarray, np.ndarray]:
     return initial_coefficients(model, psi), psi
 
 
+def gaussian_overlap(a1: np.ndarray, a2: np.ndarray, xi1: np.ndarray, xi2: np.ndarray) -> complex:
+    """<g1|g2> of normalised multi-dimensional Gaussians g = N exp(sum_k a_k x_k^2 + xi_k x_k)
+    with real widths a < 0 (GauOvlMultiD, gmctdh_objects.f90:1497-1519): per dimension
+    the Gaussian integral exp((conj(xi1) + xi2)^2 / (-4 (a1 + a2))) times the norms."""
+    c = np.sum(xi1.real ** 2 / a1 + xi2.real ** 2 / a2 - (np.conj(xi1) + xi2) ** 2 / (a1 + a2))
+    d = math.sqrt(float(np.prod(4.0 * a1 * a2 / (a1 + a2) ** 2)))
+    return complex(np.exp(0.25 * c) * math.sqrt(d))
+
+
+def spf_overlap(model: Model, psi: np.ndarray, m: int, s: int) -> np.ndarray:
+    """phi^H phi of the SPFs of mode m, state s: grid SPFs by their columns,
+    Gaussian SPFs by gaussian_overlap of their parameters (widths model.gwpa)."""
+    blk = model.spf_block(psi, m, s)
+    if not model.is_gwp_mode[m]:
+        return blk.conj().T @ blk
+    i = model.modes_gwp.index(m)
+    nmd, ns = blk.shape
+    a = model.gwpa[:nmd, :ns, i]
+    S = np.eye(ns, dtype=np.complex128)
+    for j1 in range(ns):
+        for j2 in range(ns):
+            if j1 != j2:
+                S[j1, j2] = gaussian_overlap(a[:, j1], a[:, j2], blk[:, j1], blk[:, j2])
+    return S
+
+
 def initial_coefficients(model: Model, psi: np.ndarray) -> np.ndarray:
     """Coefficients of the initial mixture, packet-major (APacketOffset(W) =
     W * nAConftot).  'el' line (init_calc.f90:490-500): packet W (0-based) has the
@@ -574,7 +598,8 @@ def initial_coefficients(model: Model, psi: np.ndarray) -> np.ndarray:
             A[W * n + int(model.astate_offset[s]) + idx] = coef
     if P == 1:
         return A
-    # SPF overlap matrices (DVR modes): <A_i|A_j> = sum_s A_i,s^H (x_m S_m) A_j,s
+    # <A_i|A_j> = sum_s A_i,s^H (x_m S_m) A_j,s with the SPF overlap matrices S_m
+    # (WF_Ovl, gmctdh_objects.f90:101-180)
     Amat = A.reshape((n, P), order="F")
     ovl = np.zeros((P, P), dtype=np.complex128)
     for s in range(model.nstates):
@@ -583,8 +608,7 @@ def initial_coefficients(model: Model, psi: np.ndarray) -> np.ndarray:
         for j in range(P):
             Y = Amat[o:o + ns, j].reshape(shape, order="F")
             for m in range(model.nmodes):
-                phi = model.spf_block(psi, m, s)
-                Y = np.moveaxis(np.tensordot(phi.conj().T @ phi, Y, axes=([1], [m])), 0, m)
+                Y = np.moveaxis(np.tensordot(spf_overlap(model, psi, m, s), Y, axes=([1], [m])), 0, m)
             y = Y.reshape(-1, order="F")
             for i in range(P):
                 ovl[i, j] += np.vdot(Amat[o:o + ns, i], y)

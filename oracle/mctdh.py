@@ -699,27 +699,31 @@ class Oracle:
                 x = std_reg_sol(self.Cmat[(i, s)], self.Yvec[(i, s)], md.eps_C, "tikh")
                 o = int(md.ipsispf[mode, s])
                 dpsi[o:o + len(x)] = md.der_factor * x
-        # S^-1 and tau on the coefficients (derivatives.f90:177-235)
+        # S^-1 and tau on the coefficients of every packet (derivatives.f90:177-235)
         dA = np.zeros_like(adot)
-        for s in range(md.nstates):
-            o = int(md.astate_offset[s])
-            n = int(md.naconf[s])
-            shape = tuple(int(x) for x in md.nspf[:, s])
-            X = adot[o:o + n].reshape(shape, order="F")
-            for i, mode in enumerate(md.modes_gwp):
-                js = s if md.multiset[mode] else 0
-                X = mode_product(self.S00m1[(i, js)], X, mode)
-            A0 = md.a_state(A, s)
-            for i, mode in enumerate(md.modes_gwp):
-                js = s if md.multiset[mode] else 0
-                nmd = len(md.mode_dofs[mode])
-                ns = int(md.nspf[mode, s])
-                op = int(md.ipsispf[mode, s])
-                dxi = dpsi[op:op + nmd * ns].reshape((nmd, ns), order="F")
-                xi = psi[op:op + nmd * ns].reshape((nmd, ns), order="F")
-                tau = self._gwp_tau(i, js, xi, dxi)
-                X = X - mode_product(tau, A0, mode)
-            dA[o:o + n] = X.reshape(-1, order="F")
+        nA = md.naconftot
+        for W in range(md.npackets):
+            for s in range(md.nstates):
+                o = W * nA + int(md.astate_offset[s])
+                n = int(md.naconf[s])
+                shape = tuple(int(x) for x in md.nspf[:, s])
+                X = adot[o:o + n].reshape(shape, order="F")
+                for i, mode in enumerate(md.modes_gwp):
+                    js = s if md.multiset[mode] else 0
+                    X = mode_product(self.S00m1[(i, js)], X, mode)
+                A0 = A[o:o + n].reshape(shape, order="F")
+                for i, mode in enumerate(md.modes_gwp):
+                    js = s if md.multiset[mode] else 0
+                    nmd = len(md.mode_dofs[mode])
+                    ns = int(md.nspf[mode, s])
+                    op = int(md.ipsispf[mode, s])
+                    dxi = dpsi[op:op + nmd * ns].reshape((nmd, ns), order="F")
+                    xi = psi[op:op + nmd * ns].reshape((nmd, ns), order="F")
+                    tau = self._gwp_tau(i, js, xi, dxi)
+                    X = X - mode_product(tau, A0, mode)
+                dA[o:o + n] = X.reshape(-1, order="F")
+        if md.npackets > 1:
+            dA = self.apply_multipliers(A, dA)                  # derivatives.f90:238-242
         return dA, dpsi
 
     # ---------------- norms and overlaps ----------------

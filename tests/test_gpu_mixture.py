@@ -165,3 +165,34 @@ def test_mixture_relaxation_and_packets_block(core_cls):
     model.init_packets = [(1, (0, 0, 0, 0, 0), 0.8 + 0.0j), (0, (1, 0, 0, 0, 0), 0.6j)]
     model.finalize()
     _free_running(core_cls, model)
+
+
+def _gmodel(P=3, **kw):
+    from tests.helpers import small_gmctdh
+    return with_mixture(small_gmctdh(**kw), npackets=P, eps_pop=1e-3)
+
+
+def test_gaussian_mixture_derivs(core_cls):
+    """A dissipative mixture over grid modes and a Gaussian mode: S^-1 and tau act on
+    every packet (derivatives.f90:177-235), WPpop carries the Gaussian overlaps."""
+    model = _gmodel(3)
+    A, psi = initial_wavefunction(model)
+    orc = Oracle(model)
+    gpu = core_cls(model)
+    for scale in (0.0, 0.04):
+        if scale:
+            dA, dpsi = orc.calc_derivs(A, psi, 0.0)
+            A2, p2 = A + scale * dA, psi + scale * dpsi
+        else:
+            A2, p2 = A, psi
+        rA, rp = orc.calc_derivs(A2, p2, 0.0)
+        gA, gp = gpu.calc_derivs(A2, p2, 0.0)
+        assert _rel(gA, rA) < 1e-10
+        assert _rel(gp, rp) < 1e-10
+
+
+def test_gaussian_mixture_propagation(core_cls):
+    model = _gmodel(3, tfinal_fs=0.5, eps_int=1e-6)
+    model.tout = 0.25 / AU2FS
+    model.finalize()
+    _free_running(core_cls, model)
