@@ -245,6 +245,53 @@ def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mf
                       eom=c1["eom"] - c0["eom"], hb=c1["hb"] - c0["hb"], launches=c1["launches"] - c0["launches"])
 
 
+def run_size_scan(args):
+    """qvc12n: the benchmark model with `--nspf` SPFs per mode and state (12: 2.99 M
+    configurations per state, 143 MB of coefficients, beyond the 129 MB L2), split
+    path against the FP64 path from the same state at 1 fs, as the benchmark line
+    does (no learned extrapolator, no CPU baseline)."""
+    import torch
+    from macaw_gb300.capi import GpuCore
+    _, _, tdist = dist_setup()
+    torch.cuda.init()
+    model = qvc12(nspf=args.nspf, eps_int=EPS_CMF, eps_lanczos=1e-8, eps_spf=1e-7)
+    A0, psi0 = initial_wavefunction(model)
+    l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    pre = GpuCore(model, precision=0)
+    pre.set_state(A0, psi0, as_start=True)
+    t1, h1, _, _, _ = pre.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
+    A1, psi1 = pre.get_state()
+    pre.close()
+    state = (A0, psi0, A1, psi1)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ref_core, ref = run_arm(model, 0, state, t1, h1, args, l2, torch, tdist, profile=False)
+        mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=False)
+    cmp = {}
+    for name, core in (("fp64", ref_core), ("mixed", mix_core)):
+        core.set_state(A1, psi1, as_start=False)
+        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + ACC_FS / AU2FS, t1, h1)
+        cmp[name] = core.observables(tt)
+    value = mix["fs"] / (mix["ms"] * 1e-3)
+    fp64_value = ref["fs"] / (ref["ms"] * 1e-3)
+    ntot = int(model.naconftot)
+    line = {"metric": f"simulated fs/s (qvc12, {args.nspf} SPFs, CMF2)", "value": value, "unit": "fs/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mix["ms"] / args.steps,
+            "higher_is_better": True, "precision": args.precision,
+            "fp64_path": {"value": fp64_value, "ms_per_step": ref["ms"] / args.steps},
+            "speedup_vs_fp64_path": value / fp64_value,
+            "accuracy_vs_fp64_path": {"dC": abs(cmp["mixed"]["auto"] - cmp["fp64"]["auto"]),
+                                      "dpop": float(np.abs(cmp["mixed"]["pop"] - cmp["fp64"]["pop"]).max()),
+                                      "over_fs": ACC_FS, "from_fs": PRE_FS},
+            "eom_per_s": mix["eom"] / (mix["ms"] * 1e-3), "hb_per_s": mix["hb"] / (mix["ms"] * 1e-3),
+            "fp64_eom_per_s": ref["eom"] / (ref["ms"] * 1e-3),
+            "clocks": clk.summary(),
+            "config": {"workload": "qvc12n", "nspf": args.nspf, "coefficients": ntot,
+                       "coefficient_bytes": 16 * ntot, "dimpsi": int(model.dimpsi),
+                       "l2": "flushed (256 MB write) before every timed step"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_gpu(args):
     import torch
     from macaw_gb300.capi import GpuCore, fp64_peak_tflops
@@ -552,10 +599,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
-    ap.add_argument("--workload", default="qvc12", choices=["qvc12", "ensemble", "lvc5", "gmctdh16", "lvc5mix"],
+    ap.add_argument("--workload", default="qvc12",
+                    choices=["qvc12", "qvc12n", "ensemble", "lvc5", "gmctdh16", "lvc5mix"],
                     help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement; "
                          "lvc5 / gmctdh16: RK configurations")
     ap.add_argument("--rk-fs", type=float, default=0.5)
+    ap.add_argument("--nspf", type=int, default=12, help="qvc12n: SPFs per mode and state")
     ap.add_argument("--members", type=int, default=128)
     ap.add_argument("--max-conf", type=int, default=1 << 14)
     ap.add_argument("--ens-fs", type=float, default=0.5)
@@ -569,6 +618,8 @@ def main():
         return run_profile_case(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "qvc12n":
+        return run_size_scan(args)
     if args.workload in ("lvc5", "gmctdh16", "lvc5mix"):
         return run_rk_workload(args)
     if args.impl == "reference":
