@@ -285,6 +285,7 @@ def run_size_scan(args):
             "eom_per_s": mix["eom"] / (mix["ms"] * 1e-3), "hb_per_s": mix["hb"] / (mix["ms"] * 1e-3),
             "fp64_eom_per_s": ref["eom"] / (ref["ms"] * 1e-3),
             "clocks": clk.summary(),
+            "device_bytes": {"fp64": ref_core.device_bytes(), "split": mix_core.device_bytes()},
             "config": {"workload": "qvc12n", "nspf": args.nspf, "coefficients": ntot,
                        "coefficient_bytes": 16 * ntot, "dimpsi": int(model.dimpsi),
                        "l2": "flushed (256 MB write) before every timed step"}}

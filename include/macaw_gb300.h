@@ -185,6 +185,11 @@ int64_t mctdh_observables(mctdh_ctx_t *ctx, double t, double *energy, double *po
  *   errors ggp, poperr(ns00max, nmodgwp, nstates) (output.f90:88-140); ggp/poperr may be NULL;
  * - mctdh_densmat: the reduced density matrix rho(mode, state) as written to the densmat
  *   file (output.f90:276-300), n x n interleaved complex, both triangles filled. */
+/* Device memory the context holds (state vectors, stage and Krylov vectors, every
+ * planned intermediate, descriptors), in bytes.  The batched plan keeps all chain
+ * intermediates of one EOM alive, so this grows with terms x modes x configurations. */
+int64_t mctdh_device_bytes(mctdh_ctx_t *ctx, int64_t *bytes);
+
 /* Packet populations of the resident mixture as written by WriteOutput
  * (output.f90:44-60): WPpop normalised to unit sum and sorted decreasing
  * (npackets values), and the entropy -sum p ln p / ln npackets over p >= 1e-8

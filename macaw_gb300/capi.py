@@ -81,6 +81,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_norm_wf.argtypes = [vp, DP, DP, DP]
     lib.mctdh_expect.argtypes = [vp, DP]
     lib.mctdh_packets.argtypes = [vp, DP, DP]
+    lib.mctdh_device_bytes.argtypes = [vp, I64P]
     lib.mctdh_natpop.argtypes = [vp, DP, DP, DP]
     lib.mctdh_densmat.argtypes = [vp, C.c_int64, C.c_int64, DP]
     lib.mctdh_density.argtypes = [vp, C.c_int64, DP, C.c_int64, C.c_double, C.c_double, DP, DP]
@@ -139,7 +140,7 @@ def load_library() -> C.CDLL:
                  "mctdh_rk_attempt", "mctdh_cmf2_attempt",
                  "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
                  "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_step",
-                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets",
+                 "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets", "mctdh_device_bytes",
                  "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
                  "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc"):
         getattr(lib, name).restype = C.c_int64
@@ -151,7 +152,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_rk_attempt", "mctdh_cmf2_attempt",
             "mctdh_set_state", "mctdh_get_state", "mctdh_propagate", "mctdh_observables",
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
-            "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets",
+            "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets", "mctdh_device_bytes",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
@@ -393,6 +394,12 @@ class GpuCore:
     def set_state(self, A, psi, as_start: bool = True):
         A, psi = _cbuf(A), _cbuf(psi)
         self._check(self.lib.mctdh_set_state(self.h, _ptr(A), _ptr(psi), 1 if as_start else 0))
+
+    def device_bytes(self) -> int:
+        """Device memory held by the context (bytes)."""
+        b = C.c_int64()
+        self._check(self.lib.mctdh_device_bytes(self.h, C.byref(b)))
+        return int(b.value)
 
     def packets(self):
         """Packet populations (normalised, decreasing) and the entropy of the

@@ -4741,6 +4741,12 @@ int64_t mctdh_norm_wf(mctdh_ctx_t* ctx, const double* A, const double* psi, doub
   });
 }
 
+int64_t mctdh_device_bytes(mctdh_ctx_t* ctx, int64_t* bytes) {
+  if (!ctx || !bytes) return MCTDH_EARG;
+  *bytes = (int64_t)ctx->c->ar.total;
+  return MCTDH_OK;
+}
+
 int64_t mctdh_packets(mctdh_ctx_t* ctx, double* wppop, double* entropy) {
   if (!ctx || !wppop) return MCTDH_EARG;
   Ctx* c = ctx->c;

@@ -107,6 +107,7 @@ def test_mixture_propagation(core_cls):
         assert np.abs(g["pop"] - r["pop"]).max() < 10 * model.eps_int
         assert abs(g["norm"] - 1.0) < 1e-6
         assert abs(g["energy"] - r["energy"]) < 10 * model.eps_int
+    assert gpu.device_bytes() > 0
     Af, pf = gpu.get_state()
     w, ent = gpu.packets()
     ro = orc.observables(Af, pf, A, psi, model.tfinal)
