@@ -1689,12 +1689,16 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only) 
     cplx* cur[3] = {a1, a2, a2};
     int curfmt[3] = {TF_C64, TF_C64, TF_C64};
     const int cfmt = prec ? TF_SPLIT : TF_C64;
+    // each chain alternates between two buffers (depth i reads i - 1's output)
+    cplx* pp[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     for (size_t i = 0; i < order.size(); ++i) {
       const int m = order[i];
       const int n = sh[m];
       cplx* mats[3] = {S[m][s].s11, S[m][s].s22, S[m][s].s12};
       for (int q = 0; q < (norm_only ? 1 : 3); ++q) {
-        cplx* out = c.ar.calloc_c(N);
+        cplx*& buf = pp[q][i & 1];
+        if (!buf) buf = c.ar.calloc_c(N);
+        cplx* out = buf;
         P.chain[i + 1].add(cur[q], out, mats[q], n, 0, sh, m, n, mkc(1, 0), 0, curfmt[q], cfmt);
         cur[q] = out;
         curfmt[q] = cfmt;
