@@ -197,3 +197,47 @@ def test_gaussian_mixture_propagation(core_cls):
     model.tout = 0.25 / AU2FS
     model.finalize()
     _free_running(core_cls, model)
+
+
+def test_mixture_setup_errors(core_cls):
+    """Bad mixture set-up fields are refused at mctdh_create with a status, and the
+    device stays usable: a term kind outside 0..2 (-7), a type-1 term without its
+    operator (-7), a type-1 term between two states (-1), more than 16 packets (-1)."""
+    import ctypes as C
+    from macaw_gb300.capi import build_setup, load_library
+    lib = load_library()
+    model = _model(2, "both")
+
+    def create(mutate):
+        s, keep = build_setup(model, 0)
+        keep.append(mutate(s))
+        h = C.c_void_p()
+        rc = lib.mctdh_create(C.byref(s), C.byref(h))
+        if rc == 0:
+            lib.mctdh_destroy(h)
+        return rc
+
+    def kinds(s, values):
+        arr = np.array(values, dtype=np.int64)
+        s.term_kind = arr.ctypes.data_as(C.POINTER(C.c_int64))
+        return arr
+
+    assert create(lambda s: None) == 0
+    s0, _ = build_setup(model, 0)
+    n = s0.nham
+    base = [s0.term_kind[i] for i in range(n)]
+    assert create(lambda s: kinds(s, [5] + base[1:])) == -7
+    k1 = base.index(1)
+    assert create(lambda s: setattr(s, "ndiss1", 0)) == -7
+
+    def cross_state(s):
+        lhs = np.array([s.lhs_el[i] for i in range(n)], dtype=np.int64)
+        lhs[k1] = 1 - lhs[k1]
+        s.lhs_el = lhs.ctypes.data_as(C.POINTER(C.c_int64))
+        return lhs
+    assert create(cross_state) == -1
+    assert create(lambda s: setattr(s, "npackets", 17)) == -1
+    # still usable
+    A, psi = initial_wavefunction(model)
+    dA, _ = core_cls(model).calc_derivs(A, psi, 0.0)
+    assert np.isfinite(dA).all()
