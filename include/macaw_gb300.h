@@ -79,8 +79,9 @@ typedef struct mctdh_setup {
    * aeExtra, term_diss1 = its operator, diss1_ae = aeD1 = alpha / 2) and 2 for a term
    * of a type-2 operator beta (W rho + rho W^+) (ae = i aeD2 aeExtra, aeD2 = beta).
    * term_kind NULL: every term is Hamiltonian.  Mixtures (up to 16 packets) and
-   * dissipation (up to 4 type-1 operators, state-diagonal terms) run with the
-   * derivative-based integrators; CMF2 returns -1 for them. */
+   * dissipation (up to 4 type-1 operators; a type-1 term between two states needs
+   * equal SPF counts in both) run with the derivative-based integrators; CMF2
+   * returns -1 for them. */
   int64_t npackets;              /* npackets, 0 or 1 for a single wave packet            */
   double eps_pop;                /* eps_pop (0: the reference's default 1e-6)            */
   const int64_t *term_kind;      /* (nham) 0 Hamiltonian, 1 type-1, 2 type-2, or NULL    */

@@ -610,7 +610,9 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
         const int k = s->term_diss1 ? (int)s->term_diss1[t] : -1;
         if (k < 0 || k >= c.ndiss1) throw StatusError(MCTDH_EARG, "term_diss1 out of range");
         if (c.lhs[t] != c.rhs[t])
-          throw StatusError(MCTDH_EUNSUPPORTED, "type-1 dissipative terms must act within one electronic state");
+          for (int m = 0; m < c.nmodes; ++m)
+            if (c.m_of(m, c.lhs[t]) != c.m_of(m, c.rhs[t]))
+              throw StatusError(MCTDH_EUNSUPPORTED, "type-1 terms between states need equal SPF counts");
         c.diss1_of[t] = k;
       }
     }
@@ -1169,7 +1171,7 @@ void plan_eom(Ctx& c) {
     int lmax = 0;
     for (int im = 0; im < f; ++im)
       if (!c.is_identity[im + f * c.ioper[im + f * t]]) lmax = im;
-    if (leader >= 0) lmax = 0;
+    if (leader >= 0 || c.kind[t] == 1) lmax = 0;
     std::vector<TRef> R(f + 1), L(f);
     R[0].p = c.d_in + c.aoff[s2];
     R[0].shape = c.shape_of(s2);
@@ -1206,25 +1208,49 @@ void plan_eom(Ctx& c) {
       L[i].fmt = chain_fmt;
     }
     if (c.kind[t] == 1) {
-      // V_k A = sum_t ae_t V_t A (no der_factor) and the mean fields
-      // ae_t <A| V_t^(not im) AuxA_k> (gmctdh_objects.f90:694-744, every h1mode of a
-      // same-state term being Hermitian)
+      // V_k A = sum_t ae_t V_t A (no der_factor), and the mean fields of
+      // gmctdh_objects.f90:694-744: ae_t <V_t^(not im) A_s2 | AuxA_k,s1> over the packets,
+      // an (nSPF(s2) x nSPF(s1)) matrix added into the operator's mean field (equal
+      // counts).  The operators of the modes below im act on A_s2 (P chain), those
+      // above im act adjoint on AuxA_s1 (Q chain): <h_< h_> A | Y> = <h_< A | h_>^H Y>.
       const int k1 = c.diss1_of[t];
       srcs1[k1][s1].push_back(SumSrc{R[f].p, c.ae[t], R[f].fmt});
-      int imin = f;
+      int imin = f, imax = -1;
       for (int im = 0; im < f; ++im)
-        if (!c.is_identity[im + f * c.ioper[im + f * t]]) imin = std::min(imin, im);
-      std::vector<TRef> Q(f);
-      Q[0].p = c.pk_aux + (long long)k1 * c.naconftot + c.aoff[s2];
-      Q[0].shape = c.shape_of(s2);
+        if (!c.is_identity[im + f * c.ioper[im + f * t]]) {
+          imin = std::min(imin, im);
+          imax = im;
+        }
+      std::vector<TRef> Pc(f), Q(f);
+      Pc[0].p = c.d_in + c.aoff[s2];
+      Pc[0].shape = c.shape_of(s2);
+      for (int i = 1; i <= imax; ++i) {
+        const int m = i - 1;
+        if (c.skip_term[m + f * t]) { Pc[i] = Pc[i - 1]; continue; }
+        const int k = c.ioper[m + f * t];
+        const int n1 = c.m_of(m, s1);
+        std::vector<int> ns = Pc[i - 1].shape;
+        ns[m] = n1;
+        cplx* out = c.ar.calloc_c(prod_range(ns, 0, (int)ns.size()));
+        const auto in = prod_in(Pc[i - 1], s2);
+        c.chains[i].add(in.first, out, c.hmat[m][k], n1, 0, Pc[i - 1].shape, m, n1, mkc(1, 0), 0, in.second,
+                        chain_fmt);
+        Pc[i].p = out;
+        Pc[i].shape = ns;
+        Pc[i].fmt = chain_fmt;
+      }
+      Q[0].p = c.pk_aux + (long long)k1 * c.naconftot + c.aoff[s1];
+      Q[0].shape = c.shape_of(s1);
       for (int i = 1; i <= f - 1 - imin; ++i) {
         const int jm = f - i;
         if (c.skip_term[jm + f * t]) { Q[i] = Q[i - 1]; continue; }
         const int k = c.ioper[jm + f * t];
+        const int n1 = c.m_of(jm, s1), n2 = c.m_of(jm, s2);
         std::vector<int> ns = Q[i - 1].shape;
+        ns[jm] = n2;
         cplx* out = c.ar.calloc_c(prod_range(ns, 0, (int)ns.size()));
         if ((int)c.aux_chains.size() <= i) c.aux_chains.resize(i + 1);
-        c.aux_chains[i].add(Q[i - 1].p, out, c.hmat[jm][k], ns[jm], 0, Q[i - 1].shape, jm, ns[jm], mkc(1, 0), 0,
+        c.aux_chains[i].add(Q[i - 1].p, out, c.hmat[jm][k], n1, 1, Q[i - 1].shape, jm, n2, mkc(1, 0), 0,
                             Q[i - 1].fmt, chain_fmt);
         Q[i].p = out;
         Q[i].shape = ns;
@@ -1233,7 +1259,7 @@ void plan_eom(Ctx& c) {
       for (int im = 0; im < f; ++im) {
         const int k = c.ioper[im + f * t];
         if (c.is_identity[im + f * k]) continue;
-        const TRef& X = L[im];
+        const TRef& X = Pc[im];
         const TRef& Y = Q[f - 1 - im];
         long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, (int)X.shape.size());
         int hidx = c.aux_holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im], X.fmt, Y.fmt);

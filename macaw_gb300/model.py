@@ -318,8 +318,14 @@ class Model:
         for ty, _, dterms in self.dissipation:
             if ty not in (1, 2):
                 raise ModelError(f"dissipation type {ty} is not supported (1: V rho V^+, 2: W rho + rho W^+)")
-            if ty == 1 and any(term.lhs != term.rhs for term in dterms):
-                raise ModelError("type-1 dissipative terms must act within one electronic state")
+            for term in dterms:
+                # between two states the reference adds the (nSPF(rhs) x nSPF(lhs)) contraction
+                # into the operator's (lhs x rhs) mean field (gmctdh_objects.f90:726-741):
+                # defined for equal SPF counts on the multi-set modes
+                if ty == 1 and term.lhs != term.rhs and any(
+                        self.multiset[m] and self.nspf[m, term.lhs] != self.nspf[m, term.rhs]
+                        for m in range(self.nmodes)):
+                    raise ModelError("type-1 terms between states need equal SPF counts in both states")
         if self.npackets < 1:
             raise ModelError("npackets must be at least 1")
         self.ae = np.array([term.coeff for term in self.terms], dtype=np.complex128)

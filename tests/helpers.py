@@ -105,3 +105,14 @@ def random_mixture(model, seed=0, pops=None):
     pops = pops / pops.sum()
     A = (q * np.sqrt(pops)[None, :]).reshape(-1, order="F")
     return A, psi
+
+
+def with_decay(model, npackets=2, gamma=0.05, eps_pop=1e-6):
+    """The model as a mixture under electronic decay L = sqrt(gamma) |1><2|:
+    gamma L rho L^+ as a type-1 term between the states and -gamma/2 {|2><2|, rho}
+    as a type-2 term (state indices 0-based: |0><1| and |1><1|)."""
+    from macaw_gb300.model import Term
+    model.npackets = npackets
+    model.eps_pop = eps_pop
+    model.dissipation = [(1, gamma, [Term(1.0, 0, 1, {})]), (2, -0.5 * gamma, [Term(1.0, 1, 1, {})])]
+    return model.finalize()

@@ -202,7 +202,8 @@ def test_gaussian_mixture_propagation(core_cls):
 def test_mixture_setup_errors(core_cls):
     """Bad mixture set-up fields are refused at mctdh_create with a status, and the
     device stays usable: a term kind outside 0..2 (-7), a type-1 term without its
-    operator (-7), a type-1 term between two states (-1), more than 16 packets (-1)."""
+    operator (-7), more than 4 type-1 operators (-1), more than 16 packets (-1); a
+    type-1 term between two states with equal SPF counts is admitted."""
     import ctypes as C
     from macaw_gb300.capi import build_setup, load_library
     lib = load_library()
@@ -235,9 +236,24 @@ def test_mixture_setup_errors(core_cls):
         lhs[k1] = 1 - lhs[k1]
         s.lhs_el = lhs.ctypes.data_as(C.POINTER(C.c_int64))
         return lhs
-    assert create(cross_state) == -1
+    assert create(cross_state) == 0          # equal SPF counts: admitted (a decay channel)
+    assert create(lambda s: setattr(s, "ndiss1", 5)) == -1
     assert create(lambda s: setattr(s, "npackets", 17)) == -1
     # still usable
     A, psi = initial_wavefunction(model)
     dA, _ = core_cls(model).calc_derivs(A, psi, 0.0)
     assert np.isfinite(dA).all()
+
+
+@pytest.mark.parametrize("P,prec,tol", [(3, 0, EOM_RTOL), (1, 0, EOM_RTOL), (3, 1, 1e-6)])
+def test_decay_channel_derivs(core_cls, P, prec, tol):
+    """Electronic decay L = sqrt(gamma)|1><2|: a type-1 term between the states
+    (mean field <V^(not m) A_rhs | AuxA_lhs> added into the operator's slot,
+    gmctdh_objects.f90:696-741) and the type-2 anticommutator."""
+    from tests.helpers import with_decay
+    model = with_decay(small_lvc(nspf=3, grid=(8, 7, 6, 6, 7)), npackets=P, gamma=0.05)
+    A, psi = random_mixture(model, seed=21)
+    rA, rp = Oracle(model).calc_derivs(A, psi, 0.1)
+    dA, dpsi = core_cls(model, precision=prec).calc_derivs(A, psi, 0.1)
+    assert _rel(dA, rA) < tol
+    assert _rel(dpsi, rp) < tol

@@ -115,6 +115,32 @@ def test_mixture_input_is_parsed(tmp_path):
     assert abs(np.vdot(A, A).real - 1.0) < 1e-14
     assert abs(np.vdot(A[:n], A[n:])) < 1e-15
     bad = with_mixture(_lvc(), npackets=1, diss=False)
-    bad.dissipation = [(1, 0.1, [Term(1.0, 0, 1, {0: 1})])]
+    bad.dissipation = [(3, 0.1, [Term(1.0, 0, 0, {0: 1})])]
     with pytest.raises(ModelError):
         bad.finalize()
+
+
+def test_decay_channel_between_states():
+    """Electronic decay as a type-1 term between the states (L = sqrt(gamma)|1><2|)
+    plus its type-2 anticommutator on a 3-packet mixture: the multipliers keep the
+    trace, and state 1 gains population (gamma sum_W WPpopm1_W |<A_W|V A_j>|^2 (1 - p_1)
+    + gamma p_1 p_2 > 0 after the diagonal multiplier).  A single packet has no
+    multipliers in the reference (derivatives.f90:238), and its type-1 term is the
+    projection |<Psi|V|Psi>|^2, so decay needs a mixture."""
+    from tests.helpers import with_decay
+    P = 3
+    model = with_decay(_lvc(), npackets=P, gamma=0.05)
+    A, psi = random_mixture(model, seed=9)
+    dA, _ = Oracle(model).calc_derivs(A, psi, 0.0)
+    n = model.naconftot
+    Am, dAm = A.reshape((n, P), order="F"), dA.reshape((n, P), order="F")
+    dtrace = float(np.real(np.trace(dAm.conj().T @ Am + Am.conj().T @ dAm)))
+    assert abs(dtrace) < 1e-12 * np.abs(dAm).max()
+    ref = _lvc()
+    ref.npackets = P
+    ref.finalize()
+    dA0, _ = Oracle(ref).calc_derivs(A, psi, 0.0)
+    d0 = (dA - dA0).reshape((n, P), order="F")
+    o0, n0 = int(model.astate_offset[0]), int(model.naconf[0])
+    gain0 = 2.0 * float(np.real(np.sum(Am[o0:o0 + n0].conj() * d0[o0:o0 + n0])))
+    assert gain0 > 0.0
