@@ -1297,7 +1297,7 @@ void plan_eom(Ctx& c) {
     md.count = (int)kv.second.size();
     for (auto& x : kv.second) c.msum_src_h.push_back(x);
     c.msum_h.push_back(md);
-    c.gmat[kv.first] = md.out;
+    if (kd == 0) c.gmat[kv.first] = md.out;   // H_B of CMF2 takes the Hamiltonian's operators only
     std::vector<int> sh = c.shape_of(s);
     cplx* out = c.ar.calloc_c(prod_range(sh, 0, (int)sh.size()));
     const int gfmt = c.precision == 1 ? TF_F32 : chain_fmt;   // FP32 products in precision 1
