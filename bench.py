@@ -129,6 +129,17 @@ def barrier(tdist):
         tdist.barrier()
 
 
+def max_over_ranks(vals, tdist, device="cuda"):
+    """Each value's maximum over the ranks (the slowest rank's time); the values
+    themselves without a process group."""
+    if tdist is None:
+        return [float(v) for v in vals]
+    import torch
+    t = torch.tensor([float(v) for v in vals], device=device, dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
 def flush_l2(buf):
     buf.add_(1.0)
 
@@ -332,14 +343,7 @@ def run_gpu(args):
     dpop = float(np.abs(cmp["mixed"]["pop"] - cmp["fp64"]["pop"]).max())
     mfx_stats = mfx_core.mfx_stats()
     ms_total, fs_total = mix["ms"], mix["fs"]
-    if tdist is not None:
-        tt = torch.tensor([ms_total, ref["ms"]], device="cuda", dtype=torch.float64)
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        ms_total, ref["ms"] = float(tt[0].item()), float(tt[1].item())
-    if tdist is not None:
-        tt = torch.tensor([mfxr["ms"]], device="cuda", dtype=torch.float64)
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        mfxr["ms"] = float(tt[0].item())
+    ms_total, ref["ms"], mfxr["ms"] = max_over_ranks([ms_total, ref["ms"], mfxr["ms"]], tdist)
     value = ws * fs_total / (ms_total * 1e-3)
     fp64_value = ws * ref["fs"] / (ref["ms"] * 1e-3)
     mfx_value = ws * mfxr["fs"] / (mfxr["ms"] * 1e-3)
