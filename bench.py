@@ -460,7 +460,9 @@ def run_profile_case(args):
                           "launches": core.launch_count()}), flush=True)
         core.close()
         return 0
-    model = make_model()
+    # `--workload qvc12n`: the same with `--nspf` SPFs
+    model = (qvc12(nspf=args.nspf, eps_int=EPS_CMF, eps_lanczos=1e-8, eps_spf=1e-7)
+             if args.workload == "qvc12n" else make_model())
     A0, psi0 = initial_wavefunction(model)
     core = GpuCore(model, precision=args.precision)
     core.set_state(A0, psi0, as_start=True)
@@ -480,7 +482,7 @@ def run_profile_case(args):
     if args.profile_from_fs > 0.0:
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
-    print(json.dumps({"profile_case": "qvc12", "precision": args.precision, "t_fs": t * AU2FS,
+    print(json.dumps({"profile_case": args.workload, "precision": args.precision, "t_fs": t * AU2FS,
                       "launches": core.launch_count() - l0}), flush=True)
     core.close()
     return 0
