@@ -144,3 +144,30 @@ def test_decay_channel_between_states():
     o0, n0 = int(model.astate_offset[0]), int(model.naconf[0])
     gain0 = 2.0 * float(np.real(np.sum(Am[o0:o0 + n0].conj() * d0[o0:o0 + n0])))
     assert gain0 > 0.0
+
+
+def test_gaussian_overlap_matches_oracle():
+    """The set-up code's Gaussian overlap (natural-state start of a Gaussian-mode
+    mixture) is the oracle's GauOvlMultiD on random widths and complex centres."""
+    from macaw_gb300.model import gaussian_overlap
+    from oracle.mctdh import gau_ovl_multid
+    rng = np.random.default_rng(4)
+    for _ in range(20):
+        d = int(rng.integers(1, 5))
+        a1, a2 = -rng.uniform(0.1, 2.0, d), -rng.uniform(0.1, 2.0, d)
+        x1 = rng.normal(size=d) + 1j * rng.normal(size=d)
+        x2 = rng.normal(size=d) + 1j * rng.normal(size=d)
+        assert abs(gaussian_overlap(a1, a2, x1, x2) - gau_ovl_multid(a1, a2, x1, x2)) < 1e-14
+
+
+def test_gaussian_mixture_start_is_orthogonal():
+    """OrthoWP with Gaussian SPFs: the packets of the 'el' start are orthogonal in
+    the full SPF metric (WF_Ovl with the Gaussian overlaps) and the trace is 1."""
+    from tests.helpers import small_gmctdh
+    model = with_mixture(small_gmctdh(), npackets=3, diss=False, eps_pop=1e-3)
+    A, psi = initial_wavefunction(model)
+    orc = Oracle(model)
+    pk = orc.packets(A)
+    S = np.array([[orc.wf_ovl(pi, psi, pj, psi) for pj in pk] for pi in pk])
+    assert abs(np.trace(S).real - 1.0) < 1e-12
+    assert np.abs(S - np.diag(np.diag(S))).max() < 1e-12
