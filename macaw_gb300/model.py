@@ -19,6 +19,7 @@ reference's column-major order with mode 1 fastest (init_calc.f90:531-536).
 from __future__ import annotations
 
 import dataclasses
+import functools
 import math
 import os
 import re
@@ -105,6 +106,14 @@ def harm_dvr(n: int, x0: float, mw: float, with_trafo: bool = False):
     if with_trafo:
         return grid, w, d1, d2, xd1, trafo
     return grid, w, d1, d2, xd1
+
+
+@functools.lru_cache(maxsize=256)
+def _dvr_cached(kind: str, n: int, a: float, b: float):
+    """One DVR per (kind, size, parameters): models and ensemble members that share
+    a grid share its construction (callers get copies)."""
+    f = harm_dvr if kind == "HO" else sin_dvr
+    return tuple(np.asarray(x) for x in f(n, a, b, True))
 
 
 def sin_dvr(n: int, xi: float, xf: float, with_trafo: bool = False):
@@ -239,10 +248,9 @@ class Model:
         self.trafo: Dict[int, np.ndarray] = {}     # trafoDVR (basis x grid)
         for d in range(self.ndof):
             t = self.dvr_type[d]
-            if t == "HO":
-                g, w, d1, d2, xd1, tr = harm_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1], True)
-            elif t == "sin":
-                g, w, d1, d2, xd1, tr = sin_dvr(self.ngp[d], self.dvrpar[d][0], self.dvrpar[d][1], True)
+            if t in ("HO", "sin"):
+                g, w, d1, d2, xd1, tr = (np.array(x) for x in _dvr_cached(t, self.ngp[d], float(self.dvrpar[d][0]),
+                                                                            float(self.dvrpar[d][1])))
             elif t == "gwp":
                 continue
             else:
