@@ -443,6 +443,58 @@ def run_gpu(args):
     return 0
 
 
+def run_accuracy(args):
+    """Accuracy of the split-precision arms against the plain FP64 path over the
+    full propagation of the benchmark model (qvc12, CMF2 at tolerance 1e-5, 200 fs
+    from the initial state): every arm propagates from t = 0 with its own step
+    control, and C(t) and the state populations are compared at every output
+    time (0.5 fs).  Reported: the largest |dC| and |dpop| over the run, their
+    values at the end, device seconds and simulated fs/s of each arm."""
+    import torch
+    from macaw_gb300.capi import GpuCore
+    torch.cuda.init()
+    model = make_model()
+    A0, psi0 = initial_wavefunction(model)
+    t_end = args.acc_fs / AU2FS
+    arms = [0] + [int(p) for p in args.acc_precisions.split(",") if p.strip()]
+    series, info = {}, {}
+    for prec in arms:
+        core = GpuCore(model, precision=prec)
+        core.set_state(A0, psi0, as_start=True)
+        t, h = 0.0, model.tout * model.eps_int
+        rows = [core.observables(t)]
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        nsteps = 0
+        while t < t_end - 1e-9:
+            t, h, ns, _, _ = core.propagate_interval(INT_CMF2, min(t + model.tout, t_end), t, h)
+            nsteps += ns
+            rows.append(core.observables(t))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        series[prec] = rows
+        info[prec] = {"wall_s": wall, "fs_per_s": args.acc_fs / wall, "steps": nsteps,
+                      "device_bytes": core.device_bytes()}
+        core.close()
+    ref = series[0]
+    out = {"workload": "accuracy: qvc12 CMF2 (tolerance 1e-5) from t = 0, outputs every "
+                       f"{model.tout * AU2FS:g} fs", "over_fs": args.acc_fs, "fp64": info[0], "arms": {}}
+    for prec in arms[1:]:
+        rows = series[prec]
+        n = min(len(rows), len(ref))
+        dC = [abs(rows[i]["auto"] - ref[i]["auto"]) for i in range(n)]
+        dpop = [float(np.abs(rows[i]["pop"] - ref[i]["pop"]).max()) for i in range(n)]
+        dE = [abs(rows[i]["energy"] - ref[i]["energy"]) for i in range(n)]
+        dN = [abs(rows[i]["norm"] - ref[i]["norm"]) for i in range(n)]
+        imax = int(np.argmax(dC))
+        out["arms"][str(prec)] = dict(info[prec], max_dC=max(dC), t_max_dC_fs=rows[imax]["t"] * AU2FS,
+                                      max_dpop=max(dpop), end_dC=dC[n - 1], end_dpop=dpop[n - 1],
+                                      max_denergy=max(dE), max_dnorm=max(dN), outputs=n,
+                                      speedup_vs_fp64_wall=info[0]["wall_s"] / info[prec]["wall_s"])
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile_case(args):
     """A short, fixed piece of the workload for profiler captures: three CMF2 steps
     of 1e-3 fs from the initial state of the qvc12 model (about 1,700 launches), or
@@ -604,10 +656,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
+    ap.add_argument("--acc-fs", type=float, default=200.0, help="accuracy: propagated interval in fs")
+    ap.add_argument("--acc-precisions", default="1,3", help="accuracy: split arms compared with FP64")
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2, 3],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
     ap.add_argument("--workload", default="qvc12",
-                    choices=["qvc12", "qvc12n", "ensemble", "lvc5", "gmctdh16", "lvc5mix"],
+                    choices=["qvc12", "qvc12n", "ensemble", "lvc5", "gmctdh16", "lvc5mix", "accuracy"],
                     help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement; "
                          "lvc5 / gmctdh16: RK configurations")
     ap.add_argument("--rk-fs", type=float, default=0.5)
@@ -625,6 +679,8 @@ def main():
         return run_profile_case(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "accuracy":
+        return run_accuracy(args)
     if args.workload == "qvc12n":
         return run_size_scan(args)
     if args.workload in ("lvc5", "gmctdh16", "lvc5mix"):

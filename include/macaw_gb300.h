@@ -3,7 +3,7 @@
  *
  * The entry points replace the equation-of-motion and integrator calls of the
  * reference's time loop (Macaw, source/propagator.f90).  A Fortran driver binds
- * them with ISO_C_BINDING; every integer that crosses the
+ * them with ISO_C_BINDING (interface blocks with bind(C)); every integer that crosses the
  * boundary is int64_t because the reference is built with -fdefault-integer-8
  * (Makefile:18), every complex is interleaved FP64 (double complex), every
  * array is column-major, and every index is 0-based (the Fortran shim subtracts 1).
@@ -88,6 +88,20 @@ typedef struct mctdh_setup {
   const int64_t *term_diss1;     /* (nham) type-1 operator of a kind-1 term (0-based)    */
   int64_t ndiss1;                /* number of type-1 operators                           */
   const double *diss1_ae;        /* aeD1(ndiss1)                                         */
+  /* Parametrised DOF operators (input.f90:950-1072; values built by alloc_h1mode,
+   * hamilton.f90:210-290): an operator code 200 + j multiplies the grid by
+   * gridOper(:, j, dof); a code -200 - j applies the projector v v^T with
+   * v = gridOper(:, j, dof) (MultTensProj, hamilton.f90:632-661).  grid_oper
+   * holds gridOper(ngpmax, nopparam, ndof) column-major (j 1-based in the codes,
+   * 0-based in the array); NULL when nopparam is 0. */
+  int64_t nopparam;
+  int64_t ngpmax;
+  const double *grid_oper;
+  /* operDVR (the sin^-2 matrix of Legendre DVRs, dvr.f90:361-530) for code -4:
+   * ngp x ngp column-major per dof at oper_dvr_off[dof] (-1 where absent);
+   * both NULL when no dof uses it. */
+  const double *oper_dvr;
+  const int64_t *oper_dvr_off;
 } mctdh_setup_t;
 
 /* Build the device context: uploads the operators, plans the batched kernels
@@ -114,7 +128,9 @@ int64_t mctdh_calc_derivs(mctdh_ctx_t *ctx, const double *A, const double *psi,
 int64_t mctdh_rkqs(mctdh_ctx_t *ctx, double *A, double *psi, double *dA, double *dpsi,
                    double t, double htry, double *hdid, double *hnext, int64_t method);
 
-/* One CMF2 step on host buffers (DVR models).
+/* One CMF2 step on host buffers (grid and Gaussian-mode models; Gaussian modes
+ * propagate B = D^H S A with D = S^-1/2 recomputed at the step start, so DD0 is
+ * not an argument; mixtures and dissipative models return -1).
  * Replaces cmf2(A0, psi0, DD0, tt, htry, hdid, hnext) -- cmf2_base.f90:47. */
 int64_t mctdh_cmf2(mctdh_ctx_t *ctx, double *A, double *psi, double t, double htry,
                    double *hdid, double *hnext);
@@ -230,11 +246,15 @@ int64_t mctdh_launch_count(mctdh_ctx_t *ctx);
  *          the contraction of Calc_rho1mode (gmctdh_objects.f90:452-457) for a grid mode
  *   stream cudaStream_t to launch on (NULL: the legacy default stream); the call
  *          returns after launching, rho is ready once the stream has run.
- * Limit: nspf[mode] <= 32.  Larger sizes, host pointers or a bad mode return -7
- * (message in mctdh_last_error(NULL)) without touching the GPU.
+ * Limit: nspf[mode] <= 32.  Larger sizes, host pointers, buffers of another
+ * GPU or a bad mode return -7 (message in mctdh_last_error(NULL)) without
+ * launching anything; a CUDA error left pending by an earlier call returns -6
+ * and is not cleared.
  * Scratch: a 2 MiB file-scope __device__ array that every GPU loading this
  * library holds until exit.  The first call on a device looks up its address
- * with cudaGetSymbolAddress (make that first call before any stream capture).
+ * with cudaGetSymbolAddress (make that first call before any stream capture);
+ * the address is cached per device, so the device must not be reset
+ * (cudaDeviceReset) while the library is loaded.
  * All calls share the array: calls that overlap on the GPU (different streams
  * without ordering) race and return wrong results.  Each call writes every
  * scratch entry it later reads, so nothing carries over between calls. */

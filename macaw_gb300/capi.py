@@ -52,6 +52,8 @@ class Setup(C.Structure):
         ("expect_rhs", I64P), ("expect_ioper", I64P),
         ("npackets", C.c_int64), ("eps_pop", C.c_double), ("term_kind", I64P), ("term_diss1", I64P),
         ("ndiss1", C.c_int64), ("diss1_ae", DP),
+        ("nopparam", C.c_int64), ("ngpmax", C.c_int64), ("grid_oper", DP),
+        ("oper_dvr", DP), ("oper_dvr_off", I64P),
     ]
 
 
@@ -306,6 +308,28 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
         s.term_diss1 = I(diss1_of)
         s.ndiss1 = len(model.diss1)
         s.diss1_ae = F(model.aeD1 if model.aeD1 else [0.0])
+    # parametrised operators: gridOper(ngpmax, nopparam, ndof), and operDVR of
+    # the Legendre dofs
+    nop = len(getattr(model, "op_params", []))
+    s.nopparam = nop
+    s.ngpmax = max(model.ngp) if model.ngp else 0
+    if nop:
+        go_arr = np.zeros((s.ngpmax, nop, nd))
+        for (d, j), v in model.grid_oper.items():
+            go_arr[:len(v), j - 1, d] = v
+        s.grid_oper = F(go_arr.reshape(-1, order="F"))
+    oper_dvr = getattr(model, "oper_dvr", {})
+    if oper_dvr:
+        parts, offs, o = [], [], 0
+        for d in range(nd):
+            if d in oper_dvr:
+                parts.append(oper_dvr[d].reshape(-1, order="F"))
+                offs.append(o)
+                o += parts[-1].size
+            else:
+                offs.append(-1)
+        s.oper_dvr = F(np.concatenate(parts))
+        s.oper_dvr_off = I(offs)
     return s, keep
 
 

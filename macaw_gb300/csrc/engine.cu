@@ -347,6 +347,7 @@ struct Ctx {
   cplx der = mkc(0, -1);
   int int_type_psi = 1;
   int precision = 0;
+  int hole_prec = 0;   // single-hole contractions: 0 FP64, 1 FP32 sums, 2 compensated FP32
   std::string last_error;
   long long launches = 0;
   long long eom_count = 0, hb_count = 0;
@@ -664,7 +665,10 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.int_order = (int)s->int_order;
   c.int_par1 = (int)s->int_par1;
   c.precision = (int)s->precision;
-  if (c.precision < 0 || c.precision > 2) throw StatusError(MCTDH_EARG, "precision must be 0, 1 or 2");
+  if (c.precision < 0 || c.precision > 3) throw StatusError(MCTDH_EARG, "precision must be 0, 1, 2 or 3");
+  // precision 3: the products of precision 1 with FP32-accumulated contractions
+  c.hole_prec = c.precision == 3 ? 1 : (c.precision ? 2 : 0);
+  if (c.precision == 3) c.precision = 1;
   if (!c.modes_gwp.empty()) {
     // Gaussian widths GWPa(maxdof, ns00max, nmodgwp) (psidef: GWPa, init_calc.f90:1020-1068)
     c.gwp_lda = c.maxdof;
@@ -710,6 +714,31 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
           kind = 2;
           v.resize(ng);
           for (int i = 0; i < ng; ++i) v[i] = mkc(code == 1 ? grid[i] : pow(grid[i], (double)code), 0.0);
+        } else if (code > 200 || code <= -200) {
+          // parametrised operators: the diagonal gridOper(:, j, dof) (MultTensDiag) or
+          // the projector v v^T built like MultTensProj's dger (hamilton.f90:632-661)
+          const int j = (code > 200 ? code : -code) - 201;
+          if (!s->grid_oper || j < 0 || j >= s->nopparam || ng > s->ngpmax)
+            throw StatusError(MCTDH_EARG, "parametrised operator " + std::to_string(code) + " has no gridOper values");
+          const double* gv = s->grid_oper + (size_t)s->ngpmax * ((size_t)j + (size_t)s->nopparam * d);
+          if (code > 200) {
+            kind = 2;
+            v.resize(ng);
+            for (int i = 0; i < ng; ++i) v[i] = mkc(gv[i], 0.0);
+          } else {
+            kind = 1;
+            v.resize((size_t)ng * ng);
+            for (int a = 0; a < ng; ++a)
+              for (int b = 0; b < ng; ++b) v[a + (size_t)ng * b] = mkc(gv[a] * gv[b], 0.0);
+          }
+        } else if (code == -4) {
+          // sin^-2 of a Legendre DVR (operDVR), applied like the other dense matrices
+          if (!s->oper_dvr || !s->oper_dvr_off || s->oper_dvr_off[d] < 0)
+            throw StatusError(MCTDH_EARG, "sin^-2 on a dof without an operDVR matrix");
+          kind = 1;
+          const double* src = s->oper_dvr + s->oper_dvr_off[d];
+          v.resize((size_t)ng * ng);
+          for (int i = 0; i < ng * ng; ++i) v[i] = mkc(src[i], 0.0);
         } else {
           throw StatusError(MCTDH_EUNSUPPORTED, "primitive operator code " + std::to_string(code) + " not supported");
         }
@@ -929,7 +958,7 @@ void plan_packets(Ctx& c, std::vector<std::vector<SumSrc>>& srcs, std::vector<st
     b.prec = c.precision;
     b.finalize(c.ar);
   }
-  c.aux_holes.prec = c.precision ? 2 : 0;
+  c.aux_holes.prec = c.hole_prec;
   c.aux_holes.finalize(c.ar);
   std::map<std::pair<int, int>, int> tg;
   for (const AuxRef& r : arefs) {
@@ -1331,10 +1360,10 @@ void plan_eom(Ctx& c) {
   }
   c.gprods.prec = c.precision;
   c.gprods.finalize(c.ar);
-  c.holes.prec = c.precision ? 2 : 0;
+  c.holes.prec = c.hole_prec;
   c.holes.finalize(c.ar);
   // density matrices: compensated split FP32 (~1e-13 relative) in the split modes
-  c.rho_holes.prec = c.precision ? 2 : 0;
+  c.rho_holes.prec = c.hole_prec;
   c.rho_holes.finalize(c.ar);
   for (auto& hr : rrefs) c.red.add_term(hr.target, c.rho_holes.h[hr.hole], hr.alpha);
   for (auto& hr : hrefs) c.red.add_term(hr.target, c.holes.h[hr.hole], hr.alpha, hr.conjT);

@@ -113,13 +113,17 @@ __global__ void noalloc_rho_finish(const cplx* __restrict__ scratch, int nblk, i
   }
 }
 
-static bool device_pointer(const void* p) {
+// True for device memory of device `dev` and for managed memory; host memory,
+// unregistered pointers and buffers of another GPU are refused (a kernel given a
+// peer buffer would fault without peer access or silently read over the link).
+static bool device_pointer(const void* p, int dev) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
+    cudaGetLastError();   // the query's own error (unregistered host pointer)
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 extern "C" int64_t mctdh_density_matrix_noalloc(const double* A, const int64_t* nspf, int64_t nmodes,
@@ -160,11 +164,22 @@ extern "C" int64_t mctdh_density_matrix_noalloc(const double* A, const int64_t* 
     mctdh_set_global_error("mctdh_density_matrix_noalloc: no usable CUDA device");
     return MCTDH_ECUDA;
   }
-  if (!device_pointer(A) || !device_pointer(rho)) {
+  // an error left by an earlier, unrelated call stays with its owner: report it
+  // without clearing it rather than taking it for a failure of this call
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    snprintf(msg, sizeof msg, "mctdh_density_matrix_noalloc: a CUDA error of an earlier call is pending: %s",
+             cudaGetErrorString(pending));
+    mctdh_set_global_error(msg);
+    return MCTDH_ECUDA;
+  }
+  if (!device_pointer(A, dev) || !device_pointer(rho, dev)) {
     mctdh_set_global_error("mctdh_density_matrix_noalloc: A and rho must be device memory of the current device");
     return MCTDH_EARG;
   }
-  // once per device, with that device current: the device address of the scratch area
+  // once per device, with that device current: the device address of the scratch
+  // area.  The cached address assumes the device is not reset (cudaDeviceReset)
+  // while the library is loaded.
   if (!g_scratch_addr[dev]) {
     cplx* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);

@@ -37,6 +37,18 @@ OP_P = -1        # p = -i d/dq
 OP_DQ2 = -2      # d^2/dq^2
 OP_QP = -3       # qp + pq
 OP_SINM2 = -4    # sin^-2 (Legendre DVR only)
+# Parametrised DOF operators (input.f90:950-1072): code 200 + j applies the
+# diagonal gridOper(:, j, dof); code -200 - j the projector v v^T with
+# v = gridOper(:, j, dof) (MultTensProj, hamilton.f90:632-661); j is 1-based
+# in the order the operator files declare them.
+OP_PARAM = 200
+PAR_GAU = 0        # exp(p1 x + p2 x^2)
+PAR_INTERP = 1     # cubic spline through the points of a data file
+PAR_SQUARE = 2     # indicator of |x - p1| < p2 / 2
+PAR_HERMITE = 3    # x^r exp(p1 x + p2 x^2), r = p3
+PAR_SIN = 4        # sin(p1 x)^p2
+PAR_COS = 5        # cos(p1 x)^p2
+PAR_EIGPROJ = 6    # eigenfunction p3 of -p2 d^2/dx^2 + V(x), V splined from a data file
 
 INT_RK45 = 1     # Cash-Karp (input.f90:280-282)
 INT_DOPRI = 2    # Dormand-Prince (input.f90:283-285)
@@ -112,6 +124,8 @@ def harm_dvr(n: int, x0: float, mw: float, with_trafo: bool = False):
 def _dvr_cached(kind: str, n: int, a: float, b: float):
     """One DVR per (kind, size, parameters): models and ensemble members that share
     a grid share its construction (callers get copies)."""
+    if kind == "Leg":
+        return tuple(np.asarray(x) for x in leg_dvr(n, int(a), True))
     f = harm_dvr if kind == "HO" else sin_dvr
     return tuple(np.asarray(x) for x in f(n, a, b, True))
 
@@ -159,6 +173,182 @@ def sin_dvr(n: int, xi: float, xf: float, with_trafo: bool = False):
     return grid, w, d1, d2, xd1
 
 
+def spline(x: np.ndarray, y: np.ndarray, xx: np.ndarray) -> np.ndarray:
+    """Cubic spline of (x, y) evaluated at xx (Spline, maths.f90:651-728).
+
+    On [x_i, x_(i+1)] f(t) = y_i + a_i (t - x_i) + b_i (t - x_i)^2 + c_i (t - x_i)^3;
+    the 3(n-1) coefficients solve one dense system (dgesv in the reference,
+    LU with partial pivoting here too) made of the passage through y_(i+1), the
+    continuity of f' and f'' at the inner points, and c = 0 in the first and
+    last interval.  Points left of x_1 use the first interval's (quadratic)
+    polynomial, points right of x_(n-1) the last one's.
+    """
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    if n < 2:
+        raise ModelError("an interpolation file needs at least two points")
+    N = 3 * n - 3
+    M = np.zeros((N, N))
+    rhs = np.zeros(N)
+    M[0, 2] = 1.0
+    ieq, iabc = 1, 0          # 1-based equation counter of the reference, 0-based column offset
+    for i in range(n - 2):
+        dx = x[i + 1] - x[i]
+        M[ieq, iabc:iabc + 3] = (dx, dx ** 2, dx ** 3)
+        rhs[ieq] = y[i + 1] - y[i]
+        M[ieq + 1, iabc:iabc + 4] = (1.0, 2 * dx, 3 * dx ** 2, -1.0)
+        M[ieq + 2, iabc + 1] = 1.0
+        M[ieq + 2, iabc + 2] = 3 * dx
+        M[ieq + 2, iabc + 4] = -1.0
+        ieq += 3
+        iabc += 3
+    dx = x[n - 1] - x[n - 2]
+    M[ieq, iabc:iabc + 3] = (dx, dx ** 2, dx ** 3)
+    rhs[ieq] = y[n - 1] - y[n - 2]
+    M[ieq + 1, iabc + 2] = 1.0
+    coef = np.linalg.solve(M, rhs)
+    out = np.empty(len(xx))
+    for i, xt in enumerate(np.asarray(xx, dtype=np.float64)):
+        j = n - 1                       # 0-based interval; the reference's loop leaves j = n
+        for jj in range(n - 1):
+            if xt < x[jj + 1]:
+                j = jj
+                break
+        if xt > x[n - 2]:
+            j = n - 2
+        d = xt - x[j]
+        a, b, c = coef[3 * j:3 * j + 3]
+        out[i] = y[j] + a * d + b * d ** 2 + c * d ** 3
+    return out
+
+
+def read_xy(path: str) -> Tuple[np.ndarray, np.ndarray]:
+    """Two columns (x, f(x)) of a data file, read up to the first line that does
+    not hold two numbers (list-directed reads until an error, hamilton.f90:234-246)."""
+    xs, ys = [], []
+    with open(path) as fh:
+        for line in fh:
+            toks = line.replace(",", " ").split()
+            try:
+                xv, yv = _read_float(toks[0]), _read_float(toks[1])
+            except (IndexError, ValueError):
+                break
+            xs.append(xv)
+            ys.append(yv)
+    return np.array(xs), np.array(ys)
+
+
+_LEG_WEIGHT = (2.0, 4.0 / 3.0, 16.0 / 15.0, 32.0 / 35.0, 256.0 / 315.0, 512.0 / 693.0, 2048.0 / 3003.0,
+               4096.0 / 6435.0, 65536.0 / 109395.0, 131072.0 / 230945.0, 524288.0 / 969969.0)
+_LEG_NXL = 3001   # grid of the 1/sin(theta) quadrature for M = 0 (dvr.f90:371)
+
+
+def _sym_grid(g: np.ndarray) -> np.ndarray:
+    """Symmetrise an angular grid about pi/2 (dvr.f90:389-395)."""
+    g = g.copy()
+    n = len(g)
+    for i in range(n // 2):
+        d = 0.5 * (g[i] + math.pi - g[n - 1 - i])
+        g[i] = d
+        g[n - 1 - i] = math.pi - d
+    if n % 2 == 1:
+        g[n // 2] = 0.5 * math.pi
+    return g
+
+
+@functools.lru_cache(maxsize=8)
+def _leg_sinm1_xl():
+    """1/sin(theta) of the 3001-point Legendre grid with its eigenvectors (M = 0)."""
+    n = _LEG_NXL
+    T = np.zeros((n, n))
+    i = np.arange(1, n)
+    T[i - 1, i] = i / np.sqrt(4.0 * i ** 2 - 1.0)
+    w, U = np.linalg.eigh(T + T.T)
+    g = _sym_grid(np.arccos(np.clip(w, -1.0, 1.0)))
+    return 1.0 / np.sin(g), U
+
+
+def leg_dvr(nP: int, MM: int, with_trafo: bool = False):
+    """Legendre DVR in theta for the associated Legendre functions of order MM
+    (Leg_DVR, dvr.f90:361-530): grid, weights, d1 (d/dtheta sin theta),
+    d2 (the L0^2 operator, L^2 - M^2 sin^-2), the sin^-2 matrix and trafoDVR."""
+    if MM > 10:
+        raise ModelError("Leg DVR implemented only for M <= 10")
+    if nP < 2:
+        raise ModelError("too few grid points selected for a DVR")
+    i = np.arange(1, nP)
+    T = np.zeros((nP, nP))
+    T[i - 1, i] = np.sqrt(((MM + i) ** 2 - MM ** 2) / (4.0 * (MM + i) ** 2 - 1.0))
+    w, trafo = np.linalg.eigh(T + T.T)
+    grid = _sym_grid(np.arccos(np.clip(w, -1.0, 1.0)))
+    trafo = trafo * np.where(trafo[0, :] < 0.0, -1.0, 1.0)[None, :]
+    wts = (trafo[0, :] / np.sin(grid) ** MM) ** 2 * _LEG_WEIGHT[MM]
+    aux = np.zeros((nP, nP))
+    v = np.sqrt(((MM + i) ** 4 - (MM + i) ** 2 * MM ** 2) / (4.0 * (MM + i) ** 2 - 1.0))
+    aux[i - 1, i] = v
+    aux[i, i - 1] = -v
+    d1 = trafo.T @ (aux @ trafo)
+    d1 = 0.5 * (d1 - d1.T)
+    np.fill_diagonal(d1, 0.0)
+    if MM == 0:
+        sinv, U = _leg_sinm1_xl()
+        Uk = U[:nP, :]
+        s1 = (Uk * sinv[None, :]) @ Uk.T
+        s1 = np.triu(s1) + np.triu(s1, 1).T
+        aux1 = s1 @ trafo
+        s1 = 0.5 * (trafo.T @ aux1 + aux1.T @ trafo)
+        s1 = np.triu(s1) + np.triu(s1, 1).T
+        sinm2 = s1 @ s1.T
+        sinm2 = np.triu(sinm2) + np.triu(sinm2, 1).T
+    else:
+        aux = np.zeros((nP, nP))
+        for a in range(1, nP + 1):
+            li = a - 1 + MM
+            idm = 1
+            for k in range(2 * MM):
+                idm *= (li + MM - k)
+            for b in range(a, nP + 1, 2):
+                lj = b - 1 + MM
+                jdm = 1
+                for k in range(2 * MM):
+                    jdm *= (lj + MM - k)
+                aux[a - 1, b - 1] = math.sqrt((2 * li + 1) * (2 * lj + 1)) / (2 * MM) * math.sqrt(idm / jdm)
+        aux = np.triu(aux) + np.triu(aux, 1).T
+        aux1 = aux @ trafo
+        sinm2 = 0.5 * (trafo.T @ aux1 + aux1.T @ trafo)
+        sinm2 = np.triu(sinm2) + np.triu(sinm2, 1).T
+    ll = (MM + np.arange(1, nP + 1)) ** 2 - (MM + np.arange(1, nP + 1))
+    aux1 = ll[:, None] * trafo
+    d2 = 0.5 * (trafo.T @ aux1 + aux1.T @ trafo) - float(MM) ** 2 * sinm2
+    d2 = np.triu(d2) + np.triu(d2, 1).T
+    xd1 = np.zeros((nP, nP))
+    if with_trafo:
+        return grid, wts, d1, d2, xd1, trafo, sinm2
+    return grid, wts, d1, d2, xd1, sinm2
+
+
+def associated_legendre(L: int, M: int, theta: np.ndarray) -> np.ndarray:
+    """Normalised associated Legendre functions for L <= 2 (AssociatedLegendreP,
+    maths.f90:734-775)."""
+    if abs(M) > L:
+        raise ModelError("requested a Legendre function with M > L")
+    th = np.asarray(theta, dtype=np.float64)
+    if L == 0:
+        return np.full_like(th, math.sqrt(0.5))
+    if L == 1:
+        if M == 0:
+            return math.sqrt(1.5) * np.cos(th)
+        return -math.copysign(1.0, M) * math.sqrt(0.75) * np.sin(th)
+    if L == 2:
+        if M == 0:
+            return math.sqrt(0.15625) * (1.0 + 3.0 * np.cos(2.0 * th))
+        if abs(M) == 1:
+            return -math.copysign(1.0, M) * math.sqrt(0.9375) * np.sin(2.0 * th)
+        return math.sqrt(0.9375) * np.sin(th) ** 2
+    raise ModelError(f"Associated Legendre function not implemented for L,M = {L} {M}")
+
+
 # ----------------------------------------------------------------------------
 # Model description
 # ----------------------------------------------------------------------------
@@ -179,7 +369,7 @@ class Model:
     mode_dofs: List[List[int]]              # iDOF (0-based dofs per mode)
     multiset: List[bool]                    # MultiSet
     nspf: np.ndarray                        # (nmodes, nstates) int64
-    dvr_type: List[str]                     # per dof: 'HO', 'sin', 'gwp'
+    dvr_type: List[str]                     # per dof: 'HO', 'sin', 'Leg', 'gwp'
     ngp: List[int]                          # per dof
     dvrpar: List[Tuple[float, float]]       # per dof
     terms: List[Term]
@@ -216,6 +406,14 @@ class Model:
     # explicit mixture states of the INIT-WF 'packets' block (init_calc.f90:527-540):
     # (state, 0-based SPF index per mode, coefficient) per packet
     init_packets: Optional[List[Tuple[int, Tuple[int, ...], complex]]] = None
+    # parametrised operators (OpParam, OpParamFunc; input.f90:950-1072): (function,
+    # p1, p2, p3, data file) for operator j = index + 1 of the codes 200 + j / -200 - j
+    op_params: List[Tuple[int, float, float, float, str]] = dataclasses.field(default_factory=list)
+    # contents (x, f(x)) of the data files the parametrised operators name
+    interp_data: Dict[str, Tuple[np.ndarray, np.ndarray]] = dataclasses.field(default_factory=dict)
+    # Gaussian lattice indices read from gwpgrid_<mode> (distribution 1,
+    # init_calc.f90:1048-1060): 0-based mode -> (ndof of the mode, nS) int array
+    gwp_grid: Dict[int, np.ndarray] = dataclasses.field(default_factory=dict)
 
     # ---- derived (filled by finalize) ----
     def finalize(self) -> "Model":
@@ -234,6 +432,7 @@ class Model:
         self.modes_gwp = [m for m in range(self.nmodes) if self.is_gwp_mode[m]]
         self.der_factor = complex(-1.0, 0.0) if self.relaxation else complex(0.0, -1.0)
         self._build_dvr()
+        self._build_param_ops()
         self._build_operators()
         self._build_layout()
         return self
@@ -246,11 +445,16 @@ class Model:
         self.d2: Dict[int, np.ndarray] = {}
         self.xd1: Dict[int, np.ndarray] = {}
         self.trafo: Dict[int, np.ndarray] = {}     # trafoDVR (basis x grid)
+        self.oper_dvr: Dict[int, np.ndarray] = {}  # operDVR (sin^-2 of Legendre DVRs)
         for d in range(self.ndof):
             t = self.dvr_type[d]
             if t in ("HO", "sin"):
                 g, w, d1, d2, xd1, tr = (np.array(x) for x in _dvr_cached(t, self.ngp[d], float(self.dvrpar[d][0]),
                                                                             float(self.dvrpar[d][1])))
+            elif t == "Leg":
+                g, w, d1, d2, xd1, tr, sm2 = (np.array(x) for x in _dvr_cached(t, self.ngp[d],
+                                                                                 float(self.dvrpar[d][0]), 0.0))
+                self.oper_dvr[d] = sm2
             elif t == "gwp":
                 continue
             else:
@@ -260,6 +464,45 @@ class Model:
         self.ngpm = {}
         for m in self.modes_dvr:
             self.ngpm[m] = int(np.prod([self.ngp[d] for d in self.mode_dofs[m]]))
+
+    # hamilton.f90:210-290: values of the parametrised operators on the grids of
+    # the DVR dofs that use them
+    def _build_param_ops(self):
+        self.grid_oper: Dict[Tuple[int, int], np.ndarray] = {}
+        used = set()
+        for op in [self.terms] + self.expect + [d[2] for d in self.dissipation]:
+            for term in op:
+                for d, c in term.dof_ops.items():
+                    if c > OP_PARAM or c <= -OP_PARAM:
+                        used.add((d, abs(c) - OP_PARAM))
+        for (d, j) in sorted(used):
+            if j < 1 or j > len(self.op_params):
+                raise ModelError(f"parametrised operator {j} on dof {d + 1} is not declared")
+            if self.dvr_type[d] == "gwp":
+                raise ModelError(f"parametrised operators act on DVR dofs only (dof {d + 1})")
+            func, p1, p2, p3, fname = self.op_params[j - 1]
+            x = self.grid[d]
+            if func == PAR_GAU:
+                v = np.exp(p1 * x + p2 * x ** 2)
+            elif func == PAR_INTERP:
+                v = spline(*self.interp_data[fname], x)
+            elif func == PAR_SQUARE:
+                v = np.where(np.abs(x - p1) < 0.5 * p2, 1.0, 0.0)
+            elif func == PAR_HERMITE:
+                v = x ** int(p3) * np.exp(p1 * x + p2 * x ** 2)
+            elif func == PAR_SIN:
+                v = np.sin(p1 * x) ** p2
+            elif func == PAR_COS:
+                v = np.cos(p1 * x) ** p2
+            elif func == PAR_EIGPROJ:
+                # Eigenf1DPot_real (dvr.f90:600-650): eigenvector p3 of -p2 d2DVR + V
+                V = spline(*self.interp_data[fname], x)
+                H = -p2 * self.d2[d] + np.diag(V)
+                _, U = np.linalg.eigh(H)
+                v = U[:, int(p3)].copy()
+            else:
+                raise ModelError(f"unknown parametrised operator function {func}")
+            self.grid_oper[(d, j)] = np.asarray(v, dtype=np.float64)
 
     # hamilton.f90:91-167 (operator dedup, the extra operators after the
     # Hamiltonian's), :353-374 (IsIdentity), :377-399 (SkipTerm)
@@ -350,6 +593,10 @@ class Model:
             for code in codes[d]:
                 if code in (OP_ID, OP_P, OP_DQ2, OP_QP) or 1 <= code <= 20:
                     continue
+                if code > OP_PARAM or code <= -OP_PARAM:
+                    continue
+                if code == OP_SINM2 and self.dvr_type[d] == "Leg":
+                    continue
                 raise ModelError(f"primitive operator code {code} on dof {d + 1} is not supported")
 
     # init_calc.f90:22-53 (nAConf, AStateOffset), :160-181 (ipsiSPF, dimPsi)
@@ -408,7 +655,55 @@ class Model:
             return "dense", 1j * self.xd1[d]
         if 1 <= code <= 20:
             return "diag", self.grid[d] ** code
+        if code > OP_PARAM:
+            return "diag", self.grid_oper[(d, code - OP_PARAM)]
+        if code <= -OP_PARAM:
+            # MultTensProj builds AM = v v^T (dger) and applies it like MultTens
+            v = self.grid_oper[(d, -code - OP_PARAM)]
+            return "dense", np.outer(v, v).astype(np.complex128)
+        if code == OP_SINM2 and d in self.oper_dvr:
+            return "dense", self.oper_dvr[d].astype(np.complex128)
         raise ModelError(f"operator code {code} not supported on a DVR dof")
+
+
+def _plain(v):
+    """v with NumPy arrays and scalars replaced by Python lists and numbers."""
+    if isinstance(v, np.ndarray):
+        return _plain(v.tolist())
+    if isinstance(v, np.generic):
+        return v.item()
+    if isinstance(v, dict):
+        return {_plain(k): _plain(x) for k, x in v.items()}
+    if isinstance(v, (list, tuple)):
+        return type(v)(_plain(x) for x in v)
+    return v
+
+
+def model_fields(model: Model) -> Dict:
+    """The constructor fields of a model (what an input file declares), as plain
+    Python values (no NumPy objects, so any NumPy version reads them back):
+    ``model_from_fields`` rebuilds the same model."""
+    out = {}
+    for f in dataclasses.fields(Model):
+        v = getattr(model, f.name)
+        if f.name in ("terms",):
+            v = [(complex(t.coeff), int(t.lhs), int(t.rhs), dict(t.dof_ops)) for t in v]
+        elif f.name == "expect":
+            v = [[(complex(t.coeff), int(t.lhs), int(t.rhs), dict(t.dof_ops)) for t in op] for op in v]
+        elif f.name == "dissipation":
+            v = [(ty, c, [(complex(t.coeff), int(t.lhs), int(t.rhs), dict(t.dof_ops)) for t in op])
+                 for (ty, c, op) in v]
+        out[f.name] = _plain(v)
+    return out
+
+
+def model_from_fields(d: Dict) -> Model:
+    """Inverse of ``model_fields``: a finalised model."""
+    d = dict(d)
+    d["terms"] = [Term(*t) for t in d["terms"]]
+    d["expect"] = [[Term(*t) for t in op] for op in d.get("expect", [])]
+    d["dissipation"] = [(ty, c, [Term(*t) for t in op]) for (ty, c, op) in d.get("dissipation", [])]
+    return Model(**d).finalize()
 
 
 # ----------------------------------------------------------------------------
@@ -449,6 +744,14 @@ def initial_wavefunction(model: Model) -> Tuple[np.ndarray, np.ndarray]:
             eps = np.finfo(float).eps
             phi[d] = np.array([0.0 if max(abs(x0), abs(p0)) < eps else complex(0.5 * x0 / dx ** 2, p0)],
                               dtype=np.complex128)
+        elif kind == "Leg":
+            # associated Legendre function times the square root of the weights
+            # (init_calc.f90:578-592)
+            if model.dvr_type[d] != "Leg":
+                raise ModelError("Input Error: Legendre functions available only for Leg-DVR")
+            LL, MM = par
+            phi[d] = (associated_legendre(int(LL), int(MM), model.grid[d])
+                      * np.sqrt(model.wgrid[d])).astype(np.complex128)
         else:
             raise ModelError(f"initial SPF kind {kind!r} not supported")
     # DVR modes
@@ -517,9 +820,15 @@ def initial_wavefunction(model: Model) -> Tuple[np.ndarray, np.ndarray]:
             raise ModelError("the same GWP distribution must be used for all dofs of a mode")
         ns = int(model.nspf[m, :].max())
         index_lat = np.zeros((nmd, ns), dtype=np.int64)
-        if ns > 1:
-            if dists.pop() != 0:
-                raise ModelError("only the lattice GWP distribution (0) is supported")
+        dist = dists.pop()
+        if ns > 1 and dist == 1:
+            # distribution read from gwpgrid_<mode> (init_calc.f90:1048-1060)
+            if m not in model.gwp_grid:
+                raise ModelError(f"INPUT ERROR: Gaussian grid file gwpgrid_{m + 1} not found")
+            index_lat[:, :] = np.asarray(model.gwp_grid[m], dtype=np.int64)[:nmd, :ns]
+        elif ns > 1:
+            if dist != 0:
+                raise ModelError(f"Unknown distribution type: {dist}")
             i1, i2, l = 1, 1, 2
             done = False
             while not done:
@@ -639,21 +948,107 @@ def initial_coefficients(model: Model, psi: np.ndarray) -> np.ndarray:
 _OPNAMES = {"p": OP_P, "dq^2": OP_DQ2, "qp": OP_QP, "q": 1}
 
 
-def _parse_dof_op(name: str) -> int:
-    name = name.strip()
-    if name in _OPNAMES:
-        return _OPNAMES[name]
-    mm = re.fullmatch(r"q\^(\d+)", name)
-    if mm and 1 <= int(mm.group(1)) <= 10:
-        return int(mm.group(1))
-    raise ModelError(f"Operator {name} not implemented")
+def _first_floats(text: str, count: int, defaults=None) -> List[float]:
+    toks = text.replace(",", " ").split()
+    if not toks and defaults is not None:
+        return list(defaults)
+    try:
+        return [_read_float(t) for t in toks[:count]] + [0.0] * max(0, count - len(toks))
+    except ValueError as exc:
+        raise ModelError(f"cannot read the parameters of operator {text!r}") from exc
 
 
-def parse_operator_file(text: str, nstates: int) -> List[Term]:
+class OperatorDeclarations:
+    """The declaration state shared by every operator file of one input
+    (read_declare_ham, input.f90:812-1144, and read_declare_op, :1149-1443):
+    the parametrised operators (OpParam, OpParamFunc, nOpParam) and the data
+    files they read (strings, nStrings).  Data files are read relative to
+    ``base`` and kept in ``interp_data``."""
+
+    def __init__(self, base: str = ".", dvr_type: Optional[Sequence[str]] = None):
+        self.base = base
+        self.dvr_type = dvr_type
+        self.op_params: List[Tuple[int, float, float, float, str]] = []
+        self.interp_data: Dict[str, Tuple[np.ndarray, np.ndarray]] = {}
+
+    def _load(self, fname: str):
+        if fname not in self.interp_data:
+            path = os.path.join(self.base, fname)
+            if not os.path.exists(path):
+                raise ModelError(f"data file {fname} not found")
+            self.interp_data[fname] = read_xy(path)
+
+    def _add(self, func, p1=0.0, p2=0.0, p3=0.0, fname="") -> int:
+        self.op_params.append((func, float(p1), float(p2), float(p3), fname))
+        return len(self.op_params)
+
+    def _need_leg(self, k: int, what: str):
+        if self.dvr_type is not None and self.dvr_type[k] != "Leg":
+            raise ModelError(f"ERROR: {what} operator allowed only for Leg-DVR")
+
+    def parse(self, name: str, k: int) -> int:
+        """Code of the primitive operator text ``name`` on dof k (0-based).  The
+        keyword checks run in the reference's order (input.f90:953-1092)."""
+        name = name.strip()
+        i = name.find("gau")
+        if i >= 0:
+            p1, p2 = _first_floats(name[i + 3:], 2)
+            return OP_PARAM + self._add(PAR_GAU, p1, p2)
+        i = name.find("interp")
+        if i >= 0:
+            fname = name[i + 6:].strip().split()[0].strip("'\"")
+            for j, (func, _, _, _, fn) in enumerate(self.op_params):
+                if func == PAR_INTERP and fn == fname:   # the same file is one operator
+                    return OP_PARAM + j + 1
+            self._load(fname)
+            return OP_PARAM + self._add(PAR_INTERP, fname=fname)
+        i = name.find("square")
+        if i >= 0:
+            p1, p2 = _first_floats(name[i + 6:], 2)
+            return OP_PARAM + self._add(PAR_SQUARE, p1, p2)
+        i = name.find("hermite")
+        if i >= 0:
+            r, p1, p2 = _first_floats(name[i + 7:], 3)
+            return OP_PARAM + self._add(PAR_HERMITE, p1, p2, int(r))
+        if "sin^-2" in name:
+            self._need_leg(k, "sin^-2")
+            return OP_SINM2
+        i = name.find("sin")
+        if i >= 0:
+            p1, p2 = _first_floats(name[i + 3:], 2, defaults=(1.0, 1.0))
+            return OP_PARAM + self._add(PAR_SIN, p1, p2)
+        i = name.find("cos")
+        if i >= 0:
+            p1, p2 = _first_floats(name[i + 3:], 2, defaults=(1.0, 1.0))
+            return OP_PARAM + self._add(PAR_COS, p1, p2)
+        i = name.find("eig_proj")
+        if i >= 0:
+            toks = name[i + 8:].replace(",", " ").split()
+            if len(toks) < 3:
+                raise ModelError(f"eig_proj needs a potential file, a kinetic prefactor and a level: {name!r}")
+            fname = toks[0].strip("'\"")
+            self._load(fname)
+            j = self._add(PAR_EIGPROJ, 0.0, _read_float(toks[1]), int(toks[2]), fname)
+            return -OP_PARAM - j
+        if name == "L0^2":
+            self._need_leg(k, "L0^2")
+            return OP_DQ2
+        if name in _OPNAMES:
+            return _OPNAMES[name]
+        mm = re.fullmatch(r"q\^(\d+)", name)
+        if mm and 1 <= int(mm.group(1)) <= 10:
+            return int(mm.group(1))
+        raise ModelError(f"Operator {name} not implemented")
+
+
+def parse_operator_file(text: str, nstates: int, decl: Optional["OperatorDeclarations"] = None) -> List[Term]:
     """Operator grammar of input.f90:812-1144: ``coeff | el-op | k op | k op ...``.
 
     Supported el-ops: none or ``1`` (one term per state), ``Sa&b`` (one term, or
-    two Hermitian-conjugate terms for a != b), ``Za&b``."""
+    two Hermitian-conjugate terms for a != b), ``Za&b``.  Parametrised operators
+    are declared in ``decl`` (one per input, shared by all its operator files)."""
+    if decl is None:
+        decl = OperatorDeclarations()
     terms: List[Term] = []
     for raw in text.splitlines():
         if raw.startswith("----"):
@@ -690,7 +1085,7 @@ def parse_operator_file(text: str, nstates: int) -> List[Term]:
             opname = toks[1].strip() if len(toks) > 1 else "1"
             if opname == "1":
                 continue
-            dof_ops[k] = _parse_dof_op(opname)
+            dof_ops[k] = decl.parse(opname, k)
         for (a, b) in pairs:
             terms.append(Term(coeff, a, b, dict(dof_ops)))
     return terms
@@ -790,6 +1185,11 @@ def parse_input(path: str) -> Model:
         dvr_type[d] = t
         if t == "gwp" and len(toks) == 2:
             ngp[d], dvrpar[d] = 101, (-10.0, 10.0)
+        elif t == "Leg":
+            # 'k Leg M nP': |M| of the associated Legendre functions, grid points
+            # (read_declare_dvr, dvr.f90:58-64)
+            dvrpar[d] = (float(abs(int(toks[2]))), 0.0)
+            ngp[d] = int(toks[3])
         else:
             ngp[d] = int(toks[2])
             dvrpar[d] = (_read_float(toks[3]), _read_float(toks[4]))
@@ -800,15 +1200,16 @@ def parse_input(path: str) -> Model:
     if not os.path.exists(hpath):
         # the reference lower-cases input values (input.f90:145-147)
         raise ModelError(f"Operator file, {hfile} not found")
+    decl = OperatorDeclarations(base, dvr_type)
     with open(hpath) as fh:
-        terms = parse_operator_file(fh.read(), nstates)
+        terms = parse_operator_file(fh.read(), nstates, decl)
     expect: List[List[Term]] = []
     for ef in expect_files:
         epath = os.path.join(base, ef)
         if not os.path.exists(epath):
             raise ModelError(f"Operator file, {ef} not found")
         with open(epath) as fh:
-            expect.append(parse_operator_file(fh.read(), nstates))
+            expect.append(parse_operator_file(fh.read(), nstates, decl))
     dissipation: List[Tuple[int, float, List[Term]]] = []
     for df in diss_files:
         dpath = os.path.join(base, df)
@@ -824,11 +1225,12 @@ def parse_input(path: str) -> Model:
             raise ModelError(f"dissipation file {df} is empty")
         head = dtext[first].split("#", 1)[0].replace(",", " ").split()
         dissipation.append((int(head[0]), _read_float(head[1]),
-                            parse_operator_file("\n".join(dtext[first + 1:]), nstates)))
+                            parse_operator_file("\n".join(dtext[first + 1:]), nstates, decl)))
     model = Model(nstates=nstates, mode_dofs=mode_dofs, multiset=multiset, nspf=nspf,
                   dvr_type=dvr_type, ngp=ngp, dvrpar=dvrpar, terms=terms,
                   label=os.path.basename(path), expect=expect, dissipation=dissipation,
-                  npackets=int(kw.get("npackets", "1")))
+                  npackets=int(kw.get("npackets", "1")), op_params=decl.op_params,
+                  interp_data=decl.interp_data)
     if "eps_pop" in kw:
         model.eps_pop = _read_float(kw["eps_pop"])
     if "tinit" in kw:
@@ -909,6 +1311,26 @@ def parse_input(path: str) -> Model:
             if ms:
                 scw = _read_float(ms.group(1))
             model.init_spf[int(k) - 1] = ("gwp", (dist, x0, p0, dx, ovl, scw))
+        elif "Leg" in ln:
+            k, rest = ln.split("Leg", 1)
+            LL, MM = (int(v) for v in rest.replace(",", " ").split()[:2])
+            model.init_spf[int(k) - 1] = ("Leg", (LL, MM))
         else:
             raise ModelError(f"The chosen initial SPF is unknown: {ln}")
+    # lattice indices of Gaussian modes placed by distribution 1 (init_calc.f90:1048-1060)
+    for m in range(nmodes):
+        if dvr_type[mode_dofs[m][0]] != "gwp":
+            continue
+        dists = {model.init_spf.get(d, ("", (0,)))[1][0] for d in mode_dofs[m]}
+        gpath = os.path.join(base, f"gwpgrid_{m + 1}")
+        if 1 in dists and os.path.exists(gpath):
+            ns = int(nspf[m, :].max())
+            rows = []
+            with open(gpath) as fh:
+                for line in fh:
+                    if len(rows) == ns:
+                        break
+                    if line.strip():
+                        rows.append([int(v) for v in line.split()[:len(mode_dofs[m])]])
+            model.gwp_grid[m] = np.array(rows, dtype=np.int64).T
     return model.finalize()

@@ -1588,6 +1588,13 @@ class Oracle:
             return self._propagate_adams(A, psi, A0, psi0, t, step, maxtime, record_steps)
         if md.int_type == INT_BS:
             return self._propagate_bs(A, psi, A0, psi0, t, step, maxtime, record_steps)
+        if md.int_type == INT_DOPRI:
+            # Dormand-Prince carries the last stage's derivative into the next step
+            # (rkqs, integrator.f90:82-85).  The reference's first step reads
+            # dAVector before anything has computed it (propagator.f90:98, 116);
+            # the derivative at the start is evaluated here instead, as the device
+            # path does.
+            dA, dpsi = self.calc_derivs(A, psi, t)
         while t < maxtime:
             outputs.append(self.observables(A, psi, A0, psi0, t))
             tnext = t + md.tout
@@ -1597,8 +1604,8 @@ class Oracle:
                 else:
                     if md.int_type == INT_RK45:
                         dA, dpsi = self.calc_derivs(A, psi, t)
-                    else:
-                        raise OracleError("DOPRI driver needs the carried derivative; use rk45")
+                    elif md.int_type != INT_DOPRI:
+                        raise OracleError(f"integrator type {md.int_type} is not an RK method")
                     A, psi, dA, dpsi, sdone, snext, tries = self.rkqs(A, psi, dA, dpsi, t, step, md.int_type)
                 if record_steps:
                     steps.append((t, step, sdone, snext, tries))

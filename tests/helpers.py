@@ -2,7 +2,9 @@
 import numpy as np
 
 from macaw_gb300.generate import gmctdh16, lvc5, qvc
-from macaw_gb300.model import initial_wavefunction, INT_CMF2, INT_RK45
+from macaw_gb300.model import (AU2FS, INT_CMF2, INT_RK45, Model, OP_DQ2, OP_PARAM, OP_SINM2, PAR_COS,
+                               PAR_EIGPROJ, PAR_GAU, PAR_HERMITE, PAR_INTERP, PAR_SIN, PAR_SQUARE, Term,
+                               initial_wavefunction)
 
 
 def small_lvc(nspf=3, grid=(12, 10, 11, 9, 10), eps_int=1e-7, tfinal_fs=2.0):
@@ -116,3 +118,38 @@ def with_decay(model, npackets=2, gamma=0.05, eps_pop=1e-6):
     model.eps_pop = eps_pop
     model.dissipation = [(1, gamma, [Term(1.0, 0, 1, {})]), (2, -0.5 * gamma, [Term(1.0, 1, 1, {})])]
     return model.finalize()
+
+
+def parametrised_model(tfinal_fs=0.5):
+    """2 states; mode 1 = Legendre DOF (M = 0, 14 points) x sine DOF (9 points),
+    mode 2 = Legendre DOF (M = 1, 10 points), mode 3 = HO DOF (16 points).  The
+    Hamiltonian uses L0^2 and sin^-2 on the angles and every parametrised
+    operator; the spline data are a double well sampled on 13 points."""
+    x = np.linspace(-6.0, 6.0, 13)
+    interp = {"dw.dat": (x, 0.02 * (x ** 2 - 4.0) ** 2 / 16.0), "harm.dat": (x, 0.5 * x ** 2)}
+    ops = [(PAR_GAU, -0.1, -0.05, 0.0, ""), (PAR_INTERP, 0.0, 0.0, 0.0, "dw.dat"),
+           (PAR_SQUARE, 0.5, 3.0, 0.0, ""), (PAR_HERMITE, 0.2, -0.1, 2.0, ""),
+           (PAR_SIN, 1.0, 2.0, 0.0, ""), (PAR_COS, 1.0, 1.0, 0.0, ""),
+           (PAR_EIGPROJ, 0.0, 0.5, 1.0, "harm.dat")]
+    P = [OP_PARAM + j for j in range(1, 8)]
+    terms = []
+    for s in range(2):
+        terms += [Term(0.004 + 0j, s, s, {0: OP_DQ2}), Term(0.001 + 0j, s, s, {0: 2}),
+                  Term(-0.003 + 0j, s, s, {1: OP_DQ2}), Term(0.002 + 0j, s, s, {1: 2}),
+                  Term(0.005 + 0j, s, s, {2: OP_DQ2}), Term(0.001 + 0j, s, s, {2: OP_SINM2}),
+                  Term(-0.004 + 0j, s, s, {3: OP_DQ2}), Term(0.004 + 0j, s, s, {3: P[1]})]
+    terms += [Term(0.01 + 0j, 0, 0, {}), Term(-0.01 + 0j, 1, 1, {}),
+              Term(0.003 + 0j, 0, 0, {3: P[0]}), Term(0.002 + 0j, 1, 1, {1: P[2], 3: 1}),
+              Term(0.001 + 0j, 0, 0, {3: P[3]}), Term(0.002 + 0j, 1, 1, {0: P[4]}),
+              Term(0.003 + 0j, 0, 0, {2: P[5]}), Term(0.004 + 0j, 1, 1, {3: -P[6]}),
+              Term(0.006 + 0j, 0, 1, {3: 1}), Term(0.006 + 0j, 1, 0, {3: 1}),
+              Term(0.002 + 0j, 0, 1, {0: P[5]}), Term(0.002 + 0j, 1, 0, {0: P[5]})]
+    m = Model(nstates=2, mode_dofs=[[0, 1], [2], [3]], multiset=[True, True, True],
+              nspf=np.array([[4, 3], [3, 3], [4, 4]]), dvr_type=["Leg", "sin", "Leg", "HO"],
+              ngp=[14, 9, 10, 16], dvrpar=[(0.0, 0.0), (-4.0, 4.0), (1.0, 0.0), (0.0, 1.0)],
+              terms=terms, tfinal=tfinal_fs / AU2FS, tout=0.25 / AU2FS, eps_int=1e-7,
+              int_type=INT_RK45, init_state=1, label="parametrised",
+              op_params=ops, interp_data=interp)
+    m.init_spf[0] = ("Leg", (0, 0))
+    m.init_spf[2] = ("Leg", (1, 1))
+    return m.finalize()

@@ -156,15 +156,116 @@ def test_parser_round_trip(tmp_path):
     assert np.allclose(d1[0], d2[0], rtol=1e-12, atol=1e-15)
 
 
-def test_reference_example_is_parsed():
-    """The butadiene example grammar (SPF/GRID/INIT-WF blocks, S/M sets) parses up
-    to the features this core supports (interp splines are reported as unsupported)."""
-    from macaw_gb300.model import ModelError
-    ex = "/root/reference/Examples/Butadiene_5modes/but_5D.inp"
+def _reference_example(name):
+    from tests.golden.make_butadiene import example_input
+    ex = example_input(name)
     if not os.path.exists(ex):
-        pytest.skip("reference examples not present")
-    with pytest.raises(ModelError, match="interp|not implemented"):
-        parse_input(ex)
+        pytest.skip("the reference's examples are not present (MACAW_REFERENCE_DIR)")
+    return ex
+
+
+@pytest.mark.parametrize("name", ["butadiene_dopri", "butadiene_cmf2"])
+def test_reference_examples_parse_like_their_fixtures(name):
+    """Both example inputs of the reference parse (interp spline operators,
+    sine/HO grids, Gaussian modes, S/M sets, DOPRI and CMF2), and the committed
+    fixture the GPU tests run is what they declare."""
+    import pickle
+    from macaw_gb300.model import model_fields
+    model = parse_input(_reference_example(name))
+    with open(os.path.join(GOLDEN, name + ".pkl"), "rb") as fh:
+        assert pickle.load(fh) == model_fields(model)
+
+
+def test_butadiene_fixture_model():
+    """The fixture rebuilds the example model: the spline operators on the sine
+    grid of dof 1 (the q^2 data file is a parabola, which the spline reproduces
+    exactly, extrapolation included), a finite start energy, unit norm."""
+    import pickle
+    from macaw_gb300.model import model_from_fields, INT_DOPRI, OP_PARAM
+    with open(os.path.join(GOLDEN, "butadiene_dopri.pkl"), "rb") as fh:
+        model = model_from_fields(pickle.load(fh))
+    assert model.int_type == INT_DOPRI and model.nmodes == 3 and list(model.nspf[:, 0]) == [6, 6, 7]
+    assert len(model.op_params) == 2
+    q2 = model.grid_oper[(0, 1)]
+    assert np.allclose(q2, model.grid[0] ** 2, rtol=0, atol=1e-10)
+    assert any(c > OP_PARAM for t in model.terms for c in t.dof_ops.values())
+    A, psi = initial_wavefunction(model)
+    ob = Oracle(model).observables(A, psi, A, psi, 0.0)
+    assert abs(ob["norm"] - 1.0) < 1e-12 and np.isfinite(ob["energy"])
+
+
+def test_spline_known_answers():
+    """Spline (maths.f90:651-728): quadratic data are reproduced exactly, outside
+    the data range too (zero third derivative in the end intervals); the
+    interpolant passes through the data and is C2 at the inner knots."""
+    from macaw_gb300.model import spline
+    x = np.array([-3.0, -2.2, -1.0, 0.0, 0.7, 1.5, 3.0])
+    xx = np.linspace(-4.0, 4.0, 41)
+    assert np.allclose(spline(x, 2.0 * x ** 2 - x + 0.5, xx), 2.0 * xx ** 2 - xx + 0.5, rtol=0, atol=1e-12)
+    y = np.sin(x)
+    assert np.allclose(spline(x, y, x), y, rtol=0, atol=1e-13)
+    h = 1e-4
+    for xk in x[1:-1]:
+        left = spline(x, y, np.array([xk - 2 * h, xk - h, xk]))
+        right = spline(x, y, np.array([xk, xk + h, xk + 2 * h]))
+        d1l, d1r = (left[2] - left[1]) / h, (right[1] - right[0]) / h
+        assert abs(d1l - d1r) < 1e-3
+        d2l = (left[2] - 2 * left[1] + left[0]) / h ** 2
+        d2r = (right[2] - 2 * right[1] + right[0]) / h ** 2
+        assert abs(d2l - d2r) < 1e-2
+
+
+@pytest.mark.parametrize("MM", [0, 1, 2])
+def test_legendre_dvr_known_answers(MM):
+    """Leg_DVR (dvr.f90:361-530): the grid is symmetric about pi/2; the FBR of
+    L0^2 + M^2 sin^-2 is diag(l(l+1)), l = M .. M + n - 1; for M > 0 the FBR of
+    sin^-2 has the closed form <P_M^M|sin^-2|P_M^M> = (2M+1)/(2M); for M = 0 the
+    quadrature-built sin^-2 is symmetric positive definite; the M = 0 weights sum
+    to 2; d1 is antisymmetric."""
+    from macaw_gb300.model import leg_dvr
+    n = 12
+    g, w, d1, d2, xd1, tr, sm2 = leg_dvr(n, MM, True)
+    assert np.allclose(g + g[::-1], np.pi, atol=1e-13)
+    L2 = tr @ (d2 + MM ** 2 * sm2) @ tr.T
+    ll = MM + np.arange(n)
+    assert np.allclose(L2, np.diag(ll * (ll + 1.0)), atol=1e-9)
+    assert np.allclose(d1, -d1.T, atol=1e-14)
+    if MM > 0:
+        fbr = tr @ sm2 @ tr.T
+        assert abs(fbr[0, 0] - (2 * MM + 1) / (2.0 * MM)) < 1e-12
+    else:
+        assert abs(w.sum() - 2.0) < 1e-12
+        assert np.allclose(sm2, sm2.T) and np.linalg.eigvalsh(sm2).min() > 0.0
+
+
+def test_parametrised_operator_values():
+    """gridOper of every parametrised function (hamilton.f90:210-290) on the
+    grids of the synthetic model the GPU tests use; the eig_proj vector is the
+    normalised eigenvector of -p2 d2 + V (Eigenf1DPot_real)."""
+    from macaw_gb300.model import OP_PARAM
+    from tests.helpers import parametrised_model
+    m = parametrised_model()
+    x = m.grid[3]
+    assert np.allclose(m.grid_oper[(3, 1)], np.exp(-0.1 * x - 0.05 * x ** 2))
+    assert np.allclose(m.grid_oper[(1, 3)], (np.abs(m.grid[1] - 0.5) < 1.5).astype(float))
+    assert np.allclose(m.grid_oper[(3, 4)], x ** 2 * np.exp(0.2 * x - 0.1 * x ** 2))
+    assert np.allclose(m.grid_oper[(0, 5)], np.sin(m.grid[0]) ** 2)
+    v = m.grid_oper[(3, 7)]
+    H = -0.5 * m.d2[3] + np.diag(0.5 * x ** 2)
+    assert abs(np.linalg.norm(v) - 1.0) < 1e-12
+    assert np.linalg.norm(H @ v - (v @ H @ v) * v) < 1e-10
+    kind, P = m.dof_op_matrix(3, -OP_PARAM - 7)
+    assert kind == "dense" and np.allclose(P @ P, P)
+
+
+def test_model_fields_round_trip():
+    from macaw_gb300.model import model_fields, model_from_fields
+    from tests.helpers import parametrised_model
+    m = parametrised_model()
+    m2 = model_from_fields(model_fields(m))
+    assert np.array_equal(m.ae, m2.ae) and m.ioper.tolist() == m2.ioper.tolist()
+    for k, v in m.grid_oper.items():
+        assert np.array_equal(v, m2.grid_oper[k])
 
 
 @pytest.mark.parametrize("name", ["lvc_small", "qvc_small"])

@@ -56,6 +56,46 @@ def test_density_matrix_noalloc_matches_existing_entry_point():
     gpu.close()
 
 
+def _call_tensor(lib, torch, X, mode):
+    """The entry point on one tensor X (Fortran order), rho with ld = n + 1."""
+    nspf = np.array(X.shape, dtype=np.int64)
+    a_dev = torch.from_numpy(np.ascontiguousarray(X.reshape(-1, order="F"))).cuda()
+    n = int(nspf[mode])
+    ld = n + 1
+    rho_dev = torch.full((n * ld,), complex(np.nan, np.nan), dtype=torch.complex128, device="cuda")
+    rc = lib.mctdh_density_matrix_noalloc(C.c_void_p(a_dev.data_ptr()), nspf.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          len(nspf), mode, C.c_void_p(rho_dev.data_ptr()), ld, None)
+    assert rc == 0, lib.mctdh_last_error(None).decode()
+    torch.cuda.synchronize()
+    return rho_dev.cpu().numpy().reshape((ld, n), order="F")[:n, :]
+
+
+def _herm_ref(X, mode):
+    R = hole_contract(X, X, mode)
+    return 0.5 * (R + R.conj().T)
+
+
+def test_density_matrix_noalloc_wide_mode_and_block_cap():
+    """The branches the small model does not reach: a contracted mode of 32 SPFs
+    (1,024 pairs, four per thread), a tensor of 2,000 fibre tiles whose block
+    count is capped at the scratch area's 128 partials, then a small case again
+    (a stale partial of the large call would show up there)."""
+    torch = pytest.importorskip("torch")
+    from macaw_gb300.capi import load_library
+    lib = load_library()
+    rng = np.random.default_rng(23)
+
+    def rnd(shape):
+        return rng.normal(size=shape) + 1j * rng.normal(size=shape)
+
+    cases = [((24, 32, 20), 1), ((40, 40, 40, 6), 3), ((20, 40, 40, 6), 0), ((3, 4, 2), 1)]
+    for shape, mode in cases:
+        X = np.asfortranarray(rnd(shape))
+        rho = _call_tensor(lib, torch, X, mode)
+        ref = _herm_ref(X, mode)
+        assert np.linalg.norm(rho - ref) <= RTOL * np.linalg.norm(ref), (shape, mode)
+
+
 def test_density_matrix_noalloc_rejects_oversized_mode():
     torch = pytest.importorskip("torch")
     from macaw_gb300.capi import load_library
@@ -72,3 +112,10 @@ def test_density_matrix_noalloc_rejects_oversized_mode():
     rc = lib.mctdh_density_matrix_noalloc(host.ctypes.data_as(C.c_void_p), nspf.ctypes.data_as(C.POINTER(C.c_int64)),
                                           2, 0, C.c_void_p(rho_dev.data_ptr()), 4, None)
     assert rc == -7
+    if torch.cuda.device_count() > 1:
+        # a buffer of another GPU is refused on the host; nothing is launched
+        other = torch.zeros(16, dtype=torch.complex128, device="cuda:1")
+        rc = lib.mctdh_density_matrix_noalloc(C.c_void_p(other.data_ptr()),
+                                              nspf.ctypes.data_as(C.POINTER(C.c_int64)),
+                                              2, 0, C.c_void_p(rho_dev.data_ptr()), 4, None)
+        assert rc == -7
