@@ -102,6 +102,12 @@ typedef struct mctdh_setup {
    * both NULL when no dof uses it. */
   const double *oper_dvr;
   const int64_t *oper_dvr_off;
+  /* 1: every regularised inverse of rho starts its Jacobi eigen-decomposition
+   * from the identity.  0 (default): from the previous call's eigenvectors, the
+   * same decomposition up to rounding in fewer sweeps; rounding then depends on
+   * the call history (ensembles always start cold, so that each member repeats
+   * the arithmetic of a context created with 1). */
+  int64_t reginv_cold;
 } mctdh_setup_t;
 
 /* Build the device context: uploads the operators, plans the batched kernels

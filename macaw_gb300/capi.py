@@ -53,7 +53,7 @@ class Setup(C.Structure):
         ("npackets", C.c_int64), ("eps_pop", C.c_double), ("term_kind", I64P), ("term_diss1", I64P),
         ("ndiss1", C.c_int64), ("diss1_ae", DP),
         ("nopparam", C.c_int64), ("ngpmax", C.c_int64), ("grid_oper", DP),
-        ("oper_dvr", DP), ("oper_dvr_off", I64P),
+        ("oper_dvr", DP), ("oper_dvr_off", I64P), ("reginv_cold", C.c_int64),
     ]
 
 
@@ -181,7 +181,7 @@ def _ptr(a: np.ndarray, t=C.c_double):
     return a.ctypes.data_as(C.POINTER(t))
 
 
-def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
+def build_setup(model: Model, precision: int = 0, warm_start: bool = True) -> Tuple[Setup, list]:
     """Flatten the model into the C struct (Fortran column-major conventions)."""
     keep: list = []
     nm, ns, nd = model.nmodes, model.nstates, model.ndof
@@ -287,6 +287,7 @@ def build_setup(model: Model, precision: int = 0) -> Tuple[Setup, list]:
     s.der_factor_re, s.der_factor_im = model.der_factor.real, model.der_factor.imag
     s.int_type_psi = model.int_type_psi
     s.precision = precision
+    s.reginv_cold = 0 if warm_start else 1
     s.int_order = getattr(model, "int_order", 4)
     s.int_par1 = getattr(model, "int_par1", 0)
     expect = getattr(model, "expect", [])
@@ -340,10 +341,10 @@ def _cbuf(x: np.ndarray) -> np.ndarray:
 class GpuCore:
     """One device context for one model (one CUDA stream on the current device)."""
 
-    def __init__(self, model: Model, precision: int = 0):
+    def __init__(self, model: Model, precision: int = 0, warm_start: bool = True):
         self.lib = load_library()
         self.model = model
-        setup, self._keep = build_setup(model, precision)
+        setup, self._keep = build_setup(model, precision, warm_start)
         h = C.c_void_p()
         rc = self.lib.mctdh_create(C.byref(setup), C.byref(h))
         if rc != 0:

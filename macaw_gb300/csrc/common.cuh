@@ -94,6 +94,20 @@ __device__ __forceinline__ float4 load_split(const cplx* p, long long i, int fmt
   return w;
 }
 
+// (l, r) of fibre p < nfib = L * R (l fastest): 32-bit division whenever the
+// fibre count fits, the 64-bit one otherwise.
+__device__ __forceinline__ void fibre_lr(long long p, long long L, long long nfib, long long& l, long long& r) {
+  if (nfib <= 0xFFFFFFFFLL) {
+    const unsigned pu = (unsigned)p, Lu = (unsigned)L;
+    const unsigned ru = pu / Lu;
+    r = ru;
+    l = pu - ru * Lu;
+  } else {
+    r = p / L;
+    l = p - r * L;
+  }
+}
+
 // Status codes returned through the C-ABI (negative = error).
 enum {
   MCTDH_OK = 0,

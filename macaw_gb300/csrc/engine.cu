@@ -348,6 +348,7 @@ struct Ctx {
   int int_type_psi = 1;
   int precision = 0;
   int hole_prec = 0;   // single-hole contractions: 0 FP64, 1 FP32 sums, 2 compensated FP32
+  bool reginv_cold = false;   // regularised inverses without the Jacobi warm start
   std::string last_error;
   long long launches = 0;
   long long eom_count = 0, hb_count = 0;
@@ -664,6 +665,7 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.int_type_psi = (int)s->int_type_psi;
   c.int_order = (int)s->int_order;
   c.int_par1 = (int)s->int_par1;
+  c.reginv_cold = s->reginv_cold != 0;
   c.precision = (int)s->precision;
   if (c.precision < 0 || c.precision > 3) throw StatusError(MCTDH_EARG, "precision must be 0, 1, 2 or 3");
   // precision 3: the products of precision 1 with FP32-accumulated contractions
@@ -1381,6 +1383,11 @@ void plan_eom(Ctx& c) {
       rd.n = c.m_of(m, s);
       rd.regtype = 0;
       rd.eps = c.eps_rho;
+      if (!c.reginv_cold) {
+        rd.vprev = c.ar.calloc_c((long long)rd.n * rd.n);
+        rd.vcount = reinterpret_cast<int*>(c.ar.calloc_c(1));
+        CK(cudaMemset(rd.vcount, 0, sizeof(int)));   // no warm start before the first call
+      }
       rd.op_first = (int)c.mfop_h.size();
       for (int k = 0; k < c.noper[m]; ++k) {
         if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
@@ -3806,6 +3813,11 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
       E->msum_src_h.insert(E->msum_src_h.end(), c->msum_src_h.begin(), c->msum_src_h.end());
       for (RegInvDesc rd : c->reg_h) {
         rd.op_first += (int)E->mfop_h.size();
+        // no warm start in ensembles: the merged launches also refresh members that
+        // are not stepping, so a member's call history would differ from its own
+        // context's and its rounding with it
+        rd.vprev = nullptr;
+        rd.vcount = nullptr;
         E->reg_h.push_back(rd);
       }
       E->mfop_h.insert(E->mfop_h.end(), c->mfop_h.begin(), c->mfop_h.end());

@@ -43,6 +43,18 @@ __device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al,
   sl += t + e;
 }
 
+// acc (hi, lo) += a * b for plain FP32 a, b (no low parts): the same compensated
+// sum as df_fma without the two correction products that vanish.
+__device__ __forceinline__ void df_fma0(float& sh, float& sl, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float s = sh + p;
+  const float bp = s - sh;
+  const float t = (sh - (s - bp)) + (p - bp);
+  sh = s;
+  sl += t + e;
+}
+
 // PREC 0: FP64.  PREC 1: FP32 -- the products of the FP32-rounded x and M are
 // accumulated in FP32 (~1e-7 relative; the split's correction products would sit
 // at the accumulation's own rounding level), outputs complex FP32 (TF_F32) or
@@ -77,9 +89,10 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   }
   __syncthreads();
   const long long p = (long long)(blockIdx.x - d.block_start) * blockDim.x + threadIdx.x;
-  const long long L = d.L;
-  if (p >= L * d.R) return;
-  const long long l = p % L, r = p / L;
+  const long long L = d.L, nfib = L * d.R;
+  if (p >= nfib) return;
+  long long l, r;
+  fibre_lr(p, L, nfib, l, r);
   const long long xi0 = l + L * (long long)nin * r;
   cplx* y0 = d.Y + l + L * (long long)nout * r;
   const cplx alpha = d.alpha;
@@ -191,7 +204,10 @@ __device__ void dot_block(const HoleDesc& d, int b, cplx* red) {
 }
 
 // PREC 0: FP64.  PREC 2: operands split into FP32 hi + lo parts, products and sums
-// carried as compensated FP32 pairs (df_fma), ~1e-13 relative.
+// carried as compensated FP32 pairs (df_fma), ~1e-13 relative; complex-FP32
+// operands on both sides skip the vanishing low-part products (df_fma0).
+// PREC 1: FP32 operands (rounded to nearest), FP32 products and sums (~1e-7
+// relative), the block partials widened to FP64 for the deterministic reduction.
 template <int PREC>
 __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
   __shared__ int s_di;
@@ -199,6 +215,8 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   __shared__ cplx Ys[HOLE_TILE * MAXN_SPF];
   float4* Xf = reinterpret_cast<float4*>(Xs);   // PREC 2: (re hi, im hi, re lo, im lo)
   float4* Yf = reinterpret_cast<float4*>(Ys);
+  float2* X1 = reinterpret_cast<float2*>(Xs);   // PREC 1 and complex-FP32 operands: (re, im)
+  float2* Y1 = reinterpret_cast<float2*>(Ys);
   if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
   __syncthreads();
   const HoleDesc& d = descs[s_di];
@@ -211,6 +229,9 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   const long long L = d.L, nfib = d.L * d.R;
   const long long ntiles = (nfib + HOLE_TILE - 1) / HOLE_TILE;
   const int tid = threadIdx.x;
+  // PREC 2 with complex-FP32 operands on both sides: exact products of plain FP32
+  // numbers into the compensated sums (the staging keeps (re, im) pairs)
+  const bool f32in = PREC == 2 && d.xfmt == TF_F32 && d.yfmt == TF_F32;
   const bool small = npairs <= HOLE_THREADS;
   const int G = small ? HOLE_THREADS / npairs : 1;
   const int pair0 = small ? tid % npairs : tid;
@@ -218,26 +239,41 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   cplx acc[4] = {mkc(0, 0), mkc(0, 0), mkc(0, 0), mkc(0, 0)};
   float ah[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   float al[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  // Staging: thread tid always loads fibre q = tid % HOLE_TILE of a tile and the
+  // columns j = tid / HOLE_TILE, + HOLE_THREADS / HOLE_TILE, ...; its fibre's
+  // (l, r) is carried from tile to tile instead of divided out per element.
+  static_assert(HOLE_THREADS % HOLE_TILE == 0, "staging assumes whole tiles per thread row");
+  const int qt = tid % HOLE_TILE, jt = tid / HOLE_TILE, jstep = HOLE_THREADS / HOLE_TILE;
+  long long pcur = (long long)b * HOLE_TILE + qt;
+  long long lcur = pcur % L, rcur = pcur / L;
+  const long long pstep = (long long)d.nblk * HOLE_TILE;
+  const long long dl = pstep % L, dr = pstep / L;
   for (long long tile = b; tile < ntiles; tile += d.nblk) {
-    const long long p0 = tile * HOLE_TILE;
-    for (int e = tid; e < HOLE_TILE * n1; e += HOLE_THREADS) {
-      int q = e % HOLE_TILE, j = e / HOLE_TILE;
-      long long p = p0 + q;
-      long long idx = -1;
-      if (p < nfib) { long long l = p % L, r = p / L; idx = l + L * (j + (long long)n1 * r); }
+    const bool in_range = pcur < nfib;
+    const long long xb = lcur + L * (long long)n1 * rcur, yb = lcur + L * (long long)n2 * rcur;
+    pcur += pstep;
+    lcur += dl;
+    rcur += dr;
+    if (lcur >= L) { lcur -= L; rcur += 1; }
+    const int q = qt;
+    for (int j = jt; j < n1; j += jstep) {
+      const long long idx = in_range ? xb + L * j : -1;
       if (PREC == 0) {
         Xs[q * MAXN_SPF + j] = (idx >= 0) ? load_c(d.X, idx, d.xfmt) : mkc(0, 0);
+      } else if (PREC == 1 || f32in) {
+        const float4 w = (idx >= 0) ? load_split(d.X, idx, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
+        X1[q * MAXN_SPF + j] = make_float2(w.x + w.z, w.y + w.w);
       } else {
         Xf[q * MAXN_SPF + j] = (idx >= 0) ? load_split(d.X, idx, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    for (int e = tid; e < HOLE_TILE * n2; e += HOLE_THREADS) {
-      int q = e % HOLE_TILE, j = e / HOLE_TILE;
-      long long p = p0 + q;
-      long long idx = -1;
-      if (p < nfib) { long long l = p % L, r = p / L; idx = l + L * (j + (long long)n2 * r); }
+    for (int j = jt; j < n2; j += jstep) {
+      const long long idx = in_range ? yb + L * j : -1;
       if (PREC == 0) {
         Ys[q * MAXN_SPF + j] = (idx >= 0) ? load_c(d.Y, idx, d.yfmt) : mkc(0, 0);
+      } else if (PREC == 1 || f32in) {
+        const float4 w = (idx >= 0) ? load_split(d.Y, idx, d.yfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
+        Y1[q * MAXN_SPF + j] = make_float2(w.x + w.z, w.y + w.w);
       } else {
         Yf[q * MAXN_SPF + j] = (idx >= 0) ? load_split(d.Y, idx, d.yfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
@@ -258,6 +294,19 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
       for (int q = q0; q < HOLE_TILE; q += qs) {
         if (PREC == 0) {
           cfma_conj(acc[k], Xs[q * MAXN_SPF + j1], Ys[q * MAXN_SPF + j2]);
+        } else if (PREC == 1) {
+          const float2 x = X1[q * MAXN_SPF + j1], y = Y1[q * MAXN_SPF + j2];
+          ah[k][0] = fmaf(x.x, y.x, ah[k][0]);
+          ah[k][0] = fmaf(x.y, y.y, ah[k][0]);
+          ah[k][1] = fmaf(x.x, y.y, ah[k][1]);
+          ah[k][1] = fmaf(-x.y, y.x, ah[k][1]);
+        } else if (f32in) {
+          // complex FP32 operands on both sides (no low parts)
+          const float2 x = X1[q * MAXN_SPF + j1], y = Y1[q * MAXN_SPF + j2];
+          df_fma0(ah[k][0], al[k][0], x.x, y.x);
+          df_fma0(ah[k][0], al[k][0], x.y, y.y);
+          df_fma0(ah[k][1], al[k][1], x.x, y.y);
+          df_fma0(ah[k][1], al[k][1], -x.y, y.x);
         } else {
           // conj(x) y: re = xr yr + xi yi, im = xr yi - xi yr
           const float4 x = Xf[q * MAXN_SPF + j1], y = Yf[q * MAXN_SPF + j2];
@@ -298,6 +347,8 @@ void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStre
   if (ndesc <= 0 || nblocks <= 0) return;
   if (prec == 0)
     hole_kernel<0><<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
+  else if (prec == 1)
+    hole_kernel<1><<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
   else
     hole_kernel<2><<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
 }
@@ -680,9 +731,55 @@ __global__ void __launch_bounds__(32) reginv_kernel(const RegInvDesc* __restrict
     A[i + ld * j] = v;
   }
   __syncthreads();
+  // Warm start: rho changes little between consecutive calls (the mean-field
+  // evaluations of one propagation), so the previous eigenvectors Vp nearly
+  // diagonalise it; Jacobi then runs on Vp^H A Vp and the eigenvectors are Vp V.
+  // The same eigen-decomposition up to rounding, in one or two sweeps instead of
+  // a cold start's six to ten.  Every 64th call starts cold, which bounds the
+  // drift of the accumulated product from unitarity.
+  const int wcount = d.vprev ? *d.vcount : 0;
+  const bool warm = wcount > 0 && wcount < 64;
+  if (warm) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // Inv <- A Vp
+      const int i = e % n, j = e / n;
+      cplx s = mkc(0, 0);
+      for (int k = 0; k < n; ++k) cfma(s, A[i + ld * k], d.vprev[k + n * j]);
+      Inv[i + ld * j] = s;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // V <- Vp^H Inv
+      const int i = e % n, j = e / n;
+      cplx s = mkc(0, 0);
+      for (int k = 0; k < n; ++k) cfma_conj(s, d.vprev[k + n * i], Inv[k + ld * j]);
+      V[i + ld * j] = s;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // Hermitian from the upper triangle
+      const int i = e % n, j = e / n;
+      cplx v = (i <= j) ? V[i + ld * j] : cconj(V[j + ld * i]);
+      if (i == j) v.y = 0.0;
+      A[i + ld * j] = v;
+    }
+    __syncthreads();
+  }
   bool ok;
   jacobi_herm(A, V, n, ld, R, &ok);
   if (!ok && threadIdx.x == 0) atomicOr(status, DEVST_EIG_NOCONV);
+  if (warm) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // Inv <- Vp V
+      const int i = e % n, j = e / n;
+      cplx s = mkc(0, 0);
+      for (int k = 0; k < n; ++k) cfma(s, d.vprev[i + n * k], V[k + ld * j]);
+      Inv[i + ld * j] = s;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) V[e % n + ld * (e / n)] = Inv[e % n + ld * (e / n)];
+    __syncthreads();
+  }
+  if (d.vprev) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) d.vprev[e] = V[e % n + ld * (e / n)];
+    if (threadIdx.x == 0) *d.vcount = (warm && ok) ? wcount + 1 : (ok ? 1 : 0);
+  }
   if (threadIdx.x < n) {
     double wv = A[threadIdx.x + ld * threadIdx.x].x;
     double f;

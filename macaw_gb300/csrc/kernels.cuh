@@ -91,6 +91,10 @@ struct RegInvDesc {
   int regtype;             // 0 'poly', 1 'tikh'
   double eps;
   int op_first, op_count;
+  // optional warm start: the eigenvectors of the previous call (n x n) and the
+  // number of consecutive warm starts behind them (0: none yet)
+  cplx* vprev;
+  int* vcount;
 };
 struct MFOp {
   const cplx* mf;          // n x n2 (ld n)
