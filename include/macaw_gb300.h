@@ -345,6 +345,18 @@ int64_t mctdh_ens_counters(mctdh_ens_t *ens, int64_t *launches, int64_t *eom, in
 int64_t mctdh_ens_stream(mctdh_ens_t *ens, void **stream);
 const char *mctdh_ens_last_error(mctdh_ens_t *ens);
 
+/* Tensor-core kernels (no reference counterpart).  The FP32 mode products of the
+ * split-precision paths run as tcgen05 MMAs (TF32 parts, FP32 accumulation) for
+ * batches whose largest SPF count is at least min_n (default 9; below it the
+ * CUDA-core kernel is faster) and at most 16, with a one- or two-stage pipeline
+ * (default 2).  status: *enabled is 1 unless the environment variable
+ * MACAW_GB300_TC=0 selected the CUDA-core kernels for this process; *timeouts is
+ * 1 when a tensor-core kernel gave up waiting for its MMAs since the previous
+ * call (the flag is cleared).  config: 0 keeps a setting; it applies to launches
+ * issued afterwards (CUDA graphs captured earlier keep their kernels). */
+int64_t mctdh_tensor_core_status(int64_t *enabled, int64_t *timeouts);
+int64_t mctdh_tensor_core_config(int64_t min_n, int64_t stages);
+
 /* Last error message of the context (or of the last failed create when ctx is NULL). */
 const char *mctdh_last_error(mctdh_ctx_t *ctx);
 

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmacaw_gb300.so")
-SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu", "mlp.cu", "gwp.cu"]
+SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu", "mlp.cu", "gwp.cu", "tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

@@ -89,6 +89,8 @@ def load_library() -> C.CDLL:
     lib.mctdh_density.argtypes = [vp, C.c_int64, DP, C.c_int64, C.c_double, C.c_double, DP, DP]
     lib.mctdh_wf_ovl.argtypes = [vp, DP, DP, DP, DP, DP, DP]
     lib.mctdh_launch_count.argtypes = [vp]
+    lib.mctdh_tensor_core_status.argtypes = [I64P, I64P]
+    lib.mctdh_tensor_core_config.argtypes = [C.c_int64, C.c_int64]
     lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
     lib.mctdh_event_record.argtypes = [vp, C.c_int64]
     lib.mctdh_event_elapsed.argtypes = [vp, C.c_int64, C.c_int64, DP]
@@ -156,7 +158,8 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_norm_wf", "mctdh_wf_ovl", "mctdh_launch_count", "mctdh_last_error", "mctdh_step",
             "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets", "mctdh_device_bytes",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
-            "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc",
+            "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc", "mctdh_tensor_core_status",
+            "mctdh_tensor_core_config",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
@@ -609,6 +612,25 @@ class GpuCore:
             stats["eom"] += ne
         self.stats = stats
         return outs
+
+
+def tensor_core_status() -> Dict[str, int]:
+    """Whether the tensor-core kernels are in use (MACAW_GB300_TC) and whether one
+    of them gave up waiting for its MMAs since the previous call."""
+    lib = load_library()
+    en, to = C.c_int64(), C.c_int64()
+    rc = lib.mctdh_tensor_core_status(C.byref(en), C.byref(to))
+    if rc != 0:
+        raise MctdhError(rc, "tensor-core status")
+    return {"enabled": en.value, "timeouts": to.value}
+
+
+def tensor_core_config(min_n: int = 0, stages: int = 0) -> None:
+    """Smallest SPF count served by the tensor-core mode product and its pipeline
+    stages (0 keeps a setting)."""
+    rc = load_library().mctdh_tensor_core_config(min_n, stages)
+    if rc != 0:
+        raise MctdhError(rc, "tensor-core config")
 
 
 def fp64_peak_tflops() -> float:

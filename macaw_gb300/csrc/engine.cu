@@ -4364,6 +4364,7 @@ int64_t mctdh_create(const mctdh_setup_t* setup, mctdh_ctx_t** out) {
   *out = nullptr;
   try {
     Ctx* c = create(setup);
+    if (tc_enabled()) tc_prepare();
     *out = new mctdh_ctx{c};
     g_create_error.clear();
     return MCTDH_OK;
@@ -4866,6 +4867,7 @@ int64_t mctdh_ens_create(const mctdh_setup_t* setups, int64_t n, mctdh_ens_t** o
   *out = nullptr;
   try {
     Ens* e = ens_create(setups, (int)n);
+    if (tc_enabled()) tc_prepare();
     *out = new mctdh_ens{e};
     g_create_error.clear();
     return MCTDH_OK;

@@ -9,6 +9,7 @@
 
 #include "kernels.cuh"
 #include <stdio.h>
+#include <stdlib.h>
 
 // ---------------------------------------------------------------------------
 // descriptor lookup: descriptors are sorted by block_start
@@ -165,8 +166,21 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   }
 }
 
-void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, int prec) {
+// Tensor-core kernels (tc.cu) serve the FP32 products unless MACAW_GB300_TC=0
+// selects the CUDA-core kernels (read once per process).
+bool tc_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("MACAW_GB300_TC");
+    on = (e && e[0] == '0') ? 0 : 1;
+  }
+  return on == 1;
+}
+
+void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, int prec,
+                 bool allow_tc) {
   if (ndesc <= 0 || nblocks <= 0) return;
+  if (prec == 1 && allow_tc && tc_enabled() && launch_prod_tc(d_descs, ndesc, nblocks, maxn, st)) return;
   const unsigned nb = (unsigned)nblocks;
   if (maxn <= 12) {
     if (prec == 0) prod_kernel<12, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
