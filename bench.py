@@ -39,9 +39,15 @@ WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/
 EPS_CMF = 1e-5
 PRE_FS = 1.0
 MFX_EPOCHS = 12
-TRAFFIC_PER_ALG_BYTE = 0.51   # ncu DRAM bytes per algorithmic byte, mode products of this model
-ACC_FS = 0.5   # interval over which the split path is compared with the FP64 path
-REF_STEP_FS = 0.1   # CMF2 step length the reference arm times (steady-state steps are of this order)
+# ncu DRAM bytes per algorithmic byte of a kernel class in the benchmark regime
+# (one capture of the profile case), and what bounds each class there
+TRAFFIC_PER_ALG_BYTE = {"mode_product": 0.51}
+ROOF_BOUND = {"mode_product": "hbm", "hole_contract": "hbm", "spf_derivative": "hbm"}
+ROOF_NOTE = {"mode_product": "L2-resident operands (12.6 MB state): issue and L2 latency, not HBM",
+             "hole_contract": "compensated FP32 sums: FP32 issue",
+             "spf_derivative": "small per-mode problems: latency and occupancy"}
+ACC_FS = 0.5   # short comparison interval of the size scan
+REF_BUDGET_S = 150.0   # timed seconds after which the reference arm stops early
 
 
 def make_model():
@@ -144,52 +150,126 @@ def flush_l2(buf):
     buf.add_(1.0)
 
 
-def cpu_baseline(model, A, psi, h, budget_s=40.0):
-    """The oracle on a bounded sample: fixed-length CMF2 attempts of length h."""
+PRECISION_LABEL = {0: "fp64", 1: "fp32 products, compensated fp32 contractions",
+                   2: "compensated fp32 products and contractions", 3: "fp32 products and contractions",
+                   4: "fp32 mean-field products, compensated H_B products and contractions",
+                   5: "compensated mean-field products and contractions, fp32 H_B products"}
+
+
+def precision_label(prec):
+    return PRECISION_LABEL[prec]
+
+
+def static_config(ws):
+    """The workload definition both arms report (nothing measured in it)."""
+    return {"workload": WORKLOAD, "integrator": "cmf2", "eps_cmf": EPS_CMF, "start_fs": PRE_FS,
+            "step": "one accepted adaptive CMF2 step (reference step control)",
+            "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{ws}"}
+
+
+_ONE_THREAD = r"""
+import sys, time, numpy as np
+sys.path.insert(0, sys.argv[1])
+from bench import make_model
+from oracle.mctdh import Oracle
+d = np.load(sys.argv[2])
+o = Oracle(make_model())
+t0 = time.perf_counter()
+o.cmf2_fixed(d["A"], d["psi"], float(d["t"]), float(d["h"]))
+print(time.perf_counter() - t0)
+"""
+
+
+def cpu_baseline(model, A1, psi1, t1, h, gpu64, steps=2):
+    """The oracle on a bounded sample of the workload: `steps` CMF2 steps of the
+    GPU arm's mean step length from the state the GPU arm starts from, with all
+    host cores (NumPy's BLAS threads), and one step single-threaded in a child
+    process.  The same steps through the FP64 device path (mctdh_cmf2_attempt)
+    give the parity check carried in the line."""
+    import tempfile
     from oracle.mctdh import Oracle
     o = Oracle(model)
-    t0 = time.perf_counter()
-    n = 0
-    A_, p_ = A.copy(), psi.copy()
-    while True:
-        A_, p_, _ = o.cmf2_fixed(A_, p_, 0.0, h)
-        n += 1
-        el = time.perf_counter() - t0
-        if el > budget_s or n >= 3:
-            break
-    return dict(value=n * h * AU2FS / el, unit="fs/s", cores=os.cpu_count(), kind="port",
-                sample=f"{n} CMF2 step(s) of {h * AU2FS:.4f} fs on the full qvc12 model, NumPy oracle "
-                       f"(BLAS threads = host cores), {el:.1f} s")
+    rA, rp = A1.copy(), psi1.copy()
+    gA, gp = A1.copy(), psi1.copy()
+    el = 0.0
+    for k in range(steps):
+        w0 = time.perf_counter()
+        rA, rp, _ = o.cmf2_fixed(rA, rp, t1 + k * h, h)
+        el += time.perf_counter() - w0
+        gA, gp, _ = gpu64.cmf2_attempt(gA, gp, t1 + k * h, h)
+    tend = t1 + steps * h
+    gpu64.set_state(gA, gp, as_start=False)
+    go = gpu64.observables(tend)
+    ro = o.observables(rA, rp, *initial_wavefunction(model), tend)
+    parity = {"max_abs_dA": float(np.abs(gA - rA).max()), "max_abs_dpsi": float(np.abs(gp - rp).max()),
+              "d_auto": abs(go["auto"] - ro["auto"]), "d_pop": float(np.abs(go["pop"] - ro["pop"]).max()),
+              "d_energy": abs(go["energy"] - ro["energy"]), "d_norm": abs(go["norm"] - ro["norm"]),
+              "steps": steps, "step_fs": h * AU2FS, "from_fs": t1 * AU2FS,
+              "what": "FP64 device path vs the CPU oracle on the same CMF2 steps: observables and A within "
+                      "1e-10, SPF values within 1e-9"}
+    out = dict(value=steps * h * AU2FS / el, unit="fs/s", cores=os.cpu_count(), kind="port",
+               sample=f"{steps} CMF2 steps of {h * AU2FS:.4f} fs from the {t1 * AU2FS:.2f} fs state of the qvc12 "
+                      f"model, NumPy oracle, BLAS threads = host cores, {el:.1f} s")
+    try:
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "state.npz")
+            np.savez(path, A=A1, psi=psi1, t=t1, h=h)
+            env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
+            r = subprocess.run([sys.executable, "-c", _ONE_THREAD, ROOT, path], env=env, capture_output=True,
+                               text=True, timeout=600)
+            sec = float(r.stdout.strip().splitlines()[-1])
+        out["single_thread"] = {"value": h * AU2FS / sec, "unit": "fs/s", "cores": 1, "kind": "port",
+                                "sample": f"1 CMF2 step of {h * AU2FS:.4f} fs, NumPy oracle, one BLAS thread, "
+                                          f"{sec:.1f} s"}
+    except Exception as exc:   # the single-thread row is informative only
+        out["single_thread"] = {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
+    return out, parity
 
 
 def run_reference(args):
+    """The CPU oracle on the GPU arm's workload and schedule: it propagates the
+    qvc12 model from t = 0 to 1 fs untimed with its own adaptive CMF2 (first trial
+    step 0.01 fs instead of tout * eps_int, to keep the untimed part short), then
+    `warmup` untimed and up to `steps` timed accepted CMF2 steps under the
+    reference's step control, with all host cores (NumPy's BLAS threads); the
+    timed part stops early after REF_BUDGET_S and the line says how many steps it
+    took."""
     ws, rank, tdist = dist_setup()
     if rank != 0:
         return 0
+    from oracle.mctdh import Oracle
     model = make_model()
     A, psi = initial_wavefunction(model)
-    h = REF_STEP_FS / AU2FS
-    from oracle.mctdh import Oracle
     o = Oracle(model)
-    # each step: one fixed-length CMF2 step of the oracle; bounded to a few minutes
-    t_total, fs_total, n = 0.0, 0.0, 0
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        A, psi, _ = o.cmf2_fixed(A, psi, 0.0, h)
-        el = time.perf_counter() - t0
-        if i >= min(args.warmup, 1):
-            t_total += el
-            fs_total += h * AU2FS
-            n += 1
-        if t_total > 150.0 and n >= 1:
+    t, h = 0.0, 0.01 / AU2FS
+    w0 = time.perf_counter()
+    while t < PRE_FS / AU2FS - 1e-9:
+        A, psi, hdid, h, _ = o.cmf2(A, psi, t, min(h, PRE_FS / AU2FS - t))
+        t += hdid
+    pre_s = time.perf_counter() - w0
+    for _ in range(args.warmup):
+        A, psi, hdid, h, _ = o.cmf2(A, psi, t, h)
+        t += hdid
+    t_total, fs_total, n, hd = 0.0, 0.0, 0, []
+    for i in range(args.steps):
+        w0 = time.perf_counter()
+        A, psi, hdid, h, _ = o.cmf2(A, psi, t, h)
+        t_total += time.perf_counter() - w0
+        t += hdid
+        fs_total += hdid * AU2FS
+        hd.append(hdid * AU2FS)
+        n += 1
+        if t_total > REF_BUDGET_S:
             break
     v = fs_total / t_total
-    line = {"metric": METRIC, "value": v, "unit": "fs/s", "n_gpus": ws, "steps": n, "warmup": min(args.warmup, 1),
+    line = {"metric": METRIC, "value": v, "unit": "fs/s", "n_gpus": ws, "steps": n, "warmup": args.warmup,
             "ms_per_step": 1e3 * t_total / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c128", "data": "synthetic (seeded qvc12 model)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "integrator": "cmf2", "step_fs": h * AU2FS},
+            "config": static_config(ws), "precision": "fp64", "step_fs_mean": statistics.mean(hd),
             "cpu_baseline": {"value": v, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{n} fixed CMF2 steps of {h * AU2FS} fs, NumPy oracle on host cores"},
+                             "sample": f"{n} adaptive CMF2 steps from {PRE_FS} fs (mean {statistics.mean(hd):.4f} "
+                                       f"fs), NumPy oracle on the host cores; untimed 0 -> {PRE_FS} fs took "
+                                       f"{pre_s:.0f} s"},
             "e2e": {"value": v, "unit": "fs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -258,19 +338,29 @@ def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mf
 
 def run_size_scan(args):
     """qvc12n: the benchmark model with `--nspf` SPFs per mode and state (12: 2.99 M
-    configurations per state, 143 MB of coefficients, beyond the 129 MB L2), split
-    path against the FP64 path from the same state at 1 fs, as the benchmark line
-    does (no learned extrapolator, no CPU baseline)."""
+    configurations per state, 143 MB of coefficients, beyond the 129 MB L2); qvc24:
+    4 states, 24 DOFs in 8 three-DOF modes of 12^3 grids, 8 SPFs (16.8 M
+    configurations per state, 1.07 GB).  Split path against the FP64 path from the
+    same state (1 fs of FP64 CMF2 for qvc12n, `--pre-fs` for qvc24), as the
+    benchmark line does (no learned extrapolator, no CPU baseline)."""
     import torch
     from macaw_gb300.capi import GpuCore
+    from macaw_gb300.generate import qvc24
     _, _, tdist = dist_setup()
     torch.cuda.init()
-    model = qvc12(nspf=args.nspf, eps_int=EPS_CMF, eps_lanczos=1e-8, eps_spf=1e-7)
+    if args.workload == "qvc24":
+        model = qvc24(eps_int=EPS_CMF, eps_lanczos=1e-8, eps_spf=1e-7)
+        pre_fs = args.pre_fs
+    else:
+        model = qvc12(nspf=args.nspf, eps_int=EPS_CMF, eps_lanczos=1e-8, eps_spf=1e-7)
+        pre_fs = PRE_FS
     A0, psi0 = initial_wavefunction(model)
     l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     pre = GpuCore(model, precision=0)
     pre.set_state(A0, psi0, as_start=True)
-    t1, h1, _, _, _ = pre.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
+    w0 = time.perf_counter()
+    t1, h1, _, _, _ = pre.propagate_interval(INT_CMF2, pre_fs / AU2FS, 0.0, model.tout * model.eps_int)
+    pre_s = time.perf_counter() - w0
     A1, psi1 = pre.get_state()
     pre.close()
     state = (A0, psi0, A1, psi1)
@@ -278,26 +368,30 @@ def run_size_scan(args):
         ref_core, ref = run_arm(model, 0, state, t1, h1, args, l2, torch, tdist, profile=False)
         mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=False)
     cmp = {}
+    acc_fs = ACC_FS if args.workload != "qvc24" else 0.1
     for name, core in (("fp64", ref_core), ("mixed", mix_core)):
         core.set_state(A1, psi1, as_start=False)
-        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + ACC_FS / AU2FS, t1, h1)
+        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + acc_fs / AU2FS, t1, h1)
         cmp[name] = core.observables(tt)
     value = mix["fs"] / (mix["ms"] * 1e-3)
     fp64_value = ref["fs"] / (ref["ms"] * 1e-3)
     ntot = int(model.naconftot)
-    line = {"metric": f"simulated fs/s (qvc12, {args.nspf} SPFs, CMF2)", "value": value, "unit": "fs/s",
+    wl = f"qvc12, {args.nspf} SPFs" if args.workload != "qvc24" else "qvc24, 8 modes x 8 SPFs, 4 states"
+    line = {"metric": f"simulated fs/s ({wl}, CMF2)", "value": value, "unit": "fs/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mix["ms"] / args.steps,
-            "higher_is_better": True, "precision": args.precision,
+            "higher_is_better": True, "precision": precision_label(args.precision),
             "fp64_path": {"value": fp64_value, "ms_per_step": ref["ms"] / args.steps},
             "speedup_vs_fp64_path": value / fp64_value,
             "accuracy_vs_fp64_path": {"dC": abs(cmp["mixed"]["auto"] - cmp["fp64"]["auto"]),
                                       "dpop": float(np.abs(cmp["mixed"]["pop"] - cmp["fp64"]["pop"]).max()),
-                                      "over_fs": ACC_FS, "from_fs": PRE_FS},
+                                      "over_fs": acc_fs, "from_fs": t1 * AU2FS},
+            "untimed_pre_propagation_s": pre_s,
             "eom_per_s": mix["eom"] / (mix["ms"] * 1e-3), "hb_per_s": mix["hb"] / (mix["ms"] * 1e-3),
             "fp64_eom_per_s": ref["eom"] / (ref["ms"] * 1e-3),
             "clocks": clk.summary(),
             "device_bytes": {"fp64": ref_core.device_bytes(), "split": mix_core.device_bytes()},
-            "config": {"workload": "qvc12n", "nspf": args.nspf, "coefficients": ntot,
+            "config": {"workload": args.workload, "nspf": args.nspf if args.workload != "qvc24" else 8,
+                       "coefficients": ntot,
                        "coefficient_bytes": 16 * ntot, "dimpsi": int(model.dimpsi),
                        "l2": "flushed (256 MB write) before every timed step"}}
     print(json.dumps(line), flush=True)
@@ -306,7 +400,7 @@ def run_size_scan(args):
 
 def run_gpu(args):
     import torch
-    from macaw_gb300.capi import GpuCore, fp64_peak_tflops
+    from macaw_gb300.capi import GpuCore, fp64_peak_tflops, tensor_core_status
     ws, rank, tdist = dist_setup()
     torch.cuda.init()
     model = make_model()
@@ -314,7 +408,7 @@ def run_gpu(args):
     l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
     # leave the start-up transient of the step control (the reference starts at
     # tout * eps_int, propagator.f90:103, and grows by at most 1.5x per CMF2 step):
-    # propagate 1 fs untimed with the FP64 path; both arms start from that state
+    # propagate 1 fs untimed with the FP64 path; every arm starts from that state
     pre = GpuCore(model, precision=0)
     pre.set_state(A0, psi0, as_start=True)
     pre.mfx_record(2)   # the untimed FP64 steps are the extrapolator's training data
@@ -326,53 +420,67 @@ def run_gpu(args):
     net, fscale, tscale, tr_loss = mfx.train(X, R, steps=ks, epochs=MFX_EPOCHS)
     train_s = time.perf_counter() - tr0
     pre.close()
+    mfx_net = (net, fscale, tscale)
     state = (A0, psi0, A1, psi1)
+    head_is_mfx = args.headline == "mfx"
     with ClockSampler(torch.cuda.current_device()) as clk:
         ref_core, ref = run_arm(model, 0, state, t1, h1, args, l2, torch, tdist, profile=False)
-        mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=True)
-        mfx_core, mfxr = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=False,
-                                 mfx_net=(net, fscale, tscale))
-    # accuracy against the plain FP64 path: every arm propagates the same state over
-    # the same output interval; C(t) and populations are compared there
-    cmp = {}
-    for name, core in (("fp64", ref_core), ("mixed", mix_core), ("mfx", mfx_core)):
-        core.set_state(A1, psi1, as_start=False)
-        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + ACC_FS / AU2FS, t1, h1)
-        cmp[name] = core.observables(tt)
-    dC = abs(cmp["mixed"]["auto"] - cmp["fp64"]["auto"])
-    dpop = float(np.abs(cmp["mixed"]["pop"] - cmp["fp64"]["pop"]).max())
+        mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist,
+                                profile=not head_is_mfx)
+        mfx_core, mfxr = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist,
+                                 profile=head_is_mfx, mfx_net=mfx_net)
     mfx_stats = mfx_core.mfx_stats()
-    ms_total, fs_total = mix["ms"], mix["fs"]
-    ms_total, ref["ms"], mfxr["ms"] = max_over_ranks([ms_total, ref["ms"], mfxr["ms"]], tdist)
-    value = ws * fs_total / (ms_total * 1e-3)
+    ref["ms"], mix["ms"], mfxr["ms"] = max_over_ranks([ref["ms"], mix["ms"], mfxr["ms"]], tdist)
     fp64_value = ws * ref["fs"] / (ref["ms"] * 1e-3)
+    split_value = ws * mix["fs"] / (mix["ms"] * 1e-3)
     mfx_value = ws * mfxr["fs"] / (mfxr["ms"] * 1e-3)
+    head, head_core = (mfxr, mfx_core) if head_is_mfx else (mix, mix_core)
+    value = mfx_value if head_is_mfx else split_value
 
-    # e2e: the reference-facing host-buffer call (mctdh_cmf2) with pinned buffers,
-    # host<->device copies of A and psi inside every step
-    Ah, ph = mix_core.get_state()
+    # e2e: the reference-facing host-buffer call (mctdh_cmf2) of the headline arm
+    # with pinned buffers, host<->device copies of A and psi inside every step
+    Ah, ph = head_core.get_state()
     pA = torch.from_numpy(Ah.copy()).pin_memory()
     pP = torch.from_numpy(ph.copy()).pin_memory()
     import ctypes as C
     DPp = C.POINTER(C.c_double)
     hd, hn = C.c_double(), C.c_double()
     e2e_fs, e2e_s = 0.0, 0.0
-    te, he = mix["t"], mix["h"]
+    te, he = head["t"], head["h"]
     for _ in range(max(1, args.steps // 2)):
         flush_l2(l2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rc = mix_core.lib.mctdh_cmf2(mix_core.h, C.cast(pA.data_ptr(), DPp), C.cast(pP.data_ptr(), DPp), te, he,
-                                     C.byref(hd), C.byref(hn))
+        rc = head_core.lib.mctdh_cmf2(head_core.h, C.cast(pA.data_ptr(), DPp), C.cast(pP.data_ptr(), DPp), te, he,
+                                      C.byref(hd), C.byref(hn))
         e2e_s += time.perf_counter() - t0
         if rc != 0:
-            raise RuntimeError(mix_core.lib.mctdh_last_error(mix_core.h).decode())
+            raise RuntimeError(head_core.lib.mctdh_last_error(head_core.h).decode())
         te += hd.value
         he = hn.value
         e2e_fs += hd.value * AU2FS
     nbytes = 16 * (model.naconftot + model.dimpsi)
 
-    prof = mix["prof"]
+    tc = tensor_core_status()
+    # accuracy of the split arms against the FP64 path over the whole propagation
+    # (outside the timed region; rank 0 of a single-GPU run)
+    acc_split, acc_mfx = None, None
+    if rank == 0 and ws == 1 and args.acc_fs > 0:
+        acc = accuracy_arms(model, [args.precision], args.acc_fs, mfx_net=mfx_net, mfx_precision=args.precision)
+
+        def summary(a):
+            return {"max_dC": a["max_dC"], "max_dpop": a["max_dpop"], "end_dC": a["end_dC"],
+                    "end_dpop": a["end_dpop"], "max_denergy": a["max_denergy"], "over_fs": args.acc_fs,
+                    "from_fs": 0.0, "compared_every_fs": model.tout * AU2FS, "bars": {"dC": 1e-6, "dpop": 1e-5},
+                    "within_bars": bool(a["max_dC"] <= 1e-6 and a["max_dpop"] <= 1e-5),
+                    "free_running_fs_per_s": a["fs_per_s"],
+                    "free_running_fp64_fs_per_s": acc["fp64"]["fs_per_s"],
+                    "eom_per_fs": a["eom"] / args.acc_fs, "fp64_eom_per_fs": acc["fp64"]["eom"] / args.acc_fs}
+        acc_split = summary(acc["arms"][str(args.precision)])
+        acc_mfx = summary(acc["arms"]["mfx"])
+        acc_mfx["extrapolator"] = acc["arms"]["mfx"].get("extrapolator")
+
+    prof = head["prof"]
     peaks, peak_src = load_peaks()
     fp64_peak = fp64_peak_tflops()
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
@@ -384,55 +492,64 @@ def run_gpu(args):
     achieved_tf = fl_launch / (avg_ms * 1e-3) / 1e12 if avg_ms > 0 else 0.0
     clocks = clk.summary()
     tot_ms = max(sum(x["ms"] for x in prof.values()), 1e-9)
+    prec_label = precision_label(args.precision)
     line = {
         "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128 state; " + prec_label,
         "data": "synthetic (seeded qvc12 model)",
-        "config": {"workload": WORKLOAD, "integrator": "cmf2",
-                   "precision": {0: "fp64", 1: "split-fp32", 2: "split-fp32-compensated"}[args.precision],
-                   "eps_cmf": EPS_CMF, "l2": "flushed (256 MB write) before every timed step",
-                   "step_fs_mean": statistics.mean(mix["hdids"]), "parallelism": f"replicas x{ws}"},
+        "config": static_config(ws),
+        "arm": ("split precision with the learned mean-field extrapolator" if head_is_mfx else
+                "split precision"),
+        "precision": prec_label,
+        "tensor_cores": {"enabled": bool(tc["enabled"]), "mma_wait_timeouts": tc["timeouts"],
+                         "served": "FP32 mode products of batches with 9-16 SPFs"},
+        "step_fs_mean": statistics.mean(head["hdids"]),
         "fp64_path": {"value": fp64_value, "unit": "fs/s", "ms_per_step": ref["ms"] / args.steps,
-                      "step_fs_mean": statistics.mean(ref["hdids"])},
+                      "step_fs_mean": statistics.mean(ref["hdids"]),
+                      "eom_per_s": ref["eom"] / (ref["ms"] * 1e-3)},
         "speedup_vs_fp64_path": value / fp64_value,
-        "accuracy_vs_fp64_path": {"dC": dC, "dpop": dpop, "over_fs": ACC_FS, "from_fs": t1 * AU2FS},
+        "accuracy_vs_fp64_path": acc_mfx if head_is_mfx else acc_split,
+        "split_path": {"value": split_value, "unit": "fs/s", "ms_per_step": mix["ms"] / args.steps,
+                       "step_fs_mean": statistics.mean(mix["hdids"]),
+                       "speedup_vs_fp64_path": split_value / fp64_value,
+                       "eom_per_s": mix["eom"] / (mix["ms"] * 1e-3),
+                       "accuracy_vs_fp64_path": acc_split},
         "mfx_path": {"value": mfx_value, "unit": "fs/s", "ms_per_step": mfxr["ms"] / args.steps,
                      "step_fs_mean": statistics.mean(mfxr["hdids"]),
                      "speedup_vs_fp64_path": mfx_value / fp64_value,
-                     "accuracy_vs_fp64_path": {
-                         "dC": abs(cmp["mfx"]["auto"] - cmp["fp64"]["auto"]),
-                         "dpop": float(np.abs(cmp["mfx"]["pop"] - cmp["fp64"]["pop"]).max())},
                      "eom_per_s": mfxr["eom"] / (mfxr["ms"] * 1e-3),
                      "extrapolated_steps": mfx_stats["mlp_steps"], "fallbacks": mfx_stats["fallbacks"],
-                     "rejected": mfx_stats["rejected"], "last_step_end_mismatch": mfx_stats["last_rel"],
+                     "rejected": mfx_stats["rejected"], "last_mismatch": mfx_stats["last_rel"],
                      "training": {"rows": int(len(X)), "epochs": MFX_EPOCHS, "loss": tr_loss,
                                   "seconds": train_s,
-                                  "data": f"the untimed FP64 CMF2 steps from 0 to {PRE_FS} fs"}},
-        "eom_per_s": mix["eom"] / (ms_total * 1e-3), "hb_per_s": mix["hb"] / (ms_total * 1e-3),
+                                  "data": f"the untimed FP64 CMF2 steps from 0 to {PRE_FS} fs"},
+                     "accuracy_vs_fp64_path": acc_mfx},
+        "eom_per_s": head["eom"] / (head["ms"] * 1e-3), "hb_per_s": head["hb"] / (head["ms"] * 1e-3),
         "e2e": {"value": e2e_fs / e2e_s, "unit": "fs/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
-        "gpu_launches": mix["launches"],
-        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
-                     "traffic": by_launch * TRAFFIC_PER_ALG_BYTE if dname == "mode_product" else None,
-                     "traffic_source": "ncu DRAM bytes / algorithmic bytes of the mean-field chain product launches of "
-                                       "this model (profiles/qvc12_cmf2_split32_ncu.md), times the "
-                                       "algorithmic bytes per launch",
+        "gpu_launches": head["launches"],
+        "roofline": {"bound": ROOF_BOUND.get(dname, "hbm"), "kernel": dname, "achieved": achieved_gbs,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
+                     "traffic": (by_launch * TRAFFIC_PER_ALG_BYTE[dname]) if dname in TRAFFIC_PER_ALG_BYTE else None,
+                     "traffic_source": "scaled: DRAM bytes per algorithmic byte of this kernel class from one ncu "
+                                       "capture of the profile case (bench.py --profile-case --profile-from-fs 1), "
+                                       "times this run's algorithmic bytes per launch",
+                     "what_bounds_it": ROOF_NOTE.get(dname, ""),
                      "peak_source": peak_src},
         "compute": ({"kernel": dname, "achieved": achieved_tf, "unit": "TFLOP/s (complex MAC = 8 flop)",
                      "fp64_peak": fp64_peak, "frac_of_fp64_peak": achieved_tf / fp64_peak if fp64_peak > 0 else None,
                      "peak_source": "measured FP64 FMA chain on this GPU"} if args.precision == 0 else
-                    {"kernel": dname, "achieved": achieved_tf, "unit": "TFLOP/s (complex MAC = 8 flop)",
-                     "note": "FP32 mode products: issue-bound in ncu (issue 52-68 %, FMA pipe 27-32 %)"}),
+                    {"kernel": dname, "achieved": achieved_tf, "unit": "TFLOP/s (complex MAC = 8 flop)"}),
         "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                                "share": round(v["ms"] / tot_ms, 4)}
                            for k, v in prof.items() if v["launches"]},
-        "gpu_busy_frac_profiled_pass": tot_ms / mix["prof_ms"] if mix["prof_ms"] else None,
+        "gpu_busy_frac_profiled_pass": tot_ms / head["prof_ms"] if head["prof_ms"] else None,
         "clocks": clocks,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(model, A0, psi0, statistics.mean(mix["hdids"]) / AU2FS)
+        line["cpu_baseline"], line["parity_vs_oracle"] = cpu_baseline(
+            model, A1, psi1, t1, statistics.mean(head["hdids"]) / AU2FS, ref_core)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ref_core.close()
@@ -451,15 +568,27 @@ def run_accuracy(args):
     time (0.5 fs).  Reported: the largest |dC| and |dpop| over the run, their
     values at the end, device seconds and simulated fs/s of each arm."""
     import torch
-    from macaw_gb300.capi import GpuCore
     torch.cuda.init()
-    model = make_model()
+    out = accuracy_arms(make_model(), [int(p) for p in args.acc_precisions.split(",") if p.strip()], args.acc_fs)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def accuracy_arms(model, precisions, acc_fs, mfx_net=None, mfx_precision=1):
+    """The FP64 path and each split arm propagated from t = 0 to acc_fs (free
+    running, CMF2 step control of each arm), compared at every output time.  With
+    `mfx_net` (network, fscale, tscale) one more arm, "mfx": precision
+    `mfx_precision` with the learned extrapolator attached."""
+    import torch
+    from macaw_gb300.capi import GpuCore
     A0, psi0 = initial_wavefunction(model)
-    t_end = args.acc_fs / AU2FS
-    arms = [0] + [int(p) for p in args.acc_precisions.split(",") if p.strip()]
+    t_end = acc_fs / AU2FS
+    arms = [0] + list(precisions) + (["mfx"] if mfx_net is not None else [])
     series, info = {}, {}
     for prec in arms:
-        core = GpuCore(model, precision=prec)
+        core = GpuCore(model, precision=mfx_precision if prec == "mfx" else prec)
+        if prec == "mfx":
+            core.mfx_attach(*mfx_net, tol=model.eps_int)
         core.set_state(A0, psi0, as_start=True)
         t, h = 0.0, model.tout * model.eps_int
         rows = [core.observables(t)]
@@ -473,12 +602,14 @@ def run_accuracy(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
         series[prec] = rows
-        info[prec] = {"wall_s": wall, "fs_per_s": args.acc_fs / wall, "steps": nsteps,
-                      "device_bytes": core.device_bytes()}
+        info[prec] = {"wall_s": wall, "fs_per_s": acc_fs / wall, "steps": nsteps,
+                      "eom": core.counters()["eom"], "device_bytes": core.device_bytes()}
+        if prec == "mfx":
+            info[prec]["extrapolator"] = core.mfx_stats()
         core.close()
     ref = series[0]
     out = {"workload": "accuracy: qvc12 CMF2 (tolerance 1e-5) from t = 0, outputs every "
-                       f"{model.tout * AU2FS:g} fs", "over_fs": args.acc_fs, "fp64": info[0], "arms": {}}
+                       f"{model.tout * AU2FS:g} fs", "over_fs": acc_fs, "fp64": info[0], "arms": {}}
     for prec in arms[1:]:
         rows = series[prec]
         n = min(len(rows), len(ref))
@@ -491,8 +622,7 @@ def run_accuracy(args):
                                       max_dpop=max(dpop), end_dC=dC[n - 1], end_dpop=dpop[n - 1],
                                       max_denergy=max(dE), max_dnorm=max(dN), outputs=n,
                                       speedup_vs_fp64_wall=info[0]["wall_s"] / info[prec]["wall_s"])
-    print(json.dumps(out), flush=True)
-    return 0
+    return out
 
 
 def run_profile_case(args):
@@ -657,11 +787,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--acc-fs", type=float, default=200.0, help="accuracy: propagated interval in fs")
-    ap.add_argument("--acc-precisions", default="1,3", help="accuracy: split arms compared with FP64")
-    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2, 3],
+    ap.add_argument("--acc-precisions", default="1,4", help="accuracy: split arms compared with FP64")
+    ap.add_argument("--headline", default="mfx", choices=["mfx", "split"],
+                    help="qvc12: the arm the line's value is: split precision with (mfx) or without the extrapolator")
+    ap.add_argument("--pre-fs", type=float, default=0.3, help="qvc24: untimed FP64 propagation before the steps")
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2, 3, 4, 5],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
     ap.add_argument("--workload", default="qvc12",
-                    choices=["qvc12", "qvc12n", "ensemble", "lvc5", "gmctdh16", "lvc5mix", "accuracy"],
+                    choices=["qvc12", "qvc12n", "qvc24", "ensemble", "lvc5", "gmctdh16", "lvc5mix", "accuracy"],
                     help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement; "
                          "lvc5 / gmctdh16: RK configurations")
     ap.add_argument("--rk-fs", type=float, default=0.5)
@@ -681,7 +814,7 @@ def main():
         return run_ensemble(args)
     if args.workload == "accuracy":
         return run_accuracy(args)
-    if args.workload == "qvc12n":
+    if args.workload in ("qvc12n", "qvc24"):
         return run_size_scan(args)
     if args.workload in ("lvc5", "gmctdh16", "lvc5mix"):
         return run_rk_workload(args)

@@ -59,7 +59,10 @@ typedef struct mctdh_setup {
   double min_stepsize, writetime;
   double der_factor_re, der_factor_im;  /* -i for propagation, -1 for relaxation */
   int64_t int_type_psi;                 /* 1 = Cash-Karp for the CMF2 SPF sweeps  */
-  int64_t precision;                    /* 0 = FP64, 1 = split-FP32 contractions  */
+  int64_t precision;                    /* 0 FP64; 1 FP32 products, compensated contractions;
+                                           2 compensated products and contractions; 3 FP32 products
+                                           and contractions; 4 as 1 with compensated H_B products of the
+                                           Lanczos steps; 5 as 2 with FP32 H_B products */
   int64_t int_order, int_par1;          /* Adams PECE order and extra EC iterations (abm<order><par1>) */
   /* Operators whose expectation values are written (the 'expect' keyword,
    * input.f90:196-216, terms read by Read_Operators, input.f90:516-748).  Their
@@ -286,18 +289,22 @@ int64_t mctdh_mlp_train(mctdh_mlp_t *mlp, const float *X, const float *T, int64_
 
 /* Mean-field extrapolation inside CMF2 (no reference counterpart).  A snapshot is
  * every density matrix and mean field of the grid modes (E complex entries).
- * record: 1 start, 0 stop and clear, 2 clear and start; during plain CMF2 steps
- * each accepted step stores (t0, h, snapshot at t0, snapshot at t0 + h/2).
- * attach: with a trained network (NULL detaches) the half-step mean fields of
- * cmf2_base.f90:122-130 come from the quartic extrapolation of the last five
- * step-start snapshots plus the network's residual, and a step whose predicted
- * step-end snapshot differs from the recomputed one by more than tol (relative
- * 2-norm) is redone with the plain scheme.  The network maps
- * MCTDH_MFX_NFEAT inputs per entry (Newton increments of orders 1-4 through the
- * last five step starts at the half step and the step end, Re/Im, divided by the
- * RMS of the first-order step-end increment, then four step-length ratios; each
- * column divided by fscale[j]) to MCTDH_MFX_NOUT outputs (Re/Im residual at the
- * half step and the step end, in units of that RMS times tscale[j]). */
+ * record: 1 start, 0 stop and clear, 2 clear and start; every accepted CMF2 step
+ * computed with the plain scheme stores (t0, h, snapshot at t0, snapshot at
+ * t0 + h/2).  attach: with a trained network (NULL detaches) and the half-step
+ * snapshots of the last five accepted steps in the context's history, the mean
+ * fields at a step start (the evaluation of cmf2_base.f90:78-87) come from the
+ * quartic extrapolation of that history plus the network's residual, and only
+ * h1mode is computed there; the half-step mean fields (:122-130) are computed as
+ * always, and a step whose computed half-step snapshot differs from the
+ * extrapolation's prediction for it by more than tol (relative 2-norm) is redone
+ * with the plain scheme.  Grid-mode models only (Gaussian-mode models keep the
+ * plain scheme).  The network maps MCTDH_MFX_NFEAT inputs per entry (Newton
+ * increments of orders 1-4 through the five half-step snapshots at the step
+ * start and at its half step, Re/Im, divided by the RMS of the first-order
+ * increment at the half step, then four spacing ratios; each column divided by
+ * fscale[j]) to MCTDH_MFX_NOUT outputs (Re/Im residual at the step start and at
+ * the half step, in units of that RMS times tscale[j]). */
 #define MCTDH_MFX_NFEAT 20
 #define MCTDH_MFX_NOUT 4
 int64_t mctdh_mfx_size(mctdh_ctx_t *ctx, int64_t *E);
@@ -307,16 +314,18 @@ int64_t mctdh_mfx_fetch(mctdh_ctx_t *ctx, int64_t maxrec, double *t0, double *h,
 int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, const double *fscale, const double *tscale,
                          double tol);
 /* predict: run the attached extrapolator on a given history (5 x E complex
- * snapshots, oldest first, at times ts[5]) for a step of length h; writes the
- * half-step and step-end snapshots (E complex each) and clears the history. */
-int64_t mctdh_mfx_predict(mctdh_ctx_t *ctx, const double *hist, const double *ts, double h, double *half,
-                          double *full);
+ * snapshots, oldest first, at times ts[5]) for the times tau0 (a step start) and
+ * tau1 (its half step); writes the two predicted snapshots (E complex each) and
+ * clears the history. */
+int64_t mctdh_mfx_predict(mctdh_ctx_t *ctx, const double *hist, const double *ts, double tau0, double tau1,
+                          double *out0, double *out1);
 /* log: one row per CMF2 attempt of a context with extrapolation state
- * (t, h, error estimate / eps_int, extrapolated 0/1, step-end mismatch or -1). */
+ * (t, h, error estimate / eps_int, predicted step start 0/1, half-step mismatch or -1). */
 int64_t mctdh_mfx_log(mctdh_ctx_t *ctx, int64_t maxrows, double *rows, int64_t *n);
-/* stats: steps taken with extrapolated mean fields, steps redone because the
- * step-end check failed, steps redone because the CMF2 error estimate rejected
- * the extrapolated attempt, and the last step-end mismatch (-1 before any). */
+/* stats: steps taken with predicted step-start mean fields, steps redone because
+ * the half-step check failed, attempts with predicted mean fields rejected by the
+ * CMF2 error estimate (the retry computes them), and the last half-step mismatch
+ * (-1 before any). */
 int64_t mctdh_mfx_stats(mctdh_ctx_t *ctx, int64_t *mlp_steps, int64_t *fallbacks, int64_t *rejected,
                         double *last_rel);
 

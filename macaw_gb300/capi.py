@@ -114,7 +114,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_mfx_fetch.argtypes = [vp, C.c_int64, DP, DP, DP, DP, I64P]
     lib.mctdh_mfx_attach.argtypes = [vp, vp, DP, DP, C.c_double]
     lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P, I64P, DP]
-    lib.mctdh_mfx_predict.argtypes = [vp, DP, DP, C.c_double, DP, DP]
+    lib.mctdh_mfx_predict.argtypes = [vp, DP, DP, C.c_double, C.c_double, DP, DP]
     lib.mctdh_mfx_log.argtypes = [vp, C.c_int64, DP, I64P]
     lib.mctdh_ens_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
     lib.mctdh_ens_destroy.argtypes = [vp]
@@ -564,16 +564,17 @@ class GpuCore:
             self._check(self.lib.mctdh_mfx_attach(self.h, mlp.h, fs.ctypes.data_as(DP), ts.ctypes.data_as(DP), tol))
         self._mlp_ref = mlp
 
-    def mfx_predict(self, hist, ts, h):
-        """The attached extrapolator on a given history (5, E) at times ts: (half, full)."""
+    def mfx_predict(self, hist, ts, tau0, tau1):
+        """The attached extrapolator on a given history (5, E) at times ts: the
+        predicted snapshots at tau0 (a step start) and tau1 (its half step)."""
         Hs = np.ascontiguousarray(hist, dtype=np.complex128)
         T = np.ascontiguousarray(ts, dtype=np.float64)
         E = Hs.shape[1]
-        half = np.zeros(E, dtype=np.complex128)
-        full = np.zeros(E, dtype=np.complex128)
-        self._check(self.lib.mctdh_mfx_predict(self.h, Hs.ctypes.data_as(DP), T.ctypes.data_as(DP), h,
-                                               half.ctypes.data_as(DP), full.ctypes.data_as(DP)))
-        return half, full
+        p0 = np.zeros(E, dtype=np.complex128)
+        p1 = np.zeros(E, dtype=np.complex128)
+        self._check(self.lib.mctdh_mfx_predict(self.h, Hs.ctypes.data_as(DP), T.ctypes.data_as(DP), tau0, tau1,
+                                               p0.ctypes.data_as(DP), p1.ctypes.data_as(DP)))
+        return p0, p1
 
     def mfx_log(self):
         """One row per CMF2 attempt: t, h, error / eps_int, extrapolated, step-end mismatch."""

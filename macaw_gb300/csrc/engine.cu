@@ -348,6 +348,7 @@ struct Ctx {
   int int_type_psi = 1;
   int precision = 0;
   int hole_prec = 0;   // single-hole contractions: 0 FP64, 1 FP32 sums, 2 compensated FP32
+  int hb_prec = 0;     // H_B * B products of the Lanczos steps: 0 FP64, 1 FP32, 2 compensated FP32
   bool reginv_cold = false;   // regularised inverses without the Jacobi warm start
   std::string last_error;
   long long launches = 0;
@@ -667,10 +668,14 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.int_par1 = (int)s->int_par1;
   c.reginv_cold = s->reginv_cold != 0;
   c.precision = (int)s->precision;
-  if (c.precision < 0 || c.precision > 3) throw StatusError(MCTDH_EARG, "precision must be 0, 1, 2 or 3");
-  // precision 3: the products of precision 1 with FP32-accumulated contractions
+  if (c.precision < 0 || c.precision > 5) throw StatusError(MCTDH_EARG, "precision must be 0 .. 5");
+  // precision 3: the products of precision 1 with FP32-accumulated contractions;
+  // 4: FP32 mean-field and A-derivative products, compensated H_B products;
+  // 5: compensated mean-field and A-derivative products, FP32 H_B products
   c.hole_prec = c.precision == 3 ? 1 : (c.precision ? 2 : 0);
-  if (c.precision == 3) c.precision = 1;
+  c.hb_prec = c.precision == 4 ? 2 : (c.precision == 5 ? 1 : (c.precision == 3 ? 1 : c.precision));
+  if (c.precision == 3 || c.precision == 4) c.precision = 1;
+  if (c.precision == 5) c.precision = 2;
   if (!c.modes_gwp.empty()) {
     // Gaussian widths GWPa(maxdof, ns00max, nmodgwp) (psidef: GWPa, init_calc.f90:1020-1068)
     c.gwp_lda = c.maxdof;
@@ -1564,11 +1569,11 @@ void plan_hb(Ctx& c) {
     }
   }
   std::vector<std::vector<SumSrc>> srcs(c.nstates);
-  // FP32 products (precision 1) keep complex FP32 intermediates; compensated ones the split pairs
-  const int chain_fmt = c.precision == 1 ? TF_F32 : (c.precision ? TF_SPLIT : TF_C64);
-  // precision 1 reads the Krylov vector once converted to complex FP32 (8-byte
+  // FP32 products keep complex FP32 intermediates; compensated ones the split pairs
+  const int chain_fmt = c.hb_prec == 1 ? TF_F32 : (c.hb_prec ? TF_SPLIT : TF_C64);
+  // FP32 products read the Krylov vector once converted to complex FP32 (8-byte
   // elements: state offsets count float2)
-  const int hb_in_fmt = c.precision == 1 ? TF_F32 : TF_C64;
+  const int hb_in_fmt = c.hb_prec == 1 ? TF_F32 : TF_C64;
   auto hb_in_at = [&](int s) -> cplx* {
     if (hb_in_fmt == TF_F32) return reinterpret_cast<cplx*>(reinterpret_cast<float2*>(c.d_hbin32) + c.aoff[s]);
     return c.d_hbin + c.aoff[s];
@@ -1647,7 +1652,7 @@ void plan_hb(Ctx& c) {
   for (int s = 0; s < c.nstates; ++s)
     if (c.c0[s].x != 0.0 || c.c0[s].y != 0.0) srcs[s].push_back(SumSrc{c.d_hbin + c.aoff[s], c.c0[s]});
   for (auto& b : c.hb_chains) {
-    b.prec = c.precision;   // H_B * B feeds the Lanczos recurrence, which stays FP64
+    b.prec = c.hb_prec;   // H_B * B feeds the Lanczos recurrence, which stays FP64
     b.finalize(c.ar);
   }
   std::vector<SumRange> ranges;
@@ -2531,7 +2536,7 @@ void hb(Ctx& c, const cplx* B, cplx* out, bool with_dot = false, bool input_read
     }
   }
   for (size_t i = 1; i < c.hb_chains.size(); ++i) run_prod(c, c.hb_chains[i]);
-  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st, c.precision,
+  launch_termsum(out, c.hbsum_d, c.nstates, c.hbsrc_d, c.naconftot, c.st, c.hb_prec,
                  with_dot ? c.hb_dot : FusedDot{nullptr, nullptr, nullptr, nullptr});
   c.count();
   c.hb_count++;
@@ -3151,13 +3156,17 @@ CmfState& cmf_state(Ctx& c) {
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
 // ---------------------------------------------------------------------------
 // Learned mean-field extrapolation inside CMF2.  A snapshot is every density
-// matrix and mean field of the grid modes (the inputs of Calc_rhom1MF and of the
-// SPF error norm).  With a trained network attached and three accepted step
-// starts in the history, the mean fields at the half step (cmf2_base.f90:122-130)
-// come from the network instead of an EOM evaluation, and the network's
-// prediction for the step end is checked against the mean fields recomputed
-// there: if they differ by more than the tolerance the step is redone with the
-// plain scheme.  The end-of-step evaluation is the next step's first one.
+// matrix and mean field of the grid modes (the inputs of Calc_rhom1MF).  The
+// history holds the snapshots computed at the half steps of the last accepted
+// CMF2 steps.  With a trained network attached and a full history, the mean
+// fields at a step start (the first evaluation of cmf2_base.f90:78-87) come from
+// the quartic extrapolation of that history plus the network's residual instead
+// of an EOM evaluation (h1mode is still computed: the A-vector propagation uses
+// only h1mode, the mean fields only drive the first SPF half step).  The half-step
+// mean fields (:122-130) are always computed; the extrapolation's prediction for
+// the half step is checked against them, and a step whose mismatch exceeds the
+// tolerance is redone with the plain scheme.  One mean-field evaluation per
+// step instead of two.
 // ---------------------------------------------------------------------------
 struct MfxState {
   long long E = 0;
@@ -3167,7 +3176,10 @@ struct MfxState {
   double thist[MFX_NHIST] = {};
   int nhist = 0, head = 0;         // head: index of the newest entry
   double* S = nullptr;             // device: feature scale of the current prediction
-  cplx *half = nullptr, *pred_half = nullptr, *pred_full = nullptr, *now = nullptr, *backup = nullptr;
+  // half: the half-step snapshot of the current attempt; start: the step-start
+  // snapshot (recorded steps); pred0 / pred1: the predictions at the step start
+  // and at the half step
+  cplx *half = nullptr, *start = nullptr, *pred0 = nullptr, *pred1 = nullptr, *now = nullptr, *backup = nullptr;
   mctdh_mlp* mlp = nullptr;
   double fscale[MFX_NFEAT] = {}, tscale[MFX_NOUT] = {}, tol = 0.0;
   bool recording = false;
@@ -3176,7 +3188,7 @@ struct MfxState {
   long long mlp_steps = 0, fallbacks = 0, rejected = 0;
   double last_rel = -1.0;          // relative step-end mismatch of the last validated prediction
   std::vector<double> log;         // per CMF2 attempt: t, h, error, extrapolated (0/1), step-end mismatch
-  HoleBatch dh;                     // ||now - pred_full||^2 and ||now||^2
+  HoleBatch dh;                     // ||now - pred1||^2 and ||now||^2
   RedBatch dr;
   cplx* dres = nullptr;
   cplx* diff = nullptr;
@@ -3208,8 +3220,9 @@ MfxState& mfx_state(Ctx& c) {
   M->segs_d = upload_vec(c.ar, M->segs_h);
   for (auto& h : M->hist) h = c.ar.calloc_c(off);
   M->half = c.ar.calloc_c(off);
-  M->pred_half = c.ar.calloc_c(off);
-  M->pred_full = c.ar.calloc_c(off);
+  M->start = c.ar.calloc_c(off);
+  M->pred0 = c.ar.calloc_c(off);
+  M->pred1 = c.ar.calloc_c(off);
   M->now = c.ar.calloc_c(off);
   M->diff = c.ar.calloc_c(off);
   M->backup = c.ar.calloc_c(c.ntot);
@@ -3229,11 +3242,11 @@ void snap_gather(Ctx& c, MfxState& M, cplx* flat) {
   c.count();
 }
 
-// relative distance of the recomputed snapshot (M.now) from the predicted one
+// relative distance of the computed half-step snapshot (M.now) from its prediction
 double snap_rel_diff(Ctx& c, MfxState& M) {
   StageArgs a;
   memset(&a, 0, sizeof(a));
-  a.k[0] = M.pred_full;
+  a.k[0] = M.pred1;
   a.c[0] = -1.0;
   a.nk = 1;
   launch_stage(M.diff, M.now, a, 1.0, M.E, c.st);
@@ -3258,11 +3271,11 @@ static void lagrange_tail(const double* ts, int n, int first, double tau, double
   }
 }
 
-// Predict the half-step and step-end snapshots from the history for step length h:
-// quartic extrapolation through the last five step starts plus the network's
-// residual, whose inputs are the Newton increments of orders 1-4
-// (mfx_features_kernel).
-void mfx_predict(Ctx& c, MfxState& M, double h) {
+// Predict the snapshots at the times tau0 (a step start) and tau1 (its half step)
+// from the history: quartic extrapolation through the last five half-step
+// snapshots plus the network's residual, whose inputs are the Newton increments
+// of orders 1-4 (mfx_features_kernel).  Results in M.pred0 and M.pred1.
+void mfx_predict(Ctx& c, MfxState& M, double tau0, double tau1) {
   const int NH = MFX_NHIST;
   MfxHist hz;
   double ts[MFX_NHIST];
@@ -3273,7 +3286,7 @@ void mfx_predict(Ctx& c, MfxState& M, double h) {
   }
   MfxCoef cf;
   memset(&cf, 0, sizeof(cf));
-  const double taus[2] = {ts[NH - 1] + 0.5 * h, ts[NH - 1] + h};
+  const double taus[2] = {tau0, tau1};
   for (int tau = 0; tau < 2; ++tau) {
     double prev[MFX_NHIST] = {};
     prev[NH - 1] = 1.0;   // P_0 = newest value
@@ -3287,20 +3300,28 @@ void mfx_predict(Ctx& c, MfxState& M, double h) {
   }
   const double dlast = ts[NH - 1] - ts[NH - 2];
   for (int j = 0; j < NH - 2; ++j) cf.ratio[j] = (ts[j + 1] - ts[j]) / dlast;
-  cf.ratio[NH - 2] = h / dlast;
+  cf.ratio[NH - 2] = (tau1 - ts[NH - 1]) / dlast;
   memcpy(cf.fscale, M.fscale, sizeof(cf.fscale));
   memcpy(cf.tscale, M.tscale, sizeof(cf.tscale));
   float* X = mlp_input_buffer(M.mlp, M.E);
   launch_mfx_features(hz, cf, M.S, X, M.E, c.st);
   const float* Y = mlp_forward_on(M.mlp, M.E, c.st);
-  launch_mfx_combine(hz, cf, Y, M.S, M.pred_half, M.pred_full, M.E, c.st);
+  launch_mfx_combine(hz, cf, Y, M.S, M.pred0, M.pred1, M.E, c.st);
   c.count(7);
+}
+
+// Push the half-step snapshot M.half at time th into the history ring.
+void mfx_push_half(Ctx& c, MfxState& M, double th) {
+  M.head = (M.head + 1) % MFX_NHIST;
+  copy_dev(c, M.hist[M.head], M.half, M.E);
+  M.thist[M.head] = th;
+  M.nhist = std::min(M.nhist + 1, MFX_NHIST);
 }
 
 // One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
 // ops_fresh: the operators and mean fields at d_y are already in place.
-double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh, bool reginv_done) {
+double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_done) {
   if (c.mixture)
     throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 covers a single wave packet without dissipation (use rk45, dopri, abm or bs)");
   CmfState& S = cmf_state(c);
@@ -3386,16 +3407,8 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool use_mlp, bool ops_fresh,
   MfxState* M = nullptr;
   auto it = g_mfx.find(&c);
   if (it != g_mfx.end()) M = it->second;
-  if (use_mlp) {
-    // mean fields at the half step from the network (replaces :122-130)
-    mfx_predict(c, *M, hdid);
-    launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred_half, M->E, 1, c.st);
-    launch_reginv(c.reg_d, (int)c.reg_h.size(), c.mfop_d, c.d_status, c.st);
-    c.count(2);
-  } else {
-    operators_and_mf(c, S.AHalf);                   // :122-130
-    if (M && M->recording) snap_gather(c, *M, M->half);
-  }
+  operators_and_mf(c, S.AHalf);                     // :122-130
+  if (M) snap_gather(c, *M, M->half);               // the extrapolator's history
   copy_dev(c, S.psiHalf2, c.d_y, c.ntot);
   if (S.gwp) copy_dev(c, S.DDHalf2, S.DD0, S.nD);
   propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf2, S.DDHalf2);  // :132-141
@@ -3452,82 +3465,81 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
   MfxState* M = nullptr;
   auto it = g_mfx.find(&c);
   if (it != g_mfx.end()) M = it->second;
-  // the operators at the step start: recomputed unless the last step's validation left them
-  bool fresh = c.ops_fresh_t == t && c.ops_fresh;
-  // (the extrapolator's validation leaves the full operators, rho^-1 MF included)
   const bool overlap = c.st2 != nullptr;
-  if (!fresh) operators_and_mf(c, c.d_y, !overlap);
-  const bool reginv_first = fresh || !overlap;
-  c.ops_fresh = false;
-  if (M) {
-    // push the step-start snapshot into the history (once per accepted step start)
-    if (M->nhist == 0 || M->thist[M->head] != t) {
-      M->head = (M->head + 1) % MFX_NHIST;
-      snap_gather(c, *M, M->hist[M->head]);
-      M->thist[M->head] = t;
-      M->nhist = std::min(M->nhist + 1, MFX_NHIST);
-    }
-  }
-  bool use_mlp = M && M->mlp && M->nhist == MFX_NHIST;
-  if (use_mlp) copy_dev(c, M->backup, c.d_y, c.ntot);
+  // Step start: the operators and mean fields of d_y (cmf2_base.f90:78-87), or,
+  // with an attached extrapolator and a full half-step history, h1mode computed
+  // and rho / mean fields predicted (grid-mode models only).
+  bool predicted = M && M->mlp && M->nhist == MFX_NHIST && c.modes_gwp.empty();
   double hdid = htry;
-  bool first = true;
-  int mlp_rejects = 0;
-  while (true) {
-    ++*tries;
-    if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
-    double error = cmf2_attempt(c, t, hdid, use_mlp, first, first && reginv_first);
-    first = false;
-    if (M && M->log.size() < 5 * 100000) {
-      const double row[5] = {t, hdid, error, use_mlp ? 1.0 : 0.0, -1.0};
-      M->log.insert(M->log.end(), row, row + 5);
+  for (;;) {
+    if (predicted) {
+      copy_dev(c, M->backup, c.d_y, c.ntot);
+      mfx_predict(c, *M, t, t + 0.5 * hdid);
+      launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred0, M->E, 1, c.st);
+      c.count();
+      h1_only(c, c.d_y);
+    } else {
+      operators_and_mf(c, c.d_y, !overlap);
+      if (M && M->recording) snap_gather(c, *M, M->start);
     }
-    if (error > 1.0 && use_mlp) {
-      // rejected by the CMF2 error estimate like any attempt: shrink and retry
-      // with new extrapolated mean fields; after three rejections in a row the
-      // plain scheme takes over
-      ++M->rejected;
-      if (++mlp_rejects >= 3) use_mlp = false;
-      hdid = hdid / sqrt(error) * 0.95;
-      continue;
+    // reginv of the step start: done by operators_and_mf without a second stream;
+    // otherwise inside the attempt, beside the Lanczos build
+    const bool reginv_first = !predicted && !overlap;
+    bool first = true;
+    bool accepted_predicted = false;
+    while (true) {
+      ++*tries;
+      if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
+      const double error = cmf2_attempt(c, t, hdid, first, first && reginv_first);
+      const bool was_predicted = predicted && first;
+      first = false;
+      if (M && M->log.size() < 5 * 100000) {
+        const double row[5] = {t, hdid, error, was_predicted ? 1.0 : 0.0, -1.0};
+        M->log.insert(M->log.end(), row, row + 5);
+      }
+      if (error > 1.0) {
+        // rejected like any attempt; the retry recomputes the step-start mean fields
+        if (was_predicted) ++M->rejected;
+        hdid = hdid / sqrt(error) * 0.95;
+        continue;
+      }
+      cmf2_accept(c, hdid);
+      accepted_predicted = was_predicted;
+      double hn = (error > 0.0) ? std::min(hdid / sqrt(error), hdid * 1.5) : hdid * 1.5;
+      hn = std::min(hn, c.writetime);
+      *hdid_out = hdid;
+      *hnext_out = hn;
+      break;
     }
-    if (error > 1.0) {
-      hdid = hdid / sqrt(error) * 0.95;
-      continue;
-    }
-    cmf2_accept(c, hdid);
-    if (use_mlp) {
-      // validation against the mean fields recomputed at the step end
-      operators_and_mf(c, c.d_y);
-      snap_gather(c, *M, M->now);
+    if (accepted_predicted) {
+      // the computed half-step mean fields against the extrapolation's prediction
+      copy_dev(c, M->now, M->half, M->E);
       const double rel = snap_rel_diff(c, *M);
       M->last_rel = rel;
       if (!M->log.empty()) M->log.back() = rel;
       if (!(rel <= M->tol)) {
+        // redo the step with the plain scheme
         ++M->fallbacks;
         copy_dev(c, c.d_y, M->backup, c.ntot);
-        use_mlp = false;
-        first = false;
+        predicted = false;
+        hdid = htry;
         continue;
       }
       ++M->mlp_steps;
-      c.ops_fresh = true;
-      c.ops_fresh_t = t + hdid;
     }
-    if (M && M->recording && !use_mlp) {
-      std::vector<cplx> s0(M->E), sh(M->E);
-      CK(cudaMemcpyAsync(s0.data(), M->hist[M->head], sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
-      CK(cudaMemcpyAsync(sh.data(), M->half, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
-      CK(cudaStreamSynchronize(c.st));
-      M->rec_t0.push_back(t);
-      M->rec_h.push_back(hdid);
-      M->rec_s0.insert(M->rec_s0.end(), s0.begin(), s0.end());
-      M->rec_sh.insert(M->rec_sh.end(), sh.begin(), sh.end());
+    if (M) {
+      if (M->recording && !accepted_predicted) {
+        std::vector<cplx> s0(M->E), sh(M->E);
+        CK(cudaMemcpyAsync(s0.data(), M->start, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(sh.data(), M->half, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
+        CK(cudaStreamSynchronize(c.st));
+        M->rec_t0.push_back(t);
+        M->rec_h.push_back(*hdid_out);
+        M->rec_s0.insert(M->rec_s0.end(), s0.begin(), s0.end());
+        M->rec_sh.insert(M->rec_sh.end(), sh.begin(), sh.end());
+      }
+      mfx_push_half(c, *M, t + 0.5 * *hdid_out);
     }
-    double hn = (error > 0.0) ? std::min(hdid / sqrt(error), hdid * 1.5) : hdid * 1.5;
-    hn = std::min(hn, c.writetime);
-    *hdid_out = hdid;
-    *hnext_out = hn;
     return;
   }
 }
@@ -3592,7 +3604,7 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       // CMF2 / Lanczos buffers (ensemble members, mixtures and dissipation integrate
       // with the derivative-based integrators only)
       c->d_hbin = c->ar.calloc_c(c->naconftot);
-      if (c->precision == 1) c->d_hbin32 = c->ar.calloc_c((c->naconftot + 1) / 2);
+      if (c->hb_prec == 1) c->d_hbin32 = c->ar.calloc_c((c->naconftot + 1) / 2);
       {
         // block sums of the fused Lanczos dots (one per block of the 256-thread launches)
         const long long nb = (c->naconftot + 255) / 256;
@@ -4485,7 +4497,7 @@ int64_t mctdh_cmf2_attempt(mctdh_ctx_t* ctx, double* A, double* psi, double t, d
   return guarded(c, [&] {
     upload(*c, c->d_y, A, psi);
     c->ops_fresh = false;
-    *error = cmf2_attempt(*c, t, h, false, false, false);
+    *error = cmf2_attempt(*c, t, h, false, false);
     cmf2_accept(*c, h);
     download(*c, c->d_y, A, psi);
   });
@@ -4651,9 +4663,9 @@ int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, const double* fscale,
   });
 }
 
-int64_t mctdh_mfx_predict(mctdh_ctx_t* ctx, const double* hist, const double* ts, double h, double* half,
-                          double* full) {
-  if (!ctx || !hist || !ts || !half || !full) return MCTDH_EARG;
+int64_t mctdh_mfx_predict(mctdh_ctx_t* ctx, const double* hist, const double* ts, double tau0, double tau1,
+                          double* out0, double* out1) {
+  if (!ctx || !hist || !ts || !out0 || !out1) return MCTDH_EARG;
   Ctx* c = ctx->c;
   return guarded(c, [&] {
     MfxState& M = mfx_state(*c);
@@ -4664,9 +4676,9 @@ int64_t mctdh_mfx_predict(mctdh_ctx_t* ctx, const double* hist, const double* ts
     }
     M.head = MFX_NHIST - 1;
     M.nhist = MFX_NHIST;
-    mfx_predict(*c, M, h);
-    CK(cudaMemcpyAsync(half, M.pred_half, sizeof(cplx) * M.E, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(full, M.pred_full, sizeof(cplx) * M.E, cudaMemcpyDeviceToHost, c->st));
+    mfx_predict(*c, M, tau0, tau1);
+    CK(cudaMemcpyAsync(out0, M.pred0, sizeof(cplx) * M.E, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(out1, M.pred1, sizeof(cplx) * M.E, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     M.nhist = 0;
   });

@@ -13,7 +13,7 @@ Workloads (sizes as named by their builders):
   qvc12     3-state QVC, 12 DOFs paired into 6 modes of 20x20 grids, 8 SPFs, CMF2
   ensemble  ragged LVC instances (2-4 states, 4-10 modes, 4-10 SPFs, 16-48 points)
   gmctdh16  2-state LVC: 4 HO DVR modes + one 12-DOF Gaussian mode (32 GWPs)
-  qvc24     4-state QVC, 24 DOFs paired into 8 modes of 12x12 grids, 8 SPFs, CMF2
+  qvc24     4-state QVC, 24 DOFs in 8 three-DOF modes of 12^3 grids, 8 SPFs, CMF2
 """
 from __future__ import annotations
 
@@ -79,8 +79,9 @@ def qvc(nstates: int, ndof: int, grid: int, nspf: int, ncoup: int, seed: int,
         wrange: Tuple[float, float], lam_range: Tuple[float, float], energies_ev: Sequence[float],
         label: str, integrator: int = INT_CMF2, eps_int: float = 1e-5,
         eps_lanczos: float = 1e-8, eps_spf: float = 1e-8, tfinal_fs: float = 200.0,
-        init_state: Optional[int] = None, tout_fs: float = 0.5) -> Model:
-    """QVC model with pairs of DOFs combined into logical modes of grid x grid points."""
+        init_state: Optional[int] = None, tout_fs: float = 0.5, dofs_per_mode: int = 2) -> Model:
+    """QVC model with `dofs_per_mode` DOFs combined into each logical mode
+    (grid^dofs_per_mode points)."""
     rng = np.random.default_rng(seed)
     omegas = rng.uniform(wrange[0], wrange[1], ndof) / AU2CMM1
     kappa = rng.normal(0.0, 0.1, (nstates, ndof)) / AU2EV
@@ -93,8 +94,9 @@ def qvc(nstates: int, ndof: int, grid: int, nspf: int, ncoup: int, seed: int,
         lambdas.append((a, b, int(k), float(rng.uniform(*lam_range)) / AU2EV))
     terms = _vibronic_terms(nstates, omegas, kappa, gamma, lambdas,
                             [e / AU2EV for e in energies_ev])
-    nmodes = ndof // 2
-    model = Model(nstates=nstates, mode_dofs=[[2 * m, 2 * m + 1] for m in range(nmodes)],
+    k = dofs_per_mode
+    nmodes = ndof // k
+    model = Model(nstates=nstates, mode_dofs=[[k * m + i for i in range(k)] for m in range(nmodes)],
                   multiset=[True] * nmodes, nspf=np.full((nmodes, nstates), nspf),
                   dvr_type=["HO"] * ndof, ngp=[grid] * ndof, dvrpar=[(0.0, 1.0)] * ndof,
                   terms=terms, tfinal=tfinal_fs / AU2FS, tout=tout_fs / AU2FS, eps_int=eps_int,
@@ -110,10 +112,12 @@ def qvc12(seed: int = SEED0 + 1, grid: int = 20, nspf: int = 8, **kw) -> Model:
                "qvc12", **kw)
 
 
-def qvc24(seed: int = SEED0 + 4, grid: int = 12, nspf: int = 8, **kw) -> Model:
-    """4-state QVC, 24 DOFs -> 8 modes of 12x12 HO grids, 8 SPFs (about 1 GB of A)."""
+def qvc24(seed: int = SEED0 + 4, grid: int = 12, nspf: int = 8, dofs_per_mode: int = 3, **kw) -> Model:
+    """4-state QVC over 24 DOFs combined into 8 logical modes of three DOFs (12^3-point
+    HO product grids), 8 SPFs per mode and state: 8^8 = 16,777,216 configurations per
+    state, 1.07 GB of FP64 coefficients for the four states."""
     return qvc(4, 24, grid, nspf, 8, seed, (150.0, 3500.0), (0.02, 0.2), (0.0, 0.3, 0.7, 1.0),
-               "qvc24", tfinal_fs=300.0, **kw)
+               "qvc24", tfinal_fs=300.0, dofs_per_mode=dofs_per_mode, **kw)
 
 
 def ensemble_member(rng: np.random.Generator, idx: int, max_conf: int = 1 << 20) -> Model:

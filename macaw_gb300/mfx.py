@@ -3,21 +3,21 @@
 A snapshot is every density matrix and mean field of the grid modes at one
 time (``GpuCore.mfx_size()`` complex entries).  Plain CMF2 steps recorded with
 ``GpuCore.mfx_record`` give, per accepted step k, the snapshot at the step
-start t_k and at its half step t_k + h_k/2; the snapshot at the step end is
-the next step's start.
+start t_k and at its half step t_k + h_k/2.
 
-For a step of length h after the step starts t_0 < ... < t_4 (values z_0..z_4
-of every entry), P_o(tau) is the Lagrange polynomial through the last o+1
-values and inc_o = P_o - P_{o-1} (P_0 = z_4) its Newton increment.  The
-extrapolation without the network is P_4 (quartic through the five step
-starts).  The network sees, per entry, Re/Im of inc_1..inc_4 at the half
-step and at the step end divided by S (the RMS over all entries of |inc_1| at
-the step end), and the step-length ratios (t1-t0, t2-t1, t3-t2, h) / (t4-t3);
-every input column is divided by its scale ``fscale``.  It predicts the residual
-z(tau) - P_4(tau) at the half step and the step end in units of S times the
-output column scale ``tscale``.  The device builds the same inputs
-(mfx_features_kernel) when the trained network replaces the half-step mean
-fields inside CMF2 (cmf2_base.f90:122-130).
+The extrapolator replaces the step-start mean-field evaluation of CMF2
+(cmf2_base.f90:78-87): from the half-step snapshots z_0..z_4 of the last five
+steps (times s_j = t_j + h_j/2) it predicts the snapshot at the next step start
+tau_0 = t_k and, for the check against the computed half-step fields, at its
+half step tau_1 = t_k + h_k/2.  P_o(tau) is the Lagrange polynomial through the
+last o+1 history values and inc_o = P_o - P_{o-1} (P_0 = z_4) its Newton
+increment; the extrapolation without the network is P_4 (quartic).  The network
+sees, per entry, Re/Im of inc_1..inc_4 at tau_0 and tau_1 divided by S (the RMS
+over all entries of |inc_1| at tau_1), and the spacing ratios (s_1-s_0, s_2-s_1,
+s_3-s_2, tau_1-s_4) / (s_4-s_3); every input column is divided by its scale
+``fscale``.  It predicts the residual z(tau) - P_4(tau) at tau_0 and tau_1 in
+units of S times the output column scale ``tscale``.  The device builds the same
+inputs (mfx_features_kernel).
 """
 from __future__ import annotations
 
@@ -45,12 +45,13 @@ def lagrange_tail(ts, first, tau):
     return w
 
 
-def coefficients(ts, h):
-    """Increment weights inc[tau][o-1][j], quartic weights base[tau][j] and the ratios."""
+def coefficients(ts, taus):
+    """Increment weights inc[tau][o-1][j], quartic weights base[tau][j] and the
+    ratios for the history times ts and the two prediction times taus."""
     n = len(ts)
     inc = np.zeros((2, n - 1, n))
     base = np.zeros((2, n))
-    for it, tau in enumerate((ts[-1] + 0.5 * h, ts[-1] + h)):
+    for it, tau in enumerate(taus):
         prev = np.zeros(n)
         prev[-1] = 1.0
         for o in range(1, n):
@@ -59,14 +60,14 @@ def coefficients(ts, h):
             prev = w
         base[it] = prev
     d = ts[-1] - ts[-2]
-    ratio = np.array([(ts[j + 1] - ts[j]) / d for j in range(n - 2)] + [h / d])
+    ratio = np.array([(ts[j + 1] - ts[j]) / d for j in range(n - 2)] + [(taus[1] - ts[-1]) / d])
     return inc, base, ratio
 
 
-def features(Z, ts, h):
+def features(Z, ts, taus):
     """Unscaled inputs (E, 20), the quartic extrapolations (2, E) and S for the
-    history Z (5, E) at times ts."""
-    inc, base, ratio = coefficients(ts, h)
+    history Z (5, E) at times ts and the prediction times taus."""
+    inc, base, ratio = coefficients(ts, taus)
     incs = np.einsum("toj,je->toe", inc, Z)          # (2, 4, E)
     S = max(float(np.sqrt(np.mean(np.abs(incs[1, 0]) ** 2))), 1e-300)
     E = Z.shape[1]
@@ -83,21 +84,24 @@ def features(Z, ts, h):
 
 
 def build_dataset(t0, h, s0, sh) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
-    """Samples of consecutive recorded steps: unscaled inputs X, residual targets R
-    of the quartic extrapolation (Re/Im at the half step, Re/Im at the step end,
-    in units of S) and the step index of every row."""
+    """Samples of consecutive recorded steps: for step k, the history is the
+    half-step snapshots of steps k-5 .. k-1, the targets the snapshot at the step
+    start t_k and at its half step.  Returns the unscaled inputs X, the residual
+    targets R of the quartic extrapolation (Re/Im at the step start, Re/Im at the
+    half step, in units of S) and the step index of every row."""
     Xs, Rs, ks = [], [], []
-    for k in range(NHIST - 1, len(t0) - 1):
+    for k in range(NHIST, len(t0)):
         ok = all(np.isclose(t0[j + 1], t0[j] + h[j], rtol=0, atol=1e-9 * max(1.0, abs(t0[j])))
-                 for j in range(k - NHIST + 1, k + 1))
+                 for j in range(k - NHIST, k))
         if not ok:
             continue
-        ts = t0[k - NHIST + 1:k + 1]
-        X, Q, S = features(s0[k - NHIST + 1:k + 1], ts, h[k])
-        rh = (sh[k] - Q[0]) / S
-        rf = (s0[k + 1] - Q[1]) / S
+        ts = t0[k - NHIST:k] + 0.5 * h[k - NHIST:k]
+        taus = (t0[k], t0[k] + 0.5 * h[k])
+        X, Q, S = features(sh[k - NHIST:k], ts, taus)
+        r0 = (s0[k] - Q[0]) / S
+        r1 = (sh[k] - Q[1]) / S
         Xs.append(X)
-        Rs.append(np.stack([rh.real, rh.imag, rf.real, rf.imag], axis=1))
+        Rs.append(np.stack([r0.real, r0.imag, r1.real, r1.imag], axis=1))
         ks.append(np.full(len(X), k))
     if not Xs:
         raise ValueError("not enough consecutive recorded steps")
@@ -147,8 +151,9 @@ def predict(net, fscale, tscale, X):
 
 
 def poly_residual(X, R, order):
-    """Residual of the polynomial through the last order+1 step starts (1 <= order <= 4),
-    from the quartic residual R by adding back the increments above `order`."""
+    """Residual of the polynomial through the last order+1 history snapshots
+    (1 <= order <= 4), from the quartic residual R by adding back the increments
+    above `order`."""
     P = np.zeros_like(R)
     for o in range(order + 1, NHIST):
         P[:, 0] += X[:, 2 * (o - 1)]

@@ -41,9 +41,11 @@ def test_ratios_and_scale():
     X, R, k = mfx.build_dataset(t0, h, s0, sh)
     first = X[k == k.min()][0]
     j = int(k.min())
-    d = t0[j] - t0[j - 1]
-    np.testing.assert_allclose(first[16:], [(t0[j - 3] - t0[j - 4]) / d, (t0[j - 2] - t0[j - 3]) / d,
-                                            (t0[j - 1] - t0[j - 2]) / d, h[j] / d], rtol=1e-12)
+    s = t0 + 0.5 * h           # half-step times of the history
+    d = s[j - 1] - s[j - 2]
+    np.testing.assert_allclose(first[16:], [(s[j - 4] - s[j - 5]) / d, (s[j - 3] - s[j - 4]) / d,
+                                            (s[j - 2] - s[j - 3]) / d, (t0[j] + 0.5 * h[j] - s[j - 1]) / d],
+                               rtol=1e-12)
     # first-order step-end increment has unit RMS over the entries
     rows = X[k == k.min()]
     np.testing.assert_allclose(np.sqrt(np.mean(rows[:, 8] ** 2 + rows[:, 9] ** 2)), 1.0, rtol=1e-12)
