@@ -673,21 +673,28 @@ def run_profile_case(args):
 def run_ensemble(args):
     """Batched-ensemble workload: ragged LVC members (2-4 states, 4-10 modes,
     4-10 SPFs, 16-48 points per mode, configurations per state capped) advanced
-    together with lockstep RK45, against the same members propagated one context
-    at a time.  Unit: member-fs/s (simulated fs summed over members per second)."""
+    together with lockstep RK45 (each attempt round one CUDA graph, launch shapes
+    chosen by the ensemble autotuner), against the same members propagated one
+    context at a time.  Unit: member-fs/s (simulated fs summed over members per
+    second).  e2e: the same interval through the public calls with host buffers
+    (every member's state uploaded before and downloaded after)."""
     import torch
     from macaw_gb300.capi import Ensemble, GpuCore
     from macaw_gb300.generate import ensemble
     torch.cuda.init()
     models = ensemble(count=args.members, max_conf=args.max_conf)
     starts = [initial_wavefunction(m) for m in models]
-    ens = Ensemble(models)
+    w0 = time.perf_counter()
+    ens = Ensemble(models, precision=args.precision)
+    create_s = time.perf_counter() - w0
     for i, (A, psi) in enumerate(starts):
         ens.set_state(i, A, psi, as_start=True)
     t = np.zeros(len(models))
     step = np.array([m.tout * m.eps_int for m in models])
-    # untimed start-up transient (steps grow from tout * eps_int)
+    # untimed start-up transient (steps grow from tout * eps_int); the first call
+    # runs the autotuner and captures the attempt-round graphs
     ens.propagate(INT_RK45, 0.1 / AU2FS, t, step)
+    tuning = ens.tuning()
     t0 = t.copy()
     es = torch.cuda.ExternalStream(ens.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -700,12 +707,24 @@ def run_ensemble(args):
     ms = ev0.elapsed_time(ev1)
     c1 = ens.counters()
     fs_total = float(np.sum(t - t0)) * AU2FS
+    # e2e: host states in, the next interval, host states out
+    states = [ens.get_state(i) for i in range(len(models))]
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for i, (A, psi) in enumerate(states):
+        ens.set_state(i, A, psi, as_start=False)
+    t2 = t.copy()
+    ens.propagate(INT_RK45, (0.1 + 2 * args.ens_fs) / AU2FS, t2, step)
+    back = [ens.get_state(i) for i in range(len(models))]
+    e2e_s = time.perf_counter() - w0
+    e2e_fs = float(np.sum(t2 - t)) * AU2FS
+    nbytes = int(sum(16 * (m.naconftot + m.dimpsi) for m in models))
     # the same members one context at a time (sequential), same interval
     seq_ms = 0.0
     nseq = min(len(models), args.seq_members)
     seq_fs = 0.0
     for i in range(nseq):
-        core = GpuCore(models[i])
+        core = GpuCore(models[i], precision=args.precision)
         A, psi = starts[i]
         core.set_state(A, psi, as_start=True)
         tt, ss, _, _, _ = core.propagate_interval(INT_RK45, 0.1 / AU2FS, 0.0, models[i].tout * models[i].eps_int)
@@ -719,8 +738,14 @@ def run_ensemble(args):
     sizes = [m.naconftot + m.dimpsi for m in models]
     line = {"metric": "member-fs/s of a batched ensemble (lockstep RK45)", "value": fs_total / (ms * 1e-3),
             "unit": "member-fs/s", "n_gpus": 1, "members": len(models), "ms": ms, "rounds": rounds,
+            "precision": precision_label(args.precision),
             "eom_member_evals_per_s": (c1["eom"] - c0["eom"]) * len(models) / (ms * 1e-3),
             "launches": c1["launches"] - c0["launches"],
+            "graphs": "one CUDA graph per attempt round and per step-start derivative",
+            "autotune": tuning, "create_s": create_s,
+            "e2e": {"value": e2e_fs / e2e_s, "unit": "member-fs/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes,
+                    "what": "every member's state uploaded, the next interval, every state downloaded"},
             "sequential": {"members": nseq, "member_fs_per_s": seq_fs / (seq_ms * 1e-3) if seq_ms else None,
                            "timing": "host wall clock around each member's propagate call"},
             "config": {"workload": "ragged LVC ensemble", "interval_fs": args.ens_fs, "max_conf": args.max_conf,

@@ -352,6 +352,20 @@ int64_t mctdh_ens_observables(mctdh_ens_t *ens, int64_t i, double *energy, doubl
                               double *auto_re, double *auto_im);
 int64_t mctdh_ens_counters(mctdh_ens_t *ens, int64_t *launches, int64_t *eom, int64_t *rounds);
 int64_t mctdh_ens_stream(mctdh_ens_t *ens, void **stream);
+/* Launch-shape autotuner of an ensemble (no reference counterpart).  Unless
+ * switched off, the first mctdh_ens_propagate times one merged EOM evaluation
+ * for each candidate shape -- fibre tiles per contraction block (2, 4, 8, 16),
+ * blocks per contraction (32, 64, 128) and, for split-precision members,
+ * tensor-core or CUDA-core mode products -- and keeps the fastest.  mode 1 runs
+ * it now on the current states, mode 0 keeps the planned shapes (an ensemble
+ * whose members must repeat the arithmetic of single contexts bit for bit);
+ * -7 once a propagation has fixed the shapes.  mctdh_ens_tuning reports the
+ * chosen shape, its EOM time (ms) against the planned shape's, and the number of
+ * candidates timed (0: not tuned).  Each attempt round of mctdh_ens_propagate
+ * runs as one CUDA graph. */
+int64_t mctdh_ens_autotune(mctdh_ens_t *ens, int64_t mode);
+int64_t mctdh_ens_tuning(mctdh_ens_t *ens, int64_t *tiles_per_block, int64_t *block_cap, int64_t *tensor_cores,
+                         double *eom_ms, double *default_eom_ms, int64_t *candidates);
 const char *mctdh_ens_last_error(mctdh_ens_t *ens);
 
 /* Tensor-core kernels (no reference counterpart).  The FP32 mode products of the

@@ -91,6 +91,8 @@ def load_library() -> C.CDLL:
     lib.mctdh_launch_count.argtypes = [vp]
     lib.mctdh_tensor_core_status.argtypes = [I64P, I64P]
     lib.mctdh_tensor_core_config.argtypes = [C.c_int64, C.c_int64]
+    lib.mctdh_ens_autotune.argtypes = [vp, C.c_int64]
+    lib.mctdh_ens_tuning.argtypes = [vp, I64P, I64P, I64P, DP, DP, I64P]
     lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
     lib.mctdh_event_record.argtypes = [vp, C.c_int64]
     lib.mctdh_event_elapsed.argtypes = [vp, C.c_int64, C.c_int64, DP]
@@ -159,7 +161,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets", "mctdh_device_bytes",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc", "mctdh_tensor_core_status",
-            "mctdh_tensor_core_config",
+            "mctdh_tensor_core_config", "mctdh_ens_autotune", "mctdh_ens_tuning",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
@@ -652,7 +654,7 @@ class Ensemble:
     """Independent wavepackets of uneven shape advanced together (mctdh_ens_*): one
     launch per EOM stage over all members, lockstep adaptive RK."""
 
-    def __init__(self, models, precision: int = 0):
+    def __init__(self, models, precision: int = 0, autotune: bool = True):
         self.lib = load_library()
         self.models = list(models)
         built = [build_setup(m, precision) for m in self.models]
@@ -664,6 +666,21 @@ class Ensemble:
         if rc != 0:
             raise MctdhError(rc, self.lib.mctdh_ens_last_error(None).decode())
         self.h = h
+        if not autotune:
+            self._check(self.lib.mctdh_ens_autotune(self.h, 0))
+
+    def autotune(self):
+        """Tune the launch shapes now, on the members' current states."""
+        self._check(self.lib.mctdh_ens_autotune(self.h, 1))
+        return self.tuning()
+
+    def tuning(self) -> Dict:
+        tpb, cap, tc, cand = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        ms, ms0 = C.c_double(), C.c_double()
+        self._check(self.lib.mctdh_ens_tuning(self.h, C.byref(tpb), C.byref(cap), C.byref(tc), C.byref(ms),
+                                              C.byref(ms0), C.byref(cand)))
+        return dict(tiles_per_block=tpb.value, block_cap=cap.value, tensor_cores=tc.value, eom_ms=ms.value,
+                    default_eom_ms=ms0.value, candidates=cand.value)
 
     def close(self):
         if getattr(self, "h", None):

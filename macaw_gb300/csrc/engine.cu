@@ -137,6 +137,16 @@ struct ProdBatch {
   }
 };
 
+// Blocks per contraction: one block per HOLE_TPB fibre tiles, at most HOLE_CAP
+// blocks; the partial buffers hold up to HOLE_NBLK_MAX blocks so that the
+// ensemble autotuner can re-tile without re-planning.
+#define HOLE_TPB 8
+#define HOLE_CAP 64
+#define HOLE_NBLK_MAX 128
+inline int hole_nblk(long long ntiles, int tpb, int cap) {
+  return (int)std::min<long long>(std::max<long long>(ntiles / tpb, 1), std::min(cap, HOLE_NBLK_MAX));
+}
+
 struct HoleBatch {
   std::vector<HoleDesc> h;
   HoleDesc* d = nullptr;
@@ -158,8 +168,8 @@ struct HoleBatch {
     hd.n1 = n1;
     hd.n2 = n2;
     long long ntiles = (L * R + HOLE_TILE - 1) / HOLE_TILE;
-    hd.nblk = (int)std::min<long long>(std::max<long long>(ntiles / 8, 1), 64);
-    hd.partial = ar.calloc_c((long long)hd.nblk * n1 * n2);
+    hd.nblk = hole_nblk(ntiles, HOLE_TPB, HOLE_CAP);
+    hd.partial = ar.calloc_c((long long)hole_nblk(ntiles, 1, HOLE_NBLK_MAX) * n1 * n2);
     h.push_back(hd);
     return (int)h.size() - 1;
   }
@@ -174,6 +184,17 @@ struct HoleBatch {
       bytes += (elem_bytes(hd.xfmt) * hd.n1 + (hd.X == hd.Y ? 0.0 : elem_bytes(hd.yfmt) * hd.n2)) * fib;
     }
     d = upload_vec(ar, h);
+  }
+  // new block counts (one block per `tpb` tiles, at most `cap`), in place on the device
+  void retile(int tpb, int cap, cudaStream_t st) {
+    if (h.empty()) return;
+    nblocks = 0;
+    for (auto& hd : h) {
+      hd.nblk = hole_nblk((hd.L * hd.R + HOLE_TILE - 1) / HOLE_TILE, tpb, cap);
+      hd.block_start = nblocks;
+      nblocks += hd.nblk;
+    }
+    CK(cudaMemcpyAsync(d, h.data(), sizeof(HoleDesc) * h.size(), cudaMemcpyHostToDevice, st));
   }
 };
 
@@ -214,6 +235,19 @@ struct RedBatch {
     }
     d_tg = upload_vec(ar, tg);
     d_terms = upload_vec(ar, terms);
+  }
+  // block counts of the terms whose partials belong to re-tiled contractions
+  void sync_nblk(const std::vector<const HoleBatch*>& hbs, cudaStream_t st) {
+    if (terms.empty()) return;
+    bool changed = false;
+    for (auto& rt : terms)
+      for (const HoleBatch* hb : hbs)
+        for (const auto& hd : hb->h)
+          if (hd.partial == rt.partial && rt.nblk != hd.nblk) {
+            rt.nblk = hd.nblk;
+            changed = true;
+          }
+    if (changed) CK(cudaMemcpyAsync(d_terms, terms.data(), sizeof(RedTerm) * terms.size(), cudaMemcpyHostToDevice, st));
   }
 };
 
@@ -3743,7 +3777,66 @@ struct Ens {
   std::vector<ProdBatch> ov_chain;
   long long launches = 0, eom_count = 0, rounds = 0;
   std::string last_error;
+  // CUDA graphs of the fixed launch sequences (index: 0 step-start derivative,
+  // 1 Cash-Karp attempt round, 2 Dormand-Prince attempt round), with the launches
+  // and EOM evaluations each replay stands for
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  long long graph_launches[3] = {0, 0, 0}, graph_eoms[3] = {0, 0, 0};
+  bool graphs_off = false;
+  // autotuned launch shapes (ens_autotune): fibre tiles per contraction block,
+  // block cap per contraction, tensor-core mode products (split path)
+  bool tuned = false;
+  int tune_tpb = HOLE_TPB, tune_cap = HOLE_CAP;
+  bool tune_tc = true;
+  double tune_ms = -1.0, tune_default_ms = -1.0;
+  int tune_candidates = 0;
 };
+
+// Run `body` (launches on E.st only, no host synchronisation) as CUDA graph slot
+// `k`: captured on the first call, replayed afterwards.  The round's step
+// lengths are read from device memory, so one graph serves every round.  If
+// capture fails the body runs eagerly from then on.
+template <class F>
+void ens_graph(Ens& E, int k, F body) {
+  if (E.graphs_off) {
+    body();
+    return;
+  }
+  if (!E.graph[k]) {
+    const long long l0 = E.launches, e0 = E.eom_count;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(E.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      E.graphs_off = true;
+      body();
+      return;
+    }
+    bool ok = true;
+    try {
+      body();
+    } catch (...) {
+      ok = false;
+    }
+    cudaError_t e = cudaStreamEndCapture(E.st, &g);
+    cudaGraphExec_t ge = nullptr;
+    ok = ok && e == cudaSuccess && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    E.graph_launches[k] = E.launches - l0;
+    E.graph_eoms[k] = E.eom_count - e0;
+    E.launches = l0;
+    E.eom_count = e0;
+    if (!ok) {
+      cudaGetLastError();
+      E.graphs_off = true;
+      body();
+      return;
+    }
+    E.graph[k] = ge;
+  }
+  CK(cudaGraphLaunch(E.graph[k], E.st));
+  E.launches += E.graph_launches[k];
+  E.eom_count += E.graph_eoms[k];
+}
 
 void merge_prod(ProdBatch& d, const ProdBatch& s) {
   d.h.insert(d.h.end(), s.h.begin(), s.h.end());
@@ -3900,6 +3993,8 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
 
 void ens_destroy(Ens* E) {
   cudaStreamSynchronize(E->st);
+  for (auto& ge : E->graph)
+    if (ge) cudaGraphExecDestroy(ge);
   for (Ctx* c : E->m) {
     for (auto& kv : c->dots) delete kv.second;
     for (auto e : c->evpool) cudaEventDestroy(e);
@@ -3911,7 +4006,7 @@ void ens_destroy(Ens* E) {
 
 void ens_run_prod(Ens& E, const ProdBatch& b) {
   if (b.h.empty()) return;
-  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec);
+  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec, E.tune_tc);
   ++E.launches;
 }
 void ens_run_hole(Ens& E, const HoleBatch& b) {
@@ -3941,6 +4036,74 @@ void ens_eom(Ens& E, cplx* out) {
   launch_spf(E.spf_d, (int)E.spf_h.size(), E.spf_tiles, E.spfop_d, out, E.der, E.status_d, E.st, E.precision, E.spf_nf);
   E.launches += 5;
   E.eom_count++;
+}
+
+// Contraction tiling of every merged contraction batch and their reductions.
+void ens_retile(Ens& E, int tpb, int cap) {
+  for (HoleBatch* hb : {&E.rho_holes, &E.holes, &E.ov_spf_holes, &E.ov_dots}) hb->retile(tpb, cap, E.st);
+  E.red.sync_nblk({&E.rho_holes, &E.holes}, E.st);
+  E.ov_spf_red.sync_nblk({&E.ov_spf_holes}, E.st);
+  E.ov_dot_red.sync_nblk({&E.ov_dots}, E.st);
+}
+
+// Autotuner of the ensemble's launch shapes, run once on the members' states
+// before the first propagation (and before any graph is captured): each
+// candidate (fibre tiles per contraction block, block cap per contraction, and
+// in the split path tensor-core or CUDA-core mode products) is timed with CUDA
+// events over two EOM evaluations of all members after one untimed one, and the
+// fastest is kept.  The merged EOM and the error-norm contractions share the
+// tiling.  Block counts change the order of the partial sums, not the
+// arithmetic of a partial: results move at the rounding level only.
+void ens_autotune(Ens& E) {
+  if (E.tuned) return;
+  E.tuned = true;
+  struct Cand { int tpb, cap; bool tc; };
+  std::vector<Cand> cands;
+  const int tpbs[] = {8, 4, 16, 2};
+  const int caps[] = {64, 128, 32};
+  for (int tc = 1; tc >= 0; --tc) {
+    if (!tc && E.precision != 1) break;
+    for (int cap : caps)
+      for (int tpb : tpbs) cands.push_back(Cand{tpb, cap, tc == 1});
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaMemcpyAsync(E.IN, E.Y, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
+  const long long l0 = E.launches, q0 = E.eom_count;
+  double best = 1e300;
+  Cand bc = cands[0];
+  for (size_t i = 0; i < cands.size(); ++i) {
+    const Cand& c = cands[i];
+    E.tune_tc = c.tc;
+    ens_retile(E, c.tpb, c.cap);
+    ens_eom(E, E.K[6]);
+    CK(cudaEventRecord(e0, E.st));
+    ens_eom(E, E.K[6]);
+    ens_eom(E, E.K[6]);
+    CK(cudaEventRecord(e1, E.st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (i == 0) E.tune_default_ms = 0.5 * ms;
+    if (0.5 * ms < best) {
+      best = 0.5 * ms;
+      bc = c;
+    }
+  }
+  CK(cudaEventDestroy(e0));
+  CK(cudaEventDestroy(e1));
+  E.tune_tc = bc.tc;
+  E.tune_tpb = bc.tpb;
+  E.tune_cap = bc.cap;
+  E.tune_ms = best;
+  E.tune_candidates = (int)cands.size();
+  ens_retile(E, bc.tpb, bc.cap);
+  E.launches = l0;
+  E.eom_count = q0;
+  // the EOMs of the tuning ran on the start states: clear what they may have flagged
+  CK(cudaMemsetAsync(E.status_d, 0, sizeof(int), E.st));
+  CK(cudaStreamSynchronize(E.st));
 }
 
 void ens_stage(Ens& E, cplx* out, const cplx* base, const double* coef, int nk) {
@@ -3975,6 +4138,7 @@ void ens_check_status(Ens& E) {
 // (propagator.f90:110-134).  Dormand-Prince re-evaluates the first stage at each
 // step start instead of carrying it (the same numbers: the EOM is deterministic).
 void ens_propagate(Ens& E, int method, double tnext, double* t, double* step) {
+  ens_autotune(E);
   const int n = (int)E.m.size();
   const bool dp = (method == 2);
   const double errcon = pow(5.0 / RK_SAFETY, 1.0 / RK_PGROW);
@@ -3988,8 +4152,10 @@ void ens_propagate(Ens& E, int method, double tnext, double* t, double* step) {
     if (!any) break;
     if (guard > 1000000) throw StatusError(MCTDH_ESTEP, "ensemble propagation did not finish");
     // the derivative at every member's step start
-    CK(cudaMemcpyAsync(E.IN, E.Y, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
-    ens_eom(E, E.K[0]);
+    ens_graph(E, 0, [&] {
+      CK(cudaMemcpyAsync(E.IN, E.Y, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
+      ens_eom(E, E.K[0]);
+    });
     std::vector<int> pending(n, 0);
     for (int i = 0; i < n; ++i) {
       pending[i] = !done[i];
@@ -4003,24 +4169,26 @@ void ens_propagate(Ens& E, int method, double tnext, double* t, double* step) {
       std::vector<double> dth(n);
       for (int i = 0; i < n; ++i) dth[i] = pending[i] ? dt[i] : 0.0;
       CK(cudaMemcpyAsync(E.dt_d, dth.data(), sizeof(double) * n, cudaMemcpyHostToDevice, E.st));
-      for (int sg = 1; sg < 6; ++sg) {
-        ens_stage(E, E.IN, E.Y, dp ? DP_B[sg] : CK_B[sg], sg);
-        ens_eom(E, E.K[sg]);
-      }
-      ens_stage(E, E.TMP, E.Y, dp ? DP_C : CK_C, 6);
-      if (dp) {
-        CK(cudaMemcpyAsync(E.IN, E.TMP, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
-        ens_eom(E, E.K[6]);
-        ens_stage(E, E.ERR, E.Y, DP_D, 7);
-      } else {
-        ens_stage(E, E.ERR, E.Y, CK_D, 6);
-      }
-      // DeltaPsi (gmctdh_objects.f90:206-226) of every member
-      ens_run_hole(E, E.ov_spf_holes);
-      ens_run_red(E, E.ov_spf_red);
-      for (size_t d = 1; d < E.ov_chain.size(); ++d) ens_run_prod(E, E.ov_chain[d]);
-      ens_run_hole(E, E.ov_dots);
-      ens_run_red(E, E.ov_dot_red);
+      ens_graph(E, dp ? 2 : 1, [&] {
+        for (int sg = 1; sg < 6; ++sg) {
+          ens_stage(E, E.IN, E.Y, dp ? DP_B[sg] : CK_B[sg], sg);
+          ens_eom(E, E.K[sg]);
+        }
+        ens_stage(E, E.TMP, E.Y, dp ? DP_C : CK_C, 6);
+        if (dp) {
+          CK(cudaMemcpyAsync(E.IN, E.TMP, sizeof(cplx) * E.total, cudaMemcpyDeviceToDevice, E.st));
+          ens_eom(E, E.K[6]);
+          ens_stage(E, E.ERR, E.Y, DP_D, 7);
+        } else {
+          ens_stage(E, E.ERR, E.Y, CK_D, 6);
+        }
+        // DeltaPsi (gmctdh_objects.f90:206-226) of every member
+        ens_run_hole(E, E.ov_spf_holes);
+        ens_run_red(E, E.ov_spf_red);
+        for (size_t d = 1; d < E.ov_chain.size(); ++d) ens_run_prod(E, E.ov_chain[d]);
+        ens_run_hole(E, E.ov_dots);
+        ens_run_red(E, E.ov_dot_red);
+      });
       CK(cudaMemcpyAsync(res.data(), E.res_d, sizeof(cplx) * 3 * n, cudaMemcpyDeviceToHost, E.st));
       ens_check_status(E);
       for (int i = 0; i < n; ++i) {
@@ -4962,6 +5130,41 @@ int64_t mctdh_ens_counters(mctdh_ens_t* ens, int64_t* launches, int64_t* eom, in
   if (launches) *launches = ens->e->launches;
   if (eom) *eom = ens->e->eom_count;
   if (rounds) *rounds = ens->e->rounds;
+  return MCTDH_OK;
+}
+
+int64_t mctdh_ens_autotune(mctdh_ens_t* ens, int64_t mode) {
+  if (!ens || mode < 0 || mode > 1) return MCTDH_EARG;
+  Ens& E = *ens->e;
+  if (E.graph[0] || E.graph[1] || E.graph[2])
+    return MCTDH_EARG;   // the launch shapes are fixed once a propagation captured its graphs
+  try {
+    if (mode == 0) {
+      E.tuned = true;    // keep the planned shapes
+      return MCTDH_OK;
+    }
+    E.tuned = false;
+    ens_autotune(E);
+    return MCTDH_OK;
+  } catch (const StatusError& e) {
+    E.last_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    E.last_error = e.what();
+    return MCTDH_ECUDA;
+  }
+}
+
+int64_t mctdh_ens_tuning(mctdh_ens_t* ens, int64_t* tiles_per_block, int64_t* block_cap, int64_t* tensor_cores,
+                         double* eom_ms, double* default_eom_ms, int64_t* candidates) {
+  if (!ens) return MCTDH_EARG;
+  const Ens& E = *ens->e;
+  if (tiles_per_block) *tiles_per_block = E.tune_tpb;
+  if (block_cap) *block_cap = E.tune_cap;
+  if (tensor_cores) *tensor_cores = (E.tune_tc && E.precision == 1 && tc_enabled()) ? 1 : 0;
+  if (eom_ms) *eom_ms = E.tune_ms;
+  if (default_eom_ms) *default_eom_ms = E.tune_default_ms;
+  if (candidates) *candidates = E.tune_candidates;
   return MCTDH_OK;
 }
 

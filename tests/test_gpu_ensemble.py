@@ -44,7 +44,9 @@ def test_ensemble_propagation_matches_single_contexts(method):
     sequence its own context takes, so C(t), populations, norm and energy agree."""
     from macaw_gb300.capi import Ensemble, GpuCore
     models = _members()
-    ens = Ensemble(models)
+    # the planned launch shapes: the autotuner may re-tile the contractions, which
+    # reorders their partial sums
+    ens = Ensemble(models, autotune=False)
     starts = [initial_wavefunction(m) for m in models]
     for i, (A, psi) in enumerate(starts):
         ens.set_state(i, A, psi, as_start=True)
@@ -82,3 +84,41 @@ def test_generated_ragged_ensemble_runs():
     for i in range(len(models)):
         ob = ens.observables(i, t[i])
         assert abs(ob["norm"] - 1.0) < 1e-6
+
+
+def test_autotuned_split_precision_ensemble():
+    """Split-FP32 members (compensated contractions) with the launch-shape
+    autotuner: the chosen shape is the fastest timed one, every member's EOM
+    agrees with its own split-precision context to 1e-10 relative (re-tiling
+    only reorders compensated partial sums), and a lockstep RK45 interval of
+    0.1 fs agrees with single-context runs within 10 eps_int (free-running step
+    control)."""
+    from macaw_gb300.capi import Ensemble, GpuCore
+    models = _members()
+    ens = Ensemble(models, precision=1)
+    states = [random_state(m, seed=70 + i) for i, m in enumerate(models)]
+    for i, (A, psi) in enumerate(states):
+        ens.set_state(i, A, psi, as_start=True)
+    tun = ens.autotune()
+    assert tun["candidates"] >= 12
+    assert 0.0 < tun["eom_ms"] <= tun["default_eom_ms"]
+    got = ens.calc_derivs()
+    for m, (A, psi), (dA, dpsi) in zip(models, states, got):
+        rA, rpsi = GpuCore(m, precision=1).calc_derivs(A, psi)
+        assert _rel(dA, rA) < 1e-10
+        assert _rel(dpsi, rpsi) < 1e-10
+    starts = [initial_wavefunction(m) for m in models]
+    for i, (A, psi) in enumerate(starts):
+        ens.set_state(i, A, psi, as_start=True)
+    tnext = 0.1 / AU2FS
+    t = np.zeros(len(models))
+    step = np.array([m.tout * m.eps_int for m in models])
+    ens.propagate(INT_RK45, tnext, t, step)
+    for i, (m, (A, psi)) in enumerate(zip(models, starts)):
+        core = GpuCore(m, precision=1)
+        core.set_state(A, psi, as_start=True)
+        ts, _, _, _, _ = core.propagate_interval(INT_RK45, tnext, 0.0, m.tout * m.eps_int)
+        ref = core.observables(ts)
+        ob = ens.observables(i, t[i])
+        assert abs(ob["auto"] - ref["auto"]) < 10 * m.eps_int
+        assert np.abs(ob["pop"] - ref["pop"]).max() < 10 * m.eps_int
