@@ -503,7 +503,8 @@ def run_gpu(args):
                 "split precision"),
         "precision": prec_label,
         "tensor_cores": {"enabled": bool(tc["enabled"]), "mma_wait_timeouts": tc["timeouts"],
-                         "served": "FP32 mode products of batches with 9-16 SPFs"},
+                         "served": "not by default in single contexts: the FP32 CUDA-core mode product is "
+                                   "faster on this model (mctdh_tensor_core_config switches it on)"},
         "step_fs_mean": statistics.mean(head["hdids"]),
         "fp64_path": {"value": fp64_value, "unit": "fs/s", "ms_per_step": ref["ms"] / args.steps,
                       "step_fs_mean": statistics.mean(ref["hdids"]),

@@ -369,10 +369,11 @@ int64_t mctdh_ens_tuning(mctdh_ens_t *ens, int64_t *tiles_per_block, int64_t *bl
 const char *mctdh_ens_last_error(mctdh_ens_t *ens);
 
 /* Tensor-core kernels (no reference counterpart).  The FP32 mode products of the
- * split-precision paths run as tcgen05 MMAs (TF32 parts, FP32 accumulation) for
- * batches whose largest SPF count is at least min_n (default 9; below it the
- * CUDA-core kernel is faster) and at most 16, with a one- or two-stage pipeline
- * (default 2).  status: *enabled is 1 unless the environment variable
+ * split-precision paths can run as tcgen05 MMAs (TF32 parts, FP32 accumulation)
+ * for batches whose largest SPF count is at least min_n and at most 16, with a
+ * one- or two-stage pipeline (default 1).  Single contexts default to min_n = 17
+ * (the CUDA-core kernel, faster on the measured models); ensembles let their
+ * autotuner choose.  status: *enabled is 1 unless the environment variable
  * MACAW_GB300_TC=0 selected the CUDA-core kernels for this process; *timeouts is
  * 1 when a tensor-core kernel gave up waiting for its MMAs since the previous
  * call (the flag is cleared).  config: 0 keeps a setting; it applies to launches

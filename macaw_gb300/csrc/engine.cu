@@ -4006,7 +4006,7 @@ void ens_destroy(Ens* E) {
 
 void ens_run_prod(Ens& E, const ProdBatch& b) {
   if (b.h.empty()) return;
-  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec, E.tune_tc);
+  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec, E.tune_tc ? 2 : 0);
   ++E.launches;
 }
 void ens_run_hole(Ens& E, const HoleBatch& b) {

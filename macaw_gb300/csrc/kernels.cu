@@ -166,8 +166,8 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   }
 }
 
-// Tensor-core kernels (tc.cu) serve the FP32 products unless MACAW_GB300_TC=0
-// selects the CUDA-core kernels (read once per process).
+// Tensor-core kernels (tc.cu) may serve the FP32 products unless
+// MACAW_GB300_TC=0 selects the CUDA-core kernels (read once per process).
 bool tc_enabled() {
   static int on = -1;
   if (on < 0) {
@@ -177,10 +177,12 @@ bool tc_enabled() {
   return on == 1;
 }
 
+// tc: 0 CUDA-core kernel, 1 tensor cores from the configured SPF count on,
+// 2 tensor cores for every size they take (the ensemble autotuner's candidate)
 void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, int prec,
-                 bool allow_tc) {
+                 int tc) {
   if (ndesc <= 0 || nblocks <= 0) return;
-  if (prec == 1 && allow_tc && tc_enabled() && launch_prod_tc(d_descs, ndesc, nblocks, maxn, st)) return;
+  if (prec == 1 && tc && tc_enabled() && launch_prod_tc(d_descs, ndesc, nblocks, maxn, st, tc == 2)) return;
   const unsigned nb = (unsigned)nblocks;
   if (maxn <= 12) {
     if (prec == 0) prod_kernel<12, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);

@@ -214,10 +214,12 @@ __global__ void __launch_bounds__(TC_ROWS) prod_tc_kernel(const ProdDesc* __rest
 
 static int g_tc_nsm = 0;
 // pipeline stages of the tensor-core mode product (MACAW_GB300_TC_STAGES=1 or 2)
-static int g_tc_stages = 2;
-// smallest largest-SPF-count of a batch that goes to the tensor cores
-// (MACAW_GB300_TC_MIN_N; below it the FP32 CUDA-core kernel is faster)
-static int g_tc_min_n = 9;
+static int g_tc_stages = 1;
+// smallest largest-SPF-count of a batch that single contexts send to the tensor
+// cores (MACAW_GB300_TC_MIN_N or mctdh_tensor_core_config).  Default 17, i.e.
+// none: on the benchmark model the FP32 CUDA-core kernel is faster at 8 and at
+// 12 SPFs and its round-to-nearest sums drift less over long propagations.
+static int g_tc_min_n = 17;
 
 // Once per process, outside any stream capture (context creation calls it): the
 // SM count and the dynamic shared-memory limit of the tensor-core kernel.
@@ -229,16 +231,16 @@ void tc_prepare() {
   cudaFuncSetAttribute(prod_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        2 * TC_NPART * (TC_ROWS * 2 * TC_MAXN * 4 + 2 * TC_MAXN * 2 * TC_MAXN * 4));
   const char* e = getenv("MACAW_GB300_TC_STAGES");
-  g_tc_stages = (e && e[0] == '1') ? 1 : 2;
+  g_tc_stages = (e && e[0] == '2') ? 2 : 1;
   const char* m = getenv("MACAW_GB300_TC_MIN_N");
   if (m && atoi(m) > 0) g_tc_min_n = atoi(m);
   g_tc_nsm = nsm > 0 ? nsm : 152;
 }
 
-// Tensor-core path for FP32 products of nin, nout <= 16 (and at least the
-// threshold); false: not taken
-bool launch_prod_tc(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st) {
-  if (maxn > TC_MAXN || maxn < g_tc_min_n || ndesc <= 0 || nblocks <= 0 || !g_tc_nsm) return false;
+// Tensor-core path for FP32 products of nin, nout <= 16, from the threshold on
+// (force: any size up to 16); false: not taken
+bool launch_prod_tc(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, bool force) {
+  if (maxn > TC_MAXN || (!force && maxn < g_tc_min_n) || ndesc <= 0 || nblocks <= 0 || !g_tc_nsm) return false;
   const int K = ((2 * maxn + 7) / 8) * 8;
   const int N = 2 * maxn <= 16 ? 16 : 32;
   const size_t stage = (size_t)TC_NPART * ((size_t)TC_ROWS * K * 4 + (size_t)N * K * 4);

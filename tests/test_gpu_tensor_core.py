@@ -31,7 +31,7 @@ def capi():
         pytest.skip("tensor-core kernels switched off (MACAW_GB300_TC=0)")
     capi.tensor_core_config(min_n=1)
     yield capi
-    capi.tensor_core_config(min_n=9, stages=2)
+    capi.tensor_core_config(min_n=17, stages=1)
 
 
 def _check(capi, model, seed):
