@@ -313,6 +313,10 @@ int64_t mctdh_mfx_fetch(mctdh_ctx_t *ctx, int64_t maxrec, double *t0, double *h,
                         int64_t *n);
 int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, const double *fscale, const double *tscale,
                          double tol);
+/* orders: the polynomial orders (1-4, default 4) through the last order + 1
+ * history snapshots that the network's residual is added to, at the step start
+ * and at the half step (chosen at training on held-out steps). */
+int64_t mctdh_mfx_orders(mctdh_ctx_t *ctx, int64_t order_start, int64_t order_half);
 /* predict: run the attached extrapolator on a given history (5 x E complex
  * snapshots, oldest first, at times ts[5]) for the times tau0 (a step start) and
  * tau1 (its half step); writes the two predicted snapshots (E complex each) and

@@ -117,6 +117,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_mfx_attach.argtypes = [vp, vp, DP, DP, C.c_double]
     lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P, I64P, DP]
     lib.mctdh_mfx_predict.argtypes = [vp, DP, DP, C.c_double, C.c_double, DP, DP]
+    lib.mctdh_mfx_orders.argtypes = [vp, C.c_int64, C.c_int64]
     lib.mctdh_mfx_log.argtypes = [vp, C.c_int64, DP, I64P]
     lib.mctdh_ens_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
     lib.mctdh_ens_destroy.argtypes = [vp]
@@ -132,10 +133,11 @@ def load_library() -> C.CDLL:
     lib.mctdh_ens_last_error.restype = C.c_char_p
     for name in ("mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
                  "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
-                 "mctdh_ens_counters", "mctdh_ens_stream"):
+                 "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_autotune", "mctdh_ens_tuning",
+                 "mctdh_tensor_core_status", "mctdh_tensor_core_config"):
         getattr(lib, name).restype = C.c_int64
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
-                 "mctdh_mfx_predict", "mctdh_mfx_log"):
+                 "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders"):
         getattr(lib, name).restype = C.c_int64
     lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
                                                  C.c_int64, C.c_void_p]
@@ -165,7 +167,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
-            "mctdh_mfx_predict", "mctdh_mfx_log",
+            "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders",
             "mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
             "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
             "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_last_error"]
@@ -564,6 +566,8 @@ class GpuCore:
             if fs.size != 20 or ts.size != 4:
                 raise ValueError("fscale needs 20 entries and tscale 4")
             self._check(self.lib.mctdh_mfx_attach(self.h, mlp.h, fs.ctypes.data_as(DP), ts.ctypes.data_as(DP), tol))
+            o0, o1 = getattr(mlp, "orders", (4, 4))
+            self._check(self.lib.mctdh_mfx_orders(self.h, int(o0), int(o1)))
         self._mlp_ref = mlp
 
     def mfx_predict(self, hist, ts, tau0, tau1):

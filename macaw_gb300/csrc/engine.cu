@@ -3216,6 +3216,7 @@ struct MfxState {
   cplx *half = nullptr, *start = nullptr, *pred0 = nullptr, *pred1 = nullptr, *now = nullptr, *backup = nullptr;
   mctdh_mlp* mlp = nullptr;
   double fscale[MFX_NFEAT] = {}, tscale[MFX_NOUT] = {}, tol = 0.0;
+  int order[2] = {MFX_NHIST - 1, MFX_NHIST - 1};   // polynomial order at the step start / half step
   bool recording = false;
   std::vector<double> rec_t0, rec_h;
   std::vector<cplx> rec_s0, rec_sh;
@@ -3324,13 +3325,17 @@ void mfx_predict(Ctx& c, MfxState& M, double tau0, double tau1) {
   for (int tau = 0; tau < 2; ++tau) {
     double prev[MFX_NHIST] = {};
     prev[NH - 1] = 1.0;   // P_0 = newest value
+    double base[MFX_NHIST];
+    memcpy(base, prev, sizeof(base));
     for (int o = 1; o < NH; ++o) {
       double w[MFX_NHIST];
       lagrange_tail(ts, NH, NH - 1 - o, taus[tau], w);
       for (int j = 0; j < NH; ++j) cf.inc[tau][o - 1][j] = w[j] - prev[j];
       memcpy(prev, w, sizeof(prev));
+      if (o == M.order[tau]) memcpy(base, w, sizeof(base));
     }
-    for (int j = 0; j < NH; ++j) cf.base[tau][j] = prev[j];
+    // the polynomial of the order chosen at training for this prediction time
+    for (int j = 0; j < NH; ++j) cf.base[tau][j] = base[j];
   }
   const double dlast = ts[NH - 1] - ts[NH - 2];
   for (int j = 0; j < NH - 2; ++j) cf.ratio[j] = (ts[j + 1] - ts[j]) / dlast;
@@ -4828,6 +4833,17 @@ int64_t mctdh_mfx_attach(mctdh_ctx_t* ctx, mctdh_mlp* mlp, const double* fscale,
       for (int j = 0; j < MFX_NOUT; ++j) M.tscale[j] = tscale[j];
     }
     M.tol = tol;
+  });
+}
+
+int64_t mctdh_mfx_orders(mctdh_ctx_t* ctx, int64_t order_start, int64_t order_half) {
+  if (!ctx || order_start < 1 || order_start > MFX_NHIST - 1 || order_half < 1 || order_half > MFX_NHIST - 1)
+    return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    MfxState& M = mfx_state(*c);
+    M.order[0] = (int)order_start;
+    M.order[1] = (int)order_half;
   });
 }
 

