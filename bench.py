@@ -153,7 +153,8 @@ def flush_l2(buf):
 PRECISION_LABEL = {0: "fp64", 1: "fp32 products, compensated fp32 contractions",
                    2: "compensated fp32 products and contractions", 3: "fp32 products and contractions",
                    4: "fp32 mean-field products, compensated H_B products and contractions",
-                   5: "compensated mean-field products and contractions, fp32 H_B products"}
+                   5: "compensated mean-field products and contractions, fp32 H_B products",
+                   6: "fp32 products and mean-field contractions, compensated densities"}
 
 
 def precision_label(prec):
@@ -364,15 +365,21 @@ def run_size_scan(args):
     A1, psi1 = pre.get_state()
     pre.close()
     state = (A0, psi0, A1, psi1)
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        ref_core, ref = run_arm(model, 0, state, t1, h1, args, l2, torch, tdist, profile=False)
-        mix_core, mix = run_arm(model, args.precision, state, t1, h1, args, l2, torch, tdist, profile=False)
-    cmp = {}
+    # one context at a time (the FP64 arm is closed before the split arm is set up),
+    # so the device holds a single plan: each arm's timed steps, then its
+    # continuation over the accuracy interval
     acc_fs = ACC_FS if args.workload != "qvc24" else 0.1
-    for name, core in (("fp64", ref_core), ("mixed", mix_core)):
-        core.set_state(A1, psi1, as_start=False)
-        tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + acc_fs / AU2FS, t1, h1)
-        cmp[name] = core.observables(tt)
+    cmp, dev_bytes = {}, {}
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        arms = {}
+        for name, prec in (("fp64", 0), ("mixed", args.precision)):
+            core, arms[name] = run_arm(model, prec, state, t1, h1, args, l2, torch, tdist, profile=False)
+            dev_bytes[name] = core.device_bytes()
+            core.set_state(A1, psi1, as_start=False)
+            tt, _, _, _, _ = core.propagate_interval(INT_CMF2, t1 + acc_fs / AU2FS, t1, h1)
+            cmp[name] = core.observables(tt)
+            core.close()
+    ref, mix = arms["fp64"], arms["mixed"]
     value = mix["fs"] / (mix["ms"] * 1e-3)
     fp64_value = ref["fs"] / (ref["ms"] * 1e-3)
     ntot = int(model.naconftot)
@@ -389,7 +396,7 @@ def run_size_scan(args):
             "eom_per_s": mix["eom"] / (mix["ms"] * 1e-3), "hb_per_s": mix["hb"] / (mix["ms"] * 1e-3),
             "fp64_eom_per_s": ref["eom"] / (ref["ms"] * 1e-3),
             "clocks": clk.summary(),
-            "device_bytes": {"fp64": ref_core.device_bytes(), "split": mix_core.device_bytes()},
+            "device_bytes": {"fp64": dev_bytes["fp64"], "split": dev_bytes["mixed"]},
             "config": {"workload": args.workload, "nspf": args.nspf if args.workload != "qvc24" else 8,
                        "coefficients": ntot,
                        "coefficient_bytes": 16 * ntot, "dimpsi": int(model.dimpsi),
@@ -416,8 +423,17 @@ def run_gpu(args):
     A1, psi1 = pre.get_state()
     from macaw_gb300 import mfx
     tr0 = time.perf_counter()
-    X, R, ks = mfx.build_dataset(*pre.mfx_fetch())
-    net, fscale, tscale, tr_loss = mfx.train(X, R, steps=ks, epochs=MFX_EPOCHS)
+    # training data: the start state's own 0 -> 1 fs and that of seeded variants of
+    # it (displaced initial Gaussians); the last variant is held back for the gating
+    records = [pre.mfx_fetch()]
+    for Av, pv in mfx.variant_states(model, 1 + args.mfx_variants, seed=11)[1:]:
+        pre.set_state(Av, pv, as_start=True)
+        pre.mfx_record(2)
+        pre.propagate_interval(INT_CMF2, PRE_FS / AU2FS, 0.0, model.tout * model.eps_int)
+        records.append(pre.mfx_fetch())
+    X, R, ks = mfx.build_datasets(records)
+    net, fscale, tscale, tr_loss = mfx.train(X, R, steps=ks, epochs=MFX_EPOCHS,
+                                             val_frac=1.0 / len(records) if len(records) > 1 else 0.2)
     train_s = time.perf_counter() - tr0
     pre.close()
     mfx_net = (net, fscale, tscale)
@@ -524,7 +540,9 @@ def run_gpu(args):
                      "rejected": mfx_stats["rejected"], "last_mismatch": mfx_stats["last_rel"],
                      "training": {"rows": int(len(X)), "epochs": MFX_EPOCHS, "loss": tr_loss,
                                   "seconds": train_s,
-                                  "data": f"the untimed FP64 CMF2 steps from 0 to {PRE_FS} fs"},
+                                  "data": f"untimed FP64 CMF2 steps from 0 to {PRE_FS} fs of the start state "
+                                          f"and of {args.mfx_variants} seeded variants (initial Gaussians "
+                                          f"displaced by up to 0.3 in position and momentum)"},
                      "accuracy_vs_fp64_path": acc_mfx},
         "eom_per_s": head["eom"] / (head["ms"] * 1e-3), "hb_per_s": head["hb"] / (head["ms"] * 1e-3),
         "e2e": {"value": e2e_fs / e2e_s, "unit": "fs/s", "h2d_bytes_per_step": nbytes,
@@ -696,6 +714,8 @@ def run_ensemble(args):
     # runs the autotuner and captures the attempt-round graphs
     ens.propagate(INT_RK45, 0.1 / AU2FS, t, step)
     tuning = ens.tuning()
+    cost = ens.eom_cost()
+    hbm_peak = load_peaks()[0]["hbm_gbs"]
     t0 = t.copy()
     es = torch.cuda.ExternalStream(ens.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -744,6 +764,14 @@ def run_ensemble(args):
             "launches": c1["launches"] - c0["launches"],
             "graphs": "one CUDA graph per attempt round and per step-start derivative",
             "autotune": tuning, "create_s": create_s,
+            "roofline": {"bound": "hbm", "achieved": cost["bytes"] / (tuning["eom_ms"] * 1e-3) / 1e9,
+                         "peak": hbm_peak, "unit": "GB/s",
+                         "frac": cost["bytes"] / (tuning["eom_ms"] * 1e-3) / 1e9 / hbm_peak,
+                         "traffic": None,
+                         "kernel": "one merged EOM evaluation of all members (CUDA events, autotuner's "
+                                   "timing); algorithmic bytes of its mode products and contractions",
+                         "alg_bytes_per_eom": cost["bytes"], "alg_flops_per_eom": cost["flops"]}
+            if tuning["eom_ms"] > 0 else None,
             "e2e": {"value": e2e_fs / e2e_s, "unit": "member-fs/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes,
                     "what": "every member's state uploaded, the next interval, every state downloaded"},
@@ -816,8 +844,10 @@ def main():
     ap.add_argument("--acc-precisions", default="1,4", help="accuracy: split arms compared with FP64")
     ap.add_argument("--headline", default="mfx", choices=["mfx", "split"],
                     help="qvc12: the arm the line's value is: split precision with (mfx) or without the extrapolator")
+    ap.add_argument("--mfx-variants", type=int, default=3,
+                    help="extrapolator: seeded initial-state variants recorded besides the start state")
     ap.add_argument("--pre-fs", type=float, default=0.3, help="qvc24: untimed FP64 propagation before the steps")
-    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2, 3, 4, 5],
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2, 3, 4, 5, 6],
                     help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
     ap.add_argument("--workload", default="qvc12",
                     choices=["qvc12", "qvc12n", "qvc24", "ensemble", "lvc5", "gmctdh16", "lvc5mix", "accuracy"],

@@ -62,7 +62,8 @@ typedef struct mctdh_setup {
   int64_t precision;                    /* 0 FP64; 1 FP32 products, compensated contractions;
                                            2 compensated products and contractions; 3 FP32 products
                                            and contractions; 4 as 1 with compensated H_B products of the
-                                           Lanczos steps; 5 as 2 with FP32 H_B products */
+                                           Lanczos steps; 5 as 2 with FP32 H_B products; 6 as 1 with
+                                           FP32-summed mean-field contractions (densities compensated) */
   int64_t int_order, int_par1;          /* Adams PECE order and extra EC iterations (abm<order><par1>) */
   /* Operators whose expectation values are written (the 'expect' keyword,
    * input.f90:196-216, terms read by Read_Operators, input.f90:516-748).  Their
@@ -370,6 +371,10 @@ int64_t mctdh_ens_stream(mctdh_ens_t *ens, void **stream);
 int64_t mctdh_ens_autotune(mctdh_ens_t *ens, int64_t mode);
 int64_t mctdh_ens_tuning(mctdh_ens_t *ens, int64_t *tiles_per_block, int64_t *block_cap, int64_t *tensor_cores,
                          double *eom_ms, double *default_eom_ms, int64_t *candidates);
+/* Algorithmic cost of one merged EOM evaluation of all members: the FLOPs and
+ * bytes (operands read once, results written once) of its mode products and
+ * single-hole contractions, the roofline numerator of the EOM time. */
+int64_t mctdh_ens_eom_cost(mctdh_ens_t *ens, double *flops, double *bytes);
 const char *mctdh_ens_last_error(mctdh_ens_t *ens);
 
 /* Tensor-core kernels (no reference counterpart).  The FP32 mode products of the

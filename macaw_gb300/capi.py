@@ -93,6 +93,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_tensor_core_config.argtypes = [C.c_int64, C.c_int64]
     lib.mctdh_ens_autotune.argtypes = [vp, C.c_int64]
     lib.mctdh_ens_tuning.argtypes = [vp, I64P, I64P, I64P, DP, DP, I64P]
+    lib.mctdh_ens_eom_cost.argtypes = [vp, DP, DP]
     lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
     lib.mctdh_event_record.argtypes = [vp, C.c_int64]
     lib.mctdh_event_elapsed.argtypes = [vp, C.c_int64, C.c_int64, DP]
@@ -133,7 +134,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_ens_last_error.restype = C.c_char_p
     for name in ("mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
                  "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
-                 "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_autotune", "mctdh_ens_tuning",
+                 "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_autotune", "mctdh_ens_tuning", "mctdh_ens_eom_cost",
                  "mctdh_tensor_core_status", "mctdh_tensor_core_config"):
         getattr(lib, name).restype = C.c_int64
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
@@ -163,7 +164,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_expect", "mctdh_natpop", "mctdh_densmat", "mctdh_density", "mctdh_packets", "mctdh_device_bytes",
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc", "mctdh_tensor_core_status",
-            "mctdh_tensor_core_config", "mctdh_ens_autotune", "mctdh_ens_tuning",
+            "mctdh_tensor_core_config", "mctdh_ens_autotune", "mctdh_ens_tuning", "mctdh_ens_eom_cost",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
@@ -685,6 +686,12 @@ class Ensemble:
                                               C.byref(ms0), C.byref(cand)))
         return dict(tiles_per_block=tpb.value, block_cap=cap.value, tensor_cores=tc.value, eom_ms=ms.value,
                     default_eom_ms=ms0.value, candidates=cand.value)
+
+    def eom_cost(self) -> Dict:
+        """Algorithmic FLOPs and bytes of one merged EOM evaluation."""
+        fl, by = C.c_double(), C.c_double()
+        self._check(self.lib.mctdh_ens_eom_cost(self.h, C.byref(fl), C.byref(by)))
+        return dict(flops=fl.value, bytes=by.value)
 
     def close(self):
         if getattr(self, "h", None):

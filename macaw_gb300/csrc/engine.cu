@@ -382,6 +382,7 @@ struct Ctx {
   int int_type_psi = 1;
   int precision = 0;
   int hole_prec = 0;   // single-hole contractions: 0 FP64, 1 FP32 sums, 2 compensated FP32
+  int mf_hole_prec = 0;   // the mean-field ones (densities keep hole_prec)
   int hb_prec = 0;     // H_B * B products of the Lanczos steps: 0 FP64, 1 FP32, 2 compensated FP32
   bool reginv_cold = false;   // regularised inverses without the Jacobi warm start
   std::string last_error;
@@ -469,6 +470,7 @@ struct Ctx {
   OvlPlan dpsi_plan;   // d_tmp vs d_err
   OvlPlan cmf_ovl;     // CMF2's SPF error: d_ovl1 vs d_ovl2 (own buffers: it runs beside the SPF sweep)
   cplx* d_ovl1 = nullptr;
+  std::map<std::tuple<int, int, int>, cplx*> ovl_pool;   // shared overlap-chain buffers (state, chain, parity)
   cplx* d_ovl2 = nullptr;
   OvlPlan pk_norm;     // packet norms of d_in (mixtures with dissipation)
   OvlPlan auto_plan;   // d_y0 vs d_y (o12), d_y norm (o22)
@@ -702,13 +704,15 @@ void load_setup(Ctx& c, const mctdh_setup_t* s) {
   c.int_par1 = (int)s->int_par1;
   c.reginv_cold = s->reginv_cold != 0;
   c.precision = (int)s->precision;
-  if (c.precision < 0 || c.precision > 5) throw StatusError(MCTDH_EARG, "precision must be 0 .. 5");
+  if (c.precision < 0 || c.precision > 6) throw StatusError(MCTDH_EARG, "precision must be 0 .. 6");
   // precision 3: the products of precision 1 with FP32-accumulated contractions;
   // 4: FP32 mean-field and A-derivative products, compensated H_B products;
-  // 5: compensated mean-field and A-derivative products, FP32 H_B products
+  // 5: compensated mean-field and A-derivative products, FP32 H_B products;
+  // 6: precision 1 with FP32-accumulated mean-field contractions (densities compensated)
   c.hole_prec = c.precision == 3 ? 1 : (c.precision ? 2 : 0);
-  c.hb_prec = c.precision == 4 ? 2 : (c.precision == 5 ? 1 : (c.precision == 3 ? 1 : c.precision));
-  if (c.precision == 3 || c.precision == 4) c.precision = 1;
+  c.mf_hole_prec = (c.precision == 6) ? 1 : c.hole_prec;
+  c.hb_prec = c.precision == 4 ? 2 : (c.precision == 5 || c.precision == 3 || c.precision == 6 ? 1 : c.precision);
+  if (c.precision == 3 || c.precision == 4 || c.precision == 6) c.precision = 1;
   if (c.precision == 5) c.precision = 2;
   if (!c.modes_gwp.empty()) {
     // Gaussian widths GWPa(maxdof, ns00max, nmodgwp) (psidef: GWPa, init_calc.f90:1020-1068)
@@ -903,7 +907,7 @@ const cplx* plan_s_weighted(Ctx& c, int s, int skip) {
 // ---------------------------------------------------------------------------
 void plan_gwp_derivs(Ctx& c);
 
-void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only = false);
+void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only = false, bool shared = true);
 void run_ovl(Ctx& c, OvlPlan& P);
 
 // type-1 mean-field contribution: contraction of L_im(A) with the right chain on AuxA
@@ -999,7 +1003,7 @@ void plan_packets(Ctx& c, std::vector<std::vector<SumSrc>>& srcs, std::vector<st
     b.prec = c.precision;
     b.finalize(c.ar);
   }
-  c.aux_holes.prec = c.hole_prec;
+  c.aux_holes.prec = c.mf_hole_prec;
   c.aux_holes.finalize(c.ar);
   std::map<std::pair<int, int>, int> tg;
   for (const AuxRef& r : arefs) {
@@ -1401,7 +1405,7 @@ void plan_eom(Ctx& c) {
   }
   c.gprods.prec = c.precision;
   c.gprods.finalize(c.ar);
-  c.holes.prec = c.hole_prec;
+  c.holes.prec = c.mf_hole_prec;
   c.holes.finalize(c.ar);
   // density matrices: compensated split FP32 (~1e-13 relative) in the split modes
   c.rho_holes.prec = c.hole_prec;
@@ -1709,7 +1713,7 @@ void plan_hb(Ctx& c) {
 // products of the chains in compensated split FP32 (~1e-13 relative); used for
 // the step-error norm DeltaPsi of split-precision contexts, where 1 - Re<1|2>/..
 // is of order eps_int^2 / 2 >> 1e-13.  Norms and C(t) keep prec 0.
-void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only) {
+void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only, bool shared) {
   const int f = c.nmodes;
   P.npk = c.npk;
   P.d_result = c.ar.calloc_c(3 * c.npk);
@@ -1790,15 +1794,23 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only) 
     cplx* cur[3] = {a1, a2, a2};
     int curfmt[3] = {TF_C64, TF_C64, TF_C64};
     const int cfmt = prec ? TF_SPLIT : TF_C64;
-    // each chain alternates between two buffers (depth i reads i - 1's output)
+    // each chain alternates between two buffers (depth i reads i - 1's output);
+    // plans run on the context stream share them (c.ovl_pool: one plan runs at a
+    // time), the CMF2 error overlap, which runs beside other work, has its own
     cplx* pp[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    if (shared)
+      for (int q = 0; q < 3; ++q)
+        for (int par = 0; par < 2; ++par) pp[q][par] = c.ovl_pool[std::make_tuple(s, q, par)];
     for (size_t i = 0; i < order.size(); ++i) {
       const int m = order[i];
       const int n = sh[m];
       cplx* mats[3] = {S[m][s].s11, S[m][s].s22, S[m][s].s12};
       for (int q = 0; q < (norm_only ? 1 : 3); ++q) {
         cplx*& buf = pp[q][i & 1];
-        if (!buf) buf = c.ar.calloc_c(N);
+        if (!buf) {
+          buf = c.ar.calloc_c(N);
+          if (shared) c.ovl_pool[std::make_tuple(s, q, (int)(i & 1))] = buf;
+        }
         cplx* out = buf;
         P.chain[i + 1].add(cur[q], out, mats[q], n, 0, sh, m, n, mkc(1, 0), 0, curfmt[q], cfmt);
         cur[q] = out;
@@ -3663,7 +3675,7 @@ Ctx* create(const mctdh_setup_t* s, const MemberBufs* mb = nullptr) {
       plan_hb(*c);
       c->d_ovl1 = c->ar.calloc_c(c->ntot);
       c->d_ovl2 = c->ar.calloc_c(c->ntot);
-      plan_ovl(*c, c->cmf_ovl, c->d_ovl1, c->d_ovl2, (c->precision && c->eps_int >= 1e-5) ? 2 : 0);
+      plan_ovl(*c, c->cmf_ovl, c->d_ovl1, c->d_ovl2, (c->precision && c->eps_int >= 1e-5) ? 2 : 0, false, false);
     }
     // the compensated products of DeltaPsi (~1e-13) resolve 1 - Re<1|2>/.. ~ eps_int^2 / 2
     // only for loose tolerances; tight ones keep FP64
@@ -3901,7 +3913,9 @@ Ens* ens_create(const mctdh_setup_t* setups, int n) {
         E->der = c->der;
         E->min_stepsize = c->min_stepsize;
         E->writetime = c->writetime;
-      } else if (c->precision != E->precision || c->der.x != E->der.x || c->der.y != E->der.y) {
+      } else if (c->precision != E->precision || c->hole_prec != E->m[0]->hole_prec ||
+                 c->mf_hole_prec != E->m[0]->mf_hole_prec || c->hb_prec != E->m[0]->hb_prec ||
+                 c->der.x != E->der.x || c->der.y != E->der.y) {
         throw StatusError(MCTDH_EARG, "ensemble members must share precision and der_factor");
       }
       // merge the EOM plan
@@ -5181,6 +5195,26 @@ int64_t mctdh_ens_tuning(mctdh_ens_t* ens, int64_t* tiles_per_block, int64_t* bl
   if (eom_ms) *eom_ms = E.tune_ms;
   if (default_eom_ms) *default_eom_ms = E.tune_default_ms;
   if (candidates) *candidates = E.tune_candidates;
+  return MCTDH_OK;
+}
+
+int64_t mctdh_ens_eom_cost(mctdh_ens_t* ens, double* flops, double* bytes) {
+  if (!ens) return MCTDH_EARG;
+  const Ens& E = *ens->e;
+  double fl = 0.0, by = 0.0;
+  for (const auto* v : {&E.chains, &E.chains_full})
+    for (const ProdBatch& b : *v) {
+      fl += b.flops;
+      by += b.bytes;
+    }
+  fl += E.gprods.flops;
+  by += E.gprods.bytes;
+  for (const HoleBatch* hb : {&E.rho_holes, &E.holes}) {
+    fl += hb->flops;
+    by += hb->bytes;
+  }
+  if (flops) *flops = fl;
+  if (bytes) *bytes = by;
   return MCTDH_OK;
 }
 

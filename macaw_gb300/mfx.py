@@ -108,14 +108,58 @@ def build_dataset(t0, h, s0, sh) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
     return np.concatenate(Xs), np.concatenate(Rs), np.concatenate(ks)
 
 
+def variant_states(model, nvar, seed=0, shift=0.3):
+    """`nvar` seeded variants of the model's initial wavefunction for training
+    data: variant 0 is the model's own initial state; in the others the initial
+    Gaussian of every DVR DOF is displaced by up to +-shift in position and in
+    momentum (uniform, in the DOF's coordinate units).  Returns [(A, psi)]."""
+    from .model import initial_wavefunction
+    saved = dict(model.init_spf)
+    rng = np.random.default_rng(seed)
+    out = []
+    try:
+        for v in range(nvar):
+            model.init_spf.clear()
+            model.init_spf.update(saved)
+            if v > 0:
+                for d in range(model.ndof):
+                    kind, par = saved.get(d, ("gauss", (0.0, 0.0, 0.707107)))
+                    if kind != "gauss":
+                        continue
+                    x0, p0, dx = par
+                    model.init_spf[d] = ("gauss", (x0 + rng.uniform(-shift, shift),
+                                                   p0 + rng.uniform(-shift, shift), dx))
+            out.append(initial_wavefunction(model))
+    finally:
+        model.init_spf.clear()
+        model.init_spf.update(saved)
+    return out
+
+
+def build_datasets(records):
+    """build_dataset over several recorded runs [(t0, h, s0, sh)]: rows
+    concatenated in run order, step indices offset so that every run's steps
+    follow the previous run's (the last run is then the held-back part of train)."""
+    Xs, Rs, ks = [], [], []
+    off = 0
+    for rec in records:
+        X, R, k = build_dataset(*rec)
+        Xs.append(X)
+        Rs.append(R)
+        ks.append(k + off)
+        off += int(k.max()) + 1
+    return np.concatenate(Xs), np.concatenate(Rs), np.concatenate(ks)
+
+
 def train(X, R, steps=None, seed=1, epochs=20, batch=4096, lr=1e-3, widths=WIDTHS, val_frac=0.2):
     """Train the GPU network; returns (net, fscale, tscale, loss).  Input columns
     are scaled to an RMS of 1/4 (keeping tanh near its linear range), targets to 1.
 
-    The last `val_frac` of the steps (or of the rows, without `steps`) are held
-    back.  On them the polynomial order (1-4) is chosen per prediction time
-    (``net.orders``: the network learns the residual of that polynomial), and
-    per output column the network's correction is shrunk by the factor
+    The polynomial order (1-4) is chosen per prediction time on all rows
+    (``net.orders``: the network learns the residual of that polynomial).  The
+    last `val_frac` of the steps (or of the rows, without `steps`) are held back
+    from the fit; on them, per output column the network's correction is shrunk
+    by the factor
     beta in [0, 1] that minimises the residual on them (folded into tscale), and
     switched off (beta = 0) unless it removes at least 10 % of that residual, so
     a correction that does not generalise is not applied."""
@@ -129,12 +173,11 @@ def train(X, R, steps=None, seed=1, epochs=20, batch=4096, lr=1e-3, widths=WIDTH
         fit[:n_fit] = True
         val = ~fit
     # the polynomial order per prediction time (step start, half step) with the
-    # smallest held-out residual; the network learns the residual of that order
-    rows = val if val.any() else fit
+    # smallest residual over all rows; the network learns the residual of that order
     orders = []
     for tau in range(2):
         cols = slice(2 * tau, 2 * tau + 2)
-        rms = [np.mean(poly_residual(X[rows], R[rows], o)[:, cols] ** 2) for o in range(1, NHIST)]
+        rms = [np.mean(poly_residual(X, R, o)[:, cols] ** 2) for o in range(1, NHIST)]
         orders.append(1 + int(np.argmin(rms)))
     Ro = order_residual(X, R, orders)
     fscale = 4.0 * np.sqrt(np.mean(X[fit] ** 2, axis=0))
