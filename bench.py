@@ -841,14 +841,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--acc-fs", type=float, default=200.0, help="accuracy: propagated interval in fs")
-    ap.add_argument("--acc-precisions", default="1,4", help="accuracy: split arms compared with FP64")
+    ap.add_argument("--acc-precisions", default="1,5", help="accuracy: split arms compared with FP64")
     ap.add_argument("--headline", default="mfx", choices=["mfx", "split"],
                     help="qvc12: the arm the line's value is: split precision with (mfx) or without the extrapolator")
     ap.add_argument("--mfx-variants", type=int, default=3,
                     help="extrapolator: seeded initial-state variants recorded besides the start state")
     ap.add_argument("--pre-fs", type=float, default=0.3, help="qvc24: untimed FP64 propagation before the steps")
-    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2, 3, 4, 5, 6],
-                    help="arm timed against the FP64 path: 1 split FP32, 2 compensated split FP32")
+    ap.add_argument("--precision", type=int, default=5, choices=[0, 1, 2, 3, 4, 5, 6],
+                    help="arm timed against the FP64 path (mode of mctdh_setup_t.precision; 5: compensated "
+                         "mean-field products and contractions, FP32 Lanczos H_B products)")
     ap.add_argument("--workload", default="qvc12",
                     choices=["qvc12", "qvc12n", "qvc24", "ensemble", "lvc5", "gmctdh16", "lvc5mix", "accuracy"],
                     help="qvc12: the CMF2 benchmark line; ensemble: the batched ragged-ensemble measurement; "

@@ -3206,9 +3206,10 @@ CmfState& cmf_state(Ctx& c) {
 // history holds the snapshots computed at the half steps of the last accepted
 // CMF2 steps.  With a trained network attached and a full history, the mean
 // fields at a step start (the first evaluation of cmf2_base.f90:78-87) come from
-// the quartic extrapolation of that history plus the network's residual instead
-// of an EOM evaluation (h1mode is still computed: the A-vector propagation uses
-// only h1mode, the mean fields only drive the first SPF half step).  The half-step
+// the polynomial extrapolation of that history plus the network's residual
+// instead of the chains and contractions of an EOM evaluation; h1mode (all the
+// A-vector propagation uses) and the density matrices (one contraction of A per
+// mode and state) are still computed, so rho^-1 sees no prediction error.  The half-step
 // mean fields (:122-130) are always computed; the extrapolation's prediction for
 // the half step is checked against them, and a step whose mismatch exceeds the
 // tolerance is redone with the plain scheme.  One mean-field evaluation per
@@ -3250,16 +3251,16 @@ MfxState& mfx_state(Ctx& c) {
   const int f = c.nmodes;
   for (int m : c.modes_dvr) {
     for (int s = 0; s < c.nstates; ++s) {
-      M->segs_h.push_back(SnapSeg{c.rho[m][s], off});
+      M->segs_h.push_back(SnapSeg{c.rho[m][s], off, 1, 0});
       off += (long long)c.m_of(m, s) * c.m_of(m, s);
     }
     if (!c.multiset[m]) {
-      M->segs_h.push_back(SnapSeg{c.rho_ave[m], off});
+      M->segs_h.push_back(SnapSeg{c.rho_ave[m], off, 1, 0});
       off += (long long)c.m_of(m, 0) * c.m_of(m, 0);
     }
     for (int k = 0; k < c.noper[m]; ++k) {
       if (c.is_identity[m + f * k] || !c.ham_op[m][k]) continue;
-      M->segs_h.push_back(SnapSeg{c.mf[m][k], off});
+      M->segs_h.push_back(SnapSeg{c.mf[m][k], off, 0, 0});
       off += (long long)c.m_of(m, c.oper[m][k][0]) * c.m_of(m, c.oper[m][k][1]);
     }
   }
@@ -3526,7 +3527,13 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
     if (predicted) {
       copy_dev(c, M->backup, c.d_y, c.ntot);
       mfx_predict(c, *M, t, t + 0.5 * hdid);
-      launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred0, M->E, 1, c.st);
+      // the density matrices are contracted exactly (their regularised inverse
+      // would magnify a prediction error in the weakly occupied directions by up to
+      // 1 / eps_rho^2); the mean fields come from the prediction
+      copy_dev(c, c.d_in, c.d_y, c.naconftot);
+      run_hole(c, c.rho_holes);
+      run_red(c, c.red);
+      launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred0, M->E, 2, c.st);
       c.count();
       h1_only(c, c.d_y);
     } else {

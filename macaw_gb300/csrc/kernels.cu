@@ -1940,7 +1940,8 @@ void launch_lan_normalize(cplx* out, const cplx* in, const cplx* nrm2, double* b
 
 // ---------------------------------------------------------------------------
 // Mean-field snapshots for the learned extrapolator: all density matrices and
-// mean fields of the grid modes gathered into one complex vector (and back).
+// mean fields of the grid modes gathered into one complex vector (and back;
+// scatter 2: the mean fields only).
 // ---------------------------------------------------------------------------
 __global__ void snap_gather_kernel(const SnapSeg* __restrict__ segs, int nseg, cplx* __restrict__ flat, long long E,
                                    int scatter) {
@@ -1952,6 +1953,7 @@ __global__ void snap_gather_kernel(const SnapSeg* __restrict__ segs, int nseg, c
     if (segs[mid].offset <= i) lo = mid; else hi = mid - 1;
   }
   cplx* p = segs[lo].ptr + (i - segs[lo].offset);
+  if (scatter == 2 && segs[lo].density) return;
   if (scatter) *p = flat[i]; else flat[i] = *p;
 }
 void launch_snap(const SnapSeg* segs, int nseg, cplx* flat, long long E, int scatter, cudaStream_t st) {

@@ -200,6 +200,8 @@ void launch_density_gwp(const DensGwpArgs& a, cudaStream_t st);
 struct SnapSeg {
   cplx* ptr;               // matrix storage
   long long offset;        // first index in the flat snapshot
+  int density;             // 1: a density matrix, 0: a mean field
+  int pad;
 };
 // Learned mean-field extrapolation: five step-start snapshots, 20 network inputs
 // (Newton increments of orders 1-4 at the half step and the step end, Re/Im, and

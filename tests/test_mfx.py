@@ -9,8 +9,9 @@ prediction.  Training data are plain CMF2 runs of four seeded variants of the
 initial state (displaced Gaussians); the model's own initial state is held out.
 What these tests pin down (small QVC model, CMF2 tolerance 1e-5):
 * on the held-out run, the learned extrapolator (polynomial order chosen per
-  prediction time on the training runs, plus the gated network) is within 5 %
-  of the better of the quadratic and quartic extrapolations;
+  prediction time on the training runs, plus the gated network) leaves at least
+  15 % less RMS residual over its four outputs than the better of the quadratic
+  and quartic extrapolations, and no output more than 15 % above it;
 * the assisted propagation of the held-out state needs fewer EOM evaluations per
   simulated fs than plain CMF2 (one mean-field evaluation per step instead of
   two) and stays within 1e-6 of it in C(t) and within 1e-5 in the populations.
@@ -68,7 +69,9 @@ def test_extrapolator_held_out_variant(trained):
     quad = np.sqrt(np.mean(mfx.poly_residual(Xh, Rh, 2) ** 2, axis=0))
     print("orders", net.orders, "held-out RMS residual (units of S): quadratic", quad,
           "quartic", base, "learned", left)
-    assert np.all(left <= 1.05 * np.minimum(base, quad)), (quad, base, left)
+    best = np.minimum(base, quad)
+    assert np.sqrt(np.mean(left ** 2)) <= 0.85 * np.sqrt(np.mean(best ** 2)), (quad, base, left)
+    assert np.all(left <= 1.15 * best), (quad, base, left)
 
 
 def test_assisted_cmf2_fewer_evaluations(trained):
