@@ -3545,10 +3545,22 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
     const bool reginv_first = !predicted && !overlap;
     bool first = true;
     bool accepted_predicted = false;
+    bool redo_plain = false;
     while (true) {
       ++*tries;
       if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
-      const double error = cmf2_attempt(c, t, hdid, first, first && reginv_first);
+      double error = 0.0;
+      try {
+        error = cmf2_attempt(c, t, hdid, first, first && reginv_first);
+      } catch (const StatusError& e) {
+        if (!(predicted && first) || e.code != MCTDH_ENONFINITE) throw;
+        // an extrapolated step start that made the SPF integration non-finite:
+        // let both streams drain, then redo the step with the plain scheme
+        CK(cudaStreamSynchronize(c.st));
+        if (c.st2) CK(cudaStreamSynchronize(c.st2));
+        redo_plain = true;
+        break;
+      }
       const bool was_predicted = predicted && first;
       first = false;
       if (M && M->log.size() < 5 * 100000) {
@@ -3568,6 +3580,13 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       *hdid_out = hdid;
       *hnext_out = hn;
       break;
+    }
+    if (redo_plain) {
+      ++M->fallbacks;
+      copy_dev(c, c.d_y, M->backup, c.ntot);
+      predicted = false;
+      hdid = htry;
+      continue;
     }
     if (accepted_predicted) {
       // the computed half-step mean fields against the extrapolation's prediction

@@ -1991,8 +1991,22 @@ __global__ void __launch_bounds__(1024) mfx_scale_kernel(MfxHist hz, MfxCoef c, 
   if (threadIdx.x == 0) S[0] = fmax(sqrt(red[0] / (double)(E > 0 ? E : 1)), 1e-300);
 }
 
+// The entry's own scale: |inc_1| + |inc_2| at the step end plus 1e-12 S.
+__device__ __forceinline__ double mfx_entry_scale(const cplx* z, const MfxCoef& c, double S) {
+  cplx v1 = mkc(0, 0), v2 = mkc(0, 0);
+#pragma unroll
+  for (int j = 0; j < MFX_NHIST; ++j) {
+    v1.x += c.inc[1][0][j] * z[j].x;
+    v1.y += c.inc[1][0][j] * z[j].y;
+    v2.x += c.inc[1][1][j] * z[j].x;
+    v2.y += c.inc[1][1][j] * z[j].y;
+  }
+  return sqrt(cabs2(v1)) + sqrt(cabs2(v2)) + 1e-12 * S + 1e-300;
+}
+
 // Network inputs per entry: Re/Im of inc_1..inc_4 at the half step and the step
-// end divided by S, then the step-length ratios; each divided by its column scale.
+// end divided by the entry's scale, then the step-length ratios; each divided by
+// its column scale.
 __global__ void mfx_features_kernel(MfxHist hz, MfxCoef c, const double* __restrict__ S, float* __restrict__ X,
                                     long long E) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2000,7 +2014,7 @@ __global__ void mfx_features_kernel(MfxHist hz, MfxCoef c, const double* __restr
   cplx z[MFX_NHIST];
 #pragma unroll
   for (int j = 0; j < MFX_NHIST; ++j) z[j] = hz.z[j][i];
-  const double q = 1.0 / S[0];
+  const double q = 1.0 / mfx_entry_scale(z, c, S[0]);
   float* x = X + (long long)MFX_NFEAT * i;
   int col = 0;
 #pragma unroll
@@ -2023,7 +2037,8 @@ __global__ void mfx_features_kernel(MfxHist hz, MfxCoef c, const double* __restr
   for (int r = 0; r < MFX_NHIST - 1; ++r, ++col) x[col] = (float)(c.ratio[r] / c.fscale[col]);
 }
 
-// z(tau) = quartic extrapolation + S * tscale * y at the half step and the step end
+// z(tau) = polynomial extrapolation + s * tscale * y at the half step and the step
+// end (s the entry's scale)
 __global__ void mfx_combine_kernel(MfxHist hz, MfxCoef c, const float* __restrict__ Y, const double* __restrict__ S,
                                    cplx* __restrict__ half, cplx* __restrict__ full, long long E) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2032,7 +2047,7 @@ __global__ void mfx_combine_kernel(MfxHist hz, MfxCoef c, const float* __restric
 #pragma unroll
   for (int j = 0; j < MFX_NHIST; ++j) z[j] = hz.z[j][i];
   const float* y = Y + (long long)MFX_NOUT * i;
-  const double s = S[0];
+  const double s = mfx_entry_scale(z, c, S[0]);
   cplx out[2];
 #pragma unroll
   for (int tau = 0; tau < 2; ++tau) {

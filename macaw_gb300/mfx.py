@@ -12,12 +12,16 @@ tau_0 = t_k and, for the check against the computed half-step fields, at its
 half step tau_1 = t_k + h_k/2.  P_o(tau) is the Lagrange polynomial through the
 last o+1 history values and inc_o = P_o - P_{o-1} (P_0 = z_4) its Newton
 increment; the extrapolation without the network is P_4 (quartic).  The network
-sees, per entry, Re/Im of inc_1..inc_4 at tau_0 and tau_1 divided by S (the RMS
-over all entries of |inc_1| at tau_1), and the spacing ratios (s_1-s_0, s_2-s_1,
+sees, per entry, Re/Im of inc_1..inc_4 at tau_0 and tau_1 divided by the
+entry's own scale s = |inc_1(tau_1)| + |inc_2(tau_1)| + 1e-12 S (S the RMS over
+all entries of |inc_1(tau_1)|), and the spacing ratios (s_1-s_0, s_2-s_1,
 s_3-s_2, tau_1-s_4) / (s_4-s_3); every input column is divided by its scale
 ``fscale``.  It predicts the residual z(tau) - P_4(tau) at tau_0 and tau_1 in
-units of S times the output column scale ``tscale``.  The device builds the same
-inputs (mfx_features_kernel).
+units of s times the output column scale ``tscale``.  The per-entry scale keeps
+every correction proportional to the entry's own variation: the mean fields of
+weakly occupied SPFs are small, and the regularised inverse of rho in the SPF
+equations magnifies any error of theirs.  The device builds the same inputs
+(mfx_features_kernel).
 """
 from __future__ import annotations
 
@@ -65,11 +69,13 @@ def coefficients(ts, taus):
 
 
 def features(Z, ts, taus):
-    """Unscaled inputs (E, 20), the quartic extrapolations (2, E) and S for the
-    history Z (5, E) at times ts and the prediction times taus."""
+    """Unscaled inputs (E, 20), the quartic extrapolations (2, E) and the
+    per-entry scales s (E) for the history Z (5, E) at times ts and the
+    prediction times taus."""
     inc, base, ratio = coefficients(ts, taus)
     incs = np.einsum("toj,je->toe", inc, Z)          # (2, 4, E)
-    S = max(float(np.sqrt(np.mean(np.abs(incs[1, 0]) ** 2))), 1e-300)
+    Sg = max(float(np.sqrt(np.mean(np.abs(incs[1, 0]) ** 2))), 1e-300)
+    S = np.abs(incs[1, 0]) + np.abs(incs[1, 1]) + 1e-12 * Sg + 1e-300
     E = Z.shape[1]
     X = np.empty((E, NFEAT))
     col = 0
@@ -88,7 +94,7 @@ def build_dataset(t0, h, s0, sh) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
     half-step snapshots of steps k-5 .. k-1, the targets the snapshot at the step
     start t_k and at its half step.  Returns the unscaled inputs X, the residual
     targets R of the quartic extrapolation (Re/Im at the step start, Re/Im at the
-    half step, in units of S) and the step index of every row."""
+    half step, in units of each entry's scale s) and the step index of every row."""
     Xs, Rs, ks = [], [], []
     for k in range(NHIST, len(t0)):
         ok = all(np.isclose(t0[j + 1], t0[j] + h[j], rtol=0, atol=1e-9 * max(1.0, abs(t0[j])))

@@ -120,7 +120,7 @@ def test_device_prediction_matches_host():
             taus = (t0[kk], t0[kk] + 0.5 * h[kk])
             p0, p1 = core.mfx_predict(Z, ts, *taus)
             Xh, Q, S = mfx.features(Z, ts, taus)
-            P = mfx.predict(net, fscale, ts_scale, Xh) * S
+            P = mfx.predict(net, fscale, ts_scale, Xh) * S[:, None]
             ref0 = Q[0] + P[:, 0] + 1j * P[:, 1]
             ref1 = Q[1] + P[:, 2] + 1j * P[:, 3]
             scale = np.abs(Z).max()

@@ -46,6 +46,8 @@ def test_ratios_and_scale():
     np.testing.assert_allclose(first[16:], [(s[j - 4] - s[j - 5]) / d, (s[j - 3] - s[j - 4]) / d,
                                             (s[j - 2] - s[j - 3]) / d, (t0[j] + 0.5 * h[j] - s[j - 1]) / d],
                                rtol=1e-12)
-    # first-order step-end increment has unit RMS over the entries
+    # every entry's scale is |inc_1| + |inc_2| at the step end (plus a floor of
+    # 1e-12 of the RMS of inc_1): the scaled pair sums to one
     rows = X[k == k.min()]
-    np.testing.assert_allclose(np.sqrt(np.mean(rows[:, 8] ** 2 + rows[:, 9] ** 2)), 1.0, rtol=1e-12)
+    pair = np.hypot(rows[:, 8], rows[:, 9]) + np.hypot(rows[:, 10], rows[:, 11])
+    np.testing.assert_allclose(pair, 1.0, rtol=1e-9)
