@@ -740,11 +740,12 @@ def run_ensemble(args):
     e2e_s = time.perf_counter() - w0
     e2e_fs = float(np.sum(t2 - t)) * AU2FS
     nbytes = int(sum(16 * (m.naconftot + m.dimpsi) for m in models))
-    # the same members one context at a time (sequential), same interval
+    # a sample of the members (every len/nseq-th, so small and large ones alike)
+    # one context at a time (sequential), same interval
     seq_ms = 0.0
     nseq = min(len(models), args.seq_members)
     seq_fs = 0.0
-    for i in range(nseq):
+    for i in np.linspace(0, len(models) - 1, nseq).round().astype(int):
         core = GpuCore(models[i], precision=args.precision)
         A, psi = starts[i]
         core.set_state(A, psi, as_start=True)
@@ -776,6 +777,7 @@ def run_ensemble(args):
                     "d2h_bytes_per_step": nbytes,
                     "what": "every member's state uploaded, the next interval, every state downloaded"},
             "sequential": {"members": nseq, "member_fs_per_s": seq_fs / (seq_ms * 1e-3) if seq_ms else None,
+                           "sample": "evenly spaced member indices",
                            "timing": "host wall clock around each member's propagate call"},
             "config": {"workload": "ragged LVC ensemble", "interval_fs": args.ens_fs, "max_conf": args.max_conf,
                        "coefficients_total": int(sum(sizes)), "largest_member": int(max(sizes)),

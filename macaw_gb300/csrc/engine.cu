@@ -3533,6 +3533,35 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       copy_dev(c, c.d_in, c.d_y, c.naconftot);
       run_hole(c, c.rho_holes);
       run_red(c, c.red);
+      {
+        static int dbg = -1;
+        if (dbg < 0) { const char* e = getenv("MACAW_GB300_MFX_DEBUG"); dbg = e ? atoi(e) : 0; }
+        if (dbg) {
+          operators_and_mf(c, c.d_y, false);
+          snap_gather(c, *M, M->now);
+          std::vector<cplx> ex(M->E), pr(M->E);
+          CK(cudaMemcpyAsync(ex.data(), M->now, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
+          CK(cudaMemcpyAsync(pr.data(), M->pred0, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
+          CK(cudaStreamSynchronize(c.st));
+          double n2 = 0, d2 = 0, mx = 0; long long imx = -1; int segmx = -1;
+          for (long long i = 0; i < M->E; ++i) {
+            int lo = 0;
+            for (int q = 0; q < (int)M->segs_h.size(); ++q) if (M->segs_h[q].offset <= i) lo = q;
+            if (M->segs_h[lo].density) continue;
+            const double dx = ex[i].x - pr[i].x, dy = ex[i].y - pr[i].y;
+            n2 += ex[i].x * ex[i].x + ex[i].y * ex[i].y;
+            d2 += dx * dx + dy * dy;
+            const double a = sqrt(dx * dx + dy * dy);
+            if (a > mx) { mx = a; imx = i; segmx = lo; }
+          }
+          fprintf(stderr, "MFXDBG t=%.6e h=%.4e rel=%.3e maxabs=%.3e at %lld seg %d |ex|=%.3e\n", t, hdid,
+                  sqrt(d2 / (n2 > 0 ? n2 : 1)), mx, imx, segmx, imx >= 0 ? sqrt(ex[imx].x * ex[imx].x + ex[imx].y * ex[imx].y) : 0.0);
+          if (dbg == 1) copy_dev(c, M->pred0, M->now, M->E);
+          copy_dev(c, c.d_in, c.d_y, c.naconftot);
+          run_hole(c, c.rho_holes);
+          run_red(c, c.red);
+        }
+      }
       launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred0, M->E, 2, c.st);
       c.count();
       h1_only(c, c.d_y);
@@ -3553,8 +3582,9 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       try {
         error = cmf2_attempt(c, t, hdid, first, first && reginv_first);
       } catch (const StatusError& e) {
-        if (!(predicted && first) || e.code != MCTDH_ENONFINITE) throw;
-        // an extrapolated step start that made the SPF integration non-finite:
+        if (!(predicted && first) || (e.code != MCTDH_ENONFINITE && e.code != MCTDH_EEIG)) throw;
+        // an extrapolated step start that made the SPF integration non-finite (or
+        // its overlaps indefinite):
         // let both streams drain, then redo the step with the plain scheme
         CK(cudaStreamSynchronize(c.st));
         if (c.st2) CK(cudaStreamSynchronize(c.st2));
