@@ -318,6 +318,10 @@ int64_t mctdh_mfx_attach(mctdh_ctx_t *ctx, mctdh_mlp_t *mlp, const double *fscal
  * history snapshots that the network's residual is added to, at the step start
  * and at the half step (chosen at training on held-out steps). */
 int64_t mctdh_mfx_orders(mctdh_ctx_t *ctx, int64_t order_start, int64_t order_half);
+/* gate: extrapolate a step start only when the first attempt of the previous
+ * step had a CMF2 error (in units of the tolerance) below `gate` (default: no
+ * limit), i.e. while the step control has room for the extrapolation's error. */
+int64_t mctdh_mfx_gate(mctdh_ctx_t *ctx, double gate);
 /* predict: run the attached extrapolator on a given history (5 x E complex
  * snapshots, oldest first, at times ts[5]) for the times tau0 (a step start) and
  * tau1 (its half step); writes the two predicted snapshots (E complex each) and

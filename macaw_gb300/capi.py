@@ -119,6 +119,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_mfx_stats.argtypes = [vp, I64P, I64P, I64P, DP]
     lib.mctdh_mfx_predict.argtypes = [vp, DP, DP, C.c_double, C.c_double, DP, DP]
     lib.mctdh_mfx_orders.argtypes = [vp, C.c_int64, C.c_int64]
+    lib.mctdh_mfx_gate.argtypes = [vp, C.c_double]
     lib.mctdh_mfx_log.argtypes = [vp, C.c_int64, DP, I64P]
     lib.mctdh_ens_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
     lib.mctdh_ens_destroy.argtypes = [vp]
@@ -138,7 +139,7 @@ def load_library() -> C.CDLL:
                  "mctdh_tensor_core_status", "mctdh_tensor_core_config"):
         getattr(lib, name).restype = C.c_int64
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
-                 "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders"):
+                 "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders", "mctdh_mfx_gate"):
         getattr(lib, name).restype = C.c_int64
     lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
                                                  C.c_int64, C.c_void_p]
@@ -168,7 +169,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
-            "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders",
+            "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders", "mctdh_mfx_gate",
             "mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
             "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
             "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_last_error"]
@@ -582,6 +583,10 @@ class GpuCore:
         self._check(self.lib.mctdh_mfx_predict(self.h, Hs.ctypes.data_as(DP), T.ctypes.data_as(DP), tau0, tau1,
                                                p0.ctypes.data_as(DP), p1.ctypes.data_as(DP)))
         return p0, p1
+
+    def mfx_gate(self, gate: float):
+        """Extrapolate only after steps whose first attempt had error / tolerance < gate."""
+        self._check(self.lib.mctdh_mfx_gate(self.h, float(gate)))
 
     def mfx_log(self):
         """One row per CMF2 attempt: t, h, error / eps_int, extrapolated, step-end mismatch."""

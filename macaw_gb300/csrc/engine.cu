@@ -3235,6 +3235,8 @@ struct MfxState {
   std::vector<cplx> rec_s0, rec_sh;
   long long mlp_steps = 0, fallbacks = 0, rejected = 0;
   double last_rel = -1.0;          // relative step-end mismatch of the last validated prediction
+  double gate = 1e300;             // extrapolate only after a step whose first attempt had error < gate
+  double last_first_err = 0.0;     // error / eps_int of the first attempt of the last step
   std::vector<double> log;         // per CMF2 attempt: t, h, error, extrapolated (0/1), step-end mismatch
   HoleBatch dh;                     // ||now - pred1||^2 and ||now||^2
   RedBatch dr;
@@ -3521,7 +3523,7 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
   // Step start: the operators and mean fields of d_y (cmf2_base.f90:78-87), or,
   // with an attached extrapolator and a full half-step history, h1mode computed
   // and rho / mean fields predicted (grid-mode models only).
-  bool predicted = M && M->mlp && M->nhist == MFX_NHIST && c.modes_gwp.empty();
+  bool predicted = M && M->mlp && M->nhist == MFX_NHIST && c.modes_gwp.empty() && M->last_first_err < M->gate;
   double hdid = htry;
   for (;;) {
     if (predicted) {
@@ -3533,35 +3535,6 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       copy_dev(c, c.d_in, c.d_y, c.naconftot);
       run_hole(c, c.rho_holes);
       run_red(c, c.red);
-      {
-        static int dbg = -1;
-        if (dbg < 0) { const char* e = getenv("MACAW_GB300_MFX_DEBUG"); dbg = e ? atoi(e) : 0; }
-        if (dbg) {
-          operators_and_mf(c, c.d_y, false);
-          snap_gather(c, *M, M->now);
-          std::vector<cplx> ex(M->E), pr(M->E);
-          CK(cudaMemcpyAsync(ex.data(), M->now, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
-          CK(cudaMemcpyAsync(pr.data(), M->pred0, sizeof(cplx) * M->E, cudaMemcpyDeviceToHost, c.st));
-          CK(cudaStreamSynchronize(c.st));
-          double n2 = 0, d2 = 0, mx = 0; long long imx = -1; int segmx = -1;
-          for (long long i = 0; i < M->E; ++i) {
-            int lo = 0;
-            for (int q = 0; q < (int)M->segs_h.size(); ++q) if (M->segs_h[q].offset <= i) lo = q;
-            if (M->segs_h[lo].density) continue;
-            const double dx = ex[i].x - pr[i].x, dy = ex[i].y - pr[i].y;
-            n2 += ex[i].x * ex[i].x + ex[i].y * ex[i].y;
-            d2 += dx * dx + dy * dy;
-            const double a = sqrt(dx * dx + dy * dy);
-            if (a > mx) { mx = a; imx = i; segmx = lo; }
-          }
-          fprintf(stderr, "MFXDBG t=%.6e h=%.4e rel=%.3e maxabs=%.3e at %lld seg %d |ex|=%.3e\n", t, hdid,
-                  sqrt(d2 / (n2 > 0 ? n2 : 1)), mx, imx, segmx, imx >= 0 ? sqrt(ex[imx].x * ex[imx].x + ex[imx].y * ex[imx].y) : 0.0);
-          if (dbg == 1) copy_dev(c, M->pred0, M->now, M->E);
-          copy_dev(c, c.d_in, c.d_y, c.naconftot);
-          run_hole(c, c.rho_holes);
-          run_red(c, c.red);
-        }
-      }
       launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred0, M->E, 2, c.st);
       c.count();
       h1_only(c, c.d_y);
@@ -3592,6 +3565,7 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
         break;
       }
       const bool was_predicted = predicted && first;
+      if (M && first) M->last_first_err = error;
       first = false;
       if (M && M->log.size() < 5 * 100000) {
         const double row[5] = {t, hdid, error, was_predicted ? 1.0 : 0.0, -1.0};
@@ -4915,6 +4889,12 @@ int64_t mctdh_mfx_orders(mctdh_ctx_t* ctx, int64_t order_start, int64_t order_ha
     M.order[0] = (int)order_start;
     M.order[1] = (int)order_half;
   });
+}
+
+int64_t mctdh_mfx_gate(mctdh_ctx_t* ctx, double gate) {
+  if (!ctx || !(gate > 0.0)) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] { mfx_state(*c).gate = gate; });
 }
 
 int64_t mctdh_mfx_predict(mctdh_ctx_t* ctx, const double* hist, const double* ts, double tau0, double tau1,
