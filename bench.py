@@ -39,6 +39,11 @@ WORKLOAD = "qvc12: 3-state QVC, 12 DOFs -> 6 modes of 20x20 HO DVR, 8 SPFs/mode/
 EPS_CMF = 1e-5
 PRE_FS = 1.0
 MFX_EPOCHS = 12
+# extrapolate a step start only after a step whose first attempt used less than
+# half of the CMF2 error tolerance: at the step control's operating point (error
+# ~1) the extrapolation's error shifts the CMF2 error estimate enough to cost
+# rejected attempts
+MFX_GATE = 0.5
 # ncu DRAM bytes per algorithmic byte of a kernel class in the benchmark regime
 # (one capture of the profile case), and what bounds each class there
 TRAFFIC_PER_ALG_BYTE = {"mode_product": 0.51}
@@ -304,6 +309,7 @@ def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mf
     if mfx_net is not None:
         # the extrapolator needs five accepted step starts of history
         core.mfx_attach(*mfx_net, tol=model.eps_int)
+        core.mfx_gate(MFX_GATE)
         warm = max(warm, 6)
     t, h = t0, h0
     for _ in range(warm):
@@ -608,6 +614,7 @@ def accuracy_arms(model, precisions, acc_fs, mfx_net=None, mfx_precision=1):
         core = GpuCore(model, precision=mfx_precision if prec == "mfx" else prec)
         if prec == "mfx":
             core.mfx_attach(*mfx_net, tol=model.eps_int)
+            core.mfx_gate(MFX_GATE)
         core.set_state(A0, psi0, as_start=True)
         t, h = 0.0, model.tout * model.eps_int
         rows = [core.observables(t)]
