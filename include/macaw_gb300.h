@@ -365,9 +365,12 @@ int64_t mctdh_ens_stream(mctdh_ens_t *ens, void **stream);
  * switched off, the first mctdh_ens_propagate times one merged EOM evaluation
  * for each candidate shape -- fibre tiles per contraction block (2, 4, 8, 16),
  * blocks per contraction (32, 64, 128) and, for split-precision members,
- * tensor-core or CUDA-core mode products -- and keeps the fastest.  mode 1 runs
+ * tensor-core or CUDA-core mode products -- and keeps the fastest; then, on that
+ * shape, persistent CTAs (2 or 4 contraction CTAs and twice as many mode-product
+ * CTAs per SM, each walking the batch's blocks) against one CTA per block.  mode 1 runs
  * it now on the current states, mode 0 keeps the planned shapes (an ensemble
- * whose members must repeat the arithmetic of single contexts bit for bit);
+ * whose members must repeat the arithmetic of single contexts bit for bit),
+ * mode 2 keeps them with persistent CTAs (the same arithmetic);
  * -7 once a propagation has fixed the shapes.  mctdh_ens_tuning reports the
  * chosen shape, its EOM time (ms) against the planned shape's, and the number of
  * candidates timed (0: not tuned).  Each attempt round of mctdh_ens_propagate
@@ -379,6 +382,9 @@ int64_t mctdh_ens_tuning(mctdh_ens_t *ens, int64_t *tiles_per_block, int64_t *bl
  * bytes (operands read once, results written once) of its mode products and
  * single-hole contractions, the roofline numerator of the EOM time. */
 int64_t mctdh_ens_eom_cost(mctdh_ens_t *ens, double *flops, double *bytes);
+/* Persistent CTAs chosen by the autotuner for the merged mode products and
+ * contractions (0: one CTA per block of the batch). */
+int64_t mctdh_ens_persistent(mctdh_ens_t *ens, int64_t *prod_ctas, int64_t *hole_ctas);
 const char *mctdh_ens_last_error(mctdh_ens_t *ens);
 
 /* Tensor-core kernels (no reference counterpart).  The FP32 mode products of the

@@ -94,6 +94,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_ens_autotune.argtypes = [vp, C.c_int64]
     lib.mctdh_ens_tuning.argtypes = [vp, I64P, I64P, I64P, DP, DP, I64P]
     lib.mctdh_ens_eom_cost.argtypes = [vp, DP, DP]
+    lib.mctdh_ens_persistent.argtypes = [vp, I64P, I64P]
     lib.mctdh_step.argtypes = [vp, C.c_int64, C.c_double, C.c_double, DP, DP, I64P]
     lib.mctdh_event_record.argtypes = [vp, C.c_int64]
     lib.mctdh_event_elapsed.argtypes = [vp, C.c_int64, C.c_int64, DP]
@@ -135,7 +136,7 @@ def load_library() -> C.CDLL:
     lib.mctdh_ens_last_error.restype = C.c_char_p
     for name in ("mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
                  "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
-                 "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_autotune", "mctdh_ens_tuning", "mctdh_ens_eom_cost",
+                 "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_autotune", "mctdh_ens_tuning", "mctdh_ens_eom_cost", "mctdh_ens_persistent",
                  "mctdh_tensor_core_status", "mctdh_tensor_core_config"):
         getattr(lib, name).restype = C.c_int64
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
@@ -166,6 +167,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_event_record", "mctdh_event_elapsed", "mctdh_profile", "mctdh_profile_read",
             "mctdh_counters", "mctdh_fp64_peak", "mctdh_density_matrix_noalloc", "mctdh_tensor_core_status",
             "mctdh_tensor_core_config", "mctdh_ens_autotune", "mctdh_ens_tuning", "mctdh_ens_eom_cost",
+            "mctdh_ens_persistent",
             "mctdh_mlp_create", "mctdh_mlp_destroy", "mctdh_mlp_nparams", "mctdh_mlp_set_params",
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
@@ -676,7 +678,9 @@ class Ensemble:
         if rc != 0:
             raise MctdhError(rc, self.lib.mctdh_ens_last_error(None).decode())
         self.h = h
-        if not autotune:
+        if autotune == "persistent":
+            self._check(self.lib.mctdh_ens_autotune(self.h, 2))   # planned shapes, persistent CTAs
+        elif not autotune:
             self._check(self.lib.mctdh_ens_autotune(self.h, 0))
 
     def autotune(self):
@@ -689,8 +693,11 @@ class Ensemble:
         ms, ms0 = C.c_double(), C.c_double()
         self._check(self.lib.mctdh_ens_tuning(self.h, C.byref(tpb), C.byref(cap), C.byref(tc), C.byref(ms),
                                               C.byref(ms0), C.byref(cand)))
+        pp, ph = C.c_int64(), C.c_int64()
+        self._check(self.lib.mctdh_ens_persistent(self.h, C.byref(pp), C.byref(ph)))
         return dict(tiles_per_block=tpb.value, block_cap=cap.value, tensor_cores=tc.value, eom_ms=ms.value,
-                    default_eom_ms=ms0.value, candidates=cand.value)
+                    default_eom_ms=ms0.value, candidates=cand.value, persistent_prod_ctas=pp.value,
+                    persistent_hole_ctas=ph.value)
 
     def eom_cost(self) -> Dict:
         """Algorithmic FLOPs and bytes of one merged EOM evaluation."""

@@ -3837,6 +3837,8 @@ struct Ens {
   bool tune_tc = true;
   double tune_ms = -1.0, tune_default_ms = -1.0;
   int tune_candidates = 0;
+  // persistent CTAs of the merged mode products and contractions (0: one CTA per block)
+  int persist_prod = 0, persist_hole = 0;
 };
 
 // Run `body` (launches on E.st only, no host synchronisation) as CUDA graph slot
@@ -4055,12 +4057,12 @@ void ens_destroy(Ens* E) {
 
 void ens_run_prod(Ens& E, const ProdBatch& b) {
   if (b.h.empty()) return;
-  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec, E.tune_tc ? 2 : 0);
+  launch_prod(b.d, (int)b.h.size(), b.nblocks, b.maxn, E.st, b.prec, E.tune_tc ? 2 : 0, E.persist_prod);
   ++E.launches;
 }
 void ens_run_hole(Ens& E, const HoleBatch& b) {
   if (b.h.empty()) return;
-  launch_hole(b.d, (int)b.h.size(), b.nblocks, E.st, b.prec);
+  launch_hole(b.d, (int)b.h.size(), b.nblocks, E.st, b.prec, E.persist_hole);
   ++E.launches;
 }
 void ens_run_red(Ens& E, const RedBatch& b) {
@@ -4140,14 +4142,38 @@ void ens_autotune(Ens& E) {
       bc = c;
     }
   }
+  // then, on the best tiling, persistent CTAs (q per SM for the 256-thread
+  // contractions, 2q for the 128-thread mode products) against one CTA per block
+  E.tune_tc = bc.tc;
+  ens_retile(E, bc.tpb, bc.cap);
+  int nsm = 0, dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int best_q = 0;
+  for (int q : {2, 4}) {
+    E.persist_prod = 2 * q * nsm;
+    E.persist_hole = q * nsm;
+    ens_eom(E, E.K[6]);
+    CK(cudaEventRecord(e0, E.st));
+    ens_eom(E, E.K[6]);
+    ens_eom(E, E.K[6]);
+    CK(cudaEventRecord(e1, E.st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (0.5 * ms < best) {
+      best = 0.5 * ms;
+      best_q = q;
+    }
+  }
+  E.persist_prod = 2 * best_q * nsm;
+  E.persist_hole = best_q * nsm;
   CK(cudaEventDestroy(e0));
   CK(cudaEventDestroy(e1));
-  E.tune_tc = bc.tc;
   E.tune_tpb = bc.tpb;
   E.tune_cap = bc.cap;
   E.tune_ms = best;
-  E.tune_candidates = (int)cands.size();
-  ens_retile(E, bc.tpb, bc.cap);
+  E.tune_candidates = (int)cands.size() + 2;
   E.launches = l0;
   E.eom_count = q0;
   // the EOMs of the tuning ran on the start states: clear what they may have flagged
@@ -5200,13 +5226,21 @@ int64_t mctdh_ens_counters(mctdh_ens_t* ens, int64_t* launches, int64_t* eom, in
 }
 
 int64_t mctdh_ens_autotune(mctdh_ens_t* ens, int64_t mode) {
-  if (!ens || mode < 0 || mode > 1) return MCTDH_EARG;
+  if (!ens || mode < 0 || mode > 2) return MCTDH_EARG;
   Ens& E = *ens->e;
   if (E.graph[0] || E.graph[1] || E.graph[2])
     return MCTDH_EARG;   // the launch shapes are fixed once a propagation captured its graphs
   try {
-    if (mode == 0) {
+    if (mode == 0 || mode == 2) {
       E.tuned = true;    // keep the planned shapes
+      if (mode == 2) {
+        // with persistent CTAs: 2 contraction and 4 mode-product CTAs per SM
+        int nsm = 0, dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        E.persist_prod = 4 * nsm;
+        E.persist_hole = 2 * nsm;
+      }
       return MCTDH_OK;
     }
     E.tuned = false;
@@ -5231,6 +5265,13 @@ int64_t mctdh_ens_tuning(mctdh_ens_t* ens, int64_t* tiles_per_block, int64_t* bl
   if (eom_ms) *eom_ms = E.tune_ms;
   if (default_eom_ms) *default_eom_ms = E.tune_default_ms;
   if (candidates) *candidates = E.tune_candidates;
+  return MCTDH_OK;
+}
+
+int64_t mctdh_ens_persistent(mctdh_ens_t* ens, int64_t* prod_ctas, int64_t* hole_ctas) {
+  if (!ens) return MCTDH_EARG;
+  if (prod_ctas) *prod_ctas = ens->e->persist_prod;
+  if (hole_ctas) *hole_ctas = ens->e->persist_hole;
   return MCTDH_OK;
 }
 

@@ -15,14 +15,17 @@
 // descriptor lookup: descriptors are sorted by block_start
 // ---------------------------------------------------------------------------
 template <typename D>
-__device__ __forceinline__ int find_desc(const D* descs, int ndesc) {
+__device__ __forceinline__ int find_desc_at(const D* descs, int ndesc, long long b) {
   int lo = 0, hi = ndesc - 1;
-  const long long b = blockIdx.x;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (descs[mid].block_start <= b) lo = mid; else hi = mid - 1;
   }
   return lo;
+}
+template <typename D>
+__device__ __forceinline__ int find_desc(const D* descs, int ndesc) {
+  return find_desc_at(descs, ndesc, (long long)blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -61,13 +64,15 @@ __device__ __forceinline__ void df_fma0(float& sh, float& sl, float a, float b) 
 // at the accumulation's own rounding level), outputs complex FP32 (TF_F32) or
 // FP64.  PREC 2: x and M split into hi + lo FP32 parts, x*M = xh*Mh + xh*Ml + xl*Mh
 // with the sum carried as an FP32 hi/lo pair (compensated), ~1e-13 relative.
+// Block `bb` of the batch (blockIdx.x of the plain launch; persistent CTAs walk
+// the blocks).
 template <int MAXN, int PREC>
-__global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
+__device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, int ndesc, long long bb) {
   __shared__ int s_di;
   __shared__ cplx Ms[PREC == 0 ? MAXN * MAXN : 1];
   __shared__ cplxf Mh[PREC == 0 ? 1 : MAXN * MAXN];
   __shared__ cplxf Ml[PREC == 0 ? 1 : MAXN * MAXN];
-  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  if (threadIdx.x == 0) s_di = find_desc_at(descs, ndesc, bb);
   __syncthreads();
   const ProdDesc& d = descs[s_di];
   const int nin = d.nin, nout = d.nout;
@@ -89,7 +94,7 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
     }
   }
   __syncthreads();
-  const long long p = (long long)(blockIdx.x - d.block_start) * blockDim.x + threadIdx.x;
+  const long long p = (bb - d.block_start) * blockDim.x + threadIdx.x;
   const long long L = d.L, nfib = L * d.R;
   if (p >= nfib) return;
   long long l, r;
@@ -166,6 +171,21 @@ __global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ 
   }
 }
 
+template <int MAXN, int PREC>
+__global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
+  prod_block<MAXN, PREC>(descs, ndesc, (long long)blockIdx.x);
+}
+
+// Persistent form: gridDim.x CTAs walk the batch's blocks in a fixed stride.
+template <int MAXN, int PREC>
+__global__ void __launch_bounds__(128) prod_kernel_persistent(const ProdDesc* __restrict__ descs, int ndesc,
+                                                              long long nblocks) {
+  for (long long bb = blockIdx.x; bb < nblocks; bb += gridDim.x) {
+    prod_block<MAXN, PREC>(descs, ndesc, bb);
+    __syncthreads();   // the block's shared operands are rewritten by the next one
+  }
+}
+
 // Tensor-core kernels (tc.cu) may serve the FP32 products unless
 // MACAW_GB300_TC=0 selects the CUDA-core kernels (read once per process).
 bool tc_enabled() {
@@ -178,11 +198,25 @@ bool tc_enabled() {
 }
 
 // tc: 0 CUDA-core kernel, 1 tensor cores from the configured SPF count on,
-// 2 tensor cores for every size they take (the ensemble autotuner's candidate)
+// 2 tensor cores for every size they take (the ensemble autotuner's candidate).
+// persist > 0: at most that many persistent CTAs walk the blocks.
 void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, int prec,
-                 int tc) {
+                 int tc, int persist) {
   if (ndesc <= 0 || nblocks <= 0) return;
   if (prec == 1 && tc && tc_enabled() && launch_prod_tc(d_descs, ndesc, nblocks, maxn, st, tc == 2)) return;
+  if (persist > 0 && nblocks > persist) {
+    const unsigned g = (unsigned)persist;
+    if (maxn <= 12) {
+      if (prec == 0) prod_kernel_persistent<12, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+      else if (prec == 1) prod_kernel_persistent<12, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+      else prod_kernel_persistent<12, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+    } else {
+      if (prec == 0) prod_kernel_persistent<MAXN_SPF, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+      else if (prec == 1) prod_kernel_persistent<MAXN_SPF, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+      else prod_kernel_persistent<MAXN_SPF, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+    }
+    return;
+  }
   const unsigned nb = (unsigned)nblocks;
   if (maxn <= 12) {
     if (prec == 0) prod_kernel<12, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
@@ -225,7 +259,7 @@ __device__ void dot_block(const HoleDesc& d, int b, cplx* red) {
 // PREC 1: FP32 operands (rounded to nearest), FP32 products and sums (~1e-7
 // relative), the block partials widened to FP64 for the deterministic reduction.
 template <int PREC>
-__global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
+__device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, int ndesc, long long bb) {
   __shared__ int s_di;
   __shared__ cplx Xs[HOLE_TILE * MAXN_SPF];
   __shared__ cplx Ys[HOLE_TILE * MAXN_SPF];
@@ -233,10 +267,10 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   float4* Yf = reinterpret_cast<float4*>(Ys);
   float2* X1 = reinterpret_cast<float2*>(Xs);   // PREC 1 and complex-FP32 operands: (re, im)
   float2* Y1 = reinterpret_cast<float2*>(Ys);
-  if (threadIdx.x == 0) s_di = find_desc(descs, ndesc);
+  if (threadIdx.x == 0) s_di = find_desc_at(descs, ndesc, bb);
   __syncthreads();
   const HoleDesc& d = descs[s_di];
-  const int b = (int)(blockIdx.x - d.block_start);
+  const int b = (int)(bb - d.block_start);
   const int n1 = d.n1, n2 = d.n2, npairs = n1 * n2;
   if (npairs == 1 && d.L * d.R >= HOLE_THREADS) {
     dot_block<PREC>(d, b, Xs);
@@ -359,8 +393,31 @@ __global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __re
   }
 }
 
-void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec) {
+template <int PREC>
+__global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
+  hole_block<PREC>(descs, ndesc, (long long)blockIdx.x);
+}
+
+// Persistent form: gridDim.x CTAs walk the batch's blocks in a fixed stride (each
+// block still writes its own partial, so the sums do not depend on the grid).
+template <int PREC>
+__global__ void __launch_bounds__(HOLE_THREADS) hole_kernel_persistent(const HoleDesc* __restrict__ descs,
+                                                                       int ndesc, long long nblocks) {
+  for (long long bb = blockIdx.x; bb < nblocks; bb += gridDim.x) {
+    hole_block<PREC>(descs, ndesc, bb);
+    __syncthreads();   // the staging tiles are rewritten by the next block
+  }
+}
+
+void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec, int persist) {
   if (ndesc <= 0 || nblocks <= 0) return;
+  if (persist > 0 && nblocks > persist) {
+    const unsigned g = (unsigned)persist;
+    if (prec == 0) hole_kernel_persistent<0><<<g, HOLE_THREADS, 0, st>>>(d_descs, ndesc, nblocks);
+    else if (prec == 1) hole_kernel_persistent<1><<<g, HOLE_THREADS, 0, st>>>(d_descs, ndesc, nblocks);
+    else hole_kernel_persistent<2><<<g, HOLE_THREADS, 0, st>>>(d_descs, ndesc, nblocks);
+    return;
+  }
   if (prec == 0)
     hole_kernel<0><<<(unsigned)nblocks, HOLE_THREADS, 0, st>>>(d_descs, ndesc);
   else if (prec == 1)

@@ -231,9 +231,11 @@ bool tc_enabled();
 void tc_prepare();
 bool launch_prod_tc(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st, bool force);
 int tc_timeout_flag(bool clear);
+// persist > 0: at most `persist` persistent CTAs walk the batch's blocks
 void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn, cudaStream_t st,
-                 int prec = 0, int tc = 1);
-void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec = 0);
+                 int prec = 0, int tc = 1, int persist = 0);
+void launch_hole(const HoleDesc* d_descs, int ndesc, long long nblocks, cudaStream_t st, int prec = 0,
+                 int persist = 0);
 void launch_reduce(const RedTarget* d_tg, int ntg, const RedTerm* d_terms, cudaStream_t st);
 // with_h: also h1mode (second launch: the Hermitian part of same-state matrices);
 // prec > 0: the operator products and phi^H (O phi) in compensated split FP32

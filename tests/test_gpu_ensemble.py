@@ -38,15 +38,20 @@ def test_ensemble_eom_matches_single_contexts():
         assert _rel(dpsi, rpsi) < 1e-13
 
 
-@pytest.mark.parametrize("method", [INT_RK45, INT_DOPRI])
-def test_ensemble_propagation_matches_single_contexts(method):
+@pytest.mark.parametrize("method,shapes", [(INT_RK45, False), (INT_DOPRI, False), (INT_RK45, "persistent")])
+def test_ensemble_propagation_matches_single_contexts(method, shapes):
     """Lockstep RK with per-member step control: each member follows the step
-    sequence its own context takes, so C(t), populations, norm and energy agree."""
+    sequence its own context takes, so C(t), populations, norm and energy agree.
+    With persistent CTAs (each walking the batch's blocks) the block partials and
+    so the arithmetic are the same."""
     from macaw_gb300.capi import Ensemble, GpuCore
     models = _members()
     # the planned launch shapes: the autotuner may re-tile the contractions, which
     # reorders their partial sums
-    ens = Ensemble(models, autotune=False)
+    ens = Ensemble(models, autotune=shapes)
+    if shapes == "persistent":
+        tn = ens.tuning()
+        assert tn["persistent_prod_ctas"] > 0 and tn["persistent_hole_ctas"] > 0
     starts = [initial_wavefunction(m) for m in models]
     for i, (A, psi) in enumerate(starts):
         ens.set_state(i, A, psi, as_start=True)
