@@ -370,7 +370,8 @@ int64_t mctdh_ens_stream(mctdh_ens_t *ens, void **stream);
  * CTAs per SM, each walking the batch's blocks) against one CTA per block.  mode 1 runs
  * it now on the current states, mode 0 keeps the planned shapes (an ensemble
  * whose members must repeat the arithmetic of single contexts bit for bit),
- * mode 2 keeps them with persistent CTAs (the same arithmetic);
+ * mode 2 keeps them with the persistent kernels on a minimal grid (every CTA
+ * walks many blocks; the same arithmetic);
  * -7 once a propagation has fixed the shapes.  mctdh_ens_tuning reports the
  * chosen shape, its EOM time (ms) against the planned shape's, and the number of
  * candidates timed (0: not tuned).  Each attempt round of mctdh_ens_propagate

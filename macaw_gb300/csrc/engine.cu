@@ -5234,12 +5234,11 @@ int64_t mctdh_ens_autotune(mctdh_ens_t* ens, int64_t mode) {
     if (mode == 0 || mode == 2) {
       E.tuned = true;    // keep the planned shapes
       if (mode == 2) {
-        // with persistent CTAs: 2 contraction and 4 mode-product CTAs per SM
-        int nsm = 0, dev = 0;
-        CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        E.persist_prod = 4 * nsm;
-        E.persist_hole = 2 * nsm;
+        // persistent kernels on a minimal grid (4 mode-product and 2 contraction
+        // CTAs), so that every CTA walks many blocks: the check that the
+        // persistent forms repeat the per-block arithmetic
+        E.persist_prod = 4;
+        E.persist_hole = 2;
       }
       return MCTDH_OK;
     }
