@@ -59,6 +59,22 @@ __device__ __forceinline__ void df_fma0(float& sh, float& sl, float a, float b) 
   sl += t + e;
 }
 
+// acc += conj(x) y for complex split operands (re hi, im hi, re lo, im lo):
+// re = xr yr + xi yi, im = xr yi - xi yr, each real product compensated
+__device__ __forceinline__ void df_cfma(float* h, float* l, const float4& x, const float4& y) {
+  df_fma(h[0], l[0], x.x, x.z, y.x, y.z);
+  df_fma(h[0], l[0], x.y, x.w, y.y, y.w);
+  df_fma(h[1], l[1], x.x, x.z, y.y, y.w);
+  df_fma(h[1], l[1], -x.y, -x.w, y.x, y.z);
+}
+// the same for complex FP32 operands (no low parts)
+__device__ __forceinline__ void df_cfma0(float* h, float* l, const float2& x, const float2& y) {
+  df_fma0(h[0], l[0], x.x, y.x);
+  df_fma0(h[0], l[0], x.y, y.y);
+  df_fma0(h[1], l[1], x.x, y.y);
+  df_fma0(h[1], l[1], -x.y, y.x);
+}
+
 // PREC 0: FP64.  PREC 1: FP32 -- the products of the FP32-rounded x and M are
 // accumulated in FP32 (~1e-7 relative; the split's correction products would sit
 // at the accumulation's own rounding level), outputs complex FP32 (TF_F32) or
@@ -206,7 +222,11 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
   if (prec == 1 && tc && tc_enabled() && launch_prod_tc(d_descs, ndesc, nblocks, maxn, st, tc == 2)) return;
   if (persist > 0 && nblocks > persist) {
     const unsigned g = (unsigned)persist;
-    if (maxn <= 12) {
+    if (maxn <= 8) {
+      if (prec == 0) prod_kernel_persistent<8, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+      else if (prec == 1) prod_kernel_persistent<8, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+      else prod_kernel_persistent<8, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
+    } else if (maxn <= 12) {
       if (prec == 0) prod_kernel_persistent<12, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
       else if (prec == 1) prod_kernel_persistent<12, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
       else prod_kernel_persistent<12, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
@@ -218,7 +238,13 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
     return;
   }
   const unsigned nb = (unsigned)nblocks;
-  if (maxn <= 12) {
+  // register arrays sized for the batch's largest SPF count: no dead unrolled
+  // iterations and fewer registers (more resident warps) at 8 SPFs and below
+  if (maxn <= 8) {
+    if (prec == 0) prod_kernel<8, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
+    else if (prec == 1) prod_kernel<8, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
+    else prod_kernel<8, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
+  } else if (maxn <= 12) {
     if (prec == 0) prod_kernel<12, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
     else if (prec == 1) prod_kernel<12, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
     else prod_kernel<12, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
@@ -286,6 +312,14 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
   const int G = small ? HOLE_THREADS / npairs : 1;
   const int pair0 = small ? tid % npairs : tid;
   const int g = small ? tid / npairs : 0;
+  // PREC 2 with even n1, n2: every thread owns a 2 x 2 block of (j1, j2) pairs, so
+  // each staged value it reads feeds two products (half the shared-memory reads
+  // per product and four independent accumulation chains)
+  const bool quad = PREC == 2 && small && ((n1 | n2) & 1) == 0;
+  const int h1 = n1 >> 1, nq = h1 * (n2 >> 1);
+  const int Gq = quad ? HOLE_THREADS / nq : 0;
+  const int qd = quad ? tid % nq : 0, gq = quad ? tid / nq : 0;
+  const int i1 = 2 * (qd % (h1 > 0 ? h1 : 1)), i2 = 2 * (qd / (h1 > 0 ? h1 : 1));
   cplx acc[4] = {mkc(0, 0), mkc(0, 0), mkc(0, 0), mkc(0, 0)};
   float ah[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   float al[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
@@ -293,6 +327,7 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
   // columns j = tid / HOLE_TILE, + HOLE_THREADS / HOLE_TILE, ...; its fibre's
   // (l, r) is carried from tile to tile instead of divided out per element.
   static_assert(HOLE_THREADS % HOLE_TILE == 0, "staging assumes whole tiles per thread row");
+  static_assert(4 * HOLE_THREADS <= HOLE_TILE * MAXN_SPF, "the 2 x 2 partials fit the staging tile");
   const int qt = tid % HOLE_TILE, jt = tid / HOLE_TILE, jstep = HOLE_THREADS / HOLE_TILE;
   long long pcur = (long long)b * HOLE_TILE + qt;
   long long lcur = pcur % L, rcur = pcur / L;
@@ -329,6 +364,30 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
       }
     }
     __syncthreads();
+    if (quad) {
+      // pairs (i1, i2), (i1 + 1, i2), (i1, i2 + 1), (i1 + 1, i2 + 1) in ah/al[0..3]
+      if (gq < Gq) {
+        for (int q = gq; q < HOLE_TILE; q += Gq) {
+          if (f32in) {
+            const float2 xa = X1[q * MAXN_SPF + i1], xb = X1[q * MAXN_SPF + i1 + 1];
+            const float2 ya = Y1[q * MAXN_SPF + i2], yb = Y1[q * MAXN_SPF + i2 + 1];
+            df_cfma0(ah[0], al[0], xa, ya);
+            df_cfma0(ah[1], al[1], xb, ya);
+            df_cfma0(ah[2], al[2], xa, yb);
+            df_cfma0(ah[3], al[3], xb, yb);
+          } else {
+            const float4 xa = Xf[q * MAXN_SPF + i1], xb = Xf[q * MAXN_SPF + i1 + 1];
+            const float4 ya = Yf[q * MAXN_SPF + i2], yb = Yf[q * MAXN_SPF + i2 + 1];
+            df_cfma(ah[0], al[0], xa, ya);
+            df_cfma(ah[1], al[1], xb, ya);
+            df_cfma(ah[2], al[2], xa, yb);
+            df_cfma(ah[3], al[3], xb, yb);
+          }
+        }
+      }
+      __syncthreads();
+      continue;
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       int pr, q0, qs;
@@ -375,7 +434,19 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
       acc[k] = mkc(f2d_exact(ah[k][0]) + f2d_exact(al[k][0]), f2d_exact(ah[k][1]) + f2d_exact(al[k][1]));
   }
   cplx* out = d.partial + (long long)b * npairs;
-  if (small) {
+  if (quad) {
+    cplx* red = Xs;   // 4 * HOLE_THREADS <= HOLE_TILE * MAXN_SPF entries
+#pragma unroll
+    for (int k = 0; k < 4; ++k) red[4 * tid + k] = acc[k];
+    __syncthreads();
+    if (tid < npairs) {
+      const int j1 = tid % n1, j2 = tid / n1;
+      const int qq = (j1 >> 1) + h1 * (j2 >> 1), k = (j1 & 1) + 2 * (j2 & 1);
+      cplx s = mkc(0, 0);
+      for (int gg = 0; gg < Gq; ++gg) s = cadd(s, red[4 * (gg * nq + qq) + k]);
+      out[tid] = s;
+    }
+  } else if (small) {
     cplx* red = Xs;   // reuse (HOLE_TILE*MAXN_SPF >= HOLE_THREADS)
     red[tid] = acc[0];
     __syncthreads();
@@ -394,14 +465,14 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(HOLE_THREADS) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
+__global__ void __launch_bounds__(HOLE_THREADS, 4) hole_kernel(const HoleDesc* __restrict__ descs, int ndesc) {
   hole_block<PREC>(descs, ndesc, (long long)blockIdx.x);
 }
 
 // Persistent form: gridDim.x CTAs walk the batch's blocks in a fixed stride (each
 // block still writes its own partial, so the sums do not depend on the grid).
 template <int PREC>
-__global__ void __launch_bounds__(HOLE_THREADS) hole_kernel_persistent(const HoleDesc* __restrict__ descs,
+__global__ void __launch_bounds__(HOLE_THREADS, 4) hole_kernel_persistent(const HoleDesc* __restrict__ descs,
                                                                        int ndesc, long long nblocks) {
   for (long long bb = blockIdx.x; bb < nblocks; bb += gridDim.x) {
     hole_block<PREC>(descs, ndesc, bb);
