@@ -1776,6 +1776,9 @@ void plan_ovl(Ctx& c, OvlPlan& P, cplx* y1, cplx* y2, int prec, bool norm_only, 
     }
   }
   P.gwp_d = upload_vec(c.ar, P.gwp_h);
+  // the SPF overlaps over the grid: compensated split FP32 (~1e-13) where the
+  // plan's chains are (the step-error overlaps of the split paths), else FP64
+  P.spf_holes.prec = prec;
   P.spf_holes.finalize(c.ar);
   for (auto& hr : hrefs) P.spf_red.add_term(hr.target, P.spf_holes.h[hr.hole], hr.alpha);
   P.spf_red.finalize(c.ar);
@@ -3027,6 +3030,8 @@ void plan_cmf(Ctx& c, CmfState& S) {
   }
   if (!c.modes_gwp.empty()) plan_cmf_gwp(c, S, em);
   S.elem_mode = upload_vec(c.ar, em);
+  // the SPF error norms: compensated split FP32 (~1e-13) in the split modes
+  S.err_holes.prec = c.precision ? 2 : 0;
   S.err_holes.finalize(c.ar);
   for (auto& hr : hrefs) S.err_red.add_term(hr.target, S.err_holes.h[hr.hole], hr.alpha);
   S.err_red.finalize(c.ar);
