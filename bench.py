@@ -46,9 +46,16 @@ MFX_EPOCHS = 12
 MFX_GATE = 0.5
 # ncu DRAM bytes per algorithmic byte of a kernel class in the benchmark regime
 # (one capture of the profile case), and what bounds each class there
-TRAFFIC_PER_ALG_BYTE = {"mode_product": 0.51}
+# DRAM bytes per algorithmic byte of the mode products: 177.5 MB of DRAM traffic
+# over 461 MB of operand bytes in the eight mode-product launches of one ncu
+# capture of the profile case at precision 5 (`--profile-case --precision 5
+# --profile-from-fs 1`: five compensated mean-field chain launches, three FP32
+# H_B*B launches)
+TRAFFIC_PER_ALG_BYTE = {"mode_product": 0.385}
 ROOF_BOUND = {"mode_product": "hbm", "hole_contract": "hbm", "spf_derivative": "hbm"}
-ROOF_NOTE = {"mode_product": "L2-resident operands (12.6 MB state): issue and L2 latency, not HBM",
+ROOF_NOTE = {"mode_product": "not HBM: the compensated mean-field products are FMA-issue bound (55 % of the FMA "
+                             "pipe), the FP32 H_B products load-latency bound; operands mostly L2-resident "
+                             "(12.6 MB state)",
              "hole_contract": "compensated FP32 sums: FP32 issue",
              "spf_derivative": "small per-mode problems: latency and occupancy"}
 ACC_FS = 0.5   # short comparison interval of the size scan
@@ -558,7 +565,7 @@ def run_gpu(args):
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
                      "traffic": (by_launch * TRAFFIC_PER_ALG_BYTE[dname]) if dname in TRAFFIC_PER_ALG_BYTE else None,
                      "traffic_source": "scaled: DRAM bytes per algorithmic byte of this kernel class from one ncu "
-                                       "capture of the profile case (bench.py --profile-case --profile-from-fs 1), "
+                                       "capture of the profile case (bench.py --profile-case --precision 5 --profile-from-fs 1), "
                                        "times this run's algorithmic bytes per launch",
                      "what_bounds_it": ROOF_NOTE.get(dname, ""),
                      "peak_source": peak_src},
