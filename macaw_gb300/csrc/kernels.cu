@@ -84,36 +84,14 @@ __device__ __forceinline__ void df_cfma0(float* h, float* l, const float2& x, co
 // the blocks).
 template <int MAXN, int PREC>
 __device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, int ndesc, long long bb) {
+  __shared__ int s_di;
   __shared__ cplx Ms[PREC == 0 ? MAXN * MAXN : 1];
   __shared__ cplxf Mh[PREC == 0 ? 1 : MAXN * MAXN];
   __shared__ cplxf Ml[PREC == 0 ? 1 : MAXN * MAXN];
-  // every thread finds the descriptor (a broadcast binary search) and issues its
-  // fibre's loads first: they are in flight while the matrix is staged
-  const ProdDesc& d = descs[find_desc_at(descs, ndesc, bb)];
+  if (threadIdx.x == 0) s_di = find_desc_at(descs, ndesc, bb);
+  __syncthreads();
+  const ProdDesc& d = descs[s_di];
   const int nin = d.nin, nout = d.nout;
-  const long long p = (bb - d.block_start) * blockDim.x + threadIdx.x;
-  const long long L = d.L, nfib = L * d.R;
-  const bool active = p < nfib;
-  long long l = 0, r = 0;
-  if (active) fibre_lr(p, L, nfib, l, r);
-  const long long xi0 = l + L * (long long)nin * r;
-  cplx x[PREC == 0 ? MAXN : 1];
-  cplxf xh[PREC == 0 ? 1 : MAXN], xl[PREC == 2 ? MAXN : 1];
-  if (PREC == 0) {
-#pragma unroll
-    for (int j = 0; j < MAXN; ++j) x[j] = (active && j < nin) ? load_c(d.X, xi0 + L * j, d.xfmt) : mkc(0.0, 0.0);
-  } else {
-#pragma unroll
-    for (int j = 0; j < MAXN; ++j) {
-      const float4 w = (active && j < nin) ? load_split(d.X, xi0 + L * j, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
-      if (PREC == 1) {
-        xh[j] = make_float2(w.x + w.z, w.y + w.w);   // rounded to nearest
-      } else {
-        xh[j] = make_float2(w.x, w.y);
-        xl[j] = make_float2(w.z, w.w);
-      }
-    }
-  }
   for (int e = threadIdx.x; e < nin * nout; e += blockDim.x) {
     int jo = e % nout, ji = e / nout;
     cplx v = d.conjT ? cconj(d.M[ji + (long long)d.ldm * jo]) : d.M[jo + (long long)d.ldm * ji];
@@ -132,10 +110,18 @@ __device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, i
     }
   }
   __syncthreads();
-  if (!active) return;
+  const long long p = (bb - d.block_start) * blockDim.x + threadIdx.x;
+  const long long L = d.L, nfib = L * d.R;
+  if (p >= nfib) return;
+  long long l, r;
+  fibre_lr(p, L, nfib, l, r);
+  const long long xi0 = l + L * (long long)nin * r;
   cplx* y0 = d.Y + l + L * (long long)nout * r;
   const cplx alpha = d.alpha;
   if (PREC == 0) {
+    cplx x[MAXN];
+#pragma unroll
+    for (int j = 0; j < MAXN; ++j) x[j] = (j < nin) ? load_c(d.X, xi0 + L * j, d.xfmt) : mkc(0.0, 0.0);
     for (int jo = 0; jo < nout; ++jo) {
       cplx acc = mkc(0.0, 0.0);
 #pragma unroll
@@ -146,6 +132,17 @@ __device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, i
       y0[L * jo] = v;
     }
   } else {
+    cplxf xh[MAXN], xl[MAXN];
+#pragma unroll
+    for (int j = 0; j < MAXN; ++j) {
+      const float4 w = (j < nin) ? load_split(d.X, xi0 + L * j, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (PREC == 1) {
+        xh[j] = make_float2(w.x + w.z, w.y + w.w);   // rounded to nearest
+      } else {
+        xh[j] = make_float2(w.x, w.y);
+        xl[j] = make_float2(w.z, w.w);
+      }
+    }
     const bool unit_alpha = (alpha.x == 1.0 && alpha.y == 0.0);
     float4* y0f = reinterpret_cast<float4*>(y0);
     for (int jo = 0; jo < nout; ++jo) {
