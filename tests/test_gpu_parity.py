@@ -193,10 +193,12 @@ def test_cmf2_free_running(core_cls):
     _compare(outs, ref, 10 * model.eps_int)
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-10)])
+@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-10), (3, 1e-5), (4, 1e-6), (5, 1e-10), (6, 1e-5)])
 def test_split_precision_eom(core_cls, prec, tol):
     """Split-FP32 mode products (1: FP32 sums, 2: compensated FP32 sums; mean
-    fields always compensated) against the FP64 oracle."""
+    fields compensated) against the FP64 oracle; 3 and 6 sum the contractions
+    (all of them, or the mean fields') in FP32; 4 and 5 differ from 1 and 2 only
+    in the Lanczos H_B products, which the EOM does not use."""
     for builder, seed in ((lambda: small_lvc(), 21), (lambda: small_qvc(), 22)):
         model = builder()
         A, psi = random_state(model, seed=seed)
@@ -206,12 +208,14 @@ def test_split_precision_eom(core_cls, prec, tol):
         assert _rel(dpsi, ref_dpsi) < tol
 
 
-def test_split_precision_cmf2_replay(core_cls):
-    """The split-FP32 CMF2 path on the oracle's step sequence stays within 1e-7 of C(t)."""
+@pytest.mark.parametrize("prec", [1, 5])
+def test_split_precision_cmf2_replay(core_cls, prec):
+    """The split-FP32 CMF2 path on the oracle's step sequence stays within 1e-7 of
+    C(t) (FP32 Lanczos products in both modes)."""
     model = small_qvc(tfinal_fs=1.0)
     A, psi = initial_wavefunction(model)
     ref, steps, _ = Oracle(model).propagate(A, psi, record_steps=True)
-    gpu = core_cls(model, precision=1)
+    gpu = core_cls(model, precision=prec)
     outs, _ = _replay(gpu, model, A, psi, steps, lambda A, psi, t, h: gpu.cmf2_attempt(A, psi, t, h))
     _compare(outs, ref, 1e-7)
 
