@@ -2792,6 +2792,14 @@ struct CmfState {
   std::vector<SpfErrDesc> errd_h;
   SpfErrDesc* errd_d = nullptr;
   long long rk_iters = 0;
+  // the step-start operators (h1mode, h·phi, the pre-summed single-mode
+  // operators, rho, the mean fields) of grid-mode models, saved after their
+  // evaluation so that a rejected attempt's retry from the same state restores
+  // them instead of evaluating them again
+  std::vector<SnapSeg> opseg_h;
+  SnapSeg* opseg_d = nullptr;
+  long long opE = 0;
+  cplx* opsave = nullptr;
   // Gaussian modes (cmf2_base.f90): the D matrices of every (mode, set) block,
   // concatenated into one vector per role; B = D^H S A is the propagated vector
   bool gwp = false;
@@ -3029,6 +3037,31 @@ void plan_cmf(Ctx& c, CmfState& S) {
     }
   }
   if (!c.modes_gwp.empty()) plan_cmf_gwp(c, S, em);
+  if (c.modes_gwp.empty()) {
+    long long off = 0;
+    auto seg = [&](cplx* p, long long n) {
+      if (!p || n <= 0) return;
+      S.opseg_h.push_back(SnapSeg{p, off, 0, 0});
+      off += n;
+    };
+    for (int m : c.modes_dvr) {
+      for (int k = 0; k < c.noper[m]; ++k) {
+        const long long n1 = c.m_of(m, c.oper[m][k][0]), n2 = c.m_of(m, c.oper[m][k][1]);
+        if (!c.is_identity[m + f * k]) seg(c.hmat[m][k], n1 * n2);
+        seg(c.ophi[m][k], (long long)c.gmode[m] * n2);
+        seg(c.mf[m][k], n1 * n2);
+      }
+      for (int st = 0; st < c.nstates; ++st)
+        if (c.rho[m][st]) seg(c.rho[m][st], (long long)c.m_of(m, st) * c.m_of(m, st));
+      if (c.rho_ave[m]) seg(c.rho_ave[m], (long long)c.m_of(m, 0) * c.m_of(m, 0));
+    }
+    for (const MatSumDesc& md : c.msum_h) seg(md.out, (long long)md.n1 * md.n2);
+    S.opE = off;
+    if (off > 0) {
+      S.opseg_d = upload_vec(c.ar, S.opseg_h);
+      S.opsave = c.ar.calloc_c(off);
+    }
+  }
   S.elem_mode = upload_vec(c.ar, em);
   // the SPF error norms: compensated split FP32 (~1e-13) in the split modes
   S.err_holes.prec = c.precision ? 2 : 0;
@@ -3380,7 +3413,7 @@ void mfx_push_half(Ctx& c, MfxState& M, double th) {
 // One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
 // ops_fresh: the operators and mean fields at d_y are already in place.
-double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_done) {
+double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_done, bool ops_saved = false) {
   if (c.mixture)
     throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 covers a single wave packet without dissipation (use rk45, dopri, abm or bs)");
   CmfState& S = cmf_state(c);
@@ -3388,7 +3421,16 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_d
   // With a second stream the regularised inverse of rho and the SPF half step
   // (which needs it) run beside the Lanczos build (which needs only h1mode).
   const bool overlap = c.st2 != nullptr;
-  if (!ops_fresh) {
+  if (!ops_fresh && ops_saved && S.opE > 0) {
+    // a retry from the same state: the step-start operators saved after their
+    // evaluation (cmf2_base.f90:78-87 gives the same values again); rho^-1 MF as
+    // in the evaluation (inside it without a second stream, below with one)
+    copy_dev(c, c.d_in, c.d_y, c.ntot);
+    launch_snap(S.opseg_d, (int)S.opseg_h.size(), S.opsave, S.opE, 1, c.st);
+    c.count();
+    if (!overlap) run_reginv(c);
+    reginv_done = !overlap;
+  } else if (!ops_fresh) {
     operators_and_mf(c, c.d_y, !overlap);           // cmf2_base.f90:78-87
     reginv_done = !overlap;
   }
@@ -3546,6 +3588,12 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
     } else {
       operators_and_mf(c, c.d_y, !overlap);
       if (M && M->recording) snap_gather(c, *M, M->start);
+      // kept for the retries of a rejected attempt (same state, same operators)
+      CmfState& S = cmf_state(c);
+      if (S.opE > 0) {
+        launch_snap(S.opseg_d, (int)S.opseg_h.size(), S.opsave, S.opE, 0, c.st);
+        c.count();
+      }
     }
     // reginv of the step start: done by operators_and_mf without a second stream;
     // otherwise inside the attempt, beside the Lanczos build
@@ -3558,7 +3606,7 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       if (*tries > 1000) throw StatusError(MCTDH_ESTEP, "CMF2 step not accepted after 1000 attempts");
       double error = 0.0;
       try {
-        error = cmf2_attempt(c, t, hdid, first, first && reginv_first);
+        error = cmf2_attempt(c, t, hdid, first, first && reginv_first, !first && !predicted);
       } catch (const StatusError& e) {
         if (!(predicted && first) || (e.code != MCTDH_ENONFINITE && e.code != MCTDH_EEIG)) throw;
         // an extrapolated step start that made the SPF integration non-finite (or

@@ -175,6 +175,22 @@ def test_cmf2_step(core_cls, int_type_psi):
     assert np.abs(gp - rp).max() < 1e-10
 
 
+def test_cmf2_step_with_rejected_attempts(core_cls):
+    """A trial step far above the tolerated one: the step control rejects it and
+    retries from the same state, where the device restores the step-start
+    operators saved after their evaluation instead of evaluating them again;
+    the accepted step equals the oracle's (cmf2_base.f90:176-201)."""
+    model = small_qvc()
+    A, psi = initial_wavefunction(model)
+    o = Oracle(model)
+    rA, rp, rh, rn, tries = o.cmf2(A, psi, 0.0, 40.0)
+    assert tries >= 2
+    gA, gp, gh, gn = core_cls(model).cmf2(A, psi, 0.0, 40.0)
+    assert abs(gh - rh) <= 1e-6 * rh
+    assert np.abs(gA - rA).max() < 1e-10
+    assert np.abs(gp - rp).max() < 1e-10
+
+
 def test_cmf2_replay_observables(core_cls):
     model = small_qvc(tfinal_fs=1.0)
     A, psi = initial_wavefunction(model)
