@@ -188,8 +188,18 @@ int64_t mctdh_fp64_peak(double *tflops);
 int64_t mctdh_event_record(mctdh_ctx_t *ctx, int64_t slot);
 int64_t mctdh_event_elapsed(mctdh_ctx_t *ctx, int64_t slot0, int64_t slot1, double *ms);
 
-/* Per-kernel-class timing (replaces the 8 timers of timingmod.f90:16-103 with
- * CUDA events).  enable: 0 off, 1 on, 2 on and reset.  kid: 0 mode products,
+/* The reference's routine timers (timingmod.f90:16-103) on CUDA events: timer
+ * 1 CalcDerivs, 2 normWF/wf_ovl, 3 Calc_MeanField, 4 Calc_CY, 5 Calc_h1mode,
+ * 6 Calc_Der_SPF_DVR, 7 Calc_Der_SPF_GWP, 8 Lanczos (the reference's numbering),
+ * device time between the routine's first and last launch on the context's
+ * streams.  mode: 0 off, 1 on, 2 on and reset; while on, the CUDA graphs of the
+ * CMF2 sweeps are not used.  mctdh_write_timings writes the `timing` file
+ * (write_timings, timingmod.f90:72-103) with the caller's wall time. */
+int64_t mctdh_timing(mctdh_ctx_t *ctx, int64_t mode);
+int64_t mctdh_timing_read(mctdh_ctx_t *ctx, int64_t timer, int64_t *calls, double *ms);
+int64_t mctdh_write_timings(mctdh_ctx_t *ctx, const char *path, double walltime_s);
+
+/* Per-kernel-class timing with CUDA events.  enable: 0 off, 1 on, 2 on and reset.  kid: 0 mode products,
  * 1 single-hole contractions, 2 reductions, 3 h1mode/SPF operators, 4 regularised
  * inverses, 5 term sums, 6 SPF derivatives, 7 elementwise.  flops/bytes are the
  * algorithmic work of the timed launches. */

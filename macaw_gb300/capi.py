@@ -99,6 +99,9 @@ def load_library() -> C.CDLL:
     lib.mctdh_event_record.argtypes = [vp, C.c_int64]
     lib.mctdh_event_elapsed.argtypes = [vp, C.c_int64, C.c_int64, DP]
     lib.mctdh_profile.argtypes = [vp, C.c_int64]
+    lib.mctdh_timing.argtypes = [vp, C.c_int64]
+    lib.mctdh_timing_read.argtypes = [vp, C.c_int64, I64P, DP]
+    lib.mctdh_write_timings.argtypes = [vp, C.c_char_p, C.c_double]
     lib.mctdh_counters.argtypes = [vp, I64P, I64P, I64P]
     lib.mctdh_fp64_peak.argtypes = [DP]
     FP = C.POINTER(C.c_float)
@@ -140,7 +143,8 @@ def load_library() -> C.CDLL:
                  "mctdh_tensor_core_status", "mctdh_tensor_core_config"):
         getattr(lib, name).restype = C.c_int64
     for name in ("mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
-                 "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders", "mctdh_mfx_gate"):
+                 "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders", "mctdh_mfx_gate",
+                 "mctdh_timing", "mctdh_timing_read", "mctdh_write_timings"):
         getattr(lib, name).restype = C.c_int64
     lib.mctdh_density_matrix_noalloc.argtypes = [C.c_void_p, I64P, C.c_int64, C.c_int64, C.c_void_p,
                                                  C.c_int64, C.c_void_p]
@@ -172,6 +176,7 @@ EXPORTED = ["mctdh_create", "mctdh_destroy", "mctdh_calc_derivs", "mctdh_rkqs", 
             "mctdh_mlp_get_params", "mctdh_mlp_predict", "mctdh_mlp_grad", "mctdh_mlp_train",
             "mctdh_mfx_size", "mctdh_mfx_record", "mctdh_mfx_fetch", "mctdh_mfx_attach", "mctdh_mfx_stats",
             "mctdh_mfx_predict", "mctdh_mfx_log", "mctdh_mfx_orders", "mctdh_mfx_gate",
+            "mctdh_timing", "mctdh_timing_read", "mctdh_write_timings",
             "mctdh_ens_create", "mctdh_ens_destroy", "mctdh_ens_set_state", "mctdh_ens_get_state",
             "mctdh_ens_calc_derivs", "mctdh_ens_get_derivs", "mctdh_ens_propagate", "mctdh_ens_observables",
             "mctdh_ens_counters", "mctdh_ens_stream", "mctdh_ens_last_error"]
@@ -519,6 +524,25 @@ class GpuCore:
         ms = C.c_double()
         self._check(self.lib.mctdh_event_elapsed(self.h, s0, s1, C.byref(ms)))
         return ms.value
+
+    TIMERS = ("CalcDerivs", "normWF/wf_ovl", "Calc_MeanField", "Calc_CY", "Calc_h1mode",
+              "Calc_Der_SPF_DVR", "Calc_Der_SPF_GWP", "Lanczos")
+
+    def timing(self, mode: int):
+        """The reference's routine timers on CUDA events: 0 off, 1 on, 2 on and reset."""
+        self._check(self.lib.mctdh_timing(self.h, mode))
+
+    def timing_read(self) -> Dict[str, Dict]:
+        out = {}
+        for i, name in enumerate(self.TIMERS):
+            n, ms = C.c_int64(), C.c_double()
+            self._check(self.lib.mctdh_timing_read(self.h, i + 1, C.byref(n), C.byref(ms)))
+            out[name] = dict(calls=n.value, ms=ms.value)
+        return out
+
+    def write_timings(self, path: str, walltime_s: float):
+        """The reference's `timing` file (timingmod.f90:72-103)."""
+        self._check(self.lib.mctdh_write_timings(self.h, path.encode(), float(walltime_s)))
 
     def profile(self, enable: int):
         self._check(self.lib.mctdh_profile(self.h, enable))

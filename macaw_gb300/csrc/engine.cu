@@ -294,6 +294,13 @@ struct Ctx {
   bool ops_fresh = false;    // operators/mean fields at d_y are in place (time ops_fresh_t)
   double ops_fresh_t = -1.0;
   bool profiling = false;
+  // the reference's eight named routine timers (timingmod.f90:20-27) on CUDA
+  // events: accumulated device time and calls per routine
+  bool timing = false;
+  double rt_ms[8] = {};
+  long long rt_calls[8] = {};
+  struct RtEv { int id; cudaEvent_t a, b; bool call; };
+  std::vector<RtEv> rt_pending;
   // CUDA graphs of launch sequences that repeat with the same buffers: (kind, key
   // buffer) -> (executable graph, kernel launches it holds)
   struct GraphRec {
@@ -1874,6 +1881,41 @@ struct ProfScope {
     }
   }
 };
+// Routine timers: RT_* are the reference's timer numbers minus one.
+enum { RT_CALCDERIVS, RT_OVL, RT_MEANFIELD, RT_CY, RT_H1MODE, RT_SPF_DVR, RT_SPF_GWP, RT_LANCZOS };
+struct RtScope {
+  Ctx& c;
+  int id;
+  bool call;
+  cudaEvent_t a = nullptr;
+  RtScope(Ctx& cc, int i, bool counts_call = true, bool on = true) : c(cc), id(i), call(counts_call) {
+    if (c.timing && on) {
+      a = take_event(c);
+      CK(cudaEventRecord(a, c.st));
+    }
+  }
+  ~RtScope() {
+    if (c.timing && a) {
+      cudaEvent_t b = take_event(c);
+      cudaEventRecord(b, c.st);
+      c.rt_pending.push_back(Ctx::RtEv{id, a, b, call});
+    }
+  }
+};
+void drain_timing(Ctx& c) {
+  if (c.rt_pending.empty()) return;
+  CK(cudaDeviceSynchronize());
+  for (auto& p : c.rt_pending) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, p.a, p.b));
+    c.rt_ms[p.id] += ms;
+    if (p.call) c.rt_calls[p.id] += 1;
+    c.evpool.push_back(p.a);
+    c.evpool.push_back(p.b);
+  }
+  c.rt_pending.clear();
+}
+
 void drain_profile(Ctx& c) {
   if (c.pending.empty()) return;
   CK(cudaStreamSynchronize(c.st));
@@ -1896,7 +1938,7 @@ void drain_profile(Ctx& c) {
 // possible the sequence is launched directly from then on.
 template <typename F>
 void run_graphed(Ctx& c, int kind, const void* key, F&& body) {
-  if (c.profiling || c.graphs_off) {
+  if (c.profiling || c.graphs_off || c.timing) {
     body();
     return;
   }
@@ -1987,6 +2029,7 @@ void gwp_setup_run(Ctx& c) {
 // corrected dA into out's coefficient part (from d_adot).
 // Calc_CY and the Tikhonov parameter solve: der_factor * x into out's psi part, tau
 void gwp_solve_run(Ctx& c, cplx* out) {
+  RtScope rt(c, RT_CY);   // Calc_CY and the parameter solve (gmctdh_objects.f90:1198-1333)
   ProfScope ps(c, KP_GWP);
   launch_gwp_cy(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.cy_maxn, c.cy_maxops, c.yop_d, c.cy_part, c.st);
   launch_gwp_solve(c.cy_d, (int)c.cy_h.size(), c.cy_maxG, c.der, out, c.d_status, c.st);
@@ -1994,6 +2037,7 @@ void gwp_solve_run(Ctx& c, cplx* out) {
 }
 
 void gwp_derivs_run(Ctx& c, cplx* out) {
+  RtScope rt(c, RT_SPF_GWP);
   gwp_solve_run(c, out);
   for (auto& b : c.gwp_sinv) run_prod(c, b);
   for (auto& b : c.gwp_tau) run_prod(c, b);
@@ -2035,6 +2079,7 @@ void run_packets(Ctx& c) {
 }
 
 void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
+  RtScope rt_all(c, RT_CALCDERIVS, true, !mf_only);   // derivatives.f90:92-476
   const bool gwp = !c.modes_gwp.empty();
   if (gwp) gwp_setup_run(c);
   if (c.d_in32) {
@@ -2042,11 +2087,13 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
     c.count();
   }
   {
+    RtScope rt(c, RT_H1MODE);
     ProfScope ps(c, KP_H1);
     launch_h1(c.h1_d, (int)c.h1_h.size(), c.h1_maxn2, c.h1_smem, true, c.st, c.precision);
     launch_matsum(c.msum_d, (int)c.msum_h.size(), c.msum_src_d, c.st);
     c.count(3);
   }
+  RtScope rt_mf(c, RT_MEANFIELD);   // gmctdh_objects.f90:511-1140
   // the deepest level holds only the full products H_t A of the right chains (dA)
   const size_t depth_end = mf_only ? c.chains.size() - 1 : c.chains.size();
   for (size_t i = 1; i < depth_end; ++i) run_prod(c, c.chains[i]);
@@ -2069,6 +2116,7 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
     c.count();
   }
   {
+    RtScope rt(c, RT_SPF_DVR);
     ProfScope ps(c, KP_SPF);
     launch_spf(c.spf_d, (int)c.spf_h.size(), c.spf_tiles, c.spfop_d, out, c.der, c.d_status, c.st, c.precision, c.spf_nf);
     c.count(3);
@@ -2088,6 +2136,7 @@ void eom_from(Ctx& c, const cplx* y, cplx* out) {
 }
 
 void run_ovl(Ctx& c, OvlPlan& P) {
+  RtScope rt(c, RT_OVL);   // norm_wf / WF_Ovl / DeltaPsi
   if (!P.gwp_h.empty()) {
     launch_gwp_ovl(P.gwp_d, (int)P.gwp_h.size(), c.st);
     c.count();
@@ -2638,6 +2687,7 @@ struct LanRun {
 };
 
 void lan_issue(Ctx& c, LanRun& R) {
+  RtScope rt(c, RT_LANCZOS, false);   // Lanczos (cmf2_integration.f90:30-103): the Krylov steps
   const long long n = c.naconftot;
   cplx* K = c.d_krylov;
   double* d_alpha = c.d_lan;
@@ -2692,6 +2742,7 @@ void lan_check(Ctx& c, LanRun& R) {
 }
 
 void lan_finish(Ctx& c, LanRun& R) {
+  RtScope rt(c, RT_LANCZOS);   // one call per Lanczos run
   const int nk = R.nk;
   launch_jacobi_tridiag(c.d_lan, c.d_lan + NKRYLOV_MAX, nk, c.d_lan + 2 * NKRYLOV_MAX,
                         c.d_lan + 3 * NKRYLOV_MAX, c.d_status, c.st);
@@ -2708,6 +2759,7 @@ void lan_finish(Ctx& c, LanRun& R) {
 
 // BT = sum_j BK_j * (sum_r U_jr U_1r exp(f alpha_r dt)), renormalised (:85-99)
 void lan_combine(Ctx& c, cplx* BT, double dt) {
+  RtScope rt(c, RT_LANCZOS, false);
   const long long n = c.naconftot;
   const int nk = c.lan_nk;
   std::vector<cplx> coef(nk, mkc(0, 0));
@@ -2759,6 +2811,7 @@ void copy_dev(Ctx& c, cplx* dst, const cplx* src, long long n) {
 
 // h1mode only (no mean fields) on the SPFs of y: used before the back-propagation.
 void h1_only(Ctx& c, const cplx* y) {
+  RtScope rt(c, RT_H1MODE);
   copy_dev(c, c.d_in + c.naconftot, y + c.naconftot, c.dimpsi);
   if (!c.modes_gwp.empty()) {
     // Calc_S00 and Calc_h1mode of the Gaussian modes (cmf2_base.f90:158-163)
@@ -2869,6 +2922,7 @@ void stage_D(Ctx& c, CmfState& S, cplx* out, const cplx* base, const double* coe
 // Tikhonov solve (der_factor * x into out) and dD = -tau D into Dout.
 void spf_eval_all(Ctx& c, CmfState& S, cplx* out, cplx* Dout) {
   if (!c.modes_dvr.empty()) {
+    RtScope rt(c, RT_SPF_DVR);   // Calc_Der_SPF (cmf2_derivatives.f90:84-235), h1 refresh included
     {
       ProfScope ps(c, KP_H1);
       launch_h1(S.h1_d, (int)S.h1.size(), c.h1_maxn2, c.h1_smem, false, c.st, c.precision);
@@ -2880,6 +2934,7 @@ void spf_eval_all(Ctx& c, CmfState& S, cplx* out, cplx* Dout) {
     c.count(4);
   }
   if (S.gwp) {
+    RtScope rt(c, RT_SPF_GWP);
     gwp_setup_run(c);
     gwp_solve_run(c, out);
     ProfScope ps(c, KP_GWP);
@@ -5054,6 +5109,58 @@ int64_t mctdh_event_elapsed(mctdh_ctx_t* ctx, int64_t s0, int64_t s1, double* ms
     float f = 0;
     CK(cudaEventElapsedTime(&f, c->user_ev[s0], c->user_ev[s1]));
     *ms = f;
+  });
+}
+
+int64_t mctdh_timing(mctdh_ctx_t* ctx, int64_t mode) {
+  if (!ctx || mode < 0 || mode > 2) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    drain_timing(*c);
+    if (mode == 2) {
+      for (int i = 0; i < 8; ++i) {
+        c->rt_ms[i] = 0.0;
+        c->rt_calls[i] = 0;
+      }
+    }
+    c->timing = mode != 0;
+  });
+}
+
+int64_t mctdh_timing_read(mctdh_ctx_t* ctx, int64_t timer, int64_t* calls, double* ms) {
+  if (!ctx || timer < 1 || timer > 8) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    drain_timing(*c);
+    if (calls) *calls = c->rt_calls[timer - 1];
+    if (ms) *ms = c->rt_ms[timer - 1];
+  });
+}
+
+// The `timing` file of write_timings (timingmod.f90:72-103): total wall time,
+// then per routine the calls, ms per call, minutes and % of the wall time, with
+// the routine times measured on the device.
+int64_t mctdh_write_timings(mctdh_ctx_t* ctx, const char* path, double walltime_s) {
+  if (!ctx || !path || !(walltime_s > 0.0)) return MCTDH_EARG;
+  Ctx* c = ctx->c;
+  return guarded(c, [&] {
+    drain_timing(*c);
+    static const char* names[8] = {"CalcDerivs",  "normWF/wf_ovl",    "Calc_MeanField",   "Calc_CY",
+                                   "Calc_h1mode", "Calc_Der_SPF_DVR", "Calc_Der_SPF_GWP", "Lanczos"};
+    FILE* fp = fopen(path, "w");
+    if (!fp) throw StatusError(MCTDH_EARG, std::string("cannot open ") + path);
+    const int h = (int)(walltime_s / 3600.0);
+    const int m = (int)((walltime_s - h * 3600.0) / 60.0);
+    const int sec = (int)(walltime_s - h * 3600.0 - m * 60.0);
+    fprintf(fp, "Total time:   %d h   %d m   %d s\n \n \n", h, m, sec);
+    fprintf(fp, "          Subroutine    Calls N    time/N [ms]      time [min]    %%time\n \n");
+    for (int i = 0; i < 8; ++i) {
+      const long long n = c->rt_calls[i];
+      const double sub = c->rt_ms[i] * 1e-3;
+      const double per = n > 0 ? sub / (double)n * 1000.0 : 0.0;
+      fprintf(fp, "%20s    %7lld   %9.2f   %11.2f      %6.2f\n", names[i], n, per, sub / 60.0, sub / walltime_s * 100.0);
+    }
+    fclose(fp);
   });
 }
 
