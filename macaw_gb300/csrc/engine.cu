@@ -465,6 +465,9 @@ struct Ctx {
   cplx* d_hbin = nullptr;
   cplx* d_hbin32 = nullptr;   // precision 1: d_hbin as complex FP32, the input of the H_B products
   cplx* d_in32 = nullptr;     // precision 1: the coefficients of d_in as complex FP32 (chain inputs)
+  // compensated contractions (and precision-2 chains): the coefficients of d_in as
+  // FP32 split pairs, converted once per evaluation instead of at every staging
+  cplx* d_insplit = nullptr;
   FusedDot hb_dot{nullptr, nullptr, nullptr, nullptr};    // <d_hbin | H_B d_hbin> in the term sum
   FusedDot lan_nrm{nullptr, nullptr, nullptr, nullptr};   // ||Kn||^2 in the Lanczos axpy
   std::vector<ProdBatch> hb_chains;
@@ -1109,6 +1112,13 @@ void plan_eom(Ctx& c) {
   c.xh1_d = upload_vec(c.ar, c.xh1_h);
   if (!c.modes_gwp.empty()) plan_gwp_setup(c);
 
+  if (c.hole_prec == 2 && !c.member && c.modes_gwp.empty() && !c.mixture)
+    c.d_insplit = c.ar.calloc_c(c.naconftot);
+  // the contractions' operand for A itself: its split copy where there is one
+  auto hole_in = [&](const cplx* p, int fmt, int s) -> std::pair<const cplx*, int> {
+    if (c.d_insplit && p == c.d_in + c.aoff[s]) return std::make_pair((const cplx*)(c.d_insplit + c.aoff[s]), (int)TF_SPLIT);
+    return std::make_pair(p, fmt);
+  };
   // density matrices (Calc_rho1mode, gmctdh_objects.f90:408-477)
   std::vector<HoleRef> hrefs;       // mean-field contractions (c.holes)
   std::vector<HoleRef> rrefs;       // density-matrix contractions (c.rho_holes, FP64)
@@ -1133,8 +1143,9 @@ void plan_eom(Ctx& c) {
         if (!weighted.count(key)) weighted[key] = plan_s_weighted(c, s, key.second);
         Y = weighted[key];
       }
-      int hidx = c.rho_holes.add(c.ar, Y, c.d_in + c.aoff[s], prod_range(sh, 0, m),
-                                 prod_range(sh, m + 1, (int)sh.size()), n, n);
+      const auto hy = hole_in(Y, TF_C64, s), hx = hole_in(c.d_in + c.aoff[s], TF_C64, s);
+      int hidx = c.rho_holes.add(c.ar, hy.first, hx.first, prod_range(sh, 0, m),
+                                 prod_range(sh, m + 1, (int)sh.size()), n, n, hy.second, hx.second);
       rho_hole[m][s] = hidx;
       int tg = c.red.add_target(c.rho[m][s], n, n, n, 1);
       rrefs.push_back(HoleRef{hidx, tg, mkc(1, 0)});
@@ -1160,6 +1171,8 @@ void plan_eom(Ctx& c) {
     if (c.d_in32 && X.p == c.d_in + c.aoff[s])   // 8-byte elements: offsets count float2
       return std::make_pair(reinterpret_cast<const cplx*>(reinterpret_cast<float2*>(c.d_in32) + c.aoff[s]),
                             (int)TF_F32);
+    if (c.precision == 2 && c.d_insplit && X.p == c.d_in + c.aoff[s])
+      return std::make_pair((const cplx*)(c.d_insplit + c.aoff[s]), (int)TF_SPLIT);
     return std::make_pair((const cplx*)X.p, X.fmt);
   };
   std::map<std::pair<int, int>, int> mf_target;   // (m,k) -> red target
@@ -1360,7 +1373,9 @@ void plan_eom(Ctx& c) {
       const TRef& X = L[im];
       const TRef& Y = R[f - 1 - im];
       long long Ll = prod_range(X.shape, 0, im), Rr = prod_range(X.shape, im + 1, (int)X.shape.size());
-      int hidx = c.holes.add(c.ar, X.p, Y.p, Ll, Rr, X.shape[im], Y.shape[im], X.fmt, Y.fmt);
+      const auto hx = c.mf_hole_prec == 2 ? hole_in(X.p, X.fmt, s1) : std::make_pair((const cplx*)X.p, X.fmt);
+      const auto hy = c.mf_hole_prec == 2 ? hole_in(Y.p, Y.fmt, s2) : std::make_pair((const cplx*)Y.p, Y.fmt);
+      int hidx = c.holes.add(c.ar, hx.first, hy.first, Ll, Rr, X.shape[im], Y.shape[im], hx.second, hy.second);
       term_hole[std::make_pair(t, im)] = hidx;
       hrefs.push_back(HoleRef{hidx, mf_tg(im, k), c.ae[t]});
     }
@@ -2084,6 +2099,10 @@ void eom(Ctx& c, cplx* out, bool mf_only = false, bool reginv = true) {
   if (gwp) gwp_setup_run(c);
   if (c.d_in32) {
     launch_to_f32(c.d_in32, c.d_in, c.naconftot, c.st);
+    c.count();
+  }
+  if (c.d_insplit) {
+    launch_to_split(c.d_insplit, c.d_in, c.naconftot, c.st);
     c.count();
   }
   {
@@ -3635,6 +3654,10 @@ void cmf2(Ctx& c, double t, double htry, double* hdid_out, double* hnext_out, lo
       // would magnify a prediction error in the weakly occupied directions by up to
       // 1 / eps_rho^2); the mean fields come from the prediction
       copy_dev(c, c.d_in, c.d_y, c.naconftot);
+      if (c.d_insplit) {
+        launch_to_split(c.d_insplit, c.d_in, c.naconftot, c.st);
+        c.count();
+      }
       run_hole(c, c.rho_holes);
       run_red(c, c.red);
       launch_snap(M->segs_d, (int)M->segs_h.size(), M->pred0, M->E, 2, c.st);

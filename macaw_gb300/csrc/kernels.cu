@@ -1841,6 +1841,21 @@ __global__ void to_f32_kernel(float2* __restrict__ out, const cplx* __restrict__
   split_d2f(v.y, hy, ly);
   out[i] = make_float2(hx + lx, hy + ly);
 }
+// complex128 -> FP32 split pairs (re hi, im hi, re lo, im lo), the exact split
+// of load_split done once per element
+__global__ void to_split_kernel(float4* __restrict__ out, const cplx* __restrict__ in, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cplx v = in[i];
+  float4 w;
+  split_d2f(v.x, w.x, w.z);
+  split_d2f(v.y, w.y, w.w);
+  out[i] = w;
+}
+void launch_to_split(cplx* out, const cplx* in, long long n, cudaStream_t st) {
+  if (n <= 0) return;
+  to_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<float4*>(out), in, n);
+}
 void launch_to_f32(cplx* out, const cplx* in, long long n, cudaStream_t st) {
   if (n <= 0) return;
   to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<float2*>(out), in, n);

@@ -327,6 +327,7 @@ void launch_copy_scale(cplx* out, const cplx* in, cplx s, long long n, cudaStrea
 void launch_axpy(cplx* y, const cplx* x, cplx a, long long n, cudaStream_t st);
 // out (complex FP32, TF_F32 storage) = in rounded to nearest
 void launch_to_f32(cplx* out, const cplx* in, long long n, cudaStream_t st);
+void launch_to_split(cplx* out, const cplx* in, long long n, cudaStream_t st);
 void launch_gemv_cols(cplx* out, const cplx* basis, long long ld, const cplx* coef, int ncol, long long n,
                       cudaStream_t st);
 void launch_jacobi_tridiag(const double* alpha, const double* beta, int n, double* evals, double* evecs,
