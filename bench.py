@@ -478,7 +478,7 @@ def run_gpu(args):
     hd, hn = C.c_double(), C.c_double()
     e2e_fs, e2e_s = 0.0, 0.0
     te, he = head["t"], head["h"]
-    for _ in range(max(1, args.steps // 2)):
+    for _ in range(max(1, args.steps)):
         flush_l2(l2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
