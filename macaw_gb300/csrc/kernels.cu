@@ -110,12 +110,7 @@ __device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, i
     }
   }
   __syncthreads();
-  // PREC 1: two threads per fibre (256-thread blocks), each computing every second
-  // output: twice the warps in flight for these load-latency-bound products; the
-  // pair's input loads are the same addresses (one transaction)
-  constexpr int TPF = PREC == 1 ? 2 : 1;
-  const int half = (int)threadIdx.x % TPF;
-  const long long p = (bb - d.block_start) * 128 + (long long)(threadIdx.x / TPF);
+  const long long p = (bb - d.block_start) * blockDim.x + threadIdx.x;
   const long long L = d.L, nfib = L * d.R;
   if (p >= nfib) return;
   long long l, r;
@@ -150,7 +145,7 @@ __device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, i
     }
     const bool unit_alpha = (alpha.x == 1.0 && alpha.y == 0.0);
     float4* y0f = reinterpret_cast<float4*>(y0);
-    for (int jo = half; jo < nout; jo += TPF) {
+    for (int jo = 0; jo < nout; ++jo) {
       cplx accd;
       if (PREC == 1) {
         // FP32 values rounded to nearest: hi + lo of the split, added in FP32
@@ -193,13 +188,13 @@ __device__ __forceinline__ void prod_block(const ProdDesc* __restrict__ descs, i
 }
 
 template <int MAXN, int PREC>
-__global__ void __launch_bounds__(PREC == 1 ? 256 : 128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
+__global__ void __launch_bounds__(128) prod_kernel(const ProdDesc* __restrict__ descs, int ndesc) {
   prod_block<MAXN, PREC>(descs, ndesc, (long long)blockIdx.x);
 }
 
 // Persistent form: gridDim.x CTAs walk the batch's blocks in a fixed stride.
 template <int MAXN, int PREC>
-__global__ void __launch_bounds__(PREC == 1 ? 256 : 128) prod_kernel_persistent(const ProdDesc* __restrict__ descs, int ndesc,
+__global__ void __launch_bounds__(128) prod_kernel_persistent(const ProdDesc* __restrict__ descs, int ndesc,
                                                               long long nblocks) {
   for (long long bb = blockIdx.x; bb < nblocks; bb += gridDim.x) {
     prod_block<MAXN, PREC>(descs, ndesc, bb);
@@ -229,15 +224,15 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
     const unsigned g = (unsigned)persist;
     if (maxn <= 8) {
       if (prec == 0) prod_kernel_persistent<8, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
-      else if (prec == 1) prod_kernel_persistent<8, 1><<<g, 256, 0, st>>>(d_descs, ndesc, nblocks);
+      else if (prec == 1) prod_kernel_persistent<8, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
       else prod_kernel_persistent<8, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
     } else if (maxn <= 12) {
       if (prec == 0) prod_kernel_persistent<12, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
-      else if (prec == 1) prod_kernel_persistent<12, 1><<<g, 256, 0, st>>>(d_descs, ndesc, nblocks);
+      else if (prec == 1) prod_kernel_persistent<12, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
       else prod_kernel_persistent<12, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
     } else {
       if (prec == 0) prod_kernel_persistent<MAXN_SPF, 0><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
-      else if (prec == 1) prod_kernel_persistent<MAXN_SPF, 1><<<g, 256, 0, st>>>(d_descs, ndesc, nblocks);
+      else if (prec == 1) prod_kernel_persistent<MAXN_SPF, 1><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
       else prod_kernel_persistent<MAXN_SPF, 2><<<g, 128, 0, st>>>(d_descs, ndesc, nblocks);
     }
     return;
@@ -247,15 +242,15 @@ void launch_prod(const ProdDesc* d_descs, int ndesc, long long nblocks, int maxn
   // iterations and fewer registers (more resident warps) at 8 SPFs and below
   if (maxn <= 8) {
     if (prec == 0) prod_kernel<8, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
-    else if (prec == 1) prod_kernel<8, 1><<<nb, 256, 0, st>>>(d_descs, ndesc);
+    else if (prec == 1) prod_kernel<8, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
     else prod_kernel<8, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
   } else if (maxn <= 12) {
     if (prec == 0) prod_kernel<12, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
-    else if (prec == 1) prod_kernel<12, 1><<<nb, 256, 0, st>>>(d_descs, ndesc);
+    else if (prec == 1) prod_kernel<12, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
     else prod_kernel<12, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
   } else {
     if (prec == 0) prod_kernel<MAXN_SPF, 0><<<nb, 128, 0, st>>>(d_descs, ndesc);
-    else if (prec == 1) prod_kernel<MAXN_SPF, 1><<<nb, 256, 0, st>>>(d_descs, ndesc);
+    else if (prec == 1) prod_kernel<MAXN_SPF, 1><<<nb, 128, 0, st>>>(d_descs, ndesc);
     else prod_kernel<MAXN_SPF, 2><<<nb, 128, 0, st>>>(d_descs, ndesc);
   }
 }
