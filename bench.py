@@ -324,6 +324,8 @@ def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mf
     for _ in range(warm):
         hdid, h, _ = core.step(INT_CMF2, t, h)
         t += hdid
+    # the state the timed steps start from (the e2e leg repeats the same steps)
+    start = (*core.get_state(), t, h)
     c0 = core.counters()
     barrier(tdist)
     torch.cuda.synchronize()
@@ -348,7 +350,7 @@ def run_arm(model, precision, state, t0, h0, args, l2, torch, tdist, profile, mf
         prof_ms = core.event_elapsed(0, 1)
         prof = core.profile_read()
         core.profile(0)
-    return core, dict(t=t, h=h, ms=ms, fs=fs, hdids=hdids, prof=prof, prof_ms=prof_ms,
+    return core, dict(t=t, h=h, ms=ms, fs=fs, hdids=hdids, prof=prof, prof_ms=prof_ms, start=start,
                       eom=c1["eom"] - c0["eom"], hb=c1["hb"] - c0["hb"], launches=c1["launches"] - c0["launches"])
 
 
@@ -469,15 +471,16 @@ def run_gpu(args):
     value = mfx_value if head_is_mfx else split_value
 
     # e2e: the reference-facing host-buffer call (mctdh_cmf2) of the headline arm
-    # with pinned buffers, host<->device copies of A and psi inside every step
-    Ah, ph = head_core.get_state()
+    # with pinned buffers, host<->device copies of A and psi inside every step,
+    # over the same steps as the device-timed ones (from the same state, the same
+    # step sequence)
+    Ah, ph, te, he = head["start"]
     pA = torch.from_numpy(Ah.copy()).pin_memory()
     pP = torch.from_numpy(ph.copy()).pin_memory()
     import ctypes as C
     DPp = C.POINTER(C.c_double)
     hd, hn = C.c_double(), C.c_double()
     e2e_fs, e2e_s = 0.0, 0.0
-    te, he = head["t"], head["h"]
     for _ in range(max(1, args.steps)):
         flush_l2(l2)
         torch.cuda.synchronize()
