@@ -51,3 +51,40 @@ def test_ratios_and_scale():
     rows = X[k == k.min()]
     pair = np.hypot(rows[:, 8], rows[:, 9]) + np.hypot(rows[:, 10], rows[:, 11])
     np.testing.assert_allclose(pair, 1.0, rtol=1e-9)
+
+
+def test_build_datasets_offsets_runs():
+    """Several recorded runs: rows concatenated in run order, every run's step
+    indices after the previous run's, so train()'s held-back part is the last run."""
+    runs = [_poly_history(3, n=10, seed=s) for s in (1, 2, 3)]
+    X, R, k = mfx.build_datasets(runs)
+    parts = [mfx.build_dataset(*r) for r in runs]
+    assert len(X) == sum(len(p[0]) for p in parts)
+    np.testing.assert_array_equal(X[:len(parts[0][0])], parts[0][0])
+    off, start = 0, 0
+    for Xp, Rp, kp in parts:
+        sl = slice(start, start + len(kp))
+        np.testing.assert_array_equal(k[sl], kp + off)
+        np.testing.assert_array_equal(R[sl], Rp)
+        assert start == 0 or k[sl].min() > k[start - 1]
+        off += int(kp.max()) + 1
+        start += len(kp)
+
+
+def test_variant_states_are_seeded_displacements():
+    """Variant 0 is the model's own initial state; the others displace every
+    initial Gaussian (normalised wavefunctions, reproducible from the seed, the
+    model left unchanged)."""
+    from macaw_gb300.model import initial_wavefunction
+    from tests.helpers import small_qvc
+    model = small_qvc()
+    before = dict(model.init_spf)
+    a = mfx.variant_states(model, 3, seed=5)
+    b = mfx.variant_states(model, 3, seed=5)
+    assert model.init_spf == before
+    A0, p0 = initial_wavefunction(model)
+    np.testing.assert_array_equal(a[0][1], p0)
+    np.testing.assert_array_equal(a[0][0], A0)
+    for (Aa, pa), (Ab, pb) in zip(a, b):
+        np.testing.assert_array_equal(pa, pb)
+    assert np.abs(a[1][1] - p0).max() > 1e-3 and np.abs(a[2][1] - a[1][1]).max() > 1e-3
