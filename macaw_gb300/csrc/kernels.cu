@@ -797,11 +797,7 @@ __device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, JacRot* R, bool* ok
           const cplx apq = A[p + ld * q];
           const double m2 = cabs2(apq);
           const double app = A[p + ld * p].x, aqq = A[q + ld * q].x;
-          // rotate while |a_pq| is above both FP64 rounding relative to the pair
-          // (1e-16 sqrt|a_pp a_qq|) and the rounding floor of the whole matrix
-          // (4e-16 |A|_F): between a large and a tiny diagonal entry the relative
-          // bound alone sits below the noise the other rotations leave behind
-          rot = (m2 > 1.6e-31 * fro2) && (m2 > 1e-32 * fabs(app * aqq));
+          rot = (m2 > 1e-38 * fro2) && (m2 > 1e-32 * fabs(app * aqq));
           if (rot) {
             // one reciprocal square root for |a_pq| (the FP64 pipe is the bottleneck here)
             const double rm = rsqrt(m2);
