@@ -858,8 +858,12 @@ __device__ void jacobi_herm(cplx* A, cplx* V, int n, int ld, JacRot* R, bool* ok
   *ok = converged;
 }
 
-__global__ void __launch_bounds__(32) reginv_kernel(const RegInvDesc* __restrict__ descs, const MFOp* __restrict__ ops,
-                                                    int* status) {
+// Four warps per (mode, state): the Jacobi sweeps run on the first (its
+// rotations are one round per warp-wide step), the warm-start products, the
+// regularised inverse and the rho^-1 MF products on all four (independent
+// FP64 dot products, so more of them in flight against the FP64 latency).
+__global__ void __launch_bounds__(128) reginv_kernel(const RegInvDesc* __restrict__ descs, const MFOp* __restrict__ ops,
+                                                     int* status) {
   __shared__ cplx A[MAXN_SPF * MAXN_SPF];
   __shared__ cplx V[MAXN_SPF * MAXN_SPF];
   __shared__ cplx Inv[MAXN_SPF * MAXN_SPF];
@@ -906,8 +910,9 @@ __global__ void __launch_bounds__(32) reginv_kernel(const RegInvDesc* __restrict
     }
     __syncthreads();
   }
-  bool ok;
-  jacobi_herm(A, V, n, ld, R, &ok);
+  bool ok = true;
+  if (threadIdx.x < 32) jacobi_herm(A, V, n, ld, R, &ok);
+  __syncthreads();
   if (!ok && threadIdx.x == 0) atomicOr(status, DEVST_EIG_NOCONV);
   if (warm) {
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // Inv <- Vp V
@@ -961,7 +966,7 @@ __global__ void __launch_bounds__(32) reginv_kernel(const RegInvDesc* __restrict
 
 void launch_reginv(const RegInvDesc* d_descs, int ndesc, const MFOp* d_ops, int* d_status, cudaStream_t st) {
   if (ndesc <= 0) return;
-  reginv_kernel<<<ndesc, 32, 0, st>>>(d_descs, d_ops, d_status);
+  reginv_kernel<<<ndesc, 128, 0, st>>>(d_descs, d_ops, d_status);
 }
 
 // ---------------------------------------------------------------------------
