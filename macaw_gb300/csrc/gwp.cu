@@ -361,7 +361,8 @@ __device__ cplx warp_sum(cplx v) {
 
 // One panel of the Householder QR of M (2nG x (nG+1), the last column the
 // right-hand side).  Shared: the panel rows j0.. of columns j0..j0+pw-1.
-__global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __restrict__ descs, int j0) {
+// cpb: trailing columns per block (one warp each, cpb <= 8)
+__global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __restrict__ descs, int j0, int cpb) {
   extern __shared__ cplx P[];
   __shared__ double red[33];
   __shared__ cplx s_alpha[GWP_QR_PW];
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __re
   const int pw = min(GWP_QR_PW, nG - j0);
   const int ncol = nG + 1;
   const int trailing = ncol - (j0 + pw);
-  const int nblk = (trailing + 7) / 8;
+  const int nblk = (trailing + cpb - 1) / cpb;
   if ((int)blockIdx.x > 0 && (int)blockIdx.x >= nblk) return;
   const long long ld = 2LL * nG;
   const int rows = 2 * nG - j0;
@@ -419,8 +420,8 @@ __global__ void __launch_bounds__(256) gwp_qr_panel_kernel(const GwpCYDesc* __re
     __syncthreads();
   }
   // trailing columns of this block (the right-hand side is column nG)
-  const int c = j0 + pw + blockIdx.x * 8 + warp;
-  if (c < ncol) {
+  const int c = j0 + pw + blockIdx.x * cpb + warp;
+  if (warp < cpb && c < ncol) {
     cplx* y = d.M + ld * c;
     for (int jj = 0; jj < pw; ++jj) {
       if (s_tau[jj] == 0.0) continue;
@@ -875,10 +876,22 @@ void launch_gwp_solve(const GwpCYDesc* d, int nd, int maxG, cplx der, cplx* out,
     cudaFuncSetAttribute(gwp_qr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = smem;
   }
+  // the trailing columns spread over at most one block per SM (every block
+  // factors the panel itself, so more blocks than SMs would share an SM's FP64
+  // pipe), at most eight per block
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 152;
+  }
   for (int j0 = 0; j0 < maxG; j0 += GWP_QR_PW) {
     const int trailing = maxG + 1 - j0 - GWP_QR_PW;
-    const unsigned nblk = (unsigned)std::max(1, (trailing + 7) / 8);
-    gwp_qr_panel_kernel<<<dim3(nblk, nd), 256, smem, st>>>(d, j0);
+    const int per_desc = std::max(1, nsm / nd);
+    const int cpb = std::min(8, std::max(1, (trailing + per_desc - 1) / per_desc));
+    const unsigned nblk = (unsigned)std::max(1, (trailing + cpb - 1) / cpb);
+    gwp_qr_panel_kernel<<<dim3(nblk, nd), 256, smem, st>>>(d, j0, cpb);
   }
   gwp_backsub_kernel<<<nd, 256, sizeof(cplx) * 2 * maxG, st>>>(d, der, out, status);
 }
