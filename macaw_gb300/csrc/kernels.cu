@@ -316,10 +316,20 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
   // each staged value it reads feeds two products (half the shared-memory reads
   // per product and four independent accumulation chains)
   const bool quad = PREC == 2 && small && ((n1 | n2) & 1) == 0;
-  const int h1 = n1 >> 1, nq = h1 * (n2 >> 1);
+  // X = Y (density matrices, SPF overlaps): C is Hermitian, so only the blocks on
+  // and above the diagonal are computed (the others are their conjugates) and the
+  // tensor is staged once
+  const bool sym = quad && d.X == d.Y && n1 == n2 && d.xfmt == d.yfmt;
+  const int h1 = n1 >> 1, nq = sym ? h1 * (h1 + 1) / 2 : h1 * (n2 >> 1);
   const int Gq = quad ? HOLE_THREADS / nq : 0;
   const int qd = quad ? tid % nq : 0, gq = quad ? tid / nq : 0;
-  const int i1 = 2 * (qd % (h1 > 0 ? h1 : 1)), i2 = 2 * (qd / (h1 > 0 ? h1 : 1));
+  int i1 = 2 * (qd % (h1 > 0 ? h1 : 1)), i2 = 2 * (qd / (h1 > 0 ? h1 : 1));
+  if (sym) {   // qd -> (qi <= qj), qj-major: qd = qj (qj + 1) / 2 + qi
+    int rem = qd, qj = 0;
+    while (rem > qj) { rem -= qj + 1; ++qj; }
+    i1 = 2 * rem;
+    i2 = 2 * qj;
+  }
   cplx acc[4] = {mkc(0, 0), mkc(0, 0), mkc(0, 0), mkc(0, 0)};
   float ah[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   float al[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
@@ -352,7 +362,7 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
         Xf[q * MAXN_SPF + j] = (idx >= 0) ? load_split(d.X, idx, d.xfmt) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    for (int j = jt; j < n2; j += jstep) {
+    for (int j = jt; j < (sym ? 0 : n2); j += jstep) {
       const long long idx = in_range ? yb + L * j : -1;
       if (PREC == 0) {
         Ys[q * MAXN_SPF + j] = (idx >= 0) ? load_c(d.Y, idx, d.yfmt) : mkc(0, 0);
@@ -366,18 +376,20 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
     __syncthreads();
     if (quad) {
       // pairs (i1, i2), (i1 + 1, i2), (i1, i2 + 1), (i1 + 1, i2 + 1) in ah/al[0..3]
+      const float2* Y1r = sym ? X1 : Y1;
+      const float4* Yfr = sym ? Xf : Yf;
       if (gq < Gq) {
         for (int q = gq; q < HOLE_TILE; q += Gq) {
           if (f32in) {
             const float2 xa = X1[q * MAXN_SPF + i1], xb = X1[q * MAXN_SPF + i1 + 1];
-            const float2 ya = Y1[q * MAXN_SPF + i2], yb = Y1[q * MAXN_SPF + i2 + 1];
+            const float2 ya = Y1r[q * MAXN_SPF + i2], yb = Y1r[q * MAXN_SPF + i2 + 1];
             df_cfma0(ah[0], al[0], xa, ya);
             df_cfma0(ah[1], al[1], xb, ya);
             df_cfma0(ah[2], al[2], xa, yb);
             df_cfma0(ah[3], al[3], xb, yb);
           } else {
             const float4 xa = Xf[q * MAXN_SPF + i1], xb = Xf[q * MAXN_SPF + i1 + 1];
-            const float4 ya = Yf[q * MAXN_SPF + i2], yb = Yf[q * MAXN_SPF + i2 + 1];
+            const float4 ya = Yfr[q * MAXN_SPF + i2], yb = Yfr[q * MAXN_SPF + i2 + 1];
             df_cfma(ah[0], al[0], xa, ya);
             df_cfma(ah[1], al[1], xb, ya);
             df_cfma(ah[2], al[2], xa, yb);
@@ -440,11 +452,14 @@ __device__ __forceinline__ void hole_block(const HoleDesc* __restrict__ descs, i
     for (int k = 0; k < 4; ++k) red[4 * tid + k] = acc[k];
     __syncthreads();
     if (tid < npairs) {
-      const int j1 = tid % n1, j2 = tid / n1;
-      const int qq = (j1 >> 1) + h1 * (j2 >> 1), k = (j1 & 1) + 2 * (j2 & 1);
+      int j1 = tid % n1, j2 = tid / n1;
+      const bool lower = sym && (j1 >> 1) > (j2 >> 1);   // conj of the transposed pair
+      if (lower) { const int tmp = j1; j1 = j2; j2 = tmp; }
+      const int qq = sym ? (j2 >> 1) * ((j2 >> 1) + 1) / 2 + (j1 >> 1) : (j1 >> 1) + h1 * (j2 >> 1);
+      const int k = (j1 & 1) + 2 * (j2 & 1);
       cplx s = mkc(0, 0);
       for (int gg = 0; gg < Gq; ++gg) s = cadd(s, red[4 * (gg * nq + qq) + k]);
-      out[tid] = s;
+      out[tid] = lower ? cconj(s) : s;
     }
   } else if (small) {
     cplx* red = Xs;   // reuse (HOLE_TILE*MAXN_SPF >= HOLE_THREADS)
