@@ -2872,6 +2872,12 @@ struct CmfState {
   SnapSeg* opseg_d = nullptr;
   long long opE = 0;
   cplx* opsave = nullptr;
+  // the Krylov space of the step-start Lanczos run (its vectors, alpha and beta):
+  // a retry from the same state with a shorter step uses its leading vectors
+  cplx* krylov0 = nullptr;
+  double* lan0 = nullptr;
+  std::vector<double> beta0;
+  bool k0_valid = false;
   // Gaussian modes (cmf2_base.f90): the D matrices of every (mode, set) block,
   // concatenated into one vector per role; B = D^H S A is the propagated vector
   bool gwp = false;
@@ -3135,6 +3141,8 @@ void plan_cmf(Ctx& c, CmfState& S) {
       S.opseg_d = upload_vec(c.ar, S.opseg_h);
       S.opsave = c.ar.calloc_c(off);
     }
+    S.krylov0 = c.ar.calloc_c(c.naconftot * (NKRYLOV_MAX + 1));
+    S.lan0 = (double*)c.ar.alloc(sizeof(double) * (3 * NKRYLOV_MAX + NKRYLOV_MAX * NKRYLOV_MAX));
   }
   S.elem_mode = upload_vec(c.ar, em);
   // the SPF error norms: compensated split FP32 (~1e-13) in the split modes
@@ -3487,6 +3495,45 @@ void mfx_push_half(Ctx& c, MfxState& M, double th) {
 // One CMF2 attempt of length hdid from d_y (cmf2_base.f90:76-176); returns
 // max(err_A, err_psi) / eps_int and leaves BHalf / psiHalf2 for cmf2_accept.
 // ops_fresh: the operators and mean fields at d_y are already in place.
+// The step-start Lanczos run works on the saved Krylov space (vectors and
+// alpha/beta): the context's pointers are swapped for the scope.
+struct KrylovScope {
+  Ctx& c;
+  cplx* k;
+  double* l;
+  KrylovScope(Ctx& cc, cplx* k0, double* l0) : c(cc), k(cc.d_krylov), l(cc.d_lan) {
+    if (k0) {
+      c.d_krylov = k0;
+      c.d_lan = l0;
+    }
+  }
+  ~KrylovScope() {
+    c.d_krylov = k;
+    c.d_lan = l;
+  }
+};
+
+// The Krylov size at which a build from the same vector and operator stops for
+// the step dt (lan_check's rule, cmf2_integration.f90:64-80) from the saved
+// betas; 0 when they do not reach it.
+int lan_reuse_count(const std::vector<double>& beta, double dt) {
+  if (beta.empty()) return 0;
+  double error = beta[0] * fabs(dt);
+  for (int j = 2; j <= (int)beta.size(); ++j) {
+    error = error * beta[j - 1] / (double)j * fabs(dt);
+    if (error < EPS_B) return j;
+  }
+  return 0;
+}
+
+// after lan_finish of a step-start build: keep its betas for the retries
+void lan_record(Ctx& c, CmfState& S) {
+  if (!S.krylov0) return;
+  const double* h_beta = c.h_scal + 64;
+  S.beta0.assign(h_beta, h_beta + c.lan_nk);
+  S.k0_valid = true;
+}
+
 double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_done, bool ops_saved = false) {
   if (c.mixture)
     throw StatusError(MCTDH_EUNSUPPORTED, "CMF2 covers a single wave packet without dissipation (use rk45, dopri, abm or bs)");
@@ -3520,11 +3567,29 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_d
   }
   copy_dev(c, S.psiHalf, c.d_y, c.ntot);
   if (S.gwp) copy_dev(c, S.DDHalf, S.DD0, S.nD);
+  // A retry from the same state (ops_saved) runs the step-start Lanczos on the
+  // Krylov space of the rejected attempt's: the same B0 and operator give the
+  // same vectors, alpha and beta, and a shorter step stops the build earlier, at
+  // the size lan_reuse_count finds among the saved betas.
+  const int nk_reuse = (ops_saved && S.k0_valid && S.krylov0) ? lan_reuse_count(S.beta0, 0.5 * hdid) : 0;
+  if (!ops_saved) S.k0_valid = false;
   if (!overlap) {
     if (!reginv_done) run_reginv(c);
-    lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);    // :97
+    {
+      KrylovScope ks(c, S.krylov0, S.lan0);
+      if (nk_reuse > 0) {
+        LanRun L;
+        L.nk = nk_reuse;
+        lan_finish(c, L);
+        lan_combine(c, S.BHalf, 0.5 * hdid);
+      } else {
+        lanczos(c, S.B0, S.BHalf, 0.5 * hdid, true);    // :97
+        lan_record(c, S);
+      }
+    }
     propagate_spf_all(c, S, 0.5 * hdid, S.psiHalf, S.DDHalf);   // :109-115
   } else {
+    KrylovScope ks(c, S.krylov0, S.lan0);
     // the Krylov build on c.st, the SPF integration (:109-115) on st2, in
     // lockstep: issue one step of each, wait for both, apply both controls
     CK(cudaEventRecord(c.ev_fork, c.st));
@@ -3538,8 +3603,13 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_d
       if (!reginv_done) run_reginv(c);
       spf_begin(c, P, 0.5 * hdid, S.psiHalf, S.DDHalf);
     }
-    lan_issue(c, L);
-    bool lan_pending = true, spf_pending = false;
+    bool lan_pending = false, spf_pending = false;
+    if (nk_reuse > 0) {
+      L.nk = nk_reuse;
+    } else {
+      lan_issue(c, L);
+      lan_pending = true;
+    }
     if (!P.finished) {
       StreamSwap sw(c, c.st2);
       spf_issue(c, S, P);
@@ -3567,6 +3637,7 @@ double cmf2_attempt(Ctx& c, double t, double hdid, bool ops_fresh, bool reginv_d
       }
     }
     lan_finish(c, L);
+    if (nk_reuse == 0) lan_record(c, S);
     lan_combine(c, S.BHalf, 0.5 * hdid);            // :97
     // the last SPF control's copies were issued on st2 after the last wait
     CK(cudaEventRecord(c.ev_join, c.st2));
