@@ -1573,9 +1573,7 @@ void launch_spf(const SpfDesc* d_descs, int ndesc, long long ntiles, const SpfOp
     spf_tile_split_kernel<2><<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
   else
     spf_tile_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, d_ops, out, der_factor);
-  // two warps: the Gauss-Jordan's three barriers per pivot cost less with fewer
-  // warps, and n x 2n entries per pivot leave 256 threads mostly idle
-  spf_solve_kernel<<<ndesc, 64, 0, st>>>(d_descs, d_status);
+  spf_solve_kernel<<<ndesc, 256, 0, st>>>(d_descs, d_status);
   if (prec > 0) spf_proj_split_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
   else spf_proj_kernel<<<(unsigned)ntiles, 256, 0, st>>>(d_descs, ndesc, out);
 }
